@@ -1,0 +1,385 @@
+"""Python face of the C ABI, mirroring the reference library's interface.
+
+Names follow the reference (lib/*.h): ``SignalCovarParams``, ``PCGParams``,
+``PCGResult``, ``WFVectorSN`` / ``WFVectorW`` with ``A``, ``A_product``,
+``A_residual``, ``preconditioner_solve``, ``norm_b`` and ``solve_pcg``, plus
+``smp_product`` and ``sigma_m_noise_dom``.  Arrays are numpy float64 (host) or
+CUDA float64 torch tensors for the ``*_dev`` calls.  Every call runs on the
+GPU through ``libdsgb300.so``; errors raise :class:`DsError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import weakref
+
+import numpy as np
+
+from . import _lib
+from ._lib import DsError
+
+FORMS = {"sn": _lib.DS_FORM_SN, "w": _lib.DS_FORM_W}
+EVALS = {"table": _lib.DS_EVAL_TABLE, "exact": _lib.DS_EVAL_EXACT}
+
+
+def _f64(a, n=None, name="array"):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"{name} has {a.size} elements, expected {n}")
+    return a
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _dev_ptr(t, n=None):
+    """A CUDA float64 tensor's device pointer (contiguous)."""
+    import torch  # device buffers only
+
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64
+            and t.is_contiguous()):
+        raise TypeError("expected a contiguous CUDA float64 tensor")
+    if n is not None and t.numel() != n:
+        raise ValueError(f"tensor has {t.numel()} elements, expected {n}")
+    return C.c_void_p(t.data_ptr())
+
+
+def table_init():
+    """SignalCovarParams' 200-knot table and its index scale 1/dx."""
+    t = np.zeros(_lib.DS_TABLE_N)
+    dx_inv = C.c_double()
+    _lib.load().ds_table_init(_ptr(t), C.byref(dx_inv))
+    return t, dx_inv.value
+
+
+@dataclasses.dataclass
+class SignalCovarParams:
+    """lib/signal_covar.h:10-46, plus the evaluation mode."""
+
+    var_s: float
+    l_perp: float
+    l_para: float
+    eval: str = "table"            # "table" (reference default) or "exact"
+    exact_cutoff: float = 0.0      # <= 0: library default (40)
+    table: np.ndarray | None = None
+
+    def as_c(self):
+        kp = _lib.KernelParamsC()
+        kp.var_s = self.var_s
+        kp.l_perp = self.l_perp
+        kp.l_para = self.l_para
+        kp.eval = EVALS[self.eval]
+        kp.exact_cutoff = self.exact_cutoff
+        if self.table is not None:
+            self._table_c = _f64(self.table, _lib.DS_TABLE_N, "table")
+            kp.table = _ptr(self._table_c)
+        else:
+            kp.table = None
+        return kp
+
+
+@dataclasses.dataclass
+class PCGParams:
+    """lib/pcg.h:13-19 (n is implied by the operator)."""
+
+    max_iter: int
+    step_r: int
+    tol: float
+    verbose: bool = False
+
+
+@dataclasses.dataclass
+class PCGResult:
+    """lib/pcg.h:21-25, plus device timing and mixed-precision counters."""
+
+    success: bool
+    num_iters: int
+    residual_norms: np.ndarray
+    norm_b: float
+    final_norm: float
+    status: int
+    seconds: float
+    n_outer: int = 0
+    n_inner: int = 0
+
+
+def signal_covar(perp2, para2, params: SignalCovarParams):
+    """signal_covar / signal_covar_exact (lib/signal_covar.h:67-86) on the GPU."""
+    perp2 = _f64(perp2).ravel()
+    para2 = _f64(para2, perp2.size, "para2").ravel()
+    out = np.empty_like(perp2)
+    kp = params.as_c()
+    rc = _lib.load().ds_signal_covar(C.byref(kp), perp2.size, _ptr(perp2), _ptr(para2), _ptr(out))
+    if rc != _lib.DS_OK:
+        raise DsError(rc, _lib.status_string(rc))
+    return out
+
+
+class Context:
+    """One device + one CUDA stream."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        rc = self._lib.ds_context_create(device, C.byref(h))
+        if rc != _lib.DS_OK:
+            raise DsError(rc, "ds_context_create: " + _lib.status_string(rc))
+        self.handle = h
+        self.device = device
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, child):
+        self._children.add(child)
+
+    def check(self, rc, what):
+        if rc not in (_lib.DS_OK,):
+            msg = self._lib.ds_context_last_error(self.handle).decode()
+            raise DsError(rc, f"{what}: {_lib.status_string(rc)}: {msg}")
+
+    @property
+    def stream(self) -> int:
+        return self._lib.ds_context_stream(self.handle) or 0
+
+    def synchronize(self):
+        self.check(self._lib.ds_context_synchronize(self.handle), "synchronize")
+
+    def close(self):
+        """Destroys the operators and maps made on this context, then the context."""
+        if getattr(self, "handle", None):
+            for child in list(self._children):
+                child.close()
+            self._lib.ds_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _WFVector:
+    """Common body of WFVectorSN / WFVectorW (lib/wf_vector.h:14-96)."""
+
+    FORM = None
+
+    def __init__(self, ctx: Context, records, s_params: SignalCovarParams):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        rec = _f64(records)
+        if rec.ndim != 2 or rec.shape[1] != 5:
+            raise ValueError("records must have shape (n, 5)")
+        self.n = rec.shape[0]
+        self.s_params = s_params
+        kp = s_params.as_c()
+        h = C.c_void_p()
+        ctx.check(self._lib.ds_operator_create(ctx.handle, self.FORM, self.n, _ptr(rec),
+                                               C.byref(kp), C.byref(h)), "ds_operator_create")
+        self.handle = h
+        ctx._adopt(self)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.ds_operator_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        inf = _lib.OperatorInfoC()
+        self.ctx.check(self._lib.ds_operator_get_info(self.handle, C.byref(inf)), "info")
+        return {k: getattr(inf, k) for k, _ in inf._fields_}
+
+    def _vec_call(self, fn, v, name):
+        v = _f64(v, self.n, name)
+        out = np.empty(self.n)
+        self.ctx.check(fn(self.handle, _ptr(v), _ptr(out)), fn.__name__)
+        return out
+
+    def A_product(self, a):
+        return self._vec_call(self._lib.ds_A_product, a, "a")
+
+    def A_residual(self, x):
+        return self._vec_call(self._lib.ds_A_residual, x, "x")
+
+    def preconditioner_solve(self, b):
+        return self._vec_call(self._lib.ds_preconditioner_solve, b, "b")
+
+    def A_product_dev(self, a, b):
+        self.ctx.check(self._lib.ds_A_product_dev(self.handle, _dev_ptr(a, self.n),
+                                                  _dev_ptr(b, self.n)), "ds_A_product_dev")
+
+    def A_residual_dev(self, x, r):
+        self.ctx.check(self._lib.ds_A_residual_dev(self.handle, _dev_ptr(x, self.n),
+                                                   _dev_ptr(r, self.n)), "ds_A_residual_dev")
+
+    def norm_b(self) -> float:
+        v = C.c_double()
+        self.ctx.check(self._lib.ds_norm_b(self.handle, C.byref(v)), "ds_norm_b")
+        return v.value
+
+    def A(self, i, j, exact=None):
+        """A(i, j, exact) for scalars or arrays of indices."""
+        ii = np.ascontiguousarray(np.atleast_1d(i), dtype=np.int32)
+        jj = np.ascontiguousarray(np.atleast_1d(j), dtype=np.int32)
+        if ii.shape != jj.shape:
+            raise ValueError("i and j must have the same shape")
+        out = np.empty(ii.size)
+        ev = -1 if exact is None else (_lib.DS_EVAL_EXACT if exact else _lib.DS_EVAL_TABLE)
+        self.ctx.check(self._lib.ds_A_entries(self.handle, ev, ii.size,
+                                              ii.ctypes.data_as(C.POINTER(C.c_int)),
+                                              jj.ctypes.data_as(C.POINTER(C.c_int)), _ptr(out)),
+                       "ds_A_entries")
+        return out if np.ndim(i) else float(out[0])
+
+    def _solve(self, fn, pp: PCGParams, x, dev: bool):
+        c = _lib.PcgParamsC(pp.max_iter, pp.step_r, pp.tol, int(bool(pp.verbose)))
+        res = _lib.PcgResultC()
+        hist = np.zeros(max(pp.max_iter, 1) + 1)
+        xp = _dev_ptr(x, self.n) if dev else _ptr(x)
+        rc = fn(self.handle, C.byref(c), xp, C.byref(res), _ptr(hist))
+        if rc not in (_lib.DS_OK, _lib.DS_ERR_NOT_CONVERGED, _lib.DS_ERR_NORM_B):
+            self.ctx.check(rc, fn.__name__)
+        nh = 0 if rc == _lib.DS_ERR_NORM_B else min(hist.size, max(res.n_inner, 0) + 1)
+        return PCGResult(bool(res.success), res.num_iters, hist[:nh].copy(), res.norm_b,
+                         res.final_norm, rc, res.seconds, res.n_outer, res.n_inner)
+
+    def solve_pcg(self, pcg_params: PCGParams, x=None):
+        """Returns (x, PCGResult); x is the initial guess (zeros if None)."""
+        x = np.zeros(self.n) if x is None else _f64(x, self.n, "x").copy()
+        res = self._solve(self._lib.ds_solve_pcg, pcg_params, x, False)
+        return x, res
+
+    def solve_pcg_dev(self, pcg_params: PCGParams, x):
+        """In-place solve on a CUDA float64 tensor (initial guess in, solution out)."""
+        return self._solve(self._lib.ds_solve_pcg_dev, pcg_params, x, True)
+
+
+class WFVectorSN(_WFVector):
+    """x = (S + N)^-1 d over NPixel records {x, y, z, N, d}."""
+
+    FORM = _lib.DS_FORM_SN
+
+
+class WFVectorW(_WFVector):
+    """x = w (w S w + I)^-1 w d over WPixel records {x, y, z, w, wd}."""
+
+    FORM = _lib.DS_FORM_W
+
+
+class MapGrid:
+    """Map points sorted and tiled on the device once (for repeated products)."""
+
+    def __init__(self, ctx: Context, points):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        pts = _f64(points)
+        if pts.ndim != 2 or pts.shape[1] != 3:
+            raise ValueError("points must have shape (n_map, 3)")
+        self.n_map = pts.shape[0]
+        h = C.c_void_p()
+        ctx.check(self._lib.ds_map_create(ctx.handle, self.n_map, _ptr(pts), C.byref(h)),
+                  "ds_map_create")
+        self.handle = h
+        ctx._adopt(self)
+
+    def product(self, op: _WFVector, x):
+        """smp_product with the operator's pixels and kernel."""
+        x = _f64(x, op.n, "x")
+        m = np.empty(self.n_map)
+        self.ctx.check(self._lib.ds_map_product(self.handle, op.handle, _ptr(x), _ptr(m)),
+                       "ds_map_product")
+        return m
+
+    def product_dev(self, op: _WFVector, x, m):
+        self.ctx.check(self._lib.ds_map_product_dev(self.handle, op.handle, _dev_ptr(x, op.n),
+                                                    _dev_ptr(m, self.n_map)),
+                       "ds_map_product_dev")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.ds_map_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def smp_product(ctx: Context, pixel_coords, map_coords, s_params: SignalCovarParams, x):
+    """lib/map.cc:20-43 with the reference's argument list."""
+    pix = _f64(pixel_coords)
+    mp = _f64(map_coords)
+    x = _f64(x, pix.shape[0], "x")
+    m = np.empty(mp.shape[0])
+    kp = s_params.as_c()
+    ctx.check(ctx._lib.ds_smp_product(ctx.handle, pix.shape[0], _ptr(pix), mp.shape[0], _ptr(mp),
+                                      C.byref(kp), _ptr(x), _ptr(m)), "ds_smp_product")
+    return m
+
+
+def sigma_m_noise_dom(ctx: Context, npixels, map_coords, s_params: SignalCovarParams):
+    """lib/map_covar.cc:11-38."""
+    rec = _f64(npixels)
+    mp = _f64(map_coords)
+    out = np.empty(mp.shape[0])
+    kp = s_params.as_c()
+    ctx.check(ctx._lib.ds_sigma_m_noise_dom(ctx.handle, rec.shape[0], _ptr(rec), mp.shape[0],
+                                            _ptr(mp), C.byref(kp), _ptr(out)),
+              "ds_sigma_m_noise_dom")
+    return out
+
+
+# Pixel format conversions (lib/pixel.cc:9-71), host-side like the reference.
+def points_from_pixels(pixels):
+    return np.ascontiguousarray(np.asarray(pixels, dtype=np.float64)[:, :3])
+
+
+def pixel_to_npixel(pixels):
+    p = np.array(pixels, dtype=np.float64, copy=True)
+    p[:, 3] = p[:, 3] * p[:, 3]
+    return p
+
+
+def npixel_to_pixel(npixels):
+    p = np.array(npixels, dtype=np.float64, copy=True)
+    p[:, 3] = np.sqrt(p[:, 3])
+    return p
+
+
+def pixel_to_wpixel(pixels):
+    p = np.array(pixels, dtype=np.float64, copy=True)
+    n = p[:, 3].copy()
+    p[:, 3] = 1.0 / n
+    p[:, 4] = p[:, 4] / n
+    return p
+
+
+def wpixel_to_pixel(wpixels):
+    p = np.array(wpixels, dtype=np.float64, copy=True)
+    w = p[:, 3].copy()
+    p[:, 3] = 1.0 / w
+    p[:, 4] = p[:, 4] / w
+    return p
+
+
+def read_pixel_data(path, num_pixels):
+    """lib/util.cc:11-23, with the record count checked against the file size."""
+    data = np.fromfile(path, dtype=np.float64)
+    if data.size < 5 * num_pixels:
+        raise ValueError(f"{path}: {data.size // 5} records, expected {num_pixels}")
+    return data[: 5 * num_pixels].reshape(num_pixels, 5).copy()
+
+
+def init_uniform_map_coords(lx, ly, lz, nx, ny, nz):
+    """lib/util.cc:25-46: cell centres, z fastest."""
+    from .synth import uniform_map_coords
+
+    return uniform_map_coords(lx, ly, lz, nx, ny, nz)

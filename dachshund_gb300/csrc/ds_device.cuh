@@ -1,0 +1,86 @@
+// Device helpers shared by the kernels: deterministic block reductions, the
+// "last block finishes" pattern, and the FP64 signal-covariance evaluations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ds_internal.cuh"
+
+namespace ds {
+
+// Sum of v over the block; valid in thread 0.  Fixed order (shuffle tree
+// within warps, then warps in order), so results are run-to-run identical.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sm /* NT/32 */) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();  // sm may still be read by a previous call
+  if (lane == 0) sm[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < NT / 32; ++w) s += sm[w];
+  return s;
+}
+
+// Every block calls this once after writing its partial result (thread 0);
+// returns true in exactly one block, the last to arrive, which then sees all
+// partials.  The counter is reset by that block.
+__device__ __forceinline__ bool last_block_arrive(unsigned int* counter) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int prev = atomicAdd(counter, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last;
+}
+
+// Deterministic sum of n partials (stride `stride`, offset `off`) by one block.
+template <int NT>
+__device__ __forceinline__ double reduce_partials(const double* part, int n, int stride, int off,
+                                                  double* sm) {
+  double v = 0.0;
+  for (int k = threadIdx.x; k < n; k += NT) v += __ldcg(part + (size_t)k * stride + off);
+  return block_sum<NT>(v, sm);
+}
+
+// Table kernel in the reference's exact operation order
+// (lib/signal_covar.h:53-77, argument as in lib/wf_vector.cc:162-167):
+// products and sums rounded separately, truncating index, zero once the
+// index passes the second-to-last knot.  Same-skewer pixels 8 Mpc/h apart
+// land exactly on xx = 199.0 with l_para = 2, so the argument must round
+// exactly like the reference for the cutoff to agree.
+__device__ __forceinline__ double s_table_f64(double dx, double dy, double dz,
+                                              const KernelConsts& k, const double* tf) {
+  const double perp2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  const double para2 = __dmul_rn(dz, dz);
+  const double g = __dadd_rn(__dmul_rn(k.c_perp, perp2), __dmul_rn(k.c_para, para2));
+  const double xx = __dmul_rn(g, k.dx_inv);
+  const bool inside = xx < (double)(TABLE_N - 1);
+  int ix = __double2int_rz(xx);
+  ix = min(max(ix, 0), TABLE_N - 2);
+  const double lo = __dsub_rn((double)(ix + 1), xx);
+  const double hi = __dsub_rn(xx, (double)ix);
+  const double gp = __dadd_rn(__dmul_rn(tf[ix], lo), __dmul_rn(tf[ix + 1], hi));
+  return inside ? __dmul_rn(k.var_s, gp) : 0.0;
+}
+
+// Exact kernel var_s exp(-arg) with the per-element cutoff arg >= exact_cut -> 0.
+__device__ __forceinline__ double s_exact_f64(double dx, double dy, double dz,
+                                              const KernelConsts& k) {
+  const double arg = k.c_perp * (dx * dx + dy * dy) + k.c_para * (dz * dz);
+  return arg < k.exact_cut ? k.var_s * exp(-arg) : 0.0;
+}
+
+template <int EVAL>
+__device__ __forceinline__ double s_eval_f64(double dx, double dy, double dz,
+                                             const KernelConsts& k, const double* tf) {
+  if (EVAL == DS_EVAL_TABLE) return s_table_f64(dx, dy, dz, k, tf);
+  return s_exact_f64(dx, dy, dz, k);
+}
+
+}  // namespace ds

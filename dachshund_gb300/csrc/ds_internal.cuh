@@ -1,0 +1,231 @@
+// Internal declarations of the dachshund-gb300 CUDA library.
+//
+// Layout in HBM (one operator):
+//   * pixel coordinates as three FP64 SoA arrays x[], y[], z[] in a spatially
+//     sorted order (3-D Morton order of the points scaled by the correlation
+//     lengths), padded to a multiple of TILE with copies of the last point;
+//   * per-pixel operator coefficients in the same order: wl (left scale),
+//     wr (right scale), e (diagonal), b (right-hand side), pdiag (Jacobi);
+//     padding rows carry zeros, so padded vector entries stay exactly zero;
+//   * perm[] (sorted -> caller index) and the per-tile bounding boxes;
+//   * the culled tile-pair list in CSR form (row tile -> column tiles).
+// All vectors that iterate (x, r, d, q, s) live in sorted order; the caller's
+// order is restored only at the API boundary.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ds_gb300.h"
+
+namespace ds {
+
+constexpr int TILE = 128;        // points per tile (rows per CTA in the FP64 kernels)
+constexpr int TABLE_N = DS_TABLE_N;
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define DS_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      throw ::ds::Error{e_ == cudaErrorMemoryAllocation ? DS_ERR_OOM         \
+                                                        : DS_ERR_CUDA,       \
+                        std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+
+#define DS_CHECK_LAUNCH() DS_CUDA(cudaGetLastError())
+
+inline void require(bool ok, const char* msg) {
+  if (!ok) throw Error{DS_ERR_ARG, msg};
+}
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    DS_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Pinned host buffer.
+template <class T>
+struct HostBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf&) = delete;
+  HostBuf& operator=(const HostBuf&) = delete;
+  ~HostBuf() { if (p) cudaFreeHost(p); }
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    DS_CUDA(cudaMallocHost(&p, count * sizeof(T)));
+    n = count;
+  }
+};
+
+// Kernel constants shared by every pair kernel.
+struct KernelConsts {
+  double var_s;
+  double c_perp;     // 1 / (2 l_perp^2)
+  double c_para;     // 1 / (2 l_para^2)
+  double dx_inv;     // table index scale, 199/8
+  double exact_cut;  // exponent cutoff of the exact kernel
+  double cull_arg;   // tile-pair culling threshold on c_perp dperp^2 + c_para dz^2
+  int eval;          // DS_EVAL_TABLE / DS_EVAL_EXACT
+};
+
+KernelConsts make_consts(const ds_kernel_params& kp);
+void host_table(double* table, double* dx_inv);
+
+// A spatially sorted, tiled point set on the device.
+struct PointSet {
+  int n = 0;
+  int n_pad = 0;
+  int n_tiles = 0;
+  DevBuf<double> x, y, z;  // sorted + padded
+  DevBuf<int> perm;        // sorted position -> caller index (-1 on padding)
+  DevBuf<double> box;      // 6 per tile: lo x, y, z, hi x, y, z
+};
+
+// Builds a PointSet from n records of `stride` doubles (x, y, z first) that
+// are already in device memory.  sx, sy, sz scale the coordinates for the
+// spatial key only (the stored coordinates are unscaled).
+void build_point_set(PointSet& ps, const double* d_rec, int n, int stride,
+                     double sx, double sy, double sz, cudaStream_t st);
+
+// Culled tile-pair list (CSR over row tiles).
+struct PairList {
+  int n_rows = 0;
+  long long n_pairs = 0;
+  DevBuf<int> row_ptr;  // n_rows + 1
+  DevBuf<int> cols;     // n_pairs
+};
+
+void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
+                     const KernelConsts& kc, cudaStream_t st);
+
+// ---- pair kernels (FP64) -------------------------------------------------
+// Column weight u_j and epilogue selection.
+enum PairEpi {
+  EPI_PRODUCT = 0,   // out_i = wl_i acc + e_i v_i      (u_j = wr_j v_j)
+  EPI_RESIDUAL = 1,  // out_i = b_i - (wl_i acc + e_i v_i)
+  EPI_MAP = 2,       // out[perm_i] = acc               (u_j = v_j)
+  EPI_NOISE = 3      // out[perm_i] = sum S^2 u_j       (u_j = 1 / N_j)
+};
+
+struct PairArgs {
+  // geometry
+  const double* rx; const double* ry; const double* rz;
+  const double* cx; const double* cy; const double* cz;
+  const int* row_ptr; const int* cols;
+  int n_row_tiles;
+  // coefficients (sorted order)
+  const double* wl; const double* wr; const double* e; const double* b;
+  const double* v;      // the vector being multiplied (column side)
+  const double* vrow;   // the same vector on the row side (diagonal term)
+  double* out;
+  const int* row_perm;  // EPI_MAP / EPI_NOISE scatter
+  // fused dot product: partial[tile] = sum_i dotv_i out_i (if dot_partial)
+  const double* dotv;
+  double* dot_partial;
+  // early exit when *skip_flag != 0
+  const int* skip_flag;
+  // last-block reduction of dot_partial -> pcg alpha
+  struct PcgState* pcg;
+  unsigned int* counter;
+  const double* table;  // TABLE_N knots
+};
+
+void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a,
+                     cudaStream_t st);
+
+// ---- PCG -----------------------------------------------------------------
+struct PcgState {
+  double delta;       // r . s (current)
+  double delta_old;
+  double alpha;
+  double beta;
+  double dq;
+  double norm_r;
+  double norm_b;
+  double tol_norm_b;
+  int iter;           // completed iterations
+  int max_iter;
+  int done;
+  int converged;
+  unsigned int counter[4];
+};
+
+}  // namespace ds
+
+// Opaque handles of the C ABI.
+struct ds_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+};
+
+struct ds_operator {
+  ds_context* ctx = nullptr;
+  int form = 0;
+  int n = 0;
+  ds::KernelConsts kc{};
+  ds::PointSet pix;
+  ds::PairList pairs;
+  ds::DevBuf<double> table;
+  ds::DevBuf<double> wl, wr, e, b;  // sorted, padded operator coefficients
+  ds::DevBuf<double> pdiag;         // Jacobi diagonal (1 on padding)
+  ds::DevBuf<int> inv;              // caller index -> sorted position
+  ds::DevBuf<double> io_a, io_b;    // caller-order device staging
+  double norm_b = 0.0;
+  // PCG work space (sorted, padded)
+  ds::DevBuf<double> x, r, d, q, s, tmp, tmp2;
+  ds::DevBuf<double> partial;      // per-block partial sums
+  ds::DevBuf<double> partial2;
+  ds::DevBuf<ds::PcgState> state;
+  ds::DevBuf<double> hist, dhist;  // residual norms and deltas per iteration
+  ds::HostBuf<double> h_io;        // pinned staging
+  ds::HostBuf<int> h_flag;
+  unsigned long long serial = 0;   // identity for caches keyed on operators
+};
+
+struct ds_map {
+  ds_context* ctx = nullptr;
+  ds::PointSet pts;
+  // pair list cache for the last operator used
+  unsigned long long op_serial = 0;
+  ds::KernelConsts kc{};
+  ds::PairList pairs;
+  ds::DevBuf<double> out_dev;  // caller-order map staging
+};

@@ -1,0 +1,21 @@
+// Internal entry points shared between the translation units of the library.
+#pragma once
+
+#include "ds_internal.cuh"
+
+namespace ds {
+
+void gather_sorted(const PointSet& ps, const double* src, double* dst, cudaStream_t st);
+void scatter_sorted(const PointSet& ps, const double* src, const double* scale, double* dst,
+                    cudaStream_t st);
+void vec_mul(int n, const double* a, const double* b, double* c, cudaStream_t st);
+
+PairArgs op_pair_args(ds_operator* op, const double* v, double* out);
+void op_apply_sorted(ds_operator* op, int epi, const double* v, double* out, cudaStream_t st);
+void ensure_pcg_workspace(ds_operator* op);
+void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, double* hist_out);
+
+// Operator set-up helpers (capi.cu).
+void op_init_coeffs(ds_operator* op, const double* d_rec);
+
+}  // namespace ds

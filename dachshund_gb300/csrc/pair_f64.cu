@@ -1,0 +1,106 @@
+// FP64 matrix-free pair kernel: one CTA per row tile, one row per thread,
+// looping over the row tile's culled column tiles.  Column coordinates and
+// weights are staged in shared memory and read as broadcasts; the 200-knot
+// table lives in shared memory.  Serves
+//   * WFVector{SN,W}::A_product / A_residual (lib/wf_vector.cc:51-103,
+//     196-251), with the CG dot d.q fused into the product epilogue;
+//   * smp_product (lib/map.cc:20-43);
+//   * sigma_m_noise_dom (lib/map_covar.cc:11-38).
+// Roofline: FP64 pipe (about 16 FP64 instructions per pair in table mode,
+// plus exp() in exact mode); no HBM traffic beyond the tiles (L2 resident).
+#include "ds_device.cuh"
+
+namespace ds {
+
+namespace {
+
+template <int EVAL, int EPI, bool DOT>
+__global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) {
+  if (a.skip_flag && *a.skip_flag) return;
+  __shared__ double sx[TILE], sy[TILE], sz[TILE], su[TILE];
+  __shared__ double tf[EVAL == DS_EVAL_TABLE ? TABLE_N : 1];
+  __shared__ double red[TILE / 32];
+  const int t = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int i = t * TILE + tid;
+  if (EVAL == DS_EVAL_TABLE)
+    for (int k = tid; k < TABLE_N; k += TILE) tf[k] = a.table[k];
+  const double xi = a.rx[i], yi = a.ry[i], zi = a.rz[i];
+  double acc = 0.0;
+  const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
+  for (int p = p0; p < p1; ++p) {
+    const int j = a.cols[p] * TILE + tid;
+    __syncthreads();
+    sx[tid] = a.cx[j];
+    sy[tid] = a.cy[j];
+    sz[tid] = a.cz[j];
+    if (EPI == EPI_PRODUCT || EPI == EPI_RESIDUAL)
+      su[tid] = a.wr[j] * a.v[j];
+    else
+      su[tid] = a.v[j];
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < TILE; ++jj) {
+      double S = s_eval_f64<EVAL>(xi - sx[jj], yi - sy[jj], zi - sz[jj], kc, tf);
+      if (EPI == EPI_NOISE) S = S * S;
+      acc = fma(S, su[jj], acc);
+    }
+  }
+  if (EPI == EPI_PRODUCT || EPI == EPI_RESIDUAL) {
+    const double q = a.wl[i] * acc + a.e[i] * a.v[i];
+    const double o = (EPI == EPI_RESIDUAL) ? a.b[i] - q : q;
+    a.out[i] = o;
+    if (DOT) {
+      const double s = block_sum<TILE>(a.dotv[i] * o, red);
+      if (tid == 0) a.dot_partial[t] = s;
+      if (last_block_arrive(a.counter)) {
+        const double dq = reduce_partials<TILE>(a.dot_partial, gridDim.x, 1, 0, red);
+        if (tid == 0) {
+          a.pcg->dq = dq;
+          a.pcg->alpha = a.pcg->delta / dq;  // lib/pcg.h:37
+          *a.counter = 0;
+        }
+      }
+    }
+  } else {
+    const int dst = a.row_perm[i];
+    if (dst >= 0) a.out[dst] = acc;
+  }
+}
+
+template <int EVAL>
+void launch_eval(const KernelConsts& kc, int epi, const PairArgs& a, cudaStream_t st) {
+  const dim3 grid(a.n_row_tiles), block(TILE);
+  switch (epi) {
+    case EPI_PRODUCT:
+      if (a.dot_partial)
+        k_pair_f64<EVAL, EPI_PRODUCT, true><<<grid, block, 0, st>>>(kc, a);
+      else
+        k_pair_f64<EVAL, EPI_PRODUCT, false><<<grid, block, 0, st>>>(kc, a);
+      break;
+    case EPI_RESIDUAL:
+      k_pair_f64<EVAL, EPI_RESIDUAL, false><<<grid, block, 0, st>>>(kc, a);
+      break;
+    case EPI_MAP:
+      k_pair_f64<EVAL, EPI_MAP, false><<<grid, block, 0, st>>>(kc, a);
+      break;
+    case EPI_NOISE:
+      k_pair_f64<EVAL, EPI_NOISE, false><<<grid, block, 0, st>>>(kc, a);
+      break;
+    default:
+      throw Error{DS_ERR_ARG, "bad pair epilogue"};
+  }
+}
+
+}  // namespace
+
+void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a, cudaStream_t st) {
+  if (a.n_row_tiles <= 0) return;
+  if (kc.eval == DS_EVAL_TABLE)
+    launch_eval<DS_EVAL_TABLE>(kc, epi, a, st);
+  else
+    launch_eval<DS_EVAL_EXACT>(kc, epi, a, st);
+  DS_CHECK_LAUNCH();
+}
+
+}  // namespace ds

@@ -1,0 +1,297 @@
+// Spatial sorting, tiling and tile-pair culling.
+//
+// The reference evaluates every (i, j) pair of every matvec
+// (lib/wf_vector.cc:51-74) even where the table kernel is exactly zero
+// (lib/signal_covar.h:60-62).  Here points are sorted along a 3-D Morton curve
+// of their coordinates scaled by the correlation lengths, cut into tiles of
+// TILE consecutive points, and a tile pair is kept only when the nearest
+// corners of the two bounding boxes are inside the kernel's cutoff.  Every
+// skipped pair therefore has S_ij == 0 (table) or S_ij < var_s exp(-cutoff)
+// (exact), and the kept relation is symmetric, so A stays symmetric.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "ds_internal.cuh"
+
+namespace ds {
+
+void host_table(double* table, double* dx_inv) {
+  // SignalCovarParams ctor, lib/signal_covar.h:25-40.
+  const double fx_max = 4.0 * 4.0 / 2.0;
+  const double ft_dx = fx_max / (TABLE_N - 1);
+  if (dx_inv) *dx_inv = 1.0 / ft_dx;
+  if (table)
+    for (int i = 0; i < TABLE_N; ++i) table[i] = std::exp(-(ft_dx * i));
+}
+
+KernelConsts make_consts(const ds_kernel_params& kp) {
+  require(kp.var_s >= 0.0 && std::isfinite(kp.var_s), "var_s must be finite and >= 0");
+  require(kp.l_perp > 0.0 && kp.l_para > 0.0, "correlation lengths must be > 0");
+  require(kp.eval == DS_EVAL_TABLE || kp.eval == DS_EVAL_EXACT, "unknown eval mode");
+  KernelConsts k{};
+  k.var_s = kp.var_s;
+  k.c_perp = 1.0 / (2.0 * kp.l_perp * kp.l_perp);
+  k.c_para = 1.0 / (2.0 * kp.l_para * kp.l_para);
+  host_table(nullptr, &k.dx_inv);
+  k.exact_cut = kp.exact_cutoff > 0.0 ? kp.exact_cutoff : DS_DEFAULT_EXACT_CUTOFF;
+  k.eval = kp.eval;
+  // Table: S == 0 once xx = arg * dx_inv reaches TABLE_N - 1.
+  const double cut = kp.eval == DS_EVAL_TABLE ? (TABLE_N - 1) / k.dx_inv : k.exact_cut;
+  k.cull_arg = cut * (1.0 + 1e-9);
+  return k;
+}
+
+namespace {
+
+constexpr int BLK = 256;
+
+__global__ void k_bbox_partial(const double* __restrict__ rec, int n, int stride,
+                               double* __restrict__ part) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY};
+  double hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      const double v = rec[(size_t)i * stride + c];
+      lo[c] = fmin(lo[c], v);
+      hi[c] = fmax(hi[c], v);
+    }
+  }
+  __shared__ double sm[6][BLK];
+  for (int c = 0; c < 3; ++c) {
+    sm[c][threadIdx.x] = lo[c];
+    sm[3 + c][threadIdx.x] = hi[c];
+  }
+  __syncthreads();
+  for (int s = BLK / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int c = 0; c < 3; ++c) {
+        sm[c][threadIdx.x] = fmin(sm[c][threadIdx.x], sm[c][threadIdx.x + s]);
+        sm[3 + c][threadIdx.x] = fmax(sm[3 + c][threadIdx.x], sm[3 + c][threadIdx.x + s]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  // 10 bits -> every third bit of 30.
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void k_morton(const double* __restrict__ rec, int n, int stride, double lx,
+                         double ly, double lz, double sx, double sy, double sz,
+                         double inv_h, uint32_t* __restrict__ keys, int* __restrict__ idx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* p = rec + (size_t)i * stride;
+  auto q = [&](double v, double lo, double s) {
+    double c = (v - lo) * s * inv_h;
+    c = fmin(fmax(c, 0.0), 1023.0);
+    return (uint32_t)c;
+  };
+  const uint32_t qx = q(p[0], lx, sx), qy = q(p[1], ly, sy), qz = q(p[2], lz, sz);
+  keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
+  idx[i] = i;
+}
+
+__global__ void k_gather_points(const double* __restrict__ rec, int n, int n_pad, int stride,
+                                const int* __restrict__ sorted_idx, double* __restrict__ x,
+                                double* __restrict__ y, double* __restrict__ z,
+                                int* __restrict__ perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  const int src = sorted_idx[i < n ? i : n - 1];
+  const double* p = rec + (size_t)src * stride;
+  x[i] = p[0];
+  y[i] = p[1];
+  z[i] = p[2];
+  perm[i] = i < n ? src : -1;
+}
+
+__global__ void k_tile_boxes(const double* __restrict__ x, const double* __restrict__ y,
+                             const double* __restrict__ z, double* __restrict__ box) {
+  const int t = blockIdx.x;
+  const int i = t * TILE + threadIdx.x;
+  __shared__ double sm[6][TILE];
+  sm[0][threadIdx.x] = x[i];
+  sm[1][threadIdx.x] = y[i];
+  sm[2][threadIdx.x] = z[i];
+  sm[3][threadIdx.x] = x[i];
+  sm[4][threadIdx.x] = y[i];
+  sm[5][threadIdx.x] = z[i];
+  __syncthreads();
+  for (int s = TILE / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int c = 0; c < 3; ++c) {
+        sm[c][threadIdx.x] = fmin(sm[c][threadIdx.x], sm[c][threadIdx.x + s]);
+        sm[3 + c][threadIdx.x] = fmax(sm[3 + c][threadIdx.x], sm[3 + c][threadIdx.x + s]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) box[t * 6 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+__device__ __forceinline__ bool tiles_interact(const double* __restrict__ bi,
+                                               const double* __restrict__ bj,
+                                               double c_perp, double c_para, double cut) {
+  const double dx = fmax(0.0, fmax(bi[0] - bj[3], bj[0] - bi[3]));
+  const double dy = fmax(0.0, fmax(bi[1] - bj[4], bj[1] - bi[4]));
+  const double dz = fmax(0.0, fmax(bi[2] - bj[5], bj[2] - bi[5]));
+  return c_perp * (dx * dx + dy * dy) + c_para * dz * dz < cut;
+}
+
+__global__ void k_pair_count(const double* __restrict__ rbox, int n_row, const double* __restrict__ cbox,
+                             int n_col, double c_perp, double c_para, double cut,
+                             int* __restrict__ counts) {
+  const int r = blockIdx.x;
+  double bi[6];
+  for (int c = 0; c < 6; ++c) bi[c] = rbox[r * 6 + c];
+  int cnt = 0;
+  for (int j = threadIdx.x; j < n_col; j += blockDim.x)
+    cnt += tiles_interact(bi, cbox + (size_t)j * 6, c_perp, c_para, cut) ? 1 : 0;
+  __shared__ int sm[BLK];
+  sm[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int s = BLK / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) counts[r] = sm[0];
+  (void)n_row;
+}
+
+__global__ void k_pair_fill(const double* __restrict__ rbox, const double* __restrict__ cbox,
+                            int n_col, double c_perp, double c_para, double cut,
+                            const int* __restrict__ row_ptr, int* __restrict__ cols) {
+  const int r = blockIdx.x;
+  double bi[6];
+  for (int c = 0; c < 6; ++c) bi[c] = rbox[r * 6 + c];
+  __shared__ int warp_tot[BLK / 32];
+  __shared__ int base;
+  if (threadIdx.x == 0) base = row_ptr[r];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n_col; j0 += blockDim.x) {
+    const int j = j0 + threadIdx.x;
+    const bool f = j < n_col && tiles_interact(bi, cbox + (size_t)j * 6, c_perp, c_para, cut);
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    const int pre = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) warp_tot[wid] = __popc(m);
+    __syncthreads();
+    int off = 0, tot = 0;
+    for (int w = 0; w < BLK / 32; ++w) {
+      if (w < wid) off += warp_tot[w];
+      tot += warp_tot[w];
+    }
+    if (f) cols[base + off + pre] = j;
+    __syncthreads();
+    if (threadIdx.x == 0) base += tot;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, double sx,
+                     double sy, double sz, cudaStream_t st) {
+  require(n > 0, "point count must be > 0");
+  ps.n = n;
+  ps.n_tiles = (n + TILE - 1) / TILE;
+  ps.n_pad = ps.n_tiles * TILE;
+
+  // Bounding box of all points.
+  const int nb = std::min(256, (n + BLK - 1) / BLK);
+  DevBuf<double> part;
+  part.alloc((size_t)nb * 6);
+  k_bbox_partial<<<nb, BLK, 0, st>>>(d_rec, n, stride, part.p);
+  DS_CHECK_LAUNCH();
+  std::vector<double> hp((size_t)nb * 6);
+  DS_CUDA(cudaMemcpyAsync(hp.data(), part.p, hp.size() * sizeof(double),
+                          cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int b = 0; b < nb; ++b)
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = std::min(lo[c], hp[b * 6 + c]);
+      hi[c] = std::max(hi[c], hp[b * 6 + 3 + c]);
+    }
+  for (int c = 0; c < 3; ++c)
+    require(std::isfinite(lo[c]) && std::isfinite(hi[c]), "non-finite coordinates");
+  const double ext = std::max({(hi[0] - lo[0]) * sx, (hi[1] - lo[1]) * sy,
+                               (hi[2] - lo[2]) * sz, 1e-300});
+  const double inv_h = 1023.0 / ext;
+
+  // Morton keys and a stable radix sort of (key, index).
+  DevBuf<uint32_t> keys, keys2;
+  DevBuf<int> idx, idx2;
+  keys.alloc(n);
+  keys2.alloc(n);
+  idx.alloc(n);
+  idx2.alloc(n);
+  k_morton<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, lo[0], lo[1], lo[2], sx, sy,
+                                                sz, inv_h, keys.p, idx.p);
+  DS_CHECK_LAUNCH();
+  size_t tmp_bytes = 0;
+  DS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
+                                          0, 30, st));
+  DevBuf<unsigned char> tmp;
+  tmp.alloc(std::max<size_t>(tmp_bytes, 1));
+  DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n, 0,
+                                          30, st));
+
+  ps.x.alloc(ps.n_pad);
+  ps.y.alloc(ps.n_pad);
+  ps.z.alloc(ps.n_pad);
+  ps.perm.alloc(ps.n_pad);
+  ps.box.alloc((size_t)ps.n_tiles * 6);
+  k_gather_points<<<(ps.n_pad + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, ps.n_pad, stride, idx2.p,
+                                                              ps.x.p, ps.y.p, ps.z.p, ps.perm.p);
+  DS_CHECK_LAUNCH();
+  k_tile_boxes<<<ps.n_tiles, TILE, 0, st>>>(ps.x.p, ps.y.p, ps.z.p, ps.box.p);
+  DS_CHECK_LAUNCH();
+  // The temporaries are freed on return; make sure the stream is done with them.
+  DS_CUDA(cudaStreamSynchronize(st));
+}
+
+void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
+                     const KernelConsts& kc, cudaStream_t st) {
+  pl.n_rows = rows.n_tiles;
+  DevBuf<int> counts;
+  counts.alloc(rows.n_tiles);
+  k_pair_count<<<rows.n_tiles, BLK, 0, st>>>(rows.box.p, rows.n_tiles, cols.box.p, cols.n_tiles,
+                                             kc.c_perp, kc.c_para, kc.cull_arg, counts.p);
+  DS_CHECK_LAUNCH();
+  std::vector<int> hc(rows.n_tiles);
+  DS_CUDA(cudaMemcpyAsync(hc.data(), counts.p, hc.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                          st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  std::vector<int> rp(rows.n_tiles + 1);
+  long long total = 0;
+  for (int r = 0; r < rows.n_tiles; ++r) {
+    rp[r] = (int)total;
+    total += hc[r];
+  }
+  require(total < (1ll << 31), "too many tile pairs");
+  rp[rows.n_tiles] = (int)total;
+  pl.n_pairs = total;
+  pl.row_ptr.alloc(rows.n_tiles + 1);
+  pl.cols.alloc(std::max<long long>(total, 1));
+  DS_CUDA(cudaMemcpyAsync(pl.row_ptr.p, rp.data(), rp.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, st));
+  k_pair_fill<<<rows.n_tiles, BLK, 0, st>>>(rows.box.p, cols.box.p, cols.n_tiles, kc.c_perp,
+                                            kc.c_para, kc.cull_arg, pl.row_ptr.p, pl.cols.p);
+  DS_CHECK_LAUNCH();
+  DS_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace ds

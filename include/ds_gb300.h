@@ -1,0 +1,199 @@
+/*
+ * dachshund-gb300 C ABI: the Wiener-filter hot path of Dachshund on one
+ * GB300 (sm_103a), behind plain pointers and sizes.
+ *
+ * The path: the Gaussian signal covariance S (table or exact exp), the
+ * operator A = S + N (SN form) or A = w S w + I (W form), Jacobi-PCG on
+ * A x = b, and the map projection m = S_mp x.  Every function here replaces
+ * one call of the reference library (caseywstark/dachshund, lib/*.h); each
+ * declaration names the reference interface it stands in for.
+ *
+ * Conventions
+ *  - Host arrays are caller-owned; nothing here keeps a host pointer after
+ *    the call returns (lib/wf_vector.h:35,70 hold non-owning pointers; the
+ *    operator here copies the records into device memory instead).
+ *  - Pixel records are 5 doubles each, in the reference layouts
+ *    (lib/pixel.h:16-50): Pixel {x,y,z,n,d}, NPixel {x,y,z,N=n^2,d},
+ *    WPixel {x,y,z,w=1/n,wd=d/n}.  Points are 3 doubles {x,y,z}.
+ *  - Vectors passed to and from an operator are in the caller's record
+ *    order.  ``*_dev`` variants take device pointers (same order) and run on
+ *    the context's stream without a host synchronisation at the end.
+ *  - Every function returns a ds_status.  The reference reports errors by
+ *    exit(1) (I/O) or PCGResult.success (solver); here the caller decides.
+ *  - One context = one device + one CUDA stream.  Calls on one context are
+ *    sequential; distinct contexts may be used from distinct threads.
+ */
+#ifndef DS_GB300_H
+#define DS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+typedef enum {
+  DS_OK = 0,
+  DS_ERR_ARG = 1,           /* bad argument (null pointer, n <= 0, bad form) */
+  DS_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  DS_ERR_NOT_CONVERGED = 3, /* PCG hit max_iter (lib/pcg.h:151-155) */
+  DS_ERR_NORM_B = 4,        /* |b| <= 0: early return (lib/pcg.h:79-86) */
+  DS_ERR_OOM = 5,           /* device allocation failed */
+  DS_ERR_NO_DEVICE = 6,     /* no CUDA device or wrong architecture */
+  DS_ERR_STATE = 7          /* object used after a fatal error */
+} ds_status;
+
+const char* ds_status_string(int status);
+
+/* ---- kernel (signal covariance) parameters ----------------------------- */
+typedef enum { DS_FORM_SN = 0, DS_FORM_W = 1 } ds_form;
+
+typedef enum {
+  DS_EVAL_TABLE = 0, /* 200-knot exp table + linear interpolation, zero for
+                        c_perp*dperp^2 + c_para*dz^2 at or beyond the last
+                        interval (lib/signal_covar.h:53-77) */
+  DS_EVAL_EXACT = 1  /* var_s * exp(-arg) (lib/signal_covar.h:79-86), zero for
+                        arg >= exact_cutoff */
+} ds_eval;
+
+#define DS_TABLE_N 200                /* default_gaussian_table_n */
+#define DS_DEFAULT_EXACT_CUTOFF 40.0  /* exp(-40) = 4.2e-18 */
+
+typedef struct {
+  double var_s;          /* SignalCovarParams::var_s */
+  double l_perp;         /* -> gaussian_const_perp = 1/(2 l_perp^2) */
+  double l_para;         /* -> gaussian_const_para = 1/(2 l_para^2) */
+  int eval;              /* ds_eval */
+  double exact_cutoff;   /* exponent cutoff for DS_EVAL_EXACT; <= 0: default */
+  const double* table;   /* optional DS_TABLE_N host-built knots f_i (e.g.
+                            SignalCovarParams::func_table); NULL: built here */
+} ds_kernel_params;
+
+/* SignalCovarParams ctor (lib/signal_covar.h:19-41): fills the 200-knot
+ * table f_i = exp(-i dx), dx = 8/199, and the index scale 1/dx. */
+void ds_table_init(double* table, double* dx_inv);
+
+/* signal_covar / signal_covar_exact (lib/signal_covar.h:67-86) evaluated on
+ * the device for n (perp^2, para^2) pairs; host arrays. */
+int ds_signal_covar(const ds_kernel_params* kp, int n, const double* perp2,
+                    const double* para2, double* out);
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct ds_context ds_context;
+
+int ds_context_create(int device, ds_context** out);
+void ds_context_destroy(ds_context* ctx);
+/* The context's CUDA stream (a cudaStream_t) for event timing and for
+ * ordering caller work against the *_dev entry points. */
+void* ds_context_stream(ds_context* ctx);
+int ds_context_synchronize(ds_context* ctx);
+/* Message of the last failed call on this context ("" when none). */
+const char* ds_context_last_error(ds_context* ctx);
+
+/* ---- the operator A over one pixel set --------------------------------- */
+typedef struct ds_operator ds_operator;
+
+/* WFVectorSN / WFVectorW ctor (lib/wf_vector.h:37-46, 72-81).  ``records``:
+ * n NPixel (form SN) or WPixel (form W) records.  Copies them to the device
+ * in a spatially sorted, tiled layout and builds the culled tile-pair list. */
+int ds_operator_create(ds_context* ctx, int form, int n, const double* records,
+                       const ds_kernel_params* kp, ds_operator** out);
+void ds_operator_destroy(ds_operator* op);
+
+/* Statistics of the tiling: tiles, interacting tile pairs, evaluated pairs
+ * per matvec (tile pairs x tile^2), and the tile size. */
+typedef struct {
+  int n;
+  int n_pad;
+  int tile;
+  int n_tiles;
+  long long n_tile_pairs;
+  long long evaluated_pairs;
+} ds_operator_info;
+int ds_operator_get_info(ds_operator* op, ds_operator_info* info);
+
+/* WFVector{SN,W}::A_product, b = A a (lib/wf_vector.cc:51-74, 196-220). */
+int ds_A_product(ds_operator* op, const double* a, double* b);
+int ds_A_product_dev(ds_operator* op, const double* a, double* b);
+
+/* WFVector{SN,W}::A_residual, r = b - A x (lib/wf_vector.cc:76-103,
+ * 222-251), b = d (SN) or wd (W) from the records. */
+int ds_A_residual(ds_operator* op, const double* x, double* r);
+int ds_A_residual_dev(ds_operator* op, const double* x, double* r);
+
+/* WFVector{SN,W}::preconditioner_solve, x = M^-1 b (lib/wf_vector.cc:42-49,
+ * 185-194). */
+int ds_preconditioner_solve(ds_operator* op, const double* b, double* x);
+
+/* WFVector{SN,W}::norm_b (lib/wf_vector.cc:105-112, 253-260). */
+int ds_norm_b(ds_operator* op, double* norm_b);
+
+/* WFVector{SN,W}::A(i, j, exact) (lib/wf_vector.cc:16-40, 157-183) for m
+ * index pairs, evaluated on the device.  ``eval``: DS_EVAL_TABLE,
+ * DS_EVAL_EXACT (the reference's ``exact`` flag), or -1 for the operator's
+ * own mode. */
+int ds_A_entries(ds_operator* op, int eval, int m, const int* ii,
+                 const int* jj, double* out);
+
+/* ---- PCG ---------------------------------------------------------------- */
+/* PCGParams (lib/pcg.h:13-19); n is the operator's. */
+typedef struct {
+  int max_iter;
+  int step_r;
+  double tol;
+  int verbose;  /* print the reference's per-iteration trace to stdout */
+} ds_pcg_params;
+
+/* PCGResult (lib/pcg.h:21-25) minus the history vector, which is written
+ * to the caller's buffer. */
+typedef struct {
+  int success;        /* PCGResult::success */
+  int num_iters;      /* PCGResult::num_iters */
+  double norm_b;      /* |b| */
+  double final_norm;  /* last |r| */
+  int n_outer;        /* FP64 true-residual evaluations (mixed form) */
+  int n_inner;        /* FP32 iterations (mixed form) */
+  double seconds;     /* device time of the solve */
+} ds_pcg_result;
+
+/* WFVector{SN,W}::solve_pcg (lib/wf_vector.cc:114-121, 263-274) driving
+ * pcg_solve (lib/pcg.h:67-160): x holds the initial guess on entry and the
+ * solution (multiplied by w in the W form) on return.  ``residual_norms``
+ * may be NULL or hold max_iter + 1 doubles; it receives |r| per iteration as
+ * PCGResult::residual_norms does.  Returns DS_OK, DS_ERR_NOT_CONVERGED or
+ * DS_ERR_NORM_B (with the result filled in each case). */
+int ds_solve_pcg(ds_operator* op, const ds_pcg_params* pp, double* x,
+                 ds_pcg_result* res, double* residual_norms);
+int ds_solve_pcg_dev(ds_operator* op, const ds_pcg_params* pp, double* x,
+                     ds_pcg_result* res, double* residual_norms);
+
+/* ---- map projection ----------------------------------------------------- */
+typedef struct ds_map ds_map;
+
+/* A map grid or point set, sorted and tiled on the device once. */
+int ds_map_create(ds_context* ctx, int n_map, const double* map_points,
+                  ds_map** out);
+void ds_map_destroy(ds_map* map);
+
+/* smp_product (lib/map.cc:20-43): m_i = sum_j S(map_i, pix_j) x_j with the
+ * operator's pixels and kernel; x in the operator's record order. */
+int ds_map_product(ds_map* map, ds_operator* op, const double* x, double* m);
+int ds_map_product_dev(ds_map* map, ds_operator* op, const double* x,
+                       double* m);
+
+/* One-shot smp_product with the reference's argument list. */
+int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points,
+                   int n_map, const double* map_points,
+                   const ds_kernel_params* kp, const double* x, double* m);
+
+/* sigma_m_noise_dom (lib/map_covar.cc:11-38): sigma_m_i = sum_j S_ij^2 / N_j
+ * over NPixel records. */
+int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels,
+                         int n_map, const double* map_points,
+                         const ds_kernel_params* kp, double* sigma_m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DS_GB300_H */

@@ -1,0 +1,31 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built library")
+
+
+@pytest.fixture(scope="session")
+def ctx():
+    """One library context on cuda:0 for the GPU tests."""
+    from dachshund_gb300 import Context, build
+
+    build()
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="session")
+def golden():
+    import numpy as np
+
+    d = os.path.join(ROOT, "tests", "golden")
+    return {k: np.load(os.path.join(d, k + ".npz")) for k in ("config1", "small", "edge")}

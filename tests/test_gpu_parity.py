@@ -1,0 +1,207 @@
+"""GPU parity tests: the CUDA path through the C ABI against the reference's
+golden vectors (tests/golden, produced by the unmodified reference) and the
+CPU oracle (oracle/), on the same seeded inputs.
+
+Tolerances (FP64 plain path):
+  * A(i, j) entries, table kernel: bit-exact (same operation order);
+  * matvecs / residuals / maps: 1e-12 relative to max |value| (the GPU sums
+    in tile order instead of record order);
+  * PCG: the solution within 1e-8 relative of the reference's at a forced
+    equal iteration count (tol 0, max_iter = the reference's count + 1), and
+    the converged iteration count within 2 of the reference's.  Residual
+    histories are compared over the first 20 iterations only: once CG loses
+    orthogonality, last-ulp differences (summation order, libm exp in the
+    table) move later residual norms by percents while the iterates still
+    agree to ~1e-10 (an independent numpy CG on the bit-identical operator
+    shows the same), so exact late histories are not a property either
+    implementation has.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from dachshund_gb300 import (DsError, MapGrid, PCGParams, SignalCovarParams, WFVectorSN,
+                             WFVectorW, pixel_to_npixel, pixel_to_wpixel, sigma_m_noise_dom,
+                             signal_covar, smp_product, synth)
+
+pytestmark = pytest.mark.gpu
+
+VS, LP, LQ = synth.VAR_S, synth.L_PERP, synth.L_PARA
+TABLE = SignalCovarParams(VS, LP, LQ)
+EXACT = SignalCovarParams(VS, LP, LQ, eval="exact")
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def make(ctx, form, pix, sp=TABLE):
+    if form == "sn":
+        return WFVectorSN(ctx, pixel_to_npixel(pix), sp), pixel_to_npixel(pix)
+    return WFVectorW(ctx, pixel_to_wpixel(pix), sp), pixel_to_wpixel(pix)
+
+
+def test_signal_covar_probes(golden):
+    e = golden["edge"]
+    s = signal_covar(e["probe_perp2"], e["probe_para2"], TABLE)
+    np.testing.assert_array_equal(s, e["probe_S"])
+    s = signal_covar(e["probe_perp2"], e["probe_para2"], EXACT)
+    np.testing.assert_allclose(s, e["probe_S_exact"], rtol=1e-15)
+
+
+@pytest.mark.parametrize("form", ["sn", "w"])
+def test_entries_bit_exact(ctx, golden, form):
+    g = golden["small"]
+    op, _ = make(ctx, form, g["pixels"])
+    np.testing.assert_array_equal(op.A(g["ii"], g["jj"], exact=False), g[f"Aij_table_{form}"])
+    # exp of arguments up to ~150: one ulp of the argument is ~3e-14 of the value.
+    np.testing.assert_allclose(op.A(g["ii"], g["jj"], exact=True), g[f"Aij_exact_{form}"],
+                               rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("form", ["sn", "w"])
+def test_A_product_residual_golden(ctx, golden, form):
+    g = golden["small"]
+    op, _ = make(ctx, form, g["pixels"])
+    assert rel(op.A_product(g["a"]), g[f"Aa_{form}"]) < 1e-12
+    assert rel(op.A_residual(g["a"]), g[f"r_{form}"]) < 1e-12
+
+
+@pytest.mark.parametrize("form", ["sn", "w"])
+def test_preconditioner_and_norm_b(ctx, golden, form):
+    g = golden["small"]
+    op, rec = make(ctx, form, g["pixels"])
+    b = np.random.default_rng(2).standard_normal(op.n)
+    k = oracle._kernel(VS, LP, LQ, False)
+    want = np.empty_like(b)
+    oracle.port_lib().dso_precond(oracle.C.byref(k), oracle._form(form), op.n, rec, b, want)
+    np.testing.assert_array_equal(op.preconditioner_solve(b), want)
+    assert op.norm_b() == oracle.port_lib().dso_norm_b(oracle._form(form), op.n, rec)
+
+
+@pytest.mark.parametrize("form", ["sn", "w"])
+@pytest.mark.parametrize("tol,step_r,key", [(1e-8, 50, ""), (1e-4, 10, "4")])
+def test_pcg_golden(ctx, golden, form, tol, step_r, key):
+    g = golden["small"]
+    op, _ = make(ctx, form, g["pixels"])
+    ref_iters = int(g[f"iters{key}_{form}"])
+    x, res = op.solve_pcg(PCGParams(1000, step_r, tol))
+    assert res.success
+    assert abs(res.num_iters - ref_iters) <= 2
+    assert res.final_norm <= tol * res.norm_b
+    assert rel(x, g[f"x{key}_{form}"]) < 1e-8
+    hist = g[f"hist{key}_{form}"]
+    k = min(20, hist.size, res.residual_norms.size)
+    np.testing.assert_allclose(res.residual_norms[:k], hist[:k], rtol=1e-9)
+    # forced equal iteration count
+    xf, resf = op.solve_pcg(PCGParams(ref_iters + 1, step_r, 0.0))
+    assert resf.num_iters == ref_iters + 1 and not resf.success
+    assert rel(xf, g[f"x{key}_{form}"]) < 1e-8
+
+
+def test_map_and_noise_golden(ctx, golden):
+    g = golden["small"]
+    pix = g["pixels"]
+    m = smp_product(ctx, pix[:, :3], g["map_pts"], TABLE, g["x_w"])
+    assert rel(m, g["map"]) < 1e-12
+    op, _ = make(ctx, "w", pix)
+    grid = MapGrid(ctx, g["map_pts"])
+    assert rel(grid.product(op, g["x_w"]), g["map"]) < 1e-12
+    s = sigma_m_noise_dom(ctx, pixel_to_npixel(pix), g["map_pts"], TABLE)
+    assert rel(s, g["sigma_nd"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["n1", "n7", "coinc"])
+@pytest.mark.parametrize("form", ["sn", "w"])
+def test_edge_golden(ctx, golden, case, form):
+    e = golden["edge"]
+    op, _ = make(ctx, form, e[f"{case}_pixels"])
+    assert rel(op.A_product(e[f"{case}_a"]), e[f"{case}_Aa_{form}"]) < 1e-13
+    x, res = op.solve_pcg(PCGParams(100, 50, 1e-10))
+    assert abs(res.num_iters - int(e[f"{case}_iters_{form}"])) <= 1
+    assert int(res.success) == int(e[f"{case}_ok_{form}"])
+    assert rel(x, e[f"{case}_x_{form}"]) < 1e-8
+
+
+def test_config1_app_path(ctx, golden):
+    """The reference app's path (app/dachshund.cc:229-264) on 4,096 pixels:
+    W-form PCG to 1e-5 then smp_product on the 32x32x128 grid.  Same
+    iteration count as the reference and the map within 1e-8 relative."""
+    g = golden["config1"]
+    pix = g["pixels"]
+    lx, ly, lz, nx, ny, nz, tol, max_iter, step_r = g["params"]
+    op = WFVectorW(ctx, pixel_to_wpixel(pix), TABLE)
+    x, res = op.solve_pcg(PCGParams(int(max_iter), int(step_r), tol))
+    assert res.success and res.num_iters == int(g["num_iters"])
+    assert rel(x, g["x"]) < 1e-8
+    grid = MapGrid(ctx, synth.uniform_map_coords(lx, ly, lz, int(nx), int(ny), int(nz)))
+    m = grid.product(op, x)
+    assert rel(m, g["map"]) < 1e-8
+
+
+@pytest.mark.parametrize("form", ["sn", "w"])
+def test_exact_mode_vs_oracle(ctx, form):
+    w = synth.small(12, 24, 10.0, seed=5)
+    op, rec = make(ctx, form, w.pixels, EXACT)
+    a = np.random.default_rng(4).standard_normal(w.n)
+    want = oracle.A_product(form, rec, a, VS, LP, LQ, exact=True)
+    assert rel(op.A_product(a), want) < 1e-12
+    x, res = op.solve_pcg(PCGParams(1000, 50, 1e-10))
+    xo, ok, it, _ = oracle.solve_pcg(form, rec, VS, LP, LQ, 1000, 50, 1e-10, exact=True)
+    assert res.success and ok
+    assert abs(res.num_iters - it) <= 1
+    assert rel(x, xo) < 1e-8
+
+
+def test_random_cloud_ragged_tiles(ctx):
+    """Unstructured points, n not a multiple of the tile, table mode."""
+    rng = np.random.default_rng(9)
+    n = 3001
+    pix = np.empty((n, 5))
+    pix[:, :3] = rng.uniform(0, 25.0, (n, 3))
+    pix[:, 3] = rng.uniform(0.05, 0.3, n)
+    pix[:, 4] = rng.standard_normal(n)
+    for form in ("sn", "w"):
+        op, rec = make(ctx, form, pix)
+        a = rng.standard_normal(n)
+        assert rel(op.A_product(a), oracle.A_product(form, rec, a, VS, LP, LQ)) < 1e-12
+    mp = rng.uniform(0, 25.0, (777, 3))
+    x = rng.standard_normal(n)
+    assert rel(smp_product(ctx, pix[:, :3], mp, TABLE, x),
+               oracle.smp_product(pix[:, :3], mp, x, VS, LP, LQ)) < 1e-12
+
+
+def test_device_entry_points(ctx, golden):
+    torch = pytest.importorskip("torch")
+    g = golden["small"]
+    op, _ = make(ctx, "w", g["pixels"])
+    a = torch.tensor(g["a"], dtype=torch.float64, device="cuda")
+    b = torch.empty_like(a)
+    torch.cuda.synchronize()
+    op.A_product_dev(a, b)
+    ctx.synchronize()
+    assert rel(b.cpu().numpy(), g["Aa_w"]) < 1e-12
+    x = torch.zeros_like(a)
+    res = op.solve_pcg_dev(PCGParams(1000, 50, 1e-8), x)
+    ctx.synchronize()
+    assert res.success and abs(res.num_iters - int(g["iters_w"])) <= 2
+    assert rel(x.cpu().numpy(), g["x_w"]) < 1e-8
+
+
+def test_error_behaviour(ctx):
+    pix = np.array([[1.0, 1.0, 1.0, 0.2, 0.0], [2.0, 1.0, 1.0, 0.1, 0.0]])
+    op = WFVectorW(ctx, pixel_to_wpixel(pix), TABLE)
+    # |b| = 0: early return (lib/pcg.h:79-86); the W form still scales x by w.
+    x0 = np.array([1.0, 2.0])
+    x, res = op.solve_pcg(PCGParams(10, 5, 1e-8), x0)
+    assert not res.success and res.status == 4
+    np.testing.assert_allclose(x, x0 * pixel_to_wpixel(pix)[:, 3])
+    # max_iter reached (lib/pcg.h:151-155)
+    g = synth.small(8, 16, 8.0, seed=2)
+    op = WFVectorW(ctx, pixel_to_wpixel(g.pixels), TABLE)
+    x, res = op.solve_pcg(PCGParams(5, 50, 1e-14))
+    assert not res.success and res.num_iters == 5 and res.status == 3
+    with pytest.raises(DsError):
+        WFVectorW(ctx, np.zeros((0, 5)), TABLE)
+    with pytest.raises(ValueError):
+        op.A_product(np.zeros(3))
