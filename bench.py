@@ -1,0 +1,402 @@
+#!/usr/bin/env python3
+"""Wiener-filter solve benchmark on GB300.
+
+One step = one full Wiener-filter solve of the chosen form on the 262,144-pixel
+workload (1,024 skewers x 256 pixels in [0,80)^2 x [0,512) Mpc/h, GRF data,
+exact Gaussian kernel var_s 0.0625, l_perp 2.5, l_para 2.0): mixed-precision
+PCG (FP32 inner, FP64 reliable updates) from x = 0 to |b - A x| <= 1e-8 |b|,
+then the map m = S_mp x on the 80 x 80 x 512 grid (FP32 evaluation, FP64
+accumulation).  The plain FP64 GPU PCG + FP64 map on the same system is run
+once beside it, as the metric asks ("chosen form vs plain FP64 GPU PCG").
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas (the solve does not shard here); rank 0
+prints one JSON line.  ``--impl reference`` times the reference's algorithm
+on the host cores (the C/OpenMP restatement in oracle/, bit-exact with the
+reference; the reference itself cannot be built on the GPU host) on a bounded
+sample of rows, extrapolated to the full solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "WF solve time & CG iters to 1e-8 resid: chosen form vs plain FP64 GPU PCG"
+SMS = 152
+# Per-SM pipe rates measured on this machine's GB300 (profiles/pipe_rates.md):
+# FP32 FMA 128 lanes/clk, MUFU ex2 32/clk, FP64 FMA 2/clk.
+FMA_LANES, MUFU_RATE, DFMA_RATE = 128.0, 32.0, 2.0
+# FP32 inner kernel (EXPANDED): 4 FMA lanes + 1 ex2 per pair; map kernel
+# (DIRECT): 7 FMA lanes + 1 ex2 per pair.
+PAIRS_PER_CLK = {"expanded": min(FMA_LANES / 4, MUFU_RATE), "direct": min(FMA_LANES / 7, MUFU_RATE)}
+# Plain FP64 iteration count of the workload (tol 1e-8, exact kernel), for the
+# CPU-baseline extrapolation of the reference arm.
+REF_ITERS = {"wf-262144px-grf": 162, "wf-32768px-grf": 150}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config3", choices=["config2", "config3"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--cpu-sample-s", type=float, default=6.0,
+                    help="seconds of CPU work per baseline sample")
+    return ap.parse_args()
+
+
+def dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(name):
+    from dachshund_gb300 import synth
+
+    return getattr(synth, name)()
+
+
+def cpu_baseline(w, iters, target_s):
+    """Times the C/OpenMP restatement of the reference (oracle port, bit-exact
+    with it) on the host cores on rows of one A_product and of smp_product and
+    extrapolates to the full solve (iters matvecs + 1 residual + iters //
+    step_r residuals + the map).  It runs the reference's table kernel, the
+    one its app uses, which costs less per pair than exp."""
+    import numpy as np
+
+    import oracle
+    from dachshund_gb300 import api, synth
+
+    rec = api.pixel_to_wpixel(w.pixels)
+    a = np.random.default_rng(0).standard_normal(w.n)
+    pts = synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz)
+
+    def rate(fn, rows_total, cols):
+        r = 64
+        t0 = time.perf_counter()
+        fn(0, r)
+        dt = time.perf_counter() - t0
+        r = int(min(rows_total, max(256, target_s / 2 / max(dt / r, 1e-9))))
+        t0 = time.perf_counter()
+        fn(0, r)
+        dt = time.perf_counter() - t0
+        return dt / (r * cols), r, dt
+
+    t_op, r_op, d_op = rate(lambda r0, r1: oracle.A_product_rows(
+        "w", rec, a, r0, r1, w.var_s, w.l_perp, w.l_para, exact=False), w.n, w.n)
+    t_map, r_map, d_map = rate(lambda r0, r1: oracle.smp_product_rows(
+        w.pixels[:, :3], pts, a, r0, r1, w.var_s, w.l_perp, w.l_para, exact=False), w.n_map, w.n)
+    matvecs = iters + 1 + iters // w.pcg_step_r
+    total = t_op * w.n * w.n * matvecs + t_map * w.n_map * w.n
+    cores = os.cpu_count()
+    return {
+        "value": total, "unit": "s", "cores": cores, "kind": "port",
+        "sample": (f"rows [0,{r_op}) of A_product ({d_op:.1f} s) and rows [0,{r_map}) of "
+                   f"smp_product ({d_map:.1f} s), the reference's table kernel (its app path; "
+                   f"cheaper per pair than exp), OpenMP on {cores} host threads; "
+                   f"extrapolated to {matvecs} matvecs + the {w.n_map}-point map"),
+        "ns_per_pair": t_op * 1e9,
+    }
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    iters = REF_ITERS[w.name]
+    vals = []
+    base = None
+    for step in range(args.warmup + args.steps):
+        base = cpu_baseline(w, iters, args.cpu_sample_s)
+        if step >= args.warmup:
+            vals.append(base["value"])
+    value = statistics.mean(vals)
+    base["value"] = value
+    line = {
+        "metric": METRIC, "value": value, "unit": "s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "n_pixels": w.n, "n_map": w.n_map, "kernel": "exact",
+                   "form": "W", "tol": w.pcg_tol, "iters": iters,
+                   "sample": "bounded row sample, extrapolated"},
+        "cpu_baseline": base,
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from dachshund_gb300 import (Context, MapGrid, MixedParams, PCGParams, SignalCovarParams,
+                                 WFVectorW, pixel_to_wpixel, synth)
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as td
+
+            td.barrier()
+
+    def allmax(v):
+        if world == 1:
+            return v
+        import torch.distributed as td
+
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        return float(t.item())
+
+    w = workload(args.workload)
+    ctx = Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    sp = SignalCovarParams(w.var_s, w.l_perp, w.l_para, eval="exact")
+    rec = pixel_to_wpixel(w.pixels)
+    pts = synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz)
+    op = WFVectorW(ctx, rec, sp)
+    grid = MapGrid(ctx, pts)
+    mp = MixedParams(max_iter=3000, tol=w.pcg_tol)
+    x = torch.zeros(w.n, dtype=torch.float64, device="cuda")
+    m = torch.empty(w.n_map, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step():
+        with torch.cuda.stream(stream):
+            x.zero_()
+        res = op.solve_mixed_dev(mp, x)
+        grid.product_f32_dev(op, x, m)
+        return res
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    times, solve_prof, map_prof, results = [], [], [], []
+    launches0 = ctx.profile()["kernel_launches"]
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ctx.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        ctx.set_profiling(True)
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            x.zero_()
+        res = op.solve_mixed_dev(mp, x)
+        solve_prof.append(ctx.profile())
+        ctx.set_profiling(True)
+        grid.product_f32_dev(op, x, m)
+        e1.record(stream)
+        e1.synchronize()
+        map_prof.append(ctx.profile())
+        ctx.set_profiling(False)
+        torch.cuda.synchronize()
+        barrier()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        results.append(res)
+    launches = (ctx.profile()["kernel_launches"] - launches0) / args.steps
+    clk = clocks.stop()
+    step_s = allmax(statistics.mean(times))
+
+    # Kernel rooflines (CUDA events around every pair-kernel launch).
+    sm_hz = (clk["sm_mhz"] or 1900.0) * 1e6
+
+    def agg(profs, key):
+        return sum(p[key] for p in profs)
+
+    f32_ms = agg(solve_prof, "f32_ms")
+    f32_pairs = agg(solve_prof, "f32_evaluated")
+    f32_n = agg(solve_prof, "f32_launches")
+    f64_ms = agg(solve_prof, "f64_ms")
+    f64_pairs = agg(solve_prof, "f64_evaluated")
+    f64_n = agg(solve_prof, "f64_launches")
+    map_ms = agg(map_prof, "f32_ms")
+    map_pairs = agg(map_prof, "f32_evaluated")
+    kernels = {
+        "fp32_inner_matvec": {
+            "launches_per_step": f32_n / args.steps, "ms_per_step": f32_ms / args.steps,
+            "Gpair_per_s": f32_pairs / (f32_ms * 1e-3) / 1e9 if f32_ms else None,
+            "peak_Gpair_per_s": PAIRS_PER_CLK["expanded"] * SMS * sm_hz / 1e9},
+        "fp64_residual": {
+            "launches_per_step": f64_n / args.steps, "ms_per_step": f64_ms / args.steps,
+            "Gpair_per_s": f64_pairs / (f64_ms * 1e-3) / 1e9 if f64_ms else None},
+        "fp32_map": {
+            "ms_per_step": map_ms / args.steps,
+            "Gpair_per_s": map_pairs / (map_ms * 1e-3) / 1e9 if map_ms else None,
+            "peak_Gpair_per_s": PAIRS_PER_CLK["direct"] * SMS * sm_hz / 1e9},
+    }
+    k = kernels["fp32_inner_matvec"]
+    roofline = {
+        "kernel": "k_pair_f32 (FP32 inner matvec, exact kernel, MUFU ex2)",
+        "bound": "fp32-fma+mufu", "unit": "Gpair/s",
+        "achieved": k["Gpair_per_s"], "peak": k["peak_Gpair_per_s"],
+        "frac": (k["Gpair_per_s"] / k["peak_Gpair_per_s"]) if k["Gpair_per_s"] else None,
+        "peak_basis": (f"{PAIRS_PER_CLK['expanded']:.0f} pairs/clk/SM (4 FMA lanes + 1 ex2 per "
+                       f"pair; FMA 128 lanes/clk/SM, ex2 32/clk/SM measured) x {SMS} SMs x "
+                       f"median SM clock under load"),
+        "traffic": None,
+    }
+
+    # Plain FP64 GPU PCG on the same system (once, untimed by the step loop).
+    plain = None
+    r0 = results[-1]
+    m_chosen = m.cpu().numpy()
+    if not args.no_plain:
+        xp = torch.zeros_like(x)
+        mpl = torch.empty_like(m)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rp = op.solve_pcg_dev(PCGParams(3000, w.pcg_step_r, w.pcg_tol), xp)
+        t_solve = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        grid.product_dev(op, xp, mpl)
+        ctx.synchronize()
+        t_map = time.perf_counter() - t0
+        mref = mpl.cpu().numpy()
+        plain = {"solve_s": rp.seconds, "map_s": t_map, "total_s": rp.seconds + t_map,
+                 "iters": rp.num_iters, "success": rp.success}
+        map_err = float(np.max(np.abs(m_chosen - mref)) / np.max(np.abs(mref)))
+        x_err = float(torch.max(torch.abs(x - xp)).item() / torch.max(torch.abs(xp)).item())
+        del t_solve
+
+    # End to end through the public API with host buffers.
+    e2e_times = []
+    h2d = rec.nbytes + w.n * 8 + pts.nbytes
+    d2h = w.n * 8 + w.n_map * 8
+    for _ in range(min(args.steps, 3)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op_h = WFVectorW(ctx, rec, sp)
+        xh, rh = op_h.solve_mixed(mp)
+        grid_h = MapGrid(ctx, pts)
+        mh = grid_h.product_f32(op_h, xh)
+        e2e_times.append(time.perf_counter() - t0)
+        grid_h.close()
+        op_h.close()
+    e2e = allmax(statistics.mean(e2e_times))
+
+    base = cpu_baseline(w, plain["iters"] if plain else REF_ITERS[w.name], args.cpu_sample_s) \
+        if rank == 0 else None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner / f64 outer",
+            "data": "synthetic (seeded GRF skewers of the workload's shapes)",
+            "config": {"workload": w.name, "n_pixels": w.n, "n_map": w.n_map,
+                       "kernel": "exact (var_s 0.0625, l_perp 2.5, l_para 2.0)", "form": "W",
+                       "tol": w.pcg_tol, "parallelism": f"replicas x{world}",
+                       "l2": "flushed between steps (256 MiB write)"},
+            "cg_iters": r0.num_iters, "fp64_updates": r0.n_outer,
+            "final_rel_residual": r0.final_norm / r0.norm_b,
+            "plain_fp64": plain,
+            "speedup_vs_plain": (plain["total_s"] / step_s) if plain else None,
+            "map_err_vs_fp64": map_err if plain else None,
+            "x_err_vs_fp64": x_err if plain else None,
+            "roofline": roofline,
+            "kernels": kernels,
+            "cpu_baseline": base,
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

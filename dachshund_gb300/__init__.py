@@ -7,6 +7,7 @@ map projection, as hand-written CUDA kernels behind the C ABI of
 from .api import (  # noqa: F401
     Context,
     MapGrid,
+    MixedParams,
     PCGParams,
     PCGResult,
     SignalCovarParams,

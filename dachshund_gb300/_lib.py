@@ -61,6 +61,16 @@ class PcgResultC(C.Structure):
     ]
 
 
+class MixedParamsC(C.Structure):
+    _fields_ = [
+        ("max_iter", C.c_int),
+        ("tol", C.c_double),
+        ("reliable_delta", C.c_double),
+        ("inner_cutoff", C.c_double),
+        ("verbose", C.c_int),
+    ]
+
+
 class OperatorInfoC(C.Structure):
     _fields_ = [
         ("n", C.c_int),
@@ -69,6 +79,21 @@ class OperatorInfoC(C.Structure):
         ("n_tiles", C.c_int),
         ("n_tile_pairs", C.c_longlong),
         ("evaluated_pairs", C.c_longlong),
+    ]
+
+
+class ProfileC(C.Structure):
+    _fields_ = [
+        ("pair_launches", C.c_longlong),
+        ("pair_ms", C.c_double),
+        ("pair_evaluated", C.c_double),
+        ("kernel_launches", C.c_longlong),
+        ("f64_launches", C.c_longlong),
+        ("f64_ms", C.c_double),
+        ("f64_evaluated", C.c_double),
+        ("f32_launches", C.c_longlong),
+        ("f32_ms", C.c_double),
+        ("f32_evaluated", C.c_double),
     ]
 
 
@@ -88,6 +113,8 @@ SIGNATURES = {
     "ds_context_stream": (_vp, [_vp]),
     "ds_context_synchronize": (_i, [_vp]),
     "ds_context_last_error": (C.c_char_p, [_vp]),
+    "ds_context_set_profiling": (_i, [_vp, _i]),
+    "ds_context_get_profile": (_i, [_vp, C.POINTER(ProfileC)]),
     "ds_operator_create": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), C.POINTER(_vp)]),
     "ds_operator_destroy": (None, [_vp]),
     "ds_operator_get_info": (_i, [_vp, C.POINTER(OperatorInfoC)]),
@@ -100,6 +127,10 @@ SIGNATURES = {
     "ds_A_entries": (_i, [_vp, _i, _i, _ip, _ip, _dp]),
     "ds_solve_pcg": (_i, [_vp, C.POINTER(PcgParamsC), _dp, C.POINTER(PcgResultC), _dp]),
     "ds_solve_pcg_dev": (_i, [_vp, C.POINTER(PcgParamsC), _vp, C.POINTER(PcgResultC), _dp]),
+    "ds_solve_mixed": (_i, [_vp, C.POINTER(MixedParamsC), _dp, C.POINTER(PcgResultC), _dp]),
+    "ds_solve_mixed_dev": (_i, [_vp, C.POINTER(MixedParamsC), _vp, C.POINTER(PcgResultC), _dp]),
+    "ds_map_product_f32": (_i, [_vp, _vp, _d, _dp, _dp]),
+    "ds_map_product_f32_dev": (_i, [_vp, _vp, _d, _vp, _vp]),
     "ds_map_create": (_i, [_vp, _i, _dp, C.POINTER(_vp)]),
     "ds_map_destroy": (None, [_vp]),
     "ds_map_product": (_i, [_vp, _vp, _dp, _dp]),

@@ -90,6 +90,21 @@ class PCGParams:
 
 
 @dataclasses.dataclass
+class MixedParams:
+    """Mixed-precision solve: FP32 PCG inside FP64 reliable updates."""
+
+    max_iter: int = 2000
+    tol: float = 1e-8
+    reliable_delta: float = 0.0   # <= 0: 1e-4
+    inner_cutoff: float = 0.0     # <= 0: 24
+    verbose: bool = False
+
+    def as_c(self):
+        return _lib.MixedParamsC(self.max_iter, self.tol, self.reliable_delta, self.inner_cutoff,
+                                 int(bool(self.verbose)))
+
+
+@dataclasses.dataclass
 class PCGResult:
     """lib/pcg.h:21-25, plus device timing and mixed-precision counters."""
 
@@ -143,6 +158,15 @@ class Context:
 
     def synchronize(self):
         self.check(self._lib.ds_context_synchronize(self.handle), "synchronize")
+
+    def set_profiling(self, enable: bool):
+        """Time every pair-kernel launch with CUDA events on this context's stream."""
+        self.check(self._lib.ds_context_set_profiling(self.handle, int(bool(enable))), "profiling")
+
+    def profile(self) -> dict:
+        p = _lib.ProfileC()
+        self.check(self._lib.ds_context_get_profile(self.handle, C.byref(p)), "profile")
+        return {k: getattr(p, k) for k, _ in p._fields_}
 
     def close(self):
         """Destroys the operators and maps made on this context, then the context."""
@@ -259,6 +283,27 @@ class _WFVector:
         """In-place solve on a CUDA float64 tensor (initial guess in, solution out)."""
         return self._solve(self._lib.ds_solve_pcg_dev, pcg_params, x, True)
 
+    def _solve_mixed(self, fn, mp: MixedParams, x, dev: bool):
+        c = mp.as_c()
+        res = _lib.PcgResultC()
+        hist = np.zeros(max(mp.max_iter, 1) + 2)
+        xp = _dev_ptr(x, self.n) if dev else _ptr(x)
+        rc = fn(self.handle, C.byref(c), xp, C.byref(res), _ptr(hist))
+        if rc not in (_lib.DS_OK, _lib.DS_ERR_NOT_CONVERGED, _lib.DS_ERR_NORM_B):
+            self.ctx.check(rc, fn.__name__)
+        nh = 0 if rc == _lib.DS_ERR_NORM_B else min(hist.size, res.n_inner + 1)
+        return PCGResult(bool(res.success), res.num_iters, hist[:nh].copy(), res.norm_b,
+                         res.final_norm, rc, res.seconds, res.n_outer, res.n_inner)
+
+    def solve_mixed(self, mp: MixedParams = None, x=None):
+        """Mixed-precision solve (exact kernel); returns (x, PCGResult)."""
+        mp = mp or MixedParams()
+        x = np.zeros(self.n) if x is None else _f64(x, self.n, "x").copy()
+        return x, self._solve_mixed(self._lib.ds_solve_mixed, mp, x, False)
+
+    def solve_mixed_dev(self, mp: MixedParams, x):
+        return self._solve_mixed(self._lib.ds_solve_mixed_dev, mp, x, True)
+
 
 class WFVectorSN(_WFVector):
     """x = (S + N)^-1 d over NPixel records {x, y, z, N, d}."""
@@ -300,6 +345,20 @@ class MapGrid:
         self.ctx.check(self._lib.ds_map_product_dev(self.handle, op.handle, _dev_ptr(x, op.n),
                                                     _dev_ptr(m, self.n_map)),
                        "ds_map_product_dev")
+
+    def product_f32(self, op: _WFVector, x, cutoff: float = 0.0):
+        """FP32-evaluated exact-kernel map product with FP64 accumulation."""
+        x = _f64(x, op.n, "x")
+        m = np.empty(self.n_map)
+        self.ctx.check(self._lib.ds_map_product_f32(self.handle, op.handle, cutoff, _ptr(x),
+                                                    _ptr(m)), "ds_map_product_f32")
+        return m
+
+    def product_f32_dev(self, op: _WFVector, x, m, cutoff: float = 0.0):
+        self.ctx.check(self._lib.ds_map_product_f32_dev(self.handle, op.handle, cutoff,
+                                                        _dev_ptr(x, op.n),
+                                                        _dev_ptr(m, self.n_map)),
+                       "ds_map_product_f32_dev")
 
     def close(self):
         if getattr(self, "handle", None):

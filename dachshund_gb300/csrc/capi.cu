@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "ds_device.cuh"
+#include "ds_f32.h"
 #include "ds_ops.h"
 
 using namespace ds;
@@ -207,6 +208,8 @@ void map_product_dev(ds_map* map, ds_operator* op, const double* x_dev, double* 
   a.out = m_dev;
   a.row_perm = map->pts.perm.p;
   a.table = op->table.p;
+  a.n_tile_pairs = map->pairs.n_pairs;
+  a.prof = &map->ctx->prof;
   launch_pair_f64(op->kc, EPI_MAP, a, st);
 }
 
@@ -268,6 +271,45 @@ int ds_context_synchronize(ds_context* ctx) {
 
 const char* ds_context_last_error(ds_context* ctx) {
   return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int ds_context_set_profiling(ds_context* ctx, int enable) {
+  if (!ctx) return DS_ERR_ARG;
+  return guarded(ctx, [&] {
+    Profiler& p = ctx->prof;
+    p.collect();
+    if (enable) {
+      if (!p.d_pairs) DS_CUDA(cudaMalloc(&p.d_pairs, 2 * sizeof(unsigned long long)));
+      DS_CUDA(cudaMemsetAsync(p.d_pairs, 0, 2 * sizeof(unsigned long long), ctx->stream));
+      DS_CUDA(cudaStreamSynchronize(ctx->stream));
+      p.launches[0] = p.launches[1] = 0;
+      p.ms[0] = p.ms[1] = 0.0;
+    }
+    p.enabled = enable != 0;
+  });
+}
+
+int ds_context_get_profile(ds_context* ctx, ds_profile* out) {
+  if (!ctx || !out) return DS_ERR_ARG;
+  return guarded(ctx, [&] {
+    Profiler& p = ctx->prof;
+    p.collect();
+    unsigned long long pairs[2] = {0, 0};
+    if (p.d_pairs) {
+      DS_CUDA(cudaStreamSynchronize(ctx->stream));
+      DS_CUDA(cudaMemcpy(pairs, p.d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost));
+    }
+    out->f64_launches = p.launches[0];
+    out->f64_ms = p.ms[0];
+    out->f64_evaluated = (double)pairs[0];
+    out->f32_launches = p.launches[1];
+    out->f32_ms = p.ms[1];
+    out->f32_evaluated = (double)pairs[1];
+    out->pair_launches = p.launches[0] + p.launches[1];
+    out->pair_ms = p.ms[0] + p.ms[1];
+    out->pair_evaluated = (double)pairs[0] + (double)pairs[1];
+    out->kernel_launches = launch_counter();
+  });
 }
 
 int ds_signal_covar(const ds_kernel_params* kp, int n, const double* perp2, const double* para2,
@@ -424,9 +466,14 @@ int ds_A_entries(ds_operator* op, int eval, int m, const int* ii, const int* jj,
   });
 }
 
-static int solve_common(ds_operator* op, const ds_pcg_params* pp, double* x, bool host,
-                        ds_pcg_result* res, double* residual_norms) {
-  if (!op || !pp || !x) return DS_ERR_ARG;
+}  // extern "C"
+
+// Shared frame of the solvers: initial guess in (host or device, caller
+// order), solve in sorted order, W-form scaling x *= w, solution out.
+template <class Solve>
+static int solve_common(ds_operator* op, double* x, bool host, ds_pcg_result* res,
+                        Solve&& solve) {
+  if (!op || !x) return DS_ERR_ARG;
   int status = DS_OK;
   const int rc = guarded(op->ctx, [&] {
     cudaStream_t st = op->ctx->stream;
@@ -444,7 +491,7 @@ static int solve_common(ds_operator* op, const ds_pcg_params* pp, double* x, boo
       r.norm_b = op->norm_b;
       status = DS_ERR_NORM_B;
     } else {
-      run_pcg(op, *pp, r, residual_norms);
+      solve(r);
       status = r.success ? DS_OK : DS_ERR_NOT_CONVERGED;
     }
     scatter_sorted(op->pix, op->x.p, op->form == DS_FORM_W ? op->wl.p : nullptr, xin, st);
@@ -457,14 +504,34 @@ static int solve_common(ds_operator* op, const ds_pcg_params* pp, double* x, boo
   return rc != DS_OK ? rc : status;
 }
 
+extern "C" {
+
 int ds_solve_pcg(ds_operator* op, const ds_pcg_params* pp, double* x, ds_pcg_result* res,
                  double* residual_norms) {
-  return solve_common(op, pp, x, true, res, residual_norms);
+  if (!pp) return DS_ERR_ARG;
+  return solve_common(op, x, true, res,
+                      [&](ds_pcg_result& r) { run_pcg(op, *pp, r, residual_norms); });
 }
 
 int ds_solve_pcg_dev(ds_operator* op, const ds_pcg_params* pp, double* x, ds_pcg_result* res,
                      double* residual_norms) {
-  return solve_common(op, pp, x, false, res, residual_norms);
+  if (!pp) return DS_ERR_ARG;
+  return solve_common(op, x, false, res,
+                      [&](ds_pcg_result& r) { run_pcg(op, *pp, r, residual_norms); });
+}
+
+int ds_solve_mixed(ds_operator* op, const ds_mixed_params* mp, double* x, ds_pcg_result* res,
+                   double* residual_norms) {
+  if (!mp) return DS_ERR_ARG;
+  return solve_common(op, x, true, res,
+                      [&](ds_pcg_result& r) { run_mixed(op, *mp, r, residual_norms); });
+}
+
+int ds_solve_mixed_dev(ds_operator* op, const ds_mixed_params* mp, double* x,
+                       ds_pcg_result* res, double* residual_norms) {
+  if (!mp) return DS_ERR_ARG;
+  return solve_common(op, x, false, res,
+                      [&](ds_pcg_result& r) { run_mixed(op, *mp, r, residual_norms); });
 }
 
 int ds_map_create(ds_context* ctx, int n_map, const double* map_points, ds_map** out) {
@@ -510,6 +577,31 @@ int ds_map_product(ds_map* map, ds_operator* op, const double* x, double* m) {
   });
 }
 
+int ds_map_product_f32_dev(ds_map* map, ds_operator* op, double cutoff, const double* x,
+                           double* m) {
+  if (!map || !op) return DS_ERR_ARG;
+  return guarded(map->ctx, [&] {
+    require(x && m, "null vector");
+    require(map->ctx == op->ctx, "map and operator belong to different contexts");
+    map_product_f32_dev(map, op, x, m, cutoff > 0.0 ? cutoff : 30.0);
+  });
+}
+
+int ds_map_product_f32(ds_map* map, ds_operator* op, double cutoff, const double* x, double* m) {
+  if (!map || !op) return DS_ERR_ARG;
+  return guarded(map->ctx, [&] {
+    require(x && m, "null vector");
+    require(map->ctx == op->ctx, "map and operator belong to different contexts");
+    cudaStream_t st = map->ctx->stream;
+    upload(x, op->n, op->io_a, st);
+    map->out_dev.alloc(map->pts.n);
+    map_product_f32_dev(map, op, op->io_a.p, map->out_dev.p, cutoff > 0.0 ? cutoff : 30.0);
+    DS_CUDA(cudaMemcpyAsync(m, map->out_dev.p, map->pts.n * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points, int n_map,
                    const double* map_points, const ds_kernel_params* kp, const double* x,
                    double* m) {
@@ -543,6 +635,8 @@ int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points, int n
     a.out = dm.p;
     a.row_perm = mp.perm.p;
     a.table = table.p;
+    a.n_tile_pairs = pl.n_pairs;
+    a.prof = &ctx->prof;
     launch_pair_f64(kc, EPI_MAP, a, st);
     DS_CUDA(cudaMemcpyAsync(m, dm.p, n_map * sizeof(double), cudaMemcpyDeviceToHost, st));
     DS_CUDA(cudaStreamSynchronize(st));
@@ -582,6 +676,8 @@ int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels, int 
     a.out = dm.p;
     a.row_perm = mp.perm.p;
     a.table = table.p;
+    a.n_tile_pairs = pl.n_pairs;
+    a.prof = &ctx->prof;
     launch_pair_f64(kc, EPI_NOISE, a, st);
     DS_CUDA(cudaMemcpyAsync(sigma_m, dm.p, n_map * sizeof(double), cudaMemcpyDeviceToHost, st));
     DS_CUDA(cudaStreamSynchronize(st));

@@ -1,0 +1,100 @@
+// FP32 side of the mixed-precision form: tile-relative scaled coordinates,
+// the FP32 pair-kernel arguments and the reliable-update PCG state.
+#pragma once
+
+#include <memory>
+
+#include "ds_internal.cuh"
+
+namespace ds {
+
+enum F32Formula { F32_EXPANDED = 0, F32_DIRECT = 1 };
+
+// Tile-relative FP32 coordinates of a PointSet, scaled so that
+// |dX|^2 = (c_perp dperp^2 + c_para dz^2) log2(e).
+struct F32Points {
+  DevBuf<float4> orig;  // per tile: origin (x, y, z, 0)
+  DevBuf<float4> xi;    // per point: (xi_x, xi_y, xi_z, |xi|^2)
+  double max_a = 0.0;   // max |xi|^2 (bounds 2^|xi|^2 of the EXPANDED formula)
+};
+
+void build_f32_points(F32Points& fp, const PointSet& ps, double sx, double sy, double sz,
+                      cudaStream_t st);
+
+struct F32Args {
+  const float4* rxi; const float4* rorig;
+  const float4* cxi; const float4* corig;
+  const int* row_ptr; const int* cols;
+  int n_row_tiles;
+  const float* colw;   // column weights (W: w_j, SN: 1)
+  const float* v;      // column vector
+  // EPI_PRODUCT
+  const float* rowf;   // wl_i var_s 2^-|xi_i|^2 (EXPANDED) or wl_i var_s (DIRECT)
+  const float* ediag;  // diagonal e_i
+  const float* vrow;   // row-side vector of the diagonal term
+  float* out;
+  const float* dotv;   // fused FP64 dot dotv . out -> *den_out, *alpha_out = *num / dot
+  double* dot_partial;
+  unsigned int* counter;
+  const double* num;
+  double* alpha_out;
+  double* den_out;
+  const int* skip_flag;
+  // EPI_MAP
+  const int* row_perm;
+  double* out64;
+  // profiling
+  long long n_tile_pairs;
+  unsigned long long* prof_pairs;
+  Profiler* prof;
+};
+
+void launch_pair_f32(int formula, int epi, const F32Args& a, cudaStream_t st);
+
+// Device state of the reliable-update mixed-precision PCG.
+struct MixedState {
+  double rz;          // r . z (FP32 vectors, FP64 sum)
+  double rz_old;
+  double alpha;
+  double beta;
+  double pq;
+  double rnorm;       // |r| of the FP32 recurrence
+  double rmax;        // largest |r| since the last reliable update
+  double rtrue;       // last FP64 true-residual norm
+  double norm_b;
+  double tol_norm_b;
+  double delta;       // reliable-update trigger: |r| < delta * rmax
+  int iter;           // FP32 iterations done
+  int max_iter;
+  int done;
+  int converged;
+  int need_update;    // a reliable update is due this iteration
+  int skip_update;    // == !need_update (skip flag of the update kernels)
+  int n_updates;      // FP64 residual evaluations
+  int pad;
+  unsigned int counter[4];
+};
+
+// FP32 operator data, built on the first mixed-precision call.
+struct OpF32 {
+  double inner_cut = 0.0;
+  int formula = F32_EXPANDED;
+  F32Points pts;
+  PairList pairs;
+  DevBuf<float> rowf, colw, ediag, pdiag;
+  DevBuf<float> p, q, r, z, xc;     // FP32 iteration vectors (sorted, padded)
+  DevBuf<MixedState> state;
+  DevBuf<double> hist, htrue;
+};
+
+// FP32 data of a map point set (DIRECT formula only).
+struct MapF32 {
+  unsigned long long op_serial = 0;
+  double cut = 0.0;
+  F32Points pts;
+  PairList pairs;
+  DevBuf<float> rowf;
+  DevBuf<float> xs;  // FP32 copy of the solution, sorted
+};
+
+}  // namespace ds

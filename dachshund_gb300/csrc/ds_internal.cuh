@@ -16,12 +16,18 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "ds_gb300.h"
 
 namespace ds {
+
+struct OpF32;   // ds_f32.h
+struct MapF32;  // ds_f32.h
+struct OpF32Deleter { void operator()(OpF32* p) const; };
+struct MapF32Deleter { void operator()(MapF32* p) const; };
 
 constexpr int TILE = 128;        // points per tile (rows per CTA in the FP64 kernels)
 constexpr int TABLE_N = DS_TABLE_N;
@@ -40,7 +46,14 @@ struct Error {
                         std::string(#call) + ": " + cudaGetErrorString(e_)}; \
   } while (0)
 
-#define DS_CHECK_LAUNCH() DS_CUDA(cudaGetLastError())
+// Every kernel launch of the library is followed by DS_CHECK_LAUNCH(), which
+// also counts it (process-wide).
+long long& launch_counter();
+#define DS_CHECK_LAUNCH()          \
+  do {                             \
+    ++::ds::launch_counter();      \
+    DS_CUDA(cudaGetLastError());   \
+  } while (0)
 
 inline void require(bool ok, const char* msg) {
   if (!ok) throw Error{DS_ERR_ARG, msg};
@@ -165,6 +178,31 @@ struct PairArgs {
   struct PcgState* pcg;
   unsigned int* counter;
   const double* table;  // TABLE_N knots
+  // profiling: total evaluated pairs of this launch, added on the device by
+  // launches that ran (not by those that exited on skip_flag)
+  long long n_tile_pairs;
+  unsigned long long* prof_pairs;
+  struct Profiler* prof;
+};
+
+// Per-context event timing of pair-kernel launches (ds_context_set_profiling).
+// Kinds: 0 = FP64 pair kernels, 1 = FP32 pair kernels.
+struct Profiler {
+  struct Pending {
+    cudaEvent_t start, stop;
+    int kind;
+  };
+  bool enabled = false;
+  std::vector<cudaEvent_t> free_events;
+  std::vector<Pending> pending;
+  long long launches[2] = {0, 0};
+  double ms[2] = {0.0, 0.0};
+  unsigned long long* d_pairs = nullptr;  // device counters of evaluated pairs, per kind
+  cudaEvent_t get_event();
+  void begin(cudaStream_t st, cudaEvent_t* ev);
+  void end(cudaStream_t st, cudaEvent_t start, int kind);
+  void collect();  // waits for pending events and folds them into the totals
+  ~Profiler();
 };
 
 void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a,
@@ -194,6 +232,7 @@ struct ds_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string last_error;
+  ds::Profiler prof;
 };
 
 struct ds_operator {
@@ -218,6 +257,7 @@ struct ds_operator {
   ds::HostBuf<double> h_io;        // pinned staging
   ds::HostBuf<int> h_flag;
   unsigned long long serial = 0;   // identity for caches keyed on operators
+  std::unique_ptr<ds::OpF32, ds::OpF32Deleter> f32;  // mixed-precision data (lazy)
 };
 
 struct ds_map {
@@ -228,4 +268,5 @@ struct ds_map {
   ds::KernelConsts kc{};
   ds::PairList pairs;
   ds::DevBuf<double> out_dev;  // caller-order map staging
+  std::unique_ptr<ds::MapF32, ds::MapF32Deleter> f32;  // FP32 map data (lazy)
 };

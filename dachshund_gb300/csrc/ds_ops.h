@@ -15,7 +15,11 @@ void op_apply_sorted(ds_operator* op, int epi, const double* v, double* out, cud
 void ensure_pcg_workspace(ds_operator* op);
 void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, double* hist_out);
 
-// Operator set-up helpers (capi.cu).
-void op_init_coeffs(ds_operator* op, const double* d_rec);
+// Mixed-precision form (mixed.cu).
+void ensure_op_f32(ds_operator* op, double inner_cut);
+void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
+               double* hist_out);
+void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
+                         double cut);
 
 }  // namespace ds

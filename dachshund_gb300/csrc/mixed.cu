@@ -1,0 +1,528 @@
+// Mixed-precision Jacobi-PCG: FP32 Krylov iteration with FP64 reliable
+// updates (residual replacement, in the manner of Sleijpen & van der Vorst).
+//
+//   FP64: the iterate x, the right-hand side b, the true residual
+//         r64 = b - A x (FP64 matrix-free kernel, same operator as the plain
+//         form), every CG scalar (r.z, p.q, |r| are FP32 vectors summed in
+//         FP64), and the stopping test |r64| <= tol |b|.
+//   FP32: the search direction p, q = A32 p (FP32 MUFU kernel), the residual
+//         recurrence r, z = M^-1 r and the correction x_c accumulated since
+//         the last reliable update.
+// A reliable update folds x_c into x, recomputes r64 in FP64 and restarts the
+// recurrence from float(r64) while keeping the search direction.  It fires
+// when the recurrence residual has dropped by `delta` since the last update,
+// when it reaches tol |b|, or at the iteration cap; the solve ends only on an
+// FP64 residual.  Per iteration: K1 q = A32 p (+ p.q, alpha), K2 the
+// recurrences, K3 the new direction; K4-K7 run only on update iterations
+// (otherwise they return at once on a device flag).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+#include "ds_device.cuh"
+#include "ds_f32.h"
+#include "ds_ops.h"
+
+namespace ds {
+
+void OpF32Deleter::operator()(OpF32* p) const { delete p; }
+void MapF32Deleter::operator()(MapF32* p) const { delete p; }
+
+namespace {
+
+constexpr int VB = 256;
+constexpr int VGRID_MAX = 1024;
+inline int vgrid(int n) { return std::max(1, std::min(VGRID_MAX, (n + VB - 1) / VB)); }
+
+const double LOG2E = 1.4426950408889634;
+
+// ---- FP32 point preparation ----------------------------------------------
+
+__global__ void k_f32_origins(int n_tiles, const double* __restrict__ box, double sx, double sy,
+                              double sz, float4* __restrict__ orig) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tiles) return;
+  const double* b = box + (size_t)t * 6;
+  orig[t] = make_float4((float)(0.5 * (b[0] + b[3]) * sx), (float)(0.5 * (b[1] + b[4]) * sy),
+                        (float)(0.5 * (b[2] + b[5]) * sz), 0.f);
+}
+
+__global__ void k_f32_xi(int n_pad, const double* __restrict__ x, const double* __restrict__ y,
+                         const double* __restrict__ z, double sx, double sy, double sz,
+                         const float4* __restrict__ orig, float4* __restrict__ xi,
+                         float* __restrict__ blockmax) {
+  __shared__ float sm[VB];
+  const int i = blockIdx.x * VB + threadIdx.x;
+  float a = 0.f;
+  if (i < n_pad) {
+    const float4 o = orig[i / TILE];
+    const float fx = (float)(x[i] * sx - (double)o.x);
+    const float fy = (float)(y[i] * sy - (double)o.y);
+    const float fz = (float)(z[i] * sz - (double)o.z);
+    a = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
+    xi[i] = make_float4(fx, fy, fz, a);
+  }
+  sm[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = VB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) blockmax[blockIdx.x] = sm[0];
+}
+
+// Row / column coefficients of the FP32 operator from the FP64 ones.
+__global__ void k_f32_coeffs(int n_pad, int expanded, double var_s, const float4* __restrict__ xi,
+                             const double* __restrict__ wl, const double* __restrict__ wr,
+                             const double* __restrict__ e, const double* __restrict__ pdiag,
+                             float* __restrict__ rowf, float* __restrict__ colw,
+                             float* __restrict__ ediag, float* __restrict__ pd) {
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n_pad; i += gridDim.x * VB) {
+    const double scale = expanded ? exp2(-(double)xi[i].w) : 1.0;
+    rowf[i] = (float)(wl[i] * var_s * scale);
+    colw[i] = (float)wr[i];
+    ediag[i] = (float)e[i];
+    pd[i] = (float)pdiag[i];
+  }
+}
+
+__global__ void k_fill_f32(int n, float v, float* __restrict__ out) {
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) out[i] = v;
+}
+
+__global__ void k_d2f(int n, const double* __restrict__ in, float* __restrict__ out) {
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) out[i] = (float)in[i];
+}
+
+// ---- the iteration kernels -----------------------------------------------
+
+// Zero test of the initial guess: flag = 1 when every entry is 0.
+__global__ void k_is_zero(int n, const double* __restrict__ x, int* __restrict__ flag) {
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB)
+    if (x[i] != 0.0) *flag = 0;
+}
+
+// r = float(r64) (or b when x0 == 0); z = r / pd; p = z; x_c = 0; r.z, |r|.
+__global__ void __launch_bounds__(VB) k_mx_init(int n, MixedState* st, const int* x_zero,
+                                                const double* __restrict__ b,
+                                                const double* __restrict__ r64,
+                                                float* __restrict__ r, float* __restrict__ z,
+                                                float* __restrict__ p, float* __restrict__ xc,
+                                                const float* __restrict__ pd,
+                                                double* __restrict__ part, double* hist,
+                                                double* htrue) {
+  __shared__ double red[VB / 32];
+  const bool zero = *x_zero != 0;
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
+    const double rd = zero ? b[i] : r64[i];
+    const float ri = (float)rd;
+    const float zi = ri / pd[i];
+    r[i] = ri;
+    z[i] = zi;
+    p[i] = zi;
+    xc[i] = 0.f;
+    rz = fma((double)ri, (double)zi, rz);
+    rr = fma(rd, rd, rr);
+  }
+  const double brz = block_sum<VB>(rz, red);
+  const double brr = block_sum<VB>(rr, red);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = brz;
+    part[2 * blockIdx.x + 1] = brr;
+  }
+  if (last_block_arrive(&st->counter[1])) {
+    const double trz = reduce_partials<VB>(part, gridDim.x, 2, 0, red);
+    const double trr = reduce_partials<VB>(part, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      st->rz = trz;
+      st->rnorm = st->rtrue = st->rmax = sqrt(trr);
+      st->iter = 0;
+      st->n_updates = 0;
+      st->need_update = 0;
+      st->skip_update = 1;
+      hist[0] = st->rtrue;
+      htrue[0] = st->rtrue;
+      st->converged = st->rtrue <= st->tol_norm_b ? 1 : 0;
+      st->done = (st->converged || st->max_iter <= 0) ? 1 : 0;
+      st->counter[1] = 0;
+    }
+  }
+}
+
+// K2: x_c += alpha p; r -= alpha q; z = r / pd; r.z, |r|; decide on an update.
+__global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, float* __restrict__ xc,
+                                                  float* __restrict__ r, float* __restrict__ z,
+                                                  const float* __restrict__ p,
+                                                  const float* __restrict__ q,
+                                                  const float* __restrict__ pd,
+                                                  double* __restrict__ part, double* hist) {
+  if (st->done) return;
+  __shared__ double red[VB / 32];
+  const float alpha = (float)st->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
+    xc[i] = fmaf(alpha, p[i], xc[i]);
+    const float ri = fmaf(-alpha, q[i], r[i]);
+    const float zi = ri / pd[i];
+    r[i] = ri;
+    z[i] = zi;
+    rz = fma((double)ri, (double)zi, rz);
+    rr = fma((double)ri, (double)ri, rr);
+  }
+  const double brz = block_sum<VB>(rz, red);
+  const double brr = block_sum<VB>(rr, red);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = brz;
+    part[2 * blockIdx.x + 1] = brr;
+  }
+  if (last_block_arrive(&st->counter[1])) {
+    const double trz = reduce_partials<VB>(part, gridDim.x, 2, 0, red);
+    const double trr = reduce_partials<VB>(part, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      st->rz_old = st->rz;
+      st->rz = trz;
+      st->rnorm = sqrt(trr);
+      const int it = st->iter + 1;
+      st->iter = it;
+      hist[it] = st->rnorm;
+      st->rmax = fmax(st->rmax, st->rnorm);
+      const bool upd = st->rnorm < st->delta * st->rmax || st->rnorm <= st->tol_norm_b ||
+                       it >= st->max_iter;
+      st->need_update = upd ? 1 : 0;
+      st->skip_update = upd ? 0 : 1;
+      st->beta = st->rz / st->rz_old;
+      st->counter[1] = 0;
+    }
+  }
+}
+
+// K3: p = z + beta p (not on update iterations).
+__global__ void __launch_bounds__(VB) k_mx_dir(int n, const MixedState* st,
+                                               const float* __restrict__ z,
+                                               float* __restrict__ p) {
+  if (st->done || st->need_update) return;
+  const float beta = (float)st->beta;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB)
+    p[i] = fmaf(beta, p[i], z[i]);
+}
+
+// K4: x += x_c (FP64); x_c = 0.
+__global__ void __launch_bounds__(VB) k_mx_fold(int n, const MixedState* st,
+                                                double* __restrict__ x,
+                                                float* __restrict__ xc) {
+  if (st->done || !st->need_update) return;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
+    x[i] += (double)xc[i];
+    xc[i] = 0.f;
+  }
+}
+
+// K6: r = float(r64); z = r / pd; r.z and |r64| (FP64); stop or continue.
+__global__ void __launch_bounds__(VB) k_mx_replace(int n, MixedState* st,
+                                                   const double* __restrict__ r64,
+                                                   float* __restrict__ r, float* __restrict__ z,
+                                                   const float* __restrict__ pd,
+                                                   double* __restrict__ part, double* hist,
+                                                   double* htrue) {
+  if (st->done || !st->need_update) return;
+  __shared__ double red[VB / 32];
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
+    const double rd = r64[i];
+    const float ri = (float)rd;
+    const float zi = ri / pd[i];
+    r[i] = ri;
+    z[i] = zi;
+    rz = fma((double)ri, (double)zi, rz);
+    rr = fma(rd, rd, rr);
+  }
+  const double brz = block_sum<VB>(rz, red);
+  const double brr = block_sum<VB>(rr, red);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = brz;
+    part[2 * blockIdx.x + 1] = brr;
+  }
+  if (last_block_arrive(&st->counter[1])) {
+    const double trz = reduce_partials<VB>(part, gridDim.x, 2, 0, red);
+    const double trr = reduce_partials<VB>(part, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      const double rt = sqrt(trr);
+      st->rtrue = rt;
+      htrue[++st->n_updates] = rt;
+      hist[st->iter] = rt;
+      if (rt <= st->tol_norm_b) {
+        st->done = 1;
+        st->converged = 1;
+      } else if (st->iter >= st->max_iter) {
+        st->done = 1;
+      } else {
+        st->rz = trz;  // rz_old keeps the previous iteration's r.z
+        st->beta = trz / st->rz_old;
+        st->rmax = rt;
+      }
+      st->counter[1] = 0;
+    }
+  }
+}
+
+// K7: p = z + beta p after an update; the last block clears the update flags.
+__global__ void __launch_bounds__(VB) k_mx_dir_update(int n, MixedState* st,
+                                                      const float* __restrict__ z,
+                                                      float* __restrict__ p) {
+  if (!st->need_update) return;
+  if (!st->done) {
+    const float beta = (float)st->beta;
+    for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB)
+      p[i] = fmaf(beta, p[i], z[i]);
+  }
+  if (last_block_arrive(&st->counter[2]) && threadIdx.x == 0) {
+    st->need_update = 0;
+    st->skip_update = 1;
+    st->counter[2] = 0;
+  }
+}
+
+}  // namespace
+
+void build_f32_points(F32Points& fp, const PointSet& ps, double sx, double sy, double sz,
+                      cudaStream_t st) {
+  fp.orig.alloc(ps.n_tiles);
+  fp.xi.alloc(ps.n_pad);
+  k_f32_origins<<<(ps.n_tiles + 127) / 128, 128, 0, st>>>(ps.n_tiles, ps.box.p, sx, sy, sz,
+                                                          fp.orig.p);
+  DS_CHECK_LAUNCH();
+  const int nb = (ps.n_pad + VB - 1) / VB;
+  DevBuf<float> bm;
+  bm.alloc(nb);
+  k_f32_xi<<<nb, VB, 0, st>>>(ps.n_pad, ps.x.p, ps.y.p, ps.z.p, sx, sy, sz, fp.orig.p, fp.xi.p,
+                              bm.p);
+  DS_CHECK_LAUNCH();
+  std::vector<float> h(nb);
+  DS_CUDA(cudaMemcpyAsync(h.data(), bm.p, nb * sizeof(float), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  fp.max_a = *std::max_element(h.begin(), h.end());
+}
+
+// Scales of the exact kernel in log2 units: |dX|^2 = arg * log2(e).
+static void exact_scales(const KernelConsts& kc, double& sp, double& sq) {
+  sp = std::sqrt(kc.c_perp * LOG2E);
+  sq = std::sqrt(kc.c_para * LOG2E);
+}
+
+void ensure_op_f32(ds_operator* op, double inner_cut) {
+  if (op->f32 && op->f32->inner_cut == inner_cut) return;
+  require(op->kc.eval == DS_EVAL_EXACT,
+          "the mixed-precision form evaluates the exact kernel (eval = DS_EVAL_EXACT)");
+  cudaStream_t st = op->ctx->stream;
+  std::unique_ptr<OpF32, OpF32Deleter> f(new OpF32());
+  f->inner_cut = inner_cut;
+  double sp, sq;
+  exact_scales(op->kc, sp, sq);
+  build_f32_points(f->pts, op->pix, sp, sp, sq, st);
+  // 2^|xi|^2 must stay well inside FP32 range for the EXPANDED formula.
+  f->formula = f->pts.max_a <= 60.0 ? F32_EXPANDED : F32_DIRECT;
+  KernelConsts kc = op->kc;
+  kc.cull_arg = inner_cut * (1.0 + 1e-9);
+  build_pair_list(f->pairs, op->pix, op->pix, kc, st);
+  const int np = op->pix.n_pad;
+  f->rowf.alloc(np);
+  f->colw.alloc(np);
+  f->ediag.alloc(np);
+  f->pdiag.alloc(np);
+  k_f32_coeffs<<<vgrid(np), VB, 0, st>>>(np, f->formula == F32_EXPANDED, op->kc.var_s,
+                                         f->pts.xi.p, op->wl.p, op->wr.p, op->e.p, op->pdiag.p,
+                                         f->rowf.p, f->colw.p, f->ediag.p, f->pdiag.p);
+  DS_CHECK_LAUNCH();
+  f->p.alloc(np);
+  f->q.alloc(np);
+  f->r.alloc(np);
+  f->z.alloc(np);
+  f->xc.alloc(np);
+  f->state.alloc(1);
+  DS_CUDA(cudaStreamSynchronize(st));
+  op->f32 = std::move(f);
+}
+
+F32Args op_f32_args(ds_operator* op, const float* v, float* out) {
+  OpF32& f = *op->f32;
+  F32Args a{};
+  a.rxi = a.cxi = f.pts.xi.p;
+  a.rorig = a.corig = f.pts.orig.p;
+  a.row_ptr = f.pairs.row_ptr.p;
+  a.cols = f.pairs.cols.p;
+  a.n_row_tiles = op->pix.n_tiles;
+  a.colw = f.colw.p;
+  a.v = v;
+  a.rowf = f.rowf.p;
+  a.ediag = f.ediag.p;
+  a.vrow = v;
+  a.out = out;
+  a.n_tile_pairs = f.pairs.n_pairs;
+  a.prof = &op->ctx->prof;
+  return a;
+}
+
+void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
+               double* hist_out) {
+  cudaStream_t st = op->ctx->stream;
+  ensure_pcg_workspace(op);
+  const double inner_cut = mp.inner_cutoff > 0.0 ? mp.inner_cutoff : 24.0;
+  ensure_op_f32(op, inner_cut);
+  OpF32& f = *op->f32;
+  const int np = op->pix.n_pad;
+  const int max_iter = std::max(mp.max_iter, 0);
+  f.hist.alloc((size_t)max_iter + 2);
+  f.htrue.alloc((size_t)max_iter + 2);
+
+  MixedState h{};
+  h.max_iter = max_iter;
+  h.norm_b = op->norm_b;
+  h.tol_norm_b = mp.tol * op->norm_b;
+  h.delta = mp.reliable_delta > 0.0 ? mp.reliable_delta : 1e-4;
+  h.pad = 1;  // "x0 is zero" flag, cleared by k_is_zero
+  DS_CUDA(cudaMemcpyAsync(f.state.p, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  MixedState* S = f.state.p;
+  int* xzero = &S->pad;
+
+  cudaEvent_t ev0, ev1;
+  DS_CUDA(cudaEventCreate(&ev0));
+  DS_CUDA(cudaEventCreate(&ev1));
+  DS_CUDA(cudaEventRecord(ev0, st));
+
+  const int g = vgrid(np);
+  // r64 = b - A x0 in FP64, skipped when x0 == 0 (then r64 = b).
+  k_is_zero<<<g, VB, 0, st>>>(np, op->x.p, xzero);
+  DS_CHECK_LAUNCH();
+  PairArgs resid = op_pair_args(op, op->x.p, op->r.p);
+  resid.skip_flag = xzero;
+  launch_pair_f64(op->kc, EPI_RESIDUAL, resid, st);
+  k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p, f.xc.p,
+                              f.pdiag.p, op->partial.p, f.hist.p, f.htrue.p);
+  DS_CHECK_LAUNCH();
+
+  F32Args prod = op_f32_args(op, f.p.p, f.q.p);
+  prod.dotv = f.p.p;
+  prod.dot_partial = op->partial2.p;
+  prod.counter = &S->counter[0];
+  prod.num = &S->rz;
+  prod.alpha_out = &S->alpha;
+  prod.den_out = &S->pq;
+  prod.skip_flag = &S->done;
+  PairArgs upd = op_pair_args(op, op->x.p, op->r.p);
+  upd.skip_flag = &S->skip_update;
+
+  constexpr int CHECK = 8;
+  constexpr int NSLOT = 64;
+  cudaEvent_t evs[NSLOT];
+  for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  int issued = 0, waited = 0;
+  for (int it = 1; it <= max_iter; ++it) {
+    launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);                       // K1
+    k_mx_update<<<g, VB, 0, st>>>(np, S, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
+                                  op->partial.p, f.hist.p);                  // K2
+    DS_CHECK_LAUNCH();
+    k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K3
+    DS_CHECK_LAUNCH();
+    k_mx_fold<<<g, VB, 0, st>>>(np, S, op->x.p, f.xc.p);                    // K4
+    DS_CHECK_LAUNCH();
+    launch_pair_f64(op->kc, EPI_RESIDUAL, upd, st);                          // K5
+    k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,
+                                   f.hist.p, f.htrue.p);                     // K6
+    DS_CHECK_LAUNCH();
+    k_mx_dir_update<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                 // K7
+    DS_CHECK_LAUNCH();
+    if (it % CHECK == 0) {
+      const int slot = issued % NSLOT;
+      DS_CUDA(cudaMemcpyAsync(&op->h_flag.p[slot], &S->done, sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
+      DS_CUDA(cudaEventRecord(evs[slot], st));
+      ++issued;
+      if (issued - waited > 2) {
+        const int ws = waited % NSLOT;
+        DS_CUDA(cudaEventSynchronize(evs[ws]));
+        ++waited;
+        if (op->h_flag.p[ws]) break;
+      }
+    }
+  }
+  DS_CUDA(cudaEventRecord(ev1, st));
+  DS_CUDA(cudaMemcpyAsync(&h, S, sizeof(h), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  DS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+  for (auto& e : evs) cudaEventDestroy(e);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+
+  const int n_hist = h.iter + 1;
+  if (hist_out)
+    DS_CUDA(cudaMemcpy(hist_out, f.hist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost));
+  res.norm_b = op->norm_b;
+  res.final_norm = h.rtrue;
+  res.seconds = ms * 1e-3;
+  res.n_outer = h.n_updates;
+  res.n_inner = h.iter;
+  res.num_iters = h.iter;
+  res.success = h.converged;
+  if (mp.verbose) {
+    std::vector<double> ht(h.n_updates + 1);
+    DS_CUDA(cudaMemcpy(ht.data(), f.htrue.p, ht.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+    printf("[PCG mixed] %d FP32 iterations, %d FP64 residual updates, |r| %e (tol |b| %e)\n",
+           h.iter, h.n_updates, h.rtrue, h.tol_norm_b);
+    for (size_t k = 0; k < ht.size(); ++k) printf("    update %zu: |r| = %e\n", k, ht[k]);
+  }
+}
+
+void ensure_map_f32(ds_map* map, ds_operator* op, double cut) {
+  if (map->f32 && map->f32->op_serial == op->serial && map->f32->cut == cut) return;
+  cudaStream_t st = map->ctx->stream;
+  std::unique_ptr<MapF32, MapF32Deleter> f(new MapF32());
+  f->op_serial = op->serial;
+  f->cut = cut;
+  double sp, sq;
+  exact_scales(op->kc, sp, sq);
+  build_f32_points(f->pts, map->pts, sp, sp, sq, st);
+  KernelConsts kc = op->kc;
+  kc.cull_arg = cut * (1.0 + 1e-9);
+  build_pair_list(f->pairs, map->pts, op->pix, kc, st);
+  f->rowf.alloc(map->pts.n_pad);
+  k_fill_f32<<<vgrid(map->pts.n_pad), VB, 0, st>>>(map->pts.n_pad, (float)op->kc.var_s,
+                                                   f->rowf.p);
+  DS_CHECK_LAUNCH();
+  f->xs.alloc(op->pix.n_pad);
+  DS_CUDA(cudaStreamSynchronize(st));
+  map->f32 = std::move(f);
+}
+
+// m = S_mp x with FP32 kernel evaluation and FP64 accumulation across tiles.
+void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
+                         double cut) {
+  require(op->kc.eval == DS_EVAL_EXACT, "the FP32 map product evaluates the exact kernel");
+  ensure_op_f32(op, op->f32 ? op->f32->inner_cut : 24.0);
+  ensure_map_f32(map, op, cut);
+  cudaStream_t st = map->ctx->stream;
+  MapF32& f = *map->f32;
+  op->tmp.alloc(op->pix.n_pad);
+  gather_sorted(op->pix, x_dev, op->tmp.p, st);
+  k_d2f<<<vgrid(op->pix.n_pad), VB, 0, st>>>(op->pix.n_pad, op->tmp.p, f.xs.p);
+  DS_CHECK_LAUNCH();
+  F32Args a{};
+  a.rxi = f.pts.xi.p;
+  a.rorig = f.pts.orig.p;
+  a.cxi = op->f32->pts.xi.p;
+  a.corig = op->f32->pts.orig.p;
+  a.row_ptr = f.pairs.row_ptr.p;
+  a.cols = f.pairs.cols.p;
+  a.n_row_tiles = map->pts.n_tiles;
+  a.v = f.xs.p;
+  a.rowf = f.rowf.p;
+  a.row_perm = map->pts.perm.p;
+  a.out64 = m_dev;
+  a.n_tile_pairs = f.pairs.n_pairs;
+  a.prof = &map->ctx->prof;
+  launch_pair_f32(F32_DIRECT, EPI_MAP, a, st);
+}
+
+}  // namespace ds

@@ -1,0 +1,198 @@
+// FP32 matrix-free pair kernels of the mixed-precision form: the exact
+// kernel var_s exp(-arg) evaluated as var_s 2^(-|dX|^2) on coordinates scaled
+// by sqrt(c log2 e), with MUFU ex2 and packed f32x2 FMAs.
+//
+// Coordinates are stored relative to their tile's origin (the bounding-box
+// centre, rounded to FP32), so FP32 differences are taken between numbers of
+// the size of a tile rather than of the box.  For a (row tile R, column tile
+// C) pair the columns are moved into R's frame once at staging:
+//   zeta_j = xi_j - (o_R - o_C).
+// Two formulations of the exponent:
+//   EXPANDED  t_ij = 2 xi_i . zeta_j - |zeta_j|^2 = |xi_i|^2 - |xi_i - zeta_j|^2,
+//             e_ij = 2^t_ij = 2^(|xi_i|^2) S'_ij, the row factor 2^-|xi_i|^2
+//             applied once at the end.  Per pair: 3 FFMA + 1 ex2 + 1 FFMA,
+//             i.e. 4 FMA-pipe lanes and 1 MUFU: FMA and MUFU (both 32/clk/SM
+//             on GB300) are co-bound at 32 pairs/clk/SM.  Relative error of
+//             S' about |zeta|^2 * 2^-24 (~1e-6): used for the inner solve,
+//             whose FP64 outer residual removes it.
+//   DIRECT    t_ij = -|xi_i - zeta_j|^2: 3 FADD + FMUL + 2 FFMA + ex2 + FFMA,
+//             7 FMA-pipe lanes (18 pairs/clk/SM); relative error ~1e-7.  Used
+//             for the map product and when a tile is too large for EXPANDED
+//             (2^|xi|^2 would leave FP32 range).
+// Each CTA owns a 128-row tile; lane l of warp w holds rows l, l+32, l+64,
+// l+96 (as two f32x2 pairs) and walks columns [32w, 32w+32) of every column
+// tile, so a column's staged data is read once per 4 rows.  Per-tile FP32
+// sums of 32 terms are folded into Kahan-compensated FP32 accumulators; the
+// four warps' partial rows are summed in FP64 at the end.
+#include "ds_device.cuh"
+#include "ds_f32.h"
+
+namespace ds {
+
+namespace {
+
+__device__ __forceinline__ float ex2f(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+template <int FORMULA, int EPI, bool DOT>
+__global__ void __launch_bounds__(TILE) k_pair_f32(F32Args a) {
+  if (a.skip_flag && *a.skip_flag) return;
+  if (a.prof_pairs && blockIdx.x == 0 && threadIdx.x == 0)
+    atomicAdd(a.prof_pairs, (unsigned long long)a.n_tile_pairs * TILE * TILE);
+  __shared__ float4 sc[TILE];
+  __shared__ float su[TILE];
+  __shared__ float sred[4][TILE];
+  __shared__ double red[TILE / 32];
+  const int t = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int base = t * TILE;
+
+  float2 x01, y01, z01, x23, y23, z23;
+  {
+    const float4 r0 = a.rxi[base + lane], r1 = a.rxi[base + lane + 32];
+    const float4 r2 = a.rxi[base + lane + 64], r3 = a.rxi[base + lane + 96];
+    x01 = make_float2(r0.x, r1.x); y01 = make_float2(r0.y, r1.y); z01 = make_float2(r0.z, r1.z);
+    x23 = make_float2(r2.x, r3.x); y23 = make_float2(r2.y, r3.y); z23 = make_float2(r2.z, r3.z);
+  }
+  const float4 ot = a.rorig[t];
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+
+  const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
+  for (int p = p0; p < p1; ++p) {
+    const int ct = a.cols[p];
+    __syncthreads();
+    {
+      const float4 oc = a.corig[ct];
+      const float dx = ot.x - oc.x, dy = ot.y - oc.y, dz = ot.z - oc.z;
+      const int j = ct * TILE + tid;
+      const float4 q = a.cxi[j];
+      const float zx = q.x - dx, zy = q.y - dy, zz = q.z - dz;
+      if (FORMULA == F32_EXPANDED) {
+        const float aj = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+        sc[tid] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -aj);
+      } else {
+        sc[tid] = make_float4(zx, zy, zz, 0.f);
+      }
+      su[tid] = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
+    }
+    __syncthreads();
+    float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
+    const float4* col = sc + warp * 32;
+    const float* cu = su + warp * 32;
+#pragma unroll 8
+    for (int jj = 0; jj < 32; ++jj) {
+      const float4 c4 = col[jj];
+      const float2 u2 = make_float2(cu[jj], cu[jj]);
+      float2 t01, t23;
+      if (FORMULA == F32_EXPANDED) {
+        const float2 cx = make_float2(c4.x, c4.x), cy = make_float2(c4.y, c4.y);
+        const float2 cz = make_float2(c4.z, c4.z), cw = make_float2(c4.w, c4.w);
+        t01 = __ffma2_rn(x01, cx, cw);
+        t23 = __ffma2_rn(x23, cx, cw);
+        t01 = __ffma2_rn(y01, cy, t01);
+        t23 = __ffma2_rn(y23, cy, t23);
+        t01 = __ffma2_rn(z01, cz, t01);
+        t23 = __ffma2_rn(z23, cz, t23);
+      } else {
+        const float2 ncx = make_float2(-c4.x, -c4.x), ncy = make_float2(-c4.y, -c4.y);
+        const float2 ncz = make_float2(-c4.z, -c4.z);
+        const float2 dx01 = __fadd2_rn(x01, ncx), dx23 = __fadd2_rn(x23, ncx);
+        const float2 dy01 = __fadd2_rn(y01, ncy), dy23 = __fadd2_rn(y23, ncy);
+        const float2 dz01 = __fadd2_rn(z01, ncz), dz23 = __fadd2_rn(z23, ncz);
+        const float2 mdx01 = make_float2(-dx01.x, -dx01.y), mdx23 = make_float2(-dx23.x, -dx23.y);
+        t01 = __fmul2_rn(dx01, mdx01);
+        t23 = __fmul2_rn(dx23, mdx23);
+        t01 = __ffma2_rn(dy01, make_float2(-dy01.x, -dy01.y), t01);
+        t23 = __ffma2_rn(dy23, make_float2(-dy23.x, -dy23.y), t23);
+        t01 = __ffma2_rn(dz01, make_float2(-dz01.x, -dz01.y), t01);
+        t23 = __ffma2_rn(dz23, make_float2(-dz23.x, -dz23.y), t23);
+      }
+      const float2 e01 = make_float2(ex2f(t01.x), ex2f(t01.y));
+      const float2 e23 = make_float2(ex2f(t23.x), ex2f(t23.y));
+      acc01 = __ffma2_rn(e01, u2, acc01);
+      acc23 = __ffma2_rn(e23, u2, acc23);
+    }
+    kahan_add(s0, c0, acc01.x);
+    kahan_add(s1, c1, acc01.y);
+    kahan_add(s2, c2, acc23.x);
+    kahan_add(s3, c3, acc23.y);
+  }
+  // Cross-warp reduction of the four column slices, in FP64.
+  sred[warp][lane] = s0 - c0;
+  sred[warp][lane + 32] = s1 - c1;
+  sred[warp][lane + 64] = s2 - c2;
+  sred[warp][lane + 96] = s3 - c3;
+  __syncthreads();
+  const double sum = ((double)sred[0][tid] + (double)sred[1][tid]) +
+                     ((double)sred[2][tid] + (double)sred[3][tid]);
+  const int i = base + tid;
+  if (EPI == EPI_PRODUCT) {
+    // q_i = wl_i var_s 2^-a_i sum_j e_ij wr_j v_j + e_i v_i
+    const float q = fmaf(a.rowf[i], (float)sum, a.ediag[i] * a.vrow[i]);
+    a.out[i] = q;
+    if (DOT) {
+      const double s = block_sum<TILE>((double)a.dotv[i] * (double)q, red);
+      if (tid == 0) a.dot_partial[t] = s;
+      if (last_block_arrive(a.counter)) {
+        const double pq = reduce_partials<TILE>(a.dot_partial, gridDim.x, 1, 0, red);
+        if (tid == 0) {
+          *a.den_out = pq;
+          *a.alpha_out = *a.num / pq;
+          *a.counter = 0;
+        }
+      }
+    }
+  } else {
+    // map: m_i = var_s * row factor * sum, accumulated in FP64
+    const int dst = a.row_perm[i];
+    if (dst >= 0) a.out64[dst] = (double)a.rowf[i] * sum;
+  }
+}
+
+template <int FORMULA>
+void launch_formula(int epi, const F32Args& a, cudaStream_t st) {
+  const dim3 grid(a.n_row_tiles), block(TILE);
+  if (epi == EPI_PRODUCT) {
+    if (a.dot_partial)
+      k_pair_f32<FORMULA, EPI_PRODUCT, true><<<grid, block, 0, st>>>(a);
+    else
+      k_pair_f32<FORMULA, EPI_PRODUCT, false><<<grid, block, 0, st>>>(a);
+  } else if (epi == EPI_MAP) {
+    k_pair_f32<FORMULA, EPI_MAP, false><<<grid, block, 0, st>>>(a);
+  } else {
+    throw Error{DS_ERR_ARG, "bad FP32 pair epilogue"};
+  }
+}
+
+}  // namespace
+
+void launch_pair_f32(int formula, int epi, const F32Args& a0, cudaStream_t st) {
+  if (a0.n_row_tiles <= 0) return;
+  F32Args a = a0;
+  cudaEvent_t ev = nullptr;
+  if (a.prof && a.prof->enabled) {
+    a.prof_pairs = a.prof->d_pairs + 1;
+    a.prof->begin(st, &ev);
+  } else {
+    a.prof_pairs = nullptr;
+  }
+  if (formula == F32_EXPANDED)
+    launch_formula<F32_EXPANDED>(epi, a, st);
+  else
+    launch_formula<F32_DIRECT>(epi, a, st);
+  DS_CHECK_LAUNCH();
+  if (ev) a.prof->end(st, ev, 1);
+}
+
+}  // namespace ds

@@ -17,6 +17,8 @@ namespace {
 template <int EVAL, int EPI, bool DOT>
 __global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) {
   if (a.skip_flag && *a.skip_flag) return;
+  if (a.prof_pairs && blockIdx.x == 0 && threadIdx.x == 0)
+    atomicAdd(a.prof_pairs, (unsigned long long)a.n_tile_pairs * TILE * TILE);
   __shared__ double sx[TILE], sy[TILE], sz[TILE], su[TILE];
   __shared__ double tf[EVAL == DS_EVAL_TABLE ? TABLE_N : 1];
   __shared__ double red[TILE / 32];
@@ -94,13 +96,71 @@ void launch_eval(const KernelConsts& kc, int epi, const PairArgs& a, cudaStream_
 
 }  // namespace
 
-void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a, cudaStream_t st) {
-  if (a.n_row_tiles <= 0) return;
+void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a0, cudaStream_t st) {
+  if (a0.n_row_tiles <= 0) return;
+  PairArgs a = a0;
+  cudaEvent_t ev = nullptr;
+  if (a.prof && a.prof->enabled) {
+    a.prof_pairs = a.prof->d_pairs;
+    a.prof->begin(st, &ev);
+  } else {
+    a.prof_pairs = nullptr;
+  }
   if (kc.eval == DS_EVAL_TABLE)
     launch_eval<DS_EVAL_TABLE>(kc, epi, a, st);
   else
     launch_eval<DS_EVAL_EXACT>(kc, epi, a, st);
   DS_CHECK_LAUNCH();
+  if (ev) a.prof->end(st, ev, 0);
+}
+
+long long& launch_counter() {
+  static long long count = 0;
+  return count;
+}
+
+cudaEvent_t Profiler::get_event() {
+  if (!free_events.empty()) {
+    cudaEvent_t e = free_events.back();
+    free_events.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  DS_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void Profiler::begin(cudaStream_t st, cudaEvent_t* ev) {
+  *ev = get_event();
+  DS_CUDA(cudaEventRecord(*ev, st));
+}
+
+void Profiler::end(cudaStream_t st, cudaEvent_t start, int kind) {
+  cudaEvent_t e = get_event();
+  DS_CUDA(cudaEventRecord(e, st));
+  pending.push_back(Pending{start, e, kind});
+}
+
+void Profiler::collect() {
+  for (auto& pr : pending) {
+    DS_CUDA(cudaEventSynchronize(pr.stop));
+    float t = 0.f;
+    DS_CUDA(cudaEventElapsedTime(&t, pr.start, pr.stop));
+    ms[pr.kind] += t;
+    ++launches[pr.kind];
+    free_events.push_back(pr.start);
+    free_events.push_back(pr.stop);
+  }
+  pending.clear();
+}
+
+Profiler::~Profiler() {
+  for (auto& pr : pending) {
+    cudaEventDestroy(pr.start);
+    cudaEventDestroy(pr.stop);
+  }
+  for (auto e : free_events) cudaEventDestroy(e);
+  if (d_pairs) cudaFree(d_pairs);
 }
 
 }  // namespace ds

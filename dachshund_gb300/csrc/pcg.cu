@@ -166,6 +166,8 @@ PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
   a.vrow = v;
   a.out = out;
   a.table = op->table.p;
+  a.n_tile_pairs = op->pairs.n_pairs;
+  a.prof = &op->ctx->prof;
   return a;
 }
 

@@ -91,6 +91,27 @@ int ds_context_synchronize(ds_context* ctx);
 /* Message of the last failed call on this context ("" when none). */
 const char* ds_context_last_error(ds_context* ctx);
 
+/* Instrumentation (no reference counterpart; the reference only has wall
+ * clocks, lib/timer.h:13-26).  When enabled, every launch of a pair kernel
+ * (the matvec / residual / map kernels) on this context is bracketed by CUDA
+ * events on the context's stream; the profile accumulates their device time,
+ * their count and the tile-evaluated pairs they covered.  Disabling keeps
+ * the totals until the next enable. */
+typedef struct {
+  long long pair_launches;   /* pair-kernel launches timed (FP64 + FP32) */
+  double pair_ms;            /* their summed device time */
+  double pair_evaluated;     /* pairs evaluated (tile pairs x tile^2) */
+  long long kernel_launches; /* every kernel this library launched (process-wide) */
+  long long f64_launches;    /* the FP64 pair kernels alone */
+  double f64_ms;
+  double f64_evaluated;
+  long long f32_launches;    /* the FP32 pair kernels alone */
+  double f32_ms;
+  double f32_evaluated;
+} ds_profile;
+int ds_context_set_profiling(ds_context* ctx, int enable);
+int ds_context_get_profile(ds_context* ctx, ds_profile* out);
+
 /* ---- the operator A over one pixel set --------------------------------- */
 typedef struct ds_operator ds_operator;
 
@@ -168,6 +189,31 @@ int ds_solve_pcg(ds_operator* op, const ds_pcg_params* pp, double* x,
 int ds_solve_pcg_dev(ds_operator* op, const ds_pcg_params* pp, double* x,
                      ds_pcg_result* res, double* residual_norms);
 
+/* ---- mixed-precision form (no reference counterpart) --------------------
+ * Solves the same system as ds_solve_pcg with the exact kernel
+ * (DS_EVAL_EXACT): FP32 Jacobi-PCG on an FP32 matrix-free operator (MUFU
+ * ex2) inside FP64 reliable updates, which recompute the true residual
+ * b - A x with the FP64 operator and stop on |r| <= tol |b| in FP64.  It is
+ * the fast path that stands in for WFVector{SN,W}::solve_pcg
+ * (lib/wf_vector.cc:114-121, 263-274) when the exact kernel is wanted. */
+typedef struct {
+  int max_iter;          /* cap on FP32 iterations */
+  double tol;            /* FP64 stopping test |b - A x| <= tol |b| */
+  double reliable_delta; /* update when the FP32 residual fell by this factor
+                            since the last update; <= 0: 1e-4 */
+  double inner_cutoff;   /* exponent cutoff of the FP32 operator; <= 0: 24 */
+  int verbose;
+} ds_mixed_params;
+
+/* x: initial guess in, solution out (times w in the W form), caller order.
+ * ``residual_norms`` (optional, max_iter + 1 doubles) receives the FP32
+ * recurrence norms, replaced by the FP64 true norm at update iterations.
+ * res->num_iters = FP32 iterations, res->n_outer = FP64 residual updates. */
+int ds_solve_mixed(ds_operator* op, const ds_mixed_params* mp, double* x,
+                   ds_pcg_result* res, double* residual_norms);
+int ds_solve_mixed_dev(ds_operator* op, const ds_mixed_params* mp, double* x,
+                       ds_pcg_result* res, double* residual_norms);
+
 /* ---- map projection ----------------------------------------------------- */
 typedef struct ds_map ds_map;
 
@@ -181,6 +227,15 @@ void ds_map_destroy(ds_map* map);
 int ds_map_product(ds_map* map, ds_operator* op, const double* x, double* m);
 int ds_map_product_dev(ds_map* map, ds_operator* op, const double* x,
                        double* m);
+
+/* smp_product of the mixed-precision form: FP32 evaluation of the exact
+ * kernel (MUFU ex2), FP32 sums per column tile, FP64 accumulation across
+ * tiles; pairs beyond ``cutoff`` (exponent; <= 0: 30) are skipped.  Map
+ * error against the FP64 product is about 1e-7 relative. */
+int ds_map_product_f32(ds_map* map, ds_operator* op, double cutoff,
+                       const double* x, double* m);
+int ds_map_product_f32_dev(ds_map* map, ds_operator* op, double cutoff,
+                           const double* x, double* m);
 
 /* One-shot smp_product with the reference's argument list. */
 int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points,

@@ -65,6 +65,8 @@ def port_lib():
         lib.dso_signal_covar.restype = C.c_double
         for name in ("dso_A_product", "dso_A_residual", "dso_precond"):
             getattr(lib, name).argtypes = [K, C.c_int, C.c_int, _dp, _dp, _dp]
+        lib.dso_A_product_rows.argtypes = [K, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int]
+        lib.dso_smp_product_rows.argtypes = [K, C.c_int, _dp, _dp, _dp, _dp, C.c_int, C.c_int]
         lib.dso_norm_b.argtypes = [C.c_int, C.c_int, _dp]
         lib.dso_norm_b.restype = C.c_double
         lib.dso_solve_pcg.argtypes = [K, C.c_int, C.c_int, _dp, C.c_int, C.c_int,
@@ -171,6 +173,24 @@ def A_product(form, rec, a, var_s, l_perp, l_para, exact=False, impl="port"):
         k = _kernel(var_s, l_perp, l_para, exact)
         port_lib().dso_A_product(C.byref(k), _form(form), n, rec, a, b)
     return b
+
+
+def A_product_rows(form, rec, a, row0, row1, var_s, l_perp, l_para, exact=False):
+    """Rows [row0, row1) of A a (the port), for bounded CPU-baseline samples."""
+    rec, a = _c(rec), _c(a)
+    b = np.empty(row1 - row0)
+    k = _kernel(var_s, l_perp, l_para, exact)
+    port_lib().dso_A_product_rows(C.byref(k), _form(form), rec.shape[0], rec, a, b, row0, row1)
+    return b
+
+
+def smp_product_rows(pix_pts, map_pts, x, row0, row1, var_s, l_perp, l_para, exact=False):
+    pix_pts, map_pts, x = _c(pix_pts), _c(map_pts), _c(x)
+    m = np.empty(row1 - row0)
+    k = _kernel(var_s, l_perp, l_para, exact)
+    port_lib().dso_smp_product_rows(C.byref(k), pix_pts.shape[0], pix_pts, map_pts, x, m,
+                                    row0, row1)
+    return m
 
 
 def A_residual(form, rec, x, var_s, l_perp, l_para, exact=False, impl="port"):

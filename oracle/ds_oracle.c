@@ -52,21 +52,37 @@ static inline double dso_pair_S(const dso_kernel* k, const double* pi,
 /* Row i of A times v.
  * SN: A_ij = S_ij + N_i delta_ij          (lib/wf_vector.cc:16-40)
  * W:  A_ij = w_i S_ij w_j + delta_ij      (lib/wf_vector.cc:157-183) */
+/* The evaluation mode and form are hoisted out of the j loop (the reference
+ * compiles one loop per form with the table kernel inlined). */
+#define DSO_ROW_LOOP(SEXPR, AEXPR)                          \
+  for (int j = 0; j < n; ++j) {                             \
+    const double* pj = rec + 5 * (size_t)j;                 \
+    const double dx = pi[0] - pj[0];                        \
+    const double dy = pi[1] - pj[1];                        \
+    const double dz = pi[2] - pj[2];                        \
+    const double perp2 = dx * dx + dy * dy;                 \
+    const double para2 = dz * dz;                           \
+    const double g = k->c_perp * perp2 + k->c_para * para2; \
+    const double S = SEXPR;                                 \
+    const double A = AEXPR;                                 \
+    sum += A * v[j];                                        \
+  }
+
 static inline double dso_row_dot(const dso_kernel* k, int form, int n,
                                  const double* rec, int i, const double* v) {
   const double* pi = rec + 5 * (size_t)i;
   double sum = 0.0;
-  if (form == 0) {
-    for (int j = 0; j < n; ++j) {
-      const double* pj = rec + 5 * (size_t)j;
-      const double A = dso_pair_S(k, pi, pj) + pi[3] * (i == j);
-      sum += A * v[j];
+  if (k->exact) {
+    if (form == 0) {
+      DSO_ROW_LOOP(k->var_s * exp(-g), S + pi[3] * (i == j))
+    } else {
+      DSO_ROW_LOOP(k->var_s * exp(-g), pi[3] * S * pj[3] + (i == j))
     }
   } else {
-    for (int j = 0; j < n; ++j) {
-      const double* pj = rec + 5 * (size_t)j;
-      const double A = pi[3] * dso_pair_S(k, pi, pj) * pj[3] + (i == j);
-      sum += A * v[j];
+    if (form == 0) {
+      DSO_ROW_LOOP(k->var_s * dso_linterp(k, g), S + pi[3] * (i == j))
+    } else {
+      DSO_ROW_LOOP(k->var_s * dso_linterp(k, g), pi[3] * S * pj[3] + (i == j))
     }
   }
   return sum;
@@ -78,6 +94,27 @@ void dso_A_product(const dso_kernel* k, int form, int n, const double* rec,
   int i;
 #pragma omp parallel for schedule(static)
   for (i = 0; i < n; ++i) b[i] = dso_row_dot(k, form, n, rec, i, a);
+}
+
+void dso_A_product_rows(const dso_kernel* k, int form, int n, const double* rec,
+                        const double* a, double* b, int row0, int row1) {
+  int i;
+#pragma omp parallel for schedule(static)
+  for (i = row0; i < row1; ++i) b[i - row0] = dso_row_dot(k, form, n, rec, i, a);
+}
+
+void dso_smp_product_rows(const dso_kernel* k, int n_pix, const double* pix_pts,
+                          const double* map_pts, const double* x, double* m,
+                          int row0, int row1) {
+  int i;
+#pragma omp parallel for schedule(static)
+  for (i = row0; i < row1; ++i) {
+    const double* mi = map_pts + 3 * (size_t)i;
+    double sum = 0.0;
+    for (int j = 0; j < n_pix; ++j)
+      sum += dso_pair_S(k, mi, pix_pts + 3 * (size_t)j) * x[j];
+    m[i - row0] = sum;
+  }
 }
 
 /* A_residual, lib/wf_vector.cc:76-103 (SN) and :222-251 (W): r = b - A x

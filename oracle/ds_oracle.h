@@ -44,6 +44,13 @@ void dso_A_product(const dso_kernel* k, int form, int n, const double* rec,
                    const double* a, double* b);
 void dso_A_residual(const dso_kernel* k, int form, int n, const double* rec,
                     const double* x, double* r);
+/* Rows [row0, row1) of A_product / smp_product: a bounded sample of the
+ * same loops, for timing the CPU baseline on part of a large workload. */
+void dso_A_product_rows(const dso_kernel* k, int form, int n, const double* rec,
+                        const double* a, double* b, int row0, int row1);
+void dso_smp_product_rows(const dso_kernel* k, int n_pix, const double* pix_pts,
+                          const double* map_pts, const double* x, double* m,
+                          int row0, int row1);
 void dso_precond(const dso_kernel* k, int form, int n, const double* rec,
                  const double* r, double* s);
 double dso_norm_b(int form, int n, const double* rec);
