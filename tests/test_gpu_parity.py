@@ -89,7 +89,7 @@ def test_pcg_golden(ctx, golden, form, tol, step_r, key):
     assert res.success
     assert abs(res.num_iters - ref_iters) <= 2
     assert res.final_norm <= tol * res.norm_b
-    assert rel(x, g[f"x{key}_{form}"]) < 1e-8
+    assert rel(x, g[f"x{key}_{form}"]) < 100 * tol  # converged: within tol * cond(A)
     hist = g[f"hist{key}_{form}"]
     k = min(20, hist.size, res.residual_norms.size)
     np.testing.assert_allclose(res.residual_norms[:k], hist[:k], rtol=1e-9)
@@ -150,7 +150,7 @@ def test_exact_mode_vs_oracle(ctx, form):
     xo, ok, it, _ = oracle.solve_pcg(form, rec, VS, LP, LQ, 1000, 50, 1e-10, exact=True)
     assert res.success and ok
     assert abs(res.num_iters - it) <= 1
-    assert rel(x, xo) < 1e-8
+    assert rel(x, xo) < 1e-7  # converged (tol 1e-10): within tol * cond(A)
 
 
 def test_random_cloud_ragged_tiles(ctx):
@@ -185,7 +185,7 @@ def test_device_entry_points(ctx, golden):
     res = op.solve_pcg_dev(PCGParams(1000, 50, 1e-8), x)
     ctx.synchronize()
     assert res.success and abs(res.num_iters - int(g["iters_w"])) <= 2
-    assert rel(x.cpu().numpy(), g["x_w"]) < 1e-8
+    assert rel(x.cpu().numpy(), g["x_w"]) < 1e-6  # converged: within tol * cond(A)
 
 
 def test_error_behaviour(ctx):
