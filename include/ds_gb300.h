@@ -189,6 +189,32 @@ int ds_solve_pcg(ds_operator* op, const ds_pcg_params* pp, double* x,
 int ds_solve_pcg_dev(ds_operator* op, const ds_pcg_params* pp, double* x,
                      ds_pcg_result* res, double* residual_norms);
 
+/* Jacobi-PCG that allocates no device memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc: a host application
+ * that hands out all device memory from its own pool or arena and keeps the
+ * rest of the GPU for other work, or a solver loop that must not stop the
+ * device (cudaMalloc can synchronise the device and can fail under memory
+ * pressure in the middle of a run).  The caller supplies every buffer:
+ * ``records`` (n NPixel / WPixel records) and ``x`` (initial guess in,
+ * solution out, times w in the W form) are DEVICE pointers in the caller's
+ * order; ``residual_norms`` is an optional HOST buffer of max_iter + 1
+ * doubles (at most the first 8192 norms are recorded).  The work space is
+ * one fixed device array in the library (about 3.3 MB, held on every GPU
+ * that loads the library until the process exits), so n is limited to
+ * 32,768 pixels; larger n returns DS_ERR_ARG with a message.  There is no
+ * spatial tiling (it needs temporary memory): every pixel pair is evaluated,
+ * so this entry point suits small and medium problems.
+ *  - The first call on a device looks up the work space's device address
+ *    (once per device); make that first call before any stream capture.
+ *  - All calls share the one work space and each call re-initialises it:
+ *    calls that overlap on the GPU (other streams or threads) race.
+ *  - ``stream`` is a cudaStream_t (NULL: the legacy default stream); the call
+ *    returns after the solve has finished on it. */
+int ds_solve_pcg_noalloc(int form, int n, const double* records,
+                         const ds_kernel_params* kp, const ds_pcg_params* pp,
+                         double* x, ds_pcg_result* res,
+                         double* residual_norms, void* stream);
+
 /* ---- mixed-precision form (no reference counterpart) --------------------
  * Solves the same system as ds_solve_pcg with the exact kernel
  * (DS_EVAL_EXACT): FP32 Jacobi-PCG on an FP32 matrix-free operator (MUFU
