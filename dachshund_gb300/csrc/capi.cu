@@ -203,6 +203,8 @@ void map_product_dev(ds_map* map, ds_operator* op, const double* x_dev, double* 
   a.cz = op->pix.z.p;
   a.row_ptr = map->pairs.row_ptr.p;
   a.cols = map->pairs.cols.p;
+  a.rsbox = map->pts.sbox.p;
+  a.csbox = op->pix.sbox.p;
   a.n_row_tiles = map->pts.n_tiles;
   a.v = op->tmp.p;
   a.out = m_dev;
@@ -544,7 +546,7 @@ int ds_map_create(ds_context* ctx, int n_map, const double* map_points, ds_map**
     map->ctx = ctx;
     DevBuf<double> pts;
     upload(map_points, (size_t)n_map * 3, pts, st);
-    build_point_set(map->pts, pts.p, n_map, 3, 1.0, 1.0, 1.0, st);
+    build_point_set(map->pts, pts.p, n_map, 3, 1.0, 1.0, 1.0, st, ORDER_MORTON);
   });
   if (rc != DS_OK) return rc;
   *out = map.release();
@@ -619,7 +621,7 @@ int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points, int n
     PointSet pix, mp;
     build_point_set(pix, dpix.p, n_pix, 3, std::sqrt(kc.c_perp), std::sqrt(kc.c_perp),
                     std::sqrt(kc.c_para), st);
-    build_point_set(mp, dmap.p, n_map, 3, 1.0, 1.0, 1.0, st);
+    build_point_set(mp, dmap.p, n_map, 3, 1.0, 1.0, 1.0, st, ORDER_MORTON);
     PairList pl;
     build_pair_list(pl, mp, pix, kc, st);
     xs.alloc(pix.n_pad);
@@ -630,6 +632,8 @@ int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points, int n
     a.cx = pix.x.p; a.cy = pix.y.p; a.cz = pix.z.p;
     a.row_ptr = pl.row_ptr.p;
     a.cols = pl.cols.p;
+    a.rsbox = mp.sbox.p;
+    a.csbox = pix.sbox.p;
     a.n_row_tiles = mp.n_tiles;
     a.v = xs.p;
     a.out = dm.p;
@@ -658,7 +662,7 @@ int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels, int 
     PointSet pix, mp;
     build_point_set(pix, drec.p, n_pix, 5, std::sqrt(kc.c_perp), std::sqrt(kc.c_perp),
                     std::sqrt(kc.c_para), st);
-    build_point_set(mp, dmap.p, n_map, 3, 1.0, 1.0, 1.0, st);
+    build_point_set(mp, dmap.p, n_map, 3, 1.0, 1.0, 1.0, st, ORDER_MORTON);
     PairList pl;
     build_pair_list(pl, mp, pix, kc, st);
     u.alloc(pix.n_pad);
@@ -671,6 +675,8 @@ int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels, int 
     a.cx = pix.x.p; a.cy = pix.y.p; a.cz = pix.z.p;
     a.row_ptr = pl.row_ptr.p;
     a.cols = pl.cols.p;
+    a.rsbox = mp.sbox.p;
+    a.csbox = pix.sbox.p;
     a.n_row_tiles = mp.n_tiles;
     a.v = u.p;
     a.out = dm.p;

@@ -30,6 +30,7 @@ struct OpF32Deleter { void operator()(OpF32* p) const; };
 struct MapF32Deleter { void operator()(MapF32* p) const; };
 
 constexpr int TILE = 128;        // points per tile (rows per CTA in the FP64 kernels)
+constexpr int SUBTILE = 32;      // points per sub-tile (one warp's rows; culled per warp)
 constexpr int TABLE_N = DS_TABLE_N;
 
 struct Error {
@@ -129,13 +130,19 @@ struct PointSet {
   DevBuf<double> x, y, z;  // sorted + padded
   DevBuf<int> perm;        // sorted position -> caller index (-1 on padding)
   DevBuf<double> box;      // 6 per tile: lo x, y, z, hi x, y, z
+  DevBuf<double> sbox;     // 6 per SUBTILE-point sub-tile, same layout
 };
 
 // Builds a PointSet from n records of `stride` doubles (x, y, z first) that
 // are already in device memory.  sx, sy, sz scale the coordinates for the
 // spatial key only (the stored coordinates are unscaled).
+// order: ORDER_MORTON cuts the Morton-sorted sequence into tiles (cheap; good
+// for regular grids); ORDER_KD refines it into a balanced k-d partition with
+// exactly TILE points per tile (compact boxes for scattered pixels).
+enum PointOrder { ORDER_MORTON = 0, ORDER_KD = 1 };
 void build_point_set(PointSet& ps, const double* d_rec, int n, int stride,
-                     double sx, double sy, double sz, cudaStream_t st);
+                     double sx, double sy, double sz, cudaStream_t st,
+                     int order = ORDER_KD);
 
 // Culled tile-pair list (CSR over row tiles).
 struct PairList {
@@ -163,6 +170,7 @@ struct PairArgs {
   const double* cx; const double* cy; const double* cz;
   const int* row_ptr; const int* cols;
   int n_row_tiles;
+  const double* rsbox; const double* csbox;  // sub-tile boxes of rows / columns
   // coefficients (sorted order)
   const double* wl; const double* wr; const double* e; const double* b;
   const double* v;      // the vector being multiplied (column side)

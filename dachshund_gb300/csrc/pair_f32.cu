@@ -44,18 +44,69 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
+// One warp's 32 staged columns against its lane's four rows, as two f32x2 row
+// pairs (01: rows lane and lane+32, 23: rows lane+64 and lane+96).  A pair
+// whose two row sub-tiles are both beyond the cutoff from the column
+// sub-tile is skipped (DO01 / DO23 false).
+template <int FORMULA, bool DO01, bool DO23>
+__device__ __forceinline__ void accumulate32(const float4* __restrict__ col,
+                                             const float* __restrict__ cu, float2 x01,
+                                             float2 y01, float2 z01, float2 x23, float2 y23,
+                                             float2 z23, float2& acc01, float2& acc23) {
+#pragma unroll 8
+  for (int jj = 0; jj < 32; ++jj) {
+    const float4 c4 = col[jj];
+    const float2 u2 = make_float2(cu[jj], cu[jj]);
+    float2 t01, t23;
+    if (FORMULA == F32_EXPANDED) {
+      const float2 cx = make_float2(c4.x, c4.x), cy = make_float2(c4.y, c4.y);
+      const float2 cz = make_float2(c4.z, c4.z), cw = make_float2(c4.w, c4.w);
+      if (DO01) {
+        t01 = __ffma2_rn(x01, cx, cw);
+        t01 = __ffma2_rn(y01, cy, t01);
+        t01 = __ffma2_rn(z01, cz, t01);
+      }
+      if (DO23) {
+        t23 = __ffma2_rn(x23, cx, cw);
+        t23 = __ffma2_rn(y23, cy, t23);
+        t23 = __ffma2_rn(z23, cz, t23);
+      }
+    } else {
+      const float2 ncx = make_float2(-c4.x, -c4.x), ncy = make_float2(-c4.y, -c4.y);
+      const float2 ncz = make_float2(-c4.z, -c4.z);
+      if (DO01) {
+        const float2 dx = __fadd2_rn(x01, ncx), dy = __fadd2_rn(y01, ncy);
+        const float2 dz = __fadd2_rn(z01, ncz);
+        t01 = __fmul2_rn(dx, make_float2(-dx.x, -dx.y));
+        t01 = __ffma2_rn(dy, make_float2(-dy.x, -dy.y), t01);
+        t01 = __ffma2_rn(dz, make_float2(-dz.x, -dz.y), t01);
+      }
+      if (DO23) {
+        const float2 dx = __fadd2_rn(x23, ncx), dy = __fadd2_rn(y23, ncy);
+        const float2 dz = __fadd2_rn(z23, ncz);
+        t23 = __fmul2_rn(dx, make_float2(-dx.x, -dx.y));
+        t23 = __ffma2_rn(dy, make_float2(-dy.x, -dy.y), t23);
+        t23 = __ffma2_rn(dz, make_float2(-dz.x, -dz.y), t23);
+      }
+    }
+    if (DO01) acc01 = __ffma2_rn(make_float2(ex2f(t01.x), ex2f(t01.y)), u2, acc01);
+    if (DO23) acc23 = __ffma2_rn(make_float2(ex2f(t23.x), ex2f(t23.y)), u2, acc23);
+  }
+}
+
 template <int FORMULA, int EPI, bool DOT>
 __global__ void __launch_bounds__(TILE) k_pair_f32(F32Args a) {
   if (a.skip_flag && *a.skip_flag) return;
-  if (a.prof_pairs && blockIdx.x == 0 && threadIdx.x == 0)
-    atomicAdd(a.prof_pairs, (unsigned long long)a.n_tile_pairs * TILE * TILE);
   __shared__ float4 sc[TILE];
   __shared__ float su[TILE];
   __shared__ float sred[4][TILE];
   __shared__ double red[TILE / 32];
+  __shared__ double srb[4][6];   // row sub-tile boxes
+  __shared__ int sflag[4][4];    // [row sub-tile][column sub-tile] interact
   const int t = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int base = t * TILE;
+  if (tid < 24) srb[tid / 6][tid % 6] = a.rsbox[(size_t)t * 24 + tid];
 
   float2 x01, y01, z01, x23, y23, z23;
   {
@@ -67,6 +118,7 @@ __global__ void __launch_bounds__(TILE) k_pair_f32(F32Args a) {
   const float4 ot = a.rorig[t];
   float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
   float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+  unsigned long long evaluated = 0;  // pairs this warp evaluates (profiling)
 
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
   for (int p = p0; p < p1; ++p) {
@@ -85,49 +137,31 @@ __global__ void __launch_bounds__(TILE) k_pair_f32(F32Args a) {
         sc[tid] = make_float4(zx, zy, zz, 0.f);
       }
       su[tid] = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
+      if (tid < 16) {
+        const int rs = tid >> 2, cs = tid & 3;
+        sflag[rs][cs] = boxes_interact(srb[rs], a.csbox + ((size_t)ct * 4 + cs) * 6, a.c_perp,
+                                       a.c_para, a.cull);
+      }
     }
     __syncthreads();
     float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
     const float4* col = sc + warp * 32;
     const float* cu = su + warp * 32;
-#pragma unroll 8
-    for (int jj = 0; jj < 32; ++jj) {
-      const float4 c4 = col[jj];
-      const float2 u2 = make_float2(cu[jj], cu[jj]);
-      float2 t01, t23;
-      if (FORMULA == F32_EXPANDED) {
-        const float2 cx = make_float2(c4.x, c4.x), cy = make_float2(c4.y, c4.y);
-        const float2 cz = make_float2(c4.z, c4.z), cw = make_float2(c4.w, c4.w);
-        t01 = __ffma2_rn(x01, cx, cw);
-        t23 = __ffma2_rn(x23, cx, cw);
-        t01 = __ffma2_rn(y01, cy, t01);
-        t23 = __ffma2_rn(y23, cy, t23);
-        t01 = __ffma2_rn(z01, cz, t01);
-        t23 = __ffma2_rn(z23, cz, t23);
-      } else {
-        const float2 ncx = make_float2(-c4.x, -c4.x), ncy = make_float2(-c4.y, -c4.y);
-        const float2 ncz = make_float2(-c4.z, -c4.z);
-        const float2 dx01 = __fadd2_rn(x01, ncx), dx23 = __fadd2_rn(x23, ncx);
-        const float2 dy01 = __fadd2_rn(y01, ncy), dy23 = __fadd2_rn(y23, ncy);
-        const float2 dz01 = __fadd2_rn(z01, ncz), dz23 = __fadd2_rn(z23, ncz);
-        const float2 mdx01 = make_float2(-dx01.x, -dx01.y), mdx23 = make_float2(-dx23.x, -dx23.y);
-        t01 = __fmul2_rn(dx01, mdx01);
-        t23 = __fmul2_rn(dx23, mdx23);
-        t01 = __ffma2_rn(dy01, make_float2(-dy01.x, -dy01.y), t01);
-        t23 = __ffma2_rn(dy23, make_float2(-dy23.x, -dy23.y), t23);
-        t01 = __ffma2_rn(dz01, make_float2(-dz01.x, -dz01.y), t01);
-        t23 = __ffma2_rn(dz23, make_float2(-dz23.x, -dz23.y), t23);
-      }
-      const float2 e01 = make_float2(ex2f(t01.x), ex2f(t01.y));
-      const float2 e23 = make_float2(ex2f(t23.x), ex2f(t23.y));
-      acc01 = __ffma2_rn(e01, u2, acc01);
-      acc23 = __ffma2_rn(e23, u2, acc23);
-    }
+    const bool do01 = sflag[0][warp] | sflag[1][warp];
+    const bool do23 = sflag[2][warp] | sflag[3][warp];
+    evaluated += (do01 ? 2 * SUBTILE * 32 : 0) + (do23 ? 2 * SUBTILE * 32 : 0);
+    if (do01 && do23)
+      accumulate32<FORMULA, true, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
+    else if (do01)
+      accumulate32<FORMULA, true, false>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
+    else if (do23)
+      accumulate32<FORMULA, false, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
     kahan_add(s0, c0, acc01.x);
     kahan_add(s1, c1, acc01.y);
     kahan_add(s2, c2, acc23.x);
     kahan_add(s3, c3, acc23.y);
   }
+  if (a.prof_pairs && lane == 0) atomicAdd(a.prof_pairs, evaluated);
   // Cross-warp reduction of the four column slices, in FP64.
   sred[warp][lane] = s0 - c0;
   sred[warp][lane + 32] = s1 - c1;

@@ -14,40 +14,91 @@ namespace ds {
 
 namespace {
 
+// Table kernel without var_s (folded into the column weights): the argument
+// and the interpolation weights are bit-identical to the reference's
+// (lib/signal_covar.h:53-65); the truncating index comes from a round-down
+// add of 1.5 * 2^52 instead of a double->int conversion (slower than an FP64
+// FMA on GB300): for 0 <= xx < 2^51, t = xx + 1.5*2^52 rounded down holds
+// floor(xx) in its low mantissa bits and t - 1.5*2^52 == floor(xx) exactly.
+__device__ __forceinline__ double gp_table_fast(double dx, double dy, double dz,
+                                                const KernelConsts& k, const double* tf) {
+  const double perp2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  const double para2 = __dmul_rn(dz, dz);
+  const double g = __dadd_rn(__dmul_rn(k.c_perp, perp2), __dmul_rn(k.c_para, para2));
+  const double xx = __dmul_rn(g, k.dx_inv);
+  const double M = 6755399441055744.0;
+  const double t = __dadd_rd(xx, M);
+  const double fl = t - M;
+  const int ix = min(max(__double2loint(t), 0), TABLE_N - 2);
+  const double lo = (fl + 1.0) - xx;
+  const double hi = xx - fl;
+  const double gp = fma(tf[ix], lo, tf[ix + 1] * hi);
+  return xx < (double)(TABLE_N - 1) ? gp : 0.0;
+}
+
+// Exact kernel without var_s, zero at and beyond the cutoff.
+__device__ __forceinline__ double g_exact_fast(double dx, double dy, double dz,
+                                               const KernelConsts& k, const double* tab) {
+  const double arg = fma(k.c_perp, fma(dx, dx, dy * dy), k.c_para * (dz * dz));
+  double g = 0.0;
+  if (arg < k.exact_cut) g = exp_neg_f64(arg, tab);
+  return g;
+}
+
+// Each warp's 32 rows form a k-d sub-tile with its own box; a staged column
+// tile is four 32-column sub-tiles, and a warp skips every column sub-tile
+// whose box is beyond the cutoff from its own (a warp-uniform branch).
 template <int EVAL, int EPI, bool DOT>
 __global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) {
   if (a.skip_flag && *a.skip_flag) return;
-  if (a.prof_pairs && blockIdx.x == 0 && threadIdx.x == 0)
-    atomicAdd(a.prof_pairs, (unsigned long long)a.n_tile_pairs * TILE * TILE);
   __shared__ double sx[TILE], sy[TILE], sz[TILE], su[TILE];
-  __shared__ double tf[EVAL == DS_EVAL_TABLE ? TABLE_N : 1];
+  __shared__ double tf[EVAL == DS_EVAL_TABLE ? TABLE_N : 32];
+  __shared__ double scb[TILE / SUBTILE][6];
   __shared__ double red[TILE / 32];
   const int t = blockIdx.x;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const int i = t * TILE + tid;
-  if (EVAL == DS_EVAL_TABLE)
+  if (EVAL == DS_EVAL_TABLE) {
     for (int k = tid; k < TABLE_N; k += TILE) tf[k] = a.table[k];
+  } else if (tid < 32) {
+    tf[tid] = exp2(-(double)tid / 32.0);
+  }
+  double rb[6];
+  for (int c = 0; c < 6; ++c) rb[c] = a.rsbox[(size_t)(t * (TILE / SUBTILE) + warp) * 6 + c];
+  // var_s, folded into the column weights (squared for the S^2 sum)
+  const double wscale = EPI == EPI_NOISE ? kc.var_s * kc.var_s : kc.var_s;
   const double xi = a.rx[i], yi = a.ry[i], zi = a.rz[i];
   double acc = 0.0;
+  unsigned long long evaluated = 0;  // pairs this warp evaluates (profiling)
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
   for (int p = p0; p < p1; ++p) {
-    const int j = a.cols[p] * TILE + tid;
+    const int ct = a.cols[p];
+    const int j = ct * TILE + tid;
     __syncthreads();
     sx[tid] = a.cx[j];
     sy[tid] = a.cy[j];
     sz[tid] = a.cz[j];
     if (EPI == EPI_PRODUCT || EPI == EPI_RESIDUAL)
-      su[tid] = a.wr[j] * a.v[j];
+      su[tid] = wscale * (a.wr[j] * a.v[j]);
     else
-      su[tid] = a.v[j];
+      su[tid] = wscale * a.v[j];
+    if (tid < (TILE / SUBTILE) * 6)
+      scb[tid / 6][tid % 6] = a.csbox[(size_t)ct * (TILE / SUBTILE) * 6 + tid];
     __syncthreads();
+    for (int cs = 0; cs < TILE / SUBTILE; ++cs) {
+      if (!boxes_interact(rb, scb[cs], kc.c_perp, kc.c_para, kc.cull_arg)) continue;
+      evaluated += SUBTILE * SUBTILE;
 #pragma unroll 4
-    for (int jj = 0; jj < TILE; ++jj) {
-      double S = s_eval_f64<EVAL>(xi - sx[jj], yi - sy[jj], zi - sz[jj], kc, tf);
-      if (EPI == EPI_NOISE) S = S * S;
-      acc = fma(S, su[jj], acc);
+      for (int jj = cs * SUBTILE; jj < (cs + 1) * SUBTILE; ++jj) {
+        const double dx = xi - sx[jj], dy = yi - sy[jj], dz = zi - sz[jj];
+        double g = EVAL == DS_EVAL_TABLE ? gp_table_fast(dx, dy, dz, kc, tf)
+                                         : g_exact_fast(dx, dy, dz, kc, tf);
+        if (EPI == EPI_NOISE) g = g * g;
+        acc = fma(g, su[jj], acc);
+      }
     }
   }
+  if (a.prof_pairs && (tid & 31) == 0) atomicAdd(a.prof_pairs, evaluated);
   if (EPI == EPI_PRODUCT || EPI == EPI_RESIDUAL) {
     const double q = a.wl[i] * acc + a.e[i] * a.v[i];
     const double o = (EPI == EPI_RESIDUAL) ? a.b[i] - q : q;

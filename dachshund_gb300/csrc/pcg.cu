@@ -157,6 +157,7 @@ PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
   a.rz = a.cz = op->pix.z.p;
   a.row_ptr = op->pairs.row_ptr.p;
   a.cols = op->pairs.cols.p;
+  a.rsbox = a.csbox = op->pix.sbox.p;
   a.n_row_tiles = op->pix.n_tiles;
   a.wl = op->wl.p;
   a.wr = op->wr.p;

@@ -117,10 +117,11 @@ __global__ void k_gather_points(const double* __restrict__ rec, int n, int n_pad
   perm[i] = i < n ? src : -1;
 }
 
+// Boxes of consecutive groups of blockDim.x (TILE or SUBTILE) sorted points.
 __global__ void k_tile_boxes(const double* __restrict__ x, const double* __restrict__ y,
                              const double* __restrict__ z, double* __restrict__ box) {
   const int t = blockIdx.x;
-  const int i = t * TILE + threadIdx.x;
+  const int i = t * blockDim.x + threadIdx.x;
   __shared__ double sm[6][TILE];
   sm[0][threadIdx.x] = x[i];
   sm[1][threadIdx.x] = y[i];
@@ -129,7 +130,7 @@ __global__ void k_tile_boxes(const double* __restrict__ x, const double* __restr
   sm[4][threadIdx.x] = y[i];
   sm[5][threadIdx.x] = z[i];
   __syncthreads();
-  for (int s = TILE / 2; s > 0; s >>= 1) {
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
       for (int c = 0; c < 3; ++c) {
         sm[c][threadIdx.x] = fmin(sm[c][threadIdx.x], sm[c][threadIdx.x + s]);
@@ -139,6 +140,71 @@ __global__ void k_tile_boxes(const double* __restrict__ x, const double* __restr
     __syncthreads();
   }
   if (threadIdx.x < 6) box[t * 6 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+// ---- k-d partition -----------------------------------------------------
+
+// Bounding boxes (scaled units) of every SUBTILE-point unit of the current
+// order idx (one CTA of SUBTILE threads per unit).
+__global__ void k_unit_boxes_idx(const double* __restrict__ rec, int n, int stride,
+                                 const int* __restrict__ idx, double sx, double sy, double sz,
+                                 double* __restrict__ box) {
+  const int t = blockIdx.x;
+  const int i = t * SUBTILE + threadIdx.x;
+  __shared__ double sm[6][SUBTILE];
+  double c[3];
+  if (i < n) {
+    const double* p = rec + (size_t)idx[i] * stride;
+    c[0] = p[0] * sx;
+    c[1] = p[1] * sy;
+    c[2] = p[2] * sz;
+    for (int k = 0; k < 3; ++k) {
+      sm[k][threadIdx.x] = c[k];
+      sm[3 + k][threadIdx.x] = c[k];
+    }
+  } else {
+    for (int k = 0; k < 3; ++k) {
+      sm[k][threadIdx.x] = INFINITY;
+      sm[3 + k][threadIdx.x] = -INFINITY;
+    }
+  }
+  __syncthreads();
+  for (int s = SUBTILE / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int k = 0; k < 3; ++k) {
+        sm[k][threadIdx.x] = fmin(sm[k][threadIdx.x], sm[k][threadIdx.x + s]);
+        sm[3 + k][threadIdx.x] = fmax(sm[3 + k][threadIdx.x], sm[3 + k][threadIdx.x + s]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) box[t * 6 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+// key = node << 32 | order-preserving bits of the coordinate along the
+// node's split axis (0 for nodes that are already leaves).
+__global__ void k_kd_keys(const double* __restrict__ rec, int n, int stride,
+                          const int* __restrict__ idx, const int* __restrict__ node_of_unit,
+                          const int* __restrict__ node_axis, double sx, double sy, double sz,
+                          unsigned long long* __restrict__ keys) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int node = node_of_unit[i / SUBTILE];
+  const int axis = node_axis[node];
+  unsigned int u = 0;
+  if (axis >= 0) {
+    const double* p = rec + (size_t)idx[i] * stride;
+    const double s = axis == 0 ? sx : (axis == 1 ? sy : sz);
+    const float f = (float)(p[axis] * s);
+    u = __float_as_uint(f);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  }
+  keys[i] = ((unsigned long long)node << 32) | u;
+}
+
+__global__ void k_iota(int n, int* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i;
 }
 
 __device__ __forceinline__ bool tiles_interact(const double* __restrict__ bi,
@@ -202,8 +268,94 @@ __global__ void k_pair_fill(const double* __restrict__ rbox, const double* __res
 
 }  // namespace
 
+// Balanced k-d partition.  Nodes cover whole SUBTILE-point units [u0, u1);
+// a node larger than a tile splits at a tile boundary near its middle, a node
+// within a tile splits at a unit boundary, so every TILE-point tile is a k-d
+// node and its four SUBTILE-point quarters are k-d nodes too (compact boxes
+// for each warp's rows).  Each level is one stable radix sort on (node,
+// coordinate along the node's longest scaled axis), which keeps every node's
+// points contiguous.  idx (sorted position -> record) is updated in place.
+void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, double sx,
+                  double sy, double sz, DevBuf<int>& idx, cudaStream_t st) {
+  (void)ps;
+  constexpr int UPT = TILE / SUBTILE;  // units per tile
+  const int nu = (n + SUBTILE - 1) / SUBTILE;
+  struct Node { int u0, u1; };
+  std::vector<Node> nodes{{0, nu}};
+  std::vector<int> node_of_unit(nu), node_axis;
+  std::vector<double> hbox((size_t)nu * 6);
+  DevBuf<double> box;
+  box.alloc((size_t)nu * 6);
+  DevBuf<int> d_not, d_axis, idx2;
+  d_not.alloc(nu);
+  idx2.alloc(n);
+  DevBuf<unsigned long long> keys, keys2;
+  keys.alloc(n);
+  keys2.alloc(n);
+  DevBuf<unsigned char> tmp;
+  for (int level = 0; level < 64; ++level) {
+    bool any = false;
+    for (auto& nd : nodes) any |= (nd.u1 - nd.u0) >= 2;
+    if (!any) break;
+    k_unit_boxes_idx<<<nu, SUBTILE, 0, st>>>(d_rec, n, stride, idx.p, sx, sy, sz, box.p);
+    DS_CHECK_LAUNCH();
+    DS_CUDA(cudaMemcpyAsync(hbox.data(), box.p, hbox.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    node_axis.assign(nodes.size(), -1);
+    for (size_t k = 0; k < nodes.size(); ++k) {
+      const Node& nd = nodes[k];
+      for (int u = nd.u0; u < nd.u1; ++u) node_of_unit[u] = (int)k;
+      if (nd.u1 - nd.u0 < 2) continue;
+      double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int u = nd.u0; u < nd.u1; ++u)
+        for (int c = 0; c < 3; ++c) {
+          lo[c] = std::min(lo[c], hbox[(size_t)u * 6 + c]);
+          hi[c] = std::max(hi[c], hbox[(size_t)u * 6 + 3 + c]);
+        }
+      int ax = 0;
+      for (int c = 1; c < 3; ++c)
+        if (hi[c] - lo[c] > hi[ax] - lo[ax]) ax = c;
+      node_axis[k] = ax;
+    }
+    d_axis.alloc(nodes.size());
+    DS_CUDA(cudaMemcpyAsync(d_not.p, node_of_unit.data(), nu * sizeof(int),
+                            cudaMemcpyHostToDevice, st));
+    DS_CUDA(cudaMemcpyAsync(d_axis.p, node_axis.data(), nodes.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, st));
+    k_kd_keys<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, idx.p, d_not.p, d_axis.p, sx,
+                                                  sy, sz, keys.p);
+    DS_CHECK_LAUNCH();
+    int node_bits = 1;
+    while ((1ull << node_bits) < nodes.size()) ++node_bits;
+    size_t tmp_bytes = 0;
+    DS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
+                                            0, 32 + node_bits, st));
+    if (tmp.n < tmp_bytes) tmp.alloc(tmp_bytes);
+    DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
+                                            0, 32 + node_bits, st));
+    std::swap(idx.p, idx2.p);
+    std::vector<Node> next;
+    next.reserve(nodes.size() * 2);
+    for (auto& nd : nodes) {
+      const int len = nd.u1 - nd.u0;
+      if (len < 2) {
+        next.push_back(nd);
+      } else {
+        const int ntile = (len + UPT - 1) / UPT;
+        const int um = ntile >= 2 ? nd.u0 + UPT * (ntile / 2) : nd.u0 + len / 2;
+        next.push_back({nd.u0, um});
+        next.push_back({um, nd.u1});
+      }
+    }
+    nodes.swap(next);
+    // The host vectors and scratch are reused next level: wait for this one.
+    DS_CUDA(cudaStreamSynchronize(st));
+  }
+}
+
 void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, double sx,
-                     double sy, double sz, cudaStream_t st) {
+                     double sy, double sz, cudaStream_t st, int order) {
   require(n > 0, "point count must be > 0");
   ps.n = n;
   ps.n_tiles = (n + TILE - 1) / TILE;
@@ -248,6 +400,7 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
   tmp.alloc(std::max<size_t>(tmp_bytes, 1));
   DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n, 0,
                                           30, st));
+  if (order == ORDER_KD && ps.n_tiles > 1) kd_partition(ps, d_rec, n, stride, sx, sy, sz, idx2, st);
 
   ps.x.alloc(ps.n_pad);
   ps.y.alloc(ps.n_pad);
@@ -258,6 +411,9 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
                                                               ps.x.p, ps.y.p, ps.z.p, ps.perm.p);
   DS_CHECK_LAUNCH();
   k_tile_boxes<<<ps.n_tiles, TILE, 0, st>>>(ps.x.p, ps.y.p, ps.z.p, ps.box.p);
+  DS_CHECK_LAUNCH();
+  ps.sbox.alloc((size_t)(ps.n_pad / SUBTILE) * 6);
+  k_tile_boxes<<<ps.n_pad / SUBTILE, SUBTILE, 0, st>>>(ps.x.p, ps.y.p, ps.z.p, ps.sbox.p);
   DS_CHECK_LAUNCH();
   // The temporaries are freed on return; make sure the stream is done with them.
   DS_CUDA(cudaStreamSynchronize(st));
