@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     WFVectorSN,
     WFVectorW,
     init_uniform_map_coords,
+    map_covar_diag,
     npixel_to_pixel,
     pixel_to_npixel,
     pixel_to_wpixel,
@@ -22,6 +23,7 @@ from .api import (  # noqa: F401
     sigma_m_noise_dom,
     signal_covar,
     smp_product,
+    solve_cf,
     table_init,
     wpixel_to_pixel,
 )

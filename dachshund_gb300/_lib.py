@@ -125,6 +125,10 @@ SIGNATURES = {
     "ds_preconditioner_solve": (_i, [_vp, _dp, _dp]),
     "ds_norm_b": (_i, [_vp, _dp]),
     "ds_A_entries": (_i, [_vp, _i, _i, _ip, _ip, _dp]),
+    "ds_operator_set_dense": (_i, [_vp, _i]),
+    "ds_solve_cf": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), _dp]),
+    "ds_map_covar_diag": (_i, [_vp, _i, _dp, _i, _dp, C.POINTER(KernelParamsC),
+                               C.POINTER(PcgParamsC), _dp, _ip, _ip]),
     "ds_solve_pcg": (_i, [_vp, C.POINTER(PcgParamsC), _dp, C.POINTER(PcgResultC), _dp]),
     "ds_solve_pcg_dev": (_i, [_vp, C.POINTER(PcgParamsC), _vp, C.POINTER(PcgResultC), _dp]),
     "ds_solve_pcg_noalloc": (_i, [_i, _i, _vp, C.POINTER(KernelParamsC), C.POINTER(PcgParamsC),

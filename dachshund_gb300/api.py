@@ -214,6 +214,11 @@ class _WFVector:
         except Exception:
             pass
 
+    def set_dense(self, enable: bool = True):
+        """Build the dense operator in HBM (or free it) for the following calls."""
+        self.ctx.check(self._lib.ds_operator_set_dense(self.handle, int(bool(enable))),
+                       "ds_operator_set_dense")
+
     def info(self) -> dict:
         inf = _lib.OperatorInfoC()
         self.ctx.check(self._lib.ds_operator_get_info(self.handle, C.byref(inf)), "info")
@@ -382,6 +387,35 @@ def smp_product(ctx: Context, pixel_coords, map_coords, s_params: SignalCovarPar
     ctx.check(ctx._lib.ds_smp_product(ctx.handle, pix.shape[0], _ptr(pix), mp.shape[0], _ptr(mp),
                                       C.byref(kp), _ptr(x), _ptr(m)), "ds_smp_product")
     return m
+
+
+def solve_cf(ctx: Context, form: str, records, s_params: SignalCovarParams):
+    """WFVector{SN,W}::solve_cf: dense FP64 Cholesky solve on the GPU."""
+    rec = _f64(records)
+    x = np.empty(rec.shape[0])
+    kp = s_params.as_c()
+    ctx.check(ctx._lib.ds_solve_cf(ctx.handle, FORMS[form], rec.shape[0], _ptr(rec), C.byref(kp),
+                                   _ptr(x)), "ds_solve_cf")
+    return x
+
+
+def map_covar_diag(ctx: Context, npixels, map_coords, s_params: SignalCovarParams,
+                   pcg_params: PCGParams):
+    """MapCovarDiag::solve_pcg; returns (sigma_m, iters, success)."""
+    rec = _f64(npixels)
+    mp = _f64(map_coords)
+    m = mp.shape[0]
+    out = np.zeros(m)
+    iters = np.zeros(m, np.int32)
+    ok = np.zeros(m, np.int32)
+    kp = s_params.as_c()
+    pp = _lib.PcgParamsC(pcg_params.max_iter, pcg_params.step_r, pcg_params.tol, 0)
+    ctx.check(ctx._lib.ds_map_covar_diag(ctx.handle, rec.shape[0], _ptr(rec), m, _ptr(mp),
+                                         C.byref(kp), C.byref(pp), _ptr(out),
+                                         iters.ctypes.data_as(C.POINTER(C.c_int)),
+                                         ok.ctypes.data_as(C.POINTER(C.c_int))),
+              "ds_map_covar_diag")
+    return out, iters, ok.astype(bool)
 
 
 def sigma_m_noise_dom(ctx: Context, npixels, map_coords, s_params: SignalCovarParams):

@@ -203,8 +203,7 @@ void map_product_dev(ds_map* map, ds_operator* op, const double* x_dev, double* 
   a.cz = op->pix.z.p;
   a.row_ptr = map->pairs.row_ptr.p;
   a.cols = map->pairs.cols.p;
-  a.rsbox = map->pts.sbox.p;
-  a.csbox = op->pix.sbox.p;
+  a.mask = map->pairs.mask.p;
   a.n_row_tiles = map->pts.n_tiles;
   a.v = op->tmp.p;
   a.out = m_dev;
@@ -632,8 +631,7 @@ int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points, int n
     a.cx = pix.x.p; a.cy = pix.y.p; a.cz = pix.z.p;
     a.row_ptr = pl.row_ptr.p;
     a.cols = pl.cols.p;
-    a.rsbox = mp.sbox.p;
-    a.csbox = pix.sbox.p;
+    a.mask = pl.mask.p;
     a.n_row_tiles = mp.n_tiles;
     a.v = xs.p;
     a.out = dm.p;
@@ -675,8 +673,7 @@ int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels, int 
     a.cx = pix.x.p; a.cy = pix.y.p; a.cz = pix.z.p;
     a.row_ptr = pl.row_ptr.p;
     a.cols = pl.cols.p;
-    a.rsbox = mp.sbox.p;
-    a.csbox = pix.sbox.p;
+    a.mask = pl.mask.p;
     a.n_row_tiles = mp.n_tiles;
     a.v = u.p;
     a.out = dm.p;
@@ -688,6 +685,59 @@ int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels, int 
     DS_CUDA(cudaMemcpyAsync(sigma_m, dm.p, n_map * sizeof(double), cudaMemcpyDeviceToHost, st));
     DS_CUDA(cudaStreamSynchronize(st));
   });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int ds_operator_set_dense(ds_operator* op, int enable) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    if (enable) {
+      if (!op->dense.p) op_build_dense(op);
+      op->use_dense = true;
+    } else {
+      op->use_dense = false;
+      op->dense.release();
+    }
+  });
+}
+
+int ds_solve_cf(ds_context* ctx, int form, int n, const double* records,
+                const ds_kernel_params* kp, double* x) {
+  if (!ctx) return DS_ERR_ARG;
+  return guarded(ctx, [&] {
+    require(form == DS_FORM_SN || form == DS_FORM_W, "form must be DS_FORM_SN or DS_FORM_W");
+    require(n > 0 && records && x, "bad arguments");
+    const ds_kernel_params k = checked_kp(kp);
+    const KernelConsts kc = make_consts(k);
+    cudaStream_t st = ctx->stream;
+    DevBuf<double> table, rec, dx;
+    load_table(table, k, st);
+    upload(records, (size_t)n * 5, rec, st);
+    dx.alloc(n);
+    solve_cf_dev(ctx, form, n, rec.p, kc, table.p, dx.p);
+    DS_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int ds_map_covar_diag(ds_context* ctx, int n_pix, const double* npixels, int n_map,
+                      const double* map_points, const ds_kernel_params* kp,
+                      const ds_pcg_params* pp, double* sigma_m, int* iters, int* success) {
+  if (!ctx || !pp) return DS_ERR_ARG;
+  ds_operator* op = nullptr;
+  int rc = ds_operator_create(ctx, DS_FORM_SN, n_pix, npixels, kp, &op);
+  if (rc != DS_OK) return rc;
+  rc = guarded(ctx, [&] {
+    require(n_map >= 0 && (n_map == 0 || (map_points && sigma_m && iters && success)),
+            "bad arguments");
+    require(pp->step_r > 0, "step_r must be > 0");
+    map_covar_diag_run(op, n_map, map_points, *pp, sigma_m, iters, success);
+  });
+  ds_operator_destroy(op);
+  return rc;
 }
 
 }  // extern "C"

@@ -26,8 +26,7 @@ struct F32Args {
   const float4* cxi; const float4* corig;
   const int* row_ptr; const int* cols;
   int n_row_tiles;
-  const double* rsbox; const double* csbox;  // sub-tile boxes (raw coordinates)
-  double c_perp, c_para, cull;               // sub-tile culling test
+  const unsigned short* mask;  // sub-tile interaction mask per tile pair
   const float* colw;   // column weights (W: w_j, SN: 1)
   const float* v;      // column vector
   // EPI_PRODUCT

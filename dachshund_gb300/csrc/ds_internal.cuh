@@ -150,6 +150,9 @@ struct PairList {
   long long n_pairs = 0;
   DevBuf<int> row_ptr;  // n_rows + 1
   DevBuf<int> cols;     // n_pairs
+  // per pair: bit (4 k + w) set when row sub-tile k interacts with column
+  // sub-tile w (the same box test at sub-tile granularity)
+  DevBuf<unsigned short> mask;
 };
 
 void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
@@ -170,7 +173,7 @@ struct PairArgs {
   const double* cx; const double* cy; const double* cz;
   const int* row_ptr; const int* cols;
   int n_row_tiles;
-  const double* rsbox; const double* csbox;  // sub-tile boxes of rows / columns
+  const unsigned short* mask;  // sub-tile interaction mask per tile pair
   // coefficients (sorted order)
   const double* wl; const double* wr; const double* e; const double* b;
   const double* v;      // the vector being multiplied (column side)
@@ -266,6 +269,8 @@ struct ds_operator {
   ds::HostBuf<int> h_flag;
   unsigned long long serial = 0;   // identity for caches keyed on operators
   std::unique_ptr<ds::OpF32, ds::OpF32Deleter> f32;  // mixed-precision data (lazy)
+  ds::DevBuf<double> dense;  // dense A (n_pad x n_pad, sorted order) when enabled
+  bool use_dense = false;
 };
 
 struct ds_map {

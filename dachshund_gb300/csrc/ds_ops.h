@@ -15,6 +15,17 @@ void op_apply_sorted(ds_operator* op, int epi, const double* v, double* out, cud
 void ensure_pcg_workspace(ds_operator* op);
 void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, double* hist_out);
 
+// Dense paths (dense.cu).
+void op_build_dense(ds_operator* op);
+void dense_apply(ds_operator* op, bool residual, const double* v, double* out,
+                 const double* dotv, double* part, PcgState* pcg, unsigned int* counter,
+                 const int* skip, cudaStream_t st);
+int dense_partials(int n_pad);
+void solve_cf_dev(ds_context* ctx, int form, int n, const double* d_rec, const KernelConsts& kc,
+                  const double* d_table, double* d_x);
+void map_covar_diag_run(ds_operator* op, int n_map, const double* map_pts,
+                        const ds_pcg_params& pp, double* sigma_m, int* iters, int* success);
+
 // Mixed-precision form (mixed.cu).
 void ensure_op_f32(ds_operator* op, double inner_cut);
 void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,

@@ -351,10 +351,7 @@ F32Args op_f32_args(ds_operator* op, const float* v, float* out) {
   a.rorig = a.corig = f.pts.orig.p;
   a.row_ptr = f.pairs.row_ptr.p;
   a.cols = f.pairs.cols.p;
-  a.rsbox = a.csbox = op->pix.sbox.p;
-  a.c_perp = op->kc.c_perp;
-  a.c_para = op->kc.c_para;
-  a.cull = f.inner_cut * (1.0 + 1e-9);
+  a.mask = f.pairs.mask.p;
   a.n_row_tiles = op->pix.n_tiles;
   a.colw = f.colw.p;
   a.v = v;
@@ -519,11 +516,7 @@ void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, doub
   a.corig = op->f32->pts.orig.p;
   a.row_ptr = f.pairs.row_ptr.p;
   a.cols = f.pairs.cols.p;
-  a.rsbox = map->pts.sbox.p;
-  a.csbox = op->pix.sbox.p;
-  a.c_perp = op->kc.c_perp;
-  a.c_para = op->kc.c_para;
-  a.cull = cut * (1.0 + 1e-9);
+  a.mask = f.pairs.mask.p;
   a.n_row_tiles = map->pts.n_tiles;
   a.v = f.xs.p;
   a.rowf = f.rowf.p;

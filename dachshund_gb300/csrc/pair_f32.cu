@@ -95,18 +95,15 @@ __device__ __forceinline__ void accumulate32(const float4* __restrict__ col,
 }
 
 template <int FORMULA, int EPI, bool DOT>
-__global__ void __launch_bounds__(TILE) k_pair_f32(F32Args a) {
+__global__ void __launch_bounds__(TILE, 7) k_pair_f32(F32Args a) {
   if (a.skip_flag && *a.skip_flag) return;
   __shared__ float4 sc[TILE];
   __shared__ float su[TILE];
   __shared__ float sred[4][TILE];
   __shared__ double red[TILE / 32];
-  __shared__ double srb[4][6];   // row sub-tile boxes
-  __shared__ int sflag[4][4];    // [row sub-tile][column sub-tile] interact
   const int t = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int base = t * TILE;
-  if (tid < 24) srb[tid / 6][tid % 6] = a.rsbox[(size_t)t * 24 + tid];
 
   float2 x01, y01, z01, x23, y23, z23;
   {
@@ -121,34 +118,41 @@ __global__ void __launch_bounds__(TILE) k_pair_f32(F32Args a) {
   unsigned long long evaluated = 0;  // pairs this warp evaluates (profiling)
 
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
-  for (int p = p0; p < p1; ++p) {
+  // The next column tile's inputs are loaded into registers while the current
+  // tile is computed, so the L2 latency of the loads is hidden.
+  float4 nq = make_float4(0.f, 0.f, 0.f, 0.f), noc = nq;
+  float nu = 0.f;
+  unsigned nm = 0;
+  auto prefetch = [&](int p) {
     const int ct = a.cols[p];
+    const int j = ct * TILE + tid;
+    noc = a.corig[ct];
+    nq = a.cxi[j];
+    nu = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
+    nm = a.mask[p];
+  };
+  if (p0 < p1) prefetch(p0);
+  for (int p = p0; p < p1; ++p) {
     __syncthreads();
     {
-      const float4 oc = a.corig[ct];
-      const float dx = ot.x - oc.x, dy = ot.y - oc.y, dz = ot.z - oc.z;
-      const int j = ct * TILE + tid;
-      const float4 q = a.cxi[j];
-      const float zx = q.x - dx, zy = q.y - dy, zz = q.z - dz;
+      const float dx = ot.x - noc.x, dy = ot.y - noc.y, dz = ot.z - noc.z;
+      const float zx = nq.x - dx, zy = nq.y - dy, zz = nq.z - dz;
       if (FORMULA == F32_EXPANDED) {
         const float aj = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
         sc[tid] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -aj);
       } else {
         sc[tid] = make_float4(zx, zy, zz, 0.f);
       }
-      su[tid] = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
-      if (tid < 16) {
-        const int rs = tid >> 2, cs = tid & 3;
-        sflag[rs][cs] = boxes_interact(srb[rs], a.csbox + ((size_t)ct * 4 + cs) * 6, a.c_perp,
-                                       a.c_para, a.cull);
-      }
+      su[tid] = nu;
     }
+    const unsigned m = nm >> warp;  // bit 4k: row sub-tile k vs this warp's columns
+    if (p + 1 < p1) prefetch(p + 1);
     __syncthreads();
     float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
     const float4* col = sc + warp * 32;
     const float* cu = su + warp * 32;
-    const bool do01 = sflag[0][warp] | sflag[1][warp];
-    const bool do23 = sflag[2][warp] | sflag[3][warp];
+    const bool do01 = (m & 0x11u) != 0;
+    const bool do23 = (m & 0x1100u) != 0;
     evaluated += (do01 ? 2 * SUBTILE * 32 : 0) + (do23 ? 2 * SUBTILE * 32 : 0);
     if (do01 && do23)
       accumulate32<FORMULA, true, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);

@@ -53,7 +53,6 @@ __global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) 
   if (a.skip_flag && *a.skip_flag) return;
   __shared__ double sx[TILE], sy[TILE], sz[TILE], su[TILE];
   __shared__ double tf[EVAL == DS_EVAL_TABLE ? TABLE_N : 32];
-  __shared__ double scb[TILE / SUBTILE][6];
   __shared__ double red[TILE / 32];
   const int t = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -63,8 +62,6 @@ __global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) 
   } else if (tid < 32) {
     tf[tid] = exp2(-(double)tid / 32.0);
   }
-  double rb[6];
-  for (int c = 0; c < 6; ++c) rb[c] = a.rsbox[(size_t)(t * (TILE / SUBTILE) + warp) * 6 + c];
   // var_s, folded into the column weights (squared for the S^2 sum)
   const double wscale = EPI == EPI_NOISE ? kc.var_s * kc.var_s : kc.var_s;
   const double xi = a.rx[i], yi = a.ry[i], zi = a.rz[i];
@@ -82,11 +79,10 @@ __global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) 
       su[tid] = wscale * (a.wr[j] * a.v[j]);
     else
       su[tid] = wscale * a.v[j];
-    if (tid < (TILE / SUBTILE) * 6)
-      scb[tid / 6][tid % 6] = a.csbox[(size_t)ct * (TILE / SUBTILE) * 6 + tid];
+    const unsigned m = a.mask[p] >> (4 * warp);  // this warp's row sub-tile
     __syncthreads();
     for (int cs = 0; cs < TILE / SUBTILE; ++cs) {
-      if (!boxes_interact(rb, scb[cs], kc.c_perp, kc.c_para, kc.cull_arg)) continue;
+      if (!((m >> cs) & 1u)) continue;
       evaluated += SUBTILE * SUBTILE;
 #pragma unroll 4
       for (int jj = cs * SUBTILE; jj < (cs + 1) * SUBTILE; ++jj) {

@@ -157,7 +157,7 @@ PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
   a.rz = a.cz = op->pix.z.p;
   a.row_ptr = op->pairs.row_ptr.p;
   a.cols = op->pairs.cols.p;
-  a.rsbox = a.csbox = op->pix.sbox.p;
+  a.mask = op->pairs.mask.p;
   a.n_row_tiles = op->pix.n_tiles;
   a.wl = op->wl.p;
   a.wr = op->wr.p;
@@ -173,6 +173,10 @@ PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
 }
 
 void op_apply_sorted(ds_operator* op, int epi, const double* v, double* out, cudaStream_t st) {
+  if (op->use_dense) {
+    dense_apply(op, epi == EPI_RESIDUAL, v, out, nullptr, nullptr, nullptr, nullptr, nullptr, st);
+    return;
+  }
   PairArgs a = op_pair_args(op, v, out);
   launch_pair_f64(op->kc, epi, a, st);
 }
@@ -185,7 +189,8 @@ void ensure_pcg_workspace(ds_operator* op) {
   op->q.alloc(np);
   op->s.alloc(np);
   op->partial.alloc(std::max<size_t>(2 * VGRID_MAX, op->pix.n_tiles));
-  op->partial2.alloc(std::max<size_t>(2 * VGRID_MAX, op->pix.n_tiles));
+  op->partial2.alloc(std::max(std::max((size_t)2 * VGRID_MAX, (size_t)op->pix.n_tiles),
+                              (size_t)dense_partials(op->pix.n_pad)));
   op->state.alloc(1);
   op->h_flag.alloc(64);
 }
@@ -233,12 +238,19 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
   for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   int issued = 0, waited = 0;
   for (int it = 1; it < pp.max_iter; ++it) {
-    launch_pair_f64(op->kc, EPI_PRODUCT, prod, st);  // q = A d, alpha
+    if (op->use_dense)  // q = A d, alpha
+      dense_apply(op, false, op->d.p, op->q.p, op->d.p, op->partial2.p, S, &S->counter[0],
+                  &S->done, st);
+    else
+      launch_pair_f64(op->kc, EPI_PRODUCT, prod, st);
     if (it % pp.step_r == 0) {
       k_pcg_update<1><<<g, VB, 0, st>>>(np, S, op->x.p, op->r.p, op->d.p, op->q.p, op->s.p,
                                         op->pdiag.p, op->partial.p, op->hist.p, op->dhist.p);
       DS_CHECK_LAUNCH();
-      launch_pair_f64(op->kc, EPI_RESIDUAL, resid, st);  // r = b - A x
+      if (op->use_dense)  // r = b - A x
+        dense_apply(op, true, op->x.p, op->r.p, nullptr, nullptr, nullptr, nullptr, &S->done, st);
+      else
+        launch_pair_f64(op->kc, EPI_RESIDUAL, resid, st);
       k_pcg_update<2><<<g, VB, 0, st>>>(np, S, op->x.p, op->r.p, op->d.p, op->q.p, op->s.p,
                                         op->pdiag.p, op->partial.p, op->hist.p, op->dhist.p);
     } else {

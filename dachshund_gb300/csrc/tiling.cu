@@ -266,6 +266,29 @@ __global__ void k_pair_fill(const double* __restrict__ rbox, const double* __res
   }
 }
 
+// Sub-tile interaction masks of every kept tile pair: bit 4 k + w for row
+// sub-tile k and column sub-tile w.
+__global__ void k_pair_mask(int n_rows, const int* __restrict__ row_ptr,
+                            const int* __restrict__ cols, const double* __restrict__ rsbox,
+                            const double* __restrict__ csbox, double c_perp, double c_para,
+                            double cut, unsigned short* __restrict__ mask) {
+  const int r = blockIdx.x;
+  if (r >= n_rows) return;
+  double rb[4][6];
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 6; ++c) rb[k][c] = rsbox[((size_t)r * 4 + k) * 6 + c];
+  for (int p = row_ptr[r] + threadIdx.x; p < row_ptr[r + 1]; p += blockDim.x) {
+    const int ct = cols[p];
+    unsigned m = 0;
+    for (int w = 0; w < 4; ++w) {
+      const double* cb = csbox + ((size_t)ct * 4 + w) * 6;
+      for (int k = 0; k < 4; ++k)
+        if (tiles_interact(rb[k], cb, c_perp, c_para, cut)) m |= 1u << (4 * k + w);
+    }
+    mask[p] = (unsigned short)m;
+  }
+}
+
 }  // namespace
 
 // Balanced k-d partition.  Nodes cover whole SUBTILE-point units [u0, u1);
@@ -446,6 +469,11 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
                           cudaMemcpyHostToDevice, st));
   k_pair_fill<<<rows.n_tiles, BLK, 0, st>>>(rows.box.p, cols.box.p, cols.n_tiles, kc.c_perp,
                                             kc.c_para, kc.cull_arg, pl.row_ptr.p, pl.cols.p);
+  DS_CHECK_LAUNCH();
+  pl.mask.alloc(std::max<long long>(total, 1));
+  k_pair_mask<<<rows.n_tiles, 64, 0, st>>>(rows.n_tiles, pl.row_ptr.p, pl.cols.p, rows.sbox.p,
+                                           cols.sbox.p, kc.c_perp, kc.c_para, kc.cull_arg,
+                                           pl.mask.p);
   DS_CHECK_LAUNCH();
   DS_CUDA(cudaStreamSynchronize(st));
 }

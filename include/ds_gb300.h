@@ -157,6 +157,13 @@ int ds_norm_b(ds_operator* op, double* norm_b);
 int ds_A_entries(ds_operator* op, int eval, int m, const int* ii,
                  const int* jj, double* out);
 
+/* Dense S_pp in HBM (no reference counterpart; the reference builds the
+ * dense matrix only inside solve_cf, lib/wf_vector.cc:127-133).  enable = 1
+ * builds the n x n FP64 operator in device memory (8 n^2 bytes; DS_ERR_OOM
+ * when it does not fit) and makes A_product, A_residual and solve_pcg use the
+ * dense matvec; enable = 0 frees it and returns to the matrix-free kernels. */
+int ds_operator_set_dense(ds_operator* op, int enable);
+
 /* ---- PCG ---------------------------------------------------------------- */
 /* PCGParams (lib/pcg.h:13-19); n is the operator's. */
 typedef struct {
@@ -214,6 +221,24 @@ int ds_solve_pcg_noalloc(int form, int n, const double* records,
                          const ds_kernel_params* kp, const ds_pcg_params* pp,
                          double* x, ds_pcg_result* res,
                          double* residual_norms, void* stream);
+
+/* WFVector{SN,W}::solve_cf (lib/wf_vector.cc:123-155, 276-319): the dense
+ * system built on the device (table or exact kernel per kp->eval, as the
+ * reference's ``exact`` flag) and solved by an FP64 Cholesky factorisation
+ * (the reference uses Eigen's LDL^T; A is SPD, so the solutions agree to
+ * round-off).  ``records``: n NPixel / WPixel host records; ``x`` receives the
+ * solution (times w in the W form).  Needs 8 n^2 bytes of device memory. */
+int ds_solve_cf(ds_context* ctx, int form, int n, const double* records,
+                const ds_kernel_params* kp, double* x);
+
+/* MapCovarDiag::solve_pcg (lib/map_covar.cc:73-113): for every map point i,
+ * the SN-form PCG solve of (S + N) x = S_pm[:, i] from x = 0, then
+ * sigma_m[i] = S_mp[i, :] . x when the solve succeeded (else 0).  Writes the
+ * per-point iteration counts and success flags. */
+int ds_map_covar_diag(ds_context* ctx, int n_pix, const double* npixels, int n_map,
+                      const double* map_points, const ds_kernel_params* kp,
+                      const ds_pcg_params* pp, double* sigma_m, int* iters,
+                      int* success);
 
 /* ---- mixed-precision form (no reference counterpart) --------------------
  * Solves the same system as ds_solve_pcg with the exact kernel

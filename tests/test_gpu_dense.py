@@ -1,0 +1,69 @@
+"""GPU tests of the dense paths: the dense operator in HBM (same matvec and
+PCG as the matrix-free kernels), the closed-form solve (GPU Cholesky vs the
+oracle's LDL^T), and MapCovarDiag against the reference's golden output."""
+import numpy as np
+import pytest
+
+import oracle
+from dachshund_gb300 import (PCGParams, SignalCovarParams, WFVectorSN, WFVectorW,
+                             map_covar_diag, pixel_to_npixel, pixel_to_wpixel, solve_cf, synth)
+
+pytestmark = pytest.mark.gpu
+
+VS, LP, LQ = synth.VAR_S, synth.L_PERP, synth.L_PARA
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("form", ["w", "sn"])
+@pytest.mark.parametrize("ev", ["table", "exact"])
+def test_dense_operator_matches_matrix_free(ctx, form, ev):
+    w = synth.small(20, 40, 14.0, seed=17)
+    sp = SignalCovarParams(VS, LP, LQ, eval=ev)
+    rec = pixel_to_wpixel(w.pixels) if form == "w" else pixel_to_npixel(w.pixels)
+    cls = WFVectorW if form == "w" else WFVectorSN
+    mf, dn = cls(ctx, rec, sp), cls(ctx, rec, sp)
+    dn.set_dense(True)
+    a = np.random.default_rng(3).standard_normal(w.n)
+    assert rel(dn.A_product(a), mf.A_product(a)) < 1e-12
+    assert rel(dn.A_residual(a), mf.A_residual(a)) < 1e-12
+    x1, r1 = mf.solve_pcg(PCGParams(1000, 50, 1e-8))
+    x2, r2 = dn.solve_pcg(PCGParams(1000, 50, 1e-8))
+    assert r1.success and r2.success and abs(r1.num_iters - r2.num_iters) <= 2
+    assert rel(x2, x1) < 1e-6
+    xf1, _ = mf.solve_pcg(PCGParams(r1.num_iters + 1, 50, 0.0))
+    xf2, _ = dn.solve_pcg(PCGParams(r1.num_iters + 1, 50, 0.0))
+    assert rel(xf2, xf1) < 1e-8
+    dn.set_dense(False)
+    assert rel(dn.A_product(a), mf.A_product(a)) < 1e-12
+
+
+@pytest.mark.parametrize("form", ["w", "sn"])
+@pytest.mark.parametrize("exact", [False, True])
+def test_solve_cf_matches_oracle(ctx, form, exact):
+    w = synth.small(9, 40, 10.0, seed=23)  # 360 pixels, not a multiple of the panel
+    rec = pixel_to_wpixel(w.pixels) if form == "w" else pixel_to_npixel(w.pixels)
+    sp = SignalCovarParams(VS, LP, LQ, eval="exact" if exact else "table")
+    x = solve_cf(ctx, form, rec, sp)
+    xo = oracle.solve_cf(form, rec, VS, LP, LQ, exact=exact)
+    assert rel(x, xo) < 1e-10
+
+
+def test_solve_cf_matches_pcg(ctx, golden):
+    g = golden["small"]
+    rec = pixel_to_wpixel(g["pixels"])
+    x = solve_cf(ctx, "w", rec, SignalCovarParams(VS, LP, LQ))
+    assert rel(x, g["x_w"]) < 1e-6  # the golden PCG stopped at |r| <= 1e-8 |b|
+
+
+def test_map_covar_diag_golden(ctx, golden):
+    g = golden["small"]
+    nrec = pixel_to_npixel(g["pixels"])
+    s, iters, ok = map_covar_diag(ctx, nrec, g["cov_pts"], SignalCovarParams(VS, LP, LQ),
+                                  PCGParams(1000, 50, 1e-6))
+    assert ok.all() == g["cov_success"].all()
+    assert np.all(np.abs(iters - g["cov_iters"]) <= 2)
+    # Both stopped at |r| <= 1e-6 |b|; sigma = b . x agrees to ~tol * cond.
+    assert rel(s, g["cov"]) < 1e-5
