@@ -204,6 +204,7 @@ void map_product_dev(ds_map* map, ds_operator* op, const double* x_dev, double* 
   a.row_ptr = map->pairs.row_ptr.p;
   a.cols = map->pairs.cols.p;
   a.mask = map->pairs.mask.p;
+  a.row_order = map->pairs.row_order.p;
   a.n_row_tiles = map->pts.n_tiles;
   a.v = op->tmp.p;
   a.out = m_dev;
@@ -632,6 +633,7 @@ int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points, int n
     a.row_ptr = pl.row_ptr.p;
     a.cols = pl.cols.p;
     a.mask = pl.mask.p;
+    a.row_order = pl.row_order.p;
     a.n_row_tiles = mp.n_tiles;
     a.v = xs.p;
     a.out = dm.p;
@@ -674,6 +676,7 @@ int ds_sigma_m_noise_dom(ds_context* ctx, int n_pix, const double* npixels, int 
     a.row_ptr = pl.row_ptr.p;
     a.cols = pl.cols.p;
     a.mask = pl.mask.p;
+    a.row_order = pl.row_order.p;
     a.n_row_tiles = mp.n_tiles;
     a.v = u.p;
     a.out = dm.p;

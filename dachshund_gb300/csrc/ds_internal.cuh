@@ -153,6 +153,7 @@ struct PairList {
   // per pair: bit (4 k + w) set when row sub-tile k interacts with column
   // sub-tile w (the same box test at sub-tile granularity)
   DevBuf<unsigned short> mask;
+  DevBuf<int> row_order;  // row tiles by decreasing pair count (launch order)
 };
 
 void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
@@ -174,6 +175,7 @@ struct PairArgs {
   const int* row_ptr; const int* cols;
   int n_row_tiles;
   const unsigned short* mask;  // sub-tile interaction mask per tile pair
+  const int* row_order;        // blockIdx -> row tile (heaviest first), or null
   // coefficients (sorted order)
   const double* wl; const double* wr; const double* e; const double* b;
   const double* v;      // the vector being multiplied (column side)

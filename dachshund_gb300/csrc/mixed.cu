@@ -352,6 +352,7 @@ F32Args op_f32_args(ds_operator* op, const float* v, float* out) {
   a.row_ptr = f.pairs.row_ptr.p;
   a.cols = f.pairs.cols.p;
   a.mask = f.pairs.mask.p;
+  a.row_order = f.pairs.row_order.p;
   a.n_row_tiles = op->pix.n_tiles;
   a.colw = f.colw.p;
   a.v = v;
@@ -517,6 +518,7 @@ void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, doub
   a.row_ptr = f.pairs.row_ptr.p;
   a.cols = f.pairs.cols.p;
   a.mask = f.pairs.mask.p;
+  a.row_order = f.pairs.row_order.p;
   a.n_row_tiles = map->pts.n_tiles;
   a.v = f.xs.p;
   a.rowf = f.rowf.p;

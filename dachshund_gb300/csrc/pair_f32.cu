@@ -95,13 +95,13 @@ __device__ __forceinline__ void accumulate32(const float4* __restrict__ col,
 }
 
 template <int FORMULA, int EPI, bool DOT>
-__global__ void __launch_bounds__(TILE, 7) k_pair_f32(F32Args a) {
+__global__ void __launch_bounds__(TILE, 8) k_pair_f32(F32Args a) {
   if (a.skip_flag && *a.skip_flag) return;
   __shared__ float4 sc[TILE];
   __shared__ float su[TILE];
   __shared__ float sred[4][TILE];
   __shared__ double red[TILE / 32];
-  const int t = blockIdx.x;
+  const int t = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;  // heaviest tiles first
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int base = t * TILE;
 
@@ -131,10 +131,16 @@ __global__ void __launch_bounds__(TILE, 7) k_pair_f32(F32Args a) {
     nu = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
     nm = a.mask[p];
   };
+  // Each warp stages and reads only its own 32 columns (sc[32 warp + lane]),
+  // so the warps of a CTA never wait for each other inside the loop (their
+  // work differs with the sub-tile mask).
   if (p0 < p1) prefetch(p0);
   for (int p = p0; p < p1; ++p) {
-    __syncthreads();
-    {
+    const unsigned m = nm >> warp;  // bit 4k: row sub-tile k vs this warp's columns
+    const bool do01 = (m & 0x11u) != 0;
+    const bool do23 = (m & 0x1100u) != 0;
+    if (do01 || do23) {
+      __syncwarp();
       const float dx = ot.x - noc.x, dy = ot.y - noc.y, dz = ot.z - noc.z;
       const float zx = nq.x - dx, zy = nq.y - dy, zz = nq.z - dz;
       if (FORMULA == F32_EXPANDED) {
@@ -144,15 +150,13 @@ __global__ void __launch_bounds__(TILE, 7) k_pair_f32(F32Args a) {
         sc[tid] = make_float4(zx, zy, zz, 0.f);
       }
       su[tid] = nu;
+      __syncwarp();
     }
-    const unsigned m = nm >> warp;  // bit 4k: row sub-tile k vs this warp's columns
     if (p + 1 < p1) prefetch(p + 1);
-    __syncthreads();
+    if (!(do01 || do23)) continue;
     float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
     const float4* col = sc + warp * 32;
     const float* cu = su + warp * 32;
-    const bool do01 = (m & 0x11u) != 0;
-    const bool do23 = (m & 0x1100u) != 0;
     evaluated += (do01 ? 2 * SUBTILE * 32 : 0) + (do23 ? 2 * SUBTILE * 32 : 0);
     if (do01 && do23)
       accumulate32<FORMULA, true, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);

@@ -51,46 +51,55 @@ __device__ __forceinline__ double g_exact_fast(double dx, double dy, double dz,
 template <int EVAL, int EPI, bool DOT>
 __global__ void __launch_bounds__(TILE) k_pair_f64(KernelConsts kc, PairArgs a) {
   if (a.skip_flag && *a.skip_flag) return;
-  __shared__ double sx[TILE], sy[TILE], sz[TILE], su[TILE];
+  // Warp-private staging of one 32-column sub-tile at a time: a warp loads
+  // only the column sub-tiles its own row sub-tile interacts with, and the
+  // warps of a CTA never wait for each other inside the loop.
+  __shared__ double sw[TILE / 32][4][SUBTILE];
   __shared__ double tf[EVAL == DS_EVAL_TABLE ? TABLE_N : 32];
   __shared__ double red[TILE / 32];
-  const int t = blockIdx.x;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int t = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;  // heaviest tiles first
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i = t * TILE + tid;
   if (EVAL == DS_EVAL_TABLE) {
     for (int k = tid; k < TABLE_N; k += TILE) tf[k] = a.table[k];
   } else if (tid < 32) {
     tf[tid] = exp2(-(double)tid / 32.0);
   }
+  __syncthreads();
   // var_s, folded into the column weights (squared for the S^2 sum)
   const double wscale = EPI == EPI_NOISE ? kc.var_s * kc.var_s : kc.var_s;
   const double xi = a.rx[i], yi = a.ry[i], zi = a.rz[i];
   double acc = 0.0;
   unsigned long long evaluated = 0;  // pairs this warp evaluates (profiling)
+  double* sxw = sw[warp][0];
+  double* syw = sw[warp][1];
+  double* szw = sw[warp][2];
+  double* suw = sw[warp][3];
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
   for (int p = p0; p < p1; ++p) {
+    const unsigned m = (a.mask[p] >> (4 * warp)) & 0xFu;  // this warp's row sub-tile
+    if (!m) continue;
     const int ct = a.cols[p];
-    const int j = ct * TILE + tid;
-    __syncthreads();
-    sx[tid] = a.cx[j];
-    sy[tid] = a.cy[j];
-    sz[tid] = a.cz[j];
-    if (EPI == EPI_PRODUCT || EPI == EPI_RESIDUAL)
-      su[tid] = wscale * (a.wr[j] * a.v[j]);
-    else
-      su[tid] = wscale * a.v[j];
-    const unsigned m = a.mask[p] >> (4 * warp);  // this warp's row sub-tile
-    __syncthreads();
     for (int cs = 0; cs < TILE / SUBTILE; ++cs) {
       if (!((m >> cs) & 1u)) continue;
+      const int j = ct * TILE + cs * SUBTILE + lane;
+      __syncwarp();
+      sxw[lane] = a.cx[j];
+      syw[lane] = a.cy[j];
+      szw[lane] = a.cz[j];
+      if (EPI == EPI_PRODUCT || EPI == EPI_RESIDUAL)
+        suw[lane] = wscale * (a.wr[j] * a.v[j]);
+      else
+        suw[lane] = wscale * a.v[j];
+      __syncwarp();
       evaluated += SUBTILE * SUBTILE;
 #pragma unroll 4
-      for (int jj = cs * SUBTILE; jj < (cs + 1) * SUBTILE; ++jj) {
-        const double dx = xi - sx[jj], dy = yi - sy[jj], dz = zi - sz[jj];
+      for (int jj = 0; jj < SUBTILE; ++jj) {
+        const double dx = xi - sxw[jj], dy = yi - syw[jj], dz = zi - szw[jj];
         double g = EVAL == DS_EVAL_TABLE ? gp_table_fast(dx, dy, dz, kc, tf)
                                          : g_exact_fast(dx, dy, dz, kc, tf);
         if (EPI == EPI_NOISE) g = g * g;
-        acc = fma(g, su[jj], acc);
+        acc = fma(g, suw[jj], acc);
       }
     }
   }

@@ -158,6 +158,7 @@ PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
   a.row_ptr = op->pairs.row_ptr.p;
   a.cols = op->pairs.cols.p;
   a.mask = op->pairs.mask.p;
+  a.row_order = op->pairs.row_order.p;
   a.n_row_tiles = op->pix.n_tiles;
   a.wl = op->wl.p;
   a.wr = op->wr.p;

@@ -463,6 +463,12 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
   require(total < (1ll << 31), "too many tile pairs");
   rp[rows.n_tiles] = (int)total;
   pl.n_pairs = total;
+  std::vector<int> order(rows.n_tiles);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hc[a] > hc[b]; });
+  pl.row_order.alloc(rows.n_tiles);
+  DS_CUDA(cudaMemcpyAsync(pl.row_order.p, order.data(), order.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, st));
   pl.row_ptr.alloc(rows.n_tiles + 1);
   pl.cols.alloc(std::max<long long>(total, 1));
   DS_CUDA(cudaMemcpyAsync(pl.row_ptr.p, rp.data(), rp.size() * sizeof(int),

@@ -63,8 +63,9 @@ def test_cxx_app_path_on_gpu(tmp_path, golden):
     pix_path = tmp_path / "pixels.bin"
     np.ascontiguousarray(pix).tofile(pix_path)
     prefix = str(tmp_path / "out")
-    args = [str(exe), str(pix_path), str(pix.shape[0]), repr(lx), repr(ly), repr(lz),
-            str(int(nx)), str(int(ny)), str(int(nz)), repr(tol), str(int(max_iter)),
+    args = [str(exe), str(pix_path), str(pix.shape[0]), repr(float(lx)), repr(float(ly)),
+            repr(float(lz)),
+            str(int(nx)), str(int(ny)), str(int(nz)), repr(float(tol)), str(int(max_iter)),
             str(int(step_r)), prefix]
     r = subprocess.run(args, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
