@@ -5,6 +5,8 @@ map projection, as hand-written CUDA kernels behind the C ABI of
 ``include/ds_gb300.h``.  See ``api`` for the Python face of that ABI.
 """
 from .api import (  # noqa: F401
+    BatchResult,
+    BatchSolver,
     Context,
     MapGrid,
     MixedParams,

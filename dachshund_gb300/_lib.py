@@ -27,6 +27,9 @@ DS_FORM_W = 1
 DS_EVAL_TABLE = 0
 DS_EVAL_EXACT = 1
 DS_TABLE_N = 200
+DS_BATCH_AUTO = -1
+DS_BATCH_CUDA_CORE = 0
+DS_BATCH_TENSOR = 1
 
 
 class KernelParamsC(C.Structure):
@@ -79,6 +82,23 @@ class OperatorInfoC(C.Structure):
         ("n_tiles", C.c_int),
         ("n_tile_pairs", C.c_longlong),
         ("evaluated_pairs", C.c_longlong),
+    ]
+
+
+class BatchInfoC(C.Structure):
+    _fields_ = [
+        ("n_chunks", C.c_int),
+        ("n_rhs", C.c_int),
+        ("n_total", C.c_int),
+        ("n_pad", C.c_int),
+        ("n_tiles", C.c_int),
+        ("inner_tile_pairs", C.c_longlong),
+        ("outer_tile_pairs", C.c_longlong),
+        ("inner_evaluated", C.c_longlong),
+        ("outer_evaluated", C.c_longlong),
+        ("variant", C.c_int),
+        ("rhs_block", C.c_int),
+        ("graph_replays", C.c_int),
     ]
 
 
@@ -137,6 +157,16 @@ SIGNATURES = {
     "ds_solve_mixed_dev": (_i, [_vp, C.POINTER(MixedParamsC), _vp, C.POINTER(PcgResultC), _dp]),
     "ds_map_product_f32": (_i, [_vp, _vp, _d, _dp, _dp]),
     "ds_map_product_f32_dev": (_i, [_vp, _vp, _d, _vp, _vp]),
+    "ds_batch_create": (_i, [_vp, _i, _i, _ip, _dp, C.POINTER(KernelParamsC), _i, _d,
+                             C.POINTER(_vp)]),
+    "ds_batch_destroy": (None, [_vp]),
+    "ds_batch_get_info": (_i, [_vp, C.POINTER(BatchInfoC)]),
+    "ds_batch_set_variant": (_i, [_vp, _i, _i]),
+    "ds_batch_solve_mixed": (_i, [_vp, C.POINTER(MixedParamsC), _dp, _dp, _ip, _ip, _ip, _dp,
+                                  _dp]),
+    "ds_batch_solve_mixed_dev": (_i, [_vp, C.POINTER(MixedParamsC), _vp, _vp, _ip, _ip, _ip,
+                                      _dp, _dp]),
+    "ds_batch_product_f32_dev": (_i, [_vp, _vp, _vp]),
     "ds_map_create": (_i, [_vp, _i, _dp, C.POINTER(_vp)]),
     "ds_map_destroy": (None, [_vp]),
     "ds_map_product": (_i, [_vp, _vp, _dp, _dp]),

@@ -322,6 +322,108 @@ class WFVectorW(_WFVector):
     FORM = _lib.DS_FORM_W
 
 
+@dataclasses.dataclass
+class BatchResult:
+    """Per-(chunk, RHS) outcome of a batched solve, arrays of (n_chunks, n_rhs)."""
+
+    iters: np.ndarray
+    converged: np.ndarray
+    n_updates: np.ndarray
+    rel_resid: np.ndarray
+    seconds: float
+    status: int
+
+
+class BatchSolver:
+    """Independent chunks (each one WFVector operator) with n_rhs right-hand
+    sides each, solved together by the mixed-precision method.
+
+    ``chunks`` is a list of (n_c, 5) record arrays in the form's layout;
+    right-hand sides and solutions are (n_total, n_rhs) arrays over the
+    concatenated records."""
+
+    VARIANTS = {"auto": _lib.DS_BATCH_AUTO, "cuda_core": _lib.DS_BATCH_CUDA_CORE,
+                "tensor": _lib.DS_BATCH_TENSOR}
+
+    def __init__(self, ctx: Context, form: str, chunks, s_params: SignalCovarParams,
+                 n_rhs: int, inner_cutoff: float = 0.0):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        recs = [_f64(c) for c in chunks]
+        for r in recs:
+            if r.ndim != 2 or r.shape[1] != 5 or r.shape[0] == 0:
+                raise ValueError("every chunk must be a non-empty (n, 5) record array")
+        self.sizes = np.array([r.shape[0] for r in recs], dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        allrec = np.ascontiguousarray(np.concatenate(recs, axis=0))
+        self.n_total = allrec.shape[0]
+        self.n_chunks = len(recs)
+        self.n_rhs = int(n_rhs)
+        kp = s_params.as_c()
+        h = C.c_void_p()
+        ctx.check(self._lib.ds_batch_create(ctx.handle, FORMS[form], self.n_chunks,
+                                            self.sizes.ctypes.data_as(C.POINTER(C.c_int)),
+                                            _ptr(allrec), C.byref(kp), self.n_rhs,
+                                            float(inner_cutoff), C.byref(h)),
+                  "ds_batch_create")
+        self.handle = h
+        ctx._adopt(self)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.ds_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        inf = _lib.BatchInfoC()
+        self.ctx.check(self._lib.ds_batch_get_info(self.handle, C.byref(inf)), "info")
+        return {k: getattr(inf, k) for k, _ in inf._fields_}
+
+    def set_variant(self, variant: str = "auto", rhs_block: int = 0):
+        self.ctx.check(self._lib.ds_batch_set_variant(self.handle, self.VARIANTS[variant],
+                                                      int(rhs_block)), "ds_batch_set_variant")
+
+    def _solve(self, fn, mp, rhs_ptr, x_ptr):
+        shape = (self.n_chunks, self.n_rhs)
+        iters = np.zeros(shape, dtype=np.int32)
+        conv = np.zeros(shape, dtype=np.int32)
+        nupd = np.zeros(shape, dtype=np.int32)
+        rel = np.zeros(shape)
+        secs = C.c_double()
+        c = (mp or MixedParams()).as_c()
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
+        rc = fn(self.handle, C.byref(c), rhs_ptr, x_ptr, ip(iters), ip(conv), ip(nupd),
+                _ptr(rel), C.byref(secs))
+        if rc not in (_lib.DS_OK, _lib.DS_ERR_NOT_CONVERGED):
+            self.ctx.check(rc, fn.__name__)
+        return BatchResult(iters, conv.astype(bool), nupd, rel, secs.value, rc)
+
+    def solve_mixed(self, rhs, mp: MixedParams = None):
+        """rhs: (n_total, n_rhs); returns (x, BatchResult)."""
+        b = _f64(rhs, self.n_total * self.n_rhs, "rhs")
+        x = np.zeros((self.n_total, self.n_rhs))
+        res = self._solve(self._lib.ds_batch_solve_mixed, mp, _ptr(b), _ptr(x))
+        return x, res
+
+    def solve_mixed_dev(self, rhs, x, mp: MixedParams = None):
+        """rhs, x: CUDA float64 tensors of n_total * n_rhs elements."""
+        n = self.n_total * self.n_rhs
+        return self._solve(self._lib.ds_batch_solve_mixed_dev, mp, _dev_ptr(rhs, n),
+                           _dev_ptr(x, n))
+
+    def product_f32_dev(self, p, q):
+        n = self.n_total * self.n_rhs
+        self.ctx.check(self._lib.ds_batch_product_f32_dev(self.handle, _dev_ptr(p, n),
+                                                          _dev_ptr(q, n)),
+                       "ds_batch_product_f32_dev")
+
+
 class MapGrid:
     """Map points sorted and tiled on the device once (for repeated products)."""
 

@@ -1,0 +1,549 @@
+// Multi-RHS matvec of the batched solver on the 5th-generation tensor cores:
+// each generated S tile (128 rows x 128 columns of one tile pair) times the
+// block of NB right-hand sides of the column tile is a BF16 contraction with
+// FP32 accumulation in tensor memory (tcgen05.mma, kind::f16, M = 128,
+// N = NB, K = 16 per instruction).
+//
+// Precision: S and u = w p are split into BF16 hi + lo parts and the product
+// is S_hi u_hi + S_hi u_lo + S_lo u_hi (three MMAs per K step), about 16
+// significant bits per term with an FP32 accumulator: an operator error near
+// 1e-5 relative, which the FP64 reliable updates of the solver remove.
+//
+// Per CTA (256 threads, one CTA per SM, persistent over (row tile, RHS
+// block) items):
+//   * every thread generates S for one row and 64 columns of the current
+//     column tile (EXPANDED exponent: 3 FFMA + ex2 per pair; DIRECT when the
+//     tiles are too wide for it: 3 FADD + 3 FMUL/FFMA + ex2), splits it into
+//     BF16 hi / lo and stores both into shared memory in the canonical
+//     K-major no-swizzle layout (8 x 16-byte core matrices); column
+//     sub-tiles outside the cutoff of the warp's row sub-tile are zero;
+//   * the u panel of the column tile (pre-packed in HBM by k_pack_panels in
+//     the same core-matrix layout) arrives by one cp.async.bulk copy on an
+//     mbarrier;
+//   * one thread issues the MMAs (K steps whose column sub-tile interacts
+//     with no row sub-tile are skipped) and commits them to an mbarrier;
+//   * S and the panels are double-buffered, so the generation of tile k + 1
+//     overlaps the MMAs of tile k;
+//   * the epilogue reads D from tensor memory (tcgen05.ld), forms
+//     q = rowf D + ediag p and the tile's p.q per RHS.
+// Every mbarrier wait is bounded: on a time-out the kernel records an error
+// code, waits (bounded) for its own MMAs and copies, frees its tensor memory
+// and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "ds_batch.h"
+
+namespace ds {
+namespace {
+
+constexpr int TC_THREADS = 256;
+constexpr uint32_t WAIT_TRIES = 1u << 24;  // x (poll + 64 ns sleep) ~ 1-2 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Waits for the completion of the phase with parity `parity`; false after
+// WAIT_TRIES polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t k = 0; k < WAIT_TRIES; ++k) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (k >= 64) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem], BF16 inputs, FP32 accumulator.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major without swizzling: start
+// address, leading-dimension byte offset (between core matrices adjacent in
+// K), stride byte offset (between 8-row groups adjacent in M or N), the
+// descriptor version bit (46) and layout type 0 (no swizzle).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at
+// bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[N]);
+
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
+               "tcgen05.wait::ld.sync.aligned;"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <>
+__device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <>
+__device__ __forceinline__ void tmem_ld<32>(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ float ex2_tc(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// hi = bf16(a), lo = bf16(a - hi) for a pair, packed as bf16x2.
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const __nv_bfloat162 l =
+      __floats2bfloat162_rn(a - __low2float(h), b - __high2float(h));
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// Elements of one S buffer (128 x 128 BF16) and one u panel (NB x 128).
+constexpr int S_ELEMS = TILE * TILE;
+// Core-matrix layout (K-major, no swizzle), in BF16 elements: element
+// (row m, k) of a 128-row operand at ((k / 8) * 16 + m / 8) * 64 + (m % 8) * 8
+// + k % 8, i.e. LBO (K-adjacent) 2048 bytes, SBO (M-adjacent) 128 bytes.  A u
+// panel (row n = RHS, k = pixel) uses ((k / 8) * (NB / 8) + n / 8) * 64 +
+// (n % 8) * 8 + k % 8: LBO NB / 8 * 128 bytes, SBO 128 bytes.
+constexpr uint32_t S_LBO = 16 * 128;
+constexpr uint32_t CORE_SBO = 128;
+
+template <int NB>
+struct TcSmem {
+  __nv_bfloat16 s[2][2][S_ELEMS];     // [buffer][hi, lo]
+  __nv_bfloat16 u[2][2 * NB * TILE];  // [buffer] hi then lo
+  float4 sc[TILE];                    // column coordinates of the current tile
+  uint64_t full[2];                   // u panel landed
+  uint64_t mma_done[2];               // MMAs reading buffer b completed
+  uint32_t tmem_addr;
+  int item;
+  int abort;
+  int any_mma;
+};
+
+template <int NB>
+constexpr size_t tc_smem_bytes() {
+  return sizeof(TcSmem<NB>) + 1024;  // + alignment slack
+}
+
+template <int NB, int FORMULA>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
+  static_assert(NB == 16 || NB == 32 || NB == 64, "RHS block");
+  constexpr uint32_t TMEM_COLS = NB < 32 ? 32 : NB;
+  constexpr uint32_t PANEL_BYTES = 2u * NB * TILE * 2u;
+  constexpr uint32_t U_LBO = (NB / 8) * 128;
+  constexpr uint32_t IDESC = idesc_bf16(128, NB);
+  extern __shared__ uint8_t smem_raw[];
+  TcSmem<NB>& sm = *reinterpret_cast<TcSmem<NB>*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (TILE - 1), half = tid >> 7, rs = row >> 5;
+  if (tid == 0) {
+    mbar_init(&sm.full[0], 1);
+    mbar_init(&sm.full[1], 1);
+    mbar_init(&sm.mma_done[0], 1);
+    mbar_init(&sm.mma_done[1], 1);
+    sm.abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(&sm.tmem_addr, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_addr;
+  const int R = a.n_rhs;
+  const int nblk = R / NB;
+  const int n_items = a.n_row_tiles * nblk;
+  uint32_t g = 0;           // pipeline position (column tiles processed by this CTA)
+  int last_copy = -1;       // g of the last u-panel copy issued (thread 0)
+  int last_commit = -1;     // g of the last MMA commit (thread 0)
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) sm.item = (int)atomicAdd(a.work, 1u);
+    __syncthreads();
+    const int item = sm.item;
+    if (item >= n_items || sm.abort) break;
+    const int t = a.row_order[item / nblk];
+    const int rb = item % nblk;
+    if (a.chunk_done[a.tile_chunk[t]]) continue;
+    const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
+    const int i = t * TILE + row;
+    const float4 me = a.xi[i];
+    const float4 ot = a.orig[t];
+    const __nv_bfloat16* panels = reinterpret_cast<const __nv_bfloat16*>(a.panel);
+    if (tid == 0) {
+      sm.any_mma = 0;
+      const int ct0 = a.cols[p0];
+      mbar_expect_tx(&sm.full[g & 1], PANEL_BYTES);
+      bulk_g2s(sm.u[g & 1], panels + ((size_t)ct0 * nblk + rb) * (2 * NB * TILE), PANEL_BYTES,
+               &sm.full[g & 1]);
+      last_copy = (int)g;
+    }
+    // register prefetch of the column coordinates (threads of half 0 stage them)
+    int ct = a.cols[p0];
+    float4 cq = half == 0 ? a.xi[ct * TILE + row] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 co = a.orig[ct];
+    uint32_t accumulate = 0;  // thread 0: the item's first MMA overwrites D
+    for (int p = p0; p < p1; ++p, ++g) {
+      const unsigned m = a.mask[p];
+      if (half == 0) {
+        const float zx = cq.x - (ot.x - co.x), zy = cq.y - (ot.y - co.y);
+        const float zz = cq.z - (ot.z - co.z);
+        if (FORMULA == F32_EXPANDED)
+          sm.sc[row] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -fmaf(zx, zx, fmaf(zy, zy, zz * zz)));
+        else
+          sm.sc[row] = make_float4(zx, zy, zz, 0.f);
+      }
+      if (p + 1 < p1) {
+        ct = a.cols[p + 1];
+        if (half == 0) cq = a.xi[ct * TILE + row];
+        co = a.orig[ct];
+      }
+      __syncthreads();  // sc staged; S[g & 1] free (MMAs of g - 2 waited below)
+      if (sm.abort) break;
+      {
+        __nv_bfloat16* shi = sm.s[g & 1][0];
+        __nv_bfloat16* slo = sm.s[g & 1][1];
+        const int rg = row >> 3, ir = row & 7;
+#pragma unroll
+        for (int c2 = 0; c2 < 2; ++c2) {
+          const int cs = 2 * half + c2;
+          const bool on = (m >> (4 * rs + cs)) & 1u;
+#pragma unroll
+          for (int kq = 0; kq < 4; ++kq) {
+            const int kg = cs * 4 + kq;
+            uint4 vh = make_uint4(0u, 0u, 0u, 0u), vl = make_uint4(0u, 0u, 0u, 0u);
+            if (on) {
+              float s8[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                const float4 c4 = sm.sc[kg * 8 + e];
+                float t2;
+                if (FORMULA == F32_EXPANDED) {
+                  t2 = fmaf(me.x, c4.x, c4.w);
+                  t2 = fmaf(me.y, c4.y, t2);
+                  t2 = fmaf(me.z, c4.z, t2);
+                } else {
+                  const float dx = me.x - c4.x, dy = me.y - c4.y, dz = me.z - c4.z;
+                  t2 = -fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                }
+                s8[e] = ex2_tc(t2);
+              }
+              split2(s8[0], s8[1], vh.x, vl.x);
+              split2(s8[2], s8[3], vh.y, vl.y);
+              split2(s8[4], s8[5], vh.z, vl.z);
+              split2(s8[6], s8[7], vh.w, vl.w);
+            }
+            const int off = (kg * 16 + rg) * 64 + ir * 8;
+            *reinterpret_cast<uint4*>(shi + off) = vh;
+            *reinterpret_cast<uint4*>(slo + off) = vl;
+          }
+        }
+      }
+      fence_async_smem();
+      __syncthreads();  // S[g & 1] written
+      if (tid == 0) {
+        if (!mbar_wait(&sm.full[g & 1], (g >> 1) & 1u)) {
+          atomicExch(a.err, 1);
+          sm.abort = 1;
+        } else {
+          tc_fence_after();
+          const uint32_t sa = smem_u32(sm.s[g & 1][0]), sl = smem_u32(sm.s[g & 1][1]);
+          const uint32_t ua = smem_u32(sm.u[g & 1]), ul = ua + NB * TILE * 2;
+#pragma unroll 1
+          for (int ks = 0; ks < TILE / 16; ++ks) {
+            if (!((m >> (ks >> 1)) & 0x1111u)) continue;  // no row sub-tile reaches it
+            const uint32_t aoff = ks * 2 * S_LBO, boff = ks * 2 * U_LBO;
+            const uint64_t ahi = sdesc(sa + aoff, S_LBO, CORE_SBO);
+            const uint64_t alo = sdesc(sl + aoff, S_LBO, CORE_SBO);
+            const uint64_t bhi = sdesc(ua + boff, U_LBO, CORE_SBO);
+            const uint64_t blo = sdesc(ul + boff, U_LBO, CORE_SBO);
+            mma_bf16(tmem, ahi, bhi, IDESC, accumulate);
+            mma_bf16(tmem, ahi, blo, IDESC, 1u);
+            mma_bf16(tmem, alo, bhi, IDESC, 1u);
+            accumulate = 1u;
+            sm.any_mma = 1;
+          }
+          mma_commit(&sm.mma_done[g & 1]);
+          last_commit = (int)g;
+          // the next tile's panel goes to the other buffer once the MMAs of
+          // tile g - 1 (its last reader) are done
+          if (p + 1 < p1) {
+            if (g >= 1 && !mbar_wait(&sm.mma_done[(g - 1) & 1], ((g - 1) >> 1) & 1u)) {
+              atomicExch(a.err, 2);
+              sm.abort = 1;
+            } else {
+              mbar_expect_tx(&sm.full[(g + 1) & 1], PANEL_BYTES);
+              bulk_g2s(sm.u[(g + 1) & 1],
+                       panels + ((size_t)a.cols[p + 1] * nblk + rb) * (2 * NB * TILE),
+                       PANEL_BYTES, &sm.full[(g + 1) & 1]);
+              last_copy = (int)g + 1;
+            }
+          }
+        }
+      }
+    }
+    // epilogue: all MMAs of the item done (the commit of the last tile
+    // tracks every earlier one)
+    if (tid == 0 && !sm.abort && !mbar_wait(&sm.mma_done[(g - 1) & 1], ((g - 1) >> 1) & 1u)) {
+      atomicExch(a.err, 3);
+      sm.abort = 1;
+    }
+    __syncthreads();
+    if (sm.abort) break;
+    tc_fence_after();
+    constexpr int HN = NB / 2;
+    float d[HN];
+    tmem_ld<HN>(tmem + ((uint32_t)(32 * rs) << 16) + (uint32_t)(half * HN), d);
+    if (!sm.any_mma) {
+#pragma unroll
+      for (int k = 0; k < HN; ++k) d[k] = 0.f;
+    }
+    tc_fence_before();
+    const float rf = a.rowf[i], ed = a.ediag[i];
+    const int r0 = rb * NB + half * HN;
+    float* red = reinterpret_cast<float*>(sm.s[0][0]);  // [TILE][NB] p.q products
+    const float4* pv4 = reinterpret_cast<const float4*>(a.p + (size_t)i * R + r0);
+    float4* qv4 = reinterpret_cast<float4*>(a.q + (size_t)i * R + r0);
+#pragma unroll
+    for (int k4 = 0; k4 < HN / 4; ++k4) {
+      const float4 pv = pv4[k4];
+      float4 qv;
+      qv.x = fmaf(rf, d[4 * k4 + 0], ed * pv.x);
+      qv.y = fmaf(rf, d[4 * k4 + 1], ed * pv.y);
+      qv.z = fmaf(rf, d[4 * k4 + 2], ed * pv.z);
+      qv.w = fmaf(rf, d[4 * k4 + 3], ed * pv.w);
+      qv4[k4] = qv;
+      float* rr = red + row * NB + half * HN + 4 * k4;
+      rr[0] = pv.x * qv.x;
+      rr[1] = pv.y * qv.y;
+      rr[2] = pv.z * qv.z;
+      rr[3] = pv.w * qv.w;
+    }
+    __syncthreads();
+    if (tid < NB) {
+      double s = 0.0;
+      for (int k = 0; k < TILE; ++k) s += (double)red[k * NB + tid];
+      a.part[(size_t)t * R + rb * NB + tid] = s;
+    }
+    if (a.prof_pairs && tid == 0) {
+      unsigned long long n_sub = 0;
+      for (int p = p0; p < p1; ++p) n_sub += __popc(a.mask[p]);
+      atomicAdd(a.prof_pairs, n_sub * SUBTILE * SUBTILE * NB);
+    }
+  }
+  // teardown: after a time-out, wait (bounded) for this CTA's own MMAs and
+  // copies in flight before the tensor memory is freed
+  __syncthreads();
+  if (tid == 0 && sm.abort) {
+    if (last_commit >= 0) mbar_wait(&sm.mma_done[last_commit & 1], (last_commit >> 1) & 1);
+    if (last_copy >= 0) mbar_wait(&sm.full[last_copy & 1], (last_copy >> 1) & 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
+}
+
+// u = colw p as BF16 hi / lo panels: per (column tile, RHS block of NB), the
+// hi panel then the lo panel, each in the core-matrix layout above.  One
+// thread per (tile, group of 8 pixels, RHS): 8 strided reads (coalesced over
+// the RHS index), one 16-byte store per part.
+template <int NB>
+__global__ void k_pack_panels(int n_tiles, int R, const float* __restrict__ p,
+                              const float* __restrict__ colw, __nv_bfloat16* __restrict__ panel) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t total = (size_t)n_tiles * (TILE / 8) * R;
+  if (k >= total) return;
+  const int r = (int)(k % R);
+  const size_t tk = k / R;
+  const int kg = (int)(tk % (TILE / 8));
+  const int ct = (int)(tk / (TILE / 8));
+  const int j0 = ct * TILE + kg * 8;
+  float u[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) u[e] = colw[j0 + e] * p[(size_t)(j0 + e) * R + r];
+  uint4 vh, vl;
+  split2(u[0], u[1], vh.x, vl.x);
+  split2(u[2], u[3], vh.y, vl.y);
+  split2(u[4], u[5], vh.z, vl.z);
+  split2(u[6], u[7], vh.w, vl.w);
+  const int rb = r / NB, rr = r % NB;
+  const size_t base = ((size_t)ct * (R / NB) + rb) * (2 * NB * TILE);
+  const int off = (kg * (NB / 8) + rr / 8) * 64 + (rr % 8) * 8;
+  *reinterpret_cast<uint4*>(panel + base + off) = vh;
+  *reinterpret_cast<uint4*>(panel + base + NB * TILE + off) = vl;
+}
+
+template <int NB, int FORMULA>
+void tc_launch(const BatchF32Args& a, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    DS_CUDA(cudaFuncSetAttribute(k_batch_mv_tc<NB, FORMULA>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc_smem_bytes<NB>()));
+    attr = true;
+  }
+  const size_t packs = (size_t)a.n_row_tiles * (TILE / 8) * a.n_rhs;
+  k_pack_panels<NB><<<(unsigned)((packs + 255) / 256), 256, 0, st>>>(
+      a.n_row_tiles, a.n_rhs, a.p, a.colw, reinterpret_cast<__nv_bfloat16*>(a.panel));
+  DS_CHECK_LAUNCH();
+  static int sms = 0;  // queried on the first (uncaptured) launch
+  if (!sms) {
+    int dev = 0;
+    DS_CUDA(cudaGetDevice(&dev));
+    DS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int items = a.n_row_tiles * (a.n_rhs / NB);
+  const int grid = std::max(1, std::min(items, sms));
+  DS_CUDA(cudaMemsetAsync(a.work, 0, sizeof(unsigned int), st));
+  k_batch_mv_tc<NB, FORMULA><<<grid, TC_THREADS, tc_smem_bytes<NB>(), st>>>(a);
+  DS_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+int batch_tc_block(int R) {
+  if (R % 64 == 0) return 64;
+  if (R % 32 == 0) return 32;
+  if (R % 16 == 0) return 16;
+  return 0;
+}
+
+size_t batch_tc_panel_elems(int n_tiles, int R) { return (size_t)n_tiles * TILE * R * 2; }
+
+template <int FORMULA>
+void tc_dispatch(const BatchF32Args& a, cudaStream_t st) {
+  switch (batch_tc_block(a.n_rhs)) {
+    case 64: tc_launch<64, FORMULA>(a, st); break;
+    case 32: tc_launch<32, FORMULA>(a, st); break;
+    case 16: tc_launch<16, FORMULA>(a, st); break;
+    default: throw Error{DS_ERR_ARG, "the tensor-core matvec needs n_rhs % 16 == 0"};
+  }
+}
+
+void launch_batch_mv_tc(const BatchF32Args& a, cudaStream_t st) {
+  if (a.formula == F32_EXPANDED)
+    tc_dispatch<F32_EXPANDED>(a, st);
+  else
+    tc_dispatch<F32_DIRECT>(a, st);
+}
+
+}  // namespace ds

@@ -7,6 +7,7 @@
 #include <memory>
 #include <vector>
 
+#include "ds_batch.h"
 #include "ds_device.cuh"
 #include "ds_f32.h"
 #include "ds_ops.h"
@@ -741,6 +742,137 @@ int ds_map_covar_diag(ds_context* ctx, int n_pix, const double* npixels, int n_m
   });
   ds_operator_destroy(op);
   return rc;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int ds_batch_create(ds_context* ctx, int form, int n_chunks, const int* chunk_sizes,
+                    const double* records, const ds_kernel_params* kp, int n_rhs,
+                    double inner_cutoff, ds_batch** out) {
+  if (!ctx || !out) return DS_ERR_ARG;
+  *out = nullptr;
+  auto b = std::make_unique<ds_batch>();
+  const int rc = guarded(ctx, [&] {
+    require(form == DS_FORM_SN || form == DS_FORM_W, "form must be DS_FORM_SN or DS_FORM_W");
+    require(n_chunks > 0 && chunk_sizes && records, "bad chunk arguments");
+    require(n_rhs > 0 && n_rhs <= 1024, "n_rhs must be in [1, 1024]");
+    long long total = 0;
+    for (int c = 0; c < n_chunks; ++c) {
+      require(chunk_sizes[c] > 0, "every chunk needs at least one record");
+      total += chunk_sizes[c];
+    }
+    require(total < (1ll << 31), "too many records");
+    const ds_kernel_params k = checked_kp(kp);
+    require(k.eval == DS_EVAL_EXACT,
+            "batched solves evaluate the exact kernel (eval = DS_EVAL_EXACT)");
+    DS_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    b->ctx = ctx;
+    b->form = form;
+    b->n_chunks = n_chunks;
+    b->n_rhs = n_rhs;
+    b->n_total = (int)total;
+    b->kc = make_consts(k);
+    b->inner_cut = inner_cutoff > 0.0 ? inner_cutoff : 24.0;
+    DevBuf<double> rec;
+    upload(records, (size_t)total * 5, rec, st);
+    batch_build(b.get(), rec.p, chunk_sizes);
+  });
+  if (rc != DS_OK) return rc;
+  *out = b.release();
+  return DS_OK;
+}
+
+void ds_batch_destroy(ds_batch* batch) { delete batch; }
+
+int ds_batch_get_info(ds_batch* batch, ds_batch_info* info) {
+  if (!batch || !info) return DS_ERR_ARG;
+  info->n_chunks = batch->n_chunks;
+  info->n_rhs = batch->n_rhs;
+  info->n_total = batch->n_total;
+  info->n_pad = batch->n_pad;
+  info->n_tiles = batch->n_tiles;
+  info->inner_tile_pairs = batch->pairs32_total;
+  info->outer_tile_pairs = batch->pairs64_total;
+  info->inner_evaluated = batch->eval32;
+  info->outer_evaluated = batch->eval64;
+  info->variant = batch->variant;
+  info->rhs_block = batch->rb;
+  info->graph_replays = batch->graph_replays;
+  return DS_OK;
+}
+
+int ds_batch_set_variant(ds_batch* batch, int variant, int rhs_block) {
+  if (!batch) return DS_ERR_ARG;
+  return guarded(batch->ctx, [&] {
+    if (variant == DS_BATCH_AUTO) {
+      batch_autotune(batch, true, nullptr);
+      return;
+    }
+    require(variant == DS_BATCH_CUDA_CORE || variant == DS_BATCH_TENSOR, "unknown batch variant");
+    require(batch_variant_supported(batch, variant),
+            "the tensor-core variant needs n_rhs % 16 == 0");
+    if (rhs_block > 0 && variant == DS_BATCH_CUDA_CORE) {
+      require(batch_rb_supported(batch->n_rhs, rhs_block), "unsupported RHS block");
+      batch->rb = rhs_block;
+    }
+    batch->variant = variant;
+    batch->tuned = true;
+  });
+}
+
+static int batch_solve_common(ds_batch* batch, const ds_mixed_params* mp, const double* rhs,
+                              double* x, int* iters, int* converged, int* n_updates,
+                              double* rel_resid, double* seconds, bool host) {
+  if (!batch || !mp) return DS_ERR_ARG;
+  int status = DS_OK;
+  const int rc = guarded(batch->ctx, [&] {
+    require(rhs && x, "null vector");
+    cudaStream_t st = batch->ctx->stream;
+    const size_t nr = (size_t)batch->n_total * batch->n_rhs;
+    const double* rd = rhs;
+    double* xd = x;
+    if (host) {
+      upload(rhs, nr, batch->io_a, st);
+      batch->io_b.alloc(nr);
+      rd = batch->io_a.p;
+      xd = batch->io_b.p;
+    }
+    std::vector<int> conv((size_t)batch->n_chunks * batch->n_rhs);
+    batch_solve_dev(batch, *mp, rd, xd, iters, conv.data(), n_updates, rel_resid, seconds);
+    if (converged) std::copy(conv.begin(), conv.end(), converged);
+    if (host) {
+      DS_CUDA(cudaMemcpyAsync(x, xd, nr * sizeof(double), cudaMemcpyDeviceToHost, st));
+      DS_CUDA(cudaStreamSynchronize(st));
+    }
+    for (int v : conv)
+      if (!v) status = DS_ERR_NOT_CONVERGED;
+  });
+  return rc != DS_OK ? rc : status;
+}
+
+int ds_batch_solve_mixed(ds_batch* batch, const ds_mixed_params* mp, const double* rhs,
+                         double* x, int* iters, int* converged, int* n_updates,
+                         double* rel_resid, double* seconds) {
+  return batch_solve_common(batch, mp, rhs, x, iters, converged, n_updates, rel_resid, seconds,
+                            true);
+}
+
+int ds_batch_solve_mixed_dev(ds_batch* batch, const ds_mixed_params* mp, const double* rhs,
+                             double* x, int* iters, int* converged, int* n_updates,
+                             double* rel_resid, double* seconds) {
+  return batch_solve_common(batch, mp, rhs, x, iters, converged, n_updates, rel_resid, seconds,
+                            false);
+}
+
+int ds_batch_product_f32_dev(ds_batch* batch, const double* p, double* q) {
+  if (!batch) return DS_ERR_ARG;
+  return guarded(batch->ctx, [&] {
+    require(p && q, "null vector");
+    batch_product_f32_dev(batch, p, q);
+  });
 }
 
 }  // extern "C"

@@ -198,16 +198,21 @@ void Profiler::end(cudaStream_t st, cudaEvent_t start, int kind) {
 }
 
 void Profiler::collect() {
-  for (auto& pr : pending) {
+  // The events go back to the free list before they are read, so that an
+  // error thrown from the checks never leaves an event in both lists.
+  std::vector<Pending> work;
+  work.swap(pending);
+  for (const Pending& pr : work) {
+    free_events.push_back(pr.start);
+    free_events.push_back(pr.stop);
+  }
+  for (const Pending& pr : work) {
     DS_CUDA(cudaEventSynchronize(pr.stop));
     float t = 0.f;
     DS_CUDA(cudaEventElapsedTime(&t, pr.start, pr.stop));
     ms[pr.kind] += t;
     ++launches[pr.kind];
-    free_events.push_back(pr.start);
-    free_events.push_back(pr.stop);
   }
-  pending.clear();
 }
 
 Profiler::~Profiler() {

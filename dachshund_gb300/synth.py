@@ -206,27 +206,34 @@ def small(n_sk=16, n_per=32, box_xy=12.0, seed=0, tol=1e-8) -> Workload:
                          (max(1, int(box_xy)), max(1, int(box_xy)), int(lz)), tol)
 
 
-def chunks(n_chunks=512, seed=0, sk_range=(16, 192), per_range=(64, 128), spacing=2.5):
+def chunks(n_chunks=512, seed=0, sk_range=(16, 192), per_range=(64, 128), spacing=2.5,
+           n_rhs=0):
     """Independent sub-volume chunks of uneven size (batched workload).
 
     Each chunk has a uniform-integer number of skewers and of pixels per skewer;
     its box side is spacing * sqrt(n_skewers), so the mean skewer spacing is
-    ``spacing`` Mpc/h.  Returns a list of (n, 5) Pixel arrays with GRF d."""
+    ``spacing`` Mpc/h; z_k = (k + 1/2) 2 Mpc/h.  d = GRF signal (1 Mpc/h grid,
+    trilinear) + n N(0, 1).  Returns a list of (n, 5) Pixel arrays; with
+    ``n_rhs`` > 0 also an (n_total, n_rhs) array of data vectors: the same
+    signal plus n_rhs independent noise realisations (column 0 is the d of
+    the records)."""
     rng = np.random.default_rng(seed)
-    out = []
+    out, rhs = [], []
     for _ in range(n_chunks):
         n_sk = int(rng.integers(sk_range[0], sk_range[1] + 1))
         n_per = int(rng.integers(per_range[0], per_range[1] + 1))
         side = spacing * np.sqrt(n_sk)
         pix = skewer_pixels(rng, n_sk, n_per, side)
-        box = (side, side, n_per * DZ)
-        cell = 1.0
-        shape = tuple(max(2, int(np.ceil(b / cell))) for b in box)
-        box_grid = tuple(s * cell for s in shape)
-        field = grf_field(rng, shape, cell)
-        pix[:, 4] = trilinear(field, pix[:, :3], cell) + pix[:, 3] * rng.standard_normal(len(pix))
-        del box_grid
+        shape = (max(2, int(np.ceil(side))), max(2, int(np.ceil(side))), n_per * int(DZ))
+        signal = trilinear(grf_field(rng, shape, 1.0), pix[:, :3], 1.0)
+        pix[:, 4] = signal + pix[:, 3] * rng.standard_normal(len(pix))
+        if n_rhs > 0:
+            r = signal[:, None] + pix[:, 3:4] * rng.standard_normal((len(pix), n_rhs))
+            r[:, 0] = pix[:, 4]
+            rhs.append(r)
         out.append(pix)
+    if n_rhs > 0:
+        return out, np.ascontiguousarray(np.concatenate(rhs, axis=0))
     return out
 
 

@@ -95,8 +95,10 @@ const char* ds_context_last_error(ds_context* ctx);
  * clocks, lib/timer.h:13-26).  When enabled, every launch of a pair kernel
  * (the matvec / residual / map kernels) on this context is bracketed by CUDA
  * events on the context's stream; the profile accumulates their device time,
- * their count and the tile-evaluated pairs they covered.  Disabling keeps
- * the totals until the next enable. */
+ * their count and the tile-evaluated pairs they covered (for the batched
+ * kernels of ds_batch_*: pair x right-hand-side products, and a profiled
+ * batched solve runs its iterations without the CUDA graph so that each
+ * launch can be timed).  Disabling keeps the totals until the next enable. */
 typedef struct {
   long long pair_launches;   /* pair-kernel launches timed (FP64 + FP32) */
   double pair_ms;            /* their summed device time */
@@ -264,6 +266,77 @@ int ds_solve_mixed(ds_operator* op, const ds_mixed_params* mp, double* x,
                    ds_pcg_result* res, double* residual_norms);
 int ds_solve_mixed_dev(ds_operator* op, const ds_mixed_params* mp, double* x,
                        ds_pcg_result* res, double* residual_norms);
+
+/* ---- batched chunks with several right-hand sides (no reference
+ * counterpart) -------------------------------------------------------------
+ * Many independent operators ("chunks", each the operator of
+ * ds_operator_create over its own records) with n_rhs right-hand sides each
+ * (e.g. noise realisations of the data), solved together by the
+ * mixed-precision method of ds_solve_mixed with per-(chunk, RHS) CG scalars
+ * and convergence.  Each (chunk, RHS) solve stands in for one
+ * WFVector{SN,W}::solve_pcg call (lib/wf_vector.cc:114-121, 263-274) on that
+ * chunk's pixels with that right-hand side, x0 = 0.  Exact kernel only. */
+typedef struct ds_batch ds_batch;
+
+typedef enum {
+  DS_BATCH_AUTO = -1,       /* autotuner's choice (timed on first solve) */
+  DS_BATCH_CUDA_CORE = 0,   /* FP32 FMA/MUFU matvec */
+  DS_BATCH_TENSOR = 1       /* BF16 hi/lo tensor-core S-tile x RHS matvec */
+} ds_batch_variant;
+
+typedef struct {
+  int n_chunks;
+  int n_rhs;
+  int n_total;             /* pixels over all chunks */
+  int n_pad;               /* padded (tiled) pixels */
+  int n_tiles;
+  long long inner_tile_pairs;   /* FP32 operator (inner cutoff) */
+  long long outer_tile_pairs;   /* FP64 residual operator (exact cutoff) */
+  long long inner_evaluated;    /* (i, j) pairs per product, after sub-tile
+                                   culling, FP32 operator */
+  long long outer_evaluated;    /* the same, FP64 residual operator */
+  int variant;             /* ds_batch_variant in use */
+  int rhs_block;           /* RHS per work item of the CUDA-core matvec */
+  int graph_replays;       /* iterations replayed by the last solve */
+} ds_batch_info;
+
+/* records: the chunks' records back to back (chunk c holds chunk_sizes[c]
+ * records, 5 doubles each, layout by form as for ds_operator_create);
+ * inner_cutoff as ds_mixed_params.inner_cutoff (<= 0: 24). */
+int ds_batch_create(ds_context* ctx, int form, int n_chunks,
+                    const int* chunk_sizes, const double* records,
+                    const ds_kernel_params* kp, int n_rhs, double inner_cutoff,
+                    ds_batch** out);
+void ds_batch_destroy(ds_batch* batch);
+int ds_batch_get_info(ds_batch* batch, ds_batch_info* info);
+
+/* Selects the matvec variant (ds_batch_variant) and, for the CUDA-core
+ * variant, the RHS block (1, 2, 4, 8, 16 or 32 dividing n_rhs; <= 0 keeps
+ * the current one).  DS_BATCH_AUTO re-runs the autotuner now. */
+int ds_batch_set_variant(ds_batch* batch, int variant, int rhs_block);
+
+/* rhs: n_total x n_rhs doubles (record-major, RHS fastest: the value for
+ * record k and right-hand side r at rhs[k * n_rhs + r]), in the form's
+ * convention (d for SN, w d for W).  x: same shape, solution out (times w in
+ * the W form).  Optional per-(chunk, RHS) outputs, n_chunks x n_rhs each
+ * (index c * n_rhs + r): FP32 iterations, converged flags, FP64 residual
+ * updates and the final FP64 relative residual |b - A x| / |b|.  *seconds:
+ * device time of the iteration.  Returns DS_ERR_NOT_CONVERGED when any
+ * (chunk, RHS) hit max_iter. */
+int ds_batch_solve_mixed(ds_batch* batch, const ds_mixed_params* mp,
+                         const double* rhs, double* x, int* iters,
+                         int* converged, int* n_updates, double* rel_resid,
+                         double* seconds);
+/* The same with rhs and x in device memory. */
+int ds_batch_solve_mixed_dev(ds_batch* batch, const ds_mixed_params* mp,
+                             const double* rhs, double* x, int* iters,
+                             int* converged, int* n_updates,
+                             double* rel_resid, double* seconds);
+
+/* One FP32 batched product q = A32 p over every chunk and RHS with the
+ * current variant (p, q: n_total x n_rhs, caller order, device memory); for
+ * testing the variants against each other and against the FP64 operator. */
+int ds_batch_product_f32_dev(ds_batch* batch, const double* p, double* q);
 
 /* ---- map projection ----------------------------------------------------- */
 typedef struct ds_map ds_map;
