@@ -37,6 +37,8 @@
 namespace ds {
 namespace {
 
+constexpr int STALL_ITERS = 30;  // iterations without halving the recurrence residual
+
 __device__ __forceinline__ float ex2_approx(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -209,18 +211,72 @@ __global__ void __launch_bounds__(TILE) k_batch_mv_f32(BatchF32Args a) {
   }
 }
 
-// ---- FP64 multi-RHS residual --------------------------------------------------
+// ---- FP64-accurate multi-RHS residual ---------------------------------------------
+
+// u = var_s wl x of the chunks with an update pending, as an unevaluated
+// float pair (hi = float(u), lo = float(u - hi)): about 48 significant bits.
+__global__ void k_resid_prep(int R, double var_s, const int* __restrict__ tile_chunk,
+                             const int* __restrict__ chunk_done,
+                             const int* __restrict__ chunk_update, const double* __restrict__ wl,
+                             const double* __restrict__ xv, float2* __restrict__ uu) {
+  const int t = blockIdx.x;
+  const int c = tile_chunk[t];
+  if (chunk_done[c] || !chunk_update[c]) return;
+  const size_t base = (size_t)t * TILE * R;
+  for (int k = threadIdx.x; k < TILE * R; k += blockDim.x) {
+    const double u = var_s * wl[t * TILE + k / R] * xv[base + k];
+    const float h = __double2float_rn(u);
+    uu[base + k] = make_float2(h, __double2float_rn(u - (double)h));
+  }
+}
+
+// s (0 or a normal number in [2^-100, 1]) as hi + lo floats: hi keeps the
+// top 24 significand bits of s exactly (bit operations, no conversion), lo is
+// the rounded remainder; values below 2^-100 count as 0.
+__device__ __forceinline__ void split_f64(double s, float& h, float& l) {
+  const long long bits = __double_as_longlong(s);
+  const long long hb = bits & ~((1ll << 29) - 1);
+  const int fexp = (int)((hb >> 52) & 0x7FF) - 1023 + 127;
+  const float hf = __int_as_float((int)((hb >> 29) & 0x7FFFFF) | (fexp << 23));
+  const float lf = __double2float_rn(s - __longlong_as_double(hb));
+  const bool tiny = !(s >= 7.888609052210118e-31);  // 2^-100
+  h = tiny ? 0.f : hf;
+  l = tiny ? 0.f : lf;
+}
+
+// (ah, al) += (sh + sl) (uh + ul): the product's rounding error from an FMA,
+// the cross terms in FP32, Knuth's two-sum for the high part.  About 12
+// FP32 operations; every operation rounds as written (no contraction).
+__device__ __forceinline__ void df_mac(float& ah, float& al, float sh, float sl, float uh,
+                                       float ul) {
+  const float p = __fmul_rn(sh, uh);
+  float e = __fmaf_rn(sh, uh, -p);
+  e = __fmaf_rn(sh, ul, e);
+  e = __fmaf_rn(sl, uh, e);
+  const float t = __fadd_rn(ah, p);
+  const float bp = __fsub_rn(t, ah);
+  const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  al = __fadd_rn(al, __fadd_rn(err, e));
+  ah = t;
+}
 
 // r64 = b - A x for the chunks with an update pending; work items as in the
-// FP32 matvec.  One row per thread; the exact kernel value of a pair (the
-// argument rounded as in the single-operator FP64 kernel, exp from
-// exp_neg_f64, zero at and beyond the cutoff) is generated once per item and
-// applied to RB right-hand sides.  Warp-private staging of the column
-// sub-tiles the warp's rows interact with.
+// FP32 matvec.  One row per thread.  The exact kernel value of a pair is
+// computed in FP64 once per item (the argument rounded as in the
+// single-operator FP64 kernel, exp from exp_neg_f64, zero at and beyond the
+// cutoff) and split into a float pair; the products with the RB right-hand
+// sides are accumulated as float pairs on the FP32 pipe (the FP64 pipe of
+// this part does 2 operations per clock per SM), which keeps about 44
+// significant bits, far below the 1e-8 relative residual it certifies.
+// Warp-private staging of the column sub-tiles the warp's rows interact
+// with: coordinates in FP64, the (hi, lo) u values padded so that the
+// staging stores avoid bank conflicts.
 template <int RB>
-__global__ void __launch_bounds__(TILE) k_batch_resid_f64(BatchF64Args a) {
+__global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
+  constexpr int ROWF = 2 * RB + 4;  // floats per staged column
+  extern __shared__ float4 resid_dyn[];
+  float* ustage = reinterpret_cast<float*>(resid_dyn);  // [TILE / 32][SUBTILE][ROWF]
   __shared__ double sw[TILE / 32][3][SUBTILE];
-  __shared__ double su[TILE / 32][SUBTILE * RB];
   __shared__ double tf[32];
   __shared__ int s_item;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -232,7 +288,7 @@ __global__ void __launch_bounds__(TILE) k_batch_resid_f64(BatchF64Args a) {
   double* sxw = sw[warp][0];
   double* syw = sw[warp][1];
   double* szw = sw[warp][2];
-  double* suw = su[warp];
+  float* suw = ustage + warp * SUBTILE * ROWF;
   for (;;) {
     __syncthreads();
     if (tid == 0) s_item = (int)atomicAdd(a.work, 1u);
@@ -245,9 +301,9 @@ __global__ void __launch_bounds__(TILE) k_batch_resid_f64(BatchF64Args a) {
     if (a.chunk_done[c] || !a.chunk_update[c]) continue;
     const int i = t * TILE + tid;
     const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
-    double acc[RB];
+    float ah[RB], al[RB];
 #pragma unroll
-    for (int r = 0; r < RB; ++r) acc[r] = 0.0;
+    for (int r = 0; r < RB; ++r) ah[r] = al[r] = 0.f;
     unsigned n_sub = 0;
     for (int p = a.row_ptr[t]; p < a.row_ptr[t + 1]; ++p) {
       const unsigned m = (a.mask[p] >> (4 * warp)) & 0xFu;
@@ -261,16 +317,24 @@ __global__ void __launch_bounds__(TILE) k_batch_resid_f64(BatchF64Args a) {
         sxw[lane] = a.x[j];
         syw[lane] = a.y[j];
         szw[lane] = a.z[j];
-        const double cw = kc.var_s * a.wl[j];
+        const float2* src = a.uu + (size_t)j * R + r0;
+        float2* dst = reinterpret_cast<float2*>(suw + lane * ROWF);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) suw[lane * RB + r] = cw * a.xv[(size_t)j * R + r0 + r];
+        for (int r = 0; r < RB; ++r) dst[r] = src[r];
         __syncwarp();
+#pragma unroll 1
         for (int jj = 0; jj < SUBTILE; ++jj) {
           const double dx = xi - sxw[jj], dy = yi - syw[jj], dz = zi - szw[jj];
           const double arg = fma(kc.c_perp, fma(dx, dx, dy * dy), kc.c_para * (dz * dz));
           const double g = arg < kc.exact_cut ? exp_neg_f64(arg, tf) : 0.0;
+          float sh, sl;
+          split_f64(g, sh, sl);
+          const float2* u2 = reinterpret_cast<const float2*>(suw + jj * ROWF);
 #pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] = fma(g, suw[jj * RB + r], acc[r]);
+          for (int r = 0; r < RB; ++r) {
+            const float2 u = u2[r];
+            df_mac(ah[r], al[r], sh, sl, u.x, u.y);
+          }
         }
       }
     }
@@ -280,7 +344,8 @@ __global__ void __launch_bounds__(TILE) k_batch_resid_f64(BatchF64Args a) {
 #pragma unroll
     for (int r = 0; r < RB; ++r) {
       const size_t k = (size_t)i * R + r0 + r;
-      a.r64[k] = a.b[k] - (wli * acc[r] + ei * a.xv[k]);
+      const double acc = (double)ah[r] + (double)al[r];
+      a.r64[k] = a.b[k] - (wli * acc + ei * a.xv[k]);
     }
   }
 }
@@ -389,8 +454,10 @@ __device__ __forceinline__ double chunk_sum(const double* part, int t0, int t1, 
 
 // MODE 0 (S1): alpha = r.z / p.q.
 // MODE 1 (S2): new r.z and |r|, beta.  A right-hand side whose recurrence
-//              residual fell by delta since its last update, reached tol |b|
-//              or hit the iteration cap is held (it stops iterating); once
+//              residual fell by delta since its last update, reached tol |b|,
+//              stagnated (did not halve in STALL_ITERS iterations; the update
+//              then restarts with beta = 0) or hit the iteration cap is held
+//              (it stops iterating); once
 //              every active RHS of the chunk is held the chunk takes an
 //              update.  The FP64 residual of a chunk costs about the same for
 //              one RHS as for all, so the chunk's updates stay in step and
@@ -424,7 +491,16 @@ __global__ void k_bs(BatchState s, const double* __restrict__ part) {
         const int it = ++s.iter[cr];
         s.rmax[cr] = fmax(s.rmax[cr], rn);
         s.beta[cr] = rz / s.rz_old[cr];
-        if (rn < s.delta * s.rmax[cr] || rn <= s.tol_norm_b[cr] || it >= s.max_iter)
+        if (rn < 0.5 * s.rbest[cr]) {
+          s.rbest[cr] = rn;
+          s.it_best[cr] = it;
+        }
+        // stagnation: the recurrence residual has not halved for STALL_ITERS
+        // iterations (the FP32 / BF16 operator's rounding can stall CG near
+        // the tolerance); the update restarts the recurrence from scratch
+        const int stall = it - s.it_best[cr] >= STALL_ITERS;
+        if (stall) s.stalled[cr] = 1;
+        if (rn < s.delta * s.rmax[cr] || rn <= s.tol_norm_b[cr] || it >= s.max_iter || stall)
           s.hold[cr] = 1;
         else
           any_iterating = 1;
@@ -443,15 +519,20 @@ __global__ void k_bs(BatchState s, const double* __restrict__ part) {
           s.done[cr] = 1;
         } else {
           s.rz[cr] = rz;  // rz_old keeps the r.z before the held iteration
-          s.beta[cr] = rz / s.rz_old[cr];
+          s.beta[cr] = s.stalled[cr] ? 0.0 : rz / s.rz_old[cr];
           s.rmax[cr] = rt;
+          s.rbest[cr] = rt;
+          s.it_best[cr] = s.iter[cr];
+          s.stalled[cr] = 0;
         }
       }
     } else if (MODE == 3) {
       const double rz = chunk_sum(part, t0, t1, 2 * R, r);
       const double rt = sqrt(chunk_sum(part, t0, t1, 2 * R, R + r));
       s.rz[cr] = rz;
-      s.rtrue[cr] = s.rmax[cr] = rt;
+      s.rtrue[cr] = s.rmax[cr] = s.rbest[cr] = rt;
+      s.it_best[cr] = 0;
+      s.stalled[cr] = 0;
       s.norm_b[cr] = rt;
       s.tol_norm_b[cr] = s.tol * rt;
       s.iter[cr] = 0;
@@ -570,13 +651,35 @@ void mv_launch(const BatchF32Args& a, int grid, cudaStream_t st) {
 }
 
 template <int RB>
-void resid_launch(const BatchF64Args& a, int grid, cudaStream_t st) {
-  const int items = a.n_row_tiles * (a.n_rhs / RB);
-  if (grid <= 0) grid = persistent_grid(k_batch_resid_f64<RB>, items);
-  k_batch_resid_f64<RB><<<grid, TILE, 0, st>>>(a);
+constexpr size_t resid_smem() {
+  return (size_t)(TILE / 32) * SUBTILE * (2 * RB + 4) * sizeof(float);
 }
 
-// RHS block of the FP64 residual: the largest of 32, 16, 8, 4, 2, 1 dividing R.
+template <int RB>
+void resid_launch(const BatchF64Args& a, int grid, cudaStream_t st) {
+  static bool attr = false;  // set on the first (uncaptured) launch
+  if (!attr) {
+    DS_CUDA(cudaFuncSetAttribute(k_batch_resid_f64<RB>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)resid_smem<RB>()));
+    attr = true;
+  }
+  const int items = a.n_row_tiles * (a.n_rhs / RB);
+  if (grid <= 0) {
+    static int full = 0;
+    if (!full) {
+      int per_sm = 0;
+      DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_resid_f64<RB>, TILE,
+                                                            resid_smem<RB>()));
+      full = std::max(per_sm, 1) * sm_count();
+    }
+    grid = std::max(1, std::min(items, full));
+  }
+  k_batch_resid_f64<RB><<<grid, TILE, resid_smem<RB>(), st>>>(a);
+}
+
+// RHS block of the FP64 residual: the largest of 32, 16, 8, 4, 2, 1 dividing R
+// (64 float-pair accumulators per thread would spill).
 int resid_block(int R) {
   for (int b : {32, 16, 8, 4, 2})
     if (R % b == 0) return b;
@@ -611,6 +714,9 @@ void launch_batch_mv_f32(const BatchF32Args& a, int formula, int rb, int grid, c
 }
 
 void launch_batch_resid_f64(const BatchF64Args& a, int grid, cudaStream_t st) {
+  k_resid_prep<<<a.n_row_tiles, 256, 0, st>>>(a.n_rhs, a.kc.var_s, a.tile_chunk, a.chunk_done,
+                                               a.chunk_update, a.wl, a.xv, a.uu);
+  DS_CHECK_LAUNCH();
   DS_CUDA(cudaMemsetAsync(a.work, 0, sizeof(unsigned int), st));
   switch (resid_block(a.n_rhs)) {
     case 32: resid_launch<32>(a, grid, st); break;
@@ -757,16 +863,18 @@ void batch_build(ds_batch* B, const double* d_rec, const int* sizes) {
 
   const size_t NR = (size_t)NP * B->n_rhs;
   for (auto* v : {&B->bv, &B->xv, &B->r64}) v->alloc(NR);
+  B->uu.alloc(NR);
   for (auto* v : {&B->p, &B->q, &B->rr, &B->zz, &B->xc}) v->alloc(NR);
   k_fill_f32v<<<blocks_for(NR), 256, 0, st>>>(NR, 0.f, B->p.p);  // defined p for tuning
   DS_CHECK_LAUNCH();
   B->part.alloc((size_t)T * 2 * B->n_rhs);
   const size_t CR = (size_t)C * B->n_rhs;
-  for (auto* v : {&B->s_rz, &B->s_rz_old, &B->s_alpha, &B->s_beta, &B->s_rmax, &B->s_rtrue,
+  for (auto* v : {&B->s_rz, &B->s_rz_old, &B->s_alpha, &B->s_beta, &B->s_rmax, &B->s_rbest,
+                  &B->s_rtrue,
                   &B->s_norm_b, &B->s_tol_norm_b})
     v->alloc(CR);
   for (auto* v : {&B->s_iter, &B->s_n_updates, &B->s_need, &B->s_hold, &B->s_done,
-                  &B->s_converged})
+                  &B->s_converged, &B->s_it_best, &B->s_stalled})
     v->alloc(CR);
   B->chunk_done.alloc(C);
   B->chunk_update.alloc(C);
@@ -828,6 +936,7 @@ BatchF64Args resid_args(ds_batch* B) {
   a.chunk_update = B->chunk_update.p;
   a.n_rhs = B->n_rhs;
   a.work = B->work.p + 1;
+  a.uu = B->uu.p;
   return a;
 }
 
@@ -843,6 +952,9 @@ BatchState state_args(ds_batch* B, const ds_mixed_params& mp) {
   s.alpha = B->s_alpha.p;
   s.beta = B->s_beta.p;
   s.rmax = B->s_rmax.p;
+  s.rbest = B->s_rbest.p;
+  s.it_best = B->s_it_best.p;
+  s.stalled = B->s_stalled.p;
   s.rtrue = B->s_rtrue.p;
   s.norm_b = B->s_norm_b.p;
   s.tol_norm_b = B->s_tol_norm_b.p;
@@ -1078,8 +1190,12 @@ void batch_solve_dev(ds_batch* B, const ds_mixed_params& mp, const double* rhs_d
   cudaGraphExec_t exec = nullptr;
   int active = C;
   int replays = 0;
+  // A held RHS does not count iterations while the rest of its chunk runs
+  // on, so the graph may run more than max_iter times; every active RHS
+  // reaches its cap long before this safety bound.
+  const long long it_cap = 4ll * S.max_iter + 64;
   if (B->ctx->prof.enabled) {
-    for (; it < S.max_iter + 1 && active > 0; ++it) {
+    for (; it < it_cap && active > 0; ++it) {
       issue_iteration();
       if (it % 8 == 7) {
         DS_CUDA(cudaMemcpyAsync(&active, B->active.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1105,7 +1221,7 @@ void batch_solve_dev(ds_batch* B, const ds_mixed_params& mp, const double* rhs_d
       cudaGraphDestroy(graph);
       DS_CUDA(inst);
     }
-    for (; it < S.max_iter + 1 && active > 0; ++it) {
+    for (; it < it_cap && active > 0; ++it) {
       DS_CUDA(cudaGraphLaunch(exec, st));
       ++replays;
       if (it % 8 == 7) {

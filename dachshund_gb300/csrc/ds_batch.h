@@ -58,6 +58,7 @@ struct BatchF64Args {
   const double* b;   // [pixel][n_rhs]
   const double* xv;  // [pixel][n_rhs]
   double* r64;       // [pixel][n_rhs]
+  float2* uu;        // [pixel][n_rhs]: var_s wl x as (hi, lo) floats
   const int* row_ptr;
   const int* cols;
   const unsigned short* mask;
@@ -83,6 +84,7 @@ struct BatchState {
   double* alpha;
   double* beta;
   double* rmax;
+  double* rbest;    // smallest recurrence |r| since the last halving
   double* rtrue;
   double* norm_b;
   double* tol_norm_b;
@@ -90,6 +92,8 @@ struct BatchState {
   int* n_updates;
   int* need;
   int* hold;
+  int* it_best;     // iteration of rbest
+  int* stalled;     // the pending update was triggered by stagnation
   int* done;
   int* converged;
   int* chunk_done;
@@ -130,10 +134,12 @@ struct ds_batch {
   ds::DevBuf<double> wl, e, pdiag;
   ds::DevBuf<float> rowf, colw, ediag, pd32;
   ds::DevBuf<double> bv, xv, r64;
+  ds::DevBuf<float2> uu;
   ds::DevBuf<float> p, q, rr, zz, xc;
   ds::DevBuf<double> part;
-  ds::DevBuf<double> s_rz, s_rz_old, s_alpha, s_beta, s_rmax, s_rtrue, s_norm_b, s_tol_norm_b;
-  ds::DevBuf<int> s_iter, s_n_updates, s_need, s_hold, s_done, s_converged;
+  ds::DevBuf<double> s_rz, s_rz_old, s_alpha, s_beta, s_rmax, s_rbest, s_rtrue, s_norm_b,
+      s_tol_norm_b;
+  ds::DevBuf<int> s_iter, s_n_updates, s_need, s_hold, s_done, s_converged, s_it_best, s_stalled;
   ds::DevBuf<int> chunk_done, chunk_update, active;
   ds::DevBuf<unsigned int> work;  // work-queue counters
   ds::DevBuf<unsigned short> panel;  // tensor-core variant: BF16 u panels (lazy)
