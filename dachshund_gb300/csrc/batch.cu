@@ -827,10 +827,21 @@ void batch_build(ds_batch* B, const double* d_rec, const int* sizes) {
       for (unsigned short m : mk) evaluated += (long long)__builtin_popcount(m) * SUBTILE * SUBTILE;
       off += src[c].n_pairs;
     }
-    std::vector<int> order(T);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return counts[a] > counts[b]; });
+    // Launch order: chunks by decreasing work (the tail of the persistent
+    // launch is short), and within a chunk its tiles in order, so that the
+    // CTAs running at one time share the chunk's column tiles in L2 (every
+    // column tile of a chunk is read by most of its row tiles).
+    std::vector<long long> work(C, 0);
+    for (int c = 0; c < C; ++c)
+      for (int t = tile0[c]; t < tile0[c + 1]; ++t) work[c] += counts[t];
+    std::vector<int> corder(C);
+    std::iota(corder.begin(), corder.end(), 0);
+    std::stable_sort(corder.begin(), corder.end(),
+                     [&](int a, int b) { return work[a] > work[b]; });
+    std::vector<int> order;
+    order.reserve(T);
+    for (int c : corder)
+      for (int t = tile0[c]; t < tile0[c + 1]; ++t) order.push_back(t);
     dst.row_order.alloc(T);
     DS_CUDA(cudaMemcpyAsync(dst.row_order.p, order.data(), T * sizeof(int),
                             cudaMemcpyHostToDevice, st));

@@ -9,23 +9,24 @@
 // significant bits per term with an FP32 accumulator: an operator error near
 // 1e-5 relative, which the FP64 reliable updates of the solver remove.
 //
-// Per CTA (256 threads, one CTA per SM, persistent over (row tile, RHS
-// block) items):
-//   * every thread generates S for one row and 64 columns of the current
-//     column tile (EXPANDED exponent: 3 FFMA + ex2 per pair; DIRECT when the
-//     tiles are too wide for it: 3 FADD + 3 FMUL/FFMA + ex2), splits it into
-//     BF16 hi / lo and stores both into shared memory in the canonical
-//     K-major no-swizzle layout (8 x 16-byte core matrices); column
-//     sub-tiles outside the cutoff of the warp's row sub-tile are zero;
-//   * the u panel of the column tile (pre-packed in HBM by k_pack_panels in
-//     the same core-matrix layout) arrives by one cp.async.bulk copy on an
-//     mbarrier;
-//   * one thread issues the MMAs (K steps whose column sub-tile interacts
-//     with no row sub-tile are skipped) and commits them to an mbarrier;
-//   * S and the panels are double-buffered, so the generation of tile k + 1
-//     overlaps the MMAs of tile k;
-//   * the epilogue reads D from tensor memory (tcgen05.ld), forms
-//     q = rowf D + ediag p and the tile's p.q per RHS.
+// Per CTA (one per SM, 10 warps, persistent over (row tile, RHS block)
+// items), warp-specialized with mbarrier hand-offs:
+//   * warps 0-7 generate S for the current column tile, two threads per row
+//     and 64 columns each (EXPANDED exponent: 3 FFMA + ex2 per pair; DIRECT
+//     when the tiles are too wide for it), split it into BF16 hi / lo and
+//     store both into shared memory in the canonical K-major no-swizzle
+//     layout (8 x 16-byte core matrices); column sub-tiles outside the cutoff
+//     of the warp's row sub-tile are zero.  After an item's last tile they
+//     read D back (tcgen05.ld), form q = rowf D + ediag p and the tile's p.q
+//     per RHS;
+//   * warp 8 stages the column coordinates of each column tile and issues
+//     the cp.async.bulk copy of its u panel (pre-packed in HBM by
+//     k_pack_panels in the same core-matrix layout);
+//   * lane 0 of warp 9 issues the MMAs (K steps whose column sub-tile
+//     interacts with no row sub-tile are skipped) and commits them;
+//   * S tiles, panels and coordinates are double-buffered and the
+//     accumulator has two TMEM buffers, so generation of tile g + 1 overlaps
+//     the MMAs of tile g and an item's epilogue overlaps the next item.
 // Every mbarrier wait is bounded: on a time-out the kernel records an error
 // code, waits (bounded) for its own MMAs and copies, frees its tensor memory
 // and returns.
@@ -39,7 +40,8 @@
 namespace ds {
 namespace {
 
-constexpr int TC_THREADS = 256;
+constexpr int GEN_WARPS = 8;                       // S generation + epilogue
+constexpr int TC_THREADS = (GEN_WARPS + 2) * 32;   // + producer warp + MMA warp
 constexpr uint32_t WAIT_TRIES = 1u << 24;  // x (poll + 64 ns sleep) ~ 1-2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -227,15 +229,17 @@ constexpr uint32_t CORE_SBO = 128;
 
 template <int NB>
 struct TcSmem {
-  __nv_bfloat16 s[2][2][S_ELEMS];     // [buffer][hi, lo]
-  __nv_bfloat16 u[2][2 * NB * TILE];  // [buffer] hi then lo
-  float4 sc[TILE];                    // column coordinates of the current tile
-  uint64_t full[2];                   // u panel landed
-  uint64_t mma_done[2];               // MMAs reading buffer b completed
+  __nv_bfloat16 s[2][2][S_ELEMS];     // [buffer][hi, lo] generated S tiles
+  __nv_bfloat16 u[2][2 * NB * TILE];  // [buffer] u panel, hi then lo
+  float4 sc[2][TILE];                 // [buffer] column coordinates of the tile
+  float red[2][GEN_WARPS][32];        // [D buffer][warp] per-column p.q sums
+  uint64_t in_full[2];   // sc staged + u panel landed      (1 arrive + tx bytes)
+  uint64_t s_full[2];    // S tile written                  (GEN_WARPS arrives)
+  uint64_t mma_done[2];  // MMAs reading buffer b completed (tcgen05.commit)
+  uint64_t d_full[2];    // all MMAs of an item completed   (tcgen05.commit)
+  uint64_t d_empty[2];   // D read back by the epilogue     (GEN_WARPS arrives)
   uint32_t tmem_addr;
-  int item;
   int abort;
-  int any_mma;
 };
 
 template <int NB>
@@ -243,23 +247,75 @@ constexpr size_t tc_smem_bytes() {
   return sizeof(TcSmem<NB>) + 1024;  // + alignment slack
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void gen_bar_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(GEN_WARPS * 32) : "memory");
+}
+
+// A bounded wait that records a time-out: error code, CTA abort flag.
+template <int NB>
+__device__ __forceinline__ bool wait_or_abort(TcSmem<NB>& sm, uint64_t* bar, uint32_t parity,
+                                              int* err, int code) {
+  if (mbar_wait(bar, parity)) return true;
+  atomicExch(err, code);
+  *(volatile int*)&sm.abort = 1;
+  return false;
+}
+
+__device__ __forceinline__ bool aborted(const int* flag) { return *(const volatile int*)flag != 0; }
+
+// Column sums over the warp's 32 rows of v[0..HN): afterwards lane l < HN
+// holds the sum of column l (recursive halving: 31 shuffles for HN = 32).
+template <int HN>
+__device__ __forceinline__ float warp_column_sums(float (&v)[HN], int lane) {
+#pragma unroll
+  for (int s = HN / 2; s >= 1; s >>= 1) {
+    const bool upper = (lane & s) != 0;
+#pragma unroll
+    for (int j = 0; j < s; ++j) {
+      const float send = upper ? v[j] : v[j + s];
+      const float keep = upper ? v[j + s] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  float r = v[0];
+#pragma unroll
+  for (int s = HN; s < 32; s <<= 1) r += __shfl_xor_sync(0xffffffffu, r, s);
+  return r;
+}
+
+// Warp roles: warps 0..7 generate S (two threads per row, 64 columns each)
+// and run the epilogue; warp 8 stages the column coordinates and issues the
+// u-panel copy of each column tile; lane 0 of warp 9 issues the MMAs.  The
+// hand-offs are mbarriers, so no role waits for another except for data:
+// generation of tile g + 1 overlaps the MMAs of tile g, and the epilogue of
+// an item (its accumulator in one of two TMEM buffers) overlaps the MMAs of
+// the next.  Items are dealt round-robin (item = CTA + k * grid), in the
+// launch order (chunks by decreasing work), so every role walks the same
+// sequence without a queue.
 template <int NB, int FORMULA>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
   static_assert(NB == 16 || NB == 32 || NB == 64, "RHS block");
-  constexpr uint32_t TMEM_COLS = NB < 32 ? 32 : NB;
+  constexpr uint32_t TMEM_COLS = 2 * NB < 32 ? 32 : 2 * NB;
   constexpr uint32_t PANEL_BYTES = 2u * NB * TILE * 2u;
   constexpr uint32_t U_LBO = (NB / 8) * 128;
   constexpr uint32_t IDESC = idesc_bf16(128, NB);
+  constexpr int HN = NB / 2;
   extern __shared__ uint8_t smem_raw[];
   TcSmem<NB>& sm = *reinterpret_cast<TcSmem<NB>*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int row = tid & (TILE - 1), half = tid >> 7, rs = row >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    mbar_init(&sm.full[0], 1);
-    mbar_init(&sm.full[1], 1);
-    mbar_init(&sm.mma_done[0], 1);
-    mbar_init(&sm.mma_done[1], 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.in_full[b], 1);
+      mbar_init(&sm.s_full[b], GEN_WARPS);
+      mbar_init(&sm.mma_done[b], 1);
+      mbar_init(&sm.d_full[b], 1);
+      mbar_init(&sm.d_empty[b], GEN_WARPS);
+    }
     sm.abort = 0;
     mbar_fence_init();
   }
@@ -271,56 +327,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
   const int R = a.n_rhs;
   const int nblk = R / NB;
   const int n_items = a.n_row_tiles * nblk;
-  uint32_t g = 0;           // pipeline position (column tiles processed by this CTA)
-  int last_copy = -1;       // g of the last u-panel copy issued (thread 0)
-  int last_commit = -1;     // g of the last MMA commit (thread 0)
-  for (;;) {
-    __syncthreads();
-    if (tid == 0) sm.item = (int)atomicAdd(a.work, 1u);
-    __syncthreads();
-    const int item = sm.item;
-    if (item >= n_items || sm.abort) break;
-    const int t = a.row_order[item / nblk];
-    const int rb = item % nblk;
-    if (a.chunk_done[a.tile_chunk[t]]) continue;
-    const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
-    const int i = t * TILE + row;
-    const float4 me = a.xi[i];
-    const float4 ot = a.orig[t];
-    const __nv_bfloat16* panels = reinterpret_cast<const __nv_bfloat16*>(a.panel);
-    if (tid == 0) {
-      sm.any_mma = 0;
-      const int ct0 = a.cols[p0];
-      mbar_expect_tx(&sm.full[g & 1], PANEL_BYTES);
-      bulk_g2s(sm.u[g & 1], panels + ((size_t)ct0 * nblk + rb) * (2 * NB * TILE), PANEL_BYTES,
-               &sm.full[g & 1]);
-      last_copy = (int)g;
-    }
-    // register prefetch of the column coordinates (threads of half 0 stage them)
-    int ct = a.cols[p0];
-    float4 cq = half == 0 ? a.xi[ct * TILE + row] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 co = a.orig[ct];
-    uint32_t accumulate = 0;  // thread 0: the item's first MMA overwrites D
-    for (int p = p0; p < p1; ++p, ++g) {
-      const unsigned m = a.mask[p];
-      if (half == 0) {
-        const float zx = cq.x - (ot.x - co.x), zy = cq.y - (ot.y - co.y);
-        const float zz = cq.z - (ot.z - co.z);
-        if (FORMULA == F32_EXPANDED)
-          sm.sc[row] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -fmaf(zx, zx, fmaf(zy, zy, zz * zz)));
-        else
-          sm.sc[row] = make_float4(zx, zy, zz, 0.f);
-      }
-      if (p + 1 < p1) {
-        ct = a.cols[p + 1];
-        if (half == 0) cq = a.xi[ct * TILE + row];
-        co = a.orig[ct];
-      }
-      __syncthreads();  // sc staged; S[g & 1] free (MMAs of g - 2 waited below)
-      if (sm.abort) break;
-      {
-        __nv_bfloat16* shi = sm.s[g & 1][0];
-        __nv_bfloat16* slo = sm.s[g & 1][1];
+  const __nv_bfloat16* panels = reinterpret_cast<const __nv_bfloat16*>(a.panel);
+  int last_g = -1;  // last tile of this role's walk (MMA commit / panel copy in flight)
+
+  if (warp < GEN_WARPS) {
+    // ---- generation and epilogue ------------------------------------------
+    const int row = tid & (TILE - 1), half = tid >> 7, rs = row >> 5;
+    uint32_t g = 0, k = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+      const int t = a.row_order[item / nblk];
+      const int rb = item % nblk;
+      if (a.chunk_done[a.tile_chunk[t]]) continue;
+      const int i = t * TILE + row;
+      const float4 me = a.xi[i];
+      const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
+      bool any = false;
+      unsigned m = a.mask[p0];
+      for (int p = p0; p < p1; ++p, ++g) {
+        const uint32_t b = g & 1;
+        const unsigned mnext = p + 1 < p1 ? a.mask[p + 1] : 0u;
+        any |= m != 0u;
+        if (!wait_or_abort(sm, &sm.in_full[b], (g >> 1) & 1u, a.err, 11)) break;
+        if (g >= 2 && !wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 12)) break;
+        __nv_bfloat16* shi = sm.s[b][0];
+        __nv_bfloat16* slo = sm.s[b][1];
+        const float4* sc = sm.sc[b];
         const int rg = row >> 3, ir = row & 7;
 #pragma unroll
         for (int c2 = 0; c2 < 2; ++c2) {
@@ -334,7 +365,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
               float s8[8];
 #pragma unroll
               for (int e = 0; e < 8; ++e) {
-                const float4 c4 = sm.sc[kg * 8 + e];
+                const float4 c4 = sc[kg * 8 + e];
                 float t2;
                 if (FORMULA == F32_EXPANDED) {
                   t2 = fmaf(me.x, c4.x, c4.w);
@@ -356,105 +387,165 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
             *reinterpret_cast<uint4*>(slo + off) = vl;
           }
         }
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.s_full[b]);
+        m = mnext;
       }
-      fence_async_smem();
-      __syncthreads();  // S[g & 1] written
-      if (tid == 0) {
-        if (!mbar_wait(&sm.full[g & 1], (g >> 1) & 1u)) {
-          atomicExch(a.err, 1);
-          sm.abort = 1;
-        } else {
-          tc_fence_after();
-          const uint32_t sa = smem_u32(sm.s[g & 1][0]), sl = smem_u32(sm.s[g & 1][1]);
-          const uint32_t ua = smem_u32(sm.u[g & 1]), ul = ua + NB * TILE * 2;
-#pragma unroll 1
-          for (int ks = 0; ks < TILE / 16; ++ks) {
-            if (!((m >> (ks >> 1)) & 0x1111u)) continue;  // no row sub-tile reaches it
-            const uint32_t aoff = ks * 2 * S_LBO, boff = ks * 2 * U_LBO;
-            const uint64_t ahi = sdesc(sa + aoff, S_LBO, CORE_SBO);
-            const uint64_t alo = sdesc(sl + aoff, S_LBO, CORE_SBO);
-            const uint64_t bhi = sdesc(ua + boff, U_LBO, CORE_SBO);
-            const uint64_t blo = sdesc(ul + boff, U_LBO, CORE_SBO);
-            mma_bf16(tmem, ahi, bhi, IDESC, accumulate);
-            mma_bf16(tmem, ahi, blo, IDESC, 1u);
-            mma_bf16(tmem, alo, bhi, IDESC, 1u);
-            accumulate = 1u;
-            sm.any_mma = 1;
-          }
-          mma_commit(&sm.mma_done[g & 1]);
-          last_commit = (int)g;
-          // the next tile's panel goes to the other buffer once the MMAs of
-          // tile g - 1 (its last reader) are done
-          if (p + 1 < p1) {
-            if (g >= 1 && !mbar_wait(&sm.mma_done[(g - 1) & 1], ((g - 1) >> 1) & 1u)) {
-              atomicExch(a.err, 2);
-              sm.abort = 1;
-            } else {
-              mbar_expect_tx(&sm.full[(g + 1) & 1], PANEL_BYTES);
-              bulk_g2s(sm.u[(g + 1) & 1],
-                       panels + ((size_t)a.cols[p + 1] * nblk + rb) * (2 * NB * TILE),
-                       PANEL_BYTES, &sm.full[(g + 1) & 1]);
-              last_copy = (int)g + 1;
-            }
-          }
+      if (aborted(&sm.abort)) break;
+      // epilogue: D of this item in TMEM buffer db; the row's p values and
+      // coefficients are loaded before the wait
+      const uint32_t db = k & 1;
+      const float rf = a.rowf[i], ed = a.ediag[i];
+      const int r0 = rb * NB + half * HN;
+      const float4* pv4 = reinterpret_cast<const float4*>(a.p + (size_t)i * R + r0);
+      float4* qv4 = reinterpret_cast<float4*>(a.q + (size_t)i * R + r0);
+      float4 pvr[HN / 4];
+#pragma unroll
+      for (int k4 = 0; k4 < HN / 4; ++k4) pvr[k4] = pv4[k4];
+      if (!wait_or_abort(sm, &sm.d_full[db], (k >> 1) & 1u, a.err, 13)) break;
+      tc_fence_after();
+      float d[HN];
+      tmem_ld<HN>(tmem + ((uint32_t)(32 * rs) << 16) + db * NB + (uint32_t)(half * HN), d);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.d_empty[db]);
+      if (!any) {
+#pragma unroll
+        for (int j = 0; j < HN; ++j) d[j] = 0.f;
+      }
+#pragma unroll
+      for (int k4 = 0; k4 < HN / 4; ++k4) {
+        const float4 pv = pvr[k4];
+        float4 qv;
+        qv.x = fmaf(rf, d[4 * k4 + 0], ed * pv.x);
+        qv.y = fmaf(rf, d[4 * k4 + 1], ed * pv.y);
+        qv.z = fmaf(rf, d[4 * k4 + 2], ed * pv.z);
+        qv.w = fmaf(rf, d[4 * k4 + 3], ed * pv.w);
+        qv4[k4] = qv;
+        d[4 * k4 + 0] = pv.x * qv.x;  // d now holds the p.q products
+        d[4 * k4 + 1] = pv.y * qv.y;
+        d[4 * k4 + 2] = pv.z * qv.z;
+        d[4 * k4 + 3] = pv.w * qv.w;
+      }
+      const float cs = warp_column_sums<HN>(d, lane);
+      if (lane < HN) sm.red[db][warp][lane] = cs;
+      gen_bar_sync();
+      if (tid < NB) {
+        const int h = tid / HN, j = tid % HN;
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) s += (double)sm.red[db][h * 4 + w][j];
+        a.part[(size_t)t * R + rb * NB + tid] = s;
+      }
+      if (a.prof_pairs && tid == 0) {
+        unsigned long long n_sub = 0;
+        for (int p = p0; p < p1; ++p) n_sub += __popc(a.mask[p]);
+        atomicAdd(a.prof_pairs, n_sub * SUBTILE * SUBTILE * NB);
+      }
+      ++k;
+    }
+  } else if (warp == GEN_WARPS) {
+    // ---- producer: column coordinates and u panels ------------------------------
+    // The next tile's indices and coordinates are loaded into registers
+    // before waiting for its buffer, so their latency overlaps that wait.
+    uint32_t g = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+      const int t = a.row_order[item / nblk];
+      const int rb = item % nblk;
+      if (a.chunk_done[a.tile_chunk[t]]) continue;
+      const float4 ot = a.orig[t];
+      const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
+      int ct = p0 < p1 ? a.cols[p0] : 0;
+      float4 co = a.orig[ct];
+      float4 cq[TILE / 32];
+#pragma unroll
+      for (int q = 0; q < TILE / 32; ++q) cq[q] = a.xi[ct * TILE + lane + 32 * q];
+      for (int p = p0; p < p1; ++p, ++g) {
+        const uint32_t b = g & 1;
+        if (aborted(&sm.abort)) break;
+        // prefetch of tile p + 1
+        const int ct_n = p + 1 < p1 ? a.cols[p + 1] : ct;
+        const float4 co_n = a.orig[ct_n];
+        float4 cq_n[TILE / 32];
+#pragma unroll
+        for (int q = 0; q < TILE / 32; ++q) cq_n[q] = a.xi[ct_n * TILE + lane + 32 * q];
+        if (g >= 2 && !wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 21)) break;
+#pragma unroll
+        for (int q = 0; q < TILE / 32; ++q) {
+          const int col = lane + 32 * q;
+          const float zx = cq[q].x - (ot.x - co.x), zy = cq[q].y - (ot.y - co.y);
+          const float zz = cq[q].z - (ot.z - co.z);
+          if (FORMULA == F32_EXPANDED)
+            sm.sc[b][col] =
+                make_float4(2.f * zx, 2.f * zy, 2.f * zz, -fmaf(zx, zx, fmaf(zy, zy, zz * zz)));
+          else
+            sm.sc[b][col] = make_float4(zx, zy, zz, 0.f);
         }
+        __syncwarp();
+        if (lane == 0) {
+          mbar_expect_tx(&sm.in_full[b], PANEL_BYTES);
+          bulk_g2s(sm.u[b], panels + ((size_t)ct * nblk + rb) * (2 * NB * TILE), PANEL_BYTES,
+                   &sm.in_full[b]);
+        }
+        last_g = (int)g;
+        ct = ct_n;
+        co = co_n;
+#pragma unroll
+        for (int q = 0; q < TILE / 32; ++q) cq[q] = cq_n[q];
       }
+      if (aborted(&sm.abort)) break;
     }
-    // epilogue: all MMAs of the item done (the commit of the last tile
-    // tracks every earlier one)
-    if (tid == 0 && !sm.abort && !mbar_wait(&sm.mma_done[(g - 1) & 1], ((g - 1) >> 1) & 1u)) {
-      atomicExch(a.err, 3);
-      sm.abort = 1;
-    }
-    __syncthreads();
-    if (sm.abort) break;
-    tc_fence_after();
-    constexpr int HN = NB / 2;
-    float d[HN];
-    tmem_ld<HN>(tmem + ((uint32_t)(32 * rs) << 16) + (uint32_t)(half * HN), d);
-    if (!sm.any_mma) {
-#pragma unroll
-      for (int k = 0; k < HN; ++k) d[k] = 0.f;
-    }
-    tc_fence_before();
-    const float rf = a.rowf[i], ed = a.ediag[i];
-    const int r0 = rb * NB + half * HN;
-    float* red = reinterpret_cast<float*>(sm.s[0][0]);  // [TILE][NB] p.q products
-    const float4* pv4 = reinterpret_cast<const float4*>(a.p + (size_t)i * R + r0);
-    float4* qv4 = reinterpret_cast<float4*>(a.q + (size_t)i * R + r0);
-#pragma unroll
-    for (int k4 = 0; k4 < HN / 4; ++k4) {
-      const float4 pv = pv4[k4];
-      float4 qv;
-      qv.x = fmaf(rf, d[4 * k4 + 0], ed * pv.x);
-      qv.y = fmaf(rf, d[4 * k4 + 1], ed * pv.y);
-      qv.z = fmaf(rf, d[4 * k4 + 2], ed * pv.z);
-      qv.w = fmaf(rf, d[4 * k4 + 3], ed * pv.w);
-      qv4[k4] = qv;
-      float* rr = red + row * NB + half * HN + 4 * k4;
-      rr[0] = pv.x * qv.x;
-      rr[1] = pv.y * qv.y;
-      rr[2] = pv.z * qv.z;
-      rr[3] = pv.w * qv.w;
-    }
-    __syncthreads();
-    if (tid < NB) {
-      double s = 0.0;
-      for (int k = 0; k < TILE; ++k) s += (double)red[k * NB + tid];
-      a.part[(size_t)t * R + rb * NB + tid] = s;
-    }
-    if (a.prof_pairs && tid == 0) {
-      unsigned long long n_sub = 0;
-      for (int p = p0; p < p1; ++p) n_sub += __popc(a.mask[p]);
-      atomicAdd(a.prof_pairs, n_sub * SUBTILE * SUBTILE * NB);
+  } else if (lane == 0) {
+    // ---- MMA issue ------------------------------------------------------------
+    uint32_t g = 0, k = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+      const int t = a.row_order[item / nblk];
+      if (a.chunk_done[a.tile_chunk[t]]) continue;
+      const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
+      const uint32_t db = k & 1;
+      if (k >= 2 && !wait_or_abort(sm, &sm.d_empty[db], ((k >> 1) - 1) & 1u, a.err, 31)) break;
+      tc_fence_after();
+      const uint32_t dt = tmem + db * NB;
+      uint32_t accumulate = 0;
+      bool ok = true;
+      for (int p = p0; p < p1; ++p, ++g) {
+        const uint32_t b = g & 1;
+        if (!wait_or_abort(sm, &sm.in_full[b], (g >> 1) & 1u, a.err, 32) ||
+            !wait_or_abort(sm, &sm.s_full[b], (g >> 1) & 1u, a.err, 33)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const unsigned m = a.mask[p];
+        const uint32_t sa = smem_u32(sm.s[b][0]), sl = smem_u32(sm.s[b][1]);
+        const uint32_t ua = smem_u32(sm.u[b]), ul = ua + NB * TILE * 2;
+#pragma unroll 1
+        for (int ks = 0; ks < TILE / 16; ++ks) {
+          if (!((m >> (ks >> 1)) & 0x1111u)) continue;  // no row sub-tile reaches it
+          const uint32_t aoff = ks * 2 * S_LBO, boff = ks * 2 * U_LBO;
+          const uint64_t ahi = sdesc(sa + aoff, S_LBO, CORE_SBO);
+          const uint64_t alo = sdesc(sl + aoff, S_LBO, CORE_SBO);
+          const uint64_t bhi = sdesc(ua + boff, U_LBO, CORE_SBO);
+          const uint64_t blo = sdesc(ul + boff, U_LBO, CORE_SBO);
+          mma_bf16(dt, ahi, bhi, IDESC, accumulate);
+          mma_bf16(dt, ahi, blo, IDESC, 1u);
+          mma_bf16(dt, alo, bhi, IDESC, 1u);
+          accumulate = 1u;
+        }
+        mma_commit(&sm.mma_done[b]);
+        last_g = (int)g;
+      }
+      if (!ok) break;
+      mma_commit(&sm.d_full[db]);
+      ++k;
     }
   }
-  // teardown: after a time-out, wait (bounded) for this CTA's own MMAs and
-  // copies in flight before the tensor memory is freed
-  __syncthreads();
-  if (tid == 0 && sm.abort) {
-    if (last_commit >= 0) mbar_wait(&sm.mma_done[last_commit & 1], (last_commit >> 1) & 1);
-    if (last_copy >= 0) mbar_wait(&sm.full[last_copy & 1], (last_copy >> 1) & 1);
+  // teardown: after a time-out, wait (bounded) for this role's MMAs or copy
+  // in flight before the tensor memory is freed
+  if (aborted(&sm.abort) && last_g >= 0 && lane == 0) {
+    if (warp == GEN_WARPS) mbar_wait(&sm.in_full[last_g & 1], (last_g >> 1) & 1u);
+    if (warp == GEN_WARPS + 1) mbar_wait(&sm.mma_done[last_g & 1], (last_g >> 1) & 1u);
   }
   tc_fence_before();
   __syncthreads();
@@ -513,7 +604,6 @@ void tc_launch(const BatchF32Args& a, cudaStream_t st) {
   }
   const int items = a.n_row_tiles * (a.n_rhs / NB);
   const int grid = std::max(1, std::min(items, sms));
-  DS_CUDA(cudaMemsetAsync(a.work, 0, sizeof(unsigned int), st));
   k_batch_mv_tc<NB, FORMULA><<<grid, TC_THREADS, tc_smem_bytes<NB>(), st>>>(a);
   DS_CHECK_LAUNCH();
 }
