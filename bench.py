@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config3", choices=["config2", "config3"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-chunks (512 chunks x 64 RHS) measurement")
     ap.add_argument("--cpu-sample-s", type=float, default=6.0,
                     help="seconds of CPU work per baseline sample")
     return ap.parse_args()
@@ -191,6 +193,103 @@ def run_reference(args, rank, world):
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def measured_peaks():
+    """The machine's measured HBM copy bandwidth and cuBLAS bf16 rate, if present."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_batched(ctx, n_chunks=512, n_rhs=64, seed=0, plain_samples=6):
+    """Batched uneven chunks: n_chunks independent sub-volumes (16-192 skewers x
+    64-128 pixels, box side 2.5 sqrt(n_skewers) Mpc/h, GRF signal), each with
+    n_rhs noise realisations, solved together to 1e-8 per (chunk, RHS) by the
+    batched mixed-precision solver (autotuned matvec variant), timed with CUDA
+    events.  Beside it: plain FP64 GPU PCG (the exact-kernel single-operator
+    solve) on a few sampled (chunk, RHS) systems, extrapolated to all of them
+    by pixel count."""
+    import numpy as np
+    import torch
+
+    from dachshund_gb300 import (BatchSolver, MixedParams, PCGParams, SignalCovarParams,
+                                 WFVectorW, pixel_to_wpixel, synth)
+
+    sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
+    pixes, rhs = synth.chunks(n_chunks, seed, n_rhs=n_rhs)
+    noise = np.concatenate([p[:, 3] for p in pixes])
+    recs = [pixel_to_wpixel(p) for p in pixes]
+    b = np.ascontiguousarray(rhs / noise[:, None])
+    t0 = time.perf_counter()
+    bs = BatchSolver(ctx, "w", recs, sp, n_rhs=n_rhs)
+    t_create = time.perf_counter() - t0
+    bs.set_variant("auto")
+    info = bs.info()
+    bd = torch.tensor(b, device="cuda")
+    xd = torch.zeros_like(bd)
+    mp = MixedParams(max_iter=3000, tol=1e-8)
+    bs.solve_mixed_dev(bd, xd, mp)  # warm-up
+    launches0 = ctx.profile()["kernel_launches"]
+    res = bs.solve_mixed_dev(bd, xd, mp)
+    launches = ctx.profile()["kernel_launches"] - launches0
+    ctx.set_profiling(True)
+    resp = bs.solve_mixed_dev(bd, xd, mp)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    mv_ms = prof["f32_ms"] / max(prof["f32_launches"], 1)
+    mv_flops = 2.0 * prof["f32_evaluated"] / (prof["f32_ms"] * 1e-3) if prof["f32_ms"] else None
+    # end to end through the host API (records already in the batch; rhs in,
+    # solutions and per-(chunk, RHS) results out)
+    t0 = time.perf_counter()
+    xh, reh = bs.solve_mixed(b, mp)
+    e2e = time.perf_counter() - t0
+    # plain FP64 GPU PCG on sampled (chunk, RHS) systems
+    rng = np.random.default_rng(1)
+    picks = rng.choice(n_chunks, size=plain_samples, replace=False)
+    offs = bs.offsets
+    t_sum, n_sum, it_sum, errs = 0.0, 0, 0, []
+    for c in picks:
+        r = int(rng.integers(n_rhs))
+        rec = recs[c].copy()
+        rec[:, 4] = b[offs[c]:offs[c + 1], r]
+        op = WFVectorW(ctx, rec, sp)
+        xp = torch.zeros(rec.shape[0], dtype=torch.float64, device="cuda")
+        rp = op.solve_pcg_dev(PCGParams(3000, 50, 1e-8), xp)
+        t_sum += rp.seconds
+        n_sum += rec.shape[0]
+        it_sum += rp.num_iters
+        xb = xh[offs[c]:offs[c + 1], r]
+        xpn = xp.cpu().numpy()
+        errs.append(float(np.max(np.abs(xb - xpn)) / np.max(np.abs(xpn))))
+        op.close()
+    n_solves = n_chunks * n_rhs
+    plain_est = t_sum / n_sum * bs.n_total * n_rhs
+    bs.close()
+    return {
+        "workload": (f"{n_chunks} chunks x {n_rhs} RHS (16-192 skewers x 64-128 px, "
+                     f"{bs.n_total} px, box side 2.5 sqrt(n_sk) Mpc/h, GRF + noise realisations)"),
+        "solves": n_solves, "value": res.seconds, "unit": "s",
+        "ms_per_solve": res.seconds / n_solves * 1e3,
+        "create_s": t_create, "e2e_s": e2e,
+        "e2e_h2d_bytes": int(b.nbytes), "e2e_d2h_bytes": int(xh.nbytes + reh.iters.nbytes * 4),
+        "iters_max": int(res.iters.max()), "iters_mean": float(res.iters.mean()),
+        "fp64_updates_max": int(res.n_updates.max()),
+        "all_converged": bool(res.converged.all()),
+        "max_rel_residual": float(res.rel_resid.max()),
+        "variant": {0: "cuda_core", 1: "tensor (tcgen05 BF16 hi/lo)"}.get(info["variant"]),
+        "matvec_ms": mv_ms, "matvec_algorithmic_tflops": mv_flops / 1e12 if mv_flops else None,
+        "matvec_tensor_frac_of_bf16_peak": None,
+        "fp64_residual_ms_per_solve": prof["f64_ms"],
+        "graph_launches_per_solve": launches,
+        "plain_fp64": {"sampled_solves": plain_samples, "sample_s": t_sum,
+                       "iters_mean": it_sum / plain_samples,
+                       "extrapolated_s": plain_est, "basis": "sample time per pixel x all pixels x RHS"},
+        "speedup_vs_plain": plain_est / res.seconds,
+        "x_err_vs_plain_fp64_max": max(errs),
+    }
 
 
 def run_ours(args, rank, world, local):
@@ -356,6 +455,13 @@ def run_ours(args, rank, world, local):
 
     base = cpu_baseline(w, plain["iters"] if plain else REF_ITERS[w.name], args.cpu_sample_s) \
         if rank == 0 else None
+    batched = None if args.no_batched else run_batched(ctx)
+    if batched and batched["matvec_algorithmic_tflops"] and batched["variant"].startswith("tensor"):
+        peak = measured_peaks().get("bf16_tflops")
+        if peak:
+            # three BF16 MMAs (hi/lo split) per algorithmic multiply-add
+            batched["matvec_tensor_frac_of_bf16_peak"] = \
+                3 * batched["matvec_algorithmic_tflops"] / peak
 
     if rank == 0:
         line = {
@@ -381,6 +487,7 @@ def run_ours(args, rank, world, local):
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": launches,
             "clocks": clk,
+            "batched_chunks": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
