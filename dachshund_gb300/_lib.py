@@ -153,6 +153,7 @@ SIGNATURES = {
     "ds_solve_pcg_dev": (_i, [_vp, C.POINTER(PcgParamsC), _vp, C.POINTER(PcgResultC), _dp]),
     "ds_solve_pcg_noalloc": (_i, [_i, _i, _vp, C.POINTER(KernelParamsC), C.POINTER(PcgParamsC),
                                   _vp, C.POINTER(PcgResultC), _dp, _vp]),
+    "ds_A_residual_ff": (_i, [_vp, _dp, _dp]),
     "ds_solve_mixed": (_i, [_vp, C.POINTER(MixedParamsC), _dp, C.POINTER(PcgResultC), _dp]),
     "ds_solve_mixed_dev": (_i, [_vp, C.POINTER(MixedParamsC), _vp, C.POINTER(PcgResultC), _dp]),
     "ds_map_product_f32": (_i, [_vp, _vp, _d, _dp, _dp]),

@@ -236,6 +236,11 @@ class _WFVector:
     def A_residual(self, x):
         return self._vec_call(self._lib.ds_A_residual, x, "x")
 
+    def A_residual_ff(self, x):
+        """b - A x with the exact kernel in float-float arithmetic (the mixed
+        form's outer residual)."""
+        return self._vec_call(self._lib.ds_A_residual_ff, x, "x")
+
     def preconditioner_solve(self, b):
         return self._vec_call(self._lib.ds_preconditioner_solve, b, "b")
 

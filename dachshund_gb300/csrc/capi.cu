@@ -523,6 +523,26 @@ int ds_solve_pcg_dev(ds_operator* op, const ds_pcg_params* pp, double* x, ds_pcg
                       [&](ds_pcg_result& r) { run_pcg(op, *pp, r, residual_norms); });
 }
 
+int ds_A_residual_ff(ds_operator* op, const double* x, double* r) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    require(x && r, "null vector");
+    require(ff_usable(op->kc), "float-float residual needs DS_EVAL_EXACT and a cutoff <= 60");
+    cudaStream_t st = op->ctx->stream;
+    ensure_op_f32(op, op->f32 ? op->f32->inner_cut : 24.0);
+    upload(x, op->n, op->io_a, st);
+    op->io_b.alloc(op->n);
+    op->tmp.alloc(op->pix.n_pad);
+    op->tmp2.alloc(op->pix.n_pad);
+    gather_sorted(op->pix, op->io_a.p, op->tmp.p, st);
+    PairArgs a = op_pair_args(op, op->tmp.p, op->tmp2.p);
+    launch_pair_ff_resid(op->kc, a, op->f32->ffd.view, st);
+    scatter_sorted(op->pix, op->tmp2.p, nullptr, op->io_b.p, st);
+    DS_CUDA(cudaMemcpyAsync(r, op->io_b.p, op->n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 int ds_solve_mixed(ds_operator* op, const ds_mixed_params* mp, double* x, ds_pcg_result* res,
                    double* residual_norms) {
   if (!mp) return DS_ERR_ARG;

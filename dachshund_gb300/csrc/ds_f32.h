@@ -53,6 +53,28 @@ struct F32Args {
 
 void launch_pair_f32(int formula, int epi, const F32Args& a, cudaStream_t st);
 
+// Float-pair coordinates for the FP64-accurate residual on the FP32 pipe
+// (pair_ff.cu): per pixel its coordinates scaled by sqrt(c_perp),
+// sqrt(c_para) relative to its tile's (scaled) origin; per tile the origin.
+struct FFPoints {
+  const float2* fx;
+  const float2* fy;
+  const float2* fz;
+  const double* orig;  // 3 per tile
+  double sp, sq;       // sqrt(c_perp), sqrt(c_para)
+};
+
+struct FFData {
+  DevBuf<float2> fx, fy, fz;
+  DevBuf<double> orig;
+  FFPoints view{};
+};
+
+bool ff_usable(const KernelConsts& kc);
+void build_ff_points(FFData& f, const PointSet& ps, const KernelConsts& kc, cudaStream_t st);
+void launch_pair_ff_resid(const KernelConsts& kc, const PairArgs& a, const FFPoints& f,
+                          cudaStream_t st);
+
 // Device state of the reliable-update mixed-precision PCG.
 struct MixedState {
   double rz;          // r . z (FP32 vectors, FP64 sum)
@@ -87,6 +109,8 @@ struct OpF32 {
   DevBuf<float> p, q, r, z, xc;     // FP32 iteration vectors (sorted, padded)
   DevBuf<MixedState> state;
   DevBuf<double> hist, htrue;
+  bool use_ff = false;  // outer residual in float-float arithmetic (else FP64)
+  FFData ffd;
 };
 
 // FP32 data of a map point set (DIRECT formula only).

@@ -340,6 +340,8 @@ void ensure_op_f32(ds_operator* op, double inner_cut) {
   f->z.alloc(np);
   f->xc.alloc(np);
   f->state.alloc(1);
+  f->use_ff = ff_usable(op->kc);
+  if (f->use_ff) build_ff_points(f->ffd, op->pix, op->kc, st);
   DS_CUDA(cudaStreamSynchronize(st));
   op->f32 = std::move(f);
 }
@@ -398,7 +400,13 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   DS_CHECK_LAUNCH();
   PairArgs resid = op_pair_args(op, op->x.p, op->r.p);
   resid.skip_flag = xzero;
-  launch_pair_f64(op->kc, EPI_RESIDUAL, resid, st);
+  auto outer_residual = [&](const PairArgs& pa) {
+    if (f.use_ff)
+      launch_pair_ff_resid(op->kc, pa, f.ffd.view, st);
+    else
+      launch_pair_f64(op->kc, EPI_RESIDUAL, pa, st);
+  };
+  outer_residual(resid);
   k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p, f.xc.p,
                               f.pdiag.p, op->partial.p, f.hist.p, f.htrue.p);
   DS_CHECK_LAUNCH();
@@ -428,7 +436,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     DS_CHECK_LAUNCH();
     k_mx_fold<<<g, VB, 0, st>>>(np, S, op->x.p, f.xc.p);                    // K4
     DS_CHECK_LAUNCH();
-    launch_pair_f64(op->kc, EPI_RESIDUAL, upd, st);                          // K5
+    outer_residual(upd);                                                      // K5
     k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,
                                    f.hist.p, f.htrue.p);                     // K6
     DS_CHECK_LAUNCH();

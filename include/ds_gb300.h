@@ -258,6 +258,14 @@ typedef struct {
   int verbose;
 } ds_mixed_params;
 
+/* The mixed form's outer residual r = b - A x on its own: the exact kernel
+ * evaluated in float-float arithmetic (unevaluated pairs of FP32 numbers,
+ * about 48 significant bits) on the FP32 pipe, agreeing with ds_A_residual
+ * (FP64, DS_EVAL_EXACT) to about 1e-13 relative.  Needs DS_EVAL_EXACT with an
+ * exponent cutoff of at most 60 (the mixed form falls back to the FP64
+ * residual otherwise).  x, r in caller order (host). */
+int ds_A_residual_ff(ds_operator* op, const double* x, double* r);
+
 /* x: initial guess in, solution out (times w in the W form), caller order.
  * ``residual_norms`` (optional, max_iter + 1 doubles) receives the FP32
  * recurrence norms, replaced by the FP64 true norm at update iterations.

@@ -98,3 +98,23 @@ def test_table_operator_rejected_by_mixed(ctx):
 
     with pytest.raises(DsError):
         op.solve_mixed(MixedParams())
+
+
+@pytest.mark.parametrize("form", ["w", "sn"])
+def test_ff_residual_matches_fp64(ctx, form):
+    """The float-float outer residual against the FP64 one: within 1e-12 of
+    the largest |r| for a random x (about 1e-14 of the summed |S_ij x_j|) and
+    within 1e-12 |b| at a converged solution (where |r| ~ 1e-8 |b|)."""
+    w = synth.small(24, 48, 14.0, seed=33)
+    op, rec = make(ctx, form, w.pixels)
+    nb = np.linalg.norm(rec[:, 4])
+    x = np.random.default_rng(3).standard_normal(op.n)
+    r64 = op.A_residual(x)
+    rff = op.A_residual_ff(x)
+    assert np.max(np.abs(rff - r64)) <= 1e-12 * np.max(np.abs(r64))
+    xs, res = op.solve_mixed(MixedParams(tol=1e-8))
+    y = xs / rec[:, 3] if form == "w" else xs
+    r64 = op.A_residual(y)
+    rff = op.A_residual_ff(y)
+    assert np.linalg.norm(rff - r64) <= 1e-12 * nb
+    assert np.linalg.norm(r64) <= 1e-8 * nb * (1 + 1e-6)
