@@ -33,6 +33,7 @@
 
 #include "ds_batch.h"
 #include "ds_device.cuh"
+#include "ds_ff.cuh"
 
 namespace ds {
 namespace {
@@ -262,32 +263,38 @@ __device__ __forceinline__ void df_mac(float& ah, float& al, float sh, float sl,
 
 // r64 = b - A x for the chunks with an update pending; work items as in the
 // FP32 matvec.  One row per thread.  The exact kernel value of a pair is
-// computed in FP64 once per item (the argument rounded as in the
-// single-operator FP64 kernel, exp from exp_neg_f64, zero at and beyond the
-// cutoff) and split into a float pair; the products with the RB right-hand
-// sides are accumulated as float pairs on the FP32 pipe (the FP64 pipe of
-// this part does 2 operations per clock per SM), which keeps about 44
-// significant bits, far below the 1e-8 relative residual it certifies.
-// Warp-private staging of the column sub-tiles the warp's rows interact
-// with: coordinates in FP64, the (hi, lo) u values padded so that the
-// staging stores avoid bank conflicts.
-template <int RB>
+// computed once per item and applied to RB right-hand sides, accumulated as
+// float pairs on the FP32 pipe (about 44 significant bits, far below the
+// 1e-8 relative residual it certifies).  With FF (the default: exact kernel,
+// cutoff <= 60) the kernel value itself is a float-pair evaluation
+// (ds_ff.cuh) from float-pair scaled coordinates; otherwise it is FP64 (the
+// argument rounded as in the single-operator FP64 kernel, exp_neg_f64) split
+// into a float pair.  GB300 runs FP64 at 1/64 of the FP32 rate, which is why
+// neither the kernel value nor the accumulation stays in FP64.  Warp-private
+// staging of the column sub-tiles the warp's rows interact with; the (hi,
+// lo) u values padded so that the staging stores avoid bank conflicts.
+template <int RB, bool FF>
 __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
   constexpr int ROWF = 2 * RB + 4;  // floats per staged column
   extern __shared__ float4 resid_dyn[];
   float* ustage = reinterpret_cast<float*>(resid_dyn);  // [TILE / 32][SUBTILE][ROWF]
-  __shared__ double sw[TILE / 32][3][SUBTILE];
+  __shared__ double sw[FF ? 1 : TILE / 32][3][SUBTILE];
+  __shared__ float sf[FF ? TILE / 32 : 1][6][SUBTILE];
   __shared__ double tf[32];
+  __shared__ float tab_h[32], tab_l[32];
   __shared__ int s_item;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (tid < 32) tf[tid] = exp2(-(double)tid / 32.0);
+  if (tid < 32) {
+    tf[tid] = exp2(-(double)tid / 32.0);
+    const ff v = ff_from_double(tf[tid]);
+    tab_h[tid] = v.h;
+    tab_l[tid] = v.l;
+  }
   const KernelConsts kc = a.kc;
+  const float cut = (float)kc.exact_cut;
   const int R = a.n_rhs;
   const int nblk = R / RB;
   const int n_items = a.n_row_tiles * nblk;
-  double* sxw = sw[warp][0];
-  double* syw = sw[warp][1];
-  double* szw = sw[warp][2];
   float* suw = ustage + warp * SUBTILE * ROWF;
   for (;;) {
     __syncthreads();
@@ -310,13 +317,30 @@ __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
       if (!m) continue;
       n_sub += __popc(m);
       const int ct = a.cols[p];
+      ff Yx{0.f, 0.f}, Yy{0.f, 0.f}, Yz{0.f, 0.f};
+      if constexpr (FF) {
+        // this row relative to the column tile's origin, scaled
+        Yx = ff_from_double(xi * a.ff.sp - a.ff.orig[3 * ct + 0]);
+        Yy = ff_from_double(yi * a.ff.sp - a.ff.orig[3 * ct + 1]);
+        Yz = ff_from_double(zi * a.ff.sq - a.ff.orig[3 * ct + 2]);
+      }
       for (int cs = 0; cs < TILE / SUBTILE; ++cs) {
         if (!((m >> cs) & 1u)) continue;
         const int j = ct * TILE + cs * SUBTILE + lane;
         __syncwarp();
-        sxw[lane] = a.x[j];
-        syw[lane] = a.y[j];
-        szw[lane] = a.z[j];
+        if constexpr (FF) {
+          const float2 cx = a.ff.fx[j], cy = a.ff.fy[j], cz = a.ff.fz[j];
+          sf[warp][0][lane] = cx.x;
+          sf[warp][1][lane] = cx.y;
+          sf[warp][2][lane] = cy.x;
+          sf[warp][3][lane] = cy.y;
+          sf[warp][4][lane] = cz.x;
+          sf[warp][5][lane] = cz.y;
+        } else {
+          sw[warp][0][lane] = a.x[j];
+          sw[warp][1][lane] = a.y[j];
+          sw[warp][2][lane] = a.z[j];
+        }
         const float2* src = a.uu + (size_t)j * R + r0;
         float2* dst = reinterpret_cast<float2*>(suw + lane * ROWF);
 #pragma unroll
@@ -324,11 +348,22 @@ __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
         __syncwarp();
 #pragma unroll 1
         for (int jj = 0; jj < SUBTILE; ++jj) {
-          const double dx = xi - sxw[jj], dy = yi - syw[jj], dz = zi - szw[jj];
-          const double arg = fma(kc.c_perp, fma(dx, dx, dy * dy), kc.c_para * (dz * dz));
-          const double g = arg < kc.exact_cut ? exp_neg_f64(arg, tf) : 0.0;
           float sh, sl;
-          split_f64(g, sh, sl);
+          if constexpr (FF) {
+            const ff d2 = ff_dist2(Yx, Yy, Yz, ff{sf[warp][0][jj], sf[warp][1][jj]},
+                                   ff{sf[warp][2][jj], sf[warp][3][jj]},
+                                   ff{sf[warp][4][jj], sf[warp][5][jj]});
+            if (!(d2.h < cut)) continue;  // warp-divergent skip of a zero term
+            const ff g = ff_exp_neg(d2, tab_h, tab_l);
+            sh = g.h;
+            sl = g.l;
+          } else {
+            const double dx = xi - sw[warp][0][jj], dy = yi - sw[warp][1][jj];
+            const double dz = zi - sw[warp][2][jj];
+            const double arg = fma(kc.c_perp, fma(dx, dx, dy * dy), kc.c_para * (dz * dz));
+            const double g = arg < kc.exact_cut ? exp_neg_f64(arg, tf) : 0.0;
+            split_f64(g, sh, sl);
+          }
           const float2* u2 = reinterpret_cast<const float2*>(suw + jj * ROWF);
 #pragma unroll
           for (int r = 0; r < RB; ++r) {
@@ -347,6 +382,29 @@ __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
       const double acc = (double)ah[r] + (double)al[r];
       a.r64[k] = a.b[k] - (wli * acc + ei * a.xv[k]);
     }
+  }
+}
+
+// Float-pair scaled coordinates of the batch's pixels, relative to the first
+// pixel of their tile (the tile origin), and the scaled origins.
+__global__ void k_ff_points_batch(int n_pad, const double* __restrict__ x,
+                                  const double* __restrict__ y, const double* __restrict__ z,
+                                  double sp, double sq, float2* __restrict__ fx,
+                                  float2* __restrict__ fy, float2* __restrict__ fz,
+                                  double* __restrict__ orig) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  const int t0 = (i / TILE) * TILE;
+  const double ox = x[t0] * sp, oy = y[t0] * sp, oz = z[t0] * sq;
+  const ff X = ff_from_double(x[i] * sp - ox), Y = ff_from_double(y[i] * sp - oy);
+  const ff Z = ff_from_double(z[i] * sq - oz);
+  fx[i] = make_float2(X.h, X.l);
+  fy[i] = make_float2(Y.h, Y.l);
+  fz[i] = make_float2(Z.h, Z.l);
+  if (i == t0) {
+    orig[3 * (i / TILE) + 0] = ox;
+    orig[3 * (i / TILE) + 1] = oy;
+    orig[3 * (i / TILE) + 2] = oz;
   }
 }
 
@@ -655,11 +713,11 @@ constexpr size_t resid_smem() {
   return (size_t)(TILE / 32) * SUBTILE * (2 * RB + 4) * sizeof(float);
 }
 
-template <int RB>
-void resid_launch(const BatchF64Args& a, int grid, cudaStream_t st) {
+template <int RB, bool FF>
+void resid_launch_t(const BatchF64Args& a, int grid, cudaStream_t st) {
   static bool attr = false;  // set on the first (uncaptured) launch
   if (!attr) {
-    DS_CUDA(cudaFuncSetAttribute(k_batch_resid_f64<RB>,
+    DS_CUDA(cudaFuncSetAttribute(k_batch_resid_f64<RB, FF>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)resid_smem<RB>()));
     attr = true;
@@ -669,13 +727,21 @@ void resid_launch(const BatchF64Args& a, int grid, cudaStream_t st) {
     static int full = 0;
     if (!full) {
       int per_sm = 0;
-      DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_resid_f64<RB>, TILE,
-                                                            resid_smem<RB>()));
+      DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, k_batch_resid_f64<RB, FF>, TILE, resid_smem<RB>()));
       full = std::max(per_sm, 1) * sm_count();
     }
     grid = std::max(1, std::min(items, full));
   }
-  k_batch_resid_f64<RB><<<grid, TILE, resid_smem<RB>(), st>>>(a);
+  k_batch_resid_f64<RB, FF><<<grid, TILE, resid_smem<RB>(), st>>>(a);
+}
+
+template <int RB>
+void resid_launch(const BatchF64Args& a, int grid, cudaStream_t st) {
+  if (a.ff.fx)
+    resid_launch_t<RB, true>(a, grid, st);
+  else
+    resid_launch_t<RB, false>(a, grid, st);
 }
 
 // RHS block of the FP64 residual: the largest of 32, 16, 8, 4, 2, 1 dividing R
@@ -893,6 +959,17 @@ void batch_build(ds_batch* B, const double* d_rec, const int* sizes) {
   B->work.alloc(2);
   B->err.alloc(1);
   DS_CUDA(cudaMemsetAsync(B->err.p, 0, sizeof(int), st));
+  if (ff_usable(B->kc)) {
+    FFData& f = B->ffd;
+    f.fx.alloc(NP);
+    f.fy.alloc(NP);
+    f.fz.alloc(NP);
+    f.orig.alloc((size_t)3 * T);
+    k_ff_points_batch<<<blocks_for(NP), 256, 0, st>>>(NP, B->x.p, B->y.p, B->z.p, sp, sq, f.fx.p,
+                                                      f.fy.p, f.fz.p, f.orig.p);
+    DS_CHECK_LAUNCH();
+    f.view = FFPoints{f.fx.p, f.fy.p, f.fz.p, f.orig.p, sp, sq};
+  }
   DS_CUDA(cudaMemsetAsync(B->chunk_done.p, 0, C * sizeof(int), st));
   DS_CUDA(cudaStreamSynchronize(st));
   B->pairs32_total = pairs32;
@@ -948,6 +1025,7 @@ BatchF64Args resid_args(ds_batch* B) {
   a.n_rhs = B->n_rhs;
   a.work = B->work.p + 1;
   a.uu = B->uu.p;
+  a.ff = B->ffd.view;  // fx == nullptr: FP64 kernel value
   return a;
 }
 

@@ -59,6 +59,7 @@ struct BatchF64Args {
   const double* xv;  // [pixel][n_rhs]
   double* r64;       // [pixel][n_rhs]
   float2* uu;        // [pixel][n_rhs]: var_s wl x as (hi, lo) floats
+  FFPoints ff;       // float-pair coordinates (fx == nullptr: FP64 kernel value)
   const int* row_ptr;
   const int* cols;
   const unsigned short* mask;
@@ -135,6 +136,7 @@ struct ds_batch {
   ds::DevBuf<float> rowf, colw, ediag, pd32;
   ds::DevBuf<double> bv, xv, r64;
   ds::DevBuf<float2> uu;
+  ds::FFData ffd;  // float-pair coordinates of the FP64-accurate residual
   ds::DevBuf<float> p, q, rr, zz, xc;
   ds::DevBuf<double> part;
   ds::DevBuf<double> s_rz, s_rz_old, s_alpha, s_beta, s_rmax, s_rbest, s_rtrue, s_norm_b,
