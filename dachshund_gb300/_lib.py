@@ -119,6 +119,7 @@ class ProfileC(C.Structure):
 
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
 _i = C.c_int
 _d = C.c_double
@@ -168,6 +169,19 @@ SIGNATURES = {
     "ds_batch_solve_mixed_dev": (_i, [_vp, C.POINTER(MixedParamsC), _vp, _vp, _ip, _ip, _ip,
                                       _dp, _dp]),
     "ds_batch_product_f32_dev": (_i, [_vp, _vp, _vp]),
+    "ds_learned_create": (_i, [_vp, C.POINTER(KernelParamsC), _i, _i, C.c_uint,
+                               C.POINTER(_vp)]),
+    "ds_learned_destroy": (None, [_vp]),
+    "ds_learned_num_params": (_i, [_vp, C.POINTER(C.c_longlong)]),
+    "ds_learned_get_params": (_i, [_vp, _fp]),
+    "ds_learned_set_params": (_i, [_vp, _fp]),
+    "ds_learned_get_grads": (_i, [_vp, _fp]),
+    "ds_learned_save": (_i, [_vp, C.c_char_p]),
+    "ds_learned_load": (_i, [_vp, C.c_char_p]),
+    "ds_learned_forward_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
+    "ds_learned_train_step_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, C.c_float, C.c_float,
+                                       C.c_float, _i, _dp]),
+    "ds_operator_set_skewer_preconditioner": (_i, [_vp, _i, _i, _i, _vp]),
     "ds_map_create": (_i, [_vp, _i, _dp, C.POINTER(_vp)]),
     "ds_map_destroy": (None, [_vp]),
     "ds_map_product": (_i, [_vp, _vp, _dp, _dp]),

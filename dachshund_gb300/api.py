@@ -45,6 +45,14 @@ def _dev_ptr(t, n=None):
     return C.c_void_p(t.data_ptr())
 
 
+def _torch_done():
+    """Finish torch's pending GPU work before the library reads tensors on its
+    own stream (the *_dev calls take tensors written on torch's stream)."""
+    import torch
+
+    torch.cuda.current_stream().synchronize()
+
+
 def table_init():
     """SignalCovarParams' 200-knot table and its index scale 1/dx."""
     t = np.zeros(_lib.DS_TABLE_N)
@@ -245,12 +253,16 @@ class _WFVector:
         return self._vec_call(self._lib.ds_preconditioner_solve, b, "b")
 
     def A_product_dev(self, a, b):
+        _torch_done()
         self.ctx.check(self._lib.ds_A_product_dev(self.handle, _dev_ptr(a, self.n),
                                                   _dev_ptr(b, self.n)), "ds_A_product_dev")
+        self.ctx.synchronize()
 
     def A_residual_dev(self, x, r):
+        _torch_done()
         self.ctx.check(self._lib.ds_A_residual_dev(self.handle, _dev_ptr(x, self.n),
                                                    _dev_ptr(r, self.n)), "ds_A_residual_dev")
+        self.ctx.synchronize()
 
     def norm_b(self) -> float:
         v = C.c_double()
@@ -275,8 +287,12 @@ class _WFVector:
         c = _lib.PcgParamsC(pp.max_iter, pp.step_r, pp.tol, int(bool(pp.verbose)))
         res = _lib.PcgResultC()
         hist = np.zeros(max(pp.max_iter, 1) + 1)
+        if dev:
+            _torch_done()
         xp = _dev_ptr(x, self.n) if dev else _ptr(x)
         rc = fn(self.handle, C.byref(c), xp, C.byref(res), _ptr(hist))
+        if dev:
+            self.ctx.synchronize()
         if rc not in (_lib.DS_OK, _lib.DS_ERR_NOT_CONVERGED, _lib.DS_ERR_NORM_B):
             self.ctx.check(rc, fn.__name__)
         nh = 0 if rc == _lib.DS_ERR_NORM_B else min(hist.size, max(res.n_inner, 0) + 1)
@@ -297,8 +313,12 @@ class _WFVector:
         c = mp.as_c()
         res = _lib.PcgResultC()
         hist = np.zeros(max(mp.max_iter, 1) + 2)
+        if dev:
+            _torch_done()
         xp = _dev_ptr(x, self.n) if dev else _ptr(x)
         rc = fn(self.handle, C.byref(c), xp, C.byref(res), _ptr(hist))
+        if dev:
+            self.ctx.synchronize()
         if rc not in (_lib.DS_OK, _lib.DS_ERR_NOT_CONVERGED, _lib.DS_ERR_NORM_B):
             self.ctx.check(rc, fn.__name__)
         nh = 0 if rc == _lib.DS_ERR_NORM_B else min(hist.size, res.n_inner + 1)
@@ -419,14 +439,17 @@ class BatchSolver:
     def solve_mixed_dev(self, rhs, x, mp: MixedParams = None):
         """rhs, x: CUDA float64 tensors of n_total * n_rhs elements."""
         n = self.n_total * self.n_rhs
+        _torch_done()
         return self._solve(self._lib.ds_batch_solve_mixed_dev, mp, _dev_ptr(rhs, n),
                            _dev_ptr(x, n))
 
     def product_f32_dev(self, p, q):
         n = self.n_total * self.n_rhs
+        _torch_done()
         self.ctx.check(self._lib.ds_batch_product_f32_dev(self.handle, _dev_ptr(p, n),
                                                           _dev_ptr(q, n)),
                        "ds_batch_product_f32_dev")
+        self.ctx.synchronize()
 
 
 class MapGrid:
@@ -454,6 +477,9 @@ class MapGrid:
         return m
 
     def product_dev(self, op: _WFVector, x, m):
+        """Device product on the context's stream (torch's pending work is
+        finished first; the caller orders the read of m on the stream)."""
+        _torch_done()
         self.ctx.check(self._lib.ds_map_product_dev(self.handle, op.handle, _dev_ptr(x, op.n),
                                                     _dev_ptr(m, self.n_map)),
                        "ds_map_product_dev")
@@ -467,6 +493,7 @@ class MapGrid:
         return m
 
     def product_f32_dev(self, op: _WFVector, x, m, cutoff: float = 0.0):
+        _torch_done()
         self.ctx.check(self._lib.ds_map_product_f32_dev(self.handle, op.handle, cutoff,
                                                         _dev_ptr(x, op.n),
                                                         _dev_ptr(m, self.n_map)),

@@ -124,22 +124,6 @@ __global__ void k_gather_recip_field(int n_pad, const int* __restrict__ perm,
   }
 }
 
-template <class F>
-int guarded(ds_context* ctx, F&& f) {
-  try {
-    f();
-    if (ctx) ctx->last_error.clear();
-    return DS_OK;
-  } catch (const Error& e) {
-    if (ctx) ctx->last_error = e.msg;
-    else fprintf(stderr, "[dachshund-gb300] %s\n", e.msg.c_str());
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    if (ctx) ctx->last_error = "host allocation failed";
-    return DS_ERR_OOM;
-  }
-}
-
 void upload(const double* h, size_t n, DevBuf<double>& d, cudaStream_t st) {
   d.alloc(n);
   DS_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(double), cudaMemcpyHostToDevice, st));

@@ -26,8 +26,10 @@ namespace ds {
 
 struct OpF32;   // ds_f32.h
 struct MapF32;  // ds_f32.h
+struct SkewerPC;  // ds_learned.h
 struct OpF32Deleter { void operator()(OpF32* p) const; };
 struct MapF32Deleter { void operator()(MapF32* p) const; };
+struct SkewerPCDeleter { void operator()(SkewerPC* p) const; };
 
 constexpr int TILE = 128;        // points per tile (rows per CTA in the FP64 kernels)
 constexpr int SUBTILE = 32;      // points per sub-tile (one warp's rows; culled per warp)
@@ -273,6 +275,8 @@ struct ds_operator {
   std::unique_ptr<ds::OpF32, ds::OpF32Deleter> f32;  // mixed-precision data (lazy)
   ds::DevBuf<double> dense;  // dense A (n_pad x n_pad, sorted order) when enabled
   bool use_dense = false;
+  // skewer-band preconditioner of the mixed form (null: Jacobi)
+  std::unique_ptr<ds::SkewerPC, ds::SkewerPCDeleter> pc;
 };
 
 struct ds_map {

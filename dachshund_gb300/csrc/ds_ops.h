@@ -1,9 +1,30 @@
 // Internal entry points shared between the translation units of the library.
 #pragma once
 
+#include <cstdio>
+#include <new>
+
 #include "ds_internal.cuh"
 
 namespace ds {
+
+// Runs f, mapping internal errors to status codes and the context's last
+// error message (the C ABI's error convention).
+template <class F>
+int guarded(ds_context* ctx, F&& f) {
+  try {
+    f();
+    if (ctx) ctx->last_error.clear();
+    return DS_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->last_error = e.msg;
+    else fprintf(stderr, "[dachshund-gb300] %s\n", e.msg.c_str());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return DS_ERR_OOM;
+  }
+}
 
 void gather_sorted(const PointSet& ps, const double* src, double* dst, cudaStream_t st);
 void scatter_sorted(const PointSet& ps, const double* src, const double* scale, double* dst,

@@ -1,0 +1,877 @@
+// Learned warm start and per-skewer preconditioner (no reference
+// counterpart): a small message-passing network over the pixels of a
+// skewer-structured pixel set (n_sk skewers of n_per pixels sharing one
+// z grid, records skewer-contiguous) predicts, for the W-form system
+// (I + w S w) y = w d,
+//   * a warm start y0 for the solve, and
+//   * per skewer a lower-triangular band factor L (bandwidth B, positive
+//     diagonal), the preconditioner M^-1 = L L^T of that skewer's block.
+// Forward, backward and optimiser are the kernels below (CUDA cores, FP32
+// arithmetic on BF16 weights); the tensor cores are left to the batched
+// S-tile x RHS matvec.
+//
+// Network (hidden width H, F_IN = 11 inputs per pixel):
+//   inputs   z position along the skewer, log noise, the whitened datum w d,
+//            and g_n = exp(-dperp_n^2 / (2 l_perp^2)) to the 8 nearest
+//            neighbour skewers;
+//   embed    h0 = relu(X W_in + b_in);
+//   layers   h_l = h_{l-1} + relu([h | A_z h | A_n h] W_l + b_l), l = 1..4,
+//            A_z h_i = h_{i-1} + h_{i+1} along the skewer, A_n h_i =
+//            sum_n g_n h_{(neighbour n, same z index)};
+//   head     Y = h_4 W_o + b_o (2 + B outputs per pixel):
+//            y0 = XS Y_0, L_ii = LD softplus(Y_1) + LMIN,
+//            L_{i,i-m} = RO tanh(Y_{1+m}) L_ii (m = 1..B, inside the skewer:
+//            off-diagonals bounded by RO times the diagonal, so that L stays
+//            well conditioned).
+// Losses (trained on solutions of the plain solver):
+//   warm start     sum (y0 - y*)^2 / sum y*^2;
+//   preconditioner per skewer, with probe vectors v:
+//                  sum |L L^T A_bb v - v|^2 / n, A_bb the skewer's own block
+//                  of I + w S w (its pixels only).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ds_f32.h"
+#include "ds_learned.h"
+#include "ds_ops.h"
+
+namespace ds {
+namespace {
+
+constexpr int NB_K = 8;   // neighbour skewers
+constexpr float XS = 0.3f, LD = 0.5f, LMIN = 0.01f, RO = 0.5f;
+constexpr float LOGN0 = -2.1f, LOGNS = 0.6f;  // log-noise normalisation
+
+inline unsigned grid1(size_t n, int nt = 256) { return (unsigned)((n + nt - 1) / nt); }
+
+__device__ __forceinline__ float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+__device__ __forceinline__ float sigmoid(float x) { return 1.f / (1.f + expf(-x)); }
+
+// ---- geometry and inputs --------------------------------------------------------
+
+// The 8 nearest skewers of every skewer (brute force over the skewer (x, y)),
+// with weights g = exp(-d^2 / (2 l_perp^2)).
+__global__ void k_knn(int n_sk, int n_per, const double* __restrict__ rec, double inv2l2,
+                      int* __restrict__ nbr, float* __restrict__ g) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_sk) return;
+  const double xs = rec[(size_t)s * n_per * 5], ys = rec[(size_t)s * n_per * 5 + 1];
+  double bd[NB_K];
+  int bi[NB_K];
+  for (int k = 0; k < NB_K; ++k) {
+    bd[k] = 1e300;
+    bi[k] = s;
+  }
+  for (int o = 0; o < n_sk; ++o) {
+    if (o == s) continue;
+    const double dx = rec[(size_t)o * n_per * 5] - xs, dy = rec[(size_t)o * n_per * 5 + 1] - ys;
+    const double d2 = dx * dx + dy * dy;
+    if (d2 >= bd[NB_K - 1]) continue;
+    int k = NB_K - 1;
+    while (k > 0 && bd[k - 1] > d2) {
+      bd[k] = bd[k - 1];
+      bi[k] = bi[k - 1];
+      --k;
+    }
+    bd[k] = d2;
+    bi[k] = o;
+  }
+  for (int k = 0; k < NB_K; ++k) {
+    nbr[s * NB_K + k] = bi[k];
+    g[s * NB_K + k] = bi[k] == s ? 0.f : (float)exp(-bd[k] * inv2l2);
+  }
+}
+
+// Input features of every pixel (caller order: i = s n_per + k).
+__global__ void k_features(int n, int n_per, const double* __restrict__ rec,
+                           const float* __restrict__ g, float* __restrict__ X) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = i / n_per, k = i % n_per;
+  const double w = rec[(size_t)i * 5 + 3], wd = rec[(size_t)i * 5 + 4];
+  float* x = X + (size_t)i * F_IN;
+  x[0] = n_per > 1 ? 2.f * k / (n_per - 1) - 1.f : 0.f;
+  x[1] = ((float)(-log(w)) - LOGN0) / LOGNS;  // log n
+  x[2] = 0.5f * (float)wd;
+  for (int m = 0; m < NB_K; ++m) x[3 + m] = g[s * NB_K + m];
+}
+
+// ---- dense layers -------------------------------------------------------------------
+
+// C[M x N] = A[M x K] B + bias, A FP32 row-major (lda), B BF16: row-major
+// K x N (ldb) or, with TB, stored N x K (B(k, n) = Bm[n ldb + k]).  Epilogue
+// (EPI): 0 plain store; 1 Z = C stored, out = relu(Z); 2 Z stored,
+// out = res + relu(Z).  64 x 64 tiles, K steps of 16, 256 threads with 4 x 4
+// outputs each.
+template <bool TB, int EPI>
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* __restrict__ A,
+                                              int lda, const __nv_bfloat16* __restrict__ Bm,
+                                              int ldb, const float* __restrict__ bias,
+                                              float* __restrict__ Z, float* __restrict__ out,
+                                              const float* __restrict__ res, int ldc) {
+  __shared__ float As[16][64 + 1];
+  __shared__ float Bs[16][64];
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const int tr = tid / 16, tc = tid % 16;  // 4 rows x 4 cols each
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int q = tid; q < 64 * 16; q += 256) {
+      const int r = q / 16, kk = q % 16;
+      const int m = m0 + r, k = k0 + kk;
+      As[kk][r] = (m < M && k < K) ? A[(size_t)m * lda + k] : 0.f;
+    }
+    for (int q = tid; q < 16 * 64; q += 256) {
+      const int kk = q / 64, c = q % 64;
+      const int k = k0 + kk, n = n0 + c;
+      float v = 0.f;
+      if (k < K && n < N)
+        v = __bfloat162float(TB ? Bm[(size_t)n * ldb + k] : Bm[(size_t)k * ldb + n]);
+      Bs[kk][c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][tr * 4 + u];
+        b[u] = Bs[kk][tc * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int m = m0 + tr * 4 + u;
+    if (m >= M) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int n = n0 + tc * 4 + v;
+      if (n >= N) continue;
+      const float c = acc[u][v] + (bias ? bias[n] : 0.f);
+      const size_t o = (size_t)m * ldc + n;
+      if (EPI == 0) {
+        out[o] = c;
+      } else {
+        Z[o] = c;
+        const float r = fmaxf(c, 0.f);
+        out[o] = EPI == 2 ? res[o] + r : r;
+      }
+    }
+  }
+}
+
+// Partial products for C[K x N] = A^T D over a chunk of rows: A [M x K],
+// D [M x N] FP32 row-major; each CTA (ky, nx, chunk) writes its 64 x 64 block
+// of the chunk's contribution; k_reduce_chunks sums the chunks (fixed order).
+constexpr int ATB_CHUNK = 2048;
+__global__ void __launch_bounds__(256) k_gemm_atb(int M, int K, int N, const float* __restrict__ A,
+                                                  int lda, const float* __restrict__ D, int ldd,
+                                                  float* __restrict__ part) {
+  __shared__ float As[16][64 + 1];
+  __shared__ float Ds[16][64];
+  const int tid = threadIdx.x;
+  const int k0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const int mc = blockIdx.z * ATB_CHUNK;
+  const int m_end = min(M, mc + ATB_CHUNK);
+  const int tr = tid / 16, tc = tid % 16;
+  float acc[4][4] = {};
+  for (int mm = mc; mm < m_end; mm += 16) {
+    for (int q = tid; q < 16 * 64; q += 256) {
+      const int r = q / 64, c = q % 64;
+      const int m = mm + r;
+      As[r][c] = (m < m_end && k0 + c < K) ? A[(size_t)m * lda + k0 + c] : 0.f;
+      Ds[r][c] = (m < m_end && n0 + c < N) ? D[(size_t)m * ldd + n0 + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      float a[4], d[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[r][tr * 4 + u];
+        d[u] = Ds[r][tc * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], d[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  float* P = part + (size_t)blockIdx.z * K * N;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int k = k0 + tr * 4 + u;
+    if (k >= K) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int n = n0 + tc * 4 + v;
+      if (n < N) P[(size_t)k * N + n] = acc[u][v];
+    }
+  }
+}
+
+__global__ void k_reduce_chunks(int n_chunks, size_t len, const float* __restrict__ part,
+                                float* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  float s = 0.f;
+  for (int c = 0; c < n_chunks; ++c) s += part[(size_t)c * len + i];
+  out[i] = s;
+}
+
+// Column sums of D [M x N] (bias gradients), in chunks then a fixed-order sum.
+__global__ void k_colsum_part(int M, int N, const float* __restrict__ D,
+                              float* __restrict__ part) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int mc = blockIdx.y * ATB_CHUNK, me = min(M, mc + ATB_CHUNK);
+  float s = 0.f;
+  for (int m = mc; m < me; ++m) s += D[(size_t)m * N + n];
+  part[(size_t)blockIdx.y * N + n] = s;
+}
+
+// ---- message passing ---------------------------------------------------------------
+
+// cat_i = [h_i | h_{i-1} + h_{i+1} | sum_n g_n h_{nb_n, k}].
+__global__ void k_agg_fwd(int n, int n_per, int H, const float* __restrict__ h,
+                          const int* __restrict__ nbr, const float* __restrict__ g,
+                          float* __restrict__ cat) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)n * H) return;
+  const int i = (int)(q / H), c = (int)(q % H);
+  const int s = i / n_per, k = i % n_per;
+  const float hi = h[q];
+  float az = 0.f;
+  if (k > 0) az += h[q - H];
+  if (k + 1 < n_per) az += h[q + H];
+  float an = 0.f;
+#pragma unroll
+  for (int m = 0; m < NB_K; ++m)
+    an = fmaf(g[s * NB_K + m], h[((size_t)nbr[s * NB_K + m] * n_per + k) * H + c], an);
+  float* o = cat + (size_t)i * 3 * H;
+  o[c] = hi;
+  o[H + c] = az;
+  o[2 * H + c] = an;
+}
+
+// dh += adjoint of the aggregation applied to dcat (the neighbour part
+// scattered with atomics: several skewers may share a neighbour).
+__global__ void k_agg_bwd(int n, int n_per, int H, const float* __restrict__ dcat,
+                          const int* __restrict__ nbr, const float* __restrict__ g,
+                          float* __restrict__ dh) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)n * H) return;
+  const int i = (int)(q / H), c = (int)(q % H);
+  const int s = i / n_per, k = i % n_per;
+  const float* d = dcat + (size_t)i * 3 * H;
+  float v = d[c];
+  if (k > 0) v += dcat[(size_t)(i - 1) * 3 * H + H + c];
+  if (k + 1 < n_per) v += dcat[(size_t)(i + 1) * 3 * H + H + c];
+  atomicAdd(&dh[q], v);
+  const float dn = d[2 * H + c];
+#pragma unroll
+  for (int m = 0; m < NB_K; ++m) {
+    const float gm = g[s * NB_K + m];
+    if (gm != 0.f) atomicAdd(&dh[((size_t)nbr[s * NB_K + m] * n_per + k) * H + c], gm * dn);
+  }
+}
+
+// dZ = dh * (Z > 0).
+__global__ void k_relu_bwd(size_t len, const float* __restrict__ dh, const float* __restrict__ Z,
+                           float* __restrict__ dZ) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < len) dZ[i] = Z[i] > 0.f ? dh[i] : 0.f;
+}
+
+// ---- head, outputs and losses -------------------------------------------------------
+
+// y0 and the band rows of L from Y (n x NO, NO = 2 + B).
+__global__ void k_outputs(int n, int n_per, int B, const float* __restrict__ Y,
+                          double* __restrict__ y0, float* __restrict__ Lr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int NO = 2 + B, k = i % n_per;
+  const float* y = Y + (size_t)i * NO;
+  if (y0) y0[i] = (double)(XS * y[0]);
+  float* l = Lr + (size_t)i * (B + 1);
+  const float d = LD * softplus(y[1]) + LMIN;
+  l[0] = d;
+  for (int m = 1; m <= B; ++m) l[m] = k - m >= 0 ? RO * tanhf(y[1 + m]) * d : 0.f;
+}
+
+// Warm-start loss sum (y0 - y*)^2 / sum y*^2: per-block partials of both
+// sums (2 per block).
+__global__ void k_xloss_part(int n, const float* __restrict__ Y, int NO,
+                             const double* __restrict__ ystar, double* __restrict__ part) {
+  __shared__ double red[2][8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e2 = 0.0, t2 = 0.0;
+  if (i < n) {
+    const double d = (double)(XS * Y[(size_t)i * NO]) - ystar[i];
+    e2 = d * d;
+    t2 = ystar[i] * ystar[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e2 += __shfl_down_sync(0xffffffffu, e2, o);
+    t2 += __shfl_down_sync(0xffffffffu, t2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = e2;
+    red[1][threadIdx.x >> 5] = t2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += red[0][w];
+      b += red[1][w];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// dY_0 of the warm-start loss (weight wx, normaliser sum y*^2 in *tot).
+__global__ void k_xloss_grad(int n, const float* __restrict__ Y, int NO,
+                             const double* __restrict__ ystar, const double* __restrict__ tot,
+                             float wx, float* __restrict__ dY) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = (double)(XS * Y[(size_t)i * NO]) - ystar[i];
+  dY[(size_t)i * NO] = (float)(wx * 2.0 * d * XS / tot[1]);
+}
+
+// Preconditioner loss of one skewer per CTA (n_per threads, n_per <= 1024):
+// u = A_bb v, t = L^T u, s = L t, rho = s - v; loss sum rho^2 / n_total;
+// dY_{1..1+B} of its pixels.
+__global__ void k_ploss(int n_per, int B, int n_total, double var_s, double c_para,
+                        const double* __restrict__ rec, const float* __restrict__ Y,
+                        const float* __restrict__ probe, float wp, float* __restrict__ dY,
+                        double* __restrict__ loss_part) {
+  extern __shared__ float sm[];
+  float* zz = sm;               // z
+  float* ww = zz + n_per;       // w
+  float* vv = ww + n_per;       // probe v
+  float* uu = vv + n_per;       // A v
+  float* tt = uu + n_per;       // L^T u
+  float* gs = tt + n_per;       // d loss / d s
+  float* L = gs + n_per;        // n_per x (B + 1) band rows
+  const int s = blockIdx.x, k = threadIdx.x;
+  const int i = s * n_per + k;
+  const int NO = 2 + B;
+  zz[k] = (float)rec[(size_t)i * 5 + 2];
+  ww[k] = (float)rec[(size_t)i * 5 + 3];
+  vv[k] = probe[i];
+  const float* y = Y + (size_t)i * NO;
+  const float dk = LD * softplus(y[1]) + LMIN;
+  L[k * (B + 1)] = dk;
+  for (int m = 1; m <= B; ++m) L[k * (B + 1) + m] = k - m >= 0 ? RO * tanhf(y[1 + m]) * dk : 0.f;
+  __syncthreads();
+  // u = v + w S_bb w v  (the skewer's own block, exact kernel in FP32)
+  float acc = 0.f;
+  for (int j = 0; j < n_per; ++j) {
+    const float dz = zz[k] - zz[j];
+    acc = fmaf(__expf(-(float)c_para * dz * dz), ww[j] * vv[j], acc);
+  }
+  uu[k] = vv[k] + ww[k] * (float)var_s * acc;
+  __syncthreads();
+  // t_k = sum_m L[k+m][m] u_{k+m}
+  float t = 0.f;
+  for (int m = 0; m <= B; ++m)
+    if (k + m < n_per) t = fmaf(L[(k + m) * (B + 1) + m], uu[k + m], t);
+  tt[k] = t;
+  __syncthreads();
+  float sk = 0.f;
+  for (int m = 0; m <= B; ++m)
+    if (k - m >= 0) sk = fmaf(L[k * (B + 1) + m], tt[k - m], sk);
+  const float rho = sk - vv[k];
+  gs[k] = 2.f * wp * rho / n_total;
+  __syncthreads();
+  // g_t = L^T g_s; dL[k][m] = g_s[k] t[k-m] + g_t[k-m] u[k]
+  float gt = 0.f;
+  for (int m = 0; m <= B; ++m)
+    if (k + m < n_per) gt = fmaf(L[(k + m) * (B + 1) + m], gs[k + m], gt);
+  __syncthreads();
+  tt[k] = gt;  // reuse: g_t (t itself kept in registers of its owner)
+  __syncthreads();
+  // this thread's t value again for the dL of rows k' = k + m is needed by
+  // other threads: recompute locally from u (cheap) instead of sharing
+  // chain rule through L_kk = LD softplus(Y1) + LMIN and
+  // L_{k,k-m} = RO tanh(Y_{1+m}) L_kk
+  float* dy = dY + (size_t)i * NO;
+  const float sg = LD * sigmoid(y[1]);
+  float dd = 0.f;  // d loss / d L_kk, through every entry of the row
+  for (int m = 0; m <= B; ++m) {
+    if (k - m < 0) {
+      if (m > 0) dy[1 + m] = 0.f;
+      continue;
+    }
+    const int j = k - m;
+    float tj = 0.f;  // t_j = sum_m' L[j+m'][m'] u_{j+m'}
+    for (int mm = 0; mm <= B; ++mm)
+      if (j + mm < n_per) tj = fmaf(L[(j + mm) * (B + 1) + mm], uu[j + mm], tj);
+    const float dl = gs[k] * tj + tt[j] * uu[k];
+    if (m == 0) {
+      dd += dl;
+    } else {
+      const float th = tanhf(y[1 + m]);
+      dd += dl * RO * th;
+      dy[1 + m] = dl * RO * (1.f - th * th) * dk;
+    }
+  }
+  dy[1] = dd * sg;
+  // loss (n_per need not be a multiple of 32: a shared-memory sum in order)
+  __syncthreads();
+  uu[k] = rho * rho;
+  __syncthreads();
+  if (k == 0) {
+    double a = 0.0;
+    for (int j = 0; j < n_per; ++j) a += (double)uu[j];
+    loss_part[s] = wp * a / n_total;
+  }
+}
+
+// ---- optimiser ---------------------------------------------------------------------
+
+__global__ void k_adam(size_t n, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                       float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+__global__ void k_to_bf16(size_t n, const float* __restrict__ p, __nv_bfloat16* __restrict__ q) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) q[i] = __float2bfloat16_rn(p[i]);
+}
+
+// Deterministic initial weights (uniform +-sqrt(3 / fan_in) from a hash).
+__global__ void k_init(size_t n, unsigned seed, const int* __restrict__ fan_in_of,
+                       const unsigned char* __restrict__ is_bias, float* __restrict__ p) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned x = (unsigned)i * 2654435761u ^ (seed * 2246822519u + 0x9e3779b9u);
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  const float u = (x >> 8) * (1.f / 16777216.f) * 2.f - 1.f;
+  p[i] = is_bias[i] ? 0.f : u * sqrtf(3.f / fan_in_of[i]);
+}
+
+}  // namespace
+
+// ---- host side ---------------------------------------------------------------------------
+
+LearnedNet::LearnedNet(ds_context* c, int hidden, int band, const KernelConsts& k, unsigned seed)
+    : ctx(c), H(hidden), B(band), kc(k) {
+  require(H >= 32 && H % 32 == 0 && H <= 512, "hidden width must be a multiple of 32 in [32, 512]");
+  require(B >= 0 && B <= 16, "band must be in [0, 16]");
+  NO = 2 + B;
+  // layout of the flat parameter vector
+  auto add = [&](size_t rows, size_t cols, bool bias) {
+    Slot sl{n_params, rows, cols, bias};
+    n_params += rows * cols;
+    return sl;
+  };
+  W_in = add(F_IN, H, false);
+  b_in = add(1, H, true);
+  for (int l = 0; l < N_LAYERS; ++l) {
+    W_l[l] = add(3 * (size_t)H, H, false);
+    b_l[l] = add(1, H, true);
+  }
+  W_o = add(H, NO, false);
+  b_o = add(1, NO, true);
+  params.alloc(n_params);
+  grads.alloc(n_params);
+  adam_m.alloc(n_params);
+  adam_v.alloc(n_params);
+  wbf.alloc(n_params);
+  cudaStream_t st = ctx->stream;
+  std::vector<int> fan(n_params);
+  std::vector<unsigned char> isb(n_params, 0);
+  auto mark = [&](const Slot& sl, int f) {
+    for (size_t q = 0; q < sl.rows * sl.cols; ++q) {
+      fan[sl.off + q] = f;
+      isb[sl.off + q] = sl.bias ? 1 : 0;
+    }
+  };
+  mark(W_in, F_IN);
+  mark(b_in, 1);
+  for (int l = 0; l < N_LAYERS; ++l) {
+    mark(W_l[l], 3 * H);
+    mark(b_l[l], 1);
+  }
+  mark(W_o, H);
+  mark(b_o, 1);
+  DevBuf<int> dfan;
+  DevBuf<unsigned char> disb;
+  dfan.alloc(n_params);
+  disb.alloc(n_params);
+  DS_CUDA(cudaMemcpyAsync(dfan.p, fan.data(), n_params * sizeof(int), cudaMemcpyHostToDevice, st));
+  DS_CUDA(cudaMemcpyAsync(disb.p, isb.data(), n_params, cudaMemcpyHostToDevice, st));
+  k_init<<<grid1(n_params), 256, 0, st>>>(n_params, seed, dfan.p, disb.p, params.p);
+  DS_CHECK_LAUNCH();
+  {
+    // head: W_o scaled by 0.1, b_o[1] = -0.2 (L_kk = 0.5 softplus(-0.2) + 0.01
+    // = 0.3 at the start, about 1 / sqrt(diag A) of the workload's noise law)
+    std::vector<float> head(W_o.rows * W_o.cols + NO);
+    DS_CUDA(cudaMemcpyAsync(head.data(), params.p + W_o.off, head.size() * sizeof(float),
+                            cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    for (size_t q = 0; q < W_o.rows * W_o.cols; ++q) head[q] *= 0.1f;
+    head[W_o.rows * W_o.cols + 1] = -0.2f;
+    DS_CUDA(cudaMemcpyAsync(params.p + W_o.off, head.data(), head.size() * sizeof(float),
+                            cudaMemcpyHostToDevice, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+  }
+  DS_CUDA(cudaMemsetAsync(adam_m.p, 0, n_params * sizeof(float), st));
+  DS_CUDA(cudaMemsetAsync(adam_v.p, 0, n_params * sizeof(float), st));
+  sync_weights();
+  DS_CUDA(cudaStreamSynchronize(st));
+}
+
+void LearnedNet::sync_weights() {
+  k_to_bf16<<<grid1(n_params), 256, 0, ctx->stream>>>(
+      n_params, params.p, reinterpret_cast<__nv_bfloat16*>(wbf.p));
+  DS_CHECK_LAUNCH();
+}
+
+void LearnedNet::ensure(int n_sk, int n_per) {
+  require(n_sk >= 1 && n_per >= 1 && n_per <= 1024, "n_per must be in [1, 1024]");
+  const size_t n = (size_t)n_sk * n_per;
+  if (n == n_cur && n_sk == nsk_cur) return;
+  n_cur = n;
+  nsk_cur = n_sk;
+  nbr.alloc((size_t)n_sk * NB_K);
+  gw.alloc((size_t)n_sk * NB_K);
+  X.alloc(n * F_IN);
+  for (int l = 0; l <= N_LAYERS; ++l) {
+    h[l].alloc(n * H);
+    Z[l].alloc(n * H);
+  }
+  for (int l = 0; l < N_LAYERS; ++l) cat[l].alloc(n * 3 * H);
+  Y.alloc(n * NO);
+  dY.alloc(n * NO);
+  dh.alloc(n * H);
+  dh2.alloc(n * H);
+  dZ.alloc(n * H);
+  dcat.alloc(n * 3 * H);
+  const size_t chunks = (n + ATB_CHUNK - 1) / ATB_CHUNK;
+  part.alloc(chunks * std::max<size_t>(3 * (size_t)H * H, (size_t)H * NO));
+  dpart.alloc(std::max<size_t>(2 * grid1(n), (size_t)n_sk) + 2);
+}
+
+void LearnedNet::gemm_fwd(int M, int N, int K, const float* A, int lda, const Slot& W, const Slot& b,
+                          float* Zp, float* out, const float* res, int epi) {
+  const dim3 grid((N + 63) / 64, (M + 63) / 64);
+  const __nv_bfloat16* Wp = reinterpret_cast<const __nv_bfloat16*>(wbf.p) + W.off;
+  const float* bp = params.p + b.off;
+  cudaStream_t st = ctx->stream;
+  if (epi == 0)
+    k_gemm<false, 0><<<grid, 256, 0, st>>>(M, N, K, A, lda, Wp, N, bp, Zp, out, res, N);
+  else if (epi == 1)
+    k_gemm<false, 1><<<grid, 256, 0, st>>>(M, N, K, A, lda, Wp, N, bp, Zp, out, res, N);
+  else
+    k_gemm<false, 2><<<grid, 256, 0, st>>>(M, N, K, A, lda, Wp, N, bp, Zp, out, res, N);
+  DS_CHECK_LAUNCH();
+}
+
+// dW (slot) = A^T D over M rows; db = column sums of D.
+void LearnedNet::grad_w(int M, int K, int N, const float* A, int lda, const float* D,
+                        const Slot& W, const Slot& b) {
+  cudaStream_t st = ctx->stream;
+  const int chunks = (M + ATB_CHUNK - 1) / ATB_CHUNK;
+  const dim3 grid((N + 63) / 64, (K + 63) / 64, chunks);
+  k_gemm_atb<<<grid, 256, 0, st>>>(M, K, N, A, lda, D, N, part.p);
+  DS_CHECK_LAUNCH();
+  k_reduce_chunks<<<grid1((size_t)K * N), 256, 0, st>>>(chunks, (size_t)K * N, part.p,
+                                                        grads.p + W.off);
+  DS_CHECK_LAUNCH();
+  k_colsum_part<<<dim3(grid1(N, 128), chunks), 128, 0, st>>>(M, N, D, part.p);
+  DS_CHECK_LAUNCH();
+  k_reduce_chunks<<<grid1(N), 256, 0, st>>>(chunks, (size_t)N, part.p, grads.p + b.off);
+  DS_CHECK_LAUNCH();
+}
+
+void LearnedNet::forward(int n_sk, int n_per, const double* rec) {
+  ensure(n_sk, n_per);
+  cudaStream_t st = ctx->stream;
+  const int n = n_sk * n_per;
+  k_knn<<<grid1(n_sk, 128), 128, 0, st>>>(n_sk, n_per, rec, kc.c_perp, nbr.p, gw.p);
+  DS_CHECK_LAUNCH();
+  k_features<<<grid1(n), 256, 0, st>>>(n, n_per, rec, gw.p, X.p);
+  DS_CHECK_LAUNCH();
+  gemm_fwd(n, H, F_IN, X.p, F_IN, W_in, b_in, Z[0].p, h[0].p, nullptr, 1);
+  for (int l = 0; l < N_LAYERS; ++l) {
+    k_agg_fwd<<<grid1((size_t)n * H), 256, 0, st>>>(n, n_per, H, h[l].p, nbr.p, gw.p, cat[l].p);
+    DS_CHECK_LAUNCH();
+    gemm_fwd(n, H, 3 * H, cat[l].p, 3 * H, W_l[l], b_l[l], Z[l + 1].p, h[l + 1].p, h[l].p, 2);
+  }
+  gemm_fwd(n, NO, H, h[N_LAYERS].p, H, W_o, b_o, nullptr, Y.p, nullptr, 0);
+}
+
+void LearnedNet::outputs(int n_sk, int n_per, double* y0, float* Lrows) {
+  const int n = n_sk * n_per;
+  k_outputs<<<grid1(n), 256, 0, ctx->stream>>>(n, n_per, B, Y.p, y0, Lrows);
+  DS_CHECK_LAUNCH();
+}
+
+void LearnedNet::loss_and_grad(int n_sk, int n_per, const double* rec, const double* ystar,
+                               const float* probe, float wx, float wp, double* losses) {
+  cudaStream_t st = ctx->stream;
+  const int n = n_sk * n_per;
+  forward(n_sk, n_per, rec);
+  DS_CUDA(cudaMemsetAsync(dY.p, 0, (size_t)n * NO * sizeof(float), st));
+  // warm-start loss
+  const unsigned gb = grid1(n);
+  k_xloss_part<<<gb, 256, 0, st>>>(n, Y.p, NO, ystar, dpart.p);
+  DS_CHECK_LAUNCH();
+  std::vector<double> hp(2 * (size_t)gb);
+  DS_CUDA(cudaMemcpyAsync(hp.data(), dpart.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                          st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  double e2 = 0.0, t2 = 0.0;
+  for (unsigned b = 0; b < gb; ++b) {
+    e2 += hp[2 * b];
+    t2 += hp[2 * b + 1];
+  }
+  require(t2 > 0.0, "the target solution is zero");
+  const double tot[2] = {e2, t2};
+  DS_CUDA(cudaMemcpyAsync(dpart.p, tot, sizeof(tot), cudaMemcpyHostToDevice, st));
+  k_xloss_grad<<<gb, 256, 0, st>>>(n, Y.p, NO, ystar, dpart.p, wx, dY.p);
+  DS_CHECK_LAUNCH();
+  DS_CUDA(cudaStreamSynchronize(st));  // tot is on this stack frame
+  // preconditioner loss
+  const size_t shm = (size_t)n_per * (6 + B + 1) * sizeof(float);
+  k_ploss<<<n_sk, n_per, shm, st>>>(n_per, B, n, kc.var_s, kc.c_para, rec, Y.p, probe, wp, dY.p,
+                                     dpart.p);
+  DS_CHECK_LAUNCH();
+  std::vector<double> lp(n_sk);
+  DS_CUDA(cudaMemcpyAsync(lp.data(), dpart.p, n_sk * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  double pl = 0.0;
+  for (double v : lp) pl += v;
+  losses[0] = wx * e2 / t2;
+  losses[1] = pl;
+  backward(n_sk, n_per);
+}
+
+void LearnedNet::backward(int n_sk, int n_per) {
+  cudaStream_t st = ctx->stream;
+  const int n = n_sk * n_per;
+  // head: dW_o = h4^T dY, dh4 = dY W_o^T
+  grad_w(n, H, NO, h[N_LAYERS].p, H, dY.p, W_o, b_o);
+  {
+    const dim3 grid((H + 63) / 64, (n + 63) / 64);
+    const __nv_bfloat16* Wp = reinterpret_cast<const __nv_bfloat16*>(wbf.p) + W_o.off;
+    k_gemm<true, 0><<<grid, 256, 0, st>>>(n, H, NO, dY.p, NO, Wp, NO, nullptr, nullptr, dh.p,
+                                          nullptr, H);
+    DS_CHECK_LAUNCH();
+  }
+  for (int l = N_LAYERS - 1; l >= 0; --l) {
+    // h_{l+1} = h_l + relu(Z_{l+1}), Z_{l+1} = cat_l W_l + b_l
+    k_relu_bwd<<<grid1((size_t)n * H), 256, 0, st>>>((size_t)n * H, dh.p, Z[l + 1].p, dZ.p);
+    DS_CHECK_LAUNCH();
+    grad_w(n, 3 * H, H, cat[l].p, 3 * H, dZ.p, W_l[l], b_l[l]);
+    const dim3 grid((3 * H + 63) / 64, (n + 63) / 64);
+    const __nv_bfloat16* Wp = reinterpret_cast<const __nv_bfloat16*>(wbf.p) + W_l[l].off;
+    k_gemm<true, 0><<<grid, 256, 0, st>>>(n, 3 * H, H, dZ.p, H, Wp, H, nullptr, nullptr, dcat.p,
+                                          nullptr, 3 * H);
+    DS_CHECK_LAUNCH();
+    // dh_l = dh_{l+1} (residual) + aggregation adjoint of dcat
+    DS_CUDA(cudaMemcpyAsync(dh2.p, dh.p, (size_t)n * H * sizeof(float), cudaMemcpyDeviceToDevice,
+                            st));
+    k_agg_bwd<<<grid1((size_t)n * H), 256, 0, st>>>(n, n_per, H, dcat.p, nbr.p, gw.p, dh2.p);
+    DS_CHECK_LAUNCH();
+    std::swap(dh, dh2);
+  }
+  // embed: h0 = relu(Z0)
+  k_relu_bwd<<<grid1((size_t)n * H), 256, 0, st>>>((size_t)n * H, dh.p, Z[0].p, dZ.p);
+  DS_CHECK_LAUNCH();
+  grad_w(n, F_IN, H, X.p, F_IN, dZ.p, W_in, b_in);
+}
+
+void LearnedNet::adam_step(float lr) {
+  ++step;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - std::pow(b1, (float)step), bc2 = 1.f - std::pow(b2, (float)step);
+  k_adam<<<grid1(n_params), 256, 0, ctx->stream>>>(n_params, lr, b1, b2, 1e-8f, bc1, bc2,
+                                                   params.p, grads.p, adam_m.p, adam_v.p);
+  DS_CHECK_LAUNCH();
+  sync_weights();
+}
+
+void SkewerPCDeleter::operator()(SkewerPC* p) const { delete p; }
+
+}  // namespace ds
+
+using namespace ds;
+
+namespace {
+
+constexpr char MAGIC[4] = {'D', 'S', 'L', 'N'};
+constexpr int FILE_VERSION = 1;
+
+}  // namespace
+
+extern "C" {
+
+int ds_operator_set_skewer_preconditioner(ds_operator* op, int n_skewers, int n_per, int band,
+                                          const float* L_rows) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    if (!L_rows) {
+      op->pc.reset();
+      return;
+    }
+    require(n_skewers > 0 && n_per > 0 && n_per <= 1024 && (long long)n_skewers * n_per == op->n,
+            "n_skewers x n_per must equal the operator's record count (n_per <= 1024)");
+    require(band >= 0 && band < n_per, "band must be in [0, n_per)");
+    std::unique_ptr<SkewerPC, SkewerPCDeleter> pc(new SkewerPC());
+    pc->n_sk = n_skewers;
+    pc->n_per = n_per;
+    pc->band = band;
+    pc->L.alloc((size_t)op->n * (band + 1));
+    DS_CUDA(cudaMemcpyAsync(pc->L.p, L_rows, pc->L.bytes(), cudaMemcpyDefault, op->ctx->stream));
+    DS_CUDA(cudaStreamSynchronize(op->ctx->stream));
+    op->pc = std::move(pc);
+  });
+}
+
+int ds_learned_create(ds_context* ctx, const ds_kernel_params* kp, int hidden, int band,
+                      unsigned seed, ds_learned** out) {
+  if (!ctx || !kp || !out) return DS_ERR_ARG;
+  *out = nullptr;
+  auto h = std::make_unique<ds_learned>();
+  const int rc = guarded(ctx, [&] {
+    require(kp->eval == DS_EVAL_EXACT, "the learned preconditioner uses the exact kernel");
+    DS_CUDA(cudaSetDevice(ctx->device));
+    h->net.reset(new LearnedNet(ctx, hidden, band, make_consts(*kp), seed));
+  });
+  if (rc != DS_OK) return rc;
+  *out = h.release();
+  return DS_OK;
+}
+
+void ds_learned_destroy(ds_learned* h) { delete h; }
+
+int ds_learned_num_params(ds_learned* h, long long* n) {
+  if (!h || !n) return DS_ERR_ARG;
+  *n = (long long)h->net->n_params;
+  return DS_OK;
+}
+
+static int learned_copy(ds_learned* h, float* dst, const float* src, bool to_host,
+                        bool sync_after) {
+  if (!h || !(to_host ? dst : src)) return DS_ERR_ARG;
+  LearnedNet& net = *h->net;
+  return guarded(net.ctx, [&] {
+    cudaStream_t st = net.ctx->stream;
+    const size_t bytes = net.n_params * sizeof(float);
+    if (to_host) {
+      DS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    } else {
+      DS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+      if (sync_after) net.sync_weights();
+    }
+    DS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int ds_learned_get_params(ds_learned* h, float* params) {
+  return h ? learned_copy(h, params, h->net->params.p, true, false) : DS_ERR_ARG;
+}
+
+int ds_learned_set_params(ds_learned* h, const float* params) {
+  return h ? learned_copy(h, h->net->params.p, params, false, true) : DS_ERR_ARG;
+}
+
+int ds_learned_get_grads(ds_learned* h, float* grads) {
+  return h ? learned_copy(h, grads, h->net->grads.p, true, false) : DS_ERR_ARG;
+}
+
+int ds_learned_save(ds_learned* h, const char* path) {
+  if (!h || !path) return DS_ERR_ARG;
+  LearnedNet& net = *h->net;
+  return guarded(net.ctx, [&] {
+    std::vector<float> p(net.n_params);
+    DS_CUDA(cudaMemcpy(p.data(), net.params.p, p.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    FILE* f = fopen(path, "wb");
+    require(f != nullptr, "cannot open the weight file for writing");
+    const int hdr[3] = {FILE_VERSION, net.H, net.B};
+    const long long np = (long long)net.n_params;
+    const bool ok = fwrite(MAGIC, 1, 4, f) == 4 && fwrite(hdr, sizeof(int), 3, f) == 3 &&
+                    fwrite(&np, sizeof(np), 1, f) == 1 &&
+                    fwrite(p.data(), sizeof(float), p.size(), f) == p.size();
+    fclose(f);
+    require(ok, "writing the weight file failed");
+  });
+}
+
+int ds_learned_load(ds_learned* h, const char* path) {
+  if (!h || !path) return DS_ERR_ARG;
+  LearnedNet& net = *h->net;
+  return guarded(net.ctx, [&] {
+    FILE* f = fopen(path, "rb");
+    require(f != nullptr, "cannot open the weight file");
+    char magic[4] = {0, 0, 0, 0};
+    int hdr[3] = {0, 0, 0};
+    long long np = 0;
+    std::vector<float> p(net.n_params);
+    const bool ok = fread(magic, 1, 4, f) == 4 && std::memcmp(magic, MAGIC, 4) == 0 &&
+                    fread(hdr, sizeof(int), 3, f) == 3 && hdr[0] == FILE_VERSION &&
+                    hdr[1] == net.H && hdr[2] == net.B && fread(&np, sizeof(np), 1, f) == 1 &&
+                    np == (long long)net.n_params &&
+                    fread(p.data(), sizeof(float), p.size(), f) == p.size();
+    fclose(f);
+    require(ok, "the weight file does not match this network (format, width or band)");
+    DS_CUDA(cudaMemcpy(net.params.p, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice));
+    net.sync_weights();
+    DS_CUDA(cudaStreamSynchronize(net.ctx->stream));
+  });
+}
+
+int ds_learned_forward_dev(ds_learned* h, int n_skewers, int n_per, const double* records,
+                           double* y0, float* L_rows) {
+  if (!h || !records || !L_rows) return DS_ERR_ARG;
+  LearnedNet& net = *h->net;
+  return guarded(net.ctx, [&] {
+    net.forward(n_skewers, n_per, records);
+    net.outputs(n_skewers, n_per, y0, L_rows);
+  });
+}
+
+int ds_learned_train_step_dev(ds_learned* h, int n_skewers, int n_per, const double* records,
+                              const double* y_star, const float* probe, float lr, float w_x,
+                              float w_p, int update, double* losses) {
+  if (!h || !records || !y_star || !probe || !losses) return DS_ERR_ARG;
+  LearnedNet& net = *h->net;
+  return guarded(net.ctx, [&] {
+    net.loss_and_grad(n_skewers, n_per, records, y_star, probe, w_x, w_p, losses);
+    if (update) net.adam_step(lr);
+  });
+}
+
+}  // extern "C"

@@ -21,6 +21,7 @@
 
 #include "ds_device.cuh"
 #include "ds_f32.h"
+#include "ds_learned.h"
 #include "ds_ops.h"
 
 namespace ds {
@@ -283,6 +284,143 @@ __global__ void __launch_bounds__(VB) k_mx_dir_update(int n, MixedState* st,
   }
 }
 
+// ---- skewer-band preconditioner (M^-1 = L L^T per skewer) ------------------------
+// The solve is the same reliable-update iteration; z = M^-1 r moves out of
+// the fused update kernels into k_pc_apply (one CTA per skewer), and the
+// scalar bookkeeping of K2 / K6 / init into k_pc_finish.
+
+// MODE 0 (K2a): x_c += alpha p; r -= alpha q; partial |r|^2.
+// MODE 1 (K6a): r = float(r64) where an update is pending; partial |r64|^2.
+// MODE 2 (init): r = float(b or r64); x_c = 0; partial |r|^2.
+template <int MODE>
+__global__ void __launch_bounds__(VB) k_pc_resid(int n, const MixedState* st, const int* x_zero,
+                                                 float* __restrict__ xc, float* __restrict__ r,
+                                                 const float* __restrict__ p,
+                                                 const float* __restrict__ q,
+                                                 const double* __restrict__ b,
+                                                 const double* __restrict__ r64,
+                                                 double* __restrict__ part) {
+  if (MODE == 0 && st->done) return;
+  if (MODE == 1 && (st->done || !st->need_update)) return;
+  __shared__ double red[VB / 32];
+  const float alpha = MODE == 0 ? (float)st->alpha : 0.f;
+  const bool zero = MODE == 2 && *x_zero != 0;
+  double rr = 0.0;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
+    double rd;
+    float ri;
+    if (MODE == 0) {
+      xc[i] = fmaf(alpha, p[i], xc[i]);
+      ri = fmaf(-alpha, q[i], r[i]);
+      rd = ri;
+    } else {
+      rd = zero ? b[i] : r64[i];
+      ri = (float)rd;
+      if (MODE == 2) xc[i] = 0.f;
+    }
+    r[i] = ri;
+    rr = fma(rd, rd, rr);
+  }
+  const double s = block_sum<VB>(rr, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// z = L L^T r over one skewer (n_per threads); the records of skewer s are
+// s n_per .. s n_per + n_per - 1, at sorted positions inv[record].  Partial
+// r.z per skewer; with SET_P also p = z.
+template <bool SET_P>
+__global__ void k_pc_apply(int n_per, int band, int gate, const MixedState* st,
+                           const int* __restrict__ inv, const float* __restrict__ L,
+                           const float* __restrict__ r, float* __restrict__ z,
+                           float* __restrict__ p, double* __restrict__ part) {
+  if (gate == 0 && st->done) return;
+  if (gate == 1 && (st->done || !st->need_update)) return;
+  extern __shared__ float pcs[];
+  float* rs = pcs;           // r of the skewer
+  float* ts = pcs + n_per;   // L^T r
+  const int s = blockIdx.x, k = threadIdx.x;
+  const int rec = s * n_per + k;
+  const int pos = inv[rec];
+  const float* Lk = L + (size_t)rec * (band + 1);
+  rs[k] = r[pos];
+  __syncthreads();
+  float t = 0.f;
+  for (int m = 0; m <= band; ++m)
+    if (k + m < n_per) t = fmaf(L[(size_t)(rec + m) * (band + 1) + m], rs[k + m], t);
+  ts[k] = t;
+  __syncthreads();
+  float zk = 0.f;
+  for (int m = 0; m <= band; ++m)
+    if (k - m >= 0) zk = fmaf(Lk[m], ts[k - m], zk);
+  z[pos] = zk;
+  if (SET_P) p[pos] = zk;
+  // r.z of the skewer (n_per need not be a multiple of 32: a shared-memory
+  // sum in order)
+  __syncthreads();
+  ts[k] = rs[k] * zk;
+  __syncthreads();
+  if (k == 0) {
+    double a = 0.0;
+    for (int j = 0; j < n_per; ++j) a += (double)ts[j];
+    part[s] = a;
+  }
+}
+
+// Scalar step after k_pc_resid + k_pc_apply: rr from n_rr block partials,
+// rz from n_rz skewer partials (one block, fixed order).
+// MODE 0: the K2 bookkeeping; 1: the K6 bookkeeping; 2: init.
+template <int MODE>
+__global__ void __launch_bounds__(VB) k_pc_finish(int n_rr, const double* __restrict__ prr,
+                                                  int n_rz, const double* __restrict__ prz,
+                                                  MixedState* st, double* hist, double* htrue) {
+  if (MODE == 0 && st->done) return;
+  if (MODE == 1 && (st->done || !st->need_update)) return;
+  __shared__ double red[VB / 32];
+  const double trr = reduce_partials<VB>(prr, n_rr, 1, 0, red);
+  const double trz = reduce_partials<VB>(prz, n_rz, 1, 0, red);
+  if (threadIdx.x != 0) return;
+  if (MODE == 2) {
+    st->rz = trz;
+    st->rnorm = st->rtrue = st->rmax = sqrt(trr);
+    st->iter = 0;
+    st->n_updates = 0;
+    st->need_update = 0;
+    st->skip_update = 1;
+    hist[0] = st->rtrue;
+    htrue[0] = st->rtrue;
+    st->converged = st->rtrue <= st->tol_norm_b ? 1 : 0;
+    st->done = (st->converged || st->max_iter <= 0) ? 1 : 0;
+  } else if (MODE == 0) {
+    st->rz_old = st->rz;
+    st->rz = trz;
+    st->rnorm = sqrt(trr);
+    const int it = st->iter + 1;
+    st->iter = it;
+    hist[it] = st->rnorm;
+    st->rmax = fmax(st->rmax, st->rnorm);
+    const bool upd = st->rnorm < st->delta * st->rmax || st->rnorm <= st->tol_norm_b ||
+                     it >= st->max_iter;
+    st->need_update = upd ? 1 : 0;
+    st->skip_update = upd ? 0 : 1;
+    st->beta = st->rz / st->rz_old;
+  } else {
+    const double rt = sqrt(trr);
+    st->rtrue = rt;
+    htrue[++st->n_updates] = rt;
+    hist[st->iter] = rt;
+    if (rt <= st->tol_norm_b) {
+      st->done = 1;
+      st->converged = 1;
+    } else if (st->iter >= st->max_iter) {
+      st->done = 1;
+    } else {
+      st->rz = trz;
+      st->beta = trz / st->rz_old;
+      st->rmax = rt;
+    }
+  }
+}
+
 }  // namespace
 
 void build_f32_points(F32Points& fp, const PointSet& ps, double sx, double sy, double sz,
@@ -407,9 +545,25 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       launch_pair_f64(op->kc, EPI_RESIDUAL, pa, st);
   };
   outer_residual(resid);
-  k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p, f.xc.p,
-                              f.pdiag.p, op->partial.p, f.hist.p, f.htrue.p);
-  DS_CHECK_LAUNCH();
+  const SkewerPC* pc = op->pc.get();
+  const size_t pc_smem = pc ? 2 * (size_t)pc->n_per * sizeof(float) : 0;
+  if (pc) {
+    DS_CUDA(cudaMemsetAsync(f.z.p, 0, np * sizeof(float), st));  // padding stays 0
+    k_pc_resid<2><<<g, VB, 0, st>>>(np, S, xzero, f.xc.p, f.r.p, nullptr, nullptr, op->b.p,
+                                    op->r.p, op->partial.p);
+    DS_CHECK_LAUNCH();
+    k_pc_apply<true><<<pc->n_sk, pc->n_per, pc_smem, st>>>(pc->n_per, pc->band, -1, S, op->inv.p,
+                                                          pc->L.p, f.r.p, f.z.p, f.p.p,
+                                                          op->partial2.p);
+    DS_CHECK_LAUNCH();
+    k_pc_finish<2><<<1, VB, 0, st>>>(g, op->partial.p, pc->n_sk, op->partial2.p, S, f.hist.p,
+                                     f.htrue.p);
+    DS_CHECK_LAUNCH();
+  } else {
+    k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p, f.xc.p,
+                                f.pdiag.p, op->partial.p, f.hist.p, f.htrue.p);
+    DS_CHECK_LAUNCH();
+  }
 
   F32Args prod = op_f32_args(op, f.p.p, f.q.p);
   prod.dotv = f.p.p;
@@ -427,19 +581,46 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   cudaEvent_t evs[NSLOT];
   for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   int issued = 0, waited = 0;
+  // partial2 holds the p.q partials of K1 (one per row tile) and, in the
+  // preconditioned form, the r.z partials per skewer after them.
+  double* pc_rz = op->partial2.p + op->pix.n_tiles;
   for (int it = 1; it <= max_iter; ++it) {
     launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);                       // K1
-    k_mx_update<<<g, VB, 0, st>>>(np, S, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
-                                  op->partial.p, f.hist.p);                  // K2
-    DS_CHECK_LAUNCH();
+    if (pc) {
+      k_pc_resid<0><<<g, VB, 0, st>>>(np, S, xzero, f.xc.p, f.r.p, f.p.p, f.q.p, nullptr,
+                                      nullptr, op->partial.p);                // K2a
+      DS_CHECK_LAUNCH();
+      k_pc_apply<false><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
+          pc->n_per, pc->band, 0, S, op->inv.p, pc->L.p, f.r.p, f.z.p, nullptr, pc_rz);
+      DS_CHECK_LAUNCH();
+      k_pc_finish<0><<<1, VB, 0, st>>>(g, op->partial.p, pc->n_sk, pc_rz, S, f.hist.p,
+                                       f.htrue.p);                           // K2b
+      DS_CHECK_LAUNCH();
+    } else {
+      k_mx_update<<<g, VB, 0, st>>>(np, S, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
+                                    op->partial.p, f.hist.p);                // K2
+      DS_CHECK_LAUNCH();
+    }
     k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K3
     DS_CHECK_LAUNCH();
     k_mx_fold<<<g, VB, 0, st>>>(np, S, op->x.p, f.xc.p);                    // K4
     DS_CHECK_LAUNCH();
     outer_residual(upd);                                                      // K5
-    k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,
-                                   f.hist.p, f.htrue.p);                     // K6
-    DS_CHECK_LAUNCH();
+    if (pc) {
+      k_pc_resid<1><<<g, VB, 0, st>>>(np, S, xzero, f.xc.p, f.r.p, nullptr, nullptr, nullptr,
+                                      op->r.p, op->partial.p);                // K6a
+      DS_CHECK_LAUNCH();
+      k_pc_apply<false><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
+          pc->n_per, pc->band, 1, S, op->inv.p, pc->L.p, f.r.p, f.z.p, nullptr, pc_rz);
+      DS_CHECK_LAUNCH();
+      k_pc_finish<1><<<1, VB, 0, st>>>(g, op->partial.p, pc->n_sk, pc_rz, S, f.hist.p,
+                                       f.htrue.p);                           // K6b
+      DS_CHECK_LAUNCH();
+    } else {
+      k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,
+                                     f.hist.p, f.htrue.p);                   // K6
+      DS_CHECK_LAUNCH();
+    }
     k_mx_dir_update<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                 // K7
     DS_CHECK_LAUNCH();
     if (it % CHECK == 0) {

@@ -346,6 +346,57 @@ int ds_batch_solve_mixed_dev(ds_batch* batch, const ds_mixed_params* mp,
  * testing the variants against each other and against the FP64 operator. */
 int ds_batch_product_f32_dev(ds_batch* batch, const double* p, double* q);
 
+/* ---- learned warm start + skewer-band preconditioner (no reference
+ * counterpart) ------------------------------------------------------------
+ * For skewer-structured pixel sets (n_skewers skewers of n_per pixels that
+ * share one z grid; records skewer-contiguous, record s n_per + k is pixel
+ * k of skewer s): a 4-layer message-passing network over each skewer and its
+ * 8 nearest neighbour skewers (inputs z, noise, w d and the perpendicular
+ * distances; hidden width `hidden`, BF16 weights with FP32 arithmetic)
+ * predicts a warm start y0 of the W-form system (I + w S w) y = w d and per
+ * skewer a lower-triangular band factor L (bandwidth `band`, positive
+ * diagonal) whose M^-1 = L L^T preconditions that skewer's block.  Trained
+ * by its own forward / backward / Adam kernels on solutions of the solver;
+ * the mixed-precision PCG then runs to the same tolerance from y0 with
+ * M^-1 (Jacobi-PCG stays the fallback and the judge of its error). */
+typedef struct ds_learned ds_learned;
+
+/* kp: the kernel parameters of the systems it is trained for (exact). */
+int ds_learned_create(ds_context* ctx, const ds_kernel_params* kp, int hidden,
+                      int band, unsigned seed, ds_learned** out);
+void ds_learned_destroy(ds_learned* net);
+int ds_learned_num_params(ds_learned* net, long long* n);
+/* Flat FP32 parameter vector (W_in, b_in, W_1, b_1, .., W_4, b_4, W_o, b_o;
+ * W row-major [inputs x outputs]); host arrays of ds_learned_num_params. */
+int ds_learned_get_params(ds_learned* net, float* params);
+int ds_learned_set_params(ds_learned* net, const float* params);
+/* Gradients of the last ds_learned_train_step_dev, same layout. */
+int ds_learned_get_grads(ds_learned* net, float* grads);
+/* Weight file: "DSLN", int32 version 1, hidden, band, int64 n, n FP32. */
+int ds_learned_save(ds_learned* net, const char* path);
+int ds_learned_load(ds_learned* net, const char* path);
+/* records: device WPixel records (x, y, z, w, w d), n = n_skewers n_per.
+ * y0 (device, n doubles, may be NULL): warm start in the operator's unscaled
+ * variable y; L_rows (device, n x (band + 1) floats): row k of skewer s
+ * holds L[k][k - m] at m = 0..band (zero outside the skewer). */
+int ds_learned_forward_dev(ds_learned* net, int n_skewers, int n_per,
+                           const double* records, double* y0, float* L_rows);
+/* One training step on one system: y_star (device) its solution y, probe
+ * (device, n floats) the probe vector of the preconditioner loss.  losses[0]
+ * = w_x sum (y0 - y*)^2 / sum y*^2, losses[1] = w_p sum |L L^T A_bb v - v|^2
+ * / n over the skewers' own blocks A_bb.  update != 0 applies an Adam step
+ * with learning rate lr. */
+int ds_learned_train_step_dev(ds_learned* net, int n_skewers, int n_per,
+                              const double* records, const double* y_star,
+                              const float* probe, float lr, float w_x,
+                              float w_p, int update, double* losses);
+/* Installs (L_rows != NULL, host or device, copied) or removes (NULL) the
+ * skewer-band preconditioner M^-1 = L L^T of the operator's mixed-precision
+ * solves (ds_solve_mixed*); n_skewers n_per must equal the operator's n. */
+int ds_operator_set_skewer_preconditioner(ds_operator* op, int n_skewers,
+                                          int n_per, int band,
+                                          const float* L_rows);
+
 /* ---- map projection ----------------------------------------------------- */
 typedef struct ds_map ds_map;
 
