@@ -88,6 +88,9 @@ struct MixedState {
   double norm_b;
   double tol_norm_b;
   double delta;       // reliable-update trigger: |r| < delta * rmax
+  double rbest;       // smallest |r| since the last halving (stagnation test)
+  int it_best;        // iteration of rbest
+  int stalled;        // the pending update was triggered by stagnation
   int iter;           // FP32 iterations done
   int max_iter;
   int done;

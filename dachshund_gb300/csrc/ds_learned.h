@@ -23,6 +23,7 @@ struct LearnedNet {
   DevBuf<unsigned short> wbf;  // BF16 copy of the parameters (forward weights)
   long long step = 0;
   // per-geometry work space
+  const double* rec_cur = nullptr;  // records of the last forward (device)
   size_t n_cur = 0;
   int nsk_cur = 0;
   DevBuf<int> nbr;

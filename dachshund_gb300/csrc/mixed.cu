@@ -11,8 +11,9 @@
 // A reliable update folds x_c into x, recomputes r64 in FP64 and restarts the
 // recurrence from float(r64) while keeping the search direction.  It fires
 // when the recurrence residual has dropped by `delta` since the last update,
-// when it reaches tol |b|, or at the iteration cap; the solve ends only on an
-// FP64 residual.  Per iteration: K1 q = A32 p (+ p.q, alpha), K2 the
+// when it reaches tol |b|, at the iteration cap, or when the recurrence
+// stagnates (then the direction is dropped, beta = 0); the solve ends only on
+// an FP64 residual.  Per iteration: K1 q = A32 p (+ p.q, alpha), K2 the
 // recurrences, K3 the new direction; K4-K7 run only on update iterations
 // (otherwise they return at once on a device flag).
 #include <algorithm>
@@ -97,6 +98,32 @@ __global__ void k_d2f(int n, const double* __restrict__ in, float* __restrict__ 
 
 // ---- the iteration kernels -----------------------------------------------
 
+// Reliable-update decision after iteration `it` (st->rnorm, st->rmax set):
+// the recurrence residual fell by delta since the last update, reached
+// tol |b|, hit the iteration cap, or stagnated (did not halve in STALL_ITERS
+// iterations, which FP32 rounding can cause far from x or near tol; the
+// update then restarts the recurrence with beta = 0).
+constexpr int STALL_ITERS = 30;
+__device__ __forceinline__ bool update_due(MixedState* st, int it) {
+  if (st->rnorm < 0.5 * st->rbest) {
+    st->rbest = st->rnorm;
+    st->it_best = it;
+  }
+  const bool stall = it - st->it_best >= STALL_ITERS;
+  if (stall) st->stalled = 1;
+  return st->rnorm < st->delta * st->rmax || st->rnorm <= st->tol_norm_b ||
+         it >= st->max_iter || stall;
+}
+
+// Recurrence restart after an FP64 update that did not end the solve.
+__device__ __forceinline__ void restart_after_update(MixedState* st, double rt, double rz) {
+  st->beta = st->stalled ? 0.0 : rz / st->rz_old;
+  st->rmax = rt;
+  st->rbest = rt;
+  st->it_best = st->iter;
+  st->stalled = 0;
+}
+
 // Zero test of the initial guess: flag = 1 when every entry is 0.
 __global__ void k_is_zero(int n, const double* __restrict__ x, int* __restrict__ flag) {
   for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB)
@@ -137,7 +164,9 @@ __global__ void __launch_bounds__(VB) k_mx_init(int n, MixedState* st, const int
     const double trr = reduce_partials<VB>(part, gridDim.x, 2, 1, red);
     if (threadIdx.x == 0) {
       st->rz = trz;
-      st->rnorm = st->rtrue = st->rmax = sqrt(trr);
+      st->rnorm = st->rtrue = st->rmax = st->rbest = sqrt(trr);
+      st->it_best = 0;
+      st->stalled = 0;
       st->iter = 0;
       st->n_updates = 0;
       st->need_update = 0;
@@ -188,8 +217,7 @@ __global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, float* 
       st->iter = it;
       hist[it] = st->rnorm;
       st->rmax = fmax(st->rmax, st->rnorm);
-      const bool upd = st->rnorm < st->delta * st->rmax || st->rnorm <= st->tol_norm_b ||
-                       it >= st->max_iter;
+      const bool upd = update_due(st, it);
       st->need_update = upd ? 1 : 0;
       st->skip_update = upd ? 0 : 1;
       st->beta = st->rz / st->rz_old;
@@ -259,8 +287,7 @@ __global__ void __launch_bounds__(VB) k_mx_replace(int n, MixedState* st,
         st->done = 1;
       } else {
         st->rz = trz;  // rz_old keeps the previous iteration's r.z
-        st->beta = trz / st->rz_old;
-        st->rmax = rt;
+        restart_after_update(st, rt, trz);
       }
       st->counter[1] = 0;
     }
@@ -285,103 +312,94 @@ __global__ void __launch_bounds__(VB) k_mx_dir_update(int n, MixedState* st,
 }
 
 // ---- skewer-band preconditioner (M^-1 = L L^T per skewer) ------------------------
-// The solve is the same reliable-update iteration; z = M^-1 r moves out of
-// the fused update kernels into k_pc_apply (one CTA per skewer), and the
-// scalar bookkeeping of K2 / K6 / init into k_pc_finish.
+// The same reliable-update iteration with z = M^-1 r over each skewer: one CTA
+// per skewer (n_per threads, thread k = pixel k of the skewer at sorted
+// position inv[record]) updates r, forms z = L L^T r from the skewer's r in
+// shared memory, writes the skewer's r.z and |r|^2 partials, and the last CTA
+// to finish does the scalar bookkeeping of K2 (MODE 0), K6 (MODE 1) or the
+// start (MODE 2).  Padding positions belong to no skewer and stay 0.
 
-// MODE 0 (K2a): x_c += alpha p; r -= alpha q; partial |r|^2.
-// MODE 1 (K6a): r = float(r64) where an update is pending; partial |r64|^2.
-// MODE 2 (init): r = float(b or r64); x_c = 0; partial |r|^2.
-template <int MODE>
-__global__ void __launch_bounds__(VB) k_pc_resid(int n, const MixedState* st, const int* x_zero,
-                                                 float* __restrict__ xc, float* __restrict__ r,
-                                                 const float* __restrict__ p,
-                                                 const float* __restrict__ q,
-                                                 const double* __restrict__ b,
-                                                 const double* __restrict__ r64,
-                                                 double* __restrict__ part) {
-  if (MODE == 0 && st->done) return;
-  if (MODE == 1 && (st->done || !st->need_update)) return;
-  __shared__ double red[VB / 32];
-  const float alpha = MODE == 0 ? (float)st->alpha : 0.f;
-  const bool zero = MODE == 2 && *x_zero != 0;
-  double rr = 0.0;
-  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
-    double rd;
-    float ri;
-    if (MODE == 0) {
-      xc[i] = fmaf(alpha, p[i], xc[i]);
-      ri = fmaf(-alpha, q[i], r[i]);
-      rd = ri;
-    } else {
-      rd = zero ? b[i] : r64[i];
-      ri = (float)rd;
-      if (MODE == 2) xc[i] = 0.f;
-    }
-    r[i] = ri;
-    rr = fma(rd, rd, rr);
+// Sum of v over the CTA (any blockDim <= 1024), valid in thread 0.
+__device__ __forceinline__ double cta_sum(double v, double* sm) {
+  const int t = threadIdx.x, n = blockDim.x;
+  __syncthreads();
+  sm[t] = v;
+  __syncthreads();
+  if (t < 32) {
+    double a = 0.0;
+    for (int k = t; k < n; k += 32) a += sm[k];
+    sm[t] = a;
   }
-  const double s = block_sum<VB>(rr, red);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  __syncthreads();
+  double s = 0.0;
+  if (t == 0)
+    for (int k = 0; k < min(32, n); ++k) s += sm[k];
+  return s;
 }
 
-// z = L L^T r over one skewer (n_per threads); the records of skewer s are
-// s n_per .. s n_per + n_per - 1, at sorted positions inv[record].  Partial
-// r.z per skewer; with SET_P also p = z.
-template <bool SET_P>
-__global__ void k_pc_apply(int n_per, int band, int gate, const MixedState* st,
-                           const int* __restrict__ inv, const float* __restrict__ L,
-                           const float* __restrict__ r, float* __restrict__ z,
-                           float* __restrict__ p, double* __restrict__ part) {
-  if (gate == 0 && st->done) return;
-  if (gate == 1 && (st->done || !st->need_update)) return;
-  extern __shared__ float pcs[];
-  float* rs = pcs;           // r of the skewer
-  float* ts = pcs + n_per;   // L^T r
+template <int MODE>
+__global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero,
+                          const int* __restrict__ inv, const float* __restrict__ L,
+                          float* __restrict__ xc, float* __restrict__ r,
+                          float* __restrict__ z, float* __restrict__ p,
+                          const float* __restrict__ q, const double* __restrict__ b,
+                          const double* __restrict__ r64, double* __restrict__ part, double* hist,
+                          double* htrue) {
+  if (MODE == 0 && st->done) return;
+  if (MODE == 1 && (st->done || !st->need_update)) return;
+  extern __shared__ double pcd[];  // [n_per] reduction scratch, then floats
+  float* rs = reinterpret_cast<float*>(pcd + n_per);  // r of the skewer
+  float* ts = rs + n_per;                              // L^T r
   const int s = blockIdx.x, k = threadIdx.x;
   const int rec = s * n_per + k;
   const int pos = inv[rec];
-  const float* Lk = L + (size_t)rec * (band + 1);
-  rs[k] = r[pos];
+  double rd;
+  float ri;
+  if (MODE == 0) {
+    const float alpha = (float)st->alpha;
+    xc[pos] = fmaf(alpha, p[pos], xc[pos]);
+    ri = fmaf(-alpha, q[pos], r[pos]);
+    rd = ri;
+  } else {
+    rd = (MODE == 2 && *x_zero) ? b[pos] : r64[pos];
+    ri = (float)rd;
+    if (MODE == 2) xc[pos] = 0.f;
+  }
+  r[pos] = ri;
+  rs[k] = ri;
   __syncthreads();
   float t = 0.f;
   for (int m = 0; m <= band; ++m)
     if (k + m < n_per) t = fmaf(L[(size_t)(rec + m) * (band + 1) + m], rs[k + m], t);
   ts[k] = t;
   __syncthreads();
+  const float* Lk = L + (size_t)rec * (band + 1);
   float zk = 0.f;
   for (int m = 0; m <= band; ++m)
     if (k - m >= 0) zk = fmaf(Lk[m], ts[k - m], zk);
   z[pos] = zk;
-  if (SET_P) p[pos] = zk;
-  // r.z of the skewer (n_per need not be a multiple of 32: a shared-memory
-  // sum in order)
-  __syncthreads();
-  ts[k] = rs[k] * zk;
-  __syncthreads();
+  if (MODE == 2) p[pos] = zk;
+  const double srz = cta_sum((double)ri * (double)zk, pcd);
+  const double srr = cta_sum(rd * rd, pcd);
   if (k == 0) {
-    double a = 0.0;
-    for (int j = 0; j < n_per; ++j) a += (double)ts[j];
-    part[s] = a;
+    part[2 * s] = srz;
+    part[2 * s + 1] = srr;
   }
-}
-
-// Scalar step after k_pc_resid + k_pc_apply: rr from n_rr block partials,
-// rz from n_rz skewer partials (one block, fixed order).
-// MODE 0: the K2 bookkeeping; 1: the K6 bookkeeping; 2: init.
-template <int MODE>
-__global__ void __launch_bounds__(VB) k_pc_finish(int n_rr, const double* __restrict__ prr,
-                                                  int n_rz, const double* __restrict__ prz,
-                                                  MixedState* st, double* hist, double* htrue) {
-  if (MODE == 0 && st->done) return;
-  if (MODE == 1 && (st->done || !st->need_update)) return;
-  __shared__ double red[VB / 32];
-  const double trr = reduce_partials<VB>(prr, n_rr, 1, 0, red);
-  const double trz = reduce_partials<VB>(prz, n_rz, 1, 0, red);
-  if (threadIdx.x != 0) return;
+  if (!last_block_arrive(&st->counter[3])) return;
+  double a = 0.0, c = 0.0;
+  for (int j = k; j < (int)gridDim.x; j += blockDim.x) {
+    a += __ldcg(part + 2 * j);
+    c += __ldcg(part + 2 * j + 1);
+  }
+  const double trz = cta_sum(a, pcd);
+  const double trr = cta_sum(c, pcd);
+  if (k != 0) return;
+  st->counter[3] = 0;
   if (MODE == 2) {
     st->rz = trz;
-    st->rnorm = st->rtrue = st->rmax = sqrt(trr);
+    st->rnorm = st->rtrue = st->rmax = st->rbest = sqrt(trr);
+    st->it_best = 0;
+    st->stalled = 0;
     st->iter = 0;
     st->n_updates = 0;
     st->need_update = 0;
@@ -398,8 +416,7 @@ __global__ void __launch_bounds__(VB) k_pc_finish(int n_rr, const double* __rest
     st->iter = it;
     hist[it] = st->rnorm;
     st->rmax = fmax(st->rmax, st->rnorm);
-    const bool upd = st->rnorm < st->delta * st->rmax || st->rnorm <= st->tol_norm_b ||
-                     it >= st->max_iter;
+    const bool upd = update_due(st, it);
     st->need_update = upd ? 1 : 0;
     st->skip_update = upd ? 0 : 1;
     st->beta = st->rz / st->rz_old;
@@ -415,8 +432,7 @@ __global__ void __launch_bounds__(VB) k_pc_finish(int n_rr, const double* __rest
       st->done = 1;
     } else {
       st->rz = trz;
-      st->beta = trz / st->rz_old;
-      st->rmax = rt;
+      restart_after_update(st, rt, trz);
     }
   }
 }
@@ -546,18 +562,17 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   };
   outer_residual(resid);
   const SkewerPC* pc = op->pc.get();
-  const size_t pc_smem = pc ? 2 * (size_t)pc->n_per * sizeof(float) : 0;
+  const size_t pc_smem = pc ? (size_t)pc->n_per * (sizeof(double) + 2 * sizeof(float)) : 0;
+  // partial2 holds the p.q partials of K1 (one per row tile) and, in the
+  // preconditioned form, the (r.z, |r|^2) partials per skewer after them.
+  double* pc_part = op->partial2.p + op->pix.n_tiles;
   if (pc) {
-    DS_CUDA(cudaMemsetAsync(f.z.p, 0, np * sizeof(float), st));  // padding stays 0
-    k_pc_resid<2><<<g, VB, 0, st>>>(np, S, xzero, f.xc.p, f.r.p, nullptr, nullptr, op->b.p,
-                                    op->r.p, op->partial.p);
-    DS_CHECK_LAUNCH();
-    k_pc_apply<true><<<pc->n_sk, pc->n_per, pc_smem, st>>>(pc->n_per, pc->band, -1, S, op->inv.p,
-                                                          pc->L.p, f.r.p, f.z.p, f.p.p,
-                                                          op->partial2.p);
-    DS_CHECK_LAUNCH();
-    k_pc_finish<2><<<1, VB, 0, st>>>(g, op->partial.p, pc->n_sk, op->partial2.p, S, f.hist.p,
-                                     f.htrue.p);
+    // padding stays 0 in every FP32 vector
+    for (float* v : {f.z.p, f.r.p, f.p.p, f.xc.p})
+      DS_CUDA(cudaMemsetAsync(v, 0, np * sizeof(float), st));
+    k_pc_iter<2><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
+        pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, f.xc.p, f.r.p, f.z.p, f.p.p, nullptr,
+        op->b.p, op->r.p, pc_part, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   } else {
     k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p, f.xc.p,
@@ -581,20 +596,12 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   cudaEvent_t evs[NSLOT];
   for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   int issued = 0, waited = 0;
-  // partial2 holds the p.q partials of K1 (one per row tile) and, in the
-  // preconditioned form, the r.z partials per skewer after them.
-  double* pc_rz = op->partial2.p + op->pix.n_tiles;
   for (int it = 1; it <= max_iter; ++it) {
     launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);                       // K1
     if (pc) {
-      k_pc_resid<0><<<g, VB, 0, st>>>(np, S, xzero, f.xc.p, f.r.p, f.p.p, f.q.p, nullptr,
-                                      nullptr, op->partial.p);                // K2a
-      DS_CHECK_LAUNCH();
-      k_pc_apply<false><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, 0, S, op->inv.p, pc->L.p, f.r.p, f.z.p, nullptr, pc_rz);
-      DS_CHECK_LAUNCH();
-      k_pc_finish<0><<<1, VB, 0, st>>>(g, op->partial.p, pc->n_sk, pc_rz, S, f.hist.p,
-                                       f.htrue.p);                           // K2b
+      k_pc_iter<0><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
+          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p,
+          nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);                    // K2
       DS_CHECK_LAUNCH();
     } else {
       k_mx_update<<<g, VB, 0, st>>>(np, S, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
@@ -607,14 +614,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     DS_CHECK_LAUNCH();
     outer_residual(upd);                                                      // K5
     if (pc) {
-      k_pc_resid<1><<<g, VB, 0, st>>>(np, S, xzero, f.xc.p, f.r.p, nullptr, nullptr, nullptr,
-                                      op->r.p, op->partial.p);                // K6a
-      DS_CHECK_LAUNCH();
-      k_pc_apply<false><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, 1, S, op->inv.p, pc->L.p, f.r.p, f.z.p, nullptr, pc_rz);
-      DS_CHECK_LAUNCH();
-      k_pc_finish<1><<<1, VB, 0, st>>>(g, op->partial.p, pc->n_sk, pc_rz, S, f.hist.p,
-                                       f.htrue.p);                           // K6b
+      k_pc_iter<1><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
+          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, f.xc.p, f.r.p, f.z.p, f.p.p,
+          nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);           // K6
       DS_CHECK_LAUNCH();
     } else {
       k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,

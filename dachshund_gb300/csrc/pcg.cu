@@ -190,10 +190,11 @@ void ensure_pcg_workspace(ds_operator* op) {
   op->q.alloc(np);
   op->s.alloc(np);
   op->partial.alloc(std::max<size_t>(2 * VGRID_MAX, op->pix.n_tiles));
-  // + n_pad: the per-skewer r.z partials of the preconditioned mixed form
+  // + 2 n_pad: the per-skewer (r.z, |r|^2) partials of the preconditioned
+  // mixed form, after the n_tiles p.q partials
   op->partial2.alloc(std::max(std::max((size_t)2 * VGRID_MAX, (size_t)op->pix.n_tiles),
                               (size_t)dense_partials(op->pix.n_pad)) +
-                     (size_t)op->pix.n_pad);
+                     2 * (size_t)op->pix.n_pad);
   op->state.alloc(1);
   op->h_flag.alloc(64);
 }

@@ -33,7 +33,7 @@ class LearnedPreconditioner:
     """The network: hidden width ``hidden``, band ``band`` (ds_learned_create)."""
 
     def __init__(self, ctx: Context, s_params: SignalCovarParams, hidden: int = 128,
-                 band: int = 4, seed: int = 0):
+                 band: int = 2, seed: int = 0):
         self.ctx, self._lib = ctx, ctx._lib
         self.hidden, self.band = hidden, band
         kp = s_params.as_c()
@@ -282,7 +282,7 @@ def main(argv=None):
     ap.add_argument("--first", type=int, default=None)
     ap.add_argument("--last", type=int, default=None)
     ap.add_argument("--hidden", type=int, default=128)
-    ap.add_argument("--band", type=int, default=4)
+    ap.add_argument("--band", type=int, default=2)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--json", default=None, help="write the per-system results here")
     a = ap.parse_args(argv)

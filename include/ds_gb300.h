@@ -354,8 +354,10 @@ int ds_batch_product_f32_dev(ds_batch* batch, const double* p, double* q);
  * 8 nearest neighbour skewers (inputs z, noise, w d and the perpendicular
  * distances; hidden width `hidden`, BF16 weights with FP32 arithmetic)
  * predicts a warm start y0 of the W-form system (I + w S w) y = w d and per
- * skewer a lower-triangular band factor L (bandwidth `band`, positive
- * diagonal) whose M^-1 = L L^T preconditions that skewer's block.  Trained
+ * skewer a lower-triangular band factor L (bandwidth `band` = 2; diagonal =
+ * the Jacobi factor 1/sqrt(1 + w^2 var_s) times a learned factor in
+ * [1/e, e]; sub-diagonals from row polynomials inside the stability
+ * triangle) whose M^-1 = L L^T preconditions that skewer's block.  Trained
  * by its own forward / backward / Adam kernels on solutions of the solver;
  * the mixed-precision PCG then runs to the same tolerance from y0 with
  * M^-1 (Jacobi-PCG stays the fallback and the judge of its error). */

@@ -12,8 +12,10 @@ reference; it is checked here against its own definition:
            skewers (ties by skewer index)
   embed    h0 = relu(X W_in + b_in)
   layers   h_l = h_{l-1} + relu([h | A_z h | A_n h] W_l + b_l)
-  head     Y = h_4 W_o + b_o;  y0 = XS Y0,  L_kk = LD softplus(Y1) + LMIN,
-           L_{k,k-m} = RO tanh(Y_{1+m}) L_kk
+  head     Y = h_4 W_o + b_o;  y0 = XS Y0,
+           L_kk = exp(SD tanh(Y1)) / sqrt(1 + w_k^2 var_s),
+           L_{k,k-1} = a1 L_kk, L_{k,k-2} = a2 L_kk (band 2) with
+           a2 = AC tanh(Y3), a1 = AC (1 + a2) tanh(Y2)
   losses   w_x sum (y0 - y*)^2 / sum y*^2  and
            w_p sum_s |L L^T A_bb v - v|^2 / n,  A_bb = I + w S_bb w (the
            skewer's own block, exact kernel)
@@ -23,7 +25,7 @@ from __future__ import annotations
 import numpy as np
 
 F_IN, N_LAYERS, NB_K = 11, 4, 8
-XS, LD, LMIN, RO = 0.3, 0.5, 0.01, 0.5
+XS, SD, AC = 0.3, 1.0, 0.9
 LOGN0, LOGNS = -2.1, 0.6
 
 
@@ -100,21 +102,20 @@ def agg_adjoint(dcat, n_sk, n_per, nbr, g, H):
     return out.reshape(-1, H)
 
 
-def softplus(x):
-    return np.where(x > 20, x, np.log1p(np.exp(np.minimum(x, 20))))
+def jacobi_factor(rec, var_s):
+    return (1.0 / np.sqrt(1.0 + rec[:, 3] ** 2 * var_s)).astype(np.float32).astype(np.float64)
 
 
-def sigmoid(x):
-    return 1.0 / (1.0 + np.exp(-x))
-
-
-def band_L(Y, n_sk, n_per, B):
+def band_L(Y, rec, n_sk, n_per, B, var_s):
     """[n_sk, n_per, B + 1] rows of L (L[k][k - m] at m)."""
+    assert B == 2
     L = np.zeros((n_sk * n_per, B + 1))
-    L[:, 0] = LD * softplus(Y[:, 1]) + LMIN
+    L[:, 0] = jacobi_factor(rec, var_s) * np.exp(SD * np.tanh(Y[:, 1]))
+    a2 = AC * np.tanh(Y[:, 3])
+    a1 = AC * (1 + a2) * np.tanh(Y[:, 2])
     k = np.tile(np.arange(n_per), n_sk)
-    for m in range(1, B + 1):
-        L[:, m] = np.where(k - m >= 0, RO * np.tanh(Y[:, 1 + m]) * L[:, 0], 0.0)
+    L[:, 1] = np.where(k >= 1, a1 * L[:, 0], 0.0)
+    L[:, 2] = np.where(k >= 2, a2 * L[:, 0], 0.0)
     return L.reshape(n_sk, n_per, B + 1)
 
 
@@ -159,7 +160,8 @@ def losses_and_dY(Y, rec, ystar, probe, n_sk, n_per, B, var_s, c_para, w_x, w_p)
     t2 = float(np.sum(ystar ** 2))
     lx = w_x * float(np.sum((y0 - ystar) ** 2)) / t2
     dY[:, 0] = w_x * 2.0 * (y0 - ystar) * XS / t2
-    Lb = band_L(Y, n_sk, n_per, B)
+    Lb = band_L(Y, rec, n_sk, n_per, B, var_s)
+    Jf = jacobi_factor(rec, var_s)
     lp = 0.0
     for s in range(n_sk):
         sl = slice(s * n_per, (s + 1) * n_per)
@@ -176,19 +178,15 @@ def losses_and_dY(Y, rec, ystar, probe, n_sk, n_per, B, var_s, c_para, w_x, w_p)
         dLd = np.outer(gs, t) + np.outer(u, gt)  # d loss / d L[k][j]
         Ys = Y[sl]
         for k in range(n_per):
-            dk = LD * softplus(Ys[k, 1]) + LMIN
-            dd = 0.0
-            for m in range(B + 1):
-                if k - m < 0:
-                    continue
-                dl = dLd[k, k - m]
-                if m == 0:
-                    dd += dl
-                else:
-                    th = np.tanh(Ys[k, 1 + m])
-                    dd += dl * RO * th
-                    dY[s * n_per + k, 1 + m] = dl * RO * (1 - th * th) * dk
-            dY[s * n_per + k, 1] = dd * LD * sigmoid(Ys[k, 1])
+            th1, th2, th3 = np.tanh(Ys[k, 1]), np.tanh(Ys[k, 2]), np.tanh(Ys[k, 3])
+            dk = Jf[s * n_per + k] * np.exp(SD * th1)
+            a2 = AC * th3
+            a1 = AC * (1 + a2) * th2
+            dl = [dLd[k, k - m] if k - m >= 0 else 0.0 for m in range(3)]
+            i = s * n_per + k
+            dY[i, 1] = (dl[0] + dl[1] * a1 + dl[2] * a2) * dk * SD * (1 - th1 * th1)
+            dY[i, 2] = dl[1] * AC * (1 + a2) * (1 - th2 * th2) * dk
+            dY[i, 3] = (dl[1] * AC * th2 + dl[2]) * AC * (1 - th3 * th3) * dk
     assert dY.shape[1] == NO
     return (lx, lp), dY
 
