@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-chunks (512 chunks x 64 RHS) measurement")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-preconditioner measurement")
     ap.add_argument("--cpu-sample-s", type=float, default=6.0,
                     help="seconds of CPU work per baseline sample")
     return ap.parse_args()
@@ -292,6 +294,40 @@ def run_batched(ctx, n_chunks=512, n_rhs=64, seed=0, plain_samples=6):
     }
 
 
+def run_learned(ctx, seeds=(10001, 10002, 10003, 10004, 10005)):
+    """Learned warm start + skewer-band preconditioner on held-out systems of
+    the 262,144-pixel geometry (seeds outside the 1-2000 training range),
+    against Jacobi, both with the mixed-precision PCG to 1e-8; wall time of
+    the learned form includes the network's forward pass."""
+    import numpy as np
+
+    from dachshund_gb300 import SignalCovarParams, synth
+    from dachshund_gb300.learned import LearnedPreconditioner, compare
+
+    path = os.path.join(ROOT, "dachshund_gb300", "weights", "learned_wf262144.bin")
+    if not os.path.exists(path):
+        return None
+    sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
+    net = LearnedPreconditioner(ctx, sp, hidden=128, band=2)
+    net.load(path)
+    compare(net, ctx, sp, seeds[:1])  # warm-up
+    rows = compare(net, ctx, sp, seeds)
+    net.close()
+    mean = lambda k: float(np.mean([r[k] for r in rows]))  # noqa: E731
+    return {
+        "workload": "262,144 px (1,024 skewers x 256), GRF systems generated on the GPU, "
+                    f"held-out seeds {seeds[0]}-{seeds[-1]}; network trained on seeds 1-2000",
+        "jacobi_iters": mean("jacobi_iters"), "learned_iters": mean("learned_iters"),
+        "jacobi_s": mean("jacobi_s"), "learned_s": mean("learned_s"),
+        "network_forward_s": mean("net_s"),
+        "iters_ratio": mean("learned_iters") / mean("jacobi_iters"),
+        "time_ratio": mean("learned_s") / mean("jacobi_s"),
+        "warm_start_rel_err": mean("x0_rel_err"),
+        "fallbacks": int(sum(r["fallback"] for r in rows)),
+        "max_rel_residual": float(max(r["learned_rel_resid"] for r in rows)),
+    }
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import torch
@@ -456,6 +492,7 @@ def run_ours(args, rank, world, local):
     base = cpu_baseline(w, plain["iters"] if plain else REF_ITERS[w.name], args.cpu_sample_s) \
         if rank == 0 else None
     batched = None if args.no_batched else run_batched(ctx)
+    learned = None if args.no_learned else run_learned(ctx)
     if batched and batched["matvec_algorithmic_tflops"] and batched["variant"].startswith("tensor"):
         peak = measured_peaks().get("bf16_tflops")
         if peak:
@@ -488,6 +525,7 @@ def run_ours(args, rank, world, local):
             "gpu_launches": launches,
             "clocks": clk,
             "batched_chunks": batched,
+            "learned_preconditioner": learned,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
