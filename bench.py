@@ -33,12 +33,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "WF solve time & CG iters to 1e-8 resid: chosen form vs plain FP64 GPU PCG"
 SMS = 152
-# Per-SM pipe rates measured on this machine's GB300 (profiles/pipe_rates.md):
+# Per-SM pipe rates measured on this machine's GB300 (profiles/pipe_rates_gb300.md):
 # FP32 FMA 128 lanes/clk, MUFU ex2 32/clk, FP64 FMA 2/clk.
 FMA_LANES, MUFU_RATE, DFMA_RATE = 128.0, 32.0, 2.0
 # FP32 inner kernel (EXPANDED): 4 FMA lanes + 1 ex2 per pair; map kernel
 # (DIRECT): 7 FMA lanes + 1 ex2 per pair.
 PAIRS_PER_CLK = {"expanded": min(FMA_LANES / 4, MUFU_RATE), "direct": min(FMA_LANES / 7, MUFU_RATE)}
+# DRAM traffic of one k_pair_f32 launch on the 262,144-pixel workload, measured
+# once with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+K_PAIR_F32_DRAM_BYTES = 9_123_840
 # Plain FP64 iteration count of the workload (tol 1e-8, exact kernel), for the
 # CPU-baseline extrapolation of the reference arm.
 REF_ITERS = {"wf-262144px-grf": 162, "wf-32768px-grf": 150}
@@ -448,7 +451,11 @@ def run_ours(args, rank, world, local):
         "peak_basis": (f"{PAIRS_PER_CLK['expanded']:.0f} pairs/clk/SM (4 FMA lanes + 1 ex2 per "
                        f"pair; FMA 128 lanes/clk/SM, ex2 32/clk/SM measured) x {SMS} SMs x "
                        f"median SM clock under load"),
-        "traffic": None,
+        # DRAM bytes (read + write) of one launch, from one ncu capture of this
+        # kernel on this workload (profiles/k_pair_f32_expanded_wf262144.md):
+        # the working set stays in L2, the kernel is pipe bound
+        "traffic": K_PAIR_F32_DRAM_BYTES,
+        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
     }
 
     # Plain FP64 GPU PCG on the same system (once, untimed by the step loop).
