@@ -2,28 +2,41 @@
 // each generated S tile (128 rows x 128 columns of one tile pair) times the
 // block of NB right-hand sides of the column tile is a BF16 contraction with
 // FP32 accumulation in tensor memory (tcgen05.mma, kind::f16, M = 128,
-// N = NB, K = 16 per instruction).
+// N = 2 NB, K = 16 per instruction).
 //
-// Precision: S and u = w p are split into BF16 hi + lo parts and the product
-// is S_hi u_hi + S_hi u_lo + S_lo u_hi (three MMAs per K step), about 16
-// significant bits per term with an FP32 accumulator: an operator error near
+// Throughput: on GB300 the tensor core's operand reads share the SM's
+// shared-memory bandwidth (about 128 bytes per clock) with the S-tile stores
+// and the panel copies.  Per 128 x 128 tile and NB = 64 that is 64 KB of S
+// written, 128 KB of operands read by the MMAs and a 32 KB panel, about
+// 1,800 clocks of shared-memory time against 1,024 clocks of MMA issue at
+// N = 128 and 512 clocks of ex2 for the S values: the kernel is bound by
+// shared-memory bandwidth.  MMAs with N = 64 run at about half their peak
+// rate on this part, so the panel is one N = 2 NB operand.
+//
+// Precision: S and u = w p are split into BF16 hi + lo parts.  The u panel
+// of a column tile is one B operand of N = 2 NB rows, [u_hi | u_lo], so two
+// MMAs per K step (S_hi [u_hi | u_lo] and S_lo [u_hi | u_lo], N = 2 NB: wide
+// MMAs run near the tensor pipe's peak where N = NB ones do not) accumulate
+// D = [S u_hi | S u_lo] and the epilogue adds the halves: about 16
+// significant bits per term with an FP32 accumulator, an operator error near
 // 1e-5 relative, which the FP64 reliable updates of the solver remove.
 //
-// Per CTA (one per SM, 10 warps, persistent over (row tile, RHS block)
-// items), warp-specialized with mbarrier hand-offs:
-//   * warps 0-7 generate S for the current column tile, two threads per row
-//     and 64 columns each (EXPANDED exponent: 3 FFMA + ex2 per pair; DIRECT
-//     when the tiles are too wide for it), split it into BF16 hi / lo and
-//     store both into shared memory in the canonical K-major no-swizzle
-//     layout (8 x 16-byte core matrices); column sub-tiles outside the cutoff
-//     of the warp's row sub-tile are zero.  After an item's last tile they
-//     read D back (tcgen05.ld), form q = rowf D + ediag p and the tile's p.q
-//     per RHS;
-//   * warp 8 stages the column coordinates of each column tile and issues
-//     the cp.async.bulk copy of its u panel (pre-packed in HBM by
+// Per CTA (one per SM, GEN_WARPS + 2 warps, persistent over (row tile, RHS
+// block) items), warp-specialized with mbarrier hand-offs:
+//   * warps 0 .. GEN_WARPS - 1 generate S for the current column tile (row
+//     sub-tile warp % 4, 128 / (GEN_WARPS / 4) columns per warp; EXPANDED
+//     exponent: 3 FFMA + ex2 per pair; DIRECT when the tiles are too wide for
+//     it), split it into BF16 hi / lo and store both into shared memory in
+//     the canonical K-major no-swizzle layout (8 x 16-byte core matrices); a
+//     32 x 32 sub-tile outside the cutoff is zero.  After an item's last tile
+//     they read D back (tcgen05.ld; warp w may read TMEM lanes
+//     32 (w % 4) .. + 31, its own rows), form q = rowf D + ediag p and the
+//     tile's p.q per RHS;
+//   * warp GEN_WARPS stages the column coordinates of each column tile and
+//     issues the cp.async.bulk copy of its u panel (pre-packed in HBM by
 //     k_pack_panels in the same core-matrix layout);
-//   * lane 0 of warp 9 issues the MMAs (K steps whose column sub-tile
-//     interacts with no row sub-tile are skipped) and commits them;
+//   * lane 0 of warp GEN_WARPS + 1 issues the MMAs (K steps whose column
+//     sub-tile interacts with no row sub-tile are skipped) and commits them;
 //   * S tiles, panels and coordinates are double-buffered and the
 //     accumulator has two TMEM buffers, so generation of tile g + 1 overlaps
 //     the MMAs of tile g and an item's epilogue overlaps the next item.
@@ -40,8 +53,13 @@
 namespace ds {
 namespace {
 
-constexpr int GEN_WARPS = 8;                       // S generation + epilogue
+constexpr int GEN_WARPS = 8;                       // S generation + epilogue (8 or 16)
+constexpr int GEN_CW = GEN_WARPS / 4;              // warps per row sub-tile
+constexpr int GEN_CS = 4 / GEN_CW;                 // column sub-tiles per warp
 constexpr int TC_THREADS = (GEN_WARPS + 2) * 32;   // + producer warp + MMA warp
+// One CTA per SM: the warps are spread over the 4 SM sub-partitions, each
+// with 16,384 registers, so the busiest one holds ceil(warps / 4) warps.
+constexpr int TC_MAXNREG = (16384 / (32 * ((TC_THREADS / 32 + 3) / 4))) & ~7;
 constexpr uint32_t WAIT_TRIES = 1u << 24;  // x (poll + 64 ns sleep) ~ 1-2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -155,6 +173,18 @@ template <int N>
 __device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[N]);
 
 template <>
+__device__ __forceinline__ void tmem_ld<4>(uint32_t taddr, float (&v)[4]) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n\t"
+               "tcgen05.wait::ld.sync.aligned;"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <>
 __device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, float (&v)[8]) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
@@ -222,8 +252,9 @@ constexpr int S_ELEMS = TILE * TILE;
 // Core-matrix layout (K-major, no swizzle), in BF16 elements: element
 // (row m, k) of a 128-row operand at ((k / 8) * 16 + m / 8) * 64 + (m % 8) * 8
 // + k % 8, i.e. LBO (K-adjacent) 2048 bytes, SBO (M-adjacent) 128 bytes.  A u
-// panel (row n = RHS, k = pixel) uses ((k / 8) * (NB / 8) + n / 8) * 64 +
-// (n % 8) * 8 + k % 8: LBO NB / 8 * 128 bytes, SBO 128 bytes.
+// panel has 2 NB rows n (u_hi of RHS n for n < NB, u_lo of RHS n - NB above)
+// and k = pixel, at ((k / 8) * (2 NB / 8) + n / 8) * 64 + (n % 8) * 8 + k % 8:
+// LBO 2 NB / 8 * 128 bytes, SBO 128 bytes.
 constexpr uint32_t S_LBO = 16 * 128;
 constexpr uint32_t CORE_SBO = 128;
 
@@ -233,11 +264,13 @@ struct TcSmem {
   __nv_bfloat16 u[2][2 * NB * TILE];  // [buffer] u panel, hi then lo
   float4 sc[2][TILE];                 // [buffer] column coordinates of the tile
   float red[2][GEN_WARPS][32];        // [D buffer][warp] per-column p.q sums
-  uint64_t in_full[2];   // sc staged + u panel landed      (1 arrive + tx bytes)
+  uint64_t sc_full[2];   // column coordinates staged       (1 arrive)
+  uint64_t u_full[2];    // u panel landed                  (1 arrive + tx bytes)
   uint64_t s_full[2];    // S tile written                  (GEN_WARPS arrives)
   uint64_t mma_done[2];  // MMAs reading buffer b completed (tcgen05.commit)
   uint64_t d_full[2];    // all MMAs of an item completed   (tcgen05.commit)
   uint64_t d_empty[2];   // D read back by the epilogue     (GEN_WARPS arrives)
+  uint64_t red_full[2];  // per-warp column sums written    (GEN_WARPS arrives)
   uint32_t tmem_addr;
   int abort;
 };
@@ -251,10 +284,6 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__device__ __forceinline__ void gen_bar_sync() {
-  asm volatile("bar.sync 1, %0;" ::"n"(GEN_WARPS * 32) : "memory");
-}
-
 // A bounded wait that records a time-out: error code, CTA abort flag.
 template <int NB>
 __device__ __forceinline__ bool wait_or_abort(TcSmem<NB>& sm, uint64_t* bar, uint32_t parity,
@@ -263,6 +292,20 @@ __device__ __forceinline__ bool wait_or_abort(TcSmem<NB>& sm, uint64_t* bar, uin
   atomicExch(err, code);
   *(volatile int*)&sm.abort = 1;
   return false;
+}
+
+// The same for a whole warp: lane 0 polls (one shared-memory access per poll
+// instead of 32) and the warp's barrier orders the other lanes' reads after
+// the observed phase.
+template <int NB>
+__device__ __forceinline__ bool warp_wait_or_abort(TcSmem<NB>& sm, uint64_t* bar,
+                                                   uint32_t parity, int* err, int code,
+                                                   int lane) {
+  int ok = 1;
+  if (lane == 0) ok = wait_or_abort(sm, bar, parity, err, code);
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
 }
 
 __device__ __forceinline__ bool aborted(const int* flag) { return *(const volatile int*)flag != 0; }
@@ -287,9 +330,9 @@ __device__ __forceinline__ float warp_column_sums(float (&v)[HN], int lane) {
   return r;
 }
 
-// Warp roles: warps 0..7 generate S (two threads per row, 64 columns each)
-// and run the epilogue; warp 8 stages the column coordinates and issues the
-// u-panel copy of each column tile; lane 0 of warp 9 issues the MMAs.  The
+// Warp roles: warps 0 .. GEN_WARPS - 1 generate S and run the epilogue; warp
+// GEN_WARPS stages the column coordinates and issues the u-panel copy of each
+// column tile; lane 0 of warp GEN_WARPS + 1 issues the MMAs.  The
 // hand-offs are mbarriers, so no role waits for another except for data:
 // generation of tile g + 1 overlaps the MMAs of tile g, and the epilogue of
 // an item (its accumulator in one of two TMEM buffers) overlaps the MMAs of
@@ -297,24 +340,27 @@ __device__ __forceinline__ float warp_column_sums(float (&v)[HN], int lane) {
 // launch order (chunks by decreasing work), so every role walks the same
 // sequence without a queue.
 template <int NB, int FORMULA>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
+__global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
   static_assert(NB == 16 || NB == 32 || NB == 64, "RHS block");
-  constexpr uint32_t TMEM_COLS = 2 * NB < 32 ? 32 : 2 * NB;
+  constexpr uint32_t D_COLS = 2 * NB;  // [S u_hi | S u_lo] per accumulator buffer
+  constexpr uint32_t TMEM_COLS = 2 * D_COLS < 32 ? 32 : 2 * D_COLS;
   constexpr uint32_t PANEL_BYTES = 2u * NB * TILE * 2u;
-  constexpr uint32_t U_LBO = (NB / 8) * 128;
-  constexpr uint32_t IDESC = idesc_bf16(128, NB);
-  constexpr int HN = NB / 2;
+  constexpr uint32_t U_LBO = (2 * NB / 8) * 128;
+  constexpr uint32_t IDESC = idesc_bf16(128, 2 * NB);
+  constexpr int HN = NB / GEN_CW;  // RHS columns of D per generation warp
   extern __shared__ uint8_t smem_raw[];
   TcSmem<NB>& sm = *reinterpret_cast<TcSmem<NB>*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&sm.in_full[b], 1);
+      mbar_init(&sm.sc_full[b], 1);
+      mbar_init(&sm.u_full[b], 1);
       mbar_init(&sm.s_full[b], GEN_WARPS);
       mbar_init(&sm.mma_done[b], 1);
       mbar_init(&sm.d_full[b], 1);
       mbar_init(&sm.d_empty[b], GEN_WARPS);
+      mbar_init(&sm.red_full[b], GEN_WARPS);
     }
     sm.abort = 0;
     mbar_fence_init();
@@ -332,14 +378,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
 
   if (warp < GEN_WARPS) {
     // ---- generation and epilogue ------------------------------------------
-    const int row = tid & (TILE - 1), half = tid >> 7, rs = row >> 5;
+    // warp = 4 cw + rs: row sub-tile rs (TMEM lanes 32 rs ..), column
+    // sub-tiles GEN_CS cw .. GEN_CS cw + GEN_CS - 1 of S, D columns cw HN ..
+    // In generation lane l forms rows 32 rs + 8 j + (l & 7), j = 0..3, times
+    // the 8 columns 8 (l >> 3) .. of each column sub-tile, so each staged
+    // column is read once per 4 rows.  128-bit shared accesses are served
+    // 8 lanes at a time: lanes 8q .. 8q + 7 read the same coordinates
+    // (broadcast) and store 8 consecutive rows (128 contiguous bytes).  In
+    // the epilogue lane l owns row 32 rs + l (its TMEM lane).
+    const int rs = warp & 3, cw = warp >> 2;
+    const int kq = lane >> 3, rl = lane & 7;
+    const int row = 32 * rs + lane;
     uint32_t g = 0, k = 0;
     for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
       const int t = a.row_order[item / nblk];
       const int rb = item % nblk;
       if (a.chunk_done[a.tile_chunk[t]]) continue;
       const int i = t * TILE + row;
-      const float4 me = a.xi[i];
+      float4 me[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) me[j] = a.xi[t * TILE + 32 * rs + 8 * j + rl];
       const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
       bool any = false;
       unsigned m = a.mask[p0];
@@ -347,44 +405,64 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
         const uint32_t b = g & 1;
         const unsigned mnext = p + 1 < p1 ? a.mask[p + 1] : 0u;
         any |= m != 0u;
-        if (!wait_or_abort(sm, &sm.in_full[b], (g >> 1) & 1u, a.err, 11)) break;
-        if (g >= 2 && !wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 12)) break;
-        __nv_bfloat16* shi = sm.s[b][0];
-        __nv_bfloat16* slo = sm.s[b][1];
+        // S values of this warp's sub-tiles are formed in registers as soon as
+        // the coordinates are staged; the S buffer is awaited only for the
+        // stores
+        if (!warp_wait_or_abort(sm, &sm.sc_full[b], (g >> 1) & 1u, a.err, 11, lane)) break;
         const float4* sc = sm.sc[b];
-        const int rg = row >> 3, ir = row & 7;
+        uint4 vh[GEN_CS][4], vl[GEN_CS][4];
 #pragma unroll
-        for (int c2 = 0; c2 < 2; ++c2) {
-          const int cs = 2 * half + c2;
+        for (int c2 = 0; c2 < GEN_CS; ++c2) {
+          const int cs = GEN_CS * cw + c2;
           const bool on = (m >> (4 * rs + cs)) & 1u;
 #pragma unroll
-          for (int kq = 0; kq < 4; ++kq) {
+          for (int j = 0; j < 4; ++j) {
+            vh[c2][j] = make_uint4(0u, 0u, 0u, 0u);
+            vl[c2][j] = make_uint4(0u, 0u, 0u, 0u);
+          }
+          if (on) {
             const int kg = cs * 4 + kq;
-            uint4 vh = make_uint4(0u, 0u, 0u, 0u), vl = make_uint4(0u, 0u, 0u, 0u);
-            if (on) {
-              float s8[8];
+            float sv[4][8];
 #pragma unroll
-              for (int e = 0; e < 8; ++e) {
-                const float4 c4 = sc[kg * 8 + e];
+            for (int e = 0; e < 8; ++e) {
+              const float4 c4 = sc[kg * 8 + e];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
                 float t2;
                 if (FORMULA == F32_EXPANDED) {
-                  t2 = fmaf(me.x, c4.x, c4.w);
-                  t2 = fmaf(me.y, c4.y, t2);
-                  t2 = fmaf(me.z, c4.z, t2);
+                  t2 = fmaf(me[j].x, c4.x, c4.w);
+                  t2 = fmaf(me[j].y, c4.y, t2);
+                  t2 = fmaf(me[j].z, c4.z, t2);
                 } else {
-                  const float dx = me.x - c4.x, dy = me.y - c4.y, dz = me.z - c4.z;
+                  const float dx = me[j].x - c4.x, dy = me[j].y - c4.y, dz = me[j].z - c4.z;
                   t2 = -fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                 }
-                s8[e] = ex2_tc(t2);
+                sv[j][e] = ex2_tc(t2);
               }
-              split2(s8[0], s8[1], vh.x, vl.x);
-              split2(s8[2], s8[3], vh.y, vl.y);
-              split2(s8[4], s8[5], vh.z, vl.z);
-              split2(s8[6], s8[7], vh.w, vl.w);
             }
-            const int off = (kg * 16 + rg) * 64 + ir * 8;
-            *reinterpret_cast<uint4*>(shi + off) = vh;
-            *reinterpret_cast<uint4*>(slo + off) = vl;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              split2(sv[j][0], sv[j][1], vh[c2][j].x, vl[c2][j].x);
+              split2(sv[j][2], sv[j][3], vh[c2][j].y, vl[c2][j].y);
+              split2(sv[j][4], sv[j][5], vh[c2][j].z, vl[c2][j].z);
+              split2(sv[j][6], sv[j][7], vh[c2][j].w, vl[c2][j].w);
+            }
+          }
+        }
+        if (g >= 2 &&
+            !warp_wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 12, lane))
+          break;
+        __nv_bfloat16* shi = sm.s[b][0];
+        __nv_bfloat16* slo = sm.s[b][1];
+#pragma unroll
+        for (int c2 = 0; c2 < GEN_CS; ++c2) {
+          const int kg = (GEN_CS * cw + c2) * 4 + kq;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            // row 32 rs + 8 j + rl: 8-row group 4 rs + j, row rl within it
+            const int off = (kg * 16 + 4 * rs + j) * 64 + rl * 8;
+            *reinterpret_cast<uint4*>(shi + off) = vh[c2][j];
+            *reinterpret_cast<uint4*>(slo + off) = vl[c2][j];
           }
         }
         fence_async_smem();
@@ -397,16 +475,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
       // coefficients are loaded before the wait
       const uint32_t db = k & 1;
       const float rf = a.rowf[i], ed = a.ediag[i];
-      const int r0 = rb * NB + half * HN;
+      const int r0 = rb * NB + cw * HN;
       const float4* pv4 = reinterpret_cast<const float4*>(a.p + (size_t)i * R + r0);
       float4* qv4 = reinterpret_cast<float4*>(a.q + (size_t)i * R + r0);
       float4 pvr[HN / 4];
 #pragma unroll
       for (int k4 = 0; k4 < HN / 4; ++k4) pvr[k4] = pv4[k4];
-      if (!wait_or_abort(sm, &sm.d_full[db], (k >> 1) & 1u, a.err, 13)) break;
+      if (!warp_wait_or_abort(sm, &sm.d_full[db], (k >> 1) & 1u, a.err, 13, lane)) break;
+      __syncwarp();
       tc_fence_after();
-      float d[HN];
-      tmem_ld<HN>(tmem + ((uint32_t)(32 * rs) << 16) + db * NB + (uint32_t)(half * HN), d);
+      float d[HN], dl[HN];
+      const uint32_t tl = tmem + ((uint32_t)(32 * rs) << 16) + db * D_COLS + (uint32_t)(cw * HN);
+      tmem_ld<HN>(tl, d);        // S u_hi
+      tmem_ld<HN>(tl + NB, dl);  // S u_lo
+#pragma unroll
+      for (int j = 0; j < HN; ++j) d[j] += dl[j];
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.d_empty[db]);
@@ -428,15 +511,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
         d[4 * k4 + 2] = pv.z * qv.z;
         d[4 * k4 + 3] = pv.w * qv.w;
       }
-      const float cs = warp_column_sums<HN>(d, lane);
-      if (lane < HN) sm.red[db][warp][lane] = cs;
-      gen_bar_sync();
+      const float csum = warp_column_sums<HN>(d, lane);
+      if (lane < HN) sm.red[db][warp][lane] = csum;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.red_full[db]);
+      // The sums of buffer db are read before this item's column sums of
+      // buffer db are rewritten two items later: those need D of that item,
+      // i.e. the S tiles of the item in between from every generation warp.
+      if (warp < NB / 32 + (NB < 32) &&
+          !warp_wait_or_abort(sm, &sm.red_full[db], (k >> 1) & 1u, a.err, 14, lane))
+        break;
       if (tid < NB) {
+        // column tid of the block: warp column group h = tid / HN, summed
+        // over the four row sub-tiles (warps 4 h .. 4 h + 3)
         const int h = tid / HN, j = tid % HN;
-        double s = 0.0;
+        double sum = 0.0;
 #pragma unroll
-        for (int w = 0; w < 4; ++w) s += (double)sm.red[db][h * 4 + w][j];
-        a.part[(size_t)t * R + rb * NB + tid] = s;
+        for (int w = 0; w < 4; ++w) sum += (double)sm.red[db][h * 4 + w][j];
+        a.part[(size_t)t * R + rb * NB + tid] = sum;
       }
       if (a.prof_pairs && tid == 0) {
         unsigned long long n_sub = 0;
@@ -470,7 +562,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
         float4 cq_n[TILE / 32];
 #pragma unroll
         for (int q = 0; q < TILE / 32; ++q) cq_n[q] = a.xi[ct_n * TILE + lane + 32 * q];
-        if (g >= 2 && !wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 21)) break;
+        // sc[b] is free once every generation warp finished tile g - 2
+        if (g >= 2 &&
+            !warp_wait_or_abort(sm, &sm.s_full[b], ((g >> 1) - 1) & 1u, a.err, 22, lane))
+          break;
 #pragma unroll
         for (int q = 0; q < TILE / 32; ++q) {
           const int col = lane + 32 * q;
@@ -483,10 +578,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
             sm.sc[b][col] = make_float4(zx, zy, zz, 0.f);
         }
         __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.sc_full[b]);
+        // u[b] is free once the MMAs of tile g - 2 completed
+        if (g >= 2 &&
+            !warp_wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 21, lane))
+          break;
         if (lane == 0) {
-          mbar_expect_tx(&sm.in_full[b], PANEL_BYTES);
+          mbar_expect_tx(&sm.u_full[b], PANEL_BYTES);
           bulk_g2s(sm.u[b], panels + ((size_t)ct * nblk + rb) * (2 * NB * TILE), PANEL_BYTES,
-                   &sm.in_full[b]);
+                   &sm.u_full[b]);
         }
         last_g = (int)g;
         ct = ct_n;
@@ -506,12 +606,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
       const uint32_t db = k & 1;
       if (k >= 2 && !wait_or_abort(sm, &sm.d_empty[db], ((k >> 1) - 1) & 1u, a.err, 31)) break;
       tc_fence_after();
-      const uint32_t dt = tmem + db * NB;
+      const uint32_t dt = tmem + db * D_COLS;
       uint32_t accumulate = 0;
       bool ok = true;
       for (int p = p0; p < p1; ++p, ++g) {
         const uint32_t b = g & 1;
-        if (!wait_or_abort(sm, &sm.in_full[b], (g >> 1) & 1u, a.err, 32) ||
+        if (!wait_or_abort(sm, &sm.u_full[b], (g >> 1) & 1u, a.err, 32) ||
             !wait_or_abort(sm, &sm.s_full[b], (g >> 1) & 1u, a.err, 33)) {
           ok = false;
           break;
@@ -519,18 +619,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
         tc_fence_after();
         const unsigned m = a.mask[p];
         const uint32_t sa = smem_u32(sm.s[b][0]), sl = smem_u32(sm.s[b][1]);
-        const uint32_t ua = smem_u32(sm.u[b]), ul = ua + NB * TILE * 2;
+        const uint32_t ua = smem_u32(sm.u[b]);
 #pragma unroll 1
         for (int ks = 0; ks < TILE / 16; ++ks) {
           if (!((m >> (ks >> 1)) & 0x1111u)) continue;  // no row sub-tile reaches it
           const uint32_t aoff = ks * 2 * S_LBO, boff = ks * 2 * U_LBO;
           const uint64_t ahi = sdesc(sa + aoff, S_LBO, CORE_SBO);
           const uint64_t alo = sdesc(sl + aoff, S_LBO, CORE_SBO);
-          const uint64_t bhi = sdesc(ua + boff, U_LBO, CORE_SBO);
-          const uint64_t blo = sdesc(ul + boff, U_LBO, CORE_SBO);
-          mma_bf16(dt, ahi, bhi, IDESC, accumulate);
-          mma_bf16(dt, ahi, blo, IDESC, 1u);
-          mma_bf16(dt, alo, bhi, IDESC, 1u);
+          const uint64_t bu = sdesc(ua + boff, U_LBO, CORE_SBO);
+          mma_bf16(dt, ahi, bu, IDESC, accumulate);
+          mma_bf16(dt, alo, bu, IDESC, 1u);
           accumulate = 1u;
         }
         mma_commit(&sm.mma_done[b]);
@@ -544,7 +642,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
   // teardown: after a time-out, wait (bounded) for this role's MMAs or copy
   // in flight before the tensor memory is freed
   if (aborted(&sm.abort) && last_g >= 0 && lane == 0) {
-    if (warp == GEN_WARPS) mbar_wait(&sm.in_full[last_g & 1], (last_g >> 1) & 1u);
+    if (warp == GEN_WARPS) mbar_wait(&sm.u_full[last_g & 1], (last_g >> 1) & 1u);
     if (warp == GEN_WARPS + 1) mbar_wait(&sm.mma_done[last_g & 1], (last_g >> 1) & 1u);
   }
   tc_fence_before();
@@ -553,8 +651,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_batch_mv_tc(BatchF32Args a) {
   if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
 }
 
-// u = colw p as BF16 hi / lo panels: per (column tile, RHS block of NB), the
-// hi panel then the lo panel, each in the core-matrix layout above.  One
+// u = colw p as BF16 hi / lo panels: per (column tile, RHS block of NB), one
+// 2 NB-row operand [u_hi | u_lo] in the core-matrix layout above.  One
 // thread per (tile, group of 8 pixels, RHS): 8 strided reads (coalesced over
 // the RHS index), one 16-byte store per part.
 template <int NB>
@@ -578,9 +676,10 @@ __global__ void k_pack_panels(int n_tiles, int R, const float* __restrict__ p,
   split2(u[6], u[7], vh.w, vl.w);
   const int rb = r / NB, rr = r % NB;
   const size_t base = ((size_t)ct * (R / NB) + rb) * (2 * NB * TILE);
-  const int off = (kg * (NB / 8) + rr / 8) * 64 + (rr % 8) * 8;
-  *reinterpret_cast<uint4*>(panel + base + off) = vh;
-  *reinterpret_cast<uint4*>(panel + base + NB * TILE + off) = vl;
+  const int offh = (kg * (2 * NB / 8) + rr / 8) * 64 + (rr % 8) * 8;
+  const int offl = (kg * (2 * NB / 8) + (NB + rr) / 8) * 64 + (rr % 8) * 8;
+  *reinterpret_cast<uint4*>(panel + base + offh) = vh;
+  *reinterpret_cast<uint4*>(panel + base + offl) = vl;
 }
 
 template <int NB, int FORMULA>
