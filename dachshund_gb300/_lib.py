@@ -27,6 +27,9 @@ DS_FORM_W = 1
 DS_EVAL_TABLE = 0
 DS_EVAL_EXACT = 1
 DS_TABLE_N = 200
+DS_INNER_AUTO = 0
+DS_INNER_CUDA_CORE = 1
+DS_INNER_TENSOR = 2
 DS_BATCH_AUTO = -1
 DS_BATCH_CUDA_CORE = 0
 DS_BATCH_TENSOR = 1
@@ -147,6 +150,7 @@ SIGNATURES = {
     "ds_norm_b": (_i, [_vp, _dp]),
     "ds_A_entries": (_i, [_vp, _i, _i, _ip, _ip, _dp]),
     "ds_operator_set_dense": (_i, [_vp, _i]),
+    "ds_operator_set_inner_matvec": (_i, [_vp, _i]),
     "ds_solve_cf": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), _dp]),
     "ds_map_covar_diag": (_i, [_vp, _i, _dp, _i, _dp, C.POINTER(KernelParamsC),
                                C.POINTER(PcgParamsC), _dp, _ip, _ip]),

@@ -227,6 +227,15 @@ class _WFVector:
         self.ctx.check(self._lib.ds_operator_set_dense(self.handle, int(bool(enable))),
                        "ds_operator_set_dense")
 
+    def set_inner_matvec(self, variant: str = "auto"):
+        """Inner matvec of solve_mixed: "auto" / "cuda_core" (the CUDA-core
+        kernel, the faster one) or "tensor" (pair exponents on the tensor
+        cores where the expanded form applies)."""
+        v = {"auto": _lib.DS_INNER_AUTO, "cuda_core": _lib.DS_INNER_CUDA_CORE,
+             "tensor": _lib.DS_INNER_TENSOR}[variant]
+        self.ctx.check(self._lib.ds_operator_set_inner_matvec(self.handle, v),
+                       "ds_operator_set_inner_matvec")
+
     def info(self) -> dict:
         inf = _lib.OperatorInfoC()
         self.ctx.check(self._lib.ds_operator_get_info(self.handle, C.byref(inf)), "info")

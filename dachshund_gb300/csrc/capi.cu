@@ -712,6 +712,14 @@ int ds_operator_set_dense(ds_operator* op, int enable) {
   });
 }
 
+int ds_operator_set_inner_matvec(ds_operator* op, int variant) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    require(variant >= DS_INNER_AUTO && variant <= DS_INNER_TENSOR, "bad inner-matvec variant");
+    op->inner_variant = variant;
+  });
+}
+
 int ds_solve_cf(ds_context* ctx, int form, int n, const double* records,
                 const ds_kernel_params* kp, double* x) {
   if (!ctx) return DS_ERR_ARG;

@@ -49,9 +49,19 @@ struct F32Args {
   long long n_tile_pairs;
   unsigned long long* prof_pairs;
   Profiler* prof;
+  int* err;        // tensor-core kernel: error code of a timed-out wait (device)
+  float* tc_cols;  // tensor-core kernel: column operands (n_row_tiles x 2048 floats)
 };
 
 void launch_pair_f32(int formula, int epi, const F32Args& a, cudaStream_t st);
+
+// The inner product q = A32 p with the pair exponents on the tensor cores
+// (pair_tc.cu): EXPANDED formula, EPI_PRODUCT epilogue, a.err set.
+bool pair_tc_usable(int formula, int epi, const F32Args& a);
+void launch_pair_tc(const F32Args& a, cudaStream_t st);
+
+// Inner-matvec kernel of the mixed-precision form (ds_operator_set_inner_matvec).
+enum InnerVariant { INNER_AUTO = 0, INNER_CUDA_CORE = 1, INNER_TENSOR = 2 };
 
 // Float-pair coordinates for the FP64-accurate residual on the FP32 pipe
 // (pair_ff.cu): per pixel its coordinates scaled by sqrt(c_perp),
@@ -114,6 +124,8 @@ struct OpF32 {
   DevBuf<double> hist, htrue;
   bool use_ff = false;  // outer residual in float-float arithmetic (else FP64)
   FFData ffd;
+  DevBuf<int> tc_err;     // error flag of the tensor-core inner matvec
+  DevBuf<float> tc_cols;  // its column operands (16 floats per point)
 };
 
 // FP32 data of a map point set (DIRECT formula only).

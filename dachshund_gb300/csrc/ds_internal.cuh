@@ -275,6 +275,7 @@ struct ds_operator {
   std::unique_ptr<ds::OpF32, ds::OpF32Deleter> f32;  // mixed-precision data (lazy)
   ds::DevBuf<double> dense;  // dense A (n_pad x n_pad, sorted order) when enabled
   bool use_dense = false;
+  int inner_variant = 0;     // inner matvec of the mixed form (InnerVariant)
   // skewer-band preconditioner of the mixed form (null: Jacobi)
   std::unique_ptr<ds::SkewerPC, ds::SkewerPCDeleter> pc;
 };

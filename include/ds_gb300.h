@@ -166,6 +166,15 @@ int ds_A_entries(ds_operator* op, int eval, int m, const int* ii,
  * dense matvec; enable = 0 frees it and returns to the matrix-free kernels. */
 int ds_operator_set_dense(ds_operator* op, int enable);
 
+/* Inner matvec of the mixed-precision form (no reference counterpart; the
+ * reference has no FP32 path).  DS_INNER_AUTO and DS_INNER_CUDA_CORE use the
+ * CUDA-core kernel (4 FMA lanes + 1 ex2 per pair, the faster one on GB300);
+ * DS_INNER_TENSOR uses the tensor-core kernel (pair exponents by tcgen05
+ * TF32 MMAs, one ex2 per pair) where the operator's tiles allow the expanded
+ * exponent form, else the CUDA-core one. */
+enum { DS_INNER_AUTO = 0, DS_INNER_CUDA_CORE = 1, DS_INNER_TENSOR = 2 };
+int ds_operator_set_inner_matvec(ds_operator* op, int variant);
+
 /* ---- PCG ---------------------------------------------------------------- */
 /* PCGParams (lib/pcg.h:13-19); n is the operator's. */
 typedef struct {
