@@ -109,6 +109,9 @@ struct MixedState {
   int skip_update;    // == !need_update (skip flag of the update kernels)
   int n_updates;      // FP64 residual evaluations
   int pad;
+  int init_skip;      // skip the FP64-accurate initial residual (x0 = 0, or the
+                      // FP32 one is far above tol)
+  int pad2;
   unsigned int counter[4];
 };
 

@@ -130,6 +130,43 @@ __global__ void k_is_zero(int n, const double* __restrict__ x, int* __restrict__
     if (x[i] != 0.0) *flag = 0;
 }
 
+// x32 = float(x0) for the FP32 initial residual (skipped when x0 == 0).
+__global__ void k_x_to_f32(int n, const int* x_zero, const double* __restrict__ x,
+                           float* __restrict__ x32) {
+  if (*x_zero) return;
+  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) x32[i] = (float)x[i];
+}
+
+// r64 = b - q32 with q32 = A32 x0 (the FP32 product), and the decision on
+// the FP64-accurate initial residual: it is needed only when x0 != 0 and
+// |b - A32 x0| <= 1e-5 |b| (the FP32 operator's error, ~1e-6 |b|, could then
+// decide convergence); otherwise the first reliable update replaces the
+// FP32 residual.
+__global__ void __launch_bounds__(VB) k_r32_init(int n, MixedState* st, const int* x_zero,
+                                                 const double* __restrict__ b,
+                                                 const float* __restrict__ q32,
+                                                 double* __restrict__ r64,
+                                                 double* __restrict__ part) {
+  __shared__ double red[VB / 32];
+  const bool zero = *x_zero != 0;
+  double rr = 0.0;
+  if (!zero)
+    for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
+      const double ri = b[i] - (double)q32[i];
+      r64[i] = ri;
+      rr = fma(ri, ri, rr);
+    }
+  const double brr = block_sum<VB>(rr, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = brr;
+  if (last_block_arrive(&st->counter[1])) {
+    const double trr = reduce_partials<VB>(part, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      st->init_skip = (zero || sqrt(trr) > 1e-5 * st->norm_b) ? 1 : 0;
+      st->counter[1] = 0;
+    }
+  }
+}
+
 // r = float(r64) (or b when x0 == 0); z = r / pd; p = z; x_c = 0; r.z, |r|.
 __global__ void __launch_bounds__(VB) k_mx_init(int n, MixedState* st, const int* x_zero,
                                                 const double* __restrict__ b,
@@ -549,11 +586,21 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   DS_CUDA(cudaEventRecord(ev0, st));
 
   const int g = vgrid(np);
-  // r64 = b - A x0 in FP64, skipped when x0 == 0 (then r64 = b).
+  // r64 = b - A x0: nothing when x0 == 0 (then r64 = b); else first with the
+  // FP32 operator, then FP64-accurate only when that one is near tol.
   k_is_zero<<<g, VB, 0, st>>>(np, op->x.p, xzero);
   DS_CHECK_LAUNCH();
+  k_x_to_f32<<<g, VB, 0, st>>>(np, xzero, op->x.p, f.p.p);
+  DS_CHECK_LAUNCH();
+  {
+    F32Args a0 = op_f32_args(op, f.p.p, f.q.p);
+    a0.skip_flag = xzero;
+    launch_pair_f32(f.formula, EPI_PRODUCT, a0, st);
+  }
+  k_r32_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, f.q.p, op->r.p, op->partial.p);
+  DS_CHECK_LAUNCH();
   PairArgs resid = op_pair_args(op, op->x.p, op->r.p);
-  resid.skip_flag = xzero;
+  resid.skip_flag = &S->init_skip;
   auto outer_residual = [&](const PairArgs& pa) {
     if (f.use_ff)
       launch_pair_ff_resid(op->kc, pa, f.ffd.view, st);

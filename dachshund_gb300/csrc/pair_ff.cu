@@ -13,6 +13,15 @@
 // numbers of a few correlation lengths.  Per pair: about 64 FP32 operations
 // for the argument, 46 for exp, 12 for the float-pair multiply-add, against
 // about 20 FP64 operations (at 1/64 of the FP32 rate) in k_pair_f64.
+//
+// Far pairs: a term with argument >= FF_FAR (24) is at most e^-24 = 3.8e-11
+// of var_s |u_j|, so FP32 evaluation (argument and exp to ~1e-6 relative)
+// leaves an absolute error below 1e-16 of it.  For each column the warp first
+// forms the FP32 argument of its 32 rows; when all of them are >= FF_FAR the
+// column's terms are evaluated in FP32 (one MUFU ex2, accumulated apart),
+// else by the float-pair path.  Between the inner cutoff of the FP32 solver
+// (24) and the operator's cutoff (40 by default) lies about half of the
+// pairs this residual evaluates.
 #include <cmath>
 
 #include "ds_device.cuh"
@@ -22,6 +31,15 @@
 namespace ds {
 
 namespace {
+
+constexpr float FF_FAR = 24.f;                   // FP32 evaluation at or beyond this argument
+constexpr float LOG2E_F = 1.4426950408889634f;   // log2(e)
+
+__device__ __forceinline__ float ex2_ff(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 // Scaled tile-relative float-pair coordinates and the scaled tile origins.
 __global__ void k_ff_points(int n_pad, const double* __restrict__ x, const double* __restrict__ y,
@@ -63,6 +81,7 @@ __global__ void __launch_bounds__(TILE) k_pair_ff_resid(KernelConsts kc, PairArg
   const float cut = (float)kc.exact_cut;
   const double xi = a.rx[i] * f.sp, yi = a.ry[i] * f.sp, zi = a.rz[i] * f.sq;
   float ah = 0.f, al = 0.f;
+  float af = 0.f;  // far terms (FP32)
   unsigned long long evaluated = 0;
   float* s = &sw[warp][0][0];
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
@@ -95,16 +114,24 @@ __global__ void __launch_bounds__(TILE) k_pair_ff_resid(KernelConsts kc, PairArg
         const ff X{s[0 * SUBTILE + jj], s[1 * SUBTILE + jj]};
         const ff Y{s[2 * SUBTILE + jj], s[3 * SUBTILE + jj]};
         const ff Z{s[4 * SUBTILE + jj], s[5 * SUBTILE + jj]};
-        const ff d2 = ff_dist2(Yx, Yy, Yz, X, Y, Z);
-        if (d2.h < cut) {
-          const ff g = ff_exp_neg(d2, tab_h, tab_l);
-          ff_mac(ah, al, g, ff{s[6 * SUBTILE + jj], s[7 * SUBTILE + jj]});
+        const float dx = (Yx.h - X.h) + (Yx.l - X.l);
+        const float dy = (Yy.h - Y.h) + (Yy.l - Y.l);
+        const float dz = (Yz.h - Z.h) + (Yz.l - Z.l);
+        const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (__all_sync(0xffffffffu, d2f >= FF_FAR)) {
+          if (d2f < cut) af = fmaf(ex2_ff(-d2f * LOG2E_F), s[6 * SUBTILE + jj], af);
+        } else {
+          const ff d2 = ff_dist2(Yx, Yy, Yz, X, Y, Z);
+          if (d2.h < cut) {
+            const ff g = ff_exp_neg(d2, tab_h, tab_l);
+            ff_mac(ah, al, g, ff{s[6 * SUBTILE + jj], s[7 * SUBTILE + jj]});
+          }
         }
       }
     }
   }
   if (a.prof_pairs && lane == 0) atomicAdd(a.prof_pairs, evaluated);
-  const double acc = (double)ah + (double)al;
+  const double acc = ((double)ah + (double)al) + (double)af;
   a.out[i] = a.b[i] - (a.wl[i] * acc + a.e[i] * a.v[i]);
 }
 

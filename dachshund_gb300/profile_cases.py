@@ -8,6 +8,11 @@ dachshund_gb300.profile_cases <case>``):
                  (k_pair_f32 launches, one per iteration)
   tc_matvec      one batched FP32 product of 64 chunks x 64 RHS with the
                  tensor-core variant (k_pack_panels + k_batch_mv_tc)
+  tc_inner       one mixed-precision solve of the 262,144-pixel system with
+                 the tensor-core inner matvec (k_tc_columns + k_pair_tc)
+  learned_solve  one held-out 262,144-pixel system: Jacobi mixed solve, the
+                 network's forward pass and the learned-preconditioned solve
+                 (trained weights in dachshund_gb300/weights)
 """
 from __future__ import annotations
 
@@ -26,7 +31,7 @@ def main(argv=None):
 
     ctx = Context(0)
     sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
-    if case in ("ff_residual", "f32_matvec"):
+    if case in ("ff_residual", "f32_matvec", "tc_inner"):
         w = synth.config3(0)
         rec = pixel_to_wpixel(w.pixels)
         op = WFVectorW(ctx, rec, sp)
@@ -35,8 +40,10 @@ def main(argv=None):
             r = op.A_residual_ff(x)
             print("ff_residual |r|", float(np.linalg.norm(r)))
         else:
+            if case == "tc_inner":
+                op.set_inner_matvec("tensor")
             x, res = op.solve_mixed(MixedParams(tol=1e-8))
-            print("f32_matvec iters", res.num_iters)
+            print(case, "iters", res.num_iters)
     elif case == "tc_matvec":
         pixes, rhs = synth.chunks(64, 0, n_rhs=64)
         recs = [pixel_to_wpixel(p) for p in pixes]
@@ -46,6 +53,17 @@ def main(argv=None):
         q = torch.zeros_like(p)
         bs.product_f32_dev(p, q)
         print("tc_matvec |q|", float(torch.linalg.norm(q)))
+    elif case == "learned_solve":
+        import os
+
+        from dachshund_gb300.learned import LearnedPreconditioner, compare
+
+        net = LearnedPreconditioner(ctx, sp, hidden=128, band=2)
+        net.load(os.path.join(os.path.dirname(__file__), "weights", "learned_wf262144.bin"))
+        row = compare(net, ctx, sp, [10001])[0]
+        print("learned_solve", {k: row[k] for k in ("jacobi_iters", "learned_iters",
+                                                    "jacobi_s", "learned_s", "net_s")})
+        net.close()
     else:
         raise SystemExit(f"unknown case {case}")
     ctx.close()
