@@ -182,6 +182,7 @@ SIGNATURES = {
     "ds_learned_get_grads": (_i, [_vp, _fp]),
     "ds_learned_save": (_i, [_vp, C.c_char_p]),
     "ds_learned_load": (_i, [_vp, C.c_char_p]),
+    "ds_learned_set_inference": (_i, [_vp, _i]),
     "ds_learned_forward_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     "ds_learned_train_step_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, C.c_float, C.c_float,
                                        C.c_float, _i, _dp]),

@@ -2,6 +2,8 @@
 // skewer-band preconditioner of the mixed-precision solver (skewer_pc.cu).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "ds_internal.cuh"
 
 namespace ds {
@@ -30,6 +32,11 @@ struct LearnedNet {
   DevBuf<float> gw, X, h[N_LAYERS + 1], Z[N_LAYERS + 1], cat[N_LAYERS], Y, dY, dh, dh2, dZ, dcat,
       part;
   DevBuf<double> dpart;
+  // inference: message-passing layers on the tensor cores (learned_tc.cu)
+  bool tc_infer = true;
+  bool tc_active = false;
+  DevBuf<float> wt;   // W^T of the layer in flight (FP32)
+  DevBuf<int> tc_err;
 
   LearnedNet(ds_context* c, int hidden, int band, const KernelConsts& k, unsigned seed);
   void sync_weights();
@@ -50,6 +57,10 @@ struct LearnedNet {
 
 // Skewer-band preconditioner M^-1 = L L^T of an operator (per skewer of
 // n_per consecutive records; L rows of bandwidth `band`, FP32).
+bool layer_tc_usable(int M, int N, int K);
+void launch_layer_tc(int M, const float* A, const __nv_bfloat16* W, const float* bias, float* Z,
+                     float* out, const float* res, float* wt, int* err, cudaStream_t st);
+
 struct SkewerPC {
   int n_sk = 0, n_per = 0, band = 0;
   DevBuf<float> L;  // [record][band + 1]: L[k][k - m] at m

@@ -628,7 +628,17 @@ void LearnedNet::forward(int n_sk, int n_per, const double* rec) {
   for (int l = 0; l < N_LAYERS; ++l) {
     k_agg_fwd<<<grid1((size_t)n * H), 256, 0, st>>>(n, n_per, H, h[l].p, nbr.p, gw.p, cat[l].p);
     DS_CHECK_LAUNCH();
-    gemm_fwd(n, H, 3 * H, cat[l].p, 3 * H, W_l[l], b_l[l], Z[l + 1].p, h[l + 1].p, h[l].p, 2);
+    if (tc_active && layer_tc_usable(n, H, 3 * H)) {
+      if (!wt.p) wt.alloc((size_t)3 * H * H);
+      if (!tc_err.p) {
+        tc_err.alloc(1);
+        DS_CUDA(cudaMemsetAsync(tc_err.p, 0, sizeof(int), st));
+      }
+      launch_layer_tc(n, cat[l].p, reinterpret_cast<const __nv_bfloat16*>(wbf.p) + W_l[l].off,
+                      params.p + b_l[l].off, Z[l + 1].p, h[l + 1].p, h[l].p, wt.p, tc_err.p, st);
+    } else {
+      gemm_fwd(n, H, 3 * H, cat[l].p, 3 * H, W_l[l], b_l[l], Z[l + 1].p, h[l + 1].p, h[l].p, 2);
+    }
   }
   gemm_fwd(n, NO, H, h[N_LAYERS].p, H, W_o, b_o, nullptr, Y.p, nullptr, 0);
 }
@@ -859,9 +869,31 @@ int ds_learned_forward_dev(ds_learned* h, int n_skewers, int n_per, const double
   if (!h || !records || !L_rows) return DS_ERR_ARG;
   LearnedNet& net = *h->net;
   return guarded(net.ctx, [&] {
-    net.forward(n_skewers, n_per, records);
+    net.tc_active = net.tc_infer;
+    try {
+      net.forward(n_skewers, n_per, records);
+    } catch (...) {
+      net.tc_active = false;
+      throw;
+    }
+    net.tc_active = false;
     net.outputs(n_skewers, n_per, y0, L_rows);
+    if (net.tc_err.p) {
+      int code = 0;
+      DS_CUDA(cudaMemcpy(&code, net.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+      if (code) {
+        DS_CUDA(cudaMemset(net.tc_err.p, 0, sizeof(int)));
+        throw Error{DS_ERR_CUDA, "tensor-core layer GEMM: an mbarrier wait timed out (code " +
+                                     std::to_string(code) + ")"};
+      }
+    }
   });
+}
+
+int ds_learned_set_inference(ds_learned* h, int tensor_cores) {
+  if (!h) return DS_ERR_ARG;
+  h->net->tc_infer = tensor_cores != 0;
+  return DS_OK;
 }
 
 int ds_learned_train_step_dev(ds_learned* h, int n_skewers, int n_per, const double* records,

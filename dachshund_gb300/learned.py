@@ -80,6 +80,12 @@ class LearnedPreconditioner:
     def load(self, path):
         self.ctx.check(self._lib.ds_learned_load(self.handle, str(path).encode()), "load")
 
+    def set_inference(self, tensor_cores: bool = True):
+        """Message-passing layers of forward_dev on the tensor cores (TF32
+        activations, the default) or on the CUDA cores in FP32 as in training."""
+        self.ctx.check(self._lib.ds_learned_set_inference(self.handle, int(bool(tensor_cores))),
+                       "ds_learned_set_inference")
+
     def forward_dev(self, n_sk, n_per, rec_dev, y0_dev=None):
         """(y0, L_rows) device tensors for W-form records ``rec_dev`` (n x 5).
         The library works on the context's stream: torch's pending work is

@@ -392,6 +392,11 @@ int ds_learned_load(ds_learned* net, const char* path);
  * holds L[k][k - m] at m = 0..band (zero outside the skewer). */
 int ds_learned_forward_dev(ds_learned* net, int n_skewers, int n_per,
                            const double* records, double* y0, float* L_rows);
+/* Inference GEMMs of ds_learned_forward_dev: 1 (default) runs the
+ * message-passing layers on the tensor cores (TF32 activations, a ~1e-3
+ * relative perturbation), 0 on the CUDA cores in FP32 like training. */
+int ds_learned_set_inference(ds_learned* net, int tensor_cores);
+
 /* One training step on one system: y_star (device) its solution y, probe
  * (device, n floats) the probe vector of the preconditioner loss.  losses[0]
  * = w_x sum (y0 - y*)^2 / sum y*^2, losses[1] = w_p sum |L L^T A_bb v - v|^2

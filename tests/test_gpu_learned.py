@@ -116,3 +116,39 @@ def test_trained_network_beats_jacobi(ctx):
         assert not r["fallback"] and r["learned_rel_resid"] <= 1e-8
         assert r["x_diff"] < 1e-6
     assert sum(r["learned_iters"] for r in rows) <= 0.85 * sum(r["jacobi_iters"] for r in rows)
+
+
+def test_tensor_core_inference_matches_cuda_core(ctx):
+    """The trained network (H = 128) with its message-passing layers on the
+    tensor cores (TF32 activations) against the FP32 CUDA-core forward pass:
+    warm start and L within 2e-2 relative, and the preconditioned solve
+    reaches 1e-8 in at most 5% more iterations."""
+    import os
+
+    import torch
+
+    path = os.path.join(os.path.dirname(__file__), "..", "dachshund_gb300", "weights",
+                        "learned_wf262144.bin")
+    net = LearnedPreconditioner(ctx, EXACT, hidden=128, band=2)
+    net.load(path)
+    n_sk, n_per = 128, 256
+    rec = gpu_system(10001, n_sk, n_per, 80.0 * (128 / 1024) ** 0.5)
+    net.set_inference(False)
+    y_c, L_c = net.forward_dev(n_sk, n_per, rec)
+    y_c, L_c = y_c.clone(), L_c.clone()
+    net.set_inference(True)
+    y_t, L_t = net.forward_dev(n_sk, n_per, rec)
+    rel = lambda a, b: float(torch.max(torch.abs(a - b)) / torch.max(torch.abs(b)))  # noqa: E731
+    assert rel(y_t, y_c) < 2e-2 and rel(L_t, L_c) < 2e-2
+    op = WFVectorW(ctx, rec.cpu().numpy(), EXACT)
+    iters = []
+    for y0, L in ((y_c, L_c), (y_t, L_t)):
+        set_skewer_preconditioner(op, n_sk, n_per, 2, L)
+        x = y0.clone()
+        r = op.solve_mixed_dev(MixedParams(max_iter=3000, tol=1e-8), x)
+        assert r.success and r.final_norm <= 1e-8 * r.norm_b * (1 + 1e-6)
+        iters.append(r.num_iters)
+    set_skewer_preconditioner(op, n_sk, n_per, 2, None)
+    assert iters[1] <= 1.05 * iters[0] + 2
+    op.close()
+    net.close()
