@@ -104,7 +104,7 @@ class MixedParams:
     max_iter: int = 2000
     tol: float = 1e-8
     reliable_delta: float = 0.0   # <= 0: 1e-4
-    inner_cutoff: float = 0.0     # <= 0: 24
+    inner_cutoff: float = 0.0     # <= 0: the library default (12)
     verbose: bool = False
 
     def as_c(self):

@@ -5,13 +5,14 @@
 // N = 2 NB, K = 16 per instruction).
 //
 // Throughput: on GB300 the tensor core's operand reads share the SM's
-// shared-memory bandwidth (about 128 bytes per clock) with the S-tile stores
-// and the panel copies.  Per 128 x 128 tile and NB = 64 that is 64 KB of S
-// written, 128 KB of operands read by the MMAs and a 32 KB panel, about
-// 1,800 clocks of shared-memory time against 1,024 clocks of MMA issue at
-// N = 128 and 512 clocks of ex2 for the S values: the kernel is bound by
-// shared-memory bandwidth.  MMAs with N = 64 run at about half their peak
-// rate on this part, so the panel is one N = 2 NB operand.
+// shared memory with the S-tile stores and the panel copies: per 128 x 128
+// tile and NB = 64, 64 KB of S written, 128 KB of operands read by the MMAs
+// and a 32 KB panel, against 1,024 clocks of MMA issue at N = 128 and 512
+// clocks of ex2 for the S values.  MMAs with N = 64 run at about half their
+// peak rate on this part (67-95 clocks each against 32), so the panel is one
+// N = 2 NB operand.  Measured (64 chunks x 64 RHS): tensor pipe 21% busy,
+// shared-memory pipes 29% (LSU) and 23% (tensor core), issue 42%: the
+// two-stage S pipeline leaves latency exposed rather than saturating a pipe.
 //
 // Precision: S and u = w p are split into BF16 hi + lo parts.  The u panel
 // of a column tile is one B operand of N = 2 NB rows, [u_hi | u_lo], so two

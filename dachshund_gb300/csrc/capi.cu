@@ -513,7 +513,7 @@ int ds_A_residual_ff(ds_operator* op, const double* x, double* r) {
     require(x && r, "null vector");
     require(ff_usable(op->kc), "float-float residual needs DS_EVAL_EXACT and a cutoff <= 60");
     cudaStream_t st = op->ctx->stream;
-    ensure_op_f32(op, op->f32 ? op->f32->inner_cut : 24.0);
+    ensure_op_f32(op, op->f32 ? op->f32->inner_cut : DS_DEFAULT_INNER_CUTOFF);
     upload(x, op->n, op->io_a, st);
     op->io_b.alloc(op->n);
     op->tmp.alloc(op->pix.n_pad);
@@ -787,7 +787,7 @@ int ds_batch_create(ds_context* ctx, int form, int n_chunks, const int* chunk_si
     b->n_rhs = n_rhs;
     b->n_total = (int)total;
     b->kc = make_consts(k);
-    b->inner_cut = inner_cutoff > 0.0 ? inner_cutoff : 24.0;
+    b->inner_cut = inner_cutoff > 0.0 ? inner_cutoff : DS_DEFAULT_INNER_CUTOFF;
     DevBuf<double> rec;
     upload(records, (size_t)total * 5, rec, st);
     batch_build(b.get(), rec.p, chunk_sizes);

@@ -562,7 +562,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
                double* hist_out) {
   cudaStream_t st = op->ctx->stream;
   ensure_pcg_workspace(op);
-  const double inner_cut = mp.inner_cutoff > 0.0 ? mp.inner_cutoff : 24.0;
+  const double inner_cut = mp.inner_cutoff > 0.0 ? mp.inner_cutoff : DS_DEFAULT_INNER_CUTOFF;
   ensure_op_f32(op, inner_cut);
   OpF32& f = *op->f32;
   const int np = op->pix.n_pad;
@@ -766,7 +766,7 @@ void ensure_map_f32(ds_map* map, ds_operator* op, double cut) {
 void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
                          double cut) {
   require(op->kc.eval == DS_EVAL_EXACT, "the FP32 map product evaluates the exact kernel");
-  ensure_op_f32(op, op->f32 ? op->f32->inner_cut : 24.0);
+  ensure_op_f32(op, op->f32 ? op->f32->inner_cut : DS_DEFAULT_INNER_CUTOFF);
   ensure_map_f32(map, op, cut);
   cudaStream_t st = map->ctx->stream;
   MapF32& f = *map->f32;

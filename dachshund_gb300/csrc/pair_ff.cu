@@ -19,9 +19,9 @@
 // leaves an absolute error below 1e-16 of it.  For each column the warp first
 // forms the FP32 argument of its 32 rows; when all of them are >= FF_FAR the
 // column's terms are evaluated in FP32 (one MUFU ex2, accumulated apart),
-// else by the float-pair path.  Between the inner cutoff of the FP32 solver
-// (24) and the operator's cutoff (40 by default) lies about half of the
-// pairs this residual evaluates.
+// else by the float-pair path.  Between argument 24 and the operator's
+// cutoff (40 by default) lies about half of the pairs this residual
+// evaluates.
 #include <cmath>
 
 #include "ds_device.cuh"
