@@ -117,6 +117,9 @@ class ProfileC(C.Structure):
         ("f32_launches", C.c_longlong),
         ("f32_ms", C.c_double),
         ("f32_evaluated", C.c_double),
+        ("map_launches", C.c_longlong),
+        ("map_ms", C.c_double),
+        ("map_evaluated", C.c_double),
     ]
 
 

@@ -266,11 +266,11 @@ int ds_context_set_profiling(ds_context* ctx, int enable) {
     Profiler& p = ctx->prof;
     p.collect();
     if (enable) {
-      if (!p.d_pairs) DS_CUDA(cudaMalloc(&p.d_pairs, 2 * sizeof(unsigned long long)));
-      DS_CUDA(cudaMemsetAsync(p.d_pairs, 0, 2 * sizeof(unsigned long long), ctx->stream));
+      if (!p.d_pairs) DS_CUDA(cudaMalloc(&p.d_pairs, 3 * sizeof(unsigned long long)));
+      DS_CUDA(cudaMemsetAsync(p.d_pairs, 0, 3 * sizeof(unsigned long long), ctx->stream));
       DS_CUDA(cudaStreamSynchronize(ctx->stream));
-      p.launches[0] = p.launches[1] = 0;
-      p.ms[0] = p.ms[1] = 0.0;
+      p.launches[0] = p.launches[1] = p.launches[2] = 0;
+      p.ms[0] = p.ms[1] = p.ms[2] = 0.0;
     }
     p.enabled = enable != 0;
   });
@@ -281,7 +281,7 @@ int ds_context_get_profile(ds_context* ctx, ds_profile* out) {
   return guarded(ctx, [&] {
     Profiler& p = ctx->prof;
     p.collect();
-    unsigned long long pairs[2] = {0, 0};
+    unsigned long long pairs[3] = {0, 0, 0};
     if (p.d_pairs) {
       DS_CUDA(cudaStreamSynchronize(ctx->stream));
       DS_CUDA(cudaMemcpy(pairs, p.d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost));
@@ -292,9 +292,12 @@ int ds_context_get_profile(ds_context* ctx, ds_profile* out) {
     out->f32_launches = p.launches[1];
     out->f32_ms = p.ms[1];
     out->f32_evaluated = (double)pairs[1];
-    out->pair_launches = p.launches[0] + p.launches[1];
-    out->pair_ms = p.ms[0] + p.ms[1];
-    out->pair_evaluated = (double)pairs[0] + (double)pairs[1];
+    out->map_launches = p.launches[2];
+    out->map_ms = p.ms[2];
+    out->map_evaluated = (double)pairs[2];
+    out->pair_launches = p.launches[0] + p.launches[1] + p.launches[2];
+    out->pair_ms = p.ms[0] + p.ms[1] + p.ms[2];
+    out->pair_evaluated = (double)pairs[0] + (double)pairs[1] + (double)pairs[2];
     out->kernel_launches = launch_counter();
   });
 }

@@ -201,7 +201,8 @@ struct PairArgs {
 };
 
 // Per-context event timing of pair-kernel launches (ds_context_set_profiling).
-// Kinds: 0 = FP64 pair kernels, 1 = FP32 pair kernels.
+// Kinds: 0 = FP64-accurate pair kernels (products, residuals), 1 = FP32 pair
+// kernels (products), 2 = map products (FP64 or FP32).
 struct Profiler {
   struct Pending {
     cudaEvent_t start, stop;
@@ -210,8 +211,8 @@ struct Profiler {
   bool enabled = false;
   std::vector<cudaEvent_t> free_events;
   std::vector<Pending> pending;
-  long long launches[2] = {0, 0};
-  double ms[2] = {0.0, 0.0};
+  long long launches[3] = {0, 0, 0};
+  double ms[3] = {0.0, 0.0, 0.0};
   unsigned long long* d_pairs = nullptr;  // device counters of evaluated pairs, per kind
   cudaEvent_t get_event();
   void begin(cudaStream_t st, cudaEvent_t* ev);

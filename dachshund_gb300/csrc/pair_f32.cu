@@ -223,8 +223,9 @@ void launch_pair_f32(int formula, int epi, const F32Args& a0, cudaStream_t st) {
   if (a0.n_row_tiles <= 0) return;
   F32Args a = a0;
   cudaEvent_t ev = nullptr;
+  const int kind = epi == EPI_MAP ? 2 : 1;
   if (a.prof && a.prof->enabled) {
-    a.prof_pairs = a.prof->d_pairs + 1;
+    a.prof_pairs = a.prof->d_pairs + kind;
     a.prof->begin(st, &ev);
   } else {
     a.prof_pairs = nullptr;
@@ -234,7 +235,7 @@ void launch_pair_f32(int formula, int epi, const F32Args& a0, cudaStream_t st) {
   else
     launch_formula<F32_DIRECT>(epi, a, st);
   DS_CHECK_LAUNCH();
-  if (ev) a.prof->end(st, ev, 1);
+  if (ev) a.prof->end(st, ev, kind);
 }
 
 }  // namespace ds

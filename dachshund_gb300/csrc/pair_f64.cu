@@ -156,8 +156,9 @@ void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a0, cudaSt
   if (a0.n_row_tiles <= 0) return;
   PairArgs a = a0;
   cudaEvent_t ev = nullptr;
+  const int kind = epi == EPI_MAP ? 2 : 0;
   if (a.prof && a.prof->enabled) {
-    a.prof_pairs = a.prof->d_pairs;
+    a.prof_pairs = a.prof->d_pairs + kind;
     a.prof->begin(st, &ev);
   } else {
     a.prof_pairs = nullptr;
@@ -167,7 +168,7 @@ void launch_pair_f64(const KernelConsts& kc, int epi, const PairArgs& a0, cudaSt
   else
     launch_eval<DS_EVAL_EXACT>(kc, epi, a, st);
   DS_CHECK_LAUNCH();
-  if (ev) a.prof->end(st, ev, 0);
+  if (ev) a.prof->end(st, ev, kind);
 }
 
 long long& launch_counter() {

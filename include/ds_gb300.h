@@ -114,9 +114,12 @@ typedef struct {
   long long f64_launches;    /* the FP64 pair kernels alone */
   double f64_ms;
   double f64_evaluated;
-  long long f32_launches;    /* the FP32 pair kernels alone */
+  long long f32_launches;    /* the FP32 pair kernels alone (products) */
   double f32_ms;
   double f32_evaluated;
+  long long map_launches;    /* map products (FP64 or FP32) */
+  double map_ms;
+  double map_evaluated;
 } ds_profile;
 int ds_context_set_profiling(ds_context* ctx, int enable);
 int ds_context_get_profile(ds_context* ctx, ds_profile* out);
