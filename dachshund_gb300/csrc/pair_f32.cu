@@ -31,6 +31,12 @@ namespace ds {
 
 namespace {
 
+// CTAs per SM the register budget is sized for (4 warps each): 96 registers
+// hold the two prefetched column tiles and a fully unrolled 32-column loop;
+// on the 262,144-pixel workload 5 CTAs per SM beat 4, 6, 7 (with spills) and
+// the one-tile prefetch at 8.
+constexpr int F32_MIN_CTAS = 5;
+
 __device__ __forceinline__ float ex2f(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -53,7 +59,7 @@ __device__ __forceinline__ void accumulate32(const float4* __restrict__ col,
                                              const float* __restrict__ cu, float2 x01,
                                              float2 y01, float2 z01, float2 x23, float2 y23,
                                              float2 z23, float2& acc01, float2& acc23) {
-#pragma unroll 8
+#pragma unroll
   for (int jj = 0; jj < 32; ++jj) {
     const float4 c4 = col[jj];
     const float2 u2 = make_float2(cu[jj], cu[jj]);
@@ -95,7 +101,7 @@ __device__ __forceinline__ void accumulate32(const float4* __restrict__ col,
 }
 
 template <int FORMULA, int EPI, bool DOT>
-__global__ void __launch_bounds__(TILE, 8) k_pair_f32(F32Args a) {
+__global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
   if (a.skip_flag && *a.skip_flag) return;
   __shared__ float4 sc[TILE];
   __shared__ float su[TILE];
@@ -118,42 +124,45 @@ __global__ void __launch_bounds__(TILE, 8) k_pair_f32(F32Args a) {
   unsigned long long evaluated = 0;  // pairs this warp evaluates (profiling)
 
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
-  // The next column tile's inputs are loaded into registers while the current
-  // tile is computed, so the L2 latency of the loads is hidden.
-  float4 nq = make_float4(0.f, 0.f, 0.f, 0.f), noc = nq;
-  float nu = 0.f;
-  unsigned nm = 0;
-  auto prefetch = [&](int p) {
+  // The inputs of column tile p + 2 are loaded into registers while tile p is
+  // computed (two register sets, used alternately so that no register copy
+  // waits for a load in flight): two tiles of compute hide the L2 latency.
+  struct ColRegs {
+    float3 q, o;   // this lane's column (tile-relative) and the tile's origin
+    float u;       // colw v (product) or v (map)
+    unsigned m;    // sub-tile interaction mask of the tile pair
+  };
+  auto load = [&](ColRegs& c, int p) {
     const int ct = a.cols[p];
     const int j = ct * TILE + tid;
-    noc = a.corig[ct];
-    nq = a.cxi[j];
-    nu = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
-    nm = a.mask[p];
+    const float4 o = a.corig[ct], q = a.cxi[j];
+    c.o = make_float3(o.x, o.y, o.z);
+    c.q = make_float3(q.x, q.y, q.z);
+    c.u = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
+    c.m = a.mask[p];
   };
   // Each warp stages and reads only its own 32 columns (sc[32 warp + lane]),
   // so the warps of a CTA never wait for each other inside the loop (their
   // work differs with the sub-tile mask).
-  if (p0 < p1) prefetch(p0);
-  for (int p = p0; p < p1; ++p) {
-    const unsigned m = nm >> warp;  // bit 4k: row sub-tile k vs this warp's columns
+  auto process = [&](ColRegs& c, int p) {
+    const unsigned m = c.m >> warp;  // bit 4k: row sub-tile k vs this warp's columns
     const bool do01 = (m & 0x11u) != 0;
     const bool do23 = (m & 0x1100u) != 0;
     if (do01 || do23) {
       __syncwarp();
-      const float dx = ot.x - noc.x, dy = ot.y - noc.y, dz = ot.z - noc.z;
-      const float zx = nq.x - dx, zy = nq.y - dy, zz = nq.z - dz;
+      const float dx = ot.x - c.o.x, dy = ot.y - c.o.y, dz = ot.z - c.o.z;
+      const float zx = c.q.x - dx, zy = c.q.y - dy, zz = c.q.z - dz;
       if (FORMULA == F32_EXPANDED) {
         const float aj = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
         sc[tid] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -aj);
       } else {
         sc[tid] = make_float4(zx, zy, zz, 0.f);
       }
-      su[tid] = nu;
+      su[tid] = c.u;
       __syncwarp();
     }
-    if (p + 1 < p1) prefetch(p + 1);
-    if (!(do01 || do23)) continue;
+    if (p + 2 < p1) load(c, p + 2);
+    if (!(do01 || do23)) return;
     float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
     const float4* col = sc + warp * 32;
     const float* cu = su + warp * 32;
@@ -162,12 +171,19 @@ __global__ void __launch_bounds__(TILE, 8) k_pair_f32(F32Args a) {
       accumulate32<FORMULA, true, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
     else if (do01)
       accumulate32<FORMULA, true, false>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
-    else if (do23)
+    else
       accumulate32<FORMULA, false, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
     kahan_add(s0, c0, acc01.x);
     kahan_add(s1, c1, acc01.y);
     kahan_add(s2, c2, acc23.x);
     kahan_add(s3, c3, acc23.y);
+  };
+  ColRegs ca, cb;
+  if (p0 < p1) load(ca, p0);
+  if (p0 + 1 < p1) load(cb, p0 + 1);
+  for (int p = p0; p < p1; p += 2) {
+    process(ca, p);
+    if (p + 1 < p1) process(cb, p + 1);
   }
   if (a.prof_pairs && lane == 0) atomicAdd(a.prof_pairs, evaluated);
   // Cross-warp reduction of the four column slices, in FP64.
