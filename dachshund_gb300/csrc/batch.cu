@@ -261,6 +261,15 @@ __device__ __forceinline__ void df_mac(float& ah, float& al, float sh, float sl,
   ah = t;
 }
 
+constexpr float BR_FAR = 24.f;                   // FP32 evaluation at or beyond this argument
+constexpr float BR_LOG2E = 1.4426950408889634f;  // log2(e)
+
+__device__ __forceinline__ float ex2_br(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // r64 = b - A x for the chunks with an update pending; work items as in the
 // FP32 matvec.  One row per thread.  The exact kernel value of a pair is
 // computed once per item and applied to RB right-hand sides, accumulated as
@@ -273,6 +282,13 @@ __device__ __forceinline__ void df_mac(float& ah, float& al, float sh, float sl,
 // neither the kernel value nor the accumulation stays in FP64.  Warp-private
 // staging of the column sub-tiles the warp's rows interact with; the (hi,
 // lo) u values padded so that the staging stores avoid bank conflicts.
+// With FF, a column whose 32 rows (the warp) all lie at argument >= 24 is
+// evaluated in FP32 (a term is then at most e^-24 = 3.8e-11 of var_s |u|):
+// one ex2 and one FMA per right-hand side into separate FP32 accumulators,
+// against the float-pair kernel value and float-pair multiply-adds.  (At 32
+// right-hand sides per item the extra accumulators spill a few registers at
+// 3 CTAs per SM; that still beats 2 CTAs per SM without spills and 16
+// right-hand sides per item on the 512-chunk batch.)
 template <int RB, bool FF>
 __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
   constexpr int ROWF = 2 * RB + 4;  // floats per staged column
@@ -308,9 +324,9 @@ __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
     if (a.chunk_done[c] || !a.chunk_update[c]) continue;
     const int i = t * TILE + tid;
     const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
-    float ah[RB], al[RB];
+    float ah[RB], al[RB], af[RB];
 #pragma unroll
-    for (int r = 0; r < RB; ++r) ah[r] = al[r] = 0.f;
+    for (int r = 0; r < RB; ++r) ah[r] = al[r] = af[r] = 0.f;
     unsigned n_sub = 0;
     for (int p = a.row_ptr[t]; p < a.row_ptr[t + 1]; ++p) {
       const unsigned m = (a.mask[p] >> (4 * warp)) & 0xFu;
@@ -350,6 +366,19 @@ __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
         for (int jj = 0; jj < SUBTILE; ++jj) {
           float sh, sl;
           if constexpr (FF) {
+            const float dx = (Yx.h - sf[warp][0][jj]) + (Yx.l - sf[warp][1][jj]);
+            const float dy = (Yy.h - sf[warp][2][jj]) + (Yy.l - sf[warp][3][jj]);
+            const float dz = (Yz.h - sf[warp][4][jj]) + (Yz.l - sf[warp][5][jj]);
+            const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (__all_sync(0xffffffffu, d2f >= BR_FAR)) {
+              if (d2f < cut) {
+                const float g = ex2_br(-d2f * BR_LOG2E);
+                const float2* u2 = reinterpret_cast<const float2*>(suw + jj * ROWF);
+#pragma unroll
+                for (int r = 0; r < RB; ++r) af[r] = fmaf(g, u2[r].x, af[r]);
+              }
+              continue;
+            }
             const ff d2 = ff_dist2(Yx, Yy, Yz, ff{sf[warp][0][jj], sf[warp][1][jj]},
                                    ff{sf[warp][2][jj], sf[warp][3][jj]},
                                    ff{sf[warp][4][jj], sf[warp][5][jj]});
@@ -379,7 +408,7 @@ __global__ void __launch_bounds__(TILE, 3) k_batch_resid_f64(BatchF64Args a) {
 #pragma unroll
     for (int r = 0; r < RB; ++r) {
       const size_t k = (size_t)i * R + r0 + r;
-      const double acc = (double)ah[r] + (double)al[r];
+      const double acc = ((double)ah[r] + (double)al[r]) + (double)af[r];
       a.r64[k] = a.b[k] - (wli * acc + ei * a.xv[k]);
     }
   }
