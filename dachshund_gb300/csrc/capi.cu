@@ -742,10 +742,113 @@ int ds_solve_cf(ds_context* ctx, int form, int n, const double* records,
   });
 }
 
+namespace {
+
+// Right-hand sides b[k * R + r] = S(pixel k, map point r) (exact kernel, as
+// the per-point path builds its column), zero for padding columns r >= m.
+__global__ void k_mc_rhs(int n, int R, int m, const double* __restrict__ rec,
+                         const double* __restrict__ mp, KernelConsts kc,
+                         double* __restrict__ b) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * R) return;
+  const int k = (int)(idx / R), r = (int)(idx % R);
+  double v = 0.0;
+  if (r < m) {
+    const double dx = mp[3 * r] - rec[5 * (size_t)k], dy = mp[3 * r + 1] - rec[5 * (size_t)k + 1];
+    const double dz = mp[3 * r + 2] - rec[5 * (size_t)k + 2];
+    v = kc.var_s * exp(-(kc.c_perp * (dx * dx + dy * dy) + kc.c_para * dz * dz));
+  }
+  b[idx] = v;
+}
+
+// sig[r] = sum_k b[k R + r] x[k R + r] (one CTA per column, fixed order).
+__global__ void k_mc_dot(int n, int R, const double* __restrict__ b, const double* __restrict__ x,
+                         double* __restrict__ sig) {
+  __shared__ double red[8];
+  const int r = blockIdx.x;
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    s = fma(b[(size_t)k * R + r], x[(size_t)k * R + r], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    sig[r] = t;
+  }
+}
+
+// MapCovarDiag with the exact kernel: groups of MC_RHS map points are the
+// right-hand sides of one batched mixed-precision SN-form solve over the
+// pixels (ds_batch_*), so each kernel value of a pixel pair serves the whole
+// group (and the tensor-core S-tile x RHS product applies); the per-point
+// FP64 solves of the table kernel stay as the reference's path.
+constexpr int MC_RHS = 64;
+
+void map_covar_diag_batched(ds_context* ctx, int n_pix, const double* npixels, int n_map,
+                            const double* map_points, const ds_kernel_params& kp,
+                            const ds_pcg_params& pp, double* sigma_m, int* iters,
+                            int* success) {
+  cudaStream_t st = ctx->stream;
+  ds_batch* batch = nullptr;
+  const int sizes[1] = {n_pix};
+  int rc = ds_batch_create(ctx, DS_FORM_SN, 1, sizes, npixels, &kp, MC_RHS, 0.0, &batch);
+  if (rc != DS_OK) throw Error{rc, ctx->last_error};
+  std::unique_ptr<ds_batch, void (*)(ds_batch*)> guard(batch, ds_batch_destroy);
+  const KernelConsts kc = make_consts(kp);
+  DevBuf<double> rec, mp, b, x, sig;
+  upload(npixels, (size_t)n_pix * 5, rec, st);
+  mp.alloc(3 * MC_RHS);
+  b.alloc((size_t)n_pix * MC_RHS);
+  x.alloc((size_t)n_pix * MC_RHS);
+  sig.alloc(MC_RHS);
+  std::vector<double> hp(3 * MC_RHS), hs(MC_RHS);
+  std::vector<int> hit(MC_RHS), hconv(MC_RHS);
+  const ds_mixed_params mpar{pp.max_iter, pp.tol, 0.0, 0.0, 0};
+  for (int g = 0; g < n_map; g += MC_RHS) {
+    const int m = std::min(MC_RHS, n_map - g);
+    for (int r = 0; r < MC_RHS; ++r)
+      for (int c = 0; c < 3; ++c) hp[3 * r + c] = r < m ? map_points[3 * (size_t)(g + r) + c] : 0.0;
+    DS_CUDA(cudaMemcpyAsync(mp.p, hp.data(), hp.size() * sizeof(double), cudaMemcpyHostToDevice,
+                            st));
+    const long long total = (long long)n_pix * MC_RHS;
+    k_mc_rhs<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n_pix, MC_RHS, m, rec.p, mp.p, kc,
+                                                             b.p);
+    DS_CHECK_LAUNCH();
+    DS_CUDA(cudaMemsetAsync(x.p, 0, (size_t)total * sizeof(double), st));
+    rc = ds_batch_solve_mixed_dev(batch, &mpar, b.p, x.p, hit.data(), hconv.data(), nullptr,
+                                  nullptr, nullptr);
+    if (rc != DS_OK && rc != DS_ERR_NOT_CONVERGED) throw Error{rc, ctx->last_error};
+    k_mc_dot<<<MC_RHS, 256, 0, st>>>(n_pix, MC_RHS, b.p, x.p, sig.p);
+    DS_CHECK_LAUNCH();
+    DS_CUDA(cudaMemcpyAsync(hs.data(), sig.p, MC_RHS * sizeof(double), cudaMemcpyDeviceToHost,
+                            st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    for (int r = 0; r < m; ++r) {
+      success[g + r] = hconv[r] ? 1 : 0;
+      iters[g + r] = hit[r];
+      sigma_m[g + r] = hconv[r] ? hs[r] : 0.0;
+    }
+  }
+}
+
+}  // namespace
+
 int ds_map_covar_diag(ds_context* ctx, int n_pix, const double* npixels, int n_map,
                       const double* map_points, const ds_kernel_params* kp,
                       const ds_pcg_params* pp, double* sigma_m, int* iters, int* success) {
   if (!ctx || !pp) return DS_ERR_ARG;
+  if (kp && kp->eval == DS_EVAL_EXACT) {
+    return guarded(ctx, [&] {
+      require(n_pix > 0 && npixels, "bad pixel records");
+      require(n_map >= 0 && (n_map == 0 || (map_points && sigma_m && iters && success)),
+              "bad arguments");
+      if (n_map > 0)
+        map_covar_diag_batched(ctx, n_pix, npixels, n_map, map_points, *kp, *pp, sigma_m, iters,
+                               success);
+    });
+  }
   ds_operator* op = nullptr;
   int rc = ds_operator_create(ctx, DS_FORM_SN, n_pix, npixels, kp, &op);
   if (rc != DS_OK) return rc;

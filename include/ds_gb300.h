@@ -255,7 +255,11 @@ int ds_solve_cf(ds_context* ctx, int form, int n, const double* records,
 /* MapCovarDiag::solve_pcg (lib/map_covar.cc:73-113): for every map point i,
  * the SN-form PCG solve of (S + N) x = S_pm[:, i] from x = 0, then
  * sigma_m[i] = S_mp[i, :] . x when the solve succeeded (else 0).  Writes the
- * per-point iteration counts and success flags. */
+ * per-point iteration counts and success flags.  Table kernel (the
+ * reference's): one FP64 Jacobi-PCG per point, as the reference.  Exact
+ * kernel (DS_EVAL_EXACT, no reference counterpart): groups of 64 map points
+ * are the right-hand sides of one batched mixed-precision solve (ds_batch_*;
+ * FP32 iterations reported, stopping test on the FP64-accurate residual). */
 int ds_map_covar_diag(ds_context* ctx, int n_pix, const double* npixels, int n_map,
                       const double* map_points, const ds_kernel_params* kp,
                       const ds_pcg_params* pp, double* sigma_m, int* iters,
