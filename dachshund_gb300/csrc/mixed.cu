@@ -33,7 +33,10 @@ void MapF32Deleter::operator()(MapF32* p) const { delete p; }
 namespace {
 
 constexpr int VB = 256;
-constexpr int VGRID_MAX = 1024;
+// Grid cap of the vector kernels (grid-stride loops): 2 CTAs per SM keeps the
+// last CTA's reduction over the partials short (measured: 304 CTAs beat 1024
+// by ~5 us per iteration on 262,144 pixels).
+constexpr int VGRID_MAX = 304;
 inline int vgrid(int n) { return std::max(1, std::min(VGRID_MAX, (n + VB - 1) / VB)); }
 
 const double LOG2E = 1.4426950408889634;
