@@ -173,6 +173,28 @@ def cpu_baseline(w, iters, target_s):
     }
 
 
+def dist_barrier():
+    """Barrier over the ranks of the default process group (no-op without one)."""
+    import torch.distributed as td
+
+    if td.is_available() and td.is_initialized() and td.get_world_size() > 1:
+        td.barrier()
+
+
+def dist_max(v: float) -> float:
+    """Maximum of v over the ranks (v itself without a process group): the
+    whole job's step time is the slowest replica's."""
+    import torch
+    import torch.distributed as td
+
+    if not (td.is_available() and td.is_initialized()) or td.get_world_size() == 1:
+        return v
+    dev = "cuda" if td.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -344,20 +366,8 @@ def run_ours(args, rank, world, local):
 
         td.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as td
-
-            td.barrier()
-
-    def allmax(v):
-        if world == 1:
-            return v
-        import torch.distributed as td
-
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        return float(t.item())
+    barrier = dist_barrier
+    allmax = dist_max
 
     w = workload(args.workload)
     ctx = Context(local)
