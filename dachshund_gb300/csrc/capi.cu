@@ -234,6 +234,12 @@ int ds_context_create(int device, ds_context** out) {
     DS_CUDA(cudaGetDeviceProperties(&prop, device));
     if (prop.major < 10) throw Error{DS_ERR_NO_DEVICE, "device is not a Blackwell-class GPU"};
     DS_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    // stream-ordered device buffers come from the default pool; keep what is
+    // freed cached for the next allocations
+    cudaMemPool_t pool;
+    DS_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = ~0ull;
+    DS_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
   });
   if (rc != DS_OK) return rc;
   *out = ctx.release();

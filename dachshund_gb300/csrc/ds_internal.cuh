@@ -62,17 +62,41 @@ inline void require(bool ok, const char* msg) {
   if (!ok) throw Error{DS_ERR_ARG, msg};
 }
 
-// Owning device buffer.
+// Stream on which device buffers are allocated and freed in stream order
+// (cudaMallocAsync / cudaFreeAsync from the device's memory pool, which the
+// context keeps cached): the calling context's stream while a library call
+// runs (set by guarded()), otherwise none (plain cudaMalloc / cudaFree, which
+// synchronise the device).  A buffer is freed on the stream it was allocated
+// on, after the work queued there; objects are destroyed before their
+// context.
+inline thread_local cudaStream_t g_alloc_stream = nullptr;
+
+// Device buffer (owning).
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;  // allocation stream (stream-ordered) when async
+  bool async = false;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), s(o.s), async(o.async) {
+    o.p = nullptr;
+    o.n = 0;
+    o.async = false;
+  }
   DevBuf& operator=(DevBuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      s = o.s;
+      async = o.async;
+      o.p = nullptr;
+      o.n = 0;
+      o.async = false;
+    }
     return *this;
   }
   ~DevBuf() { release(); }
@@ -80,13 +104,24 @@ struct DevBuf {
     if (count == n && p) return;
     release();
     if (count == 0) return;
-    DS_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    s = g_alloc_stream;
+    async = s != nullptr;
+    if (async)
+      DS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), s));
+    else
+      DS_CUDA(cudaMalloc(&p, count * sizeof(T)));
     n = count;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (async)
+        cudaFreeAsync(p, s);
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    async = false;
   }
   size_t bytes() const { return n * sizeof(T); }
 };

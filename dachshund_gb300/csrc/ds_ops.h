@@ -12,6 +12,12 @@ namespace ds {
 // error message (the C ABI's error convention).
 template <class F>
 int guarded(ds_context* ctx, F&& f) {
+  // device buffers of this call are allocated / freed on the context's stream
+  struct StreamScope {
+    cudaStream_t prev;
+    explicit StreamScope(cudaStream_t st) : prev(ds::g_alloc_stream) { ds::g_alloc_stream = st; }
+    ~StreamScope() { ds::g_alloc_stream = prev; }
+  } scope(ctx ? ctx->stream : nullptr);
   try {
     f();
     if (ctx) ctx->last_error.clear();

@@ -828,7 +828,8 @@ int ds_learned_save(ds_learned* h, const char* path) {
   LearnedNet& net = *h->net;
   return guarded(net.ctx, [&] {
     std::vector<float> p(net.n_params);
-    DS_CUDA(cudaMemcpy(p.data(), net.params.p, p.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    DS_CUDA(cudaMemcpyAsync(p.data(), net.params.p, p.size() * sizeof(float), cudaMemcpyDeviceToHost, net.ctx->stream));
+    DS_CUDA(cudaStreamSynchronize(net.ctx->stream));
     FILE* f = fopen(path, "wb");
     require(f != nullptr, "cannot open the weight file for writing");
     const int hdr[3] = {FILE_VERSION, net.H, net.B};
@@ -858,7 +859,8 @@ int ds_learned_load(ds_learned* h, const char* path) {
                     fread(p.data(), sizeof(float), p.size(), f) == p.size();
     fclose(f);
     require(ok, "the weight file does not match this network (format, width or band)");
-    DS_CUDA(cudaMemcpy(net.params.p, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice));
+    DS_CUDA(cudaMemcpyAsync(net.params.p, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice, net.ctx->stream));
+    DS_CUDA(cudaStreamSynchronize(net.ctx->stream));
     net.sync_weights();
     DS_CUDA(cudaStreamSynchronize(net.ctx->stream));
   });
@@ -880,9 +882,10 @@ int ds_learned_forward_dev(ds_learned* h, int n_skewers, int n_per, const double
     net.outputs(n_skewers, n_per, y0, L_rows);
     if (net.tc_err.p) {
       int code = 0;
-      DS_CUDA(cudaMemcpy(&code, net.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+      DS_CUDA(cudaMemcpyAsync(&code, net.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, net.ctx->stream));
+      DS_CUDA(cudaStreamSynchronize(net.ctx->stream));
       if (code) {
-        DS_CUDA(cudaMemset(net.tc_err.p, 0, sizeof(int)));
+        DS_CUDA(cudaMemsetAsync(net.tc_err.p, 0, sizeof(int), net.ctx->stream));
         throw Error{DS_ERR_CUDA, "tensor-core layer GEMM: an mbarrier wait timed out (code " +
                                      std::to_string(code) + ")"};
       }

@@ -717,16 +717,18 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
 
   if (use_tc) {
     int code = 0;
-    DS_CUDA(cudaMemcpy(&code, f.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    DS_CUDA(cudaMemcpyAsync(&code, f.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
     if (code) {
-      DS_CUDA(cudaMemset(f.tc_err.p, 0, sizeof(int)));
+      DS_CUDA(cudaMemsetAsync(f.tc_err.p, 0, sizeof(int), st));
       throw Error{DS_ERR_CUDA, "tensor-core inner matvec: an mbarrier wait timed out (code " +
                                    std::to_string(code) + ")"};
     }
   }
   const int n_hist = h.iter + 1;
   if (hist_out)
-    DS_CUDA(cudaMemcpy(hist_out, f.hist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost));
+    DS_CUDA(cudaMemcpyAsync(hist_out, f.hist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
   res.norm_b = op->norm_b;
   res.final_norm = h.rtrue;
   res.seconds = ms * 1e-3;
@@ -736,8 +738,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   res.success = h.converged;
   if (mp.verbose) {
     std::vector<double> ht(h.n_updates + 1);
-    DS_CUDA(cudaMemcpy(ht.data(), f.htrue.p, ht.size() * sizeof(double),
-                       cudaMemcpyDeviceToHost));
+    DS_CUDA(cudaMemcpyAsync(ht.data(), f.htrue.p, ht.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
     printf("[PCG mixed] %d FP32 iterations, %d FP64 residual updates, |r| %e (tol |b| %e)\n",
            h.iter, h.n_updates, h.rtrue, h.tol_norm_b);
     for (size_t k = 0; k < ht.size(); ++k) printf("    update %zu: |r| = %e\n", k, ht[k]);

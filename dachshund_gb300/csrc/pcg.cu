@@ -290,8 +290,10 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
 
   const int n_hist = h.iter + 1;
   std::vector<double> hh(n_hist), dh(n_hist);
-  DS_CUDA(cudaMemcpy(hh.data(), op->hist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost));
-  DS_CUDA(cudaMemcpy(dh.data(), op->dhist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost));
+  DS_CUDA(cudaMemcpyAsync(hh.data(), op->hist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost, op->ctx->stream));
+  DS_CUDA(cudaStreamSynchronize(op->ctx->stream));
+  DS_CUDA(cudaMemcpyAsync(dh.data(), op->dhist.p, n_hist * sizeof(double), cudaMemcpyDeviceToHost, op->ctx->stream));
+  DS_CUDA(cudaStreamSynchronize(op->ctx->stream));
   if (hist_out)
     for (int k = 0; k < n_hist; ++k) hist_out[k] = hh[k];
 

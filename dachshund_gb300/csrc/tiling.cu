@@ -216,53 +216,93 @@ __device__ __forceinline__ bool tiles_interact(const double* __restrict__ bi,
   return c_perp * (dx * dx + dy * dy) + c_para * dz * dz < cut;
 }
 
-__global__ void k_pair_count(const double* __restrict__ rbox, int n_row, const double* __restrict__ cbox,
-                             int n_col, double c_perp, double c_para, double cut,
-                             int* __restrict__ counts) {
-  const int r = blockIdx.x;
-  double bi[6];
-  for (int c = 0; c < 6; ++c) bi[c] = rbox[r * 6 + c];
-  int cnt = 0;
-  for (int j = threadIdx.x; j < n_col; j += blockDim.x)
-    cnt += tiles_interact(bi, cbox + (size_t)j * 6, c_perp, c_para, cut) ? 1 : 0;
-  __shared__ int sm[BLK];
-  sm[threadIdx.x] = cnt;
-  __syncthreads();
-  for (int s = BLK / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) counts[r] = sm[0];
-  (void)n_row;
+// Union boxes of consecutive groups of 32 column tiles (k-d order keeps a
+// group spatially compact).  A row tile that does not interact with a
+// group's box interacts with none of its tiles (the distance to a union box
+// is at most the distance to each member), so the pair search tests group
+// boxes first and tile boxes only inside interacting groups: the same kept
+// pairs as testing every tile box.
+constexpr int PGROUP = 32;
+
+__global__ void k_group_boxes(int n_col, const double* __restrict__ cbox,
+                              double* __restrict__ gbox) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_groups = (n_col + PGROUP - 1) / PGROUP;
+  if (g >= n_groups) return;
+  double b[6];
+  for (int c = 0; c < 6; ++c) b[c] = cbox[(size_t)g * PGROUP * 6 + c];
+  for (int j = g * PGROUP + 1; j < min(n_col, (g + 1) * PGROUP); ++j)
+    for (int c = 0; c < 3; ++c) {
+      b[c] = fmin(b[c], cbox[(size_t)j * 6 + c]);
+      b[c + 3] = fmax(b[c + 3], cbox[(size_t)j * 6 + c + 3]);
+    }
+  for (int c = 0; c < 6; ++c) gbox[(size_t)g * 6 + c] = b[c];
 }
 
-__global__ void k_pair_fill(const double* __restrict__ rbox, const double* __restrict__ cbox,
-                            int n_col, double c_perp, double c_para, double cut,
-                            const int* __restrict__ row_ptr, int* __restrict__ cols) {
+// Per row tile (one CTA of BLK threads): for every column group the ballot
+// of its interacting tiles (0 when the group box does not interact), in
+// shared memory gm[n_groups].  FILL then writes the kept columns in
+// ascending order at row_ptr[r]; otherwise counts[r] = their number.
+template <bool FILL>
+__global__ void k_pair_search(const double* __restrict__ rbox, const double* __restrict__ cbox,
+                              const double* __restrict__ gbox, int n_col, double c_perp,
+                              double c_para, double cut, int* __restrict__ counts,
+                              const int* __restrict__ row_ptr, int* __restrict__ cols) {
+  extern __shared__ unsigned gm[];  // [n_groups]
+  __shared__ int wsum[BLK / 32];
   const int r = blockIdx.x;
-  double bi[6];
-  for (int c = 0; c < 6; ++c) bi[c] = rbox[r * 6 + c];
-  __shared__ int warp_tot[BLK / 32];
-  __shared__ int base;
-  if (threadIdx.x == 0) base = row_ptr[r];
-  __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int j0 = 0; j0 < n_col; j0 += blockDim.x) {
-    const int j = j0 + threadIdx.x;
-    const bool f = j < n_col && tiles_interact(bi, cbox + (size_t)j * 6, c_perp, c_para, cut);
-    const unsigned m = __ballot_sync(0xffffffffu, f);
-    const int pre = __popc(m & ((1u << lane) - 1u));
-    if (lane == 0) warp_tot[wid] = __popc(m);
-    __syncthreads();
-    int off = 0, tot = 0;
-    for (int w = 0; w < BLK / 32; ++w) {
-      if (w < wid) off += warp_tot[w];
-      tot += warp_tot[w];
+  const int n_groups = (n_col + PGROUP - 1) / PGROUP;
+  double bi[6];
+  for (int c = 0; c < 6; ++c) bi[c] = rbox[(size_t)r * 6 + c];
+  int cnt = 0;
+  for (int g = wid; g < n_groups; g += BLK / 32) {
+    const bool gi = tiles_interact(bi, gbox + (size_t)g * 6, c_perp, c_para, cut);
+    unsigned m = 0;
+    if (gi) {  // warp-uniform
+      const int j = g * PGROUP + lane;
+      m = __ballot_sync(0xffffffffu,
+                        j < n_col && tiles_interact(bi, cbox + (size_t)j * 6, c_perp, c_para, cut));
     }
-    if (f) cols[base + off + pre] = j;
-    __syncthreads();
-    if (threadIdx.x == 0) base += tot;
-    __syncthreads();
+    if (lane == 0) gm[g] = m;
+    cnt += __popc(m);
+  }
+  if (lane == 0) wsum[wid] = cnt;
+  __syncthreads();
+  if (!FILL) {
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int w = 0; w < BLK / 32; ++w) t += wsum[w];
+      counts[r] = t;
+    }
+    return;
+  }
+  // ascending order: group offsets by a scan over the groups (warp 0), then
+  // every warp writes its groups' columns
+  __shared__ int base;
+  if (wid == 0) {
+    int run = 0;
+    for (int g0 = 0; g0 < n_groups; g0 += 32) {
+      const int g = g0 + lane;
+      const int c = g < n_groups ? __popc(gm[g]) : 0;
+      int incl = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int excl = run + incl - c;
+      run += __shfl_sync(0xffffffffu, incl, 31);
+      // offsets go to the second half of gm
+      if (g < n_groups) gm[n_groups + g] = (unsigned)excl;
+    }
+    if (lane == 0) base = row_ptr[r];
+  }
+  __syncthreads();
+  for (int g = wid; g < n_groups; g += BLK / 32) {
+    const unsigned m = gm[g];
+    if (!m) continue;
+    if ((m >> lane) & 1u)
+      cols[base + (int)gm[n_groups + g] + __popc(m & ((1u << lane) - 1u))] = g * PGROUP + lane;
   }
 }
 
@@ -447,8 +487,16 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
   pl.n_rows = rows.n_tiles;
   DevBuf<int> counts;
   counts.alloc(rows.n_tiles);
-  k_pair_count<<<rows.n_tiles, BLK, 0, st>>>(rows.box.p, rows.n_tiles, cols.box.p, cols.n_tiles,
-                                             kc.c_perp, kc.c_para, kc.cull_arg, counts.p);
+  const int n_groups = (cols.n_tiles + PGROUP - 1) / PGROUP;
+  DevBuf<double> gbox;
+  gbox.alloc((size_t)n_groups * 6);
+  k_group_boxes<<<(n_groups + 127) / 128, 128, 0, st>>>(cols.n_tiles, cols.box.p, gbox.p);
+  DS_CHECK_LAUNCH();
+  const size_t search_smem = (size_t)2 * n_groups * sizeof(unsigned);
+  require(search_smem <= 48 * 1024, "too many column tiles for the pair search");
+  k_pair_search<false><<<rows.n_tiles, BLK, search_smem, st>>>(
+      rows.box.p, cols.box.p, gbox.p, cols.n_tiles, kc.c_perp, kc.c_para, kc.cull_arg, counts.p,
+      nullptr, nullptr);
   DS_CHECK_LAUNCH();
   std::vector<int> hc(rows.n_tiles);
   DS_CUDA(cudaMemcpyAsync(hc.data(), counts.p, hc.size() * sizeof(int), cudaMemcpyDeviceToHost,
@@ -473,8 +521,9 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
   pl.cols.alloc(std::max<long long>(total, 1));
   DS_CUDA(cudaMemcpyAsync(pl.row_ptr.p, rp.data(), rp.size() * sizeof(int),
                           cudaMemcpyHostToDevice, st));
-  k_pair_fill<<<rows.n_tiles, BLK, 0, st>>>(rows.box.p, cols.box.p, cols.n_tiles, kc.c_perp,
-                                            kc.c_para, kc.cull_arg, pl.row_ptr.p, pl.cols.p);
+  k_pair_search<true><<<rows.n_tiles, BLK, search_smem, st>>>(
+      rows.box.p, cols.box.p, gbox.p, cols.n_tiles, kc.c_perp, kc.c_para, kc.cull_arg, nullptr,
+      pl.row_ptr.p, pl.cols.p);
   DS_CHECK_LAUNCH();
   pl.mask.alloc(std::max<long long>(total, 1));
   k_pair_mask<<<rows.n_tiles, 64, 0, st>>>(rows.n_tiles, pl.row_ptr.p, pl.cols.p, rows.sbox.p,
