@@ -485,8 +485,9 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
 void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
                      const KernelConsts& kc, cudaStream_t st) {
   pl.n_rows = rows.n_tiles;
-  DevBuf<int> counts;
-  counts.alloc(rows.n_tiles);
+  DevBuf<int> counts;  // n_rows + 1: the last one 0 for the scan's total
+  counts.alloc(rows.n_tiles + 1);
+  DS_CUDA(cudaMemsetAsync(counts.p + rows.n_tiles, 0, sizeof(int), st));
   const int n_groups = (cols.n_tiles + PGROUP - 1) / PGROUP;
   DevBuf<double> gbox;
   gbox.alloc((size_t)n_groups * 6);
@@ -498,29 +499,32 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
       rows.box.p, cols.box.p, gbox.p, cols.n_tiles, kc.c_perp, kc.c_para, kc.cull_arg, counts.p,
       nullptr, nullptr);
   DS_CHECK_LAUNCH();
-  std::vector<int> hc(rows.n_tiles);
-  DS_CUDA(cudaMemcpyAsync(hc.data(), counts.p, hc.size() * sizeof(int), cudaMemcpyDeviceToHost,
-                          st));
+  // CSR offsets (exclusive scan of the counts, one trailing 0 so that
+  // row_ptr[n_rows] is the total) and the launch order: rows by decreasing
+  // count, ties by index (CUB's radix sort is stable), all on the device.
+  const int nr = rows.n_tiles;
+  pl.row_ptr.alloc(nr + 1);
+  pl.row_order.alloc(nr);
+  DevBuf<int> iota, keys_sorted;
+  iota.alloc(nr);
+  keys_sorted.alloc(nr);
+  k_iota<<<(nr + BLK - 1) / BLK, BLK, 0, st>>>(nr, iota.p);
+  DS_CHECK_LAUNCH();
+  size_t scan_bytes = 0, sort_bytes = 0;
+  DS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, counts.p, pl.row_ptr.p, nr + 1, st));
+  DS_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, sort_bytes, counts.p, keys_sorted.p,
+                                                    iota.p, pl.row_order.p, nr, 0, 32, st));
+  DevBuf<unsigned char> tmp;
+  tmp.alloc(std::max<size_t>(std::max(scan_bytes, sort_bytes), 1));
+  DS_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, scan_bytes, counts.p, pl.row_ptr.p, nr + 1, st));
+  DS_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp.p, sort_bytes, counts.p, keys_sorted.p,
+                                                    iota.p, pl.row_order.p, nr, 0, 32, st));
+  int total = 0;
+  DS_CUDA(cudaMemcpyAsync(&total, pl.row_ptr.p + nr, sizeof(int), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
-  std::vector<int> rp(rows.n_tiles + 1);
-  long long total = 0;
-  for (int r = 0; r < rows.n_tiles; ++r) {
-    rp[r] = (int)total;
-    total += hc[r];
-  }
-  require(total < (1ll << 31), "too many tile pairs");
-  rp[rows.n_tiles] = (int)total;
+  require(total >= 0, "too many tile pairs");
   pl.n_pairs = total;
-  std::vector<int> order(rows.n_tiles);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hc[a] > hc[b]; });
-  pl.row_order.alloc(rows.n_tiles);
-  DS_CUDA(cudaMemcpyAsync(pl.row_order.p, order.data(), order.size() * sizeof(int),
-                          cudaMemcpyHostToDevice, st));
-  pl.row_ptr.alloc(rows.n_tiles + 1);
   pl.cols.alloc(std::max<long long>(total, 1));
-  DS_CUDA(cudaMemcpyAsync(pl.row_ptr.p, rp.data(), rp.size() * sizeof(int),
-                          cudaMemcpyHostToDevice, st));
   k_pair_search<true><<<rows.n_tiles, BLK, search_smem, st>>>(
       rows.box.p, cols.box.p, gbox.p, cols.n_tiles, kc.c_perp, kc.c_para, kc.cull_arg, nullptr,
       pl.row_ptr.p, pl.cols.p);
@@ -530,7 +534,6 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
                                            cols.sbox.p, kc.c_perp, kc.c_para, kc.cull_arg,
                                            pl.mask.p);
   DS_CHECK_LAUNCH();
-  DS_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace ds
