@@ -261,7 +261,7 @@ __device__ __forceinline__ void df_mac(float& ah, float& al, float sh, float sl,
   ah = t;
 }
 
-constexpr float BR_FAR = 24.f;                   // FP32 evaluation at or beyond this argument
+constexpr float BR_FAR = 16.f;                   // FP32 evaluation at or beyond this argument
 constexpr float BR_LOG2E = 1.4426950408889634f;  // log2(e)
 
 __device__ __forceinline__ float ex2_br(float x) {
@@ -282,8 +282,9 @@ __device__ __forceinline__ float ex2_br(float x) {
 // neither the kernel value nor the accumulation stays in FP64.  Warp-private
 // staging of the column sub-tiles the warp's rows interact with; the (hi,
 // lo) u values padded so that the staging stores avoid bank conflicts.
-// With FF, a column whose 32 rows (the warp) all lie at argument >= 24 is
-// evaluated in FP32 (a term is then at most e^-24 = 3.8e-11 of var_s |u|):
+// With FF, a column whose 32 rows (the warp) all lie at argument >= 16 is
+// evaluated in FP32 (a term is then at most e^-16 = 1.1e-7 of var_s |u|,
+// evaluated to ~2e-6 relative, as in k_pair_ff_resid):
 // one ex2 and one FMA per right-hand side into separate FP32 accumulators,
 // against the float-pair kernel value and float-pair multiply-adds.  (At 32
 // right-hand sides per item the extra accumulators spill a few registers at
