@@ -121,12 +121,18 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
   const float4 ot = a.rorig[t];
   float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
   float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
-  unsigned long long evaluated = 0;  // pairs this warp evaluates (profiling)
+  unsigned evaluated = 0;  // pairs this warp evaluates (profiling; < 2^32 per warp)
 
   const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
-  // The inputs of column tile p + 2 are loaded into registers while tile p is
-  // computed (two register sets, used alternately so that no register copy
-  // waits for a load in flight): two tiles of compute hide the L2 latency.
+  // Each warp walks only the tile pairs in which its 32 columns interact with
+  // some row sub-tile (mask bits 4k + warp): a window of 32 masks is read per
+  // warp (one per lane, the next window prefetched) and its work items are
+  // taken from the ballot.  The column inputs of work item i + 2 are loaded
+  // into registers while item i is computed (two register sets, used
+  // alternately so that no register copy waits for a load in flight).  With
+  // the exp(-12) inner cutoff most sub-tile pairs of a kept tile pair are
+  // beyond the cutoff, so walking every tile pair would leave skipped tiles
+  // whose loads the next items wait on.
   struct ColRegs {
     float3 q, o;   // this lane's column (tile-relative) and the tile's origin
     float u;       // colw v (product) or v (map)
@@ -141,15 +147,31 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
     c.u = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
     c.m = a.mask[p];
   };
+  constexpr unsigned full = 0xffffffffu;
+  int nbase = p0;  // first tile pair of the next mask window
+  unsigned nmask = p0 + lane < p1 ? a.mask[p0 + lane] : 0u;
+  unsigned wbits = 0;  // work items left in the current window
+  auto fetch = [&](ColRegs& c) -> bool {
+    while (wbits == 0) {
+      if (nbase >= p1) return false;
+      wbits = __ballot_sync(full, ((nmask >> warp) & 0x1111u) != 0u);
+      nbase += 32;
+      nmask = nbase + lane < p1 ? a.mask[nbase + lane] : 0u;
+    }
+    const int k = __ffs(wbits) - 1;
+    wbits &= wbits - 1;
+    load(c, nbase - 32 + k);  // the window in use starts 32 before the next
+    return true;
+  };
   // Each warp stages and reads only its own 32 columns (sc[32 warp + lane]),
   // so the warps of a CTA never wait for each other inside the loop (their
   // work differs with the sub-tile mask).
-  auto process = [&](ColRegs& c, int p) {
+  auto process = [&](ColRegs& c) -> bool {
     const unsigned m = c.m >> warp;  // bit 4k: row sub-tile k vs this warp's columns
     const bool do01 = (m & 0x11u) != 0;
     const bool do23 = (m & 0x1100u) != 0;
-    if (do01 || do23) {
-      __syncwarp();
+    __syncwarp();
+    {
       const float dx = ot.x - c.o.x, dy = ot.y - c.o.y, dz = ot.z - c.o.z;
       const float zx = c.q.x - dx, zy = c.q.y - dy, zz = c.q.z - dz;
       if (FORMULA == F32_EXPANDED) {
@@ -159,10 +181,9 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
         sc[tid] = make_float4(zx, zy, zz, 0.f);
       }
       su[tid] = c.u;
-      __syncwarp();
     }
-    if (p + 2 < p1) load(c, p + 2);
-    if (!(do01 || do23)) return;
+    __syncwarp();
+    const bool more = fetch(c);
     float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
     const float4* col = sc + warp * 32;
     const float* cu = su + warp * 32;
@@ -177,15 +198,17 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
     kahan_add(s1, c1, acc01.y);
     kahan_add(s2, c2, acc23.x);
     kahan_add(s3, c3, acc23.y);
+    return more;
   };
   ColRegs ca, cb;
-  if (p0 < p1) load(ca, p0);
-  if (p0 + 1 < p1) load(cb, p0 + 1);
-  for (int p = p0; p < p1; p += 2) {
-    process(ca, p);
-    if (p + 1 < p1) process(cb, p + 1);
+  bool va = fetch(ca);
+  bool vb = va && fetch(cb);
+  while (va) {
+    va = process(ca);  // false once no item is left for ca
+    if (!vb) break;
+    vb = process(cb);
   }
-  if (a.prof_pairs && lane == 0) atomicAdd(a.prof_pairs, evaluated);
+  if (a.prof_pairs && lane == 0) atomicAdd(a.prof_pairs, (unsigned long long)evaluated);
   // Cross-warp reduction of the four column slices, in FP64.
   sred[warp][lane] = s0 - c0;
   sred[warp][lane + 32] = s1 - c1;
