@@ -41,7 +41,7 @@ FMA_LANES, MUFU_RATE, DFMA_RATE = 128.0, 32.0, 2.0
 PAIRS_PER_CLK = {"expanded": min(FMA_LANES / 4, MUFU_RATE), "direct": min(FMA_LANES / 7, MUFU_RATE)}
 # DRAM traffic of one k_pair_f32 launch on the 262,144-pixel workload, measured
 # once with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
-K_PAIR_F32_DRAM_BYTES = 8_891_136
+K_PAIR_F32_DRAM_BYTES = 9_174_528
 # Plain FP64 iteration count of the workload (tol 1e-8, exact kernel), for the
 # CPU-baseline extrapolation of the reference arm.
 REF_ITERS = {"wf-262144px-grf": 162, "wf-32768px-grf": 150}

@@ -27,6 +27,8 @@ struct F32Args {
   const int* row_ptr; const int* cols;
   int n_row_tiles;
   const unsigned short* mask;  // sub-tile interaction mask per tile pair
+  const int* item_ptr;         // work items per row tile (PairList::items)
+  const unsigned int* items;
   const int* row_order;        // blockIdx -> row tile (heaviest first), or null
   const float* colw;   // column weights (W: w_j, SN: 1)
   const float* v;      // column vector

@@ -191,10 +191,16 @@ struct PairList {
   // sub-tile w (the same box test at sub-tile granularity)
   DevBuf<unsigned short> mask;
   DevBuf<int> row_order;  // row tiles by decreasing pair count (launch order)
+  // Work items of the FP32 kernels (build_slice_items): per tile pair, one
+  // per column sub-tile w with some interacting row sub-tile, in tile-pair
+  // then w order; entry = column tile << 6 | w << 4 | row sub-tiles (bit k).
+  DevBuf<int> item_ptr;         // n_rows + 1
+  DevBuf<unsigned int> items;
 };
 
 void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
                      const KernelConsts& kc, cudaStream_t st);
+void build_slice_items(PairList& pl, cudaStream_t st);
 
 // ---- pair kernels (FP64) -------------------------------------------------
 // Column weight u_j and epilogue selection.

@@ -519,6 +519,7 @@ void ensure_op_f32(ds_operator* op, double inner_cut) {
   KernelConsts kc = op->kc;
   kc.cull_arg = inner_cut * (1.0 + 1e-9);
   build_pair_list(f->pairs, op->pix, op->pix, kc, st);
+  build_slice_items(f->pairs, st);
   const int np = op->pix.n_pad;
   f->rowf.alloc(np);
   f->colw.alloc(np);
@@ -548,6 +549,8 @@ F32Args op_f32_args(ds_operator* op, const float* v, float* out) {
   a.row_ptr = f.pairs.row_ptr.p;
   a.cols = f.pairs.cols.p;
   a.mask = f.pairs.mask.p;
+  a.item_ptr = f.pairs.item_ptr.p;
+  a.items = f.pairs.items.p;
   a.row_order = f.pairs.row_order.p;
   a.n_row_tiles = op->pix.n_tiles;
   a.colw = f.colw.p;
@@ -759,6 +762,7 @@ void ensure_map_f32(ds_map* map, ds_operator* op, double cut) {
   KernelConsts kc = op->kc;
   kc.cull_arg = cut * (1.0 + 1e-9);
   build_pair_list(f->pairs, map->pts, op->pix, kc, st);
+  build_slice_items(f->pairs, st);
   f->rowf.alloc(map->pts.n_pad);
   k_fill_f32<<<vgrid(map->pts.n_pad), VB, 0, st>>>(map->pts.n_pad, (float)op->kc.var_s,
                                                    f->rowf.p);
@@ -788,6 +792,8 @@ void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, doub
   a.row_ptr = f.pairs.row_ptr.p;
   a.cols = f.pairs.cols.p;
   a.mask = f.pairs.mask.p;
+  a.item_ptr = f.pairs.item_ptr.p;
+  a.items = f.pairs.items.p;
   a.row_order = f.pairs.row_order.p;
   a.n_row_tiles = map->pts.n_tiles;
   a.v = f.xs.p;

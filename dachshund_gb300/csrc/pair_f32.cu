@@ -123,53 +123,53 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
   float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
   unsigned evaluated = 0;  // pairs this warp evaluates (profiling; < 2^32 per warp)
 
-  const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
-  // Each warp walks only the tile pairs in which its 32 columns interact with
-  // some row sub-tile (mask bits 4k + warp): a window of 32 masks is read per
-  // warp (one per lane, the next window prefetched) and its work items are
-  // taken from the ballot.  The column inputs of work item i + 2 are loaded
-  // into registers while item i is computed (two register sets, used
-  // alternately so that no register copy waits for a load in flight).  With
-  // the exp(-12) inner cutoff most sub-tile pairs of a kept tile pair are
-  // beyond the cutoff, so walking every tile pair would leave skipped tiles
-  // whose loads the next items wait on.
+  // Work items (column tile, column sub-tile w) of this row tile, in the
+  // order of the tile pairs and then w (build_slice_items); warp v takes
+  // items v, v + 4, v + 8, ...: the four warps carry equal work whatever the
+  // masks (each warp sums all 128 rows, so the sub-tiles may be shared out
+  // freely) and the order of every FP32 sum is fixed.  A warp reads its next
+  // 32 items in one load (lane l: its item 32 b + l, the next batch
+  // prefetched).  The column inputs of a warp's item i + 2 are loaded into
+  // registers while item i is computed (two register sets, used alternately
+  // so that no register copy waits for a load in flight).
+  const int i1 = a.item_ptr[t + 1];
   struct ColRegs {
     float3 q, o;   // this lane's column (tile-relative) and the tile's origin
     float u;       // colw v (product) or v (map)
-    unsigned m;    // sub-tile interaction mask of the tile pair
+    unsigned m;    // row sub-tiles interacting with the item's columns (bit k)
   };
-  auto load = [&](ColRegs& c, int p) {
-    const int ct = a.cols[p];
-    const int j = ct * TILE + tid;
+  auto load = [&](ColRegs& c, unsigned it) {
+    const int ct = (int)(it >> 6);
+    const int j = ct * TILE + 32 * (int)((it >> 4) & 3u) + lane;
     const float4 o = a.corig[ct], q = a.cxi[j];
     c.o = make_float3(o.x, o.y, o.z);
     c.q = make_float3(q.x, q.y, q.z);
     c.u = (EPI == EPI_PRODUCT) ? a.colw[j] * a.v[j] : a.v[j];
-    c.m = a.mask[p];
+    c.m = it & 15u;
   };
   constexpr unsigned full = 0xffffffffu;
-  int nbase = p0;  // first tile pair of the next mask window
-  unsigned nmask = p0 + lane < p1 ? a.mask[p0 + lane] : 0u;
-  unsigned wbits = 0;  // work items left in the current window
+  int nb = a.item_ptr[t] + warp;  // this warp's first item of the next batch
+  unsigned nitem = nb + 4 * lane < i1 ? a.items[nb + 4 * lane] : 0u;
+  unsigned witem = 0;  // this lane's item of the current batch
+  int pos = 0, cnt = 0;  // items taken / held of the current batch
   auto fetch = [&](ColRegs& c) -> bool {
-    while (wbits == 0) {
-      if (nbase >= p1) return false;
-      wbits = __ballot_sync(full, ((nmask >> warp) & 0x1111u) != 0u);
-      nbase += 32;
-      nmask = nbase + lane < p1 ? a.mask[nbase + lane] : 0u;
+    if (pos == cnt) {
+      if (nb >= i1) return false;
+      cnt = min(32, (i1 - nb + 3) >> 2);
+      pos = 0;
+      witem = nitem;
+      nb += 128;
+      nitem = nb + 4 * lane < i1 ? a.items[nb + 4 * lane] : 0u;
     }
-    const int k = __ffs(wbits) - 1;
-    wbits &= wbits - 1;
-    load(c, nbase - 32 + k);  // the window in use starts 32 before the next
+    load(c, __shfl_sync(full, witem, pos));
+    ++pos;
     return true;
   };
   // Each warp stages and reads only its own 32 columns (sc[32 warp + lane]),
-  // so the warps of a CTA never wait for each other inside the loop (their
-  // work differs with the sub-tile mask).
+  // so the warps of a CTA never wait for each other inside the loop.
   auto process = [&](ColRegs& c) -> bool {
-    const unsigned m = c.m >> warp;  // bit 4k: row sub-tile k vs this warp's columns
-    const bool do01 = (m & 0x11u) != 0;
-    const bool do23 = (m & 0x1100u) != 0;
+    const bool do01 = (c.m & 3u) != 0;   // row sub-tile 0 or 1
+    const bool do23 = (c.m & 12u) != 0;  // row sub-tile 2 or 3
     __syncwarp();
     {
       const float dx = ot.x - c.o.x, dy = ot.y - c.o.y, dz = ot.z - c.o.z;

@@ -482,6 +482,68 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
   DS_CUDA(cudaStreamSynchronize(st));
 }
 
+// Items per tile pair: the column sub-tiles w with (mask >> w) & 0x1111 != 0.
+__global__ void k_item_count(long long n_pairs, const unsigned short* __restrict__ mask,
+                             int* __restrict__ cnt) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const unsigned m = mask[p];
+  int c = 0;
+#pragma unroll
+  for (int w = 0; w < 4; ++w) c += ((m >> w) & 0x1111u) != 0u;
+  cnt[p] = c;
+}
+
+__global__ void k_item_fill(long long n_pairs, const unsigned short* __restrict__ mask,
+                            const int* __restrict__ cols, const int* __restrict__ off,
+                            unsigned int* __restrict__ items) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const unsigned m = mask[p], ct = (unsigned)cols[p];
+  int o = off[p];
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    const unsigned r = (m >> w) & 0x1111u;  // bit 4k: row sub-tile k
+    if (r == 0u) continue;
+    const unsigned rk = (r & 1u) | ((r >> 3) & 2u) | ((r >> 6) & 4u) | ((r >> 9) & 8u);
+    items[o++] = (ct << 6) | ((unsigned)w << 4) | rk;
+  }
+}
+
+__global__ void k_item_rows(int n_rows, const int* __restrict__ row_ptr,
+                            const int* __restrict__ off, int* __restrict__ item_ptr) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t <= n_rows) item_ptr[t] = off[row_ptr[t]];
+}
+
+void build_slice_items(PairList& pl, cudaStream_t st) {
+  const long long np = pl.n_pairs;
+  require(np < (1ll << 29), "too many tile pairs for the item list");
+  DevBuf<int> cnt, off;
+  cnt.alloc(np + 1);
+  off.alloc(np + 1);
+  DS_CUDA(cudaMemsetAsync(cnt.p + np, 0, sizeof(int), st));
+  const int g = (int)((np + BLK - 1) / BLK);
+  if (np > 0) {
+    k_item_count<<<g, BLK, 0, st>>>(np, pl.mask.p, cnt.p);
+    DS_CHECK_LAUNCH();
+  }
+  size_t scan_bytes = 0;
+  DS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, cnt.p, off.p, (int)(np + 1), st));
+  DevBuf<unsigned char> tmp;
+  tmp.alloc(std::max<size_t>(scan_bytes, 1));
+  DS_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, scan_bytes, cnt.p, off.p, (int)(np + 1), st));
+  pl.items.alloc(std::max<long long>(4 * np, 1));
+  if (np > 0) {
+    k_item_fill<<<g, BLK, 0, st>>>(np, pl.mask.p, pl.cols.p, off.p, pl.items.p);
+    DS_CHECK_LAUNCH();
+  }
+  pl.item_ptr.alloc(pl.n_rows + 1);
+  k_item_rows<<<(pl.n_rows + 1 + BLK - 1) / BLK, BLK, 0, st>>>(pl.n_rows, pl.row_ptr.p, off.p,
+                                                               pl.item_ptr.p);
+  DS_CHECK_LAUNCH();
+}
+
 void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
                      const KernelConsts& kc, cudaStream_t st) {
   pl.n_rows = rows.n_tiles;
