@@ -168,6 +168,9 @@ struct PointSet {
   DevBuf<int> perm;        // sorted position -> caller index (-1 on padding)
   DevBuf<double> box;      // 6 per tile: lo x, y, z, hi x, y, z
   DevBuf<double> sbox;     // 6 per SUBTILE-point sub-tile, same layout
+  // FP32 copies rounded outward (lo down, hi up), each containing its FP64
+  // box: the pair search's culling tests
+  DevBuf<float> box32, sbox32;
 };
 
 // Builds a PointSet from n records of `stride` doubles (x, y, z first) that

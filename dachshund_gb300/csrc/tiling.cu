@@ -207,13 +207,48 @@ __global__ void k_iota(int n, int* __restrict__ out) {
   if (i < n) out[i] = i;
 }
 
-__device__ __forceinline__ bool tiles_interact(const double* __restrict__ bi,
-                                               const double* __restrict__ bj,
-                                               double c_perp, double c_para, double cut) {
-  const double dx = fmax(0.0, fmax(bi[0] - bj[3], bj[0] - bi[3]));
-  const double dy = fmax(0.0, fmax(bi[1] - bj[4], bj[1] - bi[4]));
-  const double dz = fmax(0.0, fmax(bi[2] - bj[5], bj[2] - bi[5]));
-  return c_perp * (dx * dx + dy * dy) + c_para * dz * dz < cut;
+// Culling test of two boxes: c_perp (dx^2 + dy^2) + c_para dz^2 < cut at the
+// nearest corners, in FP32 (FP64 runs at 2 FMA per clock per SM on GB300).
+// The boxes are rounded outward, every gap, product and sum is rounded down
+// and c_perp, c_para down, cut up, so the FP32 argument never exceeds the
+// exact one: a pair that interacts is never culled (a pair within rounding of
+// the cutoff may be kept).  The test is symmetric in the two boxes, so the
+// kept relation stays symmetric.
+struct CullConsts {
+  float c_perp, c_para, cut;
+};
+
+__device__ __forceinline__ bool tiles_interact(const float* __restrict__ bi,
+                                               const float* __restrict__ bj,
+                                               const CullConsts& k) {
+  const float dx = fmaxf(0.f, fmaxf(__fsub_rd(bi[0], bj[3]), __fsub_rd(bj[0], bi[3])));
+  const float dy = fmaxf(0.f, fmaxf(__fsub_rd(bi[1], bj[4]), __fsub_rd(bj[1], bi[4])));
+  const float dz = fmaxf(0.f, fmaxf(__fsub_rd(bi[2], bj[5]), __fsub_rd(bj[2], bi[5])));
+  const float perp = __fmaf_rd(dy, dy, __fmul_rd(dx, dx));
+  return __fmaf_rd(k.c_perp, perp, __fmul_rd(k.c_para, __fmul_rd(dz, dz))) < k.cut;
+}
+
+float f32_down(double v) {
+  float f = (float)v;
+  if ((double)f > v) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+
+float f32_up(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
+CullConsts cull_consts(const KernelConsts& kc) {
+  return CullConsts{f32_down(kc.c_perp), f32_down(kc.c_para), f32_up(kc.cull_arg)};
+}
+
+// Outward FP32 copies of n boxes (6 values each: lo x, y, z, hi x, y, z).
+__global__ void k_box_f32(long long n6, const double* __restrict__ b, float* __restrict__ f) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n6) return;
+  f[i] = (i % 6) < 3 ? __double2float_rd(b[i]) : __double2float_ru(b[i]);
 }
 
 // Union boxes of consecutive groups of 32 column tiles (k-d order keeps a
@@ -224,17 +259,17 @@ __device__ __forceinline__ bool tiles_interact(const double* __restrict__ bi,
 // pairs as testing every tile box.
 constexpr int PGROUP = 32;
 
-__global__ void k_group_boxes(int n_col, const double* __restrict__ cbox,
-                              double* __restrict__ gbox) {
+__global__ void k_group_boxes(int n_col, const float* __restrict__ cbox,
+                              float* __restrict__ gbox) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const int n_groups = (n_col + PGROUP - 1) / PGROUP;
   if (g >= n_groups) return;
-  double b[6];
+  float b[6];
   for (int c = 0; c < 6; ++c) b[c] = cbox[(size_t)g * PGROUP * 6 + c];
   for (int j = g * PGROUP + 1; j < min(n_col, (g + 1) * PGROUP); ++j)
     for (int c = 0; c < 3; ++c) {
-      b[c] = fmin(b[c], cbox[(size_t)j * 6 + c]);
-      b[c + 3] = fmax(b[c + 3], cbox[(size_t)j * 6 + c + 3]);
+      b[c] = fminf(b[c], cbox[(size_t)j * 6 + c]);
+      b[c + 3] = fmaxf(b[c + 3], cbox[(size_t)j * 6 + c + 3]);
     }
   for (int c = 0; c < 6; ++c) gbox[(size_t)g * 6 + c] = b[c];
 }
@@ -244,25 +279,25 @@ __global__ void k_group_boxes(int n_col, const double* __restrict__ cbox,
 // shared memory gm[n_groups].  FILL then writes the kept columns in
 // ascending order at row_ptr[r]; otherwise counts[r] = their number.
 template <bool FILL>
-__global__ void k_pair_search(const double* __restrict__ rbox, const double* __restrict__ cbox,
-                              const double* __restrict__ gbox, int n_col, double c_perp,
-                              double c_para, double cut, int* __restrict__ counts,
-                              const int* __restrict__ row_ptr, int* __restrict__ cols) {
+__global__ void k_pair_search(const float* __restrict__ rbox, const float* __restrict__ cbox,
+                              const float* __restrict__ gbox, int n_col, CullConsts kc,
+                              int* __restrict__ counts, const int* __restrict__ row_ptr,
+                              int* __restrict__ cols) {
   extern __shared__ unsigned gm[];  // [n_groups]
   __shared__ int wsum[BLK / 32];
   const int r = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int n_groups = (n_col + PGROUP - 1) / PGROUP;
-  double bi[6];
+  float bi[6];
   for (int c = 0; c < 6; ++c) bi[c] = rbox[(size_t)r * 6 + c];
   int cnt = 0;
   for (int g = wid; g < n_groups; g += BLK / 32) {
-    const bool gi = tiles_interact(bi, gbox + (size_t)g * 6, c_perp, c_para, cut);
+    const bool gi = tiles_interact(bi, gbox + (size_t)g * 6, kc);
     unsigned m = 0;
     if (gi) {  // warp-uniform
       const int j = g * PGROUP + lane;
       m = __ballot_sync(0xffffffffu,
-                        j < n_col && tiles_interact(bi, cbox + (size_t)j * 6, c_perp, c_para, cut));
+                        j < n_col && tiles_interact(bi, cbox + (size_t)j * 6, kc));
     }
     if (lane == 0) gm[g] = m;
     cnt += __popc(m);
@@ -309,21 +344,21 @@ __global__ void k_pair_search(const double* __restrict__ rbox, const double* __r
 // Sub-tile interaction masks of every kept tile pair: bit 4 k + w for row
 // sub-tile k and column sub-tile w.
 __global__ void k_pair_mask(int n_rows, const int* __restrict__ row_ptr,
-                            const int* __restrict__ cols, const double* __restrict__ rsbox,
-                            const double* __restrict__ csbox, double c_perp, double c_para,
-                            double cut, unsigned short* __restrict__ mask) {
+                            const int* __restrict__ cols, const float* __restrict__ rsbox,
+                            const float* __restrict__ csbox, CullConsts kc,
+                            unsigned short* __restrict__ mask) {
   const int r = blockIdx.x;
   if (r >= n_rows) return;
-  double rb[4][6];
+  float rb[4][6];
   for (int k = 0; k < 4; ++k)
     for (int c = 0; c < 6; ++c) rb[k][c] = rsbox[((size_t)r * 4 + k) * 6 + c];
   for (int p = row_ptr[r] + threadIdx.x; p < row_ptr[r + 1]; p += blockDim.x) {
     const int ct = cols[p];
     unsigned m = 0;
     for (int w = 0; w < 4; ++w) {
-      const double* cb = csbox + ((size_t)ct * 4 + w) * 6;
+      const float* cb = csbox + ((size_t)ct * 4 + w) * 6;
       for (int k = 0; k < 4; ++k)
-        if (tiles_interact(rb[k], cb, c_perp, c_para, cut)) m |= 1u << (4 * k + w);
+        if (tiles_interact(rb[k], cb, kc)) m |= 1u << (4 * k + w);
     }
     mask[p] = (unsigned short)m;
   }
@@ -478,6 +513,13 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
   ps.sbox.alloc((size_t)(ps.n_pad / SUBTILE) * 6);
   k_tile_boxes<<<ps.n_pad / SUBTILE, SUBTILE, 0, st>>>(ps.x.p, ps.y.p, ps.z.p, ps.sbox.p);
   DS_CHECK_LAUNCH();
+  const long long nb6 = (long long)ps.n_tiles * 6, ns6 = (long long)(ps.n_pad / SUBTILE) * 6;
+  ps.box32.alloc(nb6);
+  ps.sbox32.alloc(ns6);
+  k_box_f32<<<(int)((nb6 + BLK - 1) / BLK), BLK, 0, st>>>(nb6, ps.box.p, ps.box32.p);
+  DS_CHECK_LAUNCH();
+  k_box_f32<<<(int)((ns6 + BLK - 1) / BLK), BLK, 0, st>>>(ns6, ps.sbox.p, ps.sbox32.p);
+  DS_CHECK_LAUNCH();
   // The temporaries are freed on return; make sure the stream is done with them.
   DS_CUDA(cudaStreamSynchronize(st));
 }
@@ -551,15 +593,15 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
   counts.alloc(rows.n_tiles + 1);
   DS_CUDA(cudaMemsetAsync(counts.p + rows.n_tiles, 0, sizeof(int), st));
   const int n_groups = (cols.n_tiles + PGROUP - 1) / PGROUP;
-  DevBuf<double> gbox;
+  const CullConsts ck = cull_consts(kc);
+  DevBuf<float> gbox;
   gbox.alloc((size_t)n_groups * 6);
-  k_group_boxes<<<(n_groups + 127) / 128, 128, 0, st>>>(cols.n_tiles, cols.box.p, gbox.p);
+  k_group_boxes<<<(n_groups + 127) / 128, 128, 0, st>>>(cols.n_tiles, cols.box32.p, gbox.p);
   DS_CHECK_LAUNCH();
   const size_t search_smem = (size_t)2 * n_groups * sizeof(unsigned);
   require(search_smem <= 48 * 1024, "too many column tiles for the pair search");
   k_pair_search<false><<<rows.n_tiles, BLK, search_smem, st>>>(
-      rows.box.p, cols.box.p, gbox.p, cols.n_tiles, kc.c_perp, kc.c_para, kc.cull_arg, counts.p,
-      nullptr, nullptr);
+      rows.box32.p, cols.box32.p, gbox.p, cols.n_tiles, ck, counts.p, nullptr, nullptr);
   DS_CHECK_LAUNCH();
   // CSR offsets (exclusive scan of the counts, one trailing 0 so that
   // row_ptr[n_rows] is the total) and the launch order: rows by decreasing
@@ -588,13 +630,11 @@ void build_pair_list(PairList& pl, const PointSet& rows, const PointSet& cols,
   pl.n_pairs = total;
   pl.cols.alloc(std::max<long long>(total, 1));
   k_pair_search<true><<<rows.n_tiles, BLK, search_smem, st>>>(
-      rows.box.p, cols.box.p, gbox.p, cols.n_tiles, kc.c_perp, kc.c_para, kc.cull_arg, nullptr,
-      pl.row_ptr.p, pl.cols.p);
+      rows.box32.p, cols.box32.p, gbox.p, cols.n_tiles, ck, nullptr, pl.row_ptr.p, pl.cols.p);
   DS_CHECK_LAUNCH();
   pl.mask.alloc(std::max<long long>(total, 1));
-  k_pair_mask<<<rows.n_tiles, 64, 0, st>>>(rows.n_tiles, pl.row_ptr.p, pl.cols.p, rows.sbox.p,
-                                           cols.sbox.p, kc.c_perp, kc.c_para, kc.cull_arg,
-                                           pl.mask.p);
+  k_pair_mask<<<rows.n_tiles, 64, 0, st>>>(rows.n_tiles, pl.row_ptr.p, pl.cols.p, rows.sbox32.p,
+                                           cols.sbox32.p, ck, pl.mask.p);
   DS_CHECK_LAUNCH();
 }
 
