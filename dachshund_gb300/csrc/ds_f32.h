@@ -124,7 +124,7 @@ struct OpF32 {
   F32Points pts;
   PairList pairs;
   DevBuf<float> rowf, colw, ediag, pdiag;
-  DevBuf<float> p, q, r, z, xc;     // FP32 iteration vectors (sorted, padded)
+  DevBuf<float> p, q, r, z;         // FP32 iteration vectors (sorted, padded)
   DevBuf<MixedState> state;
   DevBuf<double> hist, htrue;
   bool use_ff = false;  // outer residual in float-float arithmetic (else FP64)

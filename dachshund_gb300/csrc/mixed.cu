@@ -1,21 +1,21 @@
 // Mixed-precision Jacobi-PCG: FP32 Krylov iteration with FP64 reliable
 // updates (residual replacement, in the manner of Sleijpen & van der Vorst).
 //
-//   FP64: the iterate x, the right-hand side b, the true residual
-//         r64 = b - A x (FP64 matrix-free kernel, same operator as the plain
+//   FP64: the iterate x (x += alpha p every iteration: one FP64 FMA per
+//         pixel), the right-hand side b, the true residual r64 = b - A x
+//         (FP64-accurate matrix-free kernel, same operator as the plain
 //         form), every CG scalar (r.z, p.q, |r| are FP32 vectors summed in
 //         FP64), and the stopping test |r64| <= tol |b|.
 //   FP32: the search direction p, q = A32 p (FP32 MUFU kernel), the residual
-//         recurrence r, z = M^-1 r and the correction x_c accumulated since
-//         the last reliable update.
-// A reliable update folds x_c into x, recomputes r64 in FP64 and restarts the
-// recurrence from float(r64) while keeping the search direction.  It fires
-// when the recurrence residual has dropped by `delta` since the last update,
-// when it reaches tol |b|, at the iteration cap, or when the recurrence
-// stagnates (then the direction is dropped, beta = 0); the solve ends only on
-// an FP64 residual.  Per iteration: K1 q = A32 p (+ p.q, alpha), K2 the
-// recurrences, K3 the new direction; K4-K7 run only on update iterations
-// (otherwise they return at once on a device flag).
+//         recurrence r and z = M^-1 r.
+// A reliable update recomputes r64 from x and restarts the recurrence from
+// float(r64) while keeping the search direction.  It fires when the
+// recurrence residual has dropped by `delta` since the last update, when it
+// reaches tol |b|, at the iteration cap, or when the recurrence stagnates
+// (then the direction is dropped, beta = 0); the solve ends only on an FP64
+// residual.  Per iteration: K1 q = A32 p (+ p.q, alpha), K2 x and the
+// recurrences, K5 / K6 the update (they return at once on a device flag
+// unless one is due), K7 the new direction.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -170,12 +170,12 @@ __global__ void __launch_bounds__(VB) k_r32_init(int n, MixedState* st, const in
   }
 }
 
-// r = float(r64) (or b when x0 == 0); z = r / pd; p = z; x_c = 0; r.z, |r|.
+// r = float(r64) (or b when x0 == 0); z = r / pd; p = z; r.z, |r|.
 __global__ void __launch_bounds__(VB) k_mx_init(int n, MixedState* st, const int* x_zero,
                                                 const double* __restrict__ b,
                                                 const double* __restrict__ r64,
                                                 float* __restrict__ r, float* __restrict__ z,
-                                                float* __restrict__ p, float* __restrict__ xc,
+                                                float* __restrict__ p,
                                                 const float* __restrict__ pd,
                                                 double* __restrict__ part, double* hist,
                                                 double* htrue) {
@@ -189,7 +189,6 @@ __global__ void __launch_bounds__(VB) k_mx_init(int n, MixedState* st, const int
     r[i] = ri;
     z[i] = zi;
     p[i] = zi;
-    xc[i] = 0.f;
     rz = fma((double)ri, (double)zi, rz);
     rr = fma(rd, rd, rr);
   }
@@ -220,8 +219,9 @@ __global__ void __launch_bounds__(VB) k_mx_init(int n, MixedState* st, const int
   }
 }
 
-// K2: x_c += alpha p; r -= alpha q; z = r / pd; r.z, |r|; decide on an update.
-__global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, float* __restrict__ xc,
+// K2: x += alpha p (FP64); r -= alpha q; z = r / pd; r.z, |r|; decide on an
+// update.
+__global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, double* __restrict__ x,
                                                   float* __restrict__ r, float* __restrict__ z,
                                                   const float* __restrict__ p,
                                                   const float* __restrict__ q,
@@ -229,10 +229,11 @@ __global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, float* 
                                                   double* __restrict__ part, double* hist) {
   if (st->done) return;
   __shared__ double red[VB / 32];
-  const float alpha = (float)st->alpha;
+  const double alpha_d = st->alpha;
+  const float alpha = (float)alpha_d;
   double rz = 0.0, rr = 0.0;
   for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
-    xc[i] = fmaf(alpha, p[i], xc[i]);
+    x[i] = fma(alpha_d, (double)p[i], x[i]);
     const float ri = fmaf(-alpha, q[i], r[i]);
     const float zi = ri / pd[i];
     r[i] = ri;
@@ -263,27 +264,6 @@ __global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, float* 
       st->beta = st->rz / st->rz_old;
       st->counter[1] = 0;
     }
-  }
-}
-
-// K3: p = z + beta p (not on update iterations).
-__global__ void __launch_bounds__(VB) k_mx_dir(int n, const MixedState* st,
-                                               const float* __restrict__ z,
-                                               float* __restrict__ p) {
-  if (st->done || st->need_update) return;
-  const float beta = (float)st->beta;
-  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB)
-    p[i] = fmaf(beta, p[i], z[i]);
-}
-
-// K4: x += x_c (FP64); x_c = 0.
-__global__ void __launch_bounds__(VB) k_mx_fold(int n, const MixedState* st,
-                                                double* __restrict__ x,
-                                                float* __restrict__ xc) {
-  if (st->done || !st->need_update) return;
-  for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB) {
-    x[i] += (double)xc[i];
-    xc[i] = 0.f;
   }
 }
 
@@ -334,17 +314,20 @@ __global__ void __launch_bounds__(VB) k_mx_replace(int n, MixedState* st,
   }
 }
 
-// K7: p = z + beta p after an update; the last block clears the update flags.
-__global__ void __launch_bounds__(VB) k_mx_dir_update(int n, MixedState* st,
-                                                      const float* __restrict__ z,
-                                                      float* __restrict__ p) {
-  if (!st->need_update) return;
+// K7: p = z + beta p (beta from K2, or from K6's restart after an update);
+// after an update the last block clears the update flags.  Every block reads
+// the flag before it arrives, and the flag is cleared only after all have
+// arrived.
+__global__ void __launch_bounds__(VB) k_mx_dir(int n, MixedState* st,
+                                               const float* __restrict__ z,
+                                               float* __restrict__ p) {
+  const bool upd = st->need_update != 0;
   if (!st->done) {
     const float beta = (float)st->beta;
     for (int i = blockIdx.x * VB + threadIdx.x; i < n; i += gridDim.x * VB)
       p[i] = fmaf(beta, p[i], z[i]);
   }
-  if (last_block_arrive(&st->counter[2]) && threadIdx.x == 0) {
+  if (upd && last_block_arrive(&st->counter[2]) && threadIdx.x == 0) {
     st->need_update = 0;
     st->skip_update = 1;
     st->counter[2] = 0;
@@ -380,7 +363,7 @@ __device__ __forceinline__ double cta_sum(double v, double* sm) {
 template <int MODE>
 __global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero,
                           const int* __restrict__ inv, const float* __restrict__ L,
-                          float* __restrict__ xc, float* __restrict__ r,
+                          double* __restrict__ x, float* __restrict__ r,
                           float* __restrict__ z, float* __restrict__ p,
                           const float* __restrict__ q, const double* __restrict__ b,
                           const double* __restrict__ r64, double* __restrict__ part, double* hist,
@@ -396,14 +379,13 @@ __global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero
   double rd;
   float ri;
   if (MODE == 0) {
-    const float alpha = (float)st->alpha;
-    xc[pos] = fmaf(alpha, p[pos], xc[pos]);
-    ri = fmaf(-alpha, q[pos], r[pos]);
+    const double alpha_d = st->alpha;
+    x[pos] = fma(alpha_d, (double)p[pos], x[pos]);
+    ri = fmaf(-(float)alpha_d, q[pos], r[pos]);
     rd = ri;
   } else {
     rd = (MODE == 2 && *x_zero) ? b[pos] : r64[pos];
     ri = (float)rd;
-    if (MODE == 2) xc[pos] = 0.f;
   }
   r[pos] = ri;
   rs[k] = ri;
@@ -533,7 +515,6 @@ void ensure_op_f32(ds_operator* op, double inner_cut) {
   f->q.alloc(np);
   f->r.alloc(np);
   f->z.alloc(np);
-  f->xc.alloc(np);
   f->state.alloc(1);
   f->use_ff = ff_usable(op->kc);
   if (f->use_ff) build_ff_points(f->ffd, op->pix, op->kc, st);
@@ -621,14 +602,14 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   double* pc_part = op->partial2.p + op->pix.n_tiles;
   if (pc) {
     // padding stays 0 in every FP32 vector
-    for (float* v : {f.z.p, f.r.p, f.p.p, f.xc.p})
+    for (float* v : {f.z.p, f.r.p, f.p.p})
       DS_CUDA(cudaMemsetAsync(v, 0, np * sizeof(float), st));
     k_pc_iter<2><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-        pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, f.xc.p, f.r.p, f.z.p, f.p.p, nullptr,
+        pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p, f.p.p, nullptr,
         op->b.p, op->r.p, pc_part, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   } else {
-    k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p, f.xc.p,
+    k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p,
                                 f.pdiag.p, op->partial.p, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   }
@@ -670,22 +651,18 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);
     if (pc) {
       k_pc_iter<0><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p,
+          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p, f.p.p, f.q.p,
           nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);                    // K2
       DS_CHECK_LAUNCH();
     } else {
-      k_mx_update<<<g, VB, 0, st>>>(np, S, f.xc.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
+      k_mx_update<<<g, VB, 0, st>>>(np, S, op->x.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
                                     op->partial.p, f.hist.p);                // K2
       DS_CHECK_LAUNCH();
     }
-    k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K3
-    DS_CHECK_LAUNCH();
-    k_mx_fold<<<g, VB, 0, st>>>(np, S, op->x.p, f.xc.p);                    // K4
-    DS_CHECK_LAUNCH();
     outer_residual(upd);                                                      // K5
     if (pc) {
       k_pc_iter<1><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, f.xc.p, f.r.p, f.z.p, f.p.p,
+          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p, f.p.p,
           nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);           // K6
       DS_CHECK_LAUNCH();
     } else {
@@ -693,7 +670,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
                                      f.hist.p, f.htrue.p);                   // K6
       DS_CHECK_LAUNCH();
     }
-    k_mx_dir_update<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                 // K7
+    k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K7
     DS_CHECK_LAUNCH();
     if (it % CHECK == 0) {
       const int slot = issued % NSLOT;
