@@ -29,6 +29,7 @@ struct LearnedNet {
   size_t n_cur = 0;
   int nsk_cur = 0;
   DevBuf<int> nbr;
+  DevBuf<double2> skxy;  // (x, y) per skewer
   DevBuf<float> gw, X, h[N_LAYERS + 1], Z[N_LAYERS + 1], cat[N_LAYERS], Y, dY, dh, dh2, dZ, dcat,
       part;
   DevBuf<double> dpart;

@@ -61,36 +61,98 @@ inline unsigned grid1(size_t n, int nt = 256) { return (unsigned)((n + nt - 1) /
 
 // ---- geometry and inputs --------------------------------------------------------
 
-// The 8 nearest skewers of every skewer (brute force over the skewer (x, y)),
-// with weights g = exp(-d^2 / (2 l_perp^2)).
-__global__ void k_knn(int n_sk, int n_per, const double* __restrict__ rec, double inv2l2,
-                      int* __restrict__ nbr, float* __restrict__ g) {
+// (x, y) of every skewer (its first record) in one compact array.
+__global__ void k_skewer_xy(int n_sk, int n_per, const double* __restrict__ rec,
+                            double2* __restrict__ xy) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n_sk) return;
-  const double xs = rec[(size_t)s * n_per * 5], ys = rec[(size_t)s * n_per * 5 + 1];
+  if (s < n_sk) xy[s] = make_double2(rec[(size_t)s * n_per * 5], rec[(size_t)s * n_per * 5 + 1]);
+}
+
+// The 8 nearest skewers of every skewer (brute force over the skewer (x, y)),
+// with weights g = exp(-d^2 / (2 l_perp^2)); nearer first, ties by index, the
+// missing ones (fewer than 9 skewers) pointing at the skewer itself with
+// g = 0.  One warp per skewer: lane l keeps the 8 nearest of skewers
+// l, l + 32, ... in order, then 8 rounds of a warp minimum over the lanes'
+// heads merge them.
+__global__ void k_knn(int n_sk, const double2* __restrict__ xy, double inv2l2,
+                      int* __restrict__ nbr, float* __restrict__ g) {
+  const int s = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= n_sk) return;  // warp-uniform
+  const double2 ps = xy[s];
   double bd[NB_K];
   int bi[NB_K];
+#pragma unroll
   for (int k = 0; k < NB_K; ++k) {
     bd[k] = 1e300;
     bi[k] = s;
   }
-  for (int o = 0; o < n_sk; ++o) {
+  for (int o = lane; o < n_sk; o += 32) {
     if (o == s) continue;
-    const double dx = rec[(size_t)o * n_per * 5] - xs, dy = rec[(size_t)o * n_per * 5 + 1] - ys;
-    const double d2 = dx * dx + dy * dy;
-    if (d2 >= bd[NB_K - 1]) continue;
-    int k = NB_K - 1;
-    while (k > 0 && bd[k - 1] > d2) {
-      bd[k] = bd[k - 1];
-      bi[k] = bi[k - 1];
-      --k;
+    const double2 q = xy[o];
+    const double dx = q.x - ps.x, dy = q.y - ps.y;
+    const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    if (d2 >= bd[NB_K - 1]) continue;  // o only grows: an equal d2 stays behind
+    // insertion after every entry <= d2 (static indices only)
+    bool placed = false;
+#pragma unroll
+    for (int k = NB_K - 1; k > 0; --k) {
+      if (!placed) {
+        if (bd[k - 1] > d2) {
+          bd[k] = bd[k - 1];
+          bi[k] = bi[k - 1];
+        } else {
+          bd[k] = d2;
+          bi[k] = o;
+          placed = true;
+        }
+      }
     }
-    bd[k] = d2;
-    bi[k] = o;
+    if (!placed) {
+      bd[0] = d2;
+      bi[0] = o;
+    }
   }
-  for (int k = 0; k < NB_K; ++k) {
-    nbr[s * NB_K + k] = bi[k];
-    g[s * NB_K + k] = bi[k] == s ? 0.f : (float)exp(-bd[k] * inv2l2);
+  constexpr unsigned full = 0xffffffffu;
+  double od[NB_K];
+  int oi[NB_K];
+#pragma unroll
+  for (int r = 0; r < NB_K; ++r) {
+    double d = bd[0];
+    int idx = bi[0], who = lane;
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+      const double d2 = __shfl_xor_sync(full, d, m);
+      const int i2 = __shfl_xor_sync(full, idx, m), w2 = __shfl_xor_sync(full, who, m);
+      if (d2 < d || (d2 == d && (i2 < idx || (i2 == idx && w2 < who)))) {
+        d = d2;
+        idx = i2;
+        who = w2;
+      }
+    }
+    od[r] = d;
+    oi[r] = idx;
+    if (lane == who) {  // pop the head
+#pragma unroll
+      for (int k = 0; k < NB_K - 1; ++k) {
+        bd[k] = bd[k + 1];
+        bi[k] = bi[k + 1];
+      }
+      bd[NB_K - 1] = 1e300;
+      bi[NB_K - 1] = s;
+    }
+  }
+  if (lane < NB_K) {
+    double d = od[0];
+    int idx = oi[0];
+#pragma unroll
+    for (int r = 1; r < NB_K; ++r)
+      if (lane == r) {
+        d = od[r];
+        idx = oi[r];
+      }
+    nbr[s * NB_K + lane] = idx;
+    g[s * NB_K + lane] = idx == s ? 0.f : (float)exp(-d * inv2l2);
   }
 }
 
@@ -251,26 +313,39 @@ __global__ void k_colsum_part(int M, int N, const float* __restrict__ D,
 
 // ---- message passing ---------------------------------------------------------------
 
-// cat_i = [h_i | h_{i-1} + h_{i+1} | sum_n g_n h_{nb_n, k}].
+// cat_i = [h_i | h_{i-1} + h_{i+1} | sum_n g_n h_{nb_n, k}], four channels
+// per thread (H % 4 == 0; 128-bit loads and stores).
 __global__ void k_agg_fwd(int n, int n_per, int H, const float* __restrict__ h,
                           const int* __restrict__ nbr, const float* __restrict__ g,
                           float* __restrict__ cat) {
+  const int H4 = H >> 2;
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= (size_t)n * H) return;
-  const int i = (int)(q / H), c = (int)(q % H);
+  if (q >= (size_t)n * H4) return;
+  const int i = (int)(q / H4), c4 = (int)(q % H4);
   const int s = i / n_per, k = i % n_per;
-  const float hi = h[q];
-  float az = 0.f;
-  if (k > 0) az += h[q - H];
-  if (k + 1 < n_per) az += h[q + H];
-  float an = 0.f;
+  const float4* h4 = reinterpret_cast<const float4*>(h);
+  const float4 hi = h4[q];
+  float4 az = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (k > 0) {
+    const float4 v = h4[q - H4];
+    az = make_float4(az.x + v.x, az.y + v.y, az.z + v.z, az.w + v.w);
+  }
+  if (k + 1 < n_per) {
+    const float4 v = h4[q + H4];
+    az = make_float4(az.x + v.x, az.y + v.y, az.z + v.z, az.w + v.w);
+  }
+  float4 an = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-  for (int m = 0; m < NB_K; ++m)
-    an = fmaf(g[s * NB_K + m], h[((size_t)nbr[s * NB_K + m] * n_per + k) * H + c], an);
-  float* o = cat + (size_t)i * 3 * H;
-  o[c] = hi;
-  o[H + c] = az;
-  o[2 * H + c] = an;
+  for (int m = 0; m < NB_K; ++m) {
+    const float gm = g[s * NB_K + m];
+    const float4 v = h4[((size_t)nbr[s * NB_K + m] * n_per + k) * H4 + c4];
+    an = make_float4(fmaf(gm, v.x, an.x), fmaf(gm, v.y, an.y), fmaf(gm, v.z, an.z),
+                     fmaf(gm, v.w, an.w));
+  }
+  float4* o = reinterpret_cast<float4*>(cat + (size_t)i * 3 * H);
+  o[c4] = hi;
+  o[H4 + c4] = az;
+  o[2 * H4 + c4] = an;
 }
 
 // dh += adjoint of the aggregation applied to dcat (the neighbour part
@@ -566,6 +641,7 @@ void LearnedNet::ensure(int n_sk, int n_per) {
   nsk_cur = n_sk;
   nbr.alloc((size_t)n_sk * NB_K);
   gw.alloc((size_t)n_sk * NB_K);
+  skxy.alloc(n_sk);
   X.alloc(n * F_IN);
   for (int l = 0; l <= N_LAYERS; ++l) {
     h[l].alloc(n * H);
@@ -620,13 +696,16 @@ void LearnedNet::forward(int n_sk, int n_per, const double* rec) {
   rec_cur = rec;
   cudaStream_t st = ctx->stream;
   const int n = n_sk * n_per;
-  k_knn<<<grid1(n_sk, 128), 128, 0, st>>>(n_sk, n_per, rec, kc.c_perp, nbr.p, gw.p);
+  k_skewer_xy<<<grid1(n_sk), 256, 0, st>>>(n_sk, n_per, rec, skxy.p);
+  DS_CHECK_LAUNCH();
+  k_knn<<<grid1((size_t)n_sk * 32), 256, 0, st>>>(n_sk, skxy.p, kc.c_perp, nbr.p, gw.p);
   DS_CHECK_LAUNCH();
   k_features<<<grid1(n), 256, 0, st>>>(n, n_per, rec, gw.p, X.p);
   DS_CHECK_LAUNCH();
   gemm_fwd(n, H, F_IN, X.p, F_IN, W_in, b_in, Z[0].p, h[0].p, nullptr, 1);
   for (int l = 0; l < N_LAYERS; ++l) {
-    k_agg_fwd<<<grid1((size_t)n * H), 256, 0, st>>>(n, n_per, H, h[l].p, nbr.p, gw.p, cat[l].p);
+    k_agg_fwd<<<grid1((size_t)n * (H / 4)), 256, 0, st>>>(n, n_per, H, h[l].p, nbr.p, gw.p,
+                                                          cat[l].p);
     DS_CHECK_LAUNCH();
     if (tc_active && layer_tc_usable(n, H, 3 * H)) {
       if (!wt.p) wt.alloc((size_t)3 * H * H);
@@ -634,8 +713,9 @@ void LearnedNet::forward(int n_sk, int n_per, const double* rec) {
         tc_err.alloc(1);
         DS_CUDA(cudaMemsetAsync(tc_err.p, 0, sizeof(int), st));
       }
+      // inference only: no Z (the backward pass alone reads it)
       launch_layer_tc(n, cat[l].p, reinterpret_cast<const __nv_bfloat16*>(wbf.p) + W_l[l].off,
-                      params.p + b_l[l].off, Z[l + 1].p, h[l + 1].p, h[l].p, wt.p, tc_err.p, st);
+                      params.p + b_l[l].off, nullptr, h[l + 1].p, h[l].p, wt.p, tc_err.p, st);
     } else {
       gemm_fwd(n, H, 3 * H, cat[l].p, 3 * H, W_l[l], b_l[l], Z[l + 1].p, h[l + 1].p, h[l].p, 2);
     }

@@ -161,14 +161,14 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
         tmem_ld<32>(tmem + ((uint32_t)(32 * rs) << 16) + db * 128u + 32u * j, d);
         const float4* b4 = reinterpret_cast<const float4*>(bias + 32 * j);
         const float4* r4 = reinterpret_cast<const float4*>(res + m * LG_N + 32 * j);
-        float4* z4 = reinterpret_cast<float4*>(Z + m * LG_N + 32 * j);
+        float4* z4 = Z ? reinterpret_cast<float4*>(Z + m * LG_N + 32 * j) : nullptr;
         float4* o4 = reinterpret_cast<float4*>(out + m * LG_N + 32 * j);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const float4 bb = b4[q], rr = r4[q];
           const float4 zz = make_float4(d[4 * q] + bb.x, d[4 * q + 1] + bb.y, d[4 * q + 2] + bb.z,
                                         d[4 * q + 3] + bb.w);
-          z4[q] = zz;
+          if (Z) z4[q] = zz;
           o4[q] = make_float4(rr.x + fmaxf(zz.x, 0.f), rr.y + fmaxf(zz.y, 0.f),
                               rr.z + fmaxf(zz.z, 0.f), rr.w + fmaxf(zz.w, 0.f));
         }
@@ -219,7 +219,9 @@ __global__ void __launch_bounds__(LG_THREADS, 1)
 bool layer_tc_usable(int M, int N, int K) { return N == LG_N && K == LG_K && M % 128 == 0; }
 
 // out = res + relu(Z), Z = A W + b for a message-passing layer (TF32 tensor
-// cores); wt: scratch for W^T (LG_N x LG_K floats), err: device error flag.
+// cores); Z is stored only when given (training keeps it for the backward
+// pass, inference does not); wt: scratch for W^T (LG_N x LG_K floats), err:
+// device error flag.
 void launch_layer_tc(int M, const float* A, const __nv_bfloat16* W, const float* bias, float* Z,
                      float* out, const float* res, float* wt, int* err, cudaStream_t st) {
   k_wt_f32<<<(LG_K * LG_N + 255) / 256, 256, 0, st>>>(W, wt);
