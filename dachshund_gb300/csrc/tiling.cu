@@ -183,6 +183,52 @@ __global__ void k_unit_boxes_idx(const double* __restrict__ rec, int n, int stri
 
 // key = node << 32 | order-preserving bits of the coordinate along the
 // node's split axis (0 for nodes that are already leaves).
+// node_of_unit for the units of every node of a level (one CTA per node).
+__global__ void k_node_units(const int2* __restrict__ nodes, int* __restrict__ node_of_unit) {
+  const int k = blockIdx.x;
+  const int2 nd = nodes[k];
+  for (int u = nd.x + threadIdx.x; u < nd.y; u += blockDim.x) node_of_unit[u] = k;
+}
+
+// Split axis of every node of a level with at least two units: the longest
+// side of the union of its unit boxes (the first of equal sides), else -1.
+// Min and max are exact, so the order of the reduction does not matter.
+__global__ void k_node_axis(const int2* __restrict__ nodes, const double* __restrict__ box,
+                            int* __restrict__ node_axis) {
+  __shared__ double sm[6][128];
+  const int k = blockIdx.x, t = threadIdx.x;
+  const int2 nd = nodes[k];
+  if (nd.y - nd.x < 2) {
+    if (t == 0) node_axis[k] = -1;
+    return;
+  }
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int u = nd.x + t; u < nd.y; u += blockDim.x)
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = fmin(lo[c], box[(size_t)u * 6 + c]);
+      hi[c] = fmax(hi[c], box[(size_t)u * 6 + 3 + c]);
+    }
+  for (int c = 0; c < 3; ++c) {
+    sm[c][t] = lo[c];
+    sm[3 + c][t] = hi[c];
+  }
+  __syncthreads();
+  for (int s = 64; s > 0; s >>= 1) {
+    if (t < s)
+      for (int c = 0; c < 3; ++c) {
+        sm[c][t] = fmin(sm[c][t], sm[c][t + s]);
+        sm[3 + c][t] = fmax(sm[3 + c][t], sm[3 + c][t + s]);
+      }
+    __syncthreads();
+  }
+  if (t == 0) {
+    int ax = 0;
+    for (int c = 1; c < 3; ++c)
+      if (sm[3 + c][0] - sm[c][0] > sm[3 + ax][0] - sm[ax][0]) ax = c;
+    node_axis[k] = ax;
+  }
+}
+
 __global__ void k_kd_keys(const double* __restrict__ rec, int n, int stride,
                           const int* __restrict__ idx, const int* __restrict__ node_of_unit,
                           const int* __restrict__ node_axis, double sx, double sy, double sz,
@@ -378,54 +424,66 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
   (void)ps;
   constexpr int UPT = TILE / SUBTILE;  // units per tile
   const int nu = (n + SUBTILE - 1) / SUBTILE;
-  struct Node { int u0, u1; };
-  std::vector<Node> nodes{{0, nu}};
-  std::vector<int> node_of_unit(nu), node_axis;
-  std::vector<double> hbox((size_t)nu * 6);
+  // The nodes of every level follow from the unit counts alone (only the
+  // split axes depend on the points): all levels are listed here and copied
+  // once; each level then runs on the device without a host round trip.
+  std::vector<int2> all_nodes;
+  std::vector<size_t> level_off;
+  {
+    std::vector<int2> nodes{make_int2(0, nu)};
+    for (;;) {
+      bool any = false;
+      for (auto& nd : nodes) any |= (nd.y - nd.x) >= 2;
+      if (!any) break;
+      level_off.push_back(all_nodes.size());
+      all_nodes.insert(all_nodes.end(), nodes.begin(), nodes.end());
+      std::vector<int2> next;
+      next.reserve(nodes.size() * 2);
+      for (auto& nd : nodes) {
+        const int len = nd.y - nd.x;
+        if (len < 2) {
+          next.push_back(nd);
+        } else {
+          const int ntile = (len + UPT - 1) / UPT;
+          const int um = ntile >= 2 ? nd.x + UPT * (ntile / 2) : nd.x + len / 2;
+          next.push_back(make_int2(nd.x, um));
+          next.push_back(make_int2(um, nd.y));
+        }
+      }
+      nodes.swap(next);
+    }
+    level_off.push_back(all_nodes.size());
+  }
+  const int n_levels = (int)level_off.size() - 1;
+  if (n_levels <= 0) return;
+  DevBuf<int2> d_nodes;
+  d_nodes.alloc(all_nodes.size());
+  DS_CUDA(cudaMemcpyAsync(d_nodes.p, all_nodes.data(), all_nodes.size() * sizeof(int2),
+                          cudaMemcpyHostToDevice, st));
   DevBuf<double> box;
   box.alloc((size_t)nu * 6);
   DevBuf<int> d_not, d_axis, idx2;
   d_not.alloc(nu);
+  d_axis.alloc(level_off[n_levels] - level_off[n_levels - 1]);
   idx2.alloc(n);
   DevBuf<unsigned long long> keys, keys2;
   keys.alloc(n);
   keys2.alloc(n);
   DevBuf<unsigned char> tmp;
-  for (int level = 0; level < 64; ++level) {
-    bool any = false;
-    for (auto& nd : nodes) any |= (nd.u1 - nd.u0) >= 2;
-    if (!any) break;
+  for (int level = 0; level < n_levels; ++level) {
+    const int nn = (int)(level_off[level + 1] - level_off[level]);
+    const int2* nodes = d_nodes.p + level_off[level];
+    k_node_units<<<nn, 128, 0, st>>>(nodes, d_not.p);
+    DS_CHECK_LAUNCH();
     k_unit_boxes_idx<<<nu, SUBTILE, 0, st>>>(d_rec, n, stride, idx.p, sx, sy, sz, box.p);
     DS_CHECK_LAUNCH();
-    DS_CUDA(cudaMemcpyAsync(hbox.data(), box.p, hbox.size() * sizeof(double),
-                            cudaMemcpyDeviceToHost, st));
-    DS_CUDA(cudaStreamSynchronize(st));
-    node_axis.assign(nodes.size(), -1);
-    for (size_t k = 0; k < nodes.size(); ++k) {
-      const Node& nd = nodes[k];
-      for (int u = nd.u0; u < nd.u1; ++u) node_of_unit[u] = (int)k;
-      if (nd.u1 - nd.u0 < 2) continue;
-      double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-      for (int u = nd.u0; u < nd.u1; ++u)
-        for (int c = 0; c < 3; ++c) {
-          lo[c] = std::min(lo[c], hbox[(size_t)u * 6 + c]);
-          hi[c] = std::max(hi[c], hbox[(size_t)u * 6 + 3 + c]);
-        }
-      int ax = 0;
-      for (int c = 1; c < 3; ++c)
-        if (hi[c] - lo[c] > hi[ax] - lo[ax]) ax = c;
-      node_axis[k] = ax;
-    }
-    d_axis.alloc(nodes.size());
-    DS_CUDA(cudaMemcpyAsync(d_not.p, node_of_unit.data(), nu * sizeof(int),
-                            cudaMemcpyHostToDevice, st));
-    DS_CUDA(cudaMemcpyAsync(d_axis.p, node_axis.data(), nodes.size() * sizeof(int),
-                            cudaMemcpyHostToDevice, st));
+    k_node_axis<<<nn, 128, 0, st>>>(nodes, box.p, d_axis.p);
+    DS_CHECK_LAUNCH();
     k_kd_keys<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, idx.p, d_not.p, d_axis.p, sx,
                                                   sy, sz, keys.p);
     DS_CHECK_LAUNCH();
     int node_bits = 1;
-    while ((1ull << node_bits) < nodes.size()) ++node_bits;
+    while ((1ull << node_bits) < (unsigned long long)nn) ++node_bits;
     size_t tmp_bytes = 0;
     DS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
                                             0, 32 + node_bits, st));
@@ -433,22 +491,6 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
     DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
                                             0, 32 + node_bits, st));
     std::swap(idx.p, idx2.p);
-    std::vector<Node> next;
-    next.reserve(nodes.size() * 2);
-    for (auto& nd : nodes) {
-      const int len = nd.u1 - nd.u0;
-      if (len < 2) {
-        next.push_back(nd);
-      } else {
-        const int ntile = (len + UPT - 1) / UPT;
-        const int um = ntile >= 2 ? nd.u0 + UPT * (ntile / 2) : nd.u0 + len / 2;
-        next.push_back({nd.u0, um});
-        next.push_back({um, nd.u1});
-      }
-    }
-    nodes.swap(next);
-    // The host vectors and scratch are reused next level: wait for this one.
-    DS_CUDA(cudaStreamSynchronize(st));
   }
 }
 
