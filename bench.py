@@ -72,7 +72,9 @@ def dist():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region
+    (every 20 ms; only the samples taken between mark_start() and mark_end()
+    count, all of them if none fell inside)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -82,21 +84,32 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
             self.proc = None
+            return
+        deadline = time.perf_counter() + 5.0  # sampling is live before the region starts
+        while not self.lines and time.perf_counter() < deadline and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
 
     def stop(self):
         if not self.proc:
@@ -106,9 +119,13 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        lines = self.lines
+        if self.t0 is not None and self.t1 is not None:
+            inside = [x for x in lines if self.t0 <= x[0] <= self.t1]
+            lines = inside or lines
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -397,6 +414,7 @@ def run_ours(args, rank, world, local):
     clocks.start()
     times, solve_prof, map_prof, results = [], [], [], []
     launches0 = ctx.profile()["kernel_launches"]
+    clocks.mark_start()
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -423,6 +441,7 @@ def run_ours(args, rank, world, local):
         barrier()
         times.append(e0.elapsed_time(e1) / 1e3)
         results.append(res)
+    clocks.mark_end()
     launches = (ctx.profile()["kernel_launches"] - launches0) / args.steps
     clk = clocks.stop()
     step_s = allmax(statistics.mean(times))
