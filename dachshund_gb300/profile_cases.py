@@ -13,6 +13,9 @@ dachshund_gb300.profile_cases <case>``):
   learned_solve  one held-out 262,144-pixel system: Jacobi mixed solve, the
                  network's forward pass and the learned-preconditioned solve
                  (trained weights in dachshund_gb300/weights)
+  pipe_rates     per-SM throughput of FP64 FMA, FP32 FMA, MUFU ex2, FP64
+                 exp() and FP64 -> int32 (probes/pipe_rates.cu, compiled here
+                 for sm_103a; the rates behind the pair kernels' rooflines)
 """
 from __future__ import annotations
 
@@ -21,9 +24,27 @@ import sys
 import numpy as np
 
 
+def pipe_rates() -> None:
+    """Compile probes/pipe_rates.cu for sm_103a and run it."""
+    import importlib
+    import os
+    import subprocess
+
+    build = importlib.import_module("dachshund_gb300.build")  # the module, not build()
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "probes", "pipe_rates.cu")
+    os.makedirs(build.BUILD, exist_ok=True)
+    exe = os.path.join(build.BUILD, "pipe_rates")
+    subprocess.run([build.nvcc()] + build.ARCH + ["-O3", "-std=c++17", src, "-o", exe],
+                   check=True)
+    subprocess.run([exe], check=True)
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     case = argv[0] if argv else "ff_residual"
+    if case == "pipe_rates":
+        pipe_rates()
+        return
     import torch
 
     from dachshund_gb300 import (BatchSolver, Context, MixedParams, SignalCovarParams,
