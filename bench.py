@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config3", choices=["config2", "config3"])
+    ap.add_argument("--workload", default="wf262144", choices=["wf32768", "wf262144"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-chunks (512 chunks x 64 RHS) measurement")

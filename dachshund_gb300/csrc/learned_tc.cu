@@ -6,7 +6,7 @@
 // relative perturbation near 1e-3 of the hidden state against the FP32
 // CUDA-core GEMM that training uses (whose gradients the CPU oracle checks);
 // the preconditioner built from it differs correspondingly little, and the
-// solve it preconditions is still judged by its FP64-accurate residual.
+// solve it preconditions still stops on its FP64-accurate residual.
 //
 // Per CTA (one per SM, persistent over 128-row tiles):
 //   * warps 0-3 load K chunks of 32 (A rows of the tile and W^T rows) into 4

@@ -144,7 +144,7 @@ def gpu_system(seed, n_sk=1024, n_per=256, box=80.0, dz=synth.DZ, device="cuda",
     z_k = (k + 1/2) dz, noise n ~ U[0.05, 0.3], d = GRF (Gaussian power
     spectrum of the kernel, 1 Mpc/h periodic grid, trilinear) + n N(0, 1).
     Generated with torch's seeded generator on the GPU (same law as
-    ``synth.config3``, different random streams)."""
+    ``synth.wf262144``, different random streams)."""
     import torch
 
     g = torch.Generator(device=device).manual_seed(int(seed))

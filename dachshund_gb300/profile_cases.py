@@ -53,7 +53,7 @@ def main(argv=None):
     ctx = Context(0)
     sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
     if case in ("ff_residual", "f32_matvec", "tc_inner"):
-        w = synth.config3(0)
+        w = synth.wf262144(0)
         rec = pixel_to_wpixel(w.pixels)
         op = WFVectorW(ctx, rec, sp)
         if case == "ff_residual":

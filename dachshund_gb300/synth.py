@@ -177,7 +177,7 @@ def _grf_workload(name, n_sk, n_per, box_xy, seed, map_shape, tol):
                     pcg_tol=tol, n_skewers=n_sk, pix_per_skewer=n_per)
 
 
-def config1(seed: int = 0) -> Workload:
+def wf4096(seed: int = 0) -> Workload:
     """4,096 pixels: 64 skewers x 64 in [0,32)^2 x [0,128); dense-Cholesky d;
     tol 1e-5, max 200 iterations; map 32 x 32 x 128."""
     rng = np.random.default_rng(seed)
@@ -187,13 +187,13 @@ def config1(seed: int = 0) -> Workload:
                     pcg_tol=1e-5, pcg_max_iter=200, n_skewers=64, pix_per_skewer=64)
 
 
-def config2(seed: int = 0) -> Workload:
+def wf32768(seed: int = 0) -> Workload:
     """32,768 pixels: 256 skewers x 128 in [0,40)^2 x [0,256); GRF d; tol 1e-8;
     map 40 x 40 x 256."""
     return _grf_workload("wf-32768px-grf", 256, 128, 40.0, seed, (40, 40, 256), 1e-8)
 
 
-def config3(seed: int = 0) -> Workload:
+def wf262144(seed: int = 0) -> Workload:
     """262,144 pixels: 1,024 skewers x 256 in [0,80)^2 x [0,512); GRF d;
     tol 1e-8; map 80 x 80 x 512."""
     return _grf_workload("wf-262144px-grf", 1024, 256, 80.0, seed, (80, 80, 512), 1e-8)
@@ -248,4 +248,4 @@ def uniform_map_coords(lx, ly, lz, nx, ny, nz) -> np.ndarray:
     return out
 
 
-WORKLOADS = {"config1": config1, "config2": config2, "config3": config3}
+WORKLOADS = {"wf4096": wf4096, "wf32768": wf32768, "wf262144": wf262144}

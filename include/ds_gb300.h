@@ -384,7 +384,7 @@ int ds_batch_product_f32_dev(ds_batch* batch, const double* p, double* q);
  * triangle) whose M^-1 = L L^T preconditions that skewer's block.  Trained
  * by its own forward / backward / Adam kernels on solutions of the solver;
  * the mixed-precision PCG then runs to the same tolerance from y0 with
- * M^-1 (Jacobi-PCG stays the fallback and the judge of its error). */
+ * M^-1 (Jacobi-PCG stays the fallback and the yardstick for its error). */
 typedef struct ds_learned ds_learned;
 
 /* kp: the kernel parameters of the systems it is trained for (exact). */

@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE -- the CPU oracle for the Wiener-filter path.
 
-Two checkers behind one numpy interface:
+Two oracle libraries behind one numpy interface:
 
 * ``impl="port"``: ``oracle/libdsoracle.so``, the C restatement in
   ``oracle/ds_oracle.c`` (built by ``make -C oracle port``; builds on any host);

@@ -28,4 +28,4 @@ def golden():
     import numpy as np
 
     d = os.path.join(ROOT, "tests", "golden")
-    return {k: np.load(os.path.join(d, k + ".npz")) for k in ("config1", "small", "edge")}
+    return {k: np.load(os.path.join(d, k + ".npz")) for k in ("wf4096", "small", "edge")}

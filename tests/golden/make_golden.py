@@ -8,7 +8,7 @@ the oracle restatement (CPU tests) and the CUDA path (GPU tests).
     python tests/golden/make_golden.py
 
 Outputs (all float64 unless noted):
-  config1.npz   4,096-pixel workload: pixels, the reference app's map.bin,
+  wf4096.npz   4,096-pixel workload: pixels, the reference app's map.bin,
                 its iteration count (parsed from the app's trace), the W-form
                 PCG solution x and residual history from the harness.
   small.npz     512-pixel GRF workload: A_product / A_residual in both forms,
@@ -48,14 +48,14 @@ def run_app(w: synth.Workload):
     return m, (int(it.group(1)) if it else -1)
 
 
-def make_config1():
-    w = synth.config1()
+def make_wf4096():
+    w = synth.wf4096()
     m, iters = run_app(w)
     wrec = oracle.pixel_to_wpixel(w.pixels)
     x, ok, it2, hist = oracle.solve_pcg("w", wrec, VS, LP, LQ, w.pcg_max_iter, w.pcg_step_r,
                                         w.pcg_tol, impl="ref")
     assert ok and it2 == iters, (ok, it2, iters)
-    np.savez_compressed(os.path.join(HERE, "config1.npz"), pixels=w.pixels, map=m,
+    np.savez_compressed(os.path.join(HERE, "wf4096.npz"), pixels=w.pixels, map=m,
                         num_iters=iters, x=x, hist=hist,
                         params=np.array([w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz,
                                          w.pcg_tol, w.pcg_max_iter, w.pcg_step_r]))
@@ -133,5 +133,5 @@ if __name__ == "__main__":
         sys.exit("reference harness unavailable: build oracle/_ref first")
     make_edge()
     make_small()
-    make_config1()
+    make_wf4096()
     print("golden vectors written to", HERE)

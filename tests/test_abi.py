@@ -87,7 +87,7 @@ def test_map_coords_and_config_format(tmp_path):
 
 
 def test_synth_workloads_deterministic_and_shaped():
-    a, b = synth.config2(), synth.config2()
+    a, b = synth.wf32768(), synth.wf32768()
     np.testing.assert_array_equal(a.pixels, b.pixels)
     assert a.n == 32768 and a.n_map == 40 * 40 * 256
     p = a.pixels

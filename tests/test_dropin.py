@@ -53,7 +53,7 @@ def test_cxx_app_path_on_gpu(tmp_path, golden):
     the reference's iteration count, map within 1e-8 of the reference app's
     map.bin; the closed-form solve within 1e-6 of the PCG solution (tol 1e-5)."""
     _build_lib()
-    g = golden["config1"]
+    g = golden["wf4096"]
     pix = g["pixels"]
     lx, ly, lz, nx, ny, nz, tol, max_iter, step_r = g["params"]
     exe = tmp_path / "wf_app"

@@ -123,11 +123,11 @@ def test_edge_golden(ctx, golden, case, form):
     assert rel(x, e[f"{case}_x_{form}"]) < 1e-8
 
 
-def test_config1_app_path(ctx, golden):
+def test_wf4096_app_path(ctx, golden):
     """The reference app's path (app/dachshund.cc:229-264) on 4,096 pixels:
     W-form PCG to 1e-5 then smp_product on the 32x32x128 grid.  Same
     iteration count as the reference and the map within 1e-8 relative."""
-    g = golden["config1"]
+    g = golden["wf4096"]
     pix = g["pixels"]
     lx, ly, lz, nx, ny, nz, tol, max_iter, step_r = g["params"]
     op = WFVectorW(ctx, pixel_to_wpixel(pix), TABLE)

@@ -93,10 +93,10 @@ def test_edge_golden(golden, case, form):
     np.testing.assert_array_equal(x, e[f"{case}_x_{form}"])
 
 
-def test_config1_app_golden(golden):
+def test_wf4096_app_golden(golden):
     """The reference app's map on the 4,096-pixel workload: W-form PCG
     (tol 1e-5) then smp_product, restated by the port."""
-    g = golden["config1"]
+    g = golden["wf4096"]
     pix = g["pixels"]
     lx, ly, lz, nx, ny, nz, tol, max_iter, step_r = g["params"]
     wrec = oracle.pixel_to_wpixel(pix)
