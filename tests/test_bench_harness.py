@@ -1,6 +1,9 @@
 """Host logic of bench.py's measurement harness, without a GPU: the clock
 record keeps only the samples taken inside the timed region and reports the
-median SM clock under load and every throttle reason seen there."""
+median SM clock under load and every throttle reason seen there; the
+reference arm (``--impl reference``, the CPU oracle timed on a bounded row
+sample) prints one line with the contract's keys on rank 0 and nothing on
+the other ranks."""
 import os
 import sys
 
@@ -65,3 +68,38 @@ def test_unavailable_sampler_says_so():
     c = bench.ClockSampler(0)
     c.proc = None
     assert c.stop()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def _reference_arm(env_extra=None):
+    import json
+    import subprocess
+
+    env = dict(os.environ)
+    env.update(env_extra or {})
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--workload", "wf32768", "--steps", "2", "--warmup", "1",
+                        "--cpu-sample-s", "0.2"],
+                       capture_output=True, text=True, timeout=300, env=env, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_prints_one_contract_line():
+    (line,) = _reference_arm()
+    assert line["impl"] == "reference"
+    assert line["metric"] == bench.METRIC
+    assert line["unit"] == "s" and line["higher_is_better"] is False
+    assert line["steps"] == 2 and line["warmup"] == 1 and line["n_gpus"] == 1
+    assert line["value"] > 0 and abs(line["ms_per_step"] - 1e3 * line["value"]) < 1e-6 * 1e3 * line["value"]
+    assert line["config"]["workload"] == "wf-32768px-grf"
+    base = line["cpu_baseline"]
+    assert base["kind"] == "port" and base["cores"] >= 1 and base["value"] == line["value"]
+    assert "rows" in base["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["vs_baseline"] is None
+
+
+def test_reference_arm_other_ranks_do_no_work():
+    assert _reference_arm({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
