@@ -95,3 +95,15 @@ def test_synth_workloads_deterministic_and_shaped():
     z = p[:128, 2]
     np.testing.assert_allclose(np.diff(z), 2.0)
     assert abs(np.std(p[:, 4]) - np.sqrt(0.0625 + np.mean(p[:, 3] ** 2))) < 0.05
+
+
+def test_missing_library_raises_instead_of_falling_back(monkeypatch):
+    # No CPU fallback: without the built CUDA library every entry point raises.
+    from dachshund_gb300 import _lib as lib_mod
+
+    monkeypatch.setattr(lib_mod, "_lib", None)
+    monkeypatch.setattr(lib_mod, "LIB_PATH", os.path.join(ROOT, "no-such-dir", "libdsgb300.so"))
+    with pytest.raises(RuntimeError, match="not built"):
+        lib_mod.load(build_if_missing=False)
+    with pytest.raises(OSError):
+        lib_mod.load()  # builds the real library, then fails to open the missing path
