@@ -87,6 +87,11 @@ int ds_signal_covar(const ds_kernel_params* kp, int n, const double* perp2,
                     const double* para2, double* out);
 
 /* ---- context ------------------------------------------------------------ */
+/* No reference counterpart: the reference keeps no device state.  A context
+ * owns one device, one CUDA stream (every call of its objects is ordered on
+ * it, and their device buffers are allocated and freed stream-ordered on it)
+ * and the message of the last failed call.  Not thread-safe; sequential
+ * calls from one thread, as the reference's single caller thread makes them. */
 typedef struct ds_context ds_context;
 
 int ds_context_create(int device, ds_context** out);
@@ -134,8 +139,9 @@ int ds_operator_create(ds_context* ctx, int form, int n, const double* records,
                        const ds_kernel_params* kp, ds_operator** out);
 void ds_operator_destroy(ds_operator* op);
 
-/* Statistics of the tiling: tiles, interacting tile pairs, evaluated pairs
- * per matvec (tile pairs x tile^2), and the tile size. */
+/* Statistics of the tiling (no reference counterpart; the reference visits
+ * every pair): tiles, interacting tile pairs, evaluated pairs per matvec
+ * (tile pairs x tile^2), and the tile size. */
 typedef struct {
   int n;
   int n_pad;
@@ -431,7 +437,9 @@ int ds_operator_set_skewer_preconditioner(ds_operator* op, int n_skewers,
 /* ---- map projection ----------------------------------------------------- */
 typedef struct ds_map ds_map;
 
-/* A map grid or point set, sorted and tiled on the device once. */
+/* A map grid or point set (init_uniform_map_coords output or any Point
+ * array, lib/util.h:16, lib/map.h:41-44), sorted and tiled on the device once
+ * and reused by every product with it. */
 int ds_map_create(ds_context* ctx, int n_map, const double* map_points,
                   ds_map** out);
 void ds_map_destroy(ds_map* map);
@@ -442,7 +450,8 @@ int ds_map_product(ds_map* map, ds_operator* op, const double* x, double* m);
 int ds_map_product_dev(ds_map* map, ds_operator* op, const double* x,
                        double* m);
 
-/* smp_product of the mixed-precision form: FP32 evaluation of the exact
+/* smp_product (lib/map.cc:20-43) of the mixed-precision form (no reference
+ * counterpart for the FP32 evaluation): FP32 evaluation of the exact
  * kernel (MUFU ex2), FP32 sums per column tile, FP64 accumulation across
  * tiles; pairs beyond ``cutoff`` (exponent; <= 0: 30) are skipped.  Map
  * error against the FP64 product is about 1e-7 relative. */
@@ -451,7 +460,8 @@ int ds_map_product_f32(ds_map* map, ds_operator* op, double cutoff,
 int ds_map_product_f32_dev(ds_map* map, ds_operator* op, double cutoff,
                            const double* x, double* m);
 
-/* One-shot smp_product with the reference's argument list. */
+/* One-shot smp_product with the reference's argument list (lib/map.h:41-44):
+ * pixel and map points as Point arrays, x in pixel order; host arrays. */
 int ds_smp_product(ds_context* ctx, int n_pix, const double* pixel_points,
                    int n_map, const double* map_points,
                    const ds_kernel_params* kp, const double* x, double* m);
