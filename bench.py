@@ -14,8 +14,9 @@ once beside it, as the metric asks ("chosen form vs plain FP64 GPU PCG").
 N > 1 runs N independent replicas (the solve does not shard here); rank 0
 prints one JSON line.  ``--impl reference`` times the reference's algorithm
 on the host cores (the C/OpenMP restatement in oracle/, bit-exact with the
-reference; the reference itself cannot be built on the GPU host) on a bounded
-sample of rows, extrapolated to the full solve.
+reference; the reference's sources are not part of this repository, so the
+reference itself is not built where the benchmark runs) on a bounded sample
+of rows, extrapolated to the full solve.
 """
 from __future__ import annotations
 

@@ -5,11 +5,12 @@ and tests/wfx_tests.cc:49-151 (SN and W closed forms agree, table-A error,
 table against exact solve, table PCG against the closed form), with the
 reference's parameters and tolerances.  The reference runs the wfx tests on
 its 2,000-record fixture (100 skewers x 20 pixels, 1 Mpc/h apart in z,
-exponential-looking noise from 1e-4 to 1.5); that file does not travel, so
-a seeded stand-in of the same shape is drawn here, d from N(0, S + N) by a
-dense Cholesky factor.  The PCG assertion (rms of x_pcg / x_cf - 1 below
-0.01) is dominated by entries where x_cf is near zero and holds on some
-draws only; seed 1 passes it on the oracle with a 3x margin (0.0034)."""
+exponential-looking noise from 1e-4 to 1.5); that fixture is not part of
+this repository, so a seeded stand-in of the same shape is drawn here, d
+from N(0, S + N) by a dense Cholesky factor.  The PCG assertion (rms of
+x_pcg / x_cf - 1 below 0.01) is dominated by entries where x_cf is near zero
+and holds on some draws only; seed 1 passes it on the oracle with a 3x
+margin (0.0034)."""
 import numpy as np
 import pytest
 
