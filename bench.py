@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "WF solve time & CG iters to 1e-8 resid: chosen form vs plain FP64 GPU PCG"
 SMS = 152
-# Per-SM pipe rates measured on this machine's GB300 (profiles/pipe_rates_gb300.md):
+# Per-SM pipe rates measured on a GB300 (profiles/pipe_rates_gb300.md):
 # FP32 FMA 128 lanes/clk, MUFU ex2 32/clk, FP64 FMA 2/clk.
 FMA_LANES, MUFU_RATE, DFMA_RATE = 128.0, 32.0, 2.0
 # FP32 inner kernel (EXPANDED): 4 FMA lanes + 1 ex2 per pair; map kernel
@@ -241,7 +241,8 @@ def run_reference(args, rank, world):
 
 
 def measured_peaks():
-    """The machine's measured HBM copy bandwidth and cuBLAS bf16 rate, if present."""
+    """Measured HBM copy bandwidth and cuBLAS bf16 rate of this GPU model
+    (MEASURED_PEAKS.json beside this file), if present."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return json.load(f)
