@@ -107,3 +107,48 @@ def test_missing_library_raises_instead_of_falling_back(monkeypatch):
         lib_mod.load(build_if_missing=False)
     with pytest.raises(OSError):
         lib_mod.load()  # builds the real library, then fails to open the missing path
+
+
+def test_argument_checks_need_no_gpu():
+    # Calls the ABI rejects before any CUDA call return DS_ERR_ARG, also on a
+    # machine without a GPU: null handles, bad forms, sizes out of range.
+    from dachshund_gb300 import _lib as L
+
+    lib = L.load()
+    vp = ctypes.c_void_p
+    out = vp()
+    kp = api.SignalCovarParams(0.0625, 2.5, 2.0, eval="exact").as_c()
+    rec = np.zeros((8, 5))
+    vec = np.zeros(8)
+    p = rec.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    v = vec.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert lib.ds_operator_create(None, L.DS_FORM_W, 8, p, ctypes.byref(kp),
+                                  ctypes.byref(out)) == L.DS_ERR_ARG
+    assert lib.ds_A_product(None, v, v) == L.DS_ERR_ARG
+    assert lib.ds_A_residual(None, v, v) == L.DS_ERR_ARG
+    assert lib.ds_map_create(None, 8, p, ctypes.byref(out)) == L.DS_ERR_ARG
+    assert lib.ds_learned_create(None, ctypes.byref(kp), 128, 2, 0,
+                                 ctypes.byref(out)) == L.DS_ERR_ARG
+    sizes = (ctypes.c_int * 1)(8)
+    assert lib.ds_batch_create(None, L.DS_FORM_W, 1, sizes, p, ctypes.byref(kp), 4, 0.0,
+                               ctypes.byref(out)) == L.DS_ERR_ARG
+
+    # The allocation-free PCG checks its arguments and its size limit (32,768
+    # pixels, the fixed work space) before it touches the device.
+    pp = L.PcgParamsC(100, 50, 1e-8, 0)
+    res = L.PcgResultC()
+    rp = vp(rec.ctypes.data)
+    xp = vp(vec.ctypes.data)
+
+    def noalloc(form, n, records=rp, x=xp, params=pp):
+        return lib.ds_solve_pcg_noalloc(form, n, records, ctypes.byref(kp),
+                                        ctypes.byref(params) if params is not None else None,
+                                        x, ctypes.byref(res), None, None)
+
+    assert noalloc(L.DS_FORM_W, 32769) == L.DS_ERR_ARG
+    assert noalloc(L.DS_FORM_W, 0) == L.DS_ERR_ARG
+    assert noalloc(7, 8) == L.DS_ERR_ARG
+    assert noalloc(L.DS_FORM_W, 8, records=None) == L.DS_ERR_ARG
+    assert noalloc(L.DS_FORM_W, 8, x=None) == L.DS_ERR_ARG
+    assert noalloc(L.DS_FORM_W, 8, params=None) == L.DS_ERR_ARG
+    assert noalloc(L.DS_FORM_W, 8, params=L.PcgParamsC(100, 0, 1e-8, 0)) == L.DS_ERR_ARG
