@@ -4,9 +4,10 @@
  *
  * The path: the Gaussian signal covariance S (table or exact exp), the
  * operator A = S + N (SN form) or A = w S w + I (W form), Jacobi-PCG on
- * A x = b, and the map projection m = S_mp x.  Every function here replaces
- * one call of the reference library (caseywstark/dachshund, lib/*.h); each
- * declaration names the reference interface it stands in for.
+ * A x = b, and the map projection m = S_mp x.  Most functions here replace
+ * one call of the reference library (caseywstark/dachshund, the headers in
+ * lib/); each declaration names the reference interface it stands in for,
+ * or says that it has no counterpart there.
  *
  * Conventions
  *  - Host arrays are caller-owned; nothing here keeps a host pointer after
