@@ -159,3 +159,26 @@ def test_ref_known_answers_on_port():
     xcf = oracle.solve_cf("w", wrec, 0.05, 1.0, 1.0)
     xp, _, _, _ = oracle.solve_pcg("w", wrec, 0.05, 1.0, 1.0, 1000, 10, 1e-4)
     assert np.sqrt(np.mean((xp / xcf - 1.0) ** 2)) < 0.01
+
+
+@needs_ref
+def test_golden_fixtures_reproduce_from_their_script(tmp_path, monkeypatch):
+    """tests/golden/make_golden.py, run again on the reference, writes the
+    committed fixtures bit for bit."""
+    import importlib.util
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_golden",
+                                                  os.path.join(here, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    monkeypatch.setattr(mg, "HERE", str(tmp_path))
+    mg.make_edge()
+    mg.make_small()
+    mg.make_wf4096()
+    for name in ("edge", "small", "wf4096"):
+        old = np.load(os.path.join(here, name + ".npz"))
+        new = np.load(tmp_path / (name + ".npz"))
+        assert set(old.files) == set(new.files), name
+        for k in old.files:
+            np.testing.assert_array_equal(new[k], old[k], err_msg=f"{name}:{k}")
