@@ -5,7 +5,7 @@ reference (oracle/_ref, compiled from the reference's own sources by
 The reference commits no golden outputs of its own; these fixtures pin both
 the oracle restatement (CPU tests) and the CUDA path (GPU tests).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--out DIR]   (default: this folder)
 
 Outputs (all float64 unless noted):
   wf4096.npz   4,096-pixel workload: pixels, the reference app's map.bin,
@@ -30,6 +30,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
+OUT = HERE  # where the .npz files are written
 sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
@@ -55,7 +56,7 @@ def make_wf4096():
     x, ok, it2, hist = oracle.solve_pcg("w", wrec, VS, LP, LQ, w.pcg_max_iter, w.pcg_step_r,
                                         w.pcg_tol, impl="ref")
     assert ok and it2 == iters, (ok, it2, iters)
-    np.savez_compressed(os.path.join(HERE, "wf4096.npz"), pixels=w.pixels, map=m,
+    np.savez_compressed(os.path.join(OUT, "wf4096.npz"), pixels=w.pixels, map=m,
                         num_iters=iters, x=x, hist=hist,
                         params=np.array([w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz,
                                          w.pcg_tol, w.pcg_max_iter, w.pcg_step_r]))
@@ -91,7 +92,7 @@ def make_small():
     cov_pts = mp[::397][:6].copy()
     s, iters, succ = oracle.map_covar_diag(nrec, cov_pts, VS, LP, LQ, 1000, 50, 1e-6, impl="ref")
     out["cov_pts"], out["cov"], out["cov_iters"], out["cov_success"] = cov_pts, s, iters, succ
-    np.savez_compressed(os.path.join(HERE, "small.npz"), **out)
+    np.savez_compressed(os.path.join(OUT, "small.npz"), **out)
 
 
 def make_edge():
@@ -124,14 +125,18 @@ def make_edge():
     out["probe_perp2"], out["probe_para2"] = perp2, para2
     out["probe_S"] = oracle.signal_covar(perp2, para2, VS, LP, LQ, exact=False, impl="ref")
     out["probe_S_exact"] = oracle.signal_covar(perp2, para2, VS, LP, LQ, exact=True, impl="ref")
-    np.savez_compressed(os.path.join(HERE, "edge.npz"), **out)
+    np.savez_compressed(os.path.join(OUT, "edge.npz"), **out)
 
 
 if __name__ == "__main__":
+    if len(sys.argv) == 3 and sys.argv[1] == "--out":
+        OUT = sys.argv[2]
+    elif len(sys.argv) != 1:
+        sys.exit("usage: make_golden.py [--out DIR]")
     oracle.build(ref=True)
     if not oracle.ref_available():
         sys.exit("reference harness unavailable: build oracle/_ref first")
     make_edge()
     make_small()
     make_wf4096()
-    print("golden vectors written to", HERE)
+    print("golden vectors written to", OUT)

@@ -162,20 +162,17 @@ def test_ref_known_answers_on_port():
 
 
 @needs_ref
-def test_golden_fixtures_reproduce_from_their_script(tmp_path, monkeypatch):
+def test_golden_fixtures_reproduce_from_their_script(tmp_path):
     """tests/golden/make_golden.py, run again on the reference, writes the
-    committed fixtures bit for bit."""
-    import importlib.util
+    committed fixtures bit for bit (in a child process: the reference's
+    MapCovarDiag prints progress lines from C)."""
+    import subprocess
+    import sys
 
     here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-    spec = importlib.util.spec_from_file_location("make_golden",
-                                                  os.path.join(here, "make_golden.py"))
-    mg = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mg)
-    monkeypatch.setattr(mg, "HERE", str(tmp_path))
-    mg.make_edge()
-    mg.make_small()
-    mg.make_wf4096()
+    r = subprocess.run([sys.executable, os.path.join(here, "make_golden.py"), "--out",
+                        str(tmp_path)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
     for name in ("edge", "small", "wf4096"):
         old = np.load(os.path.join(here, name + ".npz"))
         new = np.load(tmp_path / (name + ".npz"))
