@@ -43,6 +43,11 @@ PAIRS_PER_CLK = {"expanded": min(FMA_LANES / 4, MUFU_RATE), "direct": min(FMA_LA
 # DRAM traffic of one k_pair_f32 launch on the 262,144-pixel workload, measured
 # once with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
 K_PAIR_F32_DRAM_BYTES = 9_174_528
+# FP64-pipe instructions per evaluated pair of the plain FP64 kernel
+# k_pair_f64<EXACT, PRODUCT> on the 262,144-pixel workload, from one ncu
+# capture (FP64-pipe busy fraction x 2 per clock x active SM cycles / the
+# launch's evaluated pairs; profiles/k_pair_f64_exact_wf262144.md)
+K_PAIR_F64_EXACT_OPS = 17.4
 # Plain FP64 iteration count of the workload (tol 1e-8, exact kernel), for the
 # CPU-baseline extrapolation of the reference arm.
 REF_ITERS = {"wf-262144px-grf": 162, "wf-32768px-grf": 150}
@@ -60,6 +65,8 @@ def parse():
                     help="skip the batched-chunks (512 chunks x 64 RHS) measurement")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner measurement")
+    ap.add_argument("--no-wf32768", action="store_true",
+                    help="skip the 32,768-pixel dense / matrix-free measurement")
     ap.add_argument("--cpu-sample-s", type=float, default=6.0,
                     help="seconds of CPU work per baseline sample")
     return ap.parse_args()
@@ -188,6 +195,9 @@ def cpu_baseline(w, iters, target_s):
                    f"cheaper per pair than exp), OpenMP on {cores} host threads; "
                    f"extrapolated to {matvecs} matvecs + the {w.n_map}-point map"),
         "ns_per_pair": t_op * 1e9,
+        "rows_A_product": r_op, "rows_smp_product": r_map,
+        "sample_s": d_op + d_map,
+        "extrapolated_to": f"{matvecs} A_product calls of {w.n} rows + smp_product of {w.n_map} rows",
     }
 
 
@@ -214,6 +224,13 @@ def dist_max(v: float) -> float:
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's own algorithm for this path (its
+    table-kernel A_product and smp_product, lib/wf_vector.cc:196-220 and
+    lib/map.cc:20-43, via the bit-exact C/OpenMP restatement in oracle/) on
+    all host cores.  A full solve of the workload takes tens of minutes on
+    the host, so each step times a bounded sample of rows and extrapolates;
+    the config says what was sampled and that the kernel is the table one
+    (the GPU arm evaluates exp)."""
     if rank != 0:
         return
     w = workload(args.workload)
@@ -231,9 +248,15 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w.name, "n_pixels": w.n, "n_map": w.n_map, "kernel": "exact",
+        "config": {"workload": w.name, "n_pixels": w.n, "n_map": w.n_map,
+                   "kernel": "table (the reference's A_product / smp_product kernel; "
+                             "the GPU arm evaluates exp)",
                    "form": "W", "tol": w.pcg_tol, "iters": iters,
-                   "sample": "bounded row sample, extrapolated"},
+                   "sample": "bounded row sample per step, extrapolated to the full solve",
+                   "sampled_rows": {"A_product": base["rows_A_product"],
+                                    "smp_product": base["rows_smp_product"]},
+                   "sampled_seconds": base["sample_s"],
+                   "extrapolated_to": base["extrapolated_to"]},
         "cpu_baseline": base,
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -336,6 +359,103 @@ def run_batched(ctx, n_chunks=512, n_rhs=64, seed=0, plain_samples=6):
         "speedup_vs_plain": plain_est / res.seconds,
         "x_err_vs_plain_fp64_max": max(errs),
     }
+
+
+def run_wf32768(ctx, hbm_gbs):
+    """The 32,768-pixel workload (256 skewers x 128 pixels in [0,40)^2 x
+    [0,256) Mpc/h, GRF data, exact kernel, W form, tol 1e-8, map 40 x 40 x
+    256), solved three ways from x = 0: the plain FP64 PCG with the dense
+    operator in HBM (32,768^2 FP64 = 8.6 GB, float-pair matvec), the plain
+    FP64 PCG with the matrix-free FP64 kernel, and the chosen mixed-precision
+    form (+ FP32 map).  Device times from CUDA events; the dense matvec's
+    achieved HBM bandwidth = 8 n_pad^2 bytes per product / its event time,
+    against the measured copy bandwidth."""
+    import numpy as np
+    import torch
+
+    from dachshund_gb300 import (MapGrid, MixedParams, PCGParams, SignalCovarParams,
+                                 WFVectorW, pixel_to_wpixel, synth)
+
+    w = synth.wf32768(0)
+    rec = pixel_to_wpixel(w.pixels)
+    sp = SignalCovarParams(w.var_s, w.l_perp, w.l_para, eval="exact")
+    pts = synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz)
+    mf = WFVectorW(ctx, rec, sp)
+    dn = WFVectorW(ctx, rec, sp)
+    grid = MapGrid(ctx, pts)
+    pp = PCGParams(3000, w.pcg_step_r, w.pcg_tol)
+    n_pad = mf.info()["n_pad"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dn.set_dense(True)
+    build_s = time.perf_counter() - t0
+    out = {"workload": f"{w.name}: 256 skewers x 128 px, [0,40)^2 x [0,256) Mpc/h, exact kernel",
+           "n_pixels": w.n, "n_pad": n_pad, "dense_bytes": 8 * n_pad * n_pad,
+           "dense_build_s": build_s, "dense_arith": dn.dense_arith()}
+    xd = torch.zeros(w.n, dtype=torch.float64, device="cuda")
+    dn.solve_pcg_dev(pp, xd)  # warm-up
+    for arith in ("float_pair", "fp64"):
+        dn.set_dense_arith(arith)
+        xd.zero_()
+        ctx.set_profiling(True)
+        rd = dn.solve_pcg_dev(pp, xd)
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        mv_s = prof["dense_ms"] * 1e-3 / max(prof["dense_launches"], 1)
+        gbs = 8.0 * n_pad * n_pad / mv_s / 1e9
+        out[f"dense_{arith}"] = {
+            "solve_s": rd.seconds, "iters": rd.num_iters, "success": rd.success,
+            "matvecs": prof["dense_launches"], "matvec_ms": mv_s * 1e3,
+            "matvec_GBps": gbs, "frac_of_measured_hbm": gbs / hbm_gbs if hbm_gbs else None}
+    dn.set_dense_arith("auto")
+    xd.zero_()
+    rd = dn.solve_pcg_dev(pp, xd)
+    xm = torch.zeros_like(xd)
+    rm = mf.solve_pcg_dev(pp, xm)
+    mref = torch.empty(w.n_map, dtype=torch.float64, device="cuda")
+    grid.product_dev(mf, xm, mref)
+    mp = MixedParams(max_iter=3000, tol=w.pcg_tol)
+    xc = torch.zeros_like(xd)
+    mf.solve_mixed_dev(mp, xc)  # warm-up
+    mc = torch.empty_like(mref)
+    times = []
+    for _ in range(3):
+        xc.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        e0.record(stream)
+        rc = mf.solve_mixed_dev(mp, xc)
+        grid.product_f32_dev(mf, xc, mc)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    # FP64 residuals of the dense and mixed solutions with the matrix-free operator
+    wv = torch.tensor(rec[:, 3], device="cuda")
+    nb = float(np.linalg.norm(rec[:, 4]))
+    r = torch.empty_like(xd)
+
+    def rel_resid(x):
+        mf.A_residual_dev(x / wv, r)
+        return float(torch.linalg.norm(r).item()) / nb
+
+    xmax = float(torch.max(torch.abs(xm)).item())
+    out.update({
+        "dense_solve_s": rd.seconds, "dense_iters": rd.num_iters,
+        "dense_rel_residual_fp64": rel_resid(xd),
+        "matrix_free_fp64_solve_s": rm.seconds, "matrix_free_fp64_iters": rm.num_iters,
+        "mixed_solve_plus_map_s": statistics.mean(times), "mixed_iters": rc.num_iters,
+        "mixed_fp64_updates": rc.n_outer, "mixed_rel_residual_fp64": rel_resid(xc),
+        "x_dense_vs_matrix_free": float(torch.max(torch.abs(xd - xm)).item()) / xmax,
+        "x_mixed_vs_matrix_free": float(torch.max(torch.abs(xc - xm)).item()) / xmax,
+        "map_err_mixed_vs_fp64": float(torch.max(torch.abs(mc - mref)).item())
+        / float(torch.max(torch.abs(mref)).item()),
+        "speedup_dense_vs_matrix_free": rm.seconds / rd.seconds,
+    })
+    grid.close()
+    dn.close()
+    mf.close()
+    return out
 
 
 def run_learned(ctx, seeds=(10001, 10002, 10003, 10004, 10005)):
@@ -467,7 +587,8 @@ def run_ours(args, rank, world, local):
             "launches_per_step": f32_n / args.steps, "ms_per_step": f32_ms / args.steps,
             "Gpair_per_s": f32_pairs / (f32_ms * 1e-3) / 1e9 if f32_ms else None,
             "peak_Gpair_per_s": PAIRS_PER_CLK["expanded"] * SMS * sm_hz / 1e9},
-        "fp64_residual": {
+        "ff_residual": {
+            "kernel": "k_pair_ff_resid (FP64-accurate outer residual in float-float)",
             "launches_per_step": f64_n / args.steps, "ms_per_step": f64_ms / args.steps,
             "Gpair_per_s": f64_pairs / (f64_ms * 1e-3) / 1e9 if f64_ms else None},
         "fp32_map": {
@@ -499,9 +620,23 @@ def run_ours(args, rank, world, local):
         xp = torch.zeros_like(x)
         mpl = torch.empty_like(m)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        ctx.set_profiling(True)
         rp = op.solve_pcg_dev(PCGParams(3000, w.pcg_step_r, w.pcg_tol), xp)
-        t_solve = time.perf_counter() - t0
+        pprof = ctx.profile()
+        ctx.set_profiling(False)
+        p_gps = pprof["f64_evaluated"] / (pprof["f64_ms"] * 1e-3) if pprof["f64_ms"] else None
+        p_peak = DFMA_RATE / K_PAIR_F64_EXACT_OPS * SMS * sm_hz
+        kernels["fp64_plain_matvec"] = {
+            "kernel": "k_pair_f64<EXACT> (plain FP64 PCG products and residuals)",
+            "launches_per_solve": pprof["f64_launches"],
+            "ms_per_launch": pprof["f64_ms"] / max(pprof["f64_launches"], 1),
+            "Gpair_per_s": p_gps / 1e9 if p_gps else None,
+            "fp64_ops_per_pair": K_PAIR_F64_EXACT_OPS,
+            "peak_Gpair_per_s": p_peak / 1e9,
+            "frac": p_gps / p_peak if p_gps else None,
+            "peak_basis": (f"FP64 pipe: {DFMA_RATE:.0f} FP64 instructions/clk/SM x {SMS} SMs "
+                           f"x median SM clock / {K_PAIR_F64_EXACT_OPS} FP64 instructions per "
+                           "evaluated pair (ncu capture)")}
         t0 = time.perf_counter()
         grid.product_dev(op, xp, mpl)
         ctx.synchronize()
@@ -511,7 +646,6 @@ def run_ours(args, rank, world, local):
                  "iters": rp.num_iters, "success": rp.success}
         map_err = float(np.max(np.abs(m_chosen - mref)) / np.max(np.abs(mref)))
         x_err = float(torch.max(torch.abs(x - xp)).item() / torch.max(torch.abs(xp)).item())
-        del t_solve
 
     # End to end through the public API with host buffers: the records and the
     # map points sit in pinned (page-locked) host memory, numpy views of
@@ -540,6 +674,7 @@ def run_ours(args, rank, world, local):
         if rank == 0 else None
     batched = None if args.no_batched else run_batched(ctx)
     learned = None if args.no_learned else run_learned(ctx)
+    wf32768 = None if args.no_wf32768 else run_wf32768(ctx, measured_peaks().get("hbm_gbs"))
     if batched and batched["matvec_algorithmic_tflops"] and batched["variant"].startswith("tensor"):
         peak = measured_peaks().get("bf16_tflops")
         if peak:
@@ -575,6 +710,7 @@ def run_ours(args, rank, world, local):
             "clocks": clk,
             "batched_chunks": batched,
             "learned_preconditioner": learned,
+            "wf32768_dense_and_matrix_free": wf32768,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

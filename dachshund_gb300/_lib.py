@@ -120,6 +120,9 @@ class ProfileC(C.Structure):
         ("map_launches", C.c_longlong),
         ("map_ms", C.c_double),
         ("map_evaluated", C.c_double),
+        ("dense_launches", C.c_longlong),
+        ("dense_ms", C.c_double),
+        ("dense_entries", C.c_double),
     ]
 
 
@@ -153,6 +156,8 @@ SIGNATURES = {
     "ds_norm_b": (_i, [_vp, _dp]),
     "ds_A_entries": (_i, [_vp, _i, _i, _ip, _ip, _dp]),
     "ds_operator_set_dense": (_i, [_vp, _i]),
+    "ds_operator_set_dense_arith": (_i, [_vp, _i]),
+    "ds_operator_get_dense_arith": (_i, [_vp, C.POINTER(C.c_int)]),
     "ds_operator_set_inner_matvec": (_i, [_vp, _i]),
     "ds_solve_cf": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), _dp]),
     "ds_map_covar_diag": (_i, [_vp, _i, _dp, _i, _dp, C.POINTER(KernelParamsC),

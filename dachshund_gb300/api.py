@@ -227,6 +227,24 @@ class _WFVector:
         self.ctx.check(self._lib.ds_operator_set_dense(self.handle, int(bool(enable))),
                        "ds_operator_set_dense")
 
+    _DENSE_ARITH = {"auto": 0, "float_pair": 1, "fp64": 2}
+
+    def set_dense_arith(self, arith: str = "auto"):
+        """Arithmetic of the dense matvec: "float_pair" (FP64 entries split
+        into float pairs, float-float sums on the FP32 pipe; the HBM-rate
+        one), "fp64" (FP64 FMAs) or "auto" (float pairs when the entries'
+        range allows)."""
+        self.ctx.check(self._lib.ds_operator_set_dense_arith(self.handle,
+                                                             self._DENSE_ARITH[arith]),
+                       "ds_operator_set_dense_arith")
+
+    def dense_arith(self) -> str:
+        """The dense matvec's arithmetic in use ("float_pair" or "fp64")."""
+        v = C.c_int()
+        self.ctx.check(self._lib.ds_operator_get_dense_arith(self.handle, C.byref(v)),
+                       "ds_operator_get_dense_arith")
+        return {1: "float_pair", 2: "fp64"}[v.value]
+
     def set_inner_matvec(self, variant: str = "auto"):
         """Inner matvec of solve_mixed: "auto" / "cuda_core" (the CUDA-core
         kernel, the faster one) or "tensor" (pair exponents on the tensor

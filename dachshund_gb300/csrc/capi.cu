@@ -233,6 +233,7 @@ int ds_context_create(int device, ds_context** out) {
     cudaDeviceProp prop;
     DS_CUDA(cudaGetDeviceProperties(&prop, device));
     if (prop.major < 10) throw Error{DS_ERR_NO_DEVICE, "device is not a Blackwell-class GPU"};
+    ctx->num_sms = prop.multiProcessorCount;
     DS_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     // stream-ordered device buffers come from the default pool; keep what is
     // freed cached for the next allocations
@@ -272,11 +273,14 @@ int ds_context_set_profiling(ds_context* ctx, int enable) {
     Profiler& p = ctx->prof;
     p.collect();
     if (enable) {
-      if (!p.d_pairs) DS_CUDA(cudaMalloc(&p.d_pairs, 3 * sizeof(unsigned long long)));
-      DS_CUDA(cudaMemsetAsync(p.d_pairs, 0, 3 * sizeof(unsigned long long), ctx->stream));
+      const size_t bytes = Profiler::KINDS * sizeof(unsigned long long);
+      if (!p.d_pairs) DS_CUDA(cudaMalloc(&p.d_pairs, bytes));
+      DS_CUDA(cudaMemsetAsync(p.d_pairs, 0, bytes, ctx->stream));
       DS_CUDA(cudaStreamSynchronize(ctx->stream));
-      p.launches[0] = p.launches[1] = p.launches[2] = 0;
-      p.ms[0] = p.ms[1] = p.ms[2] = 0.0;
+      for (int k = 0; k < Profiler::KINDS; ++k) {
+        p.launches[k] = 0;
+        p.ms[k] = 0.0;
+      }
     }
     p.enabled = enable != 0;
   });
@@ -287,7 +291,7 @@ int ds_context_get_profile(ds_context* ctx, ds_profile* out) {
   return guarded(ctx, [&] {
     Profiler& p = ctx->prof;
     p.collect();
-    unsigned long long pairs[3] = {0, 0, 0};
+    unsigned long long pairs[Profiler::KINDS] = {0, 0, 0, 0};
     if (p.d_pairs) {
       DS_CUDA(cudaStreamSynchronize(ctx->stream));
       DS_CUDA(cudaMemcpy(pairs, p.d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost));
@@ -301,6 +305,9 @@ int ds_context_get_profile(ds_context* ctx, ds_profile* out) {
     out->map_launches = p.launches[2];
     out->map_ms = p.ms[2];
     out->map_evaluated = (double)pairs[2];
+    out->dense_launches = p.launches[3];
+    out->dense_ms = p.ms[3];
+    out->dense_entries = (double)pairs[3];
     out->pair_launches = p.launches[0] + p.launches[1] + p.launches[2];
     out->pair_ms = p.ms[0] + p.ms[1] + p.ms[2];
     out->pair_evaluated = (double)pairs[0] + (double)pairs[1] + (double)pairs[2];
@@ -716,8 +723,24 @@ int ds_operator_set_dense(ds_operator* op, int enable) {
       op->use_dense = true;
     } else {
       op->use_dense = false;
-      op->dense.release();
+      op_free_dense(op);
     }
+  });
+}
+
+int ds_operator_set_dense_arith(ds_operator* op, int arith) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    require(arith >= DS_DENSE_AUTO && arith <= DS_DENSE_FP64, "bad dense arithmetic");
+    op->dense_arith = arith;
+  });
+}
+
+int ds_operator_get_dense_arith(ds_operator* op, int* arith) {
+  if (!op || !arith) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    require(op->dense.p != nullptr, "the dense operator is not built (ds_operator_set_dense)");
+    *arith = dense_arith_in_use(op);
   });
 }
 

@@ -246,7 +246,8 @@ struct PairArgs {
 
 // Per-context event timing of pair-kernel launches (ds_context_set_profiling).
 // Kinds: 0 = FP64-accurate pair kernels (products, residuals), 1 = FP32 pair
-// kernels (products), 2 = map products (FP64 or FP32).
+// kernels (products), 2 = map products (FP64 or FP32), 3 = dense matvecs
+// (their "pairs" are matrix entries read).
 struct Profiler {
   struct Pending {
     cudaEvent_t start, stop;
@@ -255,8 +256,9 @@ struct Profiler {
   bool enabled = false;
   std::vector<cudaEvent_t> free_events;
   std::vector<Pending> pending;
-  long long launches[3] = {0, 0, 0};
-  double ms[3] = {0.0, 0.0, 0.0};
+  static constexpr int KINDS = 4;
+  long long launches[KINDS] = {0, 0, 0, 0};
+  double ms[KINDS] = {0.0, 0.0, 0.0, 0.0};
   unsigned long long* d_pairs = nullptr;  // device counters of evaluated pairs, per kind
   cudaEvent_t get_event();
   void begin(cudaStream_t st, cudaEvent_t* ev);
@@ -290,6 +292,7 @@ struct PcgState {
 // Opaque handles of the C ABI.
 struct ds_context {
   int device = 0;
+  int num_sms = 0;  // streaming multiprocessors of the device (persistent grids)
   cudaStream_t stream = nullptr;
   std::string last_error;
   ds::Profiler prof;
@@ -320,6 +323,16 @@ struct ds_operator {
   std::unique_ptr<ds::OpF32, ds::OpF32Deleter> f32;  // mixed-precision data (lazy)
   ds::DevBuf<double> dense;  // dense A (n_pad x n_pad, sorted order) when enabled
   bool use_dense = false;
+  // dense matvec: arithmetic (ds_dense_arith; float pairs need every nonzero
+  // |A_ij| in [2^-100, 2^100], recorded at build time with the sign), the
+  // float-pair copy of the vector, per-column-block row partials, per-row-block
+  // dot partials and arrival counters (n_pad / 64 + 1, zero between launches)
+  int dense_arith = 0;
+  bool dense_ff_ok = false;
+  bool dense_signed = false;
+  ds::DevBuf<float2> dense_vff;
+  ds::DevBuf<double> dense_part, dense_dot;
+  ds::DevBuf<unsigned int> dense_cnt;
   int inner_variant = 0;     // inner matvec of the mixed form (InnerVariant)
   // skewer-band preconditioner of the mixed form (null: Jacobi)
   std::unique_ptr<ds::SkewerPC, ds::SkewerPCDeleter> pc;

@@ -44,10 +44,12 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
 
 // Dense paths (dense.cu).
 void op_build_dense(ds_operator* op);
+void op_free_dense(ds_operator* op);
+int dense_arith_in_use(const ds_operator* op);  // DS_DENSE_FLOAT_PAIR or DS_DENSE_FP64
+// q = A v, with alpha = delta / (dotv . q) into *pcg when dotv is given, or
+// r = b - A v (residual); returns at once when *skip != 0.
 void dense_apply(ds_operator* op, bool residual, const double* v, double* out,
-                 const double* dotv, double* part, PcgState* pcg, unsigned int* counter,
-                 const int* skip, cudaStream_t st);
-int dense_partials(int n_pad);
+                 const double* dotv, PcgState* pcg, const int* skip, cudaStream_t st);
 void solve_cf_dev(ds_context* ctx, int form, int n, const double* d_rec, const KernelConsts& kc,
                   const double* d_table, double* d_x);
 void map_covar_diag_run(ds_operator* op, int n_map, const double* map_pts,

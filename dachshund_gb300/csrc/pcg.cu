@@ -175,7 +175,7 @@ PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
 
 void op_apply_sorted(ds_operator* op, int epi, const double* v, double* out, cudaStream_t st) {
   if (op->use_dense) {
-    dense_apply(op, epi == EPI_RESIDUAL, v, out, nullptr, nullptr, nullptr, nullptr, nullptr, st);
+    dense_apply(op, epi == EPI_RESIDUAL, v, out, nullptr, nullptr, nullptr, st);
     return;
   }
   PairArgs a = op_pair_args(op, v, out);
@@ -192,8 +192,7 @@ void ensure_pcg_workspace(ds_operator* op) {
   op->partial.alloc(std::max<size_t>(2 * VGRID_MAX, op->pix.n_tiles));
   // + 2 n_pad: the per-skewer (r.z, |r|^2) partials of the preconditioned
   // mixed form, after the n_tiles p.q partials
-  op->partial2.alloc(std::max(std::max((size_t)2 * VGRID_MAX, (size_t)op->pix.n_tiles),
-                              (size_t)dense_partials(op->pix.n_pad)) +
+  op->partial2.alloc(std::max((size_t)2 * VGRID_MAX, (size_t)op->pix.n_tiles) +
                      2 * (size_t)op->pix.n_pad);
   op->state.alloc(1);
   op->h_flag.alloc(64);
@@ -243,8 +242,7 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
   int issued = 0, waited = 0;
   for (int it = 1; it < pp.max_iter; ++it) {
     if (op->use_dense)  // q = A d, alpha
-      dense_apply(op, false, op->d.p, op->q.p, op->d.p, op->partial2.p, S, &S->counter[0],
-                  &S->done, st);
+      dense_apply(op, false, op->d.p, op->q.p, op->d.p, S, &S->done, st);
     else
       launch_pair_f64(op->kc, EPI_PRODUCT, prod, st);
     if (it % pp.step_r == 0) {
@@ -252,7 +250,7 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
                                         op->pdiag.p, op->partial.p, op->hist.p, op->dhist.p);
       DS_CHECK_LAUNCH();
       if (op->use_dense)  // r = b - A x
-        dense_apply(op, true, op->x.p, op->r.p, nullptr, nullptr, nullptr, nullptr, &S->done, st);
+        dense_apply(op, true, op->x.p, op->r.p, nullptr, nullptr, &S->done, st);
       else
         launch_pair_f64(op->kc, EPI_RESIDUAL, resid, st);
       k_pcg_update<2><<<g, VB, 0, st>>>(np, S, op->x.p, op->r.p, op->d.p, op->q.p, op->s.p,

@@ -1,6 +1,7 @@
 """One invocation of a single hot kernel on a workload of the benchmark's
-shapes, for kernel profilers (``ncu -k <kernel> -c 1 python -m
-dachshund_gb300.profile_cases <case>``):
+shapes, for kernel profilers (``ncu --clock-control none -k <kernel> -c 1
+python -m dachshund_gb300.profile_cases <case>``; ``--clock-control none``
+leaves the GPU's clocks as they are):
 
   ff_residual    b - A x of the 262,144-pixel operator in float-float
                  arithmetic (k_pair_ff_resid), random x
@@ -13,9 +14,12 @@ dachshund_gb300.profile_cases <case>``):
   learned_solve  one held-out 262,144-pixel system: Jacobi mixed solve, the
                  network's forward pass and the learned-preconditioned solve
                  (trained weights in dachshund_gb300/weights)
-  pipe_rates     per-SM throughput of FP64 FMA, FP32 FMA, MUFU ex2, FP64
-                 exp() and FP64 -> int32 (probes/pipe_rates.cu, compiled here
-                 for sm_103a; the rates behind the pair kernels' rooflines)
+  plain_matvec   one FP64 product A a of the 262,144-pixel operator, exact
+                 kernel (k_pair_f64<EXACT, PRODUCT>), random a
+  dense_matvec   the dense operator of a 16,384-pixel system of the
+                 32,768-pixel workload's density (128 skewers x 128 pixels
+                 in [0,28.3)^2 x [0,256) Mpc/h, 16,384^2 FP64 = 2.1 GB):
+                 built, then three products (k_split_vec + k_dense_mv each)
 """
 from __future__ import annotations
 
@@ -24,27 +28,9 @@ import sys
 import numpy as np
 
 
-def pipe_rates() -> None:
-    """Compile probes/pipe_rates.cu for sm_103a and run it."""
-    import importlib
-    import os
-    import subprocess
-
-    build = importlib.import_module("dachshund_gb300.build")  # the module, not build()
-    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "probes", "pipe_rates.cu")
-    os.makedirs(build.BUILD, exist_ok=True)
-    exe = os.path.join(build.BUILD, "pipe_rates")
-    subprocess.run([build.nvcc()] + build.ARCH + ["-O3", "-std=c++17", src, "-o", exe],
-                   check=True)
-    subprocess.run([exe], check=True)
-
-
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     case = argv[0] if argv else "ff_residual"
-    if case == "pipe_rates":
-        pipe_rates()
-        return
     import torch
 
     from dachshund_gb300 import (BatchSolver, Context, MixedParams, SignalCovarParams,
@@ -52,11 +38,14 @@ def main(argv=None):
 
     ctx = Context(0)
     sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
-    if case in ("ff_residual", "f32_matvec", "tc_inner"):
+    if case in ("ff_residual", "f32_matvec", "tc_inner", "plain_matvec"):
         w = synth.wf262144(0)
         rec = pixel_to_wpixel(w.pixels)
         op = WFVectorW(ctx, rec, sp)
-        if case == "ff_residual":
+        if case == "plain_matvec":
+            b = op.A_product(np.random.default_rng(1).standard_normal(w.n))
+            print("plain_matvec |b|", float(np.linalg.norm(b)))
+        elif case == "ff_residual":
             x = np.random.default_rng(1).standard_normal(w.n)
             r = op.A_residual_ff(x)
             print("ff_residual |r|", float(np.linalg.norm(r)))
@@ -65,6 +54,15 @@ def main(argv=None):
                 op.set_inner_matvec("tensor")
             x, res = op.solve_mixed(MixedParams(tol=1e-8))
             print(case, "iters", res.num_iters)
+    elif case == "dense_matvec":
+        w = synth.grf_workload("wf-16384px-grf", 128, 128, 40.0 / np.sqrt(2.0), 0,
+                               (28, 28, 256), 1e-8)
+        op = WFVectorW(ctx, pixel_to_wpixel(w.pixels), sp)
+        op.set_dense(True)
+        a = np.random.default_rng(1).standard_normal(w.n)
+        for _ in range(3):
+            b = op.A_product(a)
+        print("dense_matvec", op.dense_arith(), "|b|", float(np.linalg.norm(b)))
     elif case == "tc_matvec":
         pixes, rhs = synth.chunks(64, 0, n_rhs=64)
         recs = [pixel_to_wpixel(p) for p in pixes]

@@ -168,7 +168,9 @@ def grf_data(rng, pix, box, cell=1.0, var_s=VAR_S, l_perp=L_PERP, l_para=L_PARA)
     return trilinear(field, pix[:, :3], cell) + pix[:, 3] * rng.standard_normal(pix.shape[0])
 
 
-def _grf_workload(name, n_sk, n_per, box_xy, seed, map_shape, tol):
+def grf_workload(name, n_sk, n_per, box_xy, seed, map_shape, tol):
+    """n_sk skewers of n_per pixels at uniform (x, y) in [0, box_xy)^2 with
+    GRF + noise data; map grid ``map_shape`` over the box."""
     rng = np.random.default_rng(seed)
     pix = skewer_pixels(rng, n_sk, n_per, box_xy)
     lz = n_per * DZ
@@ -190,19 +192,19 @@ def wf4096(seed: int = 0) -> Workload:
 def wf32768(seed: int = 0) -> Workload:
     """32,768 pixels: 256 skewers x 128 in [0,40)^2 x [0,256); GRF d; tol 1e-8;
     map 40 x 40 x 256."""
-    return _grf_workload("wf-32768px-grf", 256, 128, 40.0, seed, (40, 40, 256), 1e-8)
+    return grf_workload("wf-32768px-grf", 256, 128, 40.0, seed, (40, 40, 256), 1e-8)
 
 
 def wf262144(seed: int = 0) -> Workload:
     """262,144 pixels: 1,024 skewers x 256 in [0,80)^2 x [0,512); GRF d;
     tol 1e-8; map 80 x 80 x 512."""
-    return _grf_workload("wf-262144px-grf", 1024, 256, 80.0, seed, (80, 80, 512), 1e-8)
+    return grf_workload("wf-262144px-grf", 1024, 256, 80.0, seed, (80, 80, 512), 1e-8)
 
 
 def small(n_sk=16, n_per=32, box_xy=12.0, seed=0, tol=1e-8) -> Workload:
     """A scaled-down GRF workload for parity tests."""
     lz = n_per * DZ
-    return _grf_workload(f"wf-{n_sk * n_per}px-small", n_sk, n_per, box_xy, seed,
+    return grf_workload(f"wf-{n_sk * n_per}px-small", n_sk, n_per, box_xy, seed,
                          (max(1, int(box_xy)), max(1, int(box_xy)), int(lz)), tol)
 
 

@@ -126,6 +126,9 @@ typedef struct {
   long long map_launches;    /* map products (FP64 or FP32) */
   double map_ms;
   double map_evaluated;
+  long long dense_launches;  /* dense-operator matvecs (ds_operator_set_dense) */
+  double dense_ms;
+  double dense_entries;      /* matrix entries read (n_pad^2 per matvec) */
 } ds_profile;
 int ds_context_set_profiling(ds_context* ctx, int enable);
 int ds_context_get_profile(ds_context* ctx, ds_profile* out);
@@ -177,11 +180,27 @@ int ds_A_entries(ds_operator* op, int eval, int m, const int* ii,
                  const int* jj, double* out);
 
 /* Dense S_pp in HBM (no reference counterpart; the reference builds the
- * dense matrix only inside solve_cf, lib/wf_vector.cc:127-133).  enable = 1
- * builds the n x n FP64 operator in device memory (8 n^2 bytes; DS_ERR_OOM
- * when it does not fit) and makes A_product, A_residual and solve_pcg use the
- * dense matvec; enable = 0 frees it and returns to the matrix-free kernels. */
+ * dense matrix only inside solve_cf, lib/wf_vector.cc:127-133, and its
+ * A_product, lib/wf_vector.cc:51-74 and 196-220, visits every pair).
+ * enable = 1 builds the n_pad x n_pad FP64 operator in device memory
+ * (8 n_pad^2 bytes, n_pad = n rounded up to 128; DS_ERR_OOM when it does not
+ * fit) and makes A_product, A_residual and solve_pcg use the dense matvec;
+ * enable = 0 frees it and returns to the matrix-free kernels. */
 int ds_operator_set_dense(ds_operator* op, int enable);
+
+/* Arithmetic of the dense matvec (no reference counterpart).  The matrix is
+ * FP64 in either case.  DS_DENSE_FLOAT_PAIR splits each entry into two
+ * floats (47 significant bits, 2^-46 relative) and accumulates in
+ * float-float on the FP32 pipe, which keeps the product at the HBM rate;
+ * DS_DENSE_FP64 uses FP64 FMAs (GB300 issues 2 per clock per SM, which caps
+ * the product below the HBM rate).  DS_DENSE_AUTO (default) takes float
+ * pairs when every nonzero |A_ij| lies in [2^-100, 2^100] (checked when the
+ * matrix is built), else FP64; products agree to about 1e-14 relative.
+ * ds_operator_get_dense_arith reports the one in use (dense operator
+ * built). */
+enum { DS_DENSE_AUTO = 0, DS_DENSE_FLOAT_PAIR = 1, DS_DENSE_FP64 = 2 };
+int ds_operator_set_dense_arith(ds_operator* op, int arith);
+int ds_operator_get_dense_arith(ds_operator* op, int* arith);
 
 /* Inner matvec of the mixed-precision form (no reference counterpart; the
  * reference has no FP32 path).  DS_INNER_AUTO and DS_INNER_CUDA_CORE use the

@@ -85,3 +85,36 @@ def test_map_covar_diag_exact_batched(ctx):
     assert ok.all() and oko.all()
     assert rel(s, so) < 1e-6
     assert np.all(np.abs(iters - io) <= 0.25 * io + 5)
+
+
+def test_dense_signed_entries(ctx):
+    """W-form records with some negative weights give negative entries: the
+    float-pair matvec carries the signs (matrix-free FP64 as the yardstick)."""
+    w = synth.small(12, 40, 10.0, seed=29)
+    rec = pixel_to_wpixel(w.pixels)
+    rec[::3, 3] *= -1.0
+    rec[::3, 4] *= -1.0
+    sp = SignalCovarParams(VS, LP, LQ, eval="exact")
+    mf, dn = WFVectorW(ctx, rec, sp), WFVectorW(ctx, rec, sp)
+    dn.set_dense(True)
+    assert dn.dense_arith() == "float_pair"
+    a = np.random.default_rng(4).standard_normal(w.n)
+    scale = np.max(np.abs(mf.A_product(np.abs(a))))
+    assert np.max(np.abs(dn.A_product(a) - mf.A_product(a))) <= 1e-12 * scale
+    dn.close()
+    mf.close()
+
+
+def test_dense_out_of_range_entries_use_fp64(ctx):
+    """Entries below 2^-100 (var_s = 1e-40) cannot be split into float pairs;
+    the dense operator then multiplies in FP64."""
+    w = synth.small(8, 40, 8.0, seed=30)
+    rec = pixel_to_npixel(w.pixels)
+    sp = SignalCovarParams(1e-40, LP, LQ, eval="exact")
+    mf, dn = WFVectorSN(ctx, rec, sp), WFVectorSN(ctx, rec, sp)
+    dn.set_dense(True)
+    assert dn.dense_arith() == "fp64"
+    a = np.random.default_rng(5).standard_normal(w.n)
+    assert rel(dn.A_product(a), mf.A_product(a)) < 1e-12
+    dn.close()
+    mf.close()
