@@ -1,7 +1,11 @@
 // ds_solve_pcg_noalloc: Jacobi-PCG for callers that cannot allocate device
 // memory.  Everything the solve needs beyond the caller's own buffers lives
-// in one file-scope device array of fixed size, reserved when the library is
-// loaded on a device and kept until the process exits.
+// in one file-scope device array of fixed size, kept until the process
+// exits.  CUDA loads a library's device code lazily by default (since CUDA
+// 12.2), so the array is reserved on a device when this file's code is first
+// used there, i.e. by the first call on that device (which looks up the
+// array's address), unless the process runs with CUDA_MODULE_LOADING=EAGER;
+// callers should make that first call during their set-up.
 //
 // Compared with ds_solve_pcg it drops everything that needs memory of its
 // own: no spatial sort (the radix sort needs temporary storage), no tile-pair
@@ -342,9 +346,9 @@ extern "C" int ds_solve_pcg_noalloc(int form, int n, const double* records,
       DS_CUDA(cudaStreamSynchronize(st));
       r.final_norm = h.norm_r;
       r.n_inner = h.iter;
-      if (pp->max_iter <= 1) {
-        r.success = 0;
-        r.num_iters = pp->max_iter > 1 ? pp->max_iter : 1;
+      if (pp->max_iter <= 1) {  // lib/pcg.h:117-158, as ds_solve_pcg
+        r.success = pp->max_iter == 1 ? 0 : 1;
+        r.num_iters = 1;
       } else if (h.converged) {
         r.success = 1;
         r.num_iters = h.iter;
@@ -353,6 +357,7 @@ extern "C" int ds_solve_pcg_noalloc(int form, int n, const double* records,
         r.num_iters = pp->max_iter;
       }
       status = r.success ? DS_OK : DS_ERR_NOT_CONVERGED;
+      if (!r.success) puts("[WARNING] PCG reached max iteration before stop condition.");
       if (residual_norms) {
         const int nh = std::min(h.iter + 1, NA_HIST);
         DS_CUDA(cudaMemcpyAsync(residual_norms, p.hist, nh * sizeof(double),

@@ -19,11 +19,12 @@
 //             7 FMA-pipe lanes (18 pairs/clk/SM); relative error ~1e-7.  Used
 //             for the map product and when a tile is too large for EXPANDED
 //             (2^|xi|^2 would leave FP32 range).
-// Each CTA owns a 128-row tile; lane l of warp w holds rows l, l+32, l+64,
-// l+96 (as two f32x2 pairs) and walks columns [32w, 32w+32) of every column
-// tile, so a column's staged data is read once per 4 rows.  Per-tile FP32
-// sums of 32 terms are folded into Kahan-compensated FP32 accumulators; the
-// four warps' partial rows are summed in FP64 at the end.
+// Each CTA owns a 128-row tile; lane l of each warp holds rows l, l+32, l+64,
+// l+96 (as two f32x2 pairs), and the warps share out the row tile's work
+// items (32-column sub-tiles of its interacting column tiles), staging two
+// items per round, so a staged column is read once per 4 rows.  Each round's
+// FP32 sums (64 terms) are folded into Kahan-compensated FP32 accumulators;
+// the four warps' partial rows are summed in FP64 at the end.
 #include "ds_device.cuh"
 #include "ds_f32.h"
 
@@ -53,58 +54,81 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 // One warp's 32 staged columns against its lane's four rows, as two f32x2 row
 // pairs (01: rows lane and lane+32, 23: rows lane+64 and lane+96).  A pair
 // whose two row sub-tiles are both beyond the cutoff from the column
-// sub-tile is skipped (DO01 / DO23 false).
+// sub-tile is skipped (DO01 / DO23 false).  The column values come four to a
+// shared-memory load.
 template <int FORMULA, bool DO01, bool DO23>
 __device__ __forceinline__ void accumulate32(const float4* __restrict__ col,
-                                             const float* __restrict__ cu, float2 x01,
+                                             const float4* __restrict__ cu4, float2 x01,
                                              float2 y01, float2 z01, float2 x23, float2 y23,
                                              float2 z23, float2& acc01, float2& acc23) {
 #pragma unroll
-  for (int jj = 0; jj < 32; ++jj) {
-    const float4 c4 = col[jj];
-    const float2 u2 = make_float2(cu[jj], cu[jj]);
-    float2 t01, t23;
-    if (FORMULA == F32_EXPANDED) {
-      const float2 cx = make_float2(c4.x, c4.x), cy = make_float2(c4.y, c4.y);
-      const float2 cz = make_float2(c4.z, c4.z), cw = make_float2(c4.w, c4.w);
-      if (DO01) {
-        t01 = __ffma2_rn(x01, cx, cw);
-        t01 = __ffma2_rn(y01, cy, t01);
-        t01 = __ffma2_rn(z01, cz, t01);
+  for (int qd = 0; qd < 8; ++qd) {
+    const float4 u4 = cu4[qd];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 c4 = col[4 * qd + k];
+      const float uk = k == 0 ? u4.x : k == 1 ? u4.y : k == 2 ? u4.z : u4.w;
+      const float2 u2 = make_float2(uk, uk);
+      float2 t01, t23;
+      if (FORMULA == F32_EXPANDED) {
+        const float2 cx = make_float2(c4.x, c4.x), cy = make_float2(c4.y, c4.y);
+        const float2 cz = make_float2(c4.z, c4.z), cw = make_float2(c4.w, c4.w);
+        if (DO01) {
+          t01 = __ffma2_rn(x01, cx, cw);
+          t01 = __ffma2_rn(y01, cy, t01);
+          t01 = __ffma2_rn(z01, cz, t01);
+        }
+        if (DO23) {
+          t23 = __ffma2_rn(x23, cx, cw);
+          t23 = __ffma2_rn(y23, cy, t23);
+          t23 = __ffma2_rn(z23, cz, t23);
+        }
+      } else {
+        const float2 ncx = make_float2(-c4.x, -c4.x), ncy = make_float2(-c4.y, -c4.y);
+        const float2 ncz = make_float2(-c4.z, -c4.z);
+        if (DO01) {
+          const float2 dx = __fadd2_rn(x01, ncx), dy = __fadd2_rn(y01, ncy);
+          const float2 dz = __fadd2_rn(z01, ncz);
+          t01 = __fmul2_rn(dx, make_float2(-dx.x, -dx.y));
+          t01 = __ffma2_rn(dy, make_float2(-dy.x, -dy.y), t01);
+          t01 = __ffma2_rn(dz, make_float2(-dz.x, -dz.y), t01);
+        }
+        if (DO23) {
+          const float2 dx = __fadd2_rn(x23, ncx), dy = __fadd2_rn(y23, ncy);
+          const float2 dz = __fadd2_rn(z23, ncz);
+          t23 = __fmul2_rn(dx, make_float2(-dx.x, -dx.y));
+          t23 = __ffma2_rn(dy, make_float2(-dy.x, -dy.y), t23);
+          t23 = __ffma2_rn(dz, make_float2(-dz.x, -dz.y), t23);
+        }
       }
-      if (DO23) {
-        t23 = __ffma2_rn(x23, cx, cw);
-        t23 = __ffma2_rn(y23, cy, t23);
-        t23 = __ffma2_rn(z23, cz, t23);
-      }
-    } else {
-      const float2 ncx = make_float2(-c4.x, -c4.x), ncy = make_float2(-c4.y, -c4.y);
-      const float2 ncz = make_float2(-c4.z, -c4.z);
-      if (DO01) {
-        const float2 dx = __fadd2_rn(x01, ncx), dy = __fadd2_rn(y01, ncy);
-        const float2 dz = __fadd2_rn(z01, ncz);
-        t01 = __fmul2_rn(dx, make_float2(-dx.x, -dx.y));
-        t01 = __ffma2_rn(dy, make_float2(-dy.x, -dy.y), t01);
-        t01 = __ffma2_rn(dz, make_float2(-dz.x, -dz.y), t01);
-      }
-      if (DO23) {
-        const float2 dx = __fadd2_rn(x23, ncx), dy = __fadd2_rn(y23, ncy);
-        const float2 dz = __fadd2_rn(z23, ncz);
-        t23 = __fmul2_rn(dx, make_float2(-dx.x, -dx.y));
-        t23 = __ffma2_rn(dy, make_float2(-dy.x, -dy.y), t23);
-        t23 = __ffma2_rn(dz, make_float2(-dz.x, -dz.y), t23);
-      }
+      if (DO01) acc01 = __ffma2_rn(make_float2(ex2f(t01.x), ex2f(t01.y)), u2, acc01);
+      if (DO23) acc23 = __ffma2_rn(make_float2(ex2f(t23.x), ex2f(t23.y)), u2, acc23);
     }
-    if (DO01) acc01 = __ffma2_rn(make_float2(ex2f(t01.x), ex2f(t01.y)), u2, acc01);
-    if (DO23) acc23 = __ffma2_rn(make_float2(ex2f(t23.x), ex2f(t23.y)), u2, acc23);
   }
+}
+
+// The 32 columns of one staged work item with the row pairs its mask names.
+template <int FORMULA>
+__device__ __forceinline__ void accumulate_item(unsigned m, const float4* __restrict__ col,
+                                                const float4* __restrict__ cu4, float2 x01,
+                                                float2 y01, float2 z01, float2 x23, float2 y23,
+                                                float2 z23, float2& acc01, float2& acc23) {
+  const bool do01 = (m & 3u) != 0;   // row sub-tile 0 or 1
+  const bool do23 = (m & 12u) != 0;  // row sub-tile 2 or 3
+  if (do01 && do23)
+    accumulate32<FORMULA, true, true>(col, cu4, x01, y01, z01, x23, y23, z23, acc01, acc23);
+  else if (do01)
+    accumulate32<FORMULA, true, false>(col, cu4, x01, y01, z01, x23, y23, z23, acc01, acc23);
+  else if (do23)
+    accumulate32<FORMULA, false, true>(col, cu4, x01, y01, z01, x23, y23, z23, acc01, acc23);
 }
 
 template <int FORMULA, int EPI, bool DOT>
 __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
   if (a.skip_flag && *a.skip_flag) return;
-  __shared__ float4 sc[TILE];
-  __shared__ float su[TILE];
+  // per warp: two staged work items (64 columns) and their column values
+  __shared__ float4 sc[2 * TILE];
+  __shared__ float4 su4[2 * TILE / 4];
   __shared__ float sred[4][TILE];
   __shared__ double red[TILE / 32];
   const int t = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;  // heaviest tiles first
@@ -129,9 +153,9 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
   // masks (each warp sums all 128 rows, so the sub-tiles may be shared out
   // freely) and the order of every FP32 sum is fixed.  A warp reads its next
   // 32 items in one load (lane l: its item 32 b + l, the next batch
-  // prefetched).  The column inputs of a warp's item i + 2 are loaded into
-  // registers while item i is computed (two register sets, used alternately
-  // so that no register copy waits for a load in flight).
+  // prefetched).  A round stages two items (64 columns, one per lane and
+  // item) and folds them into the compensated sums once; the column inputs
+  // of the next round are loaded into registers while a round is computed.
   const int i1 = a.item_ptr[t + 1];
   struct ColRegs {
     float3 q, o;   // this lane's column (tile-relative) and the tile's origin
@@ -165,48 +189,46 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
     ++pos;
     return true;
   };
-  // Each warp stages and reads only its own 32 columns (sc[32 warp + lane]),
-  // so the warps of a CTA never wait for each other inside the loop.
-  auto process = [&](ColRegs& c) -> bool {
-    const bool do01 = (c.m & 3u) != 0;   // row sub-tile 0 or 1
-    const bool do23 = (c.m & 12u) != 0;  // row sub-tile 2 or 3
-    __syncwarp();
-    {
-      const float dx = ot.x - c.o.x, dy = ot.y - c.o.y, dz = ot.z - c.o.z;
-      const float zx = c.q.x - dx, zy = c.q.y - dy, zz = c.q.z - dz;
-      if (FORMULA == F32_EXPANDED) {
-        const float aj = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
-        sc[tid] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -aj);
-      } else {
-        sc[tid] = make_float4(zx, zy, zz, 0.f);
-      }
-      su[tid] = c.u;
+  // Each warp stages and reads only its own 64 columns, so the warps of a
+  // CTA never wait for each other inside the loop.
+  float4* const scw = sc + warp * 64;
+  float* const suw = reinterpret_cast<float*>(su4 + warp * 16);
+  auto stage = [&](const ColRegs& c, int slot) {
+    const float dx = ot.x - c.o.x, dy = ot.y - c.o.y, dz = ot.z - c.o.z;
+    const float zx = c.q.x - dx, zy = c.q.y - dy, zz = c.q.z - dz;
+    if (FORMULA == F32_EXPANDED) {
+      const float aj = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+      scw[slot + lane] = make_float4(2.f * zx, 2.f * zy, 2.f * zz, -aj);
+    } else {
+      scw[slot + lane] = make_float4(zx, zy, zz, 0.f);
     }
-    __syncwarp();
-    const bool more = fetch(c);
-    float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
-    const float4* col = sc + warp * 32;
-    const float* cu = su + warp * 32;
-    evaluated += (do01 ? 2 * SUBTILE * 32 : 0) + (do23 ? 2 * SUBTILE * 32 : 0);
-    if (do01 && do23)
-      accumulate32<FORMULA, true, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
-    else if (do01)
-      accumulate32<FORMULA, true, false>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
-    else
-      accumulate32<FORMULA, false, true>(col, cu, x01, y01, z01, x23, y23, z23, acc01, acc23);
-    kahan_add(s0, c0, acc01.x);
-    kahan_add(s1, c1, acc01.y);
-    kahan_add(s2, c2, acc23.x);
-    kahan_add(s3, c3, acc23.y);
-    return more;
+    suw[slot + lane] = c.u;
   };
   ColRegs ca, cb;
   bool va = fetch(ca);
   bool vb = va && fetch(cb);
   while (va) {
-    va = process(ca);  // false once no item is left for ca
-    if (!vb) break;
-    vb = process(cb);
+    const unsigned ma = ca.m, mb = vb ? cb.m : 0u;
+    __syncwarp();
+    stage(ca, 0);
+    if (vb) stage(cb, 32);
+    __syncwarp();
+    const bool na = vb && fetch(ca);
+    const bool nbv = na && fetch(cb);
+    if (a.prof_pairs)
+      evaluated += 2 * SUBTILE * 32 * (((ma & 3u) != 0) + ((ma & 12u) != 0) +
+                                       ((mb & 3u) != 0) + ((mb & 12u) != 0));
+    float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
+    accumulate_item<FORMULA>(ma, scw, su4 + warp * 16, x01, y01, z01, x23, y23, z23, acc01,
+                             acc23);
+    accumulate_item<FORMULA>(mb, scw + 32, su4 + warp * 16 + 8, x01, y01, z01, x23, y23, z23,
+                             acc01, acc23);
+    kahan_add(s0, c0, acc01.x);
+    kahan_add(s1, c1, acc01.y);
+    kahan_add(s2, c2, acc23.x);
+    kahan_add(s3, c3, acc23.y);
+    va = na;
+    vb = nbv;
   }
   if (a.prof_pairs && lane == 0) atomicAdd(a.prof_pairs, (unsigned long long)evaluated);
   // Cross-warp reduction of the four column slices, in FP64.

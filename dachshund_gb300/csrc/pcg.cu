@@ -300,9 +300,12 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
   res.seconds = ms * 1e-3;
   res.n_outer = 0;
   res.n_inner = h.iter;
+  // lib/pcg.h:117-158: the loop variable leaves the loop at 1 when
+  // max_iter <= 1, and success is false only when it equals max_iter, so
+  // max_iter = 1 fails and max_iter = 0 succeeds, both with one iteration.
   if (pp.max_iter <= 1) {
-    res.success = 0;
-    res.num_iters = std::max(pp.max_iter, 1);
+    res.success = pp.max_iter == 1 ? 0 : 1;
+    res.num_iters = 1;
   } else if (h.converged) {
     res.success = 1;
     res.num_iters = h.iter;
@@ -320,8 +323,9 @@ void run_pcg(ds_operator* op, const ds_pcg_params& pp, ds_pcg_result& res, doubl
       else
         printf("    iter %i, |r| %e, delta %e\n", k, hh[k], dh[k]);
     }
-    if (!res.success) puts("[WARNING] PCG reached max iteration before stop condition.");
   }
+  // printed on every failed solve, as lib/pcg.h:151-155 does
+  if (!res.success) puts("[WARNING] PCG reached max iteration before stop condition.");
 }
 
 }  // namespace ds

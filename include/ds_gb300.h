@@ -259,7 +259,12 @@ int ds_solve_pcg_dev(ds_operator* op, const ds_pcg_params* pp, double* x,
  * spatial tiling (it needs temporary memory): every pixel pair is evaluated,
  * so this entry point suits small and medium problems.
  *  - The first call on a device looks up the work space's device address
- *    (once per device); make that first call before any stream capture.
+ *    (once per device).  CUDA loads device code lazily by default, so that
+ *    first call is also when the work space is reserved on the device and
+ *    the library's code is loaded there (unless the process sets
+ *    CUDA_MODULE_LOADING=EAGER): it can then allocate, synchronise or fail
+ *    for lack of memory.  Make the first call on each device during set-up,
+ *    before any stream capture; later calls allocate nothing.
  *  - All calls share the one work space and each call re-initialises it:
  *    calls that overlap on the GPU (other streams or threads) race.
  *  - ``stream`` is a cudaStream_t (NULL: the legacy default stream); the call

@@ -41,12 +41,30 @@ class _DsoKernel(C.Structure):
     ]
 
 
-def build(ref: bool = True, quiet: bool = True) -> None:
-    """Build the port (always) and the reference harness (when sources exist)."""
+def build(ref_dir: str | None = None, quiet: bool = True) -> None:
+    """Build the port (always) and, given the reference source tree
+    (``ref_dir``, else the REF environment variable), the reference harness."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE, "port"], stdout=out)
-    if ref and os.path.isdir(os.environ.get("REF", "/root/reference") + "/lib"):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"], stdout=out)
+    ref_dir = ref_dir or os.environ.get("REF")
+    if ref_dir and os.path.isdir(os.path.join(ref_dir, "lib")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref_dir], stdout=out)
+
+
+def ref_source_dir() -> str | None:
+    """The reference source tree the harness in oracle/_ref was built from
+    (recorded by ``make ref``), or the REF environment variable; None when
+    neither names an existing tree."""
+    cands = [os.environ.get("REF")]
+    try:
+        with open(os.path.join(HERE, "_ref", "source_dir")) as f:
+            cands.insert(0, f.read().strip())
+    except OSError:
+        pass
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "lib")):
+            return c
+    return None
 
 
 _port = None
@@ -57,7 +75,7 @@ def port_lib():
     global _port
     if _port is None:
         if not os.path.exists(PORT_SO):
-            build(ref=False)
+            build()
         lib = C.CDLL(PORT_SO)
         K = C.POINTER(_DsoKernel)
         lib.dso_kernel_init.argtypes = [K, C.c_double, C.c_double, C.c_double, C.c_int]

@@ -133,9 +133,10 @@ if __name__ == "__main__":
         OUT = sys.argv[2]
     elif len(sys.argv) != 1:
         sys.exit("usage: make_golden.py [--out DIR]")
-    oracle.build(ref=True)
+    oracle.build(oracle.ref_source_dir())
     if not oracle.ref_available():
-        sys.exit("reference harness unavailable: build oracle/_ref first")
+        sys.exit("reference harness unavailable: build oracle/_ref first "
+                 "(make -C oracle ref REF=<reference source tree>)")
     make_edge()
     make_small()
     make_wf4096()

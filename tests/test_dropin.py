@@ -10,12 +10,14 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIBDIR = os.path.join(ROOT, "dachshund_gb300")
-REF = os.environ.get("REF", "/root/reference")
+import oracle  # noqa: E402  (only for the location of the reference sources)
+
+REF = oracle.ref_source_dir() or ""
 CXX = ["g++", "-std=c++11", "-O1", "-I" + os.path.join(LIBDIR, "lib"),
        "-I" + os.path.join(ROOT, "include")]
 LINK = ["-L" + LIBDIR, "-ldachshund_gb300", "-ldsgb300", "-Wl,-rpath," + LIBDIR, "-lpthread"]
 
-needs_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "app")),
+needs_ref = pytest.mark.skipif(not (REF and os.path.isdir(os.path.join(REF, "app"))),
                                reason="reference sources not present")
 
 

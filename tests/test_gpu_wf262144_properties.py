@@ -8,12 +8,16 @@ where the oracle cannot solve the whole system in seconds.
 * Rows of A a at both ends of the record order match the oracle's rows
   (lib/wf_vector.cc:196-220 with the exact kernel) to 1e-11 of A|a|.
 * The mixed-precision solve stops on |b - A x| <= 1e-8 |b|, and the FP64
-  operator agrees (lib/pcg.h:27-160 stopping rule)."""
+  operator agrees (lib/pcg.h:27-160 stopping rule).
+* The FP32 map (80 x 80 x 512 grid) of that solution matches the oracle's
+  FP64 map rows (lib/map.cc:20-43, exact kernel) on 4,096 grid points (a
+  corner slab and a slab at the box centre) to 1e-6 of max |m|."""
 import numpy as np
 import pytest
 
 import oracle
-from dachshund_gb300 import MixedParams, SignalCovarParams, WFVectorW, pixel_to_wpixel, synth
+from dachshund_gb300 import (MapGrid, MixedParams, SignalCovarParams, WFVectorW,
+                             pixel_to_wpixel, synth)
 
 pytestmark = pytest.mark.gpu
 
@@ -21,9 +25,13 @@ VS, LP, LQ = synth.VAR_S, synth.L_PERP, synth.L_PARA
 
 
 @pytest.fixture(scope="module")
-def system(ctx):
-    w = synth.wf262144(0)
-    rec = pixel_to_wpixel(w.pixels)
+def workload():
+    return synth.wf262144(0)
+
+
+@pytest.fixture(scope="module")
+def system(ctx, workload):
+    rec = pixel_to_wpixel(workload.pixels)
     op = WFVectorW(ctx, rec, SignalCovarParams(VS, LP, LQ, eval="exact"))
     yield rec, op
     op.close()
@@ -62,3 +70,20 @@ def test_mixed_solve_residual(system):
     y = x / rec[:, 3]  # the W form returns x = w y
     r = op.A_residual(y)
     assert np.linalg.norm(r) <= 1e-8 * (1 + 1e-6) * np.linalg.norm(rec[:, 4])
+
+
+def test_fp32_map_matches_oracle_rows(ctx, system, workload):
+    rec, op = system
+    w = workload
+    x, res = op.solve_mixed(MixedParams(tol=1e-8))
+    assert res.success
+    pts = synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz)
+    grid = MapGrid(ctx, pts)
+    m = grid.product_f32(op, x)
+    grid.close()
+    mid = (w.n_map // 2) - 1024
+    for r0 in (0, mid):
+        ref = oracle.smp_product_rows(w.pixels[:, :3], pts, x, r0, r0 + 2048, VS, LP, LQ,
+                                      exact=True)
+        err = np.max(np.abs(m[r0:r0 + 2048] - ref)) / np.max(np.abs(ref))
+        assert err <= 1e-6, (r0, err)

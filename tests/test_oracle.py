@@ -15,7 +15,9 @@ import oracle
 from dachshund_gb300 import synth
 
 VS, LP, LQ = synth.VAR_S, synth.L_PERP, synth.L_PARA
-REF_FIXTURE = "/root/reference/tests/small_pixel_data.bin"
+_REF_DIR = oracle.ref_source_dir()
+# the reference's own test fixture (tests/small_pixel_data.bin in its tree)
+REF_FIXTURE = os.path.join(_REF_DIR, "tests", "small_pixel_data.bin") if _REF_DIR else ""
 
 
 def rel(a, b):
