@@ -65,6 +65,8 @@ def parse():
                     help="skip the batched-chunks (512 chunks x 64 RHS) measurement")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner measurement")
+    ap.add_argument("--no-map-covar", action="store_true",
+                    help="skip the MapCovarDiag measurement")
     ap.add_argument("--no-wf32768", action="store_true",
                     help="skip the 32,768-pixel dense / matrix-free measurement")
     ap.add_argument("--cpu-sample-s", type=float, default=6.0,
@@ -263,6 +265,28 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def pipe_calibration(device: int):
+    """Pair throughput of the FP32 FMA + MUFU pipes in the pair kernel's
+    instruction mix, measured on this GPU now (bench_pipes.cu beside this
+    file, compiled for sm_103a into _build/): the practical ceiling reported
+    beside the FP32 pair kernel's nominal roofline.  None when it cannot be
+    built or run."""
+    src = os.path.join(ROOT, "bench_pipes.cu")
+    exe = os.path.join(ROOT, "_build", "bench_pipes")
+    try:
+        os.makedirs(os.path.dirname(exe), exist_ok=True)
+        if not (os.path.exists(exe) and os.path.getmtime(exe) >= os.path.getmtime(src)):
+            nvcc = os.environ.get("NVCC") or "nvcc"
+            subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe,
+                            src], check=True, capture_output=True, timeout=300)
+        env = dict(os.environ, CUDA_VISIBLE_DEVICES=str(device))
+        out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=120,
+                             env=env).stdout
+        return json.loads(out.strip().splitlines()[-1])
+    except (OSError, subprocess.SubprocessError, ValueError, IndexError):
+        return None
+
+
 def measured_peaks():
     """Measured HBM copy bandwidth and cuBLAS bf16 rate of this GPU model
     (MEASURED_PEAKS.json beside this file), if present."""
@@ -458,6 +482,34 @@ def run_wf32768(ctx, hbm_gbs):
     return out
 
 
+def run_map_covar(ctx, n_points=256):
+    """MapCovarDiag (lib/map_covar.cc:73-113) on the 4,096-pixel workload
+    (64 skewers x 64 pixels, tol 1e-5 as its app run, step_r 50) for
+    n_points map-grid points: the reference's table kernel (multi-RHS FP64
+    PCG, 16 points per solve) and the exact kernel (batched mixed precision,
+    64 points per solve); wall time per map point and the iteration counts."""
+    import numpy as np
+
+    from dachshund_gb300 import PCGParams, SignalCovarParams, map_covar_diag, pixel_to_npixel, synth
+
+    w = synth.wf4096(0)
+    nrec = pixel_to_npixel(w.pixels)
+    pts = synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz)
+    pts = pts[np.linspace(0, pts.shape[0] - 1, n_points).astype(int)]
+    pp = PCGParams(w.pcg_max_iter, w.pcg_step_r, w.pcg_tol)
+    out = {"workload": f"{w.name}, {n_points} map-grid points, tol {w.pcg_tol}"}
+    for ev in ("table", "exact"):
+        sp = SignalCovarParams(w.var_s, w.l_perp, w.l_para, eval=ev)
+        map_covar_diag(ctx, nrec, pts[:16], sp, pp)  # warm-up
+        t0 = time.perf_counter()
+        sig, iters, ok = map_covar_diag(ctx, nrec, pts, sp, pp)
+        dt = time.perf_counter() - t0
+        out[ev] = {"s": dt, "ms_per_point": dt / n_points * 1e3,
+                   "iters_mean": float(np.mean(iters[ok])) if ok.any() else None,
+                   "success": int(ok.sum())}
+    return out
+
+
 def run_learned(ctx, seeds=(10001, 10002, 10003, 10004, 10005)):
     """Learned warm start + skewer-band preconditioner on held-out systems of
     the 262,144-pixel geometry (seeds outside the 1-2000 training range),
@@ -597,14 +649,34 @@ def run_ours(args, rank, world, local):
             "peak_Gpair_per_s": PAIRS_PER_CLK["direct"] * SMS * sm_hz / 1e9},
     }
     k = kernels["fp32_inner_matvec"]
+    # Roofline of the FP32 pair kernel: its pipes' nominal pair rate, 32
+    # pairs/clk/SM (4 FMA lanes as two FFMA2 + 1 MUFU ex2 per pair; FMA 128
+    # lanes and ex2 32 per clock per SM).  Beside it, the pair rate that
+    # instruction mix reaches on this GPU with nothing else in the loop,
+    # measured now by bench_pipes.cu: the practical ceiling of the mix.
+    cal = pipe_calibration(local) if rank == 0 else None
+    peak = k["peak_Gpair_per_s"]
+    mix = None
+    if cal and cal.get("mix_pairs_per_s"):
+        mix = {
+            "Gpair_per_s": cal["mix_pairs_per_s"] / 1e9,
+            "pairs_per_clk_per_sm": cal["mix_pairs_per_s"] / (SMS * sm_hz),
+            "ex2_per_clk_per_sm": cal["ex2_per_s"] / (SMS * sm_hz),
+            "ffma_lanes_per_clk_per_sm": cal["ffma_lanes_per_s"] / (SMS * sm_hz),
+            "frac": (k["Gpair_per_s"] * 1e9 / cal["mix_pairs_per_s"]) if k["Gpair_per_s"] else None,
+            "basis": ("bench_pipes.cu in this run: 3 FFMA2 + 2 ex2 + 1 FFMA2 per two pairs in "
+                      "independent chains, no memory traffic, best of 20-64 warps/SM and 1-8 "
+                      "chains per thread, at the sampled SM clock"),
+        }
     roofline = {
         "kernel": "k_pair_f32 (FP32 inner matvec, exact kernel, MUFU ex2)",
         "bound": "fp32-fma+mufu", "unit": "Gpair/s",
-        "achieved": k["Gpair_per_s"], "peak": k["peak_Gpair_per_s"],
-        "frac": (k["Gpair_per_s"] / k["peak_Gpair_per_s"]) if k["Gpair_per_s"] else None,
-        "peak_basis": (f"{PAIRS_PER_CLK['expanded']:.0f} pairs/clk/SM (4 FMA lanes + 1 ex2 per "
-                       f"pair; FMA 128 lanes/clk/SM, ex2 32/clk/SM measured) x {SMS} SMs x "
+        "achieved": k["Gpair_per_s"], "peak": peak,
+        "frac": (k["Gpair_per_s"] / peak) if k["Gpair_per_s"] else None,
+        "peak_basis": (f"{PAIRS_PER_CLK['expanded']:.0f} pairs/clk/SM (FMA 128 lanes and ex2 32 "
+                       f"per clk per SM, nominal; each measured alone within 7%) x {SMS} SMs x "
                        f"median SM clock under load"),
+        "measured_mix_ceiling": mix,
         # DRAM bytes (read + write) of one launch, from one ncu capture of this
         # kernel on this workload (profiles/k_pair_f32_expanded_wf262144.md):
         # the working set stays in L2, the kernel is pipe bound
@@ -675,6 +747,7 @@ def run_ours(args, rank, world, local):
     batched = None if args.no_batched else run_batched(ctx)
     learned = None if args.no_learned else run_learned(ctx)
     wf32768 = None if args.no_wf32768 else run_wf32768(ctx, measured_peaks().get("hbm_gbs"))
+    map_covar = None if args.no_map_covar else run_map_covar(ctx)
     if batched and batched["matvec_algorithmic_tflops"] and batched["variant"].startswith("tensor"):
         peak = measured_peaks().get("bf16_tflops")
         if peak:
@@ -711,6 +784,7 @@ def run_ours(args, rank, world, local):
             "batched_chunks": batched,
             "learned_preconditioner": learned,
             "wf32768_dense_and_matrix_free": wf32768,
+            "map_covar_diag": map_covar,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

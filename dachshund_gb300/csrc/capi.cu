@@ -885,7 +885,7 @@ int ds_map_covar_diag(ds_context* ctx, int n_pix, const double* npixels, int n_m
     require(n_map >= 0 && (n_map == 0 || (map_points && sigma_m && iters && success)),
             "bad arguments");
     require(pp->step_r > 0, "step_r must be > 0");
-    map_covar_diag_run(op, n_map, map_points, *pp, sigma_m, iters, success);
+    if (n_map > 0) map_covar_diag_multi(op, n_map, map_points, *pp, sigma_m, iters, success);
   });
   ds_operator_destroy(op);
   return rc;

@@ -1,8 +1,6 @@
 // Dense paths: the operator A built densely in HBM, the dense FP64 matvec
-// used by PCG when the matrix fits, the closed-form solve (Cholesky) that
-// stands in for WFVector{SN,W}::solve_cf (lib/wf_vector.cc:123-155, 276-319),
-// and MapCovarDiag (lib/map_covar.cc:40-113) as one SN-form solve per map
-// point.
+// used by PCG when the matrix fits, and the closed-form solve (Cholesky) that
+// stands in for WFVector{SN,W}::solve_cf (lib/wf_vector.cc:123-155, 276-319).
 //
 // Dense matvec: A streamed once per product (8 n^2 bytes) by a persistent
 // grid over 64 x 2048 blocks, HBM-bound with float-pair arithmetic on the
@@ -419,49 +417,6 @@ __global__ void k_records_soa(int n, int form, const double* __restrict__ rec,
   b[i] = r[4];
 }
 
-// Map-covariance helpers: b_k = S(map_i, pix_k) (sorted pixel order; zero on
-// padding) and sigma = b . x.
-__global__ void k_map_column(KernelConsts kc, int n_pad, const int* __restrict__ perm,
-                             const double* __restrict__ px, const double* __restrict__ py,
-                             const double* __restrict__ pz, double mx, double my, double mz,
-                             const double* __restrict__ table, double* __restrict__ b) {
-  __shared__ double tf[TABLE_N];
-  for (int k = threadIdx.x; k < TABLE_N; k += blockDim.x) tf[k] = table[k];
-  __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_pad) return;
-  b[i] = perm[i] >= 0 ? s_eval_f64<DS_EVAL_TABLE>(mx - px[i], my - py[i], mz - pz[i], kc, tf)
-                      : 0.0;
-}
-
-__global__ void k_map_column_exact(KernelConsts kc, int n_pad, const int* __restrict__ perm,
-                                   const double* __restrict__ px, const double* __restrict__ py,
-                                   const double* __restrict__ pz, double mx, double my,
-                                   double mz, double* __restrict__ b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_pad) return;
-  const double dx = mx - px[i], dy = my - py[i], dz = mz - pz[i];
-  b[i] = perm[i] >= 0 ? kc.var_s * exp(-(kc.c_perp * (dx * dx + dy * dy) + kc.c_para * dz * dz))
-                      : 0.0;
-}
-
-__global__ void k_dot2(int n, const double* __restrict__ a, const double* __restrict__ b,
-                       const double* __restrict__ c, double* out) {
-  // out[0] = a.b, out[1] = c.c  (one CTA, deterministic)
-  __shared__ double red[8];
-  double s = 0.0, t = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    s = fma(a[i], b[i], s);
-    t = fma(c[i], c[i], t);
-  }
-  const double bs = block_sum<256>(s, red);
-  const double bt = block_sum<256>(t, red);
-  if (threadIdx.x == 0) {
-    out[0] = bs;
-    out[1] = bt;
-  }
-}
-
 }  // namespace
 
 // ---- dense operator for PCG ------------------------------------------------
@@ -629,49 +584,6 @@ void solve_cf_dev(ds_context* ctx, int form, int n, const double* d_rec,
   DS_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
   require(!h_bad, "closed-form solve: the matrix is not positive definite");
-}
-
-// ---- MapCovarDiag ---------------------------------------------------------------
-
-void map_covar_diag_run(ds_operator* op, int n_map, const double* map_pts,
-                        const ds_pcg_params& pp, double* sigma_m, int* iters, int* success) {
-  cudaStream_t st = op->ctx->stream;
-  ensure_pcg_workspace(op);
-  const int np = op->pix.n_pad;
-  DevBuf<double> out2;
-  out2.alloc(2);
-  for (int i = 0; i < n_map; ++i) {
-    const double* m = map_pts + (size_t)i * 3;
-    if (op->kc.eval == DS_EVAL_TABLE)
-      k_map_column<<<(np + 255) / 256, 256, 0, st>>>(op->kc, np, op->pix.perm.p, op->pix.x.p,
-                                                     op->pix.y.p, op->pix.z.p, m[0], m[1], m[2],
-                                                     op->table.p, op->b.p);
-    else
-      k_map_column_exact<<<(np + 255) / 256, 256, 0, st>>>(op->kc, np, op->pix.perm.p,
-                                                           op->pix.x.p, op->pix.y.p, op->pix.z.p,
-                                                           m[0], m[1], m[2], op->b.p);
-    DS_CHECK_LAUNCH();
-    DS_CUDA(cudaMemsetAsync(op->x.p, 0, np * sizeof(double), st));
-    k_dot2<<<1, 256, 0, st>>>(np, op->b.p, op->x.p, op->b.p, out2.p);
-    DS_CHECK_LAUNCH();
-    double h2[2];
-    DS_CUDA(cudaMemcpyAsync(h2, out2.p, sizeof(h2), cudaMemcpyDeviceToHost, st));
-    DS_CUDA(cudaStreamSynchronize(st));
-    op->norm_b = std::sqrt(h2[1]);
-    ds_pcg_result r{};
-    if (op->norm_b > 0.0) run_pcg(op, pp, r, nullptr);
-    double s = 0.0;
-    if (r.success) {
-      k_dot2<<<1, 256, 0, st>>>(np, op->b.p, op->x.p, op->b.p, out2.p);
-      DS_CHECK_LAUNCH();
-      DS_CUDA(cudaMemcpyAsync(h2, out2.p, sizeof(h2), cudaMemcpyDeviceToHost, st));
-      DS_CUDA(cudaStreamSynchronize(st));
-      s = h2[0];
-    }
-    sigma_m[i] = s;
-    iters[i] = r.num_iters;
-    success[i] = r.success;
-  }
 }
 
 }  // namespace ds

@@ -52,8 +52,10 @@ void dense_apply(ds_operator* op, bool residual, const double* v, double* out,
                  const double* dotv, PcgState* pcg, const int* skip, cudaStream_t st);
 void solve_cf_dev(ds_context* ctx, int form, int n, const double* d_rec, const KernelConsts& kc,
                   const double* d_table, double* d_x);
-void map_covar_diag_run(ds_operator* op, int n_map, const double* map_pts,
-                        const ds_pcg_params& pp, double* sigma_m, int* iters, int* success);
+// MapCovarDiag with the operator's table kernel: groups of map points as the
+// right-hand sides of one multi-RHS FP64 PCG each (multi.cu).
+void map_covar_diag_multi(ds_operator* op, int n_map, const double* map_pts,
+                          const ds_pcg_params& pp, double* sigma_m, int* iters, int* success);
 
 // Mixed-precision form (mixed.cu).
 void ensure_op_f32(ds_operator* op, double inner_cut);

@@ -14,28 +14,6 @@ namespace ds {
 
 namespace {
 
-// Table kernel without var_s (folded into the column weights): the argument
-// and the interpolation weights are bit-identical to the reference's
-// (lib/signal_covar.h:53-65); the truncating index comes from a round-down
-// add of 1.5 * 2^52 instead of a double->int conversion (slower than an FP64
-// FMA on GB300): for 0 <= xx < 2^51, t = xx + 1.5*2^52 rounded down holds
-// floor(xx) in its low mantissa bits and t - 1.5*2^52 == floor(xx) exactly.
-__device__ __forceinline__ double gp_table_fast(double dx, double dy, double dz,
-                                                const KernelConsts& k, const double* tf) {
-  const double perp2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-  const double para2 = __dmul_rn(dz, dz);
-  const double g = __dadd_rn(__dmul_rn(k.c_perp, perp2), __dmul_rn(k.c_para, para2));
-  const double xx = __dmul_rn(g, k.dx_inv);
-  const double M = 6755399441055744.0;
-  const double t = __dadd_rd(xx, M);
-  const double fl = t - M;
-  const int ix = min(max(__double2loint(t), 0), TABLE_N - 2);
-  const double lo = (fl + 1.0) - xx;
-  const double hi = xx - fl;
-  const double gp = fma(tf[ix], lo, tf[ix + 1] * hi);
-  return xx < (double)(TABLE_N - 1) ? gp : 0.0;
-}
-
 // Exact kernel without var_s, zero at and beyond the cutoff.
 __device__ __forceinline__ double g_exact_fast(double dx, double dy, double dz,
                                                const KernelConsts& k, const double* tab) {
