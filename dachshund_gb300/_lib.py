@@ -21,6 +21,7 @@ DS_ERR_NORM_B = 4
 DS_ERR_OOM = 5
 DS_ERR_NO_DEVICE = 6
 DS_ERR_STATE = 7
+DS_ERR_TIMEOUT = 8
 
 DS_FORM_SN = 0
 DS_FORM_W = 1
@@ -144,6 +145,7 @@ SIGNATURES = {
     "ds_context_synchronize": (_i, [_vp]),
     "ds_context_last_error": (C.c_char_p, [_vp]),
     "ds_context_set_profiling": (_i, [_vp, _i]),
+    "ds_context_set_wait_limit": (_i, [_vp, C.c_longlong]),
     "ds_context_get_profile": (_i, [_vp, C.POINTER(ProfileC)]),
     "ds_operator_create": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), C.POINTER(_vp)]),
     "ds_operator_destroy": (None, [_vp]),

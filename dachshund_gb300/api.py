@@ -171,6 +171,12 @@ class Context:
         """Time every pair-kernel launch with CUDA events on this context's stream."""
         self.check(self._lib.ds_context_set_profiling(self.handle, int(bool(enable))), "profiling")
 
+    def set_wait_limit(self, cycles: int = 0):
+        """Bound (SM clock cycles) of the batched tensor-core kernel's waits;
+        0 restores the default (4e9 cycles).  A wait that runs out makes the
+        call raise DsError with code DS_ERR_TIMEOUT."""
+        self.check(self._lib.ds_context_set_wait_limit(self.handle, int(cycles)), "wait limit")
+
     def profile(self) -> dict:
         p = _lib.ProfileC()
         self.check(self._lib.ds_context_get_profile(self.handle, C.byref(p)), "profile")

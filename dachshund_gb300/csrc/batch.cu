@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "ds_batch.h"
+#include "ds_tc.cuh"
 #include "ds_device.cuh"
 #include "ds_ff.cuh"
 
@@ -1030,6 +1031,7 @@ BatchF32Args mv_args(ds_batch* B) {
   a.formula = B->formula;
   a.panel = B->panel.p;
   a.err = B->err.p;
+  a.wait_limit = B->ctx->wait_limit > 0 ? B->ctx->wait_limit : WAIT_CYCLES;
   return a;
 }
 
@@ -1127,7 +1129,7 @@ static void check_tc_error(ds_batch* B) {
   DS_CUDA(cudaStreamSynchronize(B->ctx->stream));
   if (code) {
     DS_CUDA(cudaMemsetAsync(B->err.p, 0, sizeof(int), B->ctx->stream));
-    throw Error{DS_ERR_CUDA, "tensor-core matvec: an mbarrier wait timed out (code " +
+    throw Error{DS_ERR_TIMEOUT, "tensor-core matvec: an mbarrier wait timed out (code " +
                                  std::to_string(code) + ")"};
   }
 }

@@ -113,8 +113,8 @@ constexpr size_t tc_smem_bytes() {
 // A bounded wait that records a time-out: error code, CTA abort flag.
 template <int NB>
 __device__ __forceinline__ bool wait_or_abort(TcSmem<NB>& sm, uint64_t* bar, uint32_t parity,
-                                              int* err, int code) {
-  if (mbar_wait(bar, parity)) return true;
+                                              int* err, int code, long long limit) {
+  if (mbar_wait(bar, parity, limit)) return true;
   atomicExch(err, code);
   *(volatile int*)&sm.abort = 1;
   return false;
@@ -126,9 +126,9 @@ __device__ __forceinline__ bool wait_or_abort(TcSmem<NB>& sm, uint64_t* bar, uin
 template <int NB>
 __device__ __forceinline__ bool warp_wait_or_abort(TcSmem<NB>& sm, uint64_t* bar,
                                                    uint32_t parity, int* err, int code,
-                                                   int lane) {
+                                                   long long limit, int lane) {
   int ok = 1;
-  if (lane == 0) ok = wait_or_abort(sm, bar, parity, err, code);
+  if (lane == 0) ok = wait_or_abort(sm, bar, parity, err, code, limit);
   ok = __shfl_sync(0xffffffffu, ok, 0);
   __syncwarp();
   return ok != 0;
@@ -234,7 +234,9 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
         // S values of this warp's sub-tiles are formed in registers as soon as
         // the coordinates are staged; the S buffer is awaited only for the
         // stores
-        if (!warp_wait_or_abort(sm, &sm.sc_full[b], (g >> 1) & 1u, a.err, 11, lane)) break;
+        if (!warp_wait_or_abort(sm, &sm.sc_full[b], (g >> 1) & 1u, a.err, 11, a.wait_limit,
+                                lane))
+          break;
         const float4* sc = sm.sc[b];
         uint4 vh[GEN_CS][4], vl[GEN_CS][4];
 #pragma unroll
@@ -276,7 +278,8 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
           }
         }
         if (g >= 2 &&
-            !warp_wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 12, lane))
+            !warp_wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 12,
+                                a.wait_limit, lane))
           break;
         __nv_bfloat16* shi = sm.s[b][0];
         __nv_bfloat16* slo = sm.s[b][1];
@@ -307,7 +310,9 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
       float4 pvr[HN / 4];
 #pragma unroll
       for (int k4 = 0; k4 < HN / 4; ++k4) pvr[k4] = pv4[k4];
-      if (!warp_wait_or_abort(sm, &sm.d_full[db], (k >> 1) & 1u, a.err, 13, lane)) break;
+      if (!warp_wait_or_abort(sm, &sm.d_full[db], (k >> 1) & 1u, a.err, 13, a.wait_limit,
+                              lane))
+        break;
       __syncwarp();
       tc_fence_after();
       float d[HN], dl[HN];
@@ -345,7 +350,8 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
       // buffer db are rewritten two items later: those need D of that item,
       // i.e. the S tiles of the item in between from every generation warp.
       if (warp < NB / 32 + (NB < 32) &&
-          !warp_wait_or_abort(sm, &sm.red_full[db], (k >> 1) & 1u, a.err, 14, lane))
+          !warp_wait_or_abort(sm, &sm.red_full[db], (k >> 1) & 1u, a.err, 14, a.wait_limit,
+                              lane))
         break;
       if (tid < NB) {
         // column tid of the block: warp column group h = tid / HN, summed
@@ -390,7 +396,8 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
         for (int q = 0; q < TILE / 32; ++q) cq_n[q] = a.xi[ct_n * TILE + lane + 32 * q];
         // sc[b] is free once every generation warp finished tile g - 2
         if (g >= 2 &&
-            !warp_wait_or_abort(sm, &sm.s_full[b], ((g >> 1) - 1) & 1u, a.err, 22, lane))
+            !warp_wait_or_abort(sm, &sm.s_full[b], ((g >> 1) - 1) & 1u, a.err, 22,
+                                a.wait_limit, lane))
           break;
 #pragma unroll
         for (int q = 0; q < TILE / 32; ++q) {
@@ -407,7 +414,8 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
         if (lane == 0) mbar_arrive(&sm.sc_full[b]);
         // u[b] is free once the MMAs of tile g - 2 completed
         if (g >= 2 &&
-            !warp_wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 21, lane))
+            !warp_wait_or_abort(sm, &sm.mma_done[b], ((g >> 1) - 1) & 1u, a.err, 21,
+                                a.wait_limit, lane))
           break;
         if (lane == 0) {
           mbar_expect_tx(&sm.u_full[b], PANEL_BYTES);
@@ -430,15 +438,17 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
       if (a.chunk_done[a.tile_chunk[t]]) continue;
       const int p0 = a.row_ptr[t], p1 = a.row_ptr[t + 1];
       const uint32_t db = k & 1;
-      if (k >= 2 && !wait_or_abort(sm, &sm.d_empty[db], ((k >> 1) - 1) & 1u, a.err, 31)) break;
+      if (k >= 2 && !wait_or_abort(sm, &sm.d_empty[db], ((k >> 1) - 1) & 1u, a.err, 31,
+                                   a.wait_limit))
+        break;
       tc_fence_after();
       const uint32_t dt = tmem + db * D_COLS;
       uint32_t accumulate = 0;
       bool ok = true;
       for (int p = p0; p < p1; ++p, ++g) {
         const uint32_t b = g & 1;
-        if (!wait_or_abort(sm, &sm.u_full[b], (g >> 1) & 1u, a.err, 32) ||
-            !wait_or_abort(sm, &sm.s_full[b], (g >> 1) & 1u, a.err, 33)) {
+        if (!wait_or_abort(sm, &sm.u_full[b], (g >> 1) & 1u, a.err, 32, a.wait_limit) ||
+            !wait_or_abort(sm, &sm.s_full[b], (g >> 1) & 1u, a.err, 33, a.wait_limit)) {
           ok = false;
           break;
         }
@@ -465,10 +475,16 @@ __global__ void __maxnreg__(TC_MAXNREG) k_batch_mv_tc(BatchF32Args a) {
       ++k;
     }
   }
-  // teardown: after a time-out, wait (bounded) for this role's MMAs or copy
-  // in flight before the tensor memory is freed
+  // teardown: after a time-out, wait (bounded by the default, whatever the
+  // caller's limit) for this role's work in flight before the tensor memory
+  // and the shared memory are released: the last MMA commit (it covers every
+  // earlier MMA of the thread) and the last two panel copies (a copy into a
+  // buffer is issued only after the copy before it in that buffer was used).
   if (aborted(&sm.abort) && last_g >= 0 && lane == 0) {
-    if (warp == GEN_WARPS) mbar_wait(&sm.u_full[last_g & 1], (last_g >> 1) & 1u);
+    if (warp == GEN_WARPS) {
+      mbar_wait(&sm.u_full[last_g & 1], (last_g >> 1) & 1u);
+      if (last_g >= 1) mbar_wait(&sm.u_full[(last_g - 1) & 1], ((last_g - 1) >> 1) & 1u);
+    }
     if (warp == GEN_WARPS + 1) mbar_wait(&sm.mma_done[last_g & 1], (last_g >> 1) & 1u);
   }
   tc_fence_before();

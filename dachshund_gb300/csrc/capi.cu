@@ -214,6 +214,7 @@ const char* ds_status_string(int status) {
     case DS_ERR_OOM: return "out of memory";
     case DS_ERR_NO_DEVICE: return "no usable CUDA device";
     case DS_ERR_STATE: return "object in error state";
+    case DS_ERR_TIMEOUT: return "a bounded wait in a tensor-core kernel timed out";
     default: return "unknown status";
   }
 }
@@ -284,6 +285,12 @@ int ds_context_set_profiling(ds_context* ctx, int enable) {
     }
     p.enabled = enable != 0;
   });
+}
+
+int ds_context_set_wait_limit(ds_context* ctx, long long cycles) {
+  if (!ctx || cycles < 0) return DS_ERR_ARG;
+  ctx->wait_limit = cycles;
+  return DS_OK;
 }
 
 int ds_context_get_profile(ds_context* ctx, ds_profile* out) {

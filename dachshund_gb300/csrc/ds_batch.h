@@ -46,6 +46,7 @@ struct BatchF32Args {
   int formula;         // F32Formula of xi / rowf
   void* panel;         // tensor-core variant: BF16 hi / lo u panels
   int* err;            // tensor-core variant: error code of a timed-out wait
+  long long wait_limit;  // tensor-core variant: bound of its waits (SM clock cycles)
 };
 
 struct BatchF64Args {

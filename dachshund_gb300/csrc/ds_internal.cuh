@@ -293,6 +293,7 @@ struct PcgState {
 struct ds_context {
   int device = 0;
   int num_sms = 0;  // streaming multiprocessors of the device (persistent grids)
+  long long wait_limit = 0;  // bound of tensor-core mbarrier waits (0: default)
   cudaStream_t stream = nullptr;
   std::string last_error;
   ds::Profiler prof;

@@ -8,7 +8,10 @@
 
 namespace ds {
 
-// Bound of every mbarrier wait, in SM clock cycles (about 2 s at 2 GHz).
+// Default bound of an mbarrier wait, in SM clock cycles (about 2 s at 2 GHz).
+// The batched tensor-core kernel takes its bound from the context
+// (ds_context_set_wait_limit); teardown waits for work in flight always use
+// this one.
 constexpr long long WAIT_CYCLES = 4000000000LL;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -32,8 +35,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 
 // Waits for the completion of the phase with parity `parity` (test_wait
 // polls, with a 64 ns sleep between polls after the first 64); false once
-// WAIT_CYCLES have elapsed.  (A suspending try_wait measured slower here.)
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// `limit` cycles have elapsed.  (A suspending try_wait measured slower here.)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          long long limit = WAIT_CYCLES) {
   const uint32_t a = smem_u32(bar);
   long long t0 = 0;
   for (uint32_t k = 0;; ++k) {
@@ -48,7 +52,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (ok) return true;
     if (k == 0) {
       t0 = clock64();
-    } else if (clock64() - t0 > WAIT_CYCLES) {
+    } else if (clock64() - t0 > limit) {
       return false;
     }
     if (k >= 64) __nanosleep(64);

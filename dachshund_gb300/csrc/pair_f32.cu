@@ -23,8 +23,9 @@
 // l+96 (as two f32x2 pairs), and the warps share out the row tile's work
 // items (32-column sub-tiles of its interacting column tiles), staging two
 // items per round, so a staged column is read once per 4 rows.  Each round's
-// FP32 sums (64 terms) are folded into Kahan-compensated FP32 accumulators;
-// the four warps' partial rows are summed in FP64 at the end.
+// FP32 sums (64 terms; 32 for the map, which folds each item on its own) are
+// folded into Kahan-compensated FP32 accumulators; the four warps' partial
+// rows are summed in FP64 at the end.
 #include "ds_device.cuh"
 #include "ds_f32.h"
 
@@ -221,6 +222,15 @@ __global__ void __launch_bounds__(TILE, F32_MIN_CTAS) k_pair_f32(F32Args a) {
     float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
     accumulate_item<FORMULA>(ma, scw, su4 + warp * 16, x01, y01, z01, x23, y23, z23, acc01,
                              acc23);
+    if (EPI == EPI_MAP) {
+      // the map keeps 32-term FP32 partials: each item is folded on its own
+      kahan_add(s0, c0, acc01.x);
+      kahan_add(s1, c1, acc01.y);
+      kahan_add(s2, c2, acc23.x);
+      kahan_add(s3, c3, acc23.y);
+      acc01 = make_float2(0.f, 0.f);
+      acc23 = make_float2(0.f, 0.f);
+    }
     accumulate_item<FORMULA>(mb, scw + 32, su4 + warp * 16 + 8, x01, y01, z01, x23, y23, z23,
                              acc01, acc23);
     kahan_add(s0, c0, acc01.x);

@@ -42,7 +42,10 @@ typedef enum {
   DS_ERR_NORM_B = 4,        /* |b| <= 0: early return (lib/pcg.h:79-86) */
   DS_ERR_OOM = 5,           /* device allocation failed */
   DS_ERR_NO_DEVICE = 6,     /* no CUDA device or wrong architecture */
-  DS_ERR_STATE = 7          /* object used after a fatal error */
+  DS_ERR_STATE = 7,         /* object used after a fatal error */
+  DS_ERR_TIMEOUT = 8        /* a bounded wait inside a tensor-core kernel ran out; the
+                               kernel released its tensor memory and returned, and the
+                               context stays usable */
 } ds_status;
 
 const char* ds_status_string(int status);
@@ -132,6 +135,15 @@ typedef struct {
 } ds_profile;
 int ds_context_set_profiling(ds_context* ctx, int enable);
 int ds_context_get_profile(ds_context* ctx, ds_profile* out);
+
+/* Bound, in SM clock cycles, of every mbarrier wait of the batched
+ * tensor-core matvec (ds_batch_set_variant DS_BATCH_TENSOR) launched on this
+ * context; 0 restores the default of 4e9 cycles (about 2 s).  A wait that
+ * runs out records its code, the kernel waits (with the default bound) for
+ * its own MMAs and copies in flight, frees its tensor memory and returns, and
+ * the call returns DS_ERR_TIMEOUT.  No reference counterpart (the reference
+ * has no device code). */
+int ds_context_set_wait_limit(ds_context* ctx, long long cycles);
 
 /* ---- the operator A over one pixel set --------------------------------- */
 typedef struct ds_operator ds_operator;

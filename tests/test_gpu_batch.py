@@ -200,6 +200,39 @@ def test_batch_autotuner_choice(ctx):
     bs.close()
 
 
+def test_tensor_core_wait_timeout_is_reported_and_recoverable(ctx):
+    """The tcgen05 matvec's bounded waits: with a bound of 1 SM clock cycle
+    the first wait that is not already satisfied runs out, the kernel records
+    its code, waits (with the default bound) for its own MMAs and copies in
+    flight, frees its tensor memory and returns, and the solve raises
+    DS_ERR_TIMEOUT.  With the default bound restored the same batch on the
+    same context solves to tolerance and agrees with the CUDA-core variant,
+    so the failed launches left the context and the tensor memory usable."""
+    from dachshund_gb300 import _lib
+    from dachshund_gb300._lib import DsError
+
+    pixes, rhs = small_batch(3, 16, seed=77, sk=(3, 8), per=(16, 40))
+    recs, b = to_form("w", pixes, rhs)
+    bs = BatchSolver(ctx, "w", recs, EXACT, n_rhs=16)
+    bs.set_variant("tensor")
+    assert bs.info()["variant"] == 1
+    try:
+        ctx.set_wait_limit(1)
+        with pytest.raises(DsError) as ei:
+            bs.solve_mixed(b, MixedParams(max_iter=20, tol=1e-8))
+        assert ei.value.code == _lib.DS_ERR_TIMEOUT
+    finally:
+        ctx.set_wait_limit(0)
+    for _ in range(2):
+        x, res = bs.solve_mixed(b, MixedParams(tol=1e-8))
+        assert res.status == 0 and res.converged.all() and res.rel_resid.max() <= 1e-8
+    bs.set_variant("cuda_core")
+    xc, resc = bs.solve_mixed(b, MixedParams(tol=1e-8))
+    assert resc.converged.all()
+    assert rel(x, xc) < 1e-6
+    bs.close()
+
+
 @pytest.mark.parametrize("n_rhs", [16, 32, 64])
 def test_batch_tensor_core_product_and_solve(ctx, n_rhs):
     """The tcgen05 BF16 hi/lo matvec: product within 1e-4 of the FP64 oracle
