@@ -260,6 +260,19 @@ class _WFVector:
         self.ctx.check(self._lib.ds_operator_set_inner_matvec(self.handle, v),
                        "ds_operator_set_inner_matvec")
 
+    def set_cluster_preconditioner(self, n_skewers: int, n_per: int, cluster: int = 4,
+                                   band: int = 16) -> int:
+        """Preconditions solve_mixed with the cluster factor M^-1 = G G^T
+        (clusters of `cluster` neighbouring skewers, FSAI factor with `band`
+        sub-diagonals) instead of Jacobi; cluster = 0 removes it.  Records
+        must be skewer-contiguous (n_skewers x n_per).  Returns the number of
+        columns that fell back to Jacobi."""
+        nf = C.c_int(0)
+        self.ctx.check(self._lib.ds_operator_set_cluster_preconditioner(
+            self.handle, int(n_skewers), int(n_per), int(cluster), int(band), C.byref(nf)),
+            "ds_operator_set_cluster_preconditioner")
+        return nf.value
+
     def info(self) -> dict:
         inf = _lib.OperatorInfoC()
         self.ctx.check(self._lib.ds_operator_get_info(self.handle, C.byref(inf)), "info")

@@ -1,0 +1,255 @@
+// Cluster preconditioner of the mixed-precision solver (no reference
+// counterpart; the reference's PCG is Jacobi, lib/wf_vector.cc:42-49,185-194).
+//
+// Why clusters: the pixels of one skewer couple strongly along z, but a
+// skewer also couples to its neighbours a few Mpc/h away, and on the skewer
+// densities of these workloads that cross-skewer coupling is what Jacobi-PCG
+// spends its iterations on.  Preconditioning each skewer's own 256 x 256
+// block exactly (its full inverse) saves only a quarter of the iterations; a
+// block over a cluster of four neighbouring skewers saves more than half.
+//
+// The factor: a factorized sparse approximate inverse (FSAI, Kolotilina and
+// Yeremin 1993) of each cluster's block A_cc, in the order "by z, then by
+// skewer" (the skewers' pixels interleaved), with a lower band of `band`
+// sub-diagonals.  Column j of the lower-triangular G, on the rows
+// J = j .. j + band of its cluster, is
+//     g = A[J, J]^-1 e_1,   G[J, j] = g / sqrt(g_1),
+// the band-limited counterpart of the Cholesky factor of A_cc^-1 (with the
+// full pattern G G^T = A_cc^-1 exactly).  M^-1 = G G^T is symmetric positive
+// definite by construction (G is triangular with a positive diagonal), and
+// the solver applies it with the band kernel of mixed.cu (one CTA per
+// cluster).  Each column is an independent (band + 1)-point Cholesky solve
+// in FP32 from the operator's own coefficients, so the build is one short
+// kernel; a column whose small system is not positive definite in FP32
+// (none on the workloads here) falls back to the Jacobi factor 1/sqrt(A_jj).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "ds_device.cuh"
+#include "ds_learned.h"
+#include "ds_ops.h"
+
+namespace ds {
+namespace {
+
+constexpr int CPC_MAX_BAND = 24;
+constexpr int CPC_PACKED = (CPC_MAX_BAND + 1) * (CPC_MAX_BAND + 2) / 2;
+
+// Column `j` (a slot) of G: rows j .. j + m - 1, the next non-padding slots
+// of its block (at most band + 1).  A_ab = wl_a S_ab wr_b + e_a delta_ab with
+// the exact Gaussian S (the table kernel differs from it by ~1e-4, which is
+// immaterial to a preconditioner).
+__global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc,
+                               const int* __restrict__ crec, const int* __restrict__ inv,
+                               const double* __restrict__ px, const double* __restrict__ py,
+                               const double* __restrict__ pz, const double* __restrict__ wl,
+                               const double* __restrict__ wr, const double* __restrict__ e,
+                               float* __restrict__ L, int* __restrict__ n_fallback) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_slots) return;
+  if (crec[j] < 0) return;  // padding slot: its row stays 0
+  const int blk_end = (j / block + 1) * block;
+  int pos[CPC_MAX_BAND + 1];
+  int m = 0;
+  while (m <= band && j + m < blk_end && crec[j + m] >= 0) {
+    pos[m] = inv[crec[j + m]];
+    ++m;
+  }
+  float C[CPC_PACKED];  // packed lower Cholesky factor: row a starts at a (a + 1) / 2
+  bool ok = true;
+  for (int a = 0; a < m && ok; ++a) {
+    const int pa = pos[a];
+    const double xa = px[pa], ya = py[pa], za = pz[pa];
+    float* Ca = C + a * (a + 1) / 2;
+    for (int b = 0; b <= a; ++b) {
+      const int pb = pos[b];
+      const double dx = xa - px[pb], dy = ya - py[pb], dz = za - pz[pb];
+      const double arg = kc.c_perp * (dx * dx + dy * dy) + kc.c_para * dz * dz;
+      const double s = arg < kc.exact_cut ? kc.var_s * (double)expf(-(float)arg) : 0.0;
+      float v = (float)(wl[pa] * s * wr[pb] + (a == b ? e[pa] : 0.0));
+      const float* Cb = C + b * (b + 1) / 2;
+      for (int k = 0; k < b; ++k) v = fmaf(-Ca[k], Cb[k], v);
+      if (a == b) {
+        if (!(v > 0.f)) {
+          ok = false;
+          break;
+        }
+        Ca[a] = sqrtf(v);
+      } else {
+        Ca[b] = v / Cb[b];
+      }
+    }
+  }
+  if (!ok) {
+    const int p0 = pos[0];
+    const double a00 = wl[p0] * kc.var_s * wr[p0] + e[p0];
+    L[(size_t)j * (band + 1)] = (float)(1.0 / sqrt(a00));
+    atomicAdd(n_fallback, 1);
+    return;
+  }
+  // C y = e_1, then C^T g = y (g overwrites y)
+  float y[CPC_MAX_BAND + 1];
+  for (int a = 0; a < m; ++a) {
+    const float* Ca = C + a * (a + 1) / 2;
+    float v = a == 0 ? 1.f : 0.f;
+    for (int k = 0; k < a; ++k) v = fmaf(-Ca[k], y[k], v);
+    y[a] = v / Ca[a];
+  }
+  for (int a = m - 1; a >= 0; --a) {
+    float v = y[a];
+    for (int k = a + 1; k < m; ++k) v = fmaf(-C[k * (k + 1) / 2 + a], y[k], v);
+    y[a] = v / C[a * (a + 1) / 2 + a];
+  }
+  // row j + a of the band storage holds G[j + a][j] at offset a
+  const float sc = rsqrtf(y[0]);
+  for (int a = 0; a < m; ++a) L[(size_t)(j + a) * (band + 1) + a] = y[a] * sc;
+}
+
+// 32-bit Morton key of (x, y) quantised to 16 bits each.
+uint32_t morton2(uint32_t x, uint32_t y) {
+  auto spread = [](uint32_t v) {
+    v &= 0xFFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+  };
+  return spread(x) | (spread(y) << 1);
+}
+
+// Clusters of `g` neighbouring skewers and the slot order within each: the
+// skewers are visited in Morton order of their (x, y); each unassigned one
+// seeds a cluster with its g - 1 nearest unassigned skewers among the next
+// 256 unassigned in that order.  A cluster's slots hold its records sorted by
+// z, then by skewer; each block of g n_per slots is padded with -1.
+void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>& sx,
+                          const std::vector<double>& sy, const std::vector<double>& rz,
+                          std::vector<int>& crec, int& n_blocks) {
+  const double x0 = *std::min_element(sx.begin(), sx.end());
+  const double x1 = *std::max_element(sx.begin(), sx.end());
+  const double y0 = *std::min_element(sy.begin(), sy.end());
+  const double y1 = *std::max_element(sy.begin(), sy.end());
+  const double span = std::max({x1 - x0, y1 - y0, 1e-300});
+  std::vector<uint32_t> key(n_sk);
+  for (int s = 0; s < n_sk; ++s)
+    key[s] = morton2((uint32_t)std::lround((sx[s] - x0) / span * 65535.0),
+                     (uint32_t)std::lround((sy[s] - y0) / span * 65535.0));
+  std::vector<int> order(n_sk);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+  constexpr int WINDOW = 256;
+  std::vector<char> used(n_sk, 0);
+  std::vector<std::vector<int>> clusters;
+  std::vector<std::pair<double, int>> cand;
+  for (int oi = 0; oi < n_sk; ++oi) {
+    const int s0 = order[oi];
+    if (used[s0]) continue;
+    used[s0] = 1;
+    cand.clear();
+    for (int oj = oi + 1, seen = 0; oj < n_sk && seen < WINDOW; ++oj) {
+      const int s = order[oj];
+      if (used[s]) continue;
+      ++seen;
+      const double dx = sx[s] - sx[s0], dy = sy[s] - sy[s0];
+      cand.push_back({dx * dx + dy * dy, s});
+    }
+    const int take = std::min<int>(g - 1, (int)cand.size());
+    std::partial_sort(cand.begin(), cand.begin() + take, cand.end());
+    std::vector<int> c{s0};
+    for (int k = 0; k < take; ++k) {
+      c.push_back(cand[k].second);
+      used[cand[k].second] = 1;
+    }
+    clusters.push_back(std::move(c));
+  }
+  n_blocks = (int)clusters.size();
+  const int B = g * n_per;
+  crec.assign((size_t)n_blocks * B, -1);
+  std::vector<int> recs;
+  for (int c = 0; c < n_blocks; ++c) {
+    recs.clear();
+    for (int q : clusters[c])
+      for (int k = 0; k < n_per; ++k) recs.push_back(q * n_per + k);
+    // by z, then by the skewer's rank in the cluster (stable)
+    std::stable_sort(recs.begin(), recs.end(), [&](int a, int b) { return rz[a] < rz[b]; });
+    std::copy(recs.begin(), recs.end(), crec.begin() + (size_t)c * B);
+  }
+}
+
+void build_cluster_pc(ds_operator* op, int n_sk, int n_per, int g, int band) {
+  cudaStream_t st = op->ctx->stream;
+  const int n = op->n, np = op->pix.n_pad;
+  // record coordinates from the operator's sorted copies
+  std::vector<double> hx(np), hy(np), hz(np);
+  std::vector<int> hinv(n);
+  DS_CUDA(cudaMemcpyAsync(hx.data(), op->pix.x.p, np * sizeof(double),
+                          cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(hy.data(), op->pix.y.p, np * sizeof(double),
+                          cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(hz.data(), op->pix.z.p, np * sizeof(double),
+                          cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(hinv.data(), op->inv.p, n * sizeof(int), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  std::vector<double> sx(n_sk), sy(n_sk), rz(n);
+  for (int s = 0; s < n_sk; ++s) {
+    sx[s] = hx[hinv[(size_t)s * n_per]];
+    sy[s] = hy[hinv[(size_t)s * n_per]];
+  }
+  for (int r = 0; r < n; ++r) rz[r] = hz[hinv[r]];
+  std::vector<int> crec;
+  int n_blocks = 0;
+  plan_skewer_clusters(n_sk, n_per, g, sx, sy, rz, crec, n_blocks);
+
+  std::unique_ptr<SkewerPC, SkewerPCDeleter> pc(new SkewerPC());
+  pc->n_sk = n_blocks;
+  pc->n_per = g * n_per;
+  pc->band = band;
+  const size_t n_slots = crec.size();
+  pc->crec.alloc(n_slots);
+  pc->L.alloc(n_slots * (band + 1));
+  DevBuf<int> nfb;
+  nfb.alloc(1);
+  DS_CUDA(cudaMemcpyAsync(pc->crec.p, crec.data(), n_slots * sizeof(int),
+                          cudaMemcpyHostToDevice, st));
+  DS_CUDA(cudaMemsetAsync(pc->L.p, 0, pc->L.bytes(), st));
+  DS_CUDA(cudaMemsetAsync(nfb.p, 0, sizeof(int), st));
+  k_cluster_fsai<<<(unsigned)((n_slots + 127) / 128), 128, 0, st>>>(
+      (int)n_slots, pc->n_per, band, op->kc, pc->crec.p, op->inv.p, op->pix.x.p, op->pix.y.p,
+      op->pix.z.p, op->wl.p, op->wr.p, op->e.p, pc->L.p, nfb.p);
+  DS_CHECK_LAUNCH();
+  DS_CUDA(cudaMemcpyAsync(&pc->n_fallback, nfb.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  op->pc = std::move(pc);
+}
+
+}  // namespace
+}  // namespace ds
+
+using namespace ds;
+
+extern "C" {
+
+int ds_operator_set_cluster_preconditioner(ds_operator* op, int n_skewers, int n_per,
+                                           int cluster, int band, int* n_fallback) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    if (cluster == 0) {
+      op->pc.reset();
+      return;
+    }
+    require(n_skewers > 0 && n_per > 0 && (long long)n_skewers * n_per == op->n,
+            "n_skewers x n_per must equal the operator's record count");
+    require(cluster > 0 && (long long)cluster * n_per <= 1024,
+            "cluster x n_per must be in [1, 1024]");
+    require(band >= 0 && band <= CPC_MAX_BAND, "band must be in [0, 24]");
+    build_cluster_pc(op, n_skewers, n_per, cluster, band);
+    if (n_fallback) *n_fallback = op->pc->n_fallback;
+  });
+}
+
+}  // extern "C"

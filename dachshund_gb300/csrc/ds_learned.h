@@ -56,15 +56,19 @@ struct LearnedNet {
   void adam_step(float lr);
 };
 
-// Skewer-band preconditioner M^-1 = L L^T of an operator (per skewer of
-// n_per consecutive records; L rows of bandwidth `band`, FP32).
+// Band preconditioner M^-1 = L L^T of an operator over blocks of `n_per`
+// slots (FP32 L rows of bandwidth `band`, indexed by slot): per skewer (slot
+// = record, blocks of n_per consecutive records) or per cluster of
+// neighbouring skewers (crec: the record of each slot, -1 on padding).
 bool layer_tc_usable(int M, int N, int K);
 void launch_layer_tc(int M, const float* A, const __nv_bfloat16* W, const float* bias, float* Z,
                      float* out, const float* res, float* wt, int* err, cudaStream_t st);
 
 struct SkewerPC {
-  int n_sk = 0, n_per = 0, band = 0;
-  DevBuf<float> L;  // [record][band + 1]: L[k][k - m] at m
+  int n_sk = 0, n_per = 0, band = 0;  // blocks, slots per block, bandwidth
+  DevBuf<float> L;    // [slot][band + 1]: L[k][k - m] at m
+  DevBuf<int> crec;   // record of each slot (empty: slot = record)
+  int n_fallback = 0;  // cluster factor: columns that fell back to Jacobi
 };
 
 }  // namespace ds

@@ -334,13 +334,15 @@ __global__ void __launch_bounds__(VB) k_mx_dir(int n, MixedState* st,
   }
 }
 
-// ---- skewer-band preconditioner (M^-1 = L L^T per skewer) ------------------------
-// The same reliable-update iteration with z = M^-1 r over each skewer: one CTA
-// per skewer (n_per threads, thread k = pixel k of the skewer at sorted
-// position inv[record]) updates r, forms z = L L^T r from the skewer's r in
-// shared memory, writes the skewer's r.z and |r|^2 partials, and the last CTA
-// to finish does the scalar bookkeeping of K2 (MODE 0), K6 (MODE 1) or the
-// start (MODE 2).  Padding positions belong to no skewer and stay 0.
+// ---- band preconditioner (M^-1 = L L^T per block) -------------------------------
+// The same reliable-update iteration with z = M^-1 r over each block of
+// n_per slots (a skewer, or a cluster of neighbouring skewers in z order):
+// one CTA per block (thread k = slot k, the record crec[slot] or the slot
+// itself, at sorted position inv[record]) updates r, forms z = L L^T r from
+// the block's r in shared memory, writes the block's r.z and |r|^2 partials,
+// and the last CTA to finish does the scalar bookkeeping of K2 (MODE 0), K6
+// (MODE 1) or the start (MODE 2).  Padding positions belong to no block and
+// stay 0; padding slots (record -1) hold r = 0 and write nothing.
 
 // Sum of v over the CTA (any blockDim <= 1024), valid in thread 0.
 __device__ __forceinline__ double cta_sum(double v, double* sm) {
@@ -362,7 +364,8 @@ __device__ __forceinline__ double cta_sum(double v, double* sm) {
 
 template <int MODE>
 __global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero,
-                          const int* __restrict__ inv, const float* __restrict__ L,
+                          const int* __restrict__ crec, const int* __restrict__ inv,
+                          const float* __restrict__ L,
                           double* __restrict__ x, float* __restrict__ r,
                           float* __restrict__ z, float* __restrict__ p,
                           const float* __restrict__ q, const double* __restrict__ b,
@@ -374,33 +377,38 @@ __global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero
   float* rs = reinterpret_cast<float*>(pcd + n_per);  // r of the skewer
   float* ts = rs + n_per;                              // L^T r
   const int s = blockIdx.x, k = threadIdx.x;
-  const int rec = s * n_per + k;
-  const int pos = inv[rec];
-  double rd;
-  float ri;
-  if (MODE == 0) {
-    const double alpha_d = st->alpha;
-    x[pos] = fma(alpha_d, (double)p[pos], x[pos]);
-    ri = fmaf(-(float)alpha_d, q[pos], r[pos]);
-    rd = ri;
-  } else {
-    rd = (MODE == 2 && *x_zero) ? b[pos] : r64[pos];
-    ri = (float)rd;
+  const int slot = s * n_per + k;
+  const int rec = crec ? crec[slot] : slot;
+  const int pos = rec >= 0 ? inv[rec] : -1;
+  double rd = 0.0;
+  float ri = 0.f;
+  if (pos >= 0) {
+    if (MODE == 0) {
+      const double alpha_d = st->alpha;
+      x[pos] = fma(alpha_d, (double)p[pos], x[pos]);
+      ri = fmaf(-(float)alpha_d, q[pos], r[pos]);
+      rd = ri;
+    } else {
+      rd = (MODE == 2 && *x_zero) ? b[pos] : r64[pos];
+      ri = (float)rd;
+    }
+    r[pos] = ri;
   }
-  r[pos] = ri;
   rs[k] = ri;
   __syncthreads();
   float t = 0.f;
   for (int m = 0; m <= band; ++m)
-    if (k + m < n_per) t = fmaf(L[(size_t)(rec + m) * (band + 1) + m], rs[k + m], t);
+    if (k + m < n_per) t = fmaf(L[(size_t)(slot + m) * (band + 1) + m], rs[k + m], t);
   ts[k] = t;
   __syncthreads();
-  const float* Lk = L + (size_t)rec * (band + 1);
+  const float* Lk = L + (size_t)slot * (band + 1);
   float zk = 0.f;
   for (int m = 0; m <= band; ++m)
     if (k - m >= 0) zk = fmaf(Lk[m], ts[k - m], zk);
-  z[pos] = zk;
-  if (MODE == 2) p[pos] = zk;
+  if (pos >= 0) {
+    z[pos] = zk;
+    if (MODE == 2) p[pos] = zk;
+  }
   const double srz = cta_sum((double)ri * (double)zk, pcd);
   const double srr = cta_sum(rd * rd, pcd);
   if (k == 0) {
@@ -605,8 +613,8 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     for (float* v : {f.z.p, f.r.p, f.p.p})
       DS_CUDA(cudaMemsetAsync(v, 0, np * sizeof(float), st));
     k_pc_iter<2><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-        pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p, f.p.p, nullptr,
-        op->b.p, op->r.p, pc_part, f.hist.p, f.htrue.p);
+        pc->n_per, pc->band, S, xzero, pc->crec.p, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p,
+        f.p.p, nullptr, op->b.p, op->r.p, pc_part, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   } else {
     k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p,
@@ -651,8 +659,8 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);
     if (pc) {
       k_pc_iter<0><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p, f.p.p, f.q.p,
-          nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);                    // K2
+          pc->n_per, pc->band, S, xzero, pc->crec.p, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p,
+          f.p.p, f.q.p, nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);      // K2
       DS_CHECK_LAUNCH();
     } else {
       k_mx_update<<<g, VB, 0, st>>>(np, S, op->x.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
@@ -662,8 +670,8 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     outer_residual(upd);                                                      // K5
     if (pc) {
       k_pc_iter<1><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p, f.p.p,
-          nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);           // K6
+          pc->n_per, pc->band, S, xzero, pc->crec.p, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p,
+          f.p.p, nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);    // K6
       DS_CHECK_LAUNCH();
     } else {
       k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,

@@ -189,11 +189,11 @@ __device__ __forceinline__ bool grid_sum_by_rhs(int R, double v0, double v1, dou
   sm[0][threadIdx.x] = v0;
   sm[1][threadIdx.x] = v1;
   __syncthreads();
-  if (threadIdx.x < 2 * R) {
-    const int c = threadIdx.x / R, r = threadIdx.x % R;
+  for (int idx = threadIdx.x; idx < 2 * R; idx += MVB) {  // 2 R may exceed the block
+    const int c = idx / R, r = idx % R;
     double s = 0.0;
     for (int k = r; k < MVB; k += R) s += sm[c][k];
-    part[(size_t)blockIdx.x * 2 * R + threadIdx.x] = s;
+    part[(size_t)blockIdx.x * 2 * R + idx] = s;
   }
   __threadfence();
   __syncthreads();

@@ -471,6 +471,23 @@ int ds_operator_set_skewer_preconditioner(ds_operator* op, int n_skewers,
                                           int n_per, int band,
                                           const float* L_rows);
 
+/* Installs (cluster > 0) or removes (cluster = 0) a cluster preconditioner
+ * M^-1 = G G^T of the operator's mixed-precision solves (ds_solve_mixed*),
+ * in place of Jacobi.  No reference counterpart (the reference's PCG is
+ * Jacobi, lib/wf_vector.cc:42-49,185-194).  For skewer-structured pixel
+ * sets (records skewer-contiguous, record s n_per + k is pixel k of skewer
+ * s): the skewers are grouped into clusters of `cluster` neighbours
+ * (cluster n_per <= 1024), a cluster's pixels are ordered by z, then by
+ * skewer, and G is the factorized sparse approximate inverse of each
+ * cluster's block of A with `band` sub-diagonals (0..24): column j of G
+ * solves the (band + 1)-point system A[J, J] g = e_1, J = j .. j + band.
+ * Built on the device in FP32 from the operator's coefficients; a column
+ * whose small system is not positive definite in FP32 falls back to Jacobi,
+ * and *n_fallback (may be NULL) counts them. */
+int ds_operator_set_cluster_preconditioner(ds_operator* op, int n_skewers,
+                                           int n_per, int cluster, int band,
+                                           int* n_fallback);
+
 /* ---- map projection ----------------------------------------------------- */
 typedef struct ds_map ds_map;
 

@@ -120,23 +120,29 @@ def test_dense_out_of_range_entries_use_fp64(ctx):
     mf.close()
 
 
-def test_map_covar_diag_table_multi_rhs(ctx):
-    """The table kernel's MapCovarDiag solves 16 map points per multi-RHS
-    FP64 PCG; against the oracle's per-point solves (lib/map_covar.cc:73-113):
-    the same success flags (points far from every pixel have |b| = 0 and fail
-    as the reference's early return), iteration counts within 2, sigma within
-    1e-6 relative.  37 points: two full groups and a ragged one."""
+@pytest.mark.parametrize("n_pts", [37, 300])
+def test_map_covar_diag_table_multi_rhs(ctx, n_pts):
+    """The table kernel's MapCovarDiag solves up to 256 map points per
+    multi-RHS FP64 PCG (the smallest power of two from 16 covering them);
+    against the oracle's per-point solves (lib/map_covar.cc:73-113): the same
+    success flags (points far from every pixel have |b| = 0 and fail as the
+    reference's early return), iteration counts within 2, sigma within 1e-6
+    relative.  37 points: one ragged solve of 64; 300 points: a full solve of
+    256 (more right-hand sides than a vector-kernel block has threads) and a
+    ragged one."""
     w = synth.small(12, 48, 10.0, seed=13)
     nrec = pixel_to_npixel(w.pixels)
     rng = np.random.default_rng(9)
-    pts = np.column_stack([rng.uniform(0, 10.0, 37), rng.uniform(0, 10.0, 37),
-                           rng.uniform(0, 48 * synth.DZ, 37)])
-    pts[[3, 20, 36]] = [500.0, 500.0, 5.0]  # no pixel within the table's cutoff
+    pts = np.column_stack([rng.uniform(0, 10.0, n_pts), rng.uniform(0, 10.0, n_pts),
+                           rng.uniform(0, 48 * synth.DZ, n_pts)])
+    far = [3, 20, n_pts - 1]
+    pts[far] = [500.0, 500.0, 5.0]  # no pixel within the table's cutoff
     sp = SignalCovarParams(VS, LP, LQ)
     s, iters, ok = map_covar_diag(ctx, nrec, pts, sp, PCGParams(1000, 50, 1e-8))
     so, io, oko = oracle.map_covar_diag(nrec, pts, VS, LP, LQ, 1000, 50, 1e-8, exact=False)
     assert np.array_equal(ok.astype(bool), np.asarray(oko).astype(bool))
-    assert not ok[[3, 20, 36]].any() and np.all(s[[3, 20, 36]] == 0.0)
+    assert not ok[far].any() and np.all(s[far] == 0.0)
     good = np.asarray(oko).astype(bool)
+    assert good.sum() == n_pts - 3
     assert np.all(np.abs(iters[good] - np.asarray(io)[good]) <= 2)
     assert rel(s[good], np.asarray(so)[good]) < 1e-6
