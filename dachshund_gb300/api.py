@@ -273,6 +273,28 @@ class _WFVector:
             "ds_operator_set_cluster_preconditioner")
         return nf.value
 
+    def set_skewer_grid(self, n_skewers: int, n_per: int):
+        """Installs (n_skewers > 0) or removes (0) the structured FP64
+        operator for skewers on one uniform z grid (records skewer-contiguous,
+        n_skewers x n_per); while installed, solve_mixed's FP64-accurate outer
+        residual uses it."""
+        self.ctx.check(self._lib.ds_operator_set_skewer_grid(self.handle, int(n_skewers),
+                                                             int(n_per)),
+                       "ds_operator_set_skewer_grid")
+
+    def skewer_product(self, v, residual: bool = False):
+        """A v (or b - A v) with the structured operator (host in, host out)."""
+        import torch
+
+        vt = torch.as_tensor(np.ascontiguousarray(v, dtype=np.float64), device="cuda")
+        out = torch.empty_like(vt)
+        torch.cuda.synchronize()
+        self.ctx.check(self._lib.ds_operator_skewer_product_dev(
+            self.handle, int(bool(residual)), C.c_void_p(vt.data_ptr()),
+            C.c_void_p(out.data_ptr())), "ds_operator_skewer_product_dev")
+        self.ctx.synchronize()
+        return out.cpu().numpy()
+
     def info(self) -> dict:
         inf = _lib.OperatorInfoC()
         self.ctx.check(self._lib.ds_operator_get_info(self.handle, C.byref(inf)), "info")

@@ -27,9 +27,11 @@ namespace ds {
 struct OpF32;   // ds_f32.h
 struct MapF32;  // ds_f32.h
 struct SkewerPC;  // ds_learned.h
+struct SkewerGrid;  // ds_skewer.h
 struct OpF32Deleter { void operator()(OpF32* p) const; };
 struct MapF32Deleter { void operator()(MapF32* p) const; };
 struct SkewerPCDeleter { void operator()(SkewerPC* p) const; };
+struct SkewerGridDeleter { void operator()(SkewerGrid* p) const; };
 
 constexpr int TILE = 128;        // points per tile (rows per CTA in the FP64 kernels)
 constexpr int SUBTILE = 32;      // points per sub-tile (one warp's rows; culled per warp)
@@ -337,6 +339,8 @@ struct ds_operator {
   int inner_variant = 0;     // inner matvec of the mixed form (InnerVariant)
   // skewer-band preconditioner of the mixed form (null: Jacobi)
   std::unique_ptr<ds::SkewerPC, ds::SkewerPCDeleter> pc;
+  // structured operator for skewers on a shared z grid (null: pair kernels)
+  std::unique_ptr<ds::SkewerGrid, ds::SkewerGridDeleter> sgrid;
 };
 
 struct ds_map {

@@ -1,0 +1,37 @@
+// Structured form of the exact-kernel operator for skewers on a shared z grid
+// (skewer_op.cu): the pixels are n_sk skewers of n_per records each (record
+// s n_per + k is pixel k of skewer s), every skewer at its own (x, y) and all
+// on the same z values z_0 < ... < z_{n_per - 1}, uniformly spaced.
+#pragma once
+
+#include "ds_internal.cuh"
+
+namespace ds {
+
+// Skewer pairs (a, b) within one cutoff, CSR by a (b ascending, a itself
+// included): the perpendicular factor var_s exp(-c_perp |dxy_ab|^2) and the
+// number of z taps on each side, L_ab = max m with
+// c_perp |dxy_ab|^2 + c_para (z_m - z_0)^2 < cut.
+struct SkewerNbrs {
+  double cut = 0.0;
+  int lmax = 0;        // largest L_ab
+  long long n_terms = 0;  // sum over pairs of n_per (the apply kernel's FMAs)
+  DevBuf<int> ptr, idx, lev;
+  DevBuf<double> p64;
+};
+
+struct SkewerGrid {
+  int n_sk = 0, n_per = 0;
+  double dz = 0.0;
+  DevBuf<double> taps64;  // exp(-c_para (z_m - z_0)^2), m < n_per
+  SkewerNbrs outer;       // the operator's own cutoff (FP64-accurate residual)
+  DevBuf<double> V64;     // (lmax + 1) x n: z-convolved column values per level
+};
+
+// r = b - A v (residual) or A v (product) on vectors in the operator's
+// sorted order, with the structured FP64 operator; the launch returns at
+// once when *skip != 0 (skip may be null).
+void skewer_apply_f64(ds_operator* op, bool residual, const double* v, double* out,
+                      const int* skip, cudaStream_t st);
+
+}  // namespace ds

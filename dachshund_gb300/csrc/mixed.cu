@@ -23,6 +23,7 @@
 #include "ds_device.cuh"
 #include "ds_f32.h"
 #include "ds_learned.h"
+#include "ds_skewer.h"
 #include "ds_ops.h"
 
 namespace ds {
@@ -597,7 +598,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   PairArgs resid = op_pair_args(op, op->x.p, op->r.p);
   resid.skip_flag = &S->init_skip;
   auto outer_residual = [&](const PairArgs& pa) {
-    if (f.use_ff)
+    if (op->sgrid)
+      skewer_apply_f64(op, true, pa.v, pa.out, pa.skip_flag, st);
+    else if (f.use_ff)
       launch_pair_ff_resid(op->kc, pa, f.ffd.view, st);
     else
       launch_pair_f64(op->kc, EPI_RESIDUAL, pa, st);

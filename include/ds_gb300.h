@@ -488,6 +488,24 @@ int ds_operator_set_cluster_preconditioner(ds_operator* op, int n_skewers,
                                            int n_per, int cluster, int band,
                                            int* n_fallback);
 
+/* Structured form of the exact-kernel operator (no reference counterpart;
+ * the operator of lib/wf_vector.cc:196-251 evaluated in another order), for
+ * skewer-structured pixel sets whose skewers all sample the same uniform z
+ * grid (record s n_per + k = pixel k of skewer s; every skewer at one (x, y);
+ * the same z values in every skewer).  The exact kernel then factorises into
+ * a perpendicular factor per skewer pair times a Toeplitz z factor, so a
+ * product costs one short z convolution per skewer and one FP64 FMA per
+ * (skewer pair, pixel) instead of an exponential per pixel pair.  Installs
+ * (n_skewers > 0) or removes (0) it; while installed the FP64-accurate outer
+ * residual of the mixed-precision solves (ds_solve_mixed*) uses it.
+ * DS_ERR_ARG when the records do not have that structure or the kernel is
+ * the table kernel. */
+int ds_operator_set_skewer_grid(ds_operator* op, int n_skewers, int n_per);
+/* out = A v (residual = 0) or b - A v (residual != 0) with the structured
+ * operator; v, out: n doubles in the caller's record order, device memory. */
+int ds_operator_skewer_product_dev(ds_operator* op, int residual,
+                                   const double* v, double* out);
+
 /* ---- map projection ----------------------------------------------------- */
 typedef struct ds_map ds_map;
 
