@@ -31,6 +31,7 @@ DS_TABLE_N = 200
 DS_INNER_AUTO = 0
 DS_INNER_CUDA_CORE = 1
 DS_INNER_TENSOR = 2
+DS_INNER_STRUCTURED = 3
 DS_BATCH_AUTO = -1
 DS_BATCH_CUDA_CORE = 0
 DS_BATCH_TENSOR = 1

@@ -252,11 +252,13 @@ class _WFVector:
         return {1: "float_pair", 2: "fp64"}[v.value]
 
     def set_inner_matvec(self, variant: str = "auto"):
-        """Inner matvec of solve_mixed: "auto" / "cuda_core" (the CUDA-core
-        kernel, the faster one) or "tensor" (pair exponents on the tensor
-        cores where the expanded form applies)."""
+        """Inner matvec of solve_mixed: "cuda_core" (the CUDA-core pair
+        kernel), "tensor" (pair exponents on the tensor cores where the
+        expanded form applies), "structured" (the FP32 structured operator of
+        set_skewer_grid) or "auto" (structured when a skewer grid is
+        installed, else the CUDA-core pair kernel)."""
         v = {"auto": _lib.DS_INNER_AUTO, "cuda_core": _lib.DS_INNER_CUDA_CORE,
-             "tensor": _lib.DS_INNER_TENSOR}[variant]
+             "tensor": _lib.DS_INNER_TENSOR, "structured": _lib.DS_INNER_STRUCTURED}[variant]
         self.ctx.check(self._lib.ds_operator_set_inner_matvec(self.handle, v),
                        "ds_operator_set_inner_matvec")
 

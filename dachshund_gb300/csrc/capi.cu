@@ -754,7 +754,8 @@ int ds_operator_get_dense_arith(ds_operator* op, int* arith) {
 int ds_operator_set_inner_matvec(ds_operator* op, int variant) {
   if (!op) return DS_ERR_ARG;
   return guarded(op->ctx, [&] {
-    require(variant >= DS_INNER_AUTO && variant <= DS_INNER_TENSOR, "bad inner-matvec variant");
+    require(variant >= DS_INNER_AUTO && variant <= DS_INNER_STRUCTURED,
+            "bad inner-matvec variant");
     op->inner_variant = variant;
   });
 }

@@ -63,7 +63,7 @@ bool pair_tc_usable(int formula, int epi, const F32Args& a);
 void launch_pair_tc(const F32Args& a, cudaStream_t st);
 
 // Inner-matvec kernel of the mixed-precision form (ds_operator_set_inner_matvec).
-enum InnerVariant { INNER_AUTO = 0, INNER_CUDA_CORE = 1, INNER_TENSOR = 2 };
+enum InnerVariant { INNER_AUTO = 0, INNER_CUDA_CORE = 1, INNER_TENSOR = 2, INNER_STRUCTURED = 3 };
 
 // Float-pair coordinates for the FP64-accurate residual on the FP32 pipe
 // (pair_ff.cu): per pixel its coordinates scaled by sqrt(c_perp),

@@ -18,6 +18,7 @@ struct SkewerNbrs {
   long long n_terms = 0;  // sum over pairs of n_per (the apply kernel's FMAs)
   DevBuf<int> ptr, idx, lev;
   DevBuf<double> p64;
+  DevBuf<float> p32;   // the factor in FP32 (inner lists)
 };
 
 struct SkewerGrid {
@@ -26,7 +27,21 @@ struct SkewerGrid {
   DevBuf<double> taps64;  // exp(-c_para (z_m - z_0)^2), m < n_per
   SkewerNbrs outer;       // the operator's own cutoff (FP64-accurate residual)
   DevBuf<double> V64;     // (lmax + 1) x n: z-convolved column values per level
+  // the FP32 inner operator of the mixed solve (its cutoff, built on demand)
+  std::vector<double> sx, sy, zd;  // skewer (x, y), z_m - z_0
+  SkewerNbrs inner;
+  DevBuf<float> taps32, V32;
+  DevBuf<double> dot_part;  // per-skewer p.q partials
 };
+
+// The FP32 inner product of the mixed solve, q = A32 p on FP32 vectors in
+// sorted order, with the PCG step's p.q and alpha = *num / p.q (written by
+// the last CTA, counter reset to 0).  ensure_skewer_inner builds the lists
+// at the inner cutoff once.
+void ensure_skewer_inner(ds_operator* op, double inner_cut);
+void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int* counter,
+                        const double* num, double* alpha_out, double* den_out,
+                        const int* skip, cudaStream_t st);
 
 // r = b - A v (residual) or A v (product) on vectors in the operator's
 // sorted order, with the structured FP64 operator; the launch returns at

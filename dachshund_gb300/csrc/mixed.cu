@@ -584,6 +584,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   const int g = vgrid(np);
   // r64 = b - A x0: nothing when x0 == 0 (then r64 = b); else first with the
   // FP32 operator, then FP64-accurate only when that one is near tol.
+  // the structured FP64 residual writes the records' positions only: the
+  // padding of r64 is cleared here, before anything writes r64
+  if (op->sgrid) DS_CUDA(cudaMemsetAsync(op->r.p, 0, np * sizeof(double), st));
   k_is_zero<<<g, VB, 0, st>>>(np, op->x.p, xzero);
   DS_CHECK_LAUNCH();
   k_x_to_f32<<<g, VB, 0, st>>>(np, xzero, op->x.p, f.p.p);
@@ -649,6 +652,14 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // T / S buffers in the 512 TMEM columns).
   const bool use_tc =
       op->inner_variant == INNER_TENSOR && pair_tc_usable(f.formula, EPI_PRODUCT, prod);
+  // the structured inner operator (skewers on one z grid): q is written on
+  // the records' positions only, so its padding is cleared once here
+  const bool use_sg = op->sgrid && (op->inner_variant == INNER_AUTO ||
+                                    op->inner_variant == INNER_STRUCTURED);
+  if (use_sg) {
+    ensure_skewer_inner(op, f.inner_cut);
+    DS_CUDA(cudaMemsetAsync(f.q.p, 0, np * sizeof(float), st));
+  }
 
   constexpr int CHECK = 8;
   constexpr int NSLOT = 64;
@@ -656,7 +667,10 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   int issued = 0, waited = 0;
   for (int it = 1; it <= max_iter; ++it) {
-    if (use_tc)
+    if (use_sg)
+      skewer_product_f32(op, prod.v, prod.out, prod.counter, prod.num, prod.alpha_out,
+                         prod.den_out, prod.skip_flag, st);                  // K1
+    else if (use_tc)
       launch_pair_tc(prod, st);                                               // K1
     else
       launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);

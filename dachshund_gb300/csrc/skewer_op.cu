@@ -84,12 +84,96 @@ __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
     acc0 = fma(nb_p[q], v0, acc0);
     acc1 = fma(nb_p[q + 1], v1, acc1);
   }
-  if (q < q1) acc0 = fma(nb_p[q], V[(size_t)nb_lev[q] * n + (size_t)nb_idx[q] * n_per + k], acc0);
+  if (q < q1)
+    acc0 = fma(nb_p[q], V[(size_t)nb_lev[q] * n + (size_t)nb_idx[q] * n_per + k], acc0);
   const size_t r = (size_t)a * n_per + k;
   const int p = pos[r];
   const double y = fma(wl[p], acc0 + acc1, e[p] * v[p]);
   out[p] = RESID ? bvec[p] - y : y;
   if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
+}
+
+// FP32 levels of the inner operator: u = wr p (FP32 vectors, sorted order).
+__global__ void k_sg32_levels(int n_per, int lmax, size_t n, const int* __restrict__ pos,
+                              const double* __restrict__ wr, const float* __restrict__ p,
+                              const float* __restrict__ taps, float* __restrict__ V,
+                              const int* skip) {
+  if (skip && *skip) return;
+  extern __shared__ float sf[];
+  const int k = threadIdx.x;
+  const size_t r = (size_t)blockIdx.x * n_per + k;
+  const int ps = pos[r];
+  const float u = (float)wr[ps] * p[ps];
+  sf[k] = u;
+  __syncthreads();
+  float acc = u;
+  V[r] = acc;
+  for (int L = 1; L <= lmax; ++L) {
+    float s = 0.f;
+    if (k + L < n_per) s = sf[k + L];
+    if (k - L >= 0) s += sf[k - L];
+    acc = fmaf(taps[L], s, acc);
+    V[(size_t)L * n + r] = acc;
+  }
+}
+
+// Sum over the CTA (any blockDim <= 1024) in a fixed order; valid in thread 0.
+__device__ __forceinline__ double sg_cta_sum(double v, double* sm) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sm[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < (int)(blockDim.x + 31) / 32; ++k) s += sm[k];
+  return s;
+}
+
+// q = A32 p for one skewer per CTA, with the fused p.q of the CG step: one
+// partial per skewer, summed in skewer order by the last CTA, which also
+// forms alpha = num / p.q.
+__global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
+                             const int* __restrict__ nb_idx, const int* __restrict__ nb_lev,
+                             const float* __restrict__ nb_p, const float* __restrict__ V,
+                             const int* __restrict__ pos, const double* __restrict__ wl,
+                             const double* __restrict__ e, const float* __restrict__ p,
+                             float* __restrict__ q, double* __restrict__ part,
+                             unsigned int* counter, const double* num, double* alpha_out,
+                             double* den_out, const int* skip,
+                             unsigned long long* prof_terms) {
+  if (skip && *skip) return;
+  __shared__ double sm[32];
+  const int a = blockIdx.x, k = threadIdx.x;
+  const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
+  float acc0 = 0.f, acc1 = 0.f;
+  int j = q0;
+  for (; j + 1 < q1; j += 2) {
+    const float v0 = V[(size_t)nb_lev[j] * n + (size_t)nb_idx[j] * n_per + k];
+    const float v1 = V[(size_t)nb_lev[j + 1] * n + (size_t)nb_idx[j + 1] * n_per + k];
+    acc0 = fmaf(nb_p[j], v0, acc0);
+    acc1 = fmaf(nb_p[j + 1], v1, acc1);
+  }
+  if (j < q1)
+    acc0 = fmaf(nb_p[j], V[(size_t)nb_lev[j] * n + (size_t)nb_idx[j] * n_per + k], acc0);
+  const size_t r = (size_t)a * n_per + k;
+  const int ps = pos[r];
+  const float pv = p[ps];
+  const float qv = fmaf((float)wl[ps], acc0 + acc1, (float)e[ps] * pv);
+  q[ps] = qv;
+  if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
+  if (!part) return;
+  const double s = sg_cta_sum((double)pv * (double)qv, sm);
+  if (k == 0) part[a] = s;
+  if (!last_block_arrive(counter)) return;
+  double t = 0.0;
+  for (int c = k; c < (int)gridDim.x; c += blockDim.x) t += __ldcg(part + c);
+  const double pq = sg_cta_sum(t, sm);
+  if (k == 0) {
+    *den_out = pq;
+    *alpha_out = *num / pq;
+    *counter = 0;
+  }
 }
 
 // Skewer pairs within `cut` (cell lists of side sqrt(cut / c_perp)).
@@ -150,6 +234,10 @@ void build_nbrs(SkewerNbrs& nb, const std::vector<double>& sx, const std::vector
                           st));
   DS_CUDA(cudaMemcpyAsync(nb.p64.p, p64.data(), p64.size() * sizeof(double),
                           cudaMemcpyHostToDevice, st));
+  std::vector<float> p32(p64.begin(), p64.end());
+  nb.p32.alloc(std::max<size_t>(1, p32.size()));
+  DS_CUDA(cudaMemcpyAsync(nb.p32.p, p32.data(), p32.size() * sizeof(float),
+                          cudaMemcpyHostToDevice, st));
   DS_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
 }
 
@@ -207,6 +295,14 @@ void build_skewer_grid(ds_operator* op, int n_sk, int n_per) {
                           cudaMemcpyHostToDevice, st));
   build_nbrs(g->outer, sx, sy, zd, op->kc, op->kc.exact_cut, n_per, st);
   g->V64.alloc((size_t)(g->outer.lmax + 1) * n);
+  std::vector<float> t32(taps.begin(), taps.end());
+  g->taps32.alloc(n_per);
+  DS_CUDA(cudaMemcpyAsync(g->taps32.p, t32.data(), n_per * sizeof(float),
+                          cudaMemcpyHostToDevice, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  g->sx = std::move(sx);
+  g->sy = std::move(sy);
+  g->zd = std::move(zd);
   op->sgrid = std::move(g);
 }
 
@@ -238,6 +334,38 @@ void skewer_apply_f64(ds_operator* op, bool residual, const double* v, double* o
                                                   skip, prof_terms);
   DS_CHECK_LAUNCH();
   if (ev) pr.end(st, ev, 0);
+}
+
+void ensure_skewer_inner(ds_operator* op, double inner_cut) {
+  SkewerGrid& g = *op->sgrid;
+  if (g.inner.ptr.p && g.inner.cut == inner_cut) return;
+  build_nbrs(g.inner, g.sx, g.sy, g.zd, op->kc, inner_cut, g.n_per, op->ctx->stream);
+  g.V32.alloc((size_t)(g.inner.lmax + 1) * op->n);
+  g.dot_part.alloc(g.n_sk);
+}
+
+void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int* counter,
+                        const double* num, double* alpha_out, double* den_out,
+                        const int* skip, cudaStream_t st) {
+  SkewerGrid& g = *op->sgrid;
+  const size_t n = (size_t)op->n;
+  Profiler& pr = op->ctx->prof;
+  cudaEvent_t ev = nullptr;
+  unsigned long long* prof_terms = nullptr;
+  if (pr.enabled) {
+    prof_terms = pr.d_pairs + 1;  // kind 1: FP32 products
+    pr.begin(st, &ev);
+  }
+  k_sg32_levels<<<g.n_sk, g.n_per, g.n_per * sizeof(float), st>>>(
+      g.n_per, g.inner.lmax, n, op->inv.p, op->wr.p, p, g.taps32.p, g.V32.p, skip);
+  DS_CHECK_LAUNCH();
+  k_sg32_apply<<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.inner.ptr.p, g.inner.idx.p,
+                                           g.inner.lev.p, g.inner.p32.p, g.V32.p, op->inv.p,
+                                           op->wl.p, op->e.p, p, q,
+                                           counter ? g.dot_part.p : nullptr, counter, num,
+                                           alpha_out, den_out, skip, prof_terms);
+  DS_CHECK_LAUNCH();
+  if (ev) pr.end(st, ev, 1);
 }
 
 }  // namespace ds

@@ -215,12 +215,16 @@ int ds_operator_set_dense_arith(ds_operator* op, int arith);
 int ds_operator_get_dense_arith(ds_operator* op, int* arith);
 
 /* Inner matvec of the mixed-precision form (no reference counterpart; the
- * reference has no FP32 path).  DS_INNER_AUTO and DS_INNER_CUDA_CORE use the
- * CUDA-core kernel (4 FMA lanes + 1 ex2 per pair, the faster one on GB300);
- * DS_INNER_TENSOR uses the tensor-core kernel (pair exponents by tcgen05
- * TF32 MMAs, one ex2 per pair) where the operator's tiles allow the expanded
- * exponent form, else the CUDA-core one. */
-enum { DS_INNER_AUTO = 0, DS_INNER_CUDA_CORE = 1, DS_INNER_TENSOR = 2 };
+ * reference has no FP32 path).  DS_INNER_CUDA_CORE uses the CUDA-core pair
+ * kernel (4 FMA lanes + 1 ex2 per pair); DS_INNER_TENSOR the tensor-core
+ * pair kernel (pair exponents by tcgen05 TF32 MMAs, one ex2 per pair) where
+ * the operator's tiles allow the expanded exponent form, else the CUDA-core
+ * one; DS_INNER_STRUCTURED the FP32 structured operator (perpendicular factor
+ * per skewer pair x Toeplitz z taps) of ds_operator_set_skewer_grid, else the
+ * CUDA-core one.  DS_INNER_AUTO: the structured operator when a skewer grid
+ * is installed, else the CUDA-core pair kernel. */
+enum { DS_INNER_AUTO = 0, DS_INNER_CUDA_CORE = 1, DS_INNER_TENSOR = 2,
+       DS_INNER_STRUCTURED = 3 };
 int ds_operator_set_inner_matvec(ds_operator* op, int variant);
 
 /* ---- PCG ---------------------------------------------------------------- */

@@ -8,9 +8,10 @@ kernel of lib/signal_covar.h:79-86).
   sum) and with the pair-kernel FP64 product, in both forms.
 * Records that are not skewers on one uniform grid, and the table kernel,
   are refused with DS_ERR_ARG.
-* The mixed-precision solve with the structured outer residual stops on the
-  FP64 true residual <= tol |b| (checked with the pair-kernel operator) and
-  its solution is within 1e-6 of the FP64 oracle's.
+* The mixed-precision solve with the structured FP32 inner product and FP64
+  outer residual stops on the FP64 true residual <= tol |b| (checked with
+  the pair-kernel operator) and its solution is within 1e-6 of the FP64
+  oracle's and of the pair-kernel solve's.
 """
 import numpy as np
 import pytest
@@ -76,14 +77,19 @@ def test_refused_without_grid_structure(ctx):
 
 
 @pytest.mark.parametrize("form", ["w", "sn"])
-def test_mixed_solve_with_structured_residual(ctx, form):
-    n_sk, n_per = 32, 64
-    w = synth.small(n_sk, n_per, 12.0, seed=17)
+@pytest.mark.parametrize("n_sk,n_per,cluster", [(32, 64, 4), (10, 50, 0)])
+def test_mixed_solve_structured(ctx, form, n_sk, n_per, cluster):
+    """The structured FP32 inner product and FP64 outer residual (with the
+    cluster preconditioner, and with Jacobi on a record count that leaves
+    padding in the last tile): FP64 true residual <= tol |b|, solution within
+    1e-6 of the oracle's, and within 1e-6 of the pair-kernel solve."""
+    w = synth.small(n_sk, n_per, 12.0 * np.sqrt(n_sk / 32), seed=17)
     op, rec = make(ctx, form, w.pixels)
     mp = MixedParams(tol=1e-8)
+    if cluster:
+        op.set_cluster_preconditioner(n_sk, n_per, cluster=cluster, band=16)
     x0, r0 = op.solve_mixed(mp)
     op.set_skewer_grid(n_sk, n_per)
-    op.set_cluster_preconditioner(n_sk, n_per, cluster=4, band=16)
     x, res = op.solve_mixed(mp)
     assert res.success and r0.success and res.n_outer >= 1
     y = x / rec[:, 3] if form == "w" else x
@@ -91,5 +97,12 @@ def test_mixed_solve_with_structured_residual(ctx, form):
     xo, ok, _, _ = oracle.solve_pcg(form, rec, VS, LP, LQ, 3000, 50, 1e-10, exact=True)
     assert ok
     assert np.max(np.abs(x - xo)) / np.max(np.abs(xo)) < 1e-6
+    assert np.max(np.abs(x - x0)) / np.max(np.abs(x0)) < 1e-6
+    assert abs(res.num_iters - r0.num_iters) <= max(3, r0.num_iters // 10)
+    # the pair kernel as inner matvec, structured outer residual
+    op.set_inner_matvec("cuda_core")
+    x1, r1 = op.solve_mixed(mp)
+    assert r1.success and np.max(np.abs(x1 - xo)) / np.max(np.abs(xo)) < 1e-6
+    op.set_inner_matvec("auto")
     op.set_skewer_grid(0, 0)
     op.close()
