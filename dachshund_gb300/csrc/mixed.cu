@@ -661,12 +661,11 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     DS_CUDA(cudaMemsetAsync(f.q.p, 0, np * sizeof(float), st));
   }
 
-  constexpr int CHECK = 8;
-  constexpr int NSLOT = 64;
-  cudaEvent_t evs[NSLOT];
-  for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  int issued = 0, waited = 0;
-  for (int it = 1; it <= max_iter; ++it) {
+  // One iteration: K1 (q = A32 p, p.q, alpha), K2 (x, r updates, z = M^-1 r,
+  // r.z, update test), K5 (FP64-accurate residual when an update is due),
+  // K6 (the update), K7 (p = z + beta p).  Every kernel returns at once once
+  // the solve is done, so iterations launched past the end change nothing.
+  auto iteration = [&]() {
     if (use_sg)
       skewer_product_f32(op, prod.v, prod.out, prod.counter, prod.num, prod.alpha_out,
                          prod.den_out, prod.skip_flag, st);                  // K1
@@ -697,7 +696,44 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     }
     k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K7
     DS_CHECK_LAUNCH();
-    if (it % CHECK == 0) {
+  };
+
+  // The host reads the done flag every CHECK iterations, two reads behind,
+  // so the stream never drains.  Without profiling (and with the CUDA-core or
+  // structured inner product) the CHECK iterations are one CUDA graph,
+  // captured once per solve and replayed: 1 launch instead of ~7 CHECK.
+  constexpr int CHECK = 8;
+  constexpr int NSLOT = 64;
+  cudaEvent_t evs[NSLOT];
+  for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaGraphExec_t gexec = nullptr;
+  long long per_graph = 0;
+  if (!op->ctx->prof.enabled && !use_tc && max_iter > 0) {
+    const long long l0 = launch_counter();
+    cudaGraph_t graph = nullptr;
+    DS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int k = 0; k < CHECK; ++k) iteration();
+    } catch (...) {
+      cudaStreamEndCapture(st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    DS_CUDA(cudaStreamEndCapture(st, &graph));
+    const cudaError_t inst = cudaGraphInstantiate(&gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    DS_CUDA(inst);
+    per_graph = launch_counter() - l0;
+  }
+  int issued = 0, waited = 0, replays = 0;
+  for (int it = 1; it <= max_iter; it += gexec ? CHECK : 1) {
+    if (gexec) {
+      DS_CUDA(cudaGraphLaunch(gexec, st));
+      ++replays;
+    } else {
+      iteration();
+    }
+    if (gexec || it % CHECK == 0) {
       const int slot = issued % NSLOT;
       DS_CUDA(cudaMemcpyAsync(&op->h_flag.p[slot], &S->done, sizeof(int),
                               cudaMemcpyDeviceToHost, st));
@@ -710,6 +746,11 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
         if (op->h_flag.p[ws]) break;
       }
     }
+  }
+  if (gexec) {
+    // the capture counted one graph's launches; each further replay launches them again
+    launch_counter() += (long long)std::max(replays - 1, 0) * per_graph;
+    cudaGraphExecDestroy(gexec);
   }
   DS_CUDA(cudaEventRecord(ev1, st));
   DS_CUDA(cudaMemcpyAsync(&h, S, sizeof(h), cudaMemcpyDeviceToHost, st));

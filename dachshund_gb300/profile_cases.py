@@ -7,6 +7,12 @@ leaves the GPU's clocks as they are):
                  arithmetic (k_pair_ff_resid), random x
   f32_matvec     one mixed-precision solve of the 262,144-pixel system
                  (k_pair_f32 launches, one per iteration)
+  chosen_step    one step of the benchmark's chosen form on the 262,144-pixel
+                 system, after one untimed warm-up step: cluster
+                 preconditioner and skewer grid installed, the mixed solve
+                 (k_sg32_levels + k_sg32_apply, k_pc_iter, k_mx_dir, and
+                 k_sg_levels + k_sg_apply for the FP64 residuals) and the
+                 80 x 80 x 512 FP32 map (k_pair_f32 MAP)
   tc_matvec      one batched FP32 product of 64 chunks x 64 RHS with the
                  tensor-core variant (k_pack_panels + k_batch_mv_tc)
   tc_inner       one mixed-precision solve of the 262,144-pixel system with
@@ -38,7 +44,28 @@ def main(argv=None):
 
     ctx = Context(0)
     sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
-    if case in ("ff_residual", "f32_matvec", "tc_inner", "plain_matvec"):
+    if case == "chosen_step":
+        from dachshund_gb300 import MapGrid
+
+        w = synth.wf262144(0)
+        rec = pixel_to_wpixel(w.pixels)
+        op = WFVectorW(ctx, rec, sp)
+        op.set_cluster_preconditioner(w.n_skewers, w.pix_per_skewer, 4, 16)
+        op.set_skewer_grid(w.n_skewers, w.pix_per_skewer)
+        grid = MapGrid(ctx, synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny,
+                                                     w.map_nz))
+        x = torch.zeros(w.n, dtype=torch.float64, device="cuda")
+        m = torch.empty(w.n_map, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            torch.cuda.synchronize()
+            x.zero_()
+            torch.cuda.synchronize()
+            res = op.solve_mixed_dev(MixedParams(max_iter=3000, tol=1e-8), x)
+            grid.product_f32_dev(op, x, m)
+            ctx.synchronize()
+        print(case, "iters", res.num_iters, "updates", res.n_outer)
+        grid.close()
+    elif case in ("ff_residual", "f32_matvec", "tc_inner", "plain_matvec"):
         w = synth.wf262144(0)
         rec = pixel_to_wpixel(w.pixels)
         op = WFVectorW(ctx, rec, sp)
