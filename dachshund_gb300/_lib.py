@@ -200,6 +200,7 @@ SIGNATURES = {
     "ds_operator_set_skewer_preconditioner": (_i, [_vp, _i, _i, _i, _vp]),
     "ds_operator_set_cluster_preconditioner": (_i, [_vp, _i, _i, _i, _i, _vp]),
     "ds_operator_set_skewer_grid": (_i, [_vp, _i, _i]),
+    "ds_map_set_column_grid": (_i, [_vp, _i, _i]),
     "ds_operator_skewer_product_dev": (_i, [_vp, _i, _vp, _vp]),
     "ds_map_create": (_i, [_vp, _i, _dp, C.POINTER(_vp)]),
     "ds_map_destroy": (None, [_vp]),

@@ -538,6 +538,14 @@ class MapGrid:
         self.handle = h
         ctx._adopt(self)
 
+    def set_column_grid(self, n_columns: int, nz: int):
+        """Declares the points a grid of n_columns columns of nz points (point
+        c nz + j at column c's (x, y) and the j-th z), the layout of
+        uniform_map_coords; with an operator that has a skewer grid,
+        product_f32 is then the structured FP64 map.  0 removes it."""
+        self.ctx.check(self._lib.ds_map_set_column_grid(self.handle, int(n_columns), int(nz)),
+                       "ds_map_set_column_grid")
+
     def product(self, op: _WFVector, x):
         """smp_product with the operator's pixels and kernel."""
         x = _f64(x, op.n, "x")

@@ -87,7 +87,7 @@ __global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc
   if (!ok) {
     const int p0 = pos[0];
     const double a00 = wl[p0] * kc.var_s * wr[p0] + e[p0];
-    L[(size_t)j * (band + 1)] = (float)(1.0 / sqrt(a00));
+    L[j] = (float)(1.0 / sqrt(a00));  // plane 0: the diagonal
     atomicAdd(n_fallback, 1);
     return;
   }
@@ -104,9 +104,9 @@ __global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc
     for (int k = a + 1; k < m; ++k) v = fmaf(-C[k * (k + 1) / 2 + a], y[k], v);
     y[a] = v / C[a * (a + 1) / 2 + a];
   }
-  // row j + a of the band storage holds G[j + a][j] at offset a
+  // G[j + a][j] is plane a at slot j + a
   const float sc = rsqrtf(y[0]);
-  for (int a = 0; a < m; ++a) L[(size_t)(j + a) * (band + 1) + a] = y[a] * sc;
+  for (int a = 0; a < m; ++a) L[(size_t)a * n_slots + (j + a)] = y[a] * sc;
 }
 
 // 32-bit Morton key of (x, y) quantised to 16 bits each.

@@ -28,10 +28,12 @@ struct OpF32;   // ds_f32.h
 struct MapF32;  // ds_f32.h
 struct SkewerPC;  // ds_learned.h
 struct SkewerGrid;  // ds_skewer.h
+struct MapColumns;  // ds_skewer.h
 struct OpF32Deleter { void operator()(OpF32* p) const; };
 struct MapF32Deleter { void operator()(MapF32* p) const; };
 struct SkewerPCDeleter { void operator()(SkewerPC* p) const; };
 struct SkewerGridDeleter { void operator()(SkewerGrid* p) const; };
+struct MapColumnsDeleter { void operator()(MapColumns* p) const; };
 
 constexpr int TILE = 128;        // points per tile (rows per CTA in the FP64 kernels)
 constexpr int SUBTILE = 32;      // points per sub-tile (one warp's rows; culled per warp)
@@ -352,4 +354,6 @@ struct ds_map {
   ds::PairList pairs;
   ds::DevBuf<double> out_dev;  // caller-order map staging
   std::unique_ptr<ds::MapF32, ds::MapF32Deleter> f32;  // FP32 map data (lazy)
+  // map points declared a column grid (null: none), for the structured map
+  std::unique_ptr<ds::MapColumns, ds::MapColumnsDeleter> cols;
 };

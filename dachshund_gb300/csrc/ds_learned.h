@@ -66,7 +66,7 @@ void launch_layer_tc(int M, const float* A, const __nv_bfloat16* W, const float*
 
 struct SkewerPC {
   int n_sk = 0, n_per = 0, band = 0;  // blocks, slots per block, bandwidth
-  DevBuf<float> L;    // [slot][band + 1]: L[k][k - m] at m
+  DevBuf<float> L;    // band + 1 planes of n_sk n_per slots: L[k][k - m] at plane m
   DevBuf<int> crec;   // record of each slot (empty: slot = record)
   int n_fallback = 0;  // cluster factor: columns that fell back to Jacobi
 };

@@ -23,7 +23,7 @@ struct SkewerNbrs {
 
 struct SkewerGrid {
   int n_sk = 0, n_per = 0;
-  double dz = 0.0;
+  double z0 = 0.0, dz = 0.0;  // the pixels' z grid: z_k = z0 + zd[k]
   DevBuf<double> taps64;  // exp(-c_para (z_m - z_0)^2), m < n_per
   SkewerNbrs outer;       // the operator's own cutoff (FP64-accurate residual)
   DevBuf<double> V64;     // (lmax + 1) x n: z-convolved column values per level
@@ -42,6 +42,33 @@ void ensure_skewer_inner(ds_operator* op, double inner_cut);
 void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int* counter,
                         const double* num, double* alpha_out, double* den_out,
                         const int* skip, cudaStream_t st);
+
+// A map point set declared a grid of columns (ds_map_set_column_grid): point
+// c nz + j at (X_c, Y_c, Z_j), the same uniform Z in every column.  With an
+// operator's skewer grid the map m = S_mp x becomes, per map column c and
+// skewer b within the cutoff, P_cb times a z convolution of x_b sampled at
+// the Z_j: the |Z_j - z_k| take Q distinct values (the two grids are
+// commensurate), R_b^(q)[j] sums the pixels of the q nearest distance
+// classes, and m[c, j] = sum_b P_cb R_b^(q_cb)[j] in FP64.
+struct MapColumns {
+  int ncol = 0, nz = 0;
+  std::vector<double> cx, cy, z;  // column (x, y), Z_j
+  // built for one operator and cutoff
+  unsigned long long op_serial = 0;
+  double cut = 0.0;
+  int Q = 0, W = 0;                // distance classes, pixel window per Z_j
+  DevBuf<int> kstart;              // first pixel index of Z_j's window
+  DevBuf<signed char> cls;         // nz x W: distance class of each window pixel (-1: none)
+  DevBuf<double> taps;             // Q: exp(-c_para delta_q^2)
+  DevBuf<int> ptr, idx, lev;       // CSR column -> skewers, classes kept
+  DevBuf<double> p64;              // var_s exp(-c_perp |dxy|^2)
+  DevBuf<double> R;                // Q x n_sk x nz
+};
+
+// m = S_mp x (caller order, device) with the structured FP64 map; false when
+// the map or the operator has no grid (then nothing is launched).
+bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
+                        double cut);
 
 // r = b - A v (residual) or A v (product) on vectors in the operator's
 // sorted order, with the structured FP64 operator; the launch returns at

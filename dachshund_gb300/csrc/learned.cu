@@ -816,6 +816,14 @@ void LearnedNet::adam_step(float lr) {
 
 void SkewerPCDeleter::operator()(SkewerPC* p) const { delete p; }
 
+// Band rows [record][w] to planes [w][record] (the layout of SkewerPC::L).
+__global__ void k_band_planes(size_t n, int w, const float* __restrict__ rows,
+                              float* __restrict__ planes) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * w) return;
+  planes[(i % w) * n + i / w] = rows[i];
+}
+
 }  // namespace ds
 
 using namespace ds;
@@ -845,7 +853,12 @@ int ds_operator_set_skewer_preconditioner(ds_operator* op, int n_skewers, int n_
     pc->n_per = n_per;
     pc->band = band;
     pc->L.alloc((size_t)op->n * (band + 1));
-    DS_CUDA(cudaMemcpyAsync(pc->L.p, L_rows, pc->L.bytes(), cudaMemcpyDefault, op->ctx->stream));
+    DevBuf<float> rows;  // the caller's rows, then their planes
+    rows.alloc(pc->L.n);
+    DS_CUDA(cudaMemcpyAsync(rows.p, L_rows, rows.bytes(), cudaMemcpyDefault, op->ctx->stream));
+    k_band_planes<<<(unsigned)((rows.n + 255) / 256), 256, 0, op->ctx->stream>>>(
+        (size_t)op->n, band + 1, rows.p, pc->L.p);
+    DS_CHECK_LAUNCH();
     DS_CUDA(cudaStreamSynchronize(op->ctx->stream));
     op->pc = std::move(pc);
   });

@@ -397,15 +397,17 @@ __global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero
   }
   rs[k] = ri;
   __syncthreads();
+  // L in planes: plane m holds L[i][i - m] at slot i (consecutive threads
+  // read consecutive words in both passes)
+  const size_t ns = (size_t)gridDim.x * n_per;
   float t = 0.f;
   for (int m = 0; m <= band; ++m)
-    if (k + m < n_per) t = fmaf(L[(size_t)(slot + m) * (band + 1) + m], rs[k + m], t);
+    if (k + m < n_per) t = fmaf(L[(size_t)m * ns + slot + m], rs[k + m], t);
   ts[k] = t;
   __syncthreads();
-  const float* Lk = L + (size_t)slot * (band + 1);
   float zk = 0.f;
   for (int m = 0; m <= band; ++m)
-    if (k - m >= 0) zk = fmaf(Lk[m], ts[k - m], zk);
+    if (k - m >= 0) zk = fmaf(L[(size_t)m * ns + slot], ts[k - m], zk);
   if (pos >= 0) {
     z[pos] = zk;
     if (MODE == 2) p[pos] = zk;
@@ -819,6 +821,8 @@ void ensure_map_f32(ds_map* map, ds_operator* op, double cut) {
 void map_product_f32_dev(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
                          double cut) {
   require(op->kc.eval == DS_EVAL_EXACT, "the FP32 map product evaluates the exact kernel");
+  // a column-grid map against a skewer grid: the structured FP64 product
+  if (skewer_map_product(map, op, x_dev, m_dev, cut)) return;
   ensure_op_f32(op, op->f32 ? op->f32->inner_cut : DS_DEFAULT_INNER_CUTOFF);
   ensure_map_f32(map, op, cut);
   cudaStream_t st = map->ctx->stream;

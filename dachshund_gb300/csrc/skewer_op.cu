@@ -37,8 +37,47 @@
 namespace ds {
 
 void SkewerGridDeleter::operator()(SkewerGrid* p) const { delete p; }
+void MapColumnsDeleter::operator()(MapColumns* p) const { delete p; }
 
 namespace {
+
+constexpr int NB_CHUNK = 256;  // neighbour entries staged per round
+
+// sum_q p[q] V[(lev[q] + lev_base) plane + idx[q] stride + k] over the CSR
+// row q0 .. q1: the row's offsets and factors are staged in shared memory a
+// chunk at a time (so no V address waits on a load), and each thread keeps
+// eight independent loads in flight.  Every thread of the CTA calls it (it
+// synchronises); `live` false threads take part without loading.
+template <typename T>
+__device__ __forceinline__ T nbr_sum(int q0, int q1, const int* __restrict__ idx,
+                                     const int* __restrict__ lev, const T* __restrict__ pv,
+                                     int lev_base, size_t plane, int stride,
+                                     const T* __restrict__ V, int k, bool live,
+                                     size_t* s_off, T* s_p) {
+  T acc[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) acc[u] = T(0);
+  for (int c0 = q0; c0 < q1; c0 += NB_CHUNK) {
+    const int cnt = min(NB_CHUNK, q1 - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+      s_off[t] = (size_t)(lev[c0 + t] + lev_base) * plane + (size_t)idx[c0 + t] * stride;
+      s_p[t] = pv[c0 + t];
+    }
+    __syncthreads();
+    if (!live) continue;
+    int i = 0;
+    for (; i + 8 <= cnt; i += 8) {
+      T v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = V[s_off[i + u] + k];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc[u] = fma(s_p[i + u], v[u], acc[u]);
+    }
+    for (; i < cnt; ++i) acc[0] = fma(s_p[i], V[s_off[i] + k], acc[0]);
+  }
+  return ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+}
 
 // V^(L) for L = 0..lmax of one skewer per CTA (n_per threads).
 __global__ void k_sg_levels(int n_per, int lmax, size_t n, const int* __restrict__ pos,
@@ -74,21 +113,15 @@ __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
                            const double* __restrict__ bvec, double* __restrict__ out,
                            const int* skip, unsigned long long* prof_terms) {
   if (skip && *skip) return;
+  __shared__ size_t s_off[NB_CHUNK];
+  __shared__ double s_p[NB_CHUNK];
   const int a = blockIdx.x, k = threadIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
-  double acc0 = 0.0, acc1 = 0.0;
-  int q = q0;
-  for (; q + 1 < q1; q += 2) {  // two independent chains
-    const double v0 = V[(size_t)nb_lev[q] * n + (size_t)nb_idx[q] * n_per + k];
-    const double v1 = V[(size_t)nb_lev[q + 1] * n + (size_t)nb_idx[q + 1] * n_per + k];
-    acc0 = fma(nb_p[q], v0, acc0);
-    acc1 = fma(nb_p[q + 1], v1, acc1);
-  }
-  if (q < q1)
-    acc0 = fma(nb_p[q], V[(size_t)nb_lev[q] * n + (size_t)nb_idx[q] * n_per + k], acc0);
+  const double acc = nbr_sum<double>(q0, q1, nb_idx, nb_lev, nb_p, 0, n, n_per, V, k, true,
+                                     s_off, s_p);
   const size_t r = (size_t)a * n_per + k;
   const int p = pos[r];
-  const double y = fma(wl[p], acc0 + acc1, e[p] * v[p]);
+  const double y = fma(wl[p], acc, e[p] * v[p]);
   out[p] = RESID ? bvec[p] - y : y;
   if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
 }
@@ -144,22 +177,16 @@ __global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr
                              unsigned long long* prof_terms) {
   if (skip && *skip) return;
   __shared__ double sm[32];
+  __shared__ size_t s_off[NB_CHUNK];
+  __shared__ float s_p[NB_CHUNK];
   const int a = blockIdx.x, k = threadIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
-  float acc0 = 0.f, acc1 = 0.f;
-  int j = q0;
-  for (; j + 1 < q1; j += 2) {
-    const float v0 = V[(size_t)nb_lev[j] * n + (size_t)nb_idx[j] * n_per + k];
-    const float v1 = V[(size_t)nb_lev[j + 1] * n + (size_t)nb_idx[j + 1] * n_per + k];
-    acc0 = fmaf(nb_p[j], v0, acc0);
-    acc1 = fmaf(nb_p[j + 1], v1, acc1);
-  }
-  if (j < q1)
-    acc0 = fmaf(nb_p[j], V[(size_t)nb_lev[j] * n + (size_t)nb_idx[j] * n_per + k], acc0);
+  const float acc = nbr_sum<float>(q0, q1, nb_idx, nb_lev, nb_p, 0, n, n_per, V, k, true,
+                                   s_off, s_p);
   const size_t r = (size_t)a * n_per + k;
   const int ps = pos[r];
   const float pv = p[ps];
-  const float qv = fmaf((float)wl[ps], acc0 + acc1, (float)e[ps] * pv);
+  const float qv = fmaf((float)wl[ps], acc, (float)e[ps] * pv);
   q[ps] = qv;
   if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
   if (!part) return;
@@ -174,6 +201,85 @@ __global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr
     *alpha_out = *num / pq;
     *counter = 0;
   }
+}
+
+// ---- structured map --------------------------------------------------------------
+constexpr int MC_QMAX = 32;  // distance classes at most
+
+// Column (x, y) and the Z_j of a map declared a column grid, from its sorted
+// point set (perm: sorted position -> caller index c nz + j).
+__global__ void k_mc_info(int n_pad, int nz, const int* __restrict__ perm,
+                          const double* __restrict__ px, const double* __restrict__ py,
+                          const double* __restrict__ pz, double* __restrict__ cx,
+                          double* __restrict__ cy, double* __restrict__ zj) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  const int p = perm[i];
+  if (p < 0) return;
+  const int c = p / nz, j = p % nz;
+  if (j == 0) {
+    cx[c] = px[i];
+    cy[c] = py[i];
+  }
+  if (c == 0) zj[j] = pz[i];
+}
+
+// Flags a point that is not at its column's (x, y) and its Z_j.
+__global__ void k_mc_check(int n_pad, int nz, const int* __restrict__ perm,
+                           const double* __restrict__ px, const double* __restrict__ py,
+                           const double* __restrict__ pz, const double* __restrict__ cx,
+                           const double* __restrict__ cy, const double* __restrict__ zj,
+                           int* __restrict__ bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  const int p = perm[i];
+  if (p < 0) return;
+  const int c = p / nz, j = p % nz;
+  if (px[i] != cx[c] || py[i] != cy[c] || pz[i] != zj[j]) atomicOr(bad, 1);
+}
+
+// R_b^(q)[j] = sum of T_class x_{b,k} over the window pixels of Z_j whose
+// distance class is < q + 1 (one thread per (skewer, Z_j)); x in caller
+// order (record b n_per + k).
+__global__ void k_mc_levels(int n_sk, int n_per, int nz, int W, int Q,
+                            const int* __restrict__ kstart, const signed char* __restrict__ cls,
+                            const double* __restrict__ taps, const double* __restrict__ x,
+                            double* __restrict__ R) {
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  if (j >= nz) return;
+  const int b = blockIdx.x;
+  double acc[MC_QMAX];
+  for (int q = 0; q < Q; ++q) acc[q] = 0.0;
+  const int k0 = kstart[j];
+  for (int w = 0; w < W; ++w) {
+    const int k = k0 + w;
+    const int q = cls[(size_t)j * W + w];
+    if (q < 0 || k < 0 || k >= n_per) continue;
+    acc[q] += x[(size_t)b * n_per + k];
+  }
+  double s = 0.0;
+  const size_t plane = (size_t)n_sk * nz;
+  for (int q = 0; q < Q; ++q) {
+    s = fma(taps[q], acc[q], s);
+    R[q * plane + (size_t)b * nz + j] = s;
+  }
+}
+
+// m[c nz + j] = sum over the skewers b near column c of P_cb R_b^(q_cb)[j].
+__global__ void k_mc_apply(int n_sk, int nz, const int* __restrict__ ptr,
+                           const int* __restrict__ idx, const int* __restrict__ lev,
+                           const double* __restrict__ p64, const double* __restrict__ R,
+                           double* __restrict__ m, unsigned long long* prof_terms) {
+  __shared__ size_t s_off[NB_CHUNK];
+  __shared__ double s_p[NB_CHUNK];
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  const int c = blockIdx.x;
+  const int q0 = ptr[c], q1 = ptr[c + 1];
+  const double acc = nbr_sum<double>(q0, q1, idx, lev, p64, -1, (size_t)n_sk * nz, nz, R, j,
+                                     j < nz, s_off, s_p);
+  if (j >= nz) return;
+  m[(size_t)c * nz + j] = acc;
+  if (prof_terms && j == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * nz);
 }
 
 // Skewer pairs within `cut` (cell lists of side sqrt(cut / c_perp)).
@@ -287,6 +393,7 @@ void build_skewer_grid(ds_operator* op, int n_sk, int n_per) {
   std::unique_ptr<SkewerGrid, SkewerGridDeleter> g(new SkewerGrid());
   g->n_sk = n_sk;
   g->n_per = n_per;
+  g->z0 = z[0];
   g->dz = n_per > 1 ? zd[1] : 0.0;
   std::vector<double> taps(n_per);
   for (int m = 0; m < n_per; ++m) taps[m] = std::exp(-op->kc.c_para * zd[m] * zd[m]);
@@ -336,6 +443,146 @@ void skewer_apply_f64(ds_operator* op, bool residual, const double* v, double* o
   if (ev) pr.end(st, ev, 0);
 }
 
+// Distance classes, pixel windows and column -> skewer lists of a column
+// grid against the operator's skewer grid, for one cutoff.
+static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
+  MapColumns& mc = *map->cols;
+  const SkewerGrid& g = *op->sgrid;
+  const KernelConsts& kc = op->kc;
+  cudaStream_t st = map->ctx->stream;
+  const int nz = mc.nz, n_per = g.n_per;
+  require(g.dz > 0.0, "structured map: the skewers need at least two pixels");
+  const double dmax = std::sqrt(cut / kc.c_para);
+  std::vector<int> kstart(nz);
+  int W = 1;
+  for (int j = 0; j < nz; ++j) {
+    const int lo = (int)std::ceil((mc.z[j] - dmax - g.z0) / g.dz) - 1;
+    const int hi = (int)std::floor((mc.z[j] + dmax - g.z0) / g.dz) + 1;
+    kstart[j] = lo;
+    W = std::max(W, hi - lo + 1);
+  }
+  auto dist = [&](int j, int k) { return std::fabs(mc.z[j] - (g.z0 + g.zd[k])); };
+  std::vector<double> ds;
+  for (int j = 0; j < nz; ++j)
+    for (int w = 0; w < W; ++w) {
+      const int k = kstart[j] + w;
+      if (k < 0 || k >= n_per) continue;
+      const double d = dist(j, k);
+      if (kc.c_para * d * d < cut) ds.push_back(d);
+    }
+  std::sort(ds.begin(), ds.end());
+  std::vector<double> cls_d;  // one representative per class (ulp-level ties merged)
+  for (double d : ds)
+    if (cls_d.empty() || d - cls_d.back() > 1e-12 * std::max(1.0, d)) cls_d.push_back(d);
+  const int Q = (int)cls_d.size();
+  require(Q >= 1 && Q <= MC_QMAX,
+          "structured map: the map's z values and the pixels' z grid give more than 32 "
+          "distances within the cutoff");
+  auto class_of = [&](double d) {
+    const auto it = std::lower_bound(cls_d.begin(), cls_d.end(), d * (1.0 - 1e-12) - 1e-300);
+    return (int)(it - cls_d.begin());
+  };
+  std::vector<signed char> cls((size_t)nz * W, -1);
+  for (int j = 0; j < nz; ++j)
+    for (int w = 0; w < W; ++w) {
+      const int k = kstart[j] + w;
+      if (k < 0 || k >= n_per) continue;
+      const double d = dist(j, k);
+      if (kc.c_para * d * d < cut) cls[(size_t)j * W + w] = (signed char)class_of(d);
+    }
+  std::vector<double> taps(Q);
+  for (int q = 0; q < Q; ++q) taps[q] = std::exp(-kc.c_para * cls_d[q] * cls_d[q]);
+  // column -> skewer lists (cell lists over the skewers)
+  const int n_sk = g.n_sk;
+  const double h = std::sqrt(cut / kc.c_perp);
+  const double x0 = *std::min_element(g.sx.begin(), g.sx.end());
+  const double y0 = *std::min_element(g.sy.begin(), g.sy.end());
+  const double x1 = *std::max_element(g.sx.begin(), g.sx.end());
+  const double y1 = *std::max_element(g.sy.begin(), g.sy.end());
+  const int ncx = std::max(1, (int)std::min(4096.0, std::floor((x1 - x0) / h) + 1));
+  const int ncy = std::max(1, (int)std::min(4096.0, std::floor((y1 - y0) / h) + 1));
+  auto cell_of = [&](double v, double o, int nc) {
+    return std::min(nc - 1, std::max(0, (int)std::floor((v - o) / h)));
+  };
+  std::vector<std::vector<int>> cells((size_t)ncx * ncy);
+  for (int s = 0; s < n_sk; ++s)
+    cells[(size_t)cell_of(g.sy[s], y0, ncy) * ncx + cell_of(g.sx[s], x0, ncx)].push_back(s);
+  std::vector<int> ptr(mc.ncol + 1, 0), idx, lev;
+  std::vector<double> p64;
+  std::vector<std::pair<int, double>> row;
+  for (int c = 0; c < mc.ncol; ++c) {
+    const int qx = cell_of(mc.cx[c], x0, ncx), qy = cell_of(mc.cy[c], y0, ncy);
+    row.clear();
+    for (int jy = std::max(0, qy - 1); jy <= std::min(ncy - 1, qy + 1); ++jy)
+      for (int jx = std::max(0, qx - 1); jx <= std::min(ncx - 1, qx + 1); ++jx)
+        for (int b : cells[(size_t)jy * ncx + jx]) {
+          const double dx = mc.cx[c] - g.sx[b], dy = mc.cy[c] - g.sy[b];
+          const double parg = kc.c_perp * (dx * dx + dy * dy);
+          if (parg < cut) row.push_back({b, parg});
+        }
+    std::sort(row.begin(), row.end());
+    for (const auto& bp : row) {
+      int L = 0;
+      while (L < Q && bp.second + kc.c_para * cls_d[L] * cls_d[L] < cut) ++L;
+      if (L == 0) continue;
+      idx.push_back(bp.first);
+      lev.push_back(L);
+      p64.push_back(kc.var_s * std::exp(-bp.second));
+    }
+    ptr[c + 1] = (int)idx.size();
+  }
+  mc.Q = Q;
+  mc.W = W;
+  mc.cut = cut;
+  mc.op_serial = op->serial;
+  mc.kstart.alloc(nz);
+  mc.cls.alloc(cls.size());
+  mc.taps.alloc(Q);
+  mc.ptr.alloc(ptr.size());
+  mc.idx.alloc(std::max<size_t>(1, idx.size()));
+  mc.lev.alloc(std::max<size_t>(1, lev.size()));
+  mc.p64.alloc(std::max<size_t>(1, p64.size()));
+  mc.R.alloc((size_t)Q * n_sk * nz);
+  DS_CUDA(cudaMemcpyAsync(mc.kstart.p, kstart.data(), nz * sizeof(int), cudaMemcpyHostToDevice,
+                          st));
+  DS_CUDA(cudaMemcpyAsync(mc.cls.p, cls.data(), cls.size(), cudaMemcpyHostToDevice, st));
+  DS_CUDA(cudaMemcpyAsync(mc.taps.p, taps.data(), Q * sizeof(double), cudaMemcpyHostToDevice,
+                          st));
+  DS_CUDA(cudaMemcpyAsync(mc.ptr.p, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          st));
+  DS_CUDA(cudaMemcpyAsync(mc.idx.p, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          st));
+  DS_CUDA(cudaMemcpyAsync(mc.lev.p, lev.data(), lev.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          st));
+  DS_CUDA(cudaMemcpyAsync(mc.p64.p, p64.data(), p64.size() * sizeof(double),
+                          cudaMemcpyHostToDevice, st));
+  DS_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
+}
+
+bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
+                        double cut) {
+  if (!map->cols || !op->sgrid) return false;
+  MapColumns& mc = *map->cols;
+  if (mc.op_serial != op->serial || mc.cut != cut || !mc.ptr.p) build_map_columns(map, op, cut);
+  const SkewerGrid& g = *op->sgrid;
+  cudaStream_t st = map->ctx->stream;
+  Profiler& pr = map->ctx->prof;
+  cudaEvent_t ev = nullptr;
+  unsigned long long* prof_terms = nullptr;
+  if (pr.enabled) {
+    prof_terms = pr.d_pairs + 2;  // kind 2: map products
+    pr.begin(st, &ev);
+  }
+  k_mc_levels<<<dim3(g.n_sk, (mc.nz + 127) / 128), 128, 0, st>>>(
+      g.n_sk, g.n_per, mc.nz, mc.W, mc.Q, mc.kstart.p, mc.cls.p, mc.taps.p, x_dev, mc.R.p);
+  DS_CHECK_LAUNCH();
+  k_mc_apply<<<dim3(mc.ncol, (mc.nz + 255) / 256), 256, 0, st>>>(
+      g.n_sk, mc.nz, mc.ptr.p, mc.idx.p, mc.lev.p, mc.p64.p, mc.R.p, m_dev, prof_terms);
+  DS_CHECK_LAUNCH();
+  if (ev) pr.end(st, ev, 2);
+  return true;
+}
+
 void ensure_skewer_inner(ds_operator* op, double inner_cut) {
   SkewerGrid& g = *op->sgrid;
   if (g.inner.ptr.p && g.inner.cut == inner_cut) return;
@@ -382,6 +629,52 @@ int ds_operator_set_skewer_grid(ds_operator* op, int n_skewers, int n_per) {
       return;
     }
     build_skewer_grid(op, n_skewers, n_per);
+  });
+}
+
+int ds_map_set_column_grid(ds_map* map, int n_columns, int nz) {
+  if (!map) return DS_ERR_ARG;
+  return guarded(map->ctx, [&] {
+    if (n_columns == 0) {
+      map->cols.reset();
+      return;
+    }
+    require(n_columns > 0 && nz > 0 && (long long)n_columns * nz == map->pts.n,
+            "n_columns x nz must equal the map's point count");
+    cudaStream_t st = map->ctx->stream;
+    DevBuf<double> cx, cy, zj;
+    DevBuf<int> bad;
+    cx.alloc(n_columns);
+    cy.alloc(n_columns);
+    zj.alloc(nz);
+    bad.alloc(1);
+    DS_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+    const int np = map->pts.n_pad;
+    k_mc_info<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->pts.perm.p, map->pts.x.p,
+                                                 map->pts.y.p, map->pts.z.p, cx.p, cy.p, zj.p);
+    DS_CHECK_LAUNCH();
+    k_mc_check<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->pts.perm.p, map->pts.x.p,
+                                                  map->pts.y.p, map->pts.z.p, cx.p, cy.p, zj.p,
+                                                  bad.p);
+    DS_CHECK_LAUNCH();
+    std::unique_ptr<MapColumns, MapColumnsDeleter> mc(new MapColumns());
+    mc->ncol = n_columns;
+    mc->nz = nz;
+    mc->cx.resize(n_columns);
+    mc->cy.resize(n_columns);
+    mc->z.resize(nz);
+    int hbad = 0;
+    DS_CUDA(cudaMemcpyAsync(mc->cx.data(), cx.p, n_columns * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaMemcpyAsync(mc->cy.data(), cy.p, n_columns * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaMemcpyAsync(mc->z.data(), zj.p, nz * sizeof(double), cudaMemcpyDeviceToHost,
+                            st));
+    DS_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    require(!hbad, "map points are not a column grid (point c nz + j at column c's (x, y) "
+                   "and the j-th z of column 0)");
+    map->cols = std::move(mc);
   });
 }
 

@@ -530,11 +530,24 @@ int ds_map_product_dev(ds_map* map, ds_operator* op, const double* x,
  * counterpart for the FP32 evaluation): FP32 evaluation of the exact
  * kernel (MUFU ex2), FP32 sums per column tile, FP64 accumulation across
  * tiles; pairs beyond ``cutoff`` (exponent; <= 0: 30) are skipped.  Map
- * error against the FP64 product is about 1e-7 relative. */
+ * error against the FP64 product is about 1e-7 relative.  When the map was
+ * declared a column grid (ds_map_set_column_grid) and the operator has a
+ * skewer grid (ds_operator_set_skewer_grid), the product is instead the
+ * structured FP64 one (per map column and skewer: perpendicular factor x
+ * z-convolved solution), exact to rounding within the same cutoff. */
 int ds_map_product_f32(ds_map* map, ds_operator* op, double cutoff,
                        const double* x, double* m);
 int ds_map_product_f32_dev(ds_map* map, ds_operator* op, double cutoff,
                            const double* x, double* m);
+
+/* Declares the map points a column grid (no reference counterpart; the
+ * layout of init_uniform_map_coords, lib/util.cc:25-46): point c nz + j at
+ * column c's (x, y) and at the j-th z value of column 0, for n_columns
+ * columns of nz points.  0 columns removes the declaration.  DS_ERR_ARG when
+ * the points do not have that layout.  Used by ds_map_product_f32* with an
+ * operator that has a skewer grid; the z values of the map and of the
+ * pixels must give at most 32 distinct distances within the cutoff. */
+int ds_map_set_column_grid(ds_map* map, int n_columns, int nz);
 
 /* One-shot smp_product with the reference's argument list (lib/map.h:41-44):
  * pixel and map points as Point arrays, x in pixel order; host arrays. */

@@ -106,3 +106,49 @@ def test_mixed_solve_structured(ctx, form, n_sk, n_per, cluster):
     op.set_inner_matvec("auto")
     op.set_skewer_grid(0, 0)
     op.close()
+
+
+def test_structured_map_matches_oracle(ctx):
+    """The structured FP64 map (column grid x skewer grid) against the
+    oracle's FP64 smp_product with the exact kernel (lib/map.cc:20-43) and
+    the pair-kernel FP64 map: within 1e-12 of the largest |m| (the cutoff at
+    exponent 30 drops terms below 1e-13 of var_s |x_j|)."""
+    from dachshund_gb300 import MapGrid
+
+    n_sk, n_per = 20, 40
+    w = synth.small(n_sk, n_per, 8.0, seed=11)
+    op, rec = make(ctx, "sn", w.pixels)
+    op.set_skewer_grid(n_sk, n_per)
+    nx, ny, nz = 6, 5, 2 * n_per  # map z every 1 Mpc/h, pixels every 2
+    pts = synth.uniform_map_coords(8.0, 8.0, n_per * synth.DZ, nx, ny, nz)
+    grid = MapGrid(ctx, pts)
+    x = np.random.default_rng(3).standard_normal(rec.shape[0])
+    m_pair = grid.product_f32(op, x)  # no column grid yet: the FP32 pair kernel
+    grid.set_column_grid(nx * ny, nz)
+    m = grid.product_f32(op, x)
+    mo = oracle.smp_product(w.pixels[:, :3], pts, x, VS, LP, LQ, exact=True)
+    scale = np.max(np.abs(mo))
+    assert np.max(np.abs(m - mo)) / scale < 1e-12
+    assert np.max(np.abs(m - grid.product(op, x))) / scale < 1e-12
+    assert np.max(np.abs(m_pair - mo)) / scale < 1e-6
+    # repeated products reuse the lists; removing the grid returns to the pair kernel
+    assert np.array_equal(grid.product_f32(op, x), m)
+    grid.set_column_grid(0, 0)
+    assert np.max(np.abs(grid.product_f32(op, x) - mo)) / scale < 1e-6
+    grid.close()
+    op.close()
+
+
+def test_column_grid_refused_for_other_layouts(ctx):
+    from dachshund_gb300 import MapGrid
+
+    pts = synth.uniform_map_coords(8.0, 8.0, 40.0, 4, 4, 10)
+    grid = MapGrid(ctx, pts[np.random.default_rng(1).permutation(pts.shape[0])])
+    with pytest.raises(DsError):
+        grid.set_column_grid(16, 10)
+    grid.close()
+    grid = MapGrid(ctx, pts)
+    with pytest.raises(DsError):
+        grid.set_column_grid(15, 10)
+    grid.set_column_grid(16, 10)
+    grid.close()
