@@ -7,12 +7,16 @@ leaves the GPU's clocks as they are):
                  arithmetic (k_pair_ff_resid), random x
   f32_matvec     one mixed-precision solve of the 262,144-pixel system
                  (k_pair_f32 launches, one per iteration)
+  e2e_parts      the end-to-end call sequence of the benchmark's chosen form
+                 from pinned host buffers (operator, preconditioner, skewer
+                 grid, solve, map grid, column grid, map product), each call
+                 timed on the host after a synchronize (second pass printed)
   chosen_step    one step of the benchmark's chosen form on the 262,144-pixel
                  system, after one untimed warm-up step: cluster
                  preconditioner and skewer grid installed, the mixed solve
                  (k_sg32_levels + k_sg32_apply, k_pc_iter, k_mx_dir, and
                  k_sg_levels + k_sg_apply for the FP64 residuals) and the
-                 80 x 80 x 512 FP32 map (k_pair_f32 MAP)
+                 80 x 80 x 512 structured FP64 map (k_mc_levels + k_mc_apply)
   tc_matvec      one batched FP32 product of 64 chunks x 64 RHS with the
                  tensor-core variant (k_pack_panels + k_batch_mv_tc)
   tc_inner       one mixed-precision solve of the 262,144-pixel system with
@@ -44,7 +48,44 @@ def main(argv=None):
 
     ctx = Context(0)
     sp = SignalCovarParams(synth.VAR_S, synth.L_PERP, synth.L_PARA, eval="exact")
-    if case == "chosen_step":
+    if case == "e2e_parts":
+        import time
+
+        from dachshund_gb300 import MapGrid
+
+        w = synth.wf262144(0)
+        rec = torch.from_numpy(pixel_to_wpixel(w.pixels)).pin_memory().numpy()
+        pts = torch.from_numpy(synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny,
+                                                        w.map_nz)).pin_memory().numpy()
+        for rep in range(2):
+            t = {}
+
+            def mark(name, t0):
+                ctx.synchronize()
+                torch.cuda.synchronize()
+                t[name] = round((time.perf_counter() - t0) * 1e3, 2)
+                return time.perf_counter()
+
+            t0 = time.perf_counter()
+            op = WFVectorW(ctx, rec, sp)
+            t0 = mark("operator", t0)
+            op.set_cluster_preconditioner(w.n_skewers, w.pix_per_skewer, 4, 16)
+            t0 = mark("cluster_pc", t0)
+            op.set_skewer_grid(w.n_skewers, w.pix_per_skewer)
+            t0 = mark("skewer_grid", t0)
+            x, res = op.solve_mixed(MixedParams(max_iter=3000, tol=1e-8))
+            t0 = mark("solve", t0)
+            grid = MapGrid(ctx, pts)
+            t0 = mark("map_grid", t0)
+            grid.set_column_grid(w.map_nx * w.map_ny, w.map_nz)
+            t0 = mark("column_grid", t0)
+            m = grid.product_f32(op, x)
+            t0 = mark("map_product", t0)
+            grid.close()
+            op.close()
+            mark("close", t0)
+        print(case, "ms", t, "total", round(sum(t.values()), 2))
+    elif case == "chosen_step":
         from dachshund_gb300 import MapGrid
 
         w = synth.wf262144(0)
@@ -54,6 +95,7 @@ def main(argv=None):
         op.set_skewer_grid(w.n_skewers, w.pix_per_skewer)
         grid = MapGrid(ctx, synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny,
                                                      w.map_nz))
+        grid.set_column_grid(w.map_nx * w.map_ny, w.map_nz)
         x = torch.zeros(w.n, dtype=torch.float64, device="cuda")
         m = torch.empty(w.n_map, dtype=torch.float64, device="cuda")
         for _ in range(2):
