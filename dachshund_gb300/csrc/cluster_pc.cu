@@ -41,8 +41,8 @@ constexpr int CPC_PACKED = (CPC_MAX_BAND + 1) * (CPC_MAX_BAND + 2) / 2;
 
 // Column `j` (a slot) of G: rows j .. j + m - 1, the next non-padding slots
 // of its block (at most band + 1).  A_ab = wl_a S_ab wr_b + e_a delta_ab with
-// the exact Gaussian S (the table kernel differs from it by ~1e-4, which is
-// immaterial to a preconditioner).
+// the exact Gaussian S evaluated in FP32 (the table kernel differs from it by
+// ~1e-4, FP32 by ~1e-6: immaterial to a preconditioner).
 __global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc,
                                const int* __restrict__ crec, const int* __restrict__ inv,
                                const double* __restrict__ px, const double* __restrict__ py,
@@ -59,18 +59,32 @@ __global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc
     pos[m] = inv[crec[j + m]];
     ++m;
   }
+  // coordinates relative to the column's own pixel, in FP32 (a
+  // preconditioner needs no more), and the coefficients of each position
+  float rx[CPC_MAX_BAND + 1], ry[CPC_MAX_BAND + 1], rz[CPC_MAX_BAND + 1];
+  float wa[CPC_MAX_BAND + 1], wb[CPC_MAX_BAND + 1], ea[CPC_MAX_BAND + 1];
+  {
+    const double x0 = px[pos[0]], y0 = py[pos[0]], z0 = pz[pos[0]];
+    for (int a = 0; a < m; ++a) {
+      const int pa = pos[a];
+      rx[a] = (float)(px[pa] - x0);
+      ry[a] = (float)(py[pa] - y0);
+      rz[a] = (float)(pz[pa] - z0);
+      wa[a] = (float)(wl[pa] * kc.var_s);
+      wb[a] = (float)wr[pa];
+      ea[a] = (float)e[pa];
+    }
+  }
+  const float cp = (float)kc.c_perp, cq = (float)kc.c_para, cut = (float)kc.exact_cut;
   float C[CPC_PACKED];  // packed lower Cholesky factor: row a starts at a (a + 1) / 2
   bool ok = true;
   for (int a = 0; a < m && ok; ++a) {
-    const int pa = pos[a];
-    const double xa = px[pa], ya = py[pa], za = pz[pa];
     float* Ca = C + a * (a + 1) / 2;
     for (int b = 0; b <= a; ++b) {
-      const int pb = pos[b];
-      const double dx = xa - px[pb], dy = ya - py[pb], dz = za - pz[pb];
-      const double arg = kc.c_perp * (dx * dx + dy * dy) + kc.c_para * dz * dz;
-      const double s = arg < kc.exact_cut ? kc.var_s * (double)expf(-(float)arg) : 0.0;
-      float v = (float)(wl[pa] * s * wr[pb] + (a == b ? e[pa] : 0.0));
+      const float dx = rx[a] - rx[b], dy = ry[a] - ry[b], dz = rz[a] - rz[b];
+      const float arg = fmaf(cp, fmaf(dx, dx, dy * dy), cq * dz * dz);
+      float v = arg < cut ? wa[a] * expf(-arg) * wb[b] : 0.f;
+      if (a == b) v += ea[a];
       const float* Cb = C + b * (b + 1) / 2;
       for (int k = 0; k < b; ++k) v = fmaf(-Ca[k], Cb[k], v);
       if (a == b) {
@@ -107,6 +121,21 @@ __global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc
   // G[j + a][j] is plane a at slot j + a
   const float sc = rsqrtf(y[0]);
   for (int a = 0; a < m; ++a) L[(size_t)a * n_slots + (j + a)] = y[a] * sc;
+}
+
+// Record r's z, and skewer s's (x, y) from its first record (r = s n_per).
+__global__ void k_rec_coords(int n, int n_per, const int* __restrict__ inv,
+                             const double* __restrict__ px, const double* __restrict__ py,
+                             const double* __restrict__ pz, double* __restrict__ sx,
+                             double* __restrict__ sy, double* __restrict__ rz) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int p = inv[r];
+  rz[r] = pz[p];
+  if (r % n_per == 0) {
+    sx[r / n_per] = px[p];
+    sy[r / n_per] = py[p];
+  }
 }
 
 // 32-bit Morton key of (x, y) quantised to 16 bits each.
@@ -183,24 +212,20 @@ void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>&
 
 void build_cluster_pc(ds_operator* op, int n_sk, int n_per, int g, int band) {
   cudaStream_t st = op->ctx->stream;
-  const int n = op->n, np = op->pix.n_pad;
-  // record coordinates from the operator's sorted copies
-  std::vector<double> hx(np), hy(np), hz(np);
-  std::vector<int> hinv(n);
-  DS_CUDA(cudaMemcpyAsync(hx.data(), op->pix.x.p, np * sizeof(double),
-                          cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(hy.data(), op->pix.y.p, np * sizeof(double),
-                          cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(hz.data(), op->pix.z.p, np * sizeof(double),
-                          cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(hinv.data(), op->inv.p, n * sizeof(int), cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaStreamSynchronize(st));
+  const int n = op->n;
+  // skewer (x, y) (of each skewer's first record) and every record's z
+  DevBuf<double> dsx, dsy, drz;
+  dsx.alloc(n_sk);
+  dsy.alloc(n_sk);
+  drz.alloc(n);
+  k_rec_coords<<<(n + 255) / 256, 256, 0, st>>>(n, n_per, op->inv.p, op->pix.x.p, op->pix.y.p,
+                                                op->pix.z.p, dsx.p, dsy.p, drz.p);
+  DS_CHECK_LAUNCH();
   std::vector<double> sx(n_sk), sy(n_sk), rz(n);
-  for (int s = 0; s < n_sk; ++s) {
-    sx[s] = hx[hinv[(size_t)s * n_per]];
-    sy[s] = hy[hinv[(size_t)s * n_per]];
-  }
-  for (int r = 0; r < n; ++r) rz[r] = hz[hinv[r]];
+  DS_CUDA(cudaMemcpyAsync(sx.data(), dsx.p, n_sk * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(sy.data(), dsy.p, n_sk * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(rz.data(), drz.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
   std::vector<int> crec;
   int n_blocks = 0;
   plan_skewer_clusters(n_sk, n_per, g, sx, sy, rz, crec, n_blocks);

@@ -10,8 +10,8 @@ namespace ds {
 
 // Skewer pairs (a, b) within one cutoff, CSR by a (b ascending, a itself
 // included): the perpendicular factor var_s exp(-c_perp |dxy_ab|^2) and the
-// number of z taps on each side, L_ab = max m with
-// c_perp |dxy_ab|^2 + c_para (z_m - z_0)^2 < cut.
+// number of z levels kept, lev = 1 + max m with
+// c_perp |dxy_ab|^2 + c_para (z_m - z_0)^2 < cut (built on the device).
 struct SkewerNbrs {
   double cut = 0.0;
   int lmax = 0;        // largest L_ab
@@ -28,23 +28,46 @@ struct SkewerGrid {
   SkewerNbrs outer;       // the operator's own cutoff (FP64-accurate residual)
   DevBuf<double> V64;     // (lmax + 1) x n: z-convolved column values per level
   // the FP32 inner operator of the mixed solve (its cutoff, built on demand)
-  std::vector<double> sx, sy, zd;  // skewer (x, y), z_m - z_0
+  std::vector<double> zd;          // z_m - z_0
+  DevBuf<double> sx, sy;           // skewer (x, y)
   SkewerNbrs inner;
   DevBuf<float> taps32, V32;
   DevBuf<double> dot_part;  // per-skewer p.q partials
+  // record-order copies for the mixed solve (built on first use)
+  DevBuf<double> rwl, rwr, re, rb, rx;
+  DevBuf<float> rpd;
 };
 
-// The FP32 inner product of the mixed solve, q = A32 p on FP32 vectors in
-// sorted order, with the PCG step's p.q and alpha = *num / p.q (written by
-// the last CTA, counter reset to 0).  ensure_skewer_inner builds the lists
-// at the inner cutoff once.
+// The vectors a structured product addresses: pos maps a record to its
+// index in the vectors (null: the record's own index, the mixed solve's
+// record order), wl, wr, e, b the operator's coefficients and right-hand side
+// in that order.
+struct SkewerVecs {
+  const int* pos;
+  const double *wl, *wr, *e, *b;
+};
+SkewerVecs skewer_vecs_sorted(ds_operator* op);
+// record-order copies (built once; pdiag_sorted: the FP32 Jacobi diagonal)
+SkewerVecs skewer_vecs_rec(ds_operator* op, const float* pdiag_sorted);
+void skewer_x_to_rec(ds_operator* op, const double* x_sorted, double* x_rec, cudaStream_t st);
+void skewer_x_to_sorted(ds_operator* op, const double* x_rec, double* x_sorted, cudaStream_t st);
+
+// The FP32 inner product of the mixed solve, q = A32 p on FP32 vectors, with
+// the PCG step's p.q and alpha = *num / p.q (written by the last CTA,
+// counter reset to 0; counter null: no dot).  ensure_skewer_inner builds the
+// lists at the inner cutoff once.
 void ensure_skewer_inner(ds_operator* op, double inner_cut);
-void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int* counter,
-                        const double* num, double* alpha_out, double* den_out,
-                        const int* skip, cudaStream_t st);
+void skewer_product_f32(ds_operator* op, const SkewerVecs& c, const float* p, float* q,
+                        unsigned int* counter, const double* num, double* alpha_out,
+                        double* den_out, const int* skip, cudaStream_t st);
+
+// r = b - A v (residual) or A v (product) with the structured FP64
+// operator; the launch returns at once when *skip != 0 (skip may be null).
+void skewer_apply_f64(ds_operator* op, const SkewerVecs& c, bool residual, const double* v,
+                      double* out, const int* skip, cudaStream_t st);
 
 // A map point set declared a grid of columns (ds_map_set_column_grid): point
-// c nz + j at (X_c, Y_c, Z_j), the same uniform Z in every column.  With an
+// c nz + j at (X_c, Y_c, Z_j), the same Z_j in every column.  With an
 // operator's skewer grid the map m = S_mp x becomes, per map column c and
 // skewer b within the cutoff, P_cb times a z convolution of x_b sampled at
 // the Z_j: the |Z_j - z_k| take Q distinct values (the two grids are
@@ -52,7 +75,8 @@ void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int*
 // classes, and m[c, j] = sum_b P_cb R_b^(q_cb)[j] in FP64.
 struct MapColumns {
   int ncol = 0, nz = 0;
-  std::vector<double> cx, cy, z;  // column (x, y), Z_j
+  std::vector<double> z;   // Z_j
+  DevBuf<double> cx, cy;   // column (x, y)
   // built for one operator and cutoff
   unsigned long long op_serial = 0;
   double cut = 0.0;
@@ -69,11 +93,5 @@ struct MapColumns {
 // the map or the operator has no grid (then nothing is launched).
 bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, double* m_dev,
                         double cut);
-
-// r = b - A v (residual) or A v (product) on vectors in the operator's
-// sorted order, with the structured FP64 operator; the launch returns at
-// once when *skip != 0 (skip may be null).
-void skewer_apply_f64(ds_operator* op, bool residual, const double* v, double* out,
-                      const int* skip, cudaStream_t st);
 
 }  // namespace ds

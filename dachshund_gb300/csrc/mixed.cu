@@ -380,7 +380,7 @@ __global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero
   const int s = blockIdx.x, k = threadIdx.x;
   const int slot = s * n_per + k;
   const int rec = crec ? crec[slot] : slot;
-  const int pos = rec >= 0 ? inv[rec] : -1;
+  const int pos = rec < 0 ? -1 : inv ? inv[rec] : rec;  // inv null: record order
   double rd = 0.0;
   float ri = 0.f;
   if (pos >= 0) {
@@ -584,27 +584,55 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   DS_CUDA(cudaEventRecord(ev0, st));
 
   const int g = vgrid(np);
+  // With the structured inner operator (skewers on one z grid) the whole
+  // solve runs in record order: the structured kernels and the cluster
+  // preconditioner then read and write whole skewers' runs of the vectors
+  // instead of scattered sorted positions.  X, B, PD and POS are the
+  // solution, right-hand side, Jacobi diagonal and record -> index map of the
+  // order in use; x is converted in at the start and out at the end.
+  const bool use_sg = op->sgrid && (op->inner_variant == INNER_AUTO ||
+                                    op->inner_variant == INNER_STRUCTURED);
+  SkewerVecs sv{};
+  double* X = op->x.p;
+  const double* B = op->b.p;
+  const float* PD = f.pdiag.p;
+  const int* POS = op->inv.p;
+  if (use_sg) {
+    ensure_skewer_inner(op, f.inner_cut);
+    sv = skewer_vecs_rec(op, f.pdiag.p);
+    X = op->sgrid->rx.p;
+    B = sv.b;
+    PD = op->sgrid->rpd.p;
+    POS = nullptr;
+    skewer_x_to_rec(op, op->x.p, X, st);
+    // q is written on the records' indices only: its padding is cleared here
+    DS_CUDA(cudaMemsetAsync(f.q.p, 0, np * sizeof(float), st));
+  } else if (op->sgrid) {
+    sv = skewer_vecs_sorted(op);
+  }
   // r64 = b - A x0: nothing when x0 == 0 (then r64 = b); else first with the
   // FP32 operator, then FP64-accurate only when that one is near tol.
-  // the structured FP64 residual writes the records' positions only: the
+  // the structured FP64 residual writes the records' indices only: the
   // padding of r64 is cleared here, before anything writes r64
   if (op->sgrid) DS_CUDA(cudaMemsetAsync(op->r.p, 0, np * sizeof(double), st));
-  k_is_zero<<<g, VB, 0, st>>>(np, op->x.p, xzero);
+  k_is_zero<<<g, VB, 0, st>>>(np, X, xzero);
   DS_CHECK_LAUNCH();
-  k_x_to_f32<<<g, VB, 0, st>>>(np, xzero, op->x.p, f.p.p);
+  k_x_to_f32<<<g, VB, 0, st>>>(np, xzero, X, f.p.p);
   DS_CHECK_LAUNCH();
-  {
+  if (use_sg) {
+    skewer_product_f32(op, sv, f.p.p, f.q.p, nullptr, nullptr, nullptr, nullptr, xzero, st);
+  } else {
     F32Args a0 = op_f32_args(op, f.p.p, f.q.p);
     a0.skip_flag = xzero;
     launch_pair_f32(f.formula, EPI_PRODUCT, a0, st);
   }
-  k_r32_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, f.q.p, op->r.p, op->partial.p);
+  k_r32_init<<<g, VB, 0, st>>>(np, S, xzero, B, f.q.p, op->r.p, op->partial.p);
   DS_CHECK_LAUNCH();
-  PairArgs resid = op_pair_args(op, op->x.p, op->r.p);
+  PairArgs resid = op_pair_args(op, X, op->r.p);
   resid.skip_flag = &S->init_skip;
   auto outer_residual = [&](const PairArgs& pa) {
     if (op->sgrid)
-      skewer_apply_f64(op, true, pa.v, pa.out, pa.skip_flag, st);
+      skewer_apply_f64(op, sv, true, pa.v, pa.out, pa.skip_flag, st);
     else if (f.use_ff)
       launch_pair_ff_resid(op->kc, pa, f.ffd.view, st);
     else
@@ -621,12 +649,12 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     for (float* v : {f.z.p, f.r.p, f.p.p})
       DS_CUDA(cudaMemsetAsync(v, 0, np * sizeof(float), st));
     k_pc_iter<2><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-        pc->n_per, pc->band, S, xzero, pc->crec.p, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p,
-        f.p.p, nullptr, op->b.p, op->r.p, pc_part, f.hist.p, f.htrue.p);
+        pc->n_per, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, f.r.p, f.z.p, f.p.p,
+        nullptr, B, op->r.p, pc_part, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   } else {
-    k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, op->b.p, op->r.p, f.r.p, f.z.p, f.p.p,
-                                f.pdiag.p, op->partial.p, f.hist.p, f.htrue.p);
+    k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, B, op->r.p, f.r.p, f.z.p, f.p.p, PD,
+                                op->partial.p, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   }
 
@@ -638,7 +666,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   prod.alpha_out = &S->alpha;
   prod.den_out = &S->pq;
   prod.skip_flag = &S->done;
-  PairArgs upd = op_pair_args(op, op->x.p, op->r.p);
+  PairArgs upd = op_pair_args(op, X, op->r.p);
   upd.skip_flag = &S->skip_update;
   if (!f.tc_err.p) {
     f.tc_err.alloc(1);
@@ -654,14 +682,6 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // T / S buffers in the 512 TMEM columns).
   const bool use_tc =
       op->inner_variant == INNER_TENSOR && pair_tc_usable(f.formula, EPI_PRODUCT, prod);
-  // the structured inner operator (skewers on one z grid): q is written on
-  // the records' positions only, so its padding is cleared once here
-  const bool use_sg = op->sgrid && (op->inner_variant == INNER_AUTO ||
-                                    op->inner_variant == INNER_STRUCTURED);
-  if (use_sg) {
-    ensure_skewer_inner(op, f.inner_cut);
-    DS_CUDA(cudaMemsetAsync(f.q.p, 0, np * sizeof(float), st));
-  }
 
   // One iteration: K1 (q = A32 p, p.q, alpha), K2 (x, r updates, z = M^-1 r,
   // r.z, update test), K5 (FP64-accurate residual when an update is due),
@@ -669,7 +689,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // the solve is done, so iterations launched past the end change nothing.
   auto iteration = [&]() {
     if (use_sg)
-      skewer_product_f32(op, prod.v, prod.out, prod.counter, prod.num, prod.alpha_out,
+      skewer_product_f32(op, sv, prod.v, prod.out, prod.counter, prod.num, prod.alpha_out,
                          prod.den_out, prod.skip_flag, st);                  // K1
     else if (use_tc)
       launch_pair_tc(prod, st);                                               // K1
@@ -677,23 +697,23 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);
     if (pc) {
       k_pc_iter<0><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, pc->crec.p, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p,
-          f.p.p, f.q.p, nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);      // K2
+          pc->n_per, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, f.r.p, f.z.p, f.p.p,
+          f.q.p, nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);             // K2
       DS_CHECK_LAUNCH();
     } else {
-      k_mx_update<<<g, VB, 0, st>>>(np, S, op->x.p, f.r.p, f.z.p, f.p.p, f.q.p, f.pdiag.p,
-                                    op->partial.p, f.hist.p);                // K2
+      k_mx_update<<<g, VB, 0, st>>>(np, S, X, f.r.p, f.z.p, f.p.p, f.q.p, PD, op->partial.p,
+                                    f.hist.p);                               // K2
       DS_CHECK_LAUNCH();
     }
     outer_residual(upd);                                                      // K5
     if (pc) {
       k_pc_iter<1><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, pc->crec.p, op->inv.p, pc->L.p, op->x.p, f.r.p, f.z.p,
-          f.p.p, nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);    // K6
+          pc->n_per, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, f.r.p, f.z.p, f.p.p,
+          nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);           // K6
       DS_CHECK_LAUNCH();
     } else {
-      k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, f.pdiag.p, op->partial.p,
-                                     f.hist.p, f.htrue.p);                   // K6
+      k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, PD, op->partial.p, f.hist.p,
+                                     f.htrue.p);                             // K6
       DS_CHECK_LAUNCH();
     }
     k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K7
@@ -754,6 +774,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     launch_counter() += (long long)std::max(replays - 1, 0) * per_graph;
     cudaGraphExecDestroy(gexec);
   }
+  if (use_sg) skewer_x_to_sorted(op, X, op->x.p, st);
   DS_CUDA(cudaEventRecord(ev1, st));
   DS_CUDA(cudaMemcpyAsync(&h, S, sizeof(h), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));

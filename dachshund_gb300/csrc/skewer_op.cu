@@ -88,7 +88,7 @@ __global__ void k_sg_levels(int n_per, int lmax, size_t n, const int* __restrict
   extern __shared__ double su[];
   const int k = threadIdx.x;
   const size_t r = (size_t)blockIdx.x * n_per + k;
-  const int p = pos[r];
+  const size_t p = pos ? (size_t)pos[r] : r;
   const double u = wr[p] * v[p];
   su[k] = u;
   __syncthreads();
@@ -117,10 +117,10 @@ __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
   __shared__ double s_p[NB_CHUNK];
   const int a = blockIdx.x, k = threadIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
-  const double acc = nbr_sum<double>(q0, q1, nb_idx, nb_lev, nb_p, 0, n, n_per, V, k, true,
+  const double acc = nbr_sum<double>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, k, true,
                                      s_off, s_p);
   const size_t r = (size_t)a * n_per + k;
-  const int p = pos[r];
+  const size_t p = pos ? (size_t)pos[r] : r;
   const double y = fma(wl[p], acc, e[p] * v[p]);
   out[p] = RESID ? bvec[p] - y : y;
   if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
@@ -135,7 +135,7 @@ __global__ void k_sg32_levels(int n_per, int lmax, size_t n, const int* __restri
   extern __shared__ float sf[];
   const int k = threadIdx.x;
   const size_t r = (size_t)blockIdx.x * n_per + k;
-  const int ps = pos[r];
+  const size_t ps = pos ? (size_t)pos[r] : r;
   const float u = (float)wr[ps] * p[ps];
   sf[k] = u;
   __syncthreads();
@@ -181,10 +181,10 @@ __global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr
   __shared__ float s_p[NB_CHUNK];
   const int a = blockIdx.x, k = threadIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
-  const float acc = nbr_sum<float>(q0, q1, nb_idx, nb_lev, nb_p, 0, n, n_per, V, k, true,
+  const float acc = nbr_sum<float>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, k, true,
                                    s_off, s_p);
   const size_t r = (size_t)a * n_per + k;
-  const int ps = pos[r];
+  const size_t ps = pos ? (size_t)pos[r] : r;
   const float pv = p[ps];
   const float qv = fmaf((float)wl[ps], acc, (float)e[ps] * pv);
   q[ps] = qv;
@@ -282,100 +282,172 @@ __global__ void k_mc_apply(int n_sk, int nz, const int* __restrict__ ptr,
   if (prof_terms && j == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * nz);
 }
 
-// Skewer pairs within `cut` (cell lists of side sqrt(cut / c_perp)).
-void build_nbrs(SkewerNbrs& nb, const std::vector<double>& sx, const std::vector<double>& sy,
-                const std::vector<double>& zd, const KernelConsts& kc, double cut, int n_per,
-                cudaStream_t st) {
-  const int n_sk = (int)sx.size();
-  nb.cut = cut;
-  const double h = std::sqrt(cut / kc.c_perp);
-  const double x0 = *std::min_element(sx.begin(), sx.end());
-  const double y0 = *std::min_element(sy.begin(), sy.end());
-  const double x1 = *std::max_element(sx.begin(), sx.end());
-  const double y1 = *std::max_element(sy.begin(), sy.end());
-  const int ncx = std::max(1, (int)std::min(4096.0, std::floor((x1 - x0) / h) + 1));
-  const int ncy = std::max(1, (int)std::min(4096.0, std::floor((y1 - y0) / h) + 1));
-  auto cell_of = [&](double v, double o, int nc) {
-    return std::min(nc - 1, std::max(0, (int)std::floor((v - o) / h)));
-  };
-  std::vector<std::vector<int>> cells((size_t)ncx * ncy);
-  for (int s = 0; s < n_sk; ++s)
-    cells[(size_t)cell_of(sy[s], y0, ncy) * ncx + cell_of(sx[s], x0, ncx)].push_back(s);
-  std::vector<int> ptr(n_sk + 1, 0), idx, lev;
-  std::vector<double> p64;
-  std::vector<std::pair<int, double>> row;
-  nb.lmax = 0;
-  nb.n_terms = 0;
-  for (int a = 0; a < n_sk; ++a) {
-    const int cx = cell_of(sx[a], x0, ncx), cy = cell_of(sy[a], y0, ncy);
-    row.clear();
-    for (int jy = std::max(0, cy - 1); jy <= std::min(ncy - 1, cy + 1); ++jy)
-      for (int jx = std::max(0, cx - 1); jx <= std::min(ncx - 1, cx + 1); ++jx)
-        for (int b : cells[(size_t)jy * ncx + jx]) {
-          const double dx = sx[a] - sx[b], dy = sy[a] - sy[b];
-          const double parg = kc.c_perp * (dx * dx + dy * dy);
-          if (parg < cut) row.push_back({b, parg});
-        }
-    std::sort(row.begin(), row.end());
-    for (const auto& bp : row) {
-      int L = 0;
-      while (L + 1 < n_per && bp.second + kc.c_para * (zd[L + 1] * zd[L + 1]) < cut) ++L;
-      idx.push_back(bp.first);
-      lev.push_back(L);
-      p64.push_back(kc.var_s * std::exp(-bp.second));
-      nb.lmax = std::max(nb.lmax, L);
-    }
-    ptr[a + 1] = (int)idx.size();
-    nb.n_terms += (long long)row.size() * n_per;
+// ---- neighbour lists (on the device) --------------------------------------------
+// Target t (a skewer or a map column at (tx, ty)) and source skewer b are
+// neighbours when c_perp |dxy|^2 + th[0] < cut; the entry keeps
+// lev = #{q < Q : c_perp |dxy|^2 + th[q] < cut} (th ascending: the z part of
+// the argument per level) and var_s exp(-c_perp |dxy|^2).  One warp per
+// target scans the sources in order, so each row is in ascending b.
+__global__ void k_list_count(int nt, const double* __restrict__ tx,
+                             const double* __restrict__ ty, int ns,
+                             const double* __restrict__ sx, const double* __restrict__ sy,
+                             double c_perp, double lim, int* __restrict__ cnt) {
+  const int t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= nt) return;
+  int c = 0;
+  for (int b = lane; b < ns; b += 32) {
+    const double dx = tx[t] - sx[b], dy = ty[t] - sy[b];
+    c += c_perp * (dx * dx + dy * dy) < lim;
   }
-  nb.ptr.alloc(ptr.size());
-  nb.idx.alloc(std::max<size_t>(1, idx.size()));
-  nb.lev.alloc(std::max<size_t>(1, lev.size()));
-  nb.p64.alloc(std::max<size_t>(1, p64.size()));
-  DS_CUDA(cudaMemcpyAsync(nb.ptr.p, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice,
-                          st));
-  DS_CUDA(cudaMemcpyAsync(nb.idx.p, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice,
-                          st));
-  DS_CUDA(cudaMemcpyAsync(nb.lev.p, lev.data(), lev.size() * sizeof(int), cudaMemcpyHostToDevice,
-                          st));
-  DS_CUDA(cudaMemcpyAsync(nb.p64.p, p64.data(), p64.size() * sizeof(double),
-                          cudaMemcpyHostToDevice, st));
-  std::vector<float> p32(p64.begin(), p64.end());
-  nb.p32.alloc(std::max<size_t>(1, p32.size()));
-  DS_CUDA(cudaMemcpyAsync(nb.p32.p, p32.data(), p32.size() * sizeof(float),
-                          cudaMemcpyHostToDevice, st));
-  DS_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if (lane == 0) cnt[t] = c;
 }
+
+__global__ void k_list_fill(int nt, const double* __restrict__ tx, const double* __restrict__ ty,
+                            int ns, const double* __restrict__ sx,
+                            const double* __restrict__ sy, double c_perp, double cut,
+                            double var_s, int Q, const double* __restrict__ th,
+                            const int* __restrict__ ptr, int* __restrict__ idx,
+                            int* __restrict__ lev, double* __restrict__ p64,
+                            float* __restrict__ p32) {
+  const int t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= nt) return;
+  int base = ptr[t];
+  for (int b0 = 0; b0 < ns; b0 += 32) {
+    const int b = b0 + lane;
+    double parg = 0.0;
+    bool ok = false;
+    if (b < ns) {
+      const double dx = tx[t] - sx[b], dy = ty[t] - sy[b];
+      parg = c_perp * (dx * dx + dy * dy);
+      ok = parg + th[0] < cut;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const int at = base + __popc(m & ((1u << lane) - 1u));
+      int L = 0;
+      while (L < Q && parg + th[L] < cut) ++L;
+      const double pv = var_s * exp(-parg);
+      idx[at] = b;
+      lev[at] = L;
+      p64[at] = pv;
+      if (p32) p32[at] = (float)pv;
+    }
+    base += __popc(m);
+  }
+}
+
+// Skewer (x, y) and skewer 0's z values, then a flag for any record not at
+// its skewer's (x, y) or not at skewer 0's k-th z.
+__global__ void k_sk_info(int n_sk, int n_per, const int* __restrict__ inv,
+                          const double* __restrict__ px, const double* __restrict__ py,
+                          const double* __restrict__ pz, double* __restrict__ sx,
+                          double* __restrict__ sy, double* __restrict__ z) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_sk) {
+    const int p = inv[(size_t)i * n_per];
+    sx[i] = px[p];
+    sy[i] = py[p];
+  }
+  if (i < n_per) z[i] = pz[inv[i]];
+}
+
+__global__ void k_sk_check(size_t n, int n_per, const int* __restrict__ inv,
+                           const double* __restrict__ px, const double* __restrict__ py,
+                           const double* __restrict__ pz, const double* __restrict__ sx,
+                           const double* __restrict__ sy, const double* __restrict__ z,
+                           int* __restrict__ bad) {
+  const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int s = (int)(r / n_per), k = (int)(r % n_per);
+  const int p = inv[r];
+  if (px[p] != sx[s] || py[p] != sy[s] || pz[p] != z[k]) atomicOr(bad, 1);
+}
+
+}  // namespace
+
+// CSR lists of targets against skewers for the z thresholds th[0..Q) (see
+// k_list_fill); returns the number of entries.
+static long long build_lists(int nt, const double* tx, const double* ty, int ns,
+                             const double* sx, const double* sy, const KernelConsts& kc,
+                             double cut, const std::vector<double>& th, DevBuf<int>& ptr,
+                             DevBuf<int>& idx, DevBuf<int>& lev, DevBuf<double>& p64,
+                             DevBuf<float>* p32, cudaStream_t st) {
+  const int Q = (int)th.size();
+  DevBuf<double> dth;
+  DevBuf<int> cnt;
+  dth.alloc(Q);
+  cnt.alloc(nt);
+  DS_CUDA(cudaMemcpyAsync(dth.p, th.data(), Q * sizeof(double), cudaMemcpyHostToDevice, st));
+  const unsigned blocks = (unsigned)((nt + 7) / 8);  // 8 warps per CTA
+  k_list_count<<<blocks, 256, 0, st>>>(nt, tx, ty, ns, sx, sy, kc.c_perp, cut - th[0], cnt.p);
+  DS_CHECK_LAUNCH();
+  std::vector<int> h(nt + 1, 0);
+  DS_CUDA(cudaMemcpyAsync(h.data() + 1, cnt.p, nt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  for (int t = 0; t < nt; ++t) h[t + 1] += h[t];
+  const long long total = h[nt];
+  ptr.alloc(nt + 1);
+  idx.alloc(std::max<long long>(1, total));
+  lev.alloc(std::max<long long>(1, total));
+  p64.alloc(std::max<long long>(1, total));
+  if (p32) p32->alloc(std::max<long long>(1, total));
+  DS_CUDA(cudaMemcpyAsync(ptr.p, h.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  k_list_fill<<<blocks, 256, 0, st>>>(nt, tx, ty, ns, sx, sy, kc.c_perp, cut, kc.var_s, Q, dth.p,
+                                      ptr.p, idx.p, lev.p, p64.p, p32 ? p32->p : nullptr);
+  DS_CHECK_LAUNCH();
+  DS_CUDA(cudaStreamSynchronize(st));  // h, dth, cnt go out of scope
+  return total;
+}
+
+// Skewer pairs within `cut`: z thresholds c_para (z_m - z_0)^2 below cut.
+static void build_nbrs(SkewerGrid& g, SkewerNbrs& nb, const KernelConsts& kc, double cut,
+                       cudaStream_t st) {
+  std::vector<double> th;
+  for (int m = 0; m < g.n_per && kc.c_para * g.zd[m] * g.zd[m] < cut; ++m)
+    th.push_back(kc.c_para * g.zd[m] * g.zd[m]);
+  nb.cut = cut;
+  nb.lmax = (int)th.size() - 1;  // the pair (a, a) keeps every level
+  const long long total = build_lists(g.n_sk, g.sx.p, g.sy.p, g.n_sk, g.sx.p, g.sy.p, kc, cut,
+                                      th, nb.ptr, nb.idx, nb.lev, nb.p64, &nb.p32, st);
+  nb.n_terms = total * g.n_per;
+}
+
+namespace {
 
 void build_skewer_grid(ds_operator* op, int n_sk, int n_per) {
   require(op->kc.eval == DS_EVAL_EXACT, "the structured operator needs the exact kernel");
   require(n_sk > 0 && n_per > 0 && n_per <= 1024 && (long long)n_sk * n_per == op->n,
           "n_skewers x n_per must equal the operator's record count (n_per <= 1024)");
   cudaStream_t st = op->ctx->stream;
-  const int n = op->n, np = op->pix.n_pad;
-  std::vector<double> hx(np), hy(np), hz(np);
-  std::vector<int> hinv(n);
-  DS_CUDA(cudaMemcpyAsync(hx.data(), op->pix.x.p, np * sizeof(double),
-                          cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(hy.data(), op->pix.y.p, np * sizeof(double),
-                          cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(hz.data(), op->pix.z.p, np * sizeof(double),
-                          cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(hinv.data(), op->inv.p, n * sizeof(int), cudaMemcpyDeviceToHost, st));
+  const size_t n = (size_t)op->n;
+  std::unique_ptr<SkewerGrid, SkewerGridDeleter> g(new SkewerGrid());
+  g->n_sk = n_sk;
+  g->n_per = n_per;
+  // every skewer at one (x, y), all on skewer 0's z values (checked on the device)
+  DevBuf<double> dz;
+  DevBuf<int> bad;
+  g->sx.alloc(n_sk);
+  g->sy.alloc(n_sk);
+  dz.alloc(n_per);
+  bad.alloc(1);
+  DS_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+  const int ni = std::max(n_sk, n_per);
+  k_sk_info<<<(ni + 255) / 256, 256, 0, st>>>(n_sk, n_per, op->inv.p, op->pix.x.p, op->pix.y.p,
+                                               op->pix.z.p, g->sx.p, g->sy.p, dz.p);
+  DS_CHECK_LAUNCH();
+  k_sk_check<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, n_per, op->inv.p, op->pix.x.p,
+                                                           op->pix.y.p, op->pix.z.p, g->sx.p,
+                                                           g->sy.p, dz.p, bad.p);
+  DS_CHECK_LAUNCH();
+  std::vector<double> z(n_per);
+  int hbad = 0;
+  DS_CUDA(cudaMemcpyAsync(z.data(), dz.p, n_per * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
-  // every skewer at one (x, y), all on skewer 0's z values
-  std::vector<double> sx(n_sk), sy(n_sk), z(n_per);
-  for (int k = 0; k < n_per; ++k) z[k] = hz[hinv[k]];
-  for (int s = 0; s < n_sk; ++s) {
-    const int p0 = hinv[(size_t)s * n_per];
-    sx[s] = hx[p0];
-    sy[s] = hy[p0];
-    for (int k = 0; k < n_per; ++k) {
-      const int p = hinv[(size_t)s * n_per + k];
-      require(hx[p] == sx[s] && hy[p] == sy[s] && hz[p] == z[k],
-              "structured operator: records must be skewers (one x, y each) on one z grid");
-    }
-  }
+  require(!hbad, "structured operator: records must be skewers (one x, y each) on one z grid");
   // a uniform grid: (z_{k+m} - z_k) gives the same argument as z_m - z_0 to
   // 1e-13 (so each Toeplitz tap is the entry's own value to ~1e-13)
   std::vector<double> zd(n_per);
@@ -390,33 +462,31 @@ void build_skewer_grid(ds_operator* op, int n_sk, int n_per) {
               "structured operator: the z grid is not uniform");
     }
   }
-  std::unique_ptr<SkewerGrid, SkewerGridDeleter> g(new SkewerGrid());
-  g->n_sk = n_sk;
-  g->n_per = n_per;
   g->z0 = z[0];
   g->dz = n_per > 1 ? zd[1] : 0.0;
+  g->zd = std::move(zd);
   std::vector<double> taps(n_per);
-  for (int m = 0; m < n_per; ++m) taps[m] = std::exp(-op->kc.c_para * zd[m] * zd[m]);
+  std::vector<float> t32(n_per);
+  for (int m = 0; m < n_per; ++m) {
+    taps[m] = std::exp(-op->kc.c_para * g->zd[m] * g->zd[m]);
+    t32[m] = (float)taps[m];
+  }
   g->taps64.alloc(n_per);
+  g->taps32.alloc(n_per);
   DS_CUDA(cudaMemcpyAsync(g->taps64.p, taps.data(), n_per * sizeof(double),
                           cudaMemcpyHostToDevice, st));
-  build_nbrs(g->outer, sx, sy, zd, op->kc, op->kc.exact_cut, n_per, st);
-  g->V64.alloc((size_t)(g->outer.lmax + 1) * n);
-  std::vector<float> t32(taps.begin(), taps.end());
-  g->taps32.alloc(n_per);
   DS_CUDA(cudaMemcpyAsync(g->taps32.p, t32.data(), n_per * sizeof(float),
                           cudaMemcpyHostToDevice, st));
-  DS_CUDA(cudaStreamSynchronize(st));
-  g->sx = std::move(sx);
-  g->sy = std::move(sy);
-  g->zd = std::move(zd);
+  build_nbrs(*g, g->outer, op->kc, op->kc.exact_cut, st);
+  g->V64.alloc((size_t)(g->outer.lmax + 1) * n);
+  DS_CUDA(cudaStreamSynchronize(st));  // taps, t32 go out of scope
   op->sgrid = std::move(g);
 }
 
 }  // namespace
 
-void skewer_apply_f64(ds_operator* op, bool residual, const double* v, double* out,
-                      const int* skip, cudaStream_t st) {
+void skewer_apply_f64(ds_operator* op, const SkewerVecs& c, bool residual, const double* v,
+                      double* out, const int* skip, cudaStream_t st) {
   SkewerGrid& g = *op->sgrid;
   const size_t n = (size_t)op->n;
   Profiler& pr = op->ctx->prof;
@@ -427,20 +497,83 @@ void skewer_apply_f64(ds_operator* op, bool residual, const double* v, double* o
     pr.begin(st, &ev);
   }
   k_sg_levels<<<g.n_sk, g.n_per, g.n_per * sizeof(double), st>>>(
-      g.n_per, g.outer.lmax, n, op->inv.p, op->wr.p, v, g.taps64.p, g.V64.p, skip);
+      g.n_per, g.outer.lmax, n, c.pos, c.wr, v, g.taps64.p, g.V64.p, skip);
   DS_CHECK_LAUNCH();
   if (residual)
     k_sg_apply<true><<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.outer.ptr.p, g.outer.idx.p,
-                                                 g.outer.lev.p, g.outer.p64.p, g.V64.p,
-                                                 op->inv.p, op->wl.p, op->e.p, v, op->b.p, out,
-                                                 skip, prof_terms);
+                                                 g.outer.lev.p, g.outer.p64.p, g.V64.p, c.pos,
+                                                 c.wl, c.e, v, c.b, out, skip, prof_terms);
   else
     k_sg_apply<false><<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.outer.ptr.p, g.outer.idx.p,
-                                                  g.outer.lev.p, g.outer.p64.p, g.V64.p,
-                                                  op->inv.p, op->wl.p, op->e.p, v, op->b.p, out,
-                                                  skip, prof_terms);
+                                                  g.outer.lev.p, g.outer.p64.p, g.V64.p, c.pos,
+                                                  c.wl, c.e, v, c.b, out, skip, prof_terms);
   DS_CHECK_LAUNCH();
   if (ev) pr.end(st, ev, 0);
+}
+
+// Record-order copies of the operator's coefficients and right-hand side
+// (record r at index r, padding 1 in pdiag and 0 elsewhere), for the mixed
+// solve in record order.
+__global__ void k_sg_rec_coeffs(int n, int n_pad, const int* __restrict__ inv,
+                                const double* __restrict__ wl, const double* __restrict__ wr,
+                                const double* __restrict__ e, const double* __restrict__ b,
+                                const float* __restrict__ pd, double* __restrict__ rwl,
+                                double* __restrict__ rwr, double* __restrict__ re,
+                                double* __restrict__ rb, float* __restrict__ rpd) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_pad) return;
+  if (r < n) {
+    const int p = inv[r];
+    rwl[r] = wl[p];
+    rwr[r] = wr[p];
+    re[r] = e[p];
+    rb[r] = b[p];
+    rpd[r] = pd[p];
+  } else {
+    rwl[r] = rwr[r] = re[r] = rb[r] = 0.0;
+    rpd[r] = 1.f;
+  }
+}
+
+__global__ void k_sg_to_rec(int n, int n_pad, const int* __restrict__ inv,
+                            const double* __restrict__ sorted, double* __restrict__ rec) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_pad) rec[r] = r < n ? sorted[inv[r]] : 0.0;
+}
+
+__global__ void k_sg_to_sorted(int n, const int* __restrict__ inv, const double* __restrict__ rec,
+                               double* __restrict__ sorted) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) sorted[inv[r]] = rec[r];
+}
+
+SkewerVecs skewer_vecs_rec(ds_operator* op, const float* pdiag_sorted) {
+  SkewerGrid& g = *op->sgrid;
+  const int np = op->pix.n_pad;
+  if (!g.rb.p) {
+    g.rwl.alloc(np);
+    g.rwr.alloc(np);
+    g.re.alloc(np);
+    g.rb.alloc(np);
+    g.rpd.alloc(np);
+    g.rx.alloc(np);
+    k_sg_rec_coeffs<<<(np + 255) / 256, 256, 0, op->ctx->stream>>>(
+        op->n, np, op->inv.p, op->wl.p, op->wr.p, op->e.p, op->b.p, pdiag_sorted, g.rwl.p,
+        g.rwr.p, g.re.p, g.rb.p, g.rpd.p);
+    DS_CHECK_LAUNCH();
+  }
+  return SkewerVecs{nullptr, g.rwl.p, g.rwr.p, g.re.p, g.rb.p};
+}
+
+void skewer_x_to_rec(ds_operator* op, const double* x_sorted, double* x_rec, cudaStream_t st) {
+  const int np = op->pix.n_pad;
+  k_sg_to_rec<<<(np + 255) / 256, 256, 0, st>>>(op->n, np, op->inv.p, x_sorted, x_rec);
+  DS_CHECK_LAUNCH();
+}
+
+void skewer_x_to_sorted(ds_operator* op, const double* x_rec, double* x_sorted, cudaStream_t st) {
+  k_sg_to_sorted<<<(op->n + 255) / 256, 256, 0, st>>>(op->n, op->inv.p, x_rec, x_sorted);
+  DS_CHECK_LAUNCH();
 }
 
 // Distance classes, pixel windows and column -> skewer lists of a column
@@ -492,45 +625,12 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
     }
   std::vector<double> taps(Q);
   for (int q = 0; q < Q; ++q) taps[q] = std::exp(-kc.c_para * cls_d[q] * cls_d[q]);
-  // column -> skewer lists (cell lists over the skewers)
+  // column -> skewer lists (z thresholds: the distance classes)
+  std::vector<double> th(Q);
+  for (int q = 0; q < Q; ++q) th[q] = kc.c_para * cls_d[q] * cls_d[q];
+  build_lists(mc.ncol, mc.cx.p, mc.cy.p, g.n_sk, g.sx.p, g.sy.p, kc, cut, th, mc.ptr, mc.idx,
+              mc.lev, mc.p64, nullptr, st);
   const int n_sk = g.n_sk;
-  const double h = std::sqrt(cut / kc.c_perp);
-  const double x0 = *std::min_element(g.sx.begin(), g.sx.end());
-  const double y0 = *std::min_element(g.sy.begin(), g.sy.end());
-  const double x1 = *std::max_element(g.sx.begin(), g.sx.end());
-  const double y1 = *std::max_element(g.sy.begin(), g.sy.end());
-  const int ncx = std::max(1, (int)std::min(4096.0, std::floor((x1 - x0) / h) + 1));
-  const int ncy = std::max(1, (int)std::min(4096.0, std::floor((y1 - y0) / h) + 1));
-  auto cell_of = [&](double v, double o, int nc) {
-    return std::min(nc - 1, std::max(0, (int)std::floor((v - o) / h)));
-  };
-  std::vector<std::vector<int>> cells((size_t)ncx * ncy);
-  for (int s = 0; s < n_sk; ++s)
-    cells[(size_t)cell_of(g.sy[s], y0, ncy) * ncx + cell_of(g.sx[s], x0, ncx)].push_back(s);
-  std::vector<int> ptr(mc.ncol + 1, 0), idx, lev;
-  std::vector<double> p64;
-  std::vector<std::pair<int, double>> row;
-  for (int c = 0; c < mc.ncol; ++c) {
-    const int qx = cell_of(mc.cx[c], x0, ncx), qy = cell_of(mc.cy[c], y0, ncy);
-    row.clear();
-    for (int jy = std::max(0, qy - 1); jy <= std::min(ncy - 1, qy + 1); ++jy)
-      for (int jx = std::max(0, qx - 1); jx <= std::min(ncx - 1, qx + 1); ++jx)
-        for (int b : cells[(size_t)jy * ncx + jx]) {
-          const double dx = mc.cx[c] - g.sx[b], dy = mc.cy[c] - g.sy[b];
-          const double parg = kc.c_perp * (dx * dx + dy * dy);
-          if (parg < cut) row.push_back({b, parg});
-        }
-    std::sort(row.begin(), row.end());
-    for (const auto& bp : row) {
-      int L = 0;
-      while (L < Q && bp.second + kc.c_para * cls_d[L] * cls_d[L] < cut) ++L;
-      if (L == 0) continue;
-      idx.push_back(bp.first);
-      lev.push_back(L);
-      p64.push_back(kc.var_s * std::exp(-bp.second));
-    }
-    ptr[c + 1] = (int)idx.size();
-  }
   mc.Q = Q;
   mc.W = W;
   mc.cut = cut;
@@ -538,24 +638,12 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
   mc.kstart.alloc(nz);
   mc.cls.alloc(cls.size());
   mc.taps.alloc(Q);
-  mc.ptr.alloc(ptr.size());
-  mc.idx.alloc(std::max<size_t>(1, idx.size()));
-  mc.lev.alloc(std::max<size_t>(1, lev.size()));
-  mc.p64.alloc(std::max<size_t>(1, p64.size()));
   mc.R.alloc((size_t)Q * n_sk * nz);
   DS_CUDA(cudaMemcpyAsync(mc.kstart.p, kstart.data(), nz * sizeof(int), cudaMemcpyHostToDevice,
                           st));
   DS_CUDA(cudaMemcpyAsync(mc.cls.p, cls.data(), cls.size(), cudaMemcpyHostToDevice, st));
   DS_CUDA(cudaMemcpyAsync(mc.taps.p, taps.data(), Q * sizeof(double), cudaMemcpyHostToDevice,
                           st));
-  DS_CUDA(cudaMemcpyAsync(mc.ptr.p, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice,
-                          st));
-  DS_CUDA(cudaMemcpyAsync(mc.idx.p, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice,
-                          st));
-  DS_CUDA(cudaMemcpyAsync(mc.lev.p, lev.data(), lev.size() * sizeof(int), cudaMemcpyHostToDevice,
-                          st));
-  DS_CUDA(cudaMemcpyAsync(mc.p64.p, p64.data(), p64.size() * sizeof(double),
-                          cudaMemcpyHostToDevice, st));
   DS_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
 }
 
@@ -586,14 +674,18 @@ bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, doubl
 void ensure_skewer_inner(ds_operator* op, double inner_cut) {
   SkewerGrid& g = *op->sgrid;
   if (g.inner.ptr.p && g.inner.cut == inner_cut) return;
-  build_nbrs(g.inner, g.sx, g.sy, g.zd, op->kc, inner_cut, g.n_per, op->ctx->stream);
+  build_nbrs(g, g.inner, op->kc, inner_cut, op->ctx->stream);
   g.V32.alloc((size_t)(g.inner.lmax + 1) * op->n);
   g.dot_part.alloc(g.n_sk);
 }
 
-void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int* counter,
-                        const double* num, double* alpha_out, double* den_out,
-                        const int* skip, cudaStream_t st) {
+SkewerVecs skewer_vecs_sorted(ds_operator* op) {
+  return SkewerVecs{op->inv.p, op->wl.p, op->wr.p, op->e.p, op->b.p};
+}
+
+void skewer_product_f32(ds_operator* op, const SkewerVecs& c, const float* p, float* q,
+                        unsigned int* counter, const double* num, double* alpha_out,
+                        double* den_out, const int* skip, cudaStream_t st) {
   SkewerGrid& g = *op->sgrid;
   const size_t n = (size_t)op->n;
   Profiler& pr = op->ctx->prof;
@@ -604,13 +696,12 @@ void skewer_product_f32(ds_operator* op, const float* p, float* q, unsigned int*
     pr.begin(st, &ev);
   }
   k_sg32_levels<<<g.n_sk, g.n_per, g.n_per * sizeof(float), st>>>(
-      g.n_per, g.inner.lmax, n, op->inv.p, op->wr.p, p, g.taps32.p, g.V32.p, skip);
+      g.n_per, g.inner.lmax, n, c.pos, c.wr, p, g.taps32.p, g.V32.p, skip);
   DS_CHECK_LAUNCH();
   k_sg32_apply<<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.inner.ptr.p, g.inner.idx.p,
-                                           g.inner.lev.p, g.inner.p32.p, g.V32.p, op->inv.p,
-                                           op->wl.p, op->e.p, p, q,
-                                           counter ? g.dot_part.p : nullptr, counter, num,
-                                           alpha_out, den_out, skip, prof_terms);
+                                           g.inner.lev.p, g.inner.p32.p, g.V32.p, c.pos, c.wl,
+                                           c.e, p, q, counter ? g.dot_part.p : nullptr, counter,
+                                           num, alpha_out, den_out, skip, prof_terms);
   DS_CHECK_LAUNCH();
   if (ev) pr.end(st, ev, 1);
 }
@@ -642,32 +733,27 @@ int ds_map_set_column_grid(ds_map* map, int n_columns, int nz) {
     require(n_columns > 0 && nz > 0 && (long long)n_columns * nz == map->pts.n,
             "n_columns x nz must equal the map's point count");
     cudaStream_t st = map->ctx->stream;
-    DevBuf<double> cx, cy, zj;
+    std::unique_ptr<MapColumns, MapColumnsDeleter> mc(new MapColumns());
+    mc->ncol = n_columns;
+    mc->nz = nz;
+    mc->z.resize(nz);
+    DevBuf<double> zj;
     DevBuf<int> bad;
-    cx.alloc(n_columns);
-    cy.alloc(n_columns);
+    mc->cx.alloc(n_columns);
+    mc->cy.alloc(n_columns);
     zj.alloc(nz);
     bad.alloc(1);
     DS_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
     const int np = map->pts.n_pad;
     k_mc_info<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->pts.perm.p, map->pts.x.p,
-                                                 map->pts.y.p, map->pts.z.p, cx.p, cy.p, zj.p);
+                                                 map->pts.y.p, map->pts.z.p, mc->cx.p, mc->cy.p,
+                                                 zj.p);
     DS_CHECK_LAUNCH();
     k_mc_check<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->pts.perm.p, map->pts.x.p,
-                                                  map->pts.y.p, map->pts.z.p, cx.p, cy.p, zj.p,
-                                                  bad.p);
+                                                  map->pts.y.p, map->pts.z.p, mc->cx.p,
+                                                  mc->cy.p, zj.p, bad.p);
     DS_CHECK_LAUNCH();
-    std::unique_ptr<MapColumns, MapColumnsDeleter> mc(new MapColumns());
-    mc->ncol = n_columns;
-    mc->nz = nz;
-    mc->cx.resize(n_columns);
-    mc->cy.resize(n_columns);
-    mc->z.resize(nz);
     int hbad = 0;
-    DS_CUDA(cudaMemcpyAsync(mc->cx.data(), cx.p, n_columns * sizeof(double),
-                            cudaMemcpyDeviceToHost, st));
-    DS_CUDA(cudaMemcpyAsync(mc->cy.data(), cy.p, n_columns * sizeof(double),
-                            cudaMemcpyDeviceToHost, st));
     DS_CUDA(cudaMemcpyAsync(mc->z.data(), zj.p, nz * sizeof(double), cudaMemcpyDeviceToHost,
                             st));
     DS_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -687,7 +773,8 @@ int ds_operator_skewer_product_dev(ds_operator* op, int residual, const double* 
     op->tmp.alloc(op->pix.n_pad);
     op->tmp2.alloc(op->pix.n_pad);
     gather_sorted(op->pix, v, op->tmp.p, st);
-    skewer_apply_f64(op, residual != 0, op->tmp.p, op->tmp2.p, nullptr, st);
+    skewer_apply_f64(op, skewer_vecs_sorted(op), residual != 0, op->tmp.p, op->tmp2.p, nullptr,
+                     st);
     scatter_sorted(op->pix, op->tmp2.p, nullptr, out, st);
   });
 }
