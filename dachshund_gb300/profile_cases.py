@@ -81,10 +81,14 @@ def main(argv=None):
             t0 = mark("column_grid", t0)
             m = grid.product_f32(op, x)
             t0 = mark("map_product", t0)
+            m = grid.product_f32(op, x)
+            t0 = mark("map_product_again", t0)
+            x, res = op.solve_mixed(MixedParams(max_iter=3000, tol=1e-8))
+            t0 = mark("solve_again", t0)
             grid.close()
             op.close()
             mark("close", t0)
-        print(case, "ms", t, "total", round(sum(t.values()), 2))
+        print(case, "ms", t)
     elif case == "chosen_step":
         from dachshund_gb300 import MapGrid
 
