@@ -125,6 +125,7 @@ struct OpF32 {
   PairList pairs;
   DevBuf<float> rowf, colw, ediag, pdiag;
   DevBuf<float> p, q, r, z;         // FP32 iteration vectors (sorted, padded)
+  DevBuf<float> r2;                 // second r buffer of the band preconditioner
   DevBuf<MixedState> state;
   DevBuf<double> hist, htrue;
   bool use_ff = false;  // outer residual in float-float arithmetic (else FP64)

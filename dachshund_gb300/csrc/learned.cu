@@ -847,7 +847,7 @@ int ds_operator_set_skewer_preconditioner(ds_operator* op, int n_skewers, int n_
     }
     require(n_skewers > 0 && n_per > 0 && n_per <= 1024 && (long long)n_skewers * n_per == op->n,
             "n_skewers x n_per must equal the operator's record count (n_per <= 1024)");
-    require(band >= 0 && band < n_per, "band must be in [0, n_per)");
+    require(band >= 0 && band < n_per && band <= 32, "band must be in [0, min(n_per, 33))");
     std::unique_ptr<SkewerPC, SkewerPCDeleter> pc(new SkewerPC());
     pc->n_sk = n_skewers;
     pc->n_per = n_per;

@@ -335,98 +335,99 @@ __global__ void __launch_bounds__(VB) k_mx_dir(int n, MixedState* st,
   }
 }
 
-// ---- band preconditioner (M^-1 = L L^T per block) -------------------------------
-// The same reliable-update iteration with z = M^-1 r over each block of
-// n_per slots (a skewer, or a cluster of neighbouring skewers in z order):
-// one CTA per block (thread k = slot k, the record crec[slot] or the slot
-// itself, at sorted position inv[record]) updates r, forms z = L L^T r from
-// the block's r in shared memory, writes the block's r.z and |r|^2 partials,
-// and the last CTA to finish does the scalar bookkeeping of K2 (MODE 0), K6
-// (MODE 1) or the start (MODE 2).  Padding positions belong to no block and
-// stay 0; padding slots (record -1) hold r = 0 and write nothing.
-
-// Sum of v over the CTA (any blockDim <= 1024), valid in thread 0.
-__device__ __forceinline__ double cta_sum(double v, double* sm) {
-  const int t = threadIdx.x, n = blockDim.x;
-  __syncthreads();
-  sm[t] = v;
-  __syncthreads();
-  if (t < 32) {
-    double a = 0.0;
-    for (int k = t; k < n; k += 32) a += sm[k];
-    sm[t] = a;
-  }
-  __syncthreads();
-  double s = 0.0;
-  if (t == 0)
-    for (int k = 0; k < min(32, n); ++k) s += sm[k];
-  return s;
-}
+// ---- band preconditioner (M^-1 = L L^T) ---------------------------------------
+// The same reliable-update iteration with z = M^-1 r for a band factor L in
+// slot order (a skewer per block of slots, or a cluster of neighbouring
+// skewers in z order; L has no entries between blocks, padding slots have
+// r = 0).  One thread per slot, PCB slots per CTA plus `band` halo slots on
+// each side: the CTA forms its slots' r (updated in MODE 0), t = L^T r on
+// its slots and the `band` before them, and z = L t on its own slots, writes
+// its (r.z, |r|^2) partials, and the last CTA to finish does the scalar
+// bookkeeping of K2 (MODE 0), K6 (MODE 1) or the start (MODE 2).  Slot ->
+// record (crec, or the slot itself) -> vector index (inv, or the record
+// itself in record order).
+constexpr int PCB = 256;       // slots per CTA
+constexpr int PC_MAX_BAND = 32;
 
 template <int MODE>
-__global__ void k_pc_iter(int n_per, int band, MixedState* st, const int* x_zero,
-                          const int* __restrict__ crec, const int* __restrict__ inv,
-                          const float* __restrict__ L,
-                          double* __restrict__ x, float* __restrict__ r,
-                          float* __restrict__ z, float* __restrict__ p,
-                          const float* __restrict__ q, const double* __restrict__ b,
-                          const double* __restrict__ r64, double* __restrict__ part, double* hist,
-                          double* htrue) {
+__global__ void __launch_bounds__(PCB) k_pc_iter(int n_slots, int band, MixedState* st,
+                                                 const int* x_zero, const int* __restrict__ crec,
+                                                 const int* __restrict__ inv,
+                                                 const float* __restrict__ L,
+                                                 double* __restrict__ x,
+                                                 const float* __restrict__ rin,
+                                                 float* __restrict__ rout, float* __restrict__ z,
+                                                 float* __restrict__ p,
+                                                 const float* __restrict__ q,
+                                                 const double* __restrict__ b,
+                                                 const double* __restrict__ r64,
+                                                 double* __restrict__ part, double* hist,
+                                                 double* htrue) {
   if (MODE == 0 && st->done) return;
   if (MODE == 1 && (st->done || !st->need_update)) return;
-  extern __shared__ double pcd[];  // [n_per] reduction scratch, then floats
-  float* rs = reinterpret_cast<float*>(pcd + n_per);  // r of the skewer
-  float* ts = rs + n_per;                              // L^T r
-  const int s = blockIdx.x, k = threadIdx.x;
-  const int slot = s * n_per + k;
-  const int rec = crec ? crec[slot] : slot;
-  const int pos = rec < 0 ? -1 : inv ? inv[rec] : rec;  // inv null: record order
+  __shared__ float rs[PCB + 2 * PC_MAX_BAND];  // r of slots s0 - band ..
+  __shared__ float ts[PCB + PC_MAX_BAND];      // t of slots s0 - band ..
+  __shared__ double red[PCB / 32];
+  const int tid = threadIdx.x;
+  const int s0 = blockIdx.x * PCB;
+  const size_t ns = (size_t)n_slots;
+  auto index_of = [&](int slot) -> int {
+    if (slot < 0 || slot >= n_slots) return -1;
+    const int rec = crec ? crec[slot] : slot;
+    return rec < 0 ? -1 : inv ? inv[rec] : rec;
+  };
+  const double alpha_d = MODE == 0 ? st->alpha : 0.0;
+  const bool from_b = MODE == 2 && *x_zero;
+  // r of the CTA's slots and halos: MODE 0 updates the previous r (rin, not
+  // written by this kernel, so halos read the same values as their owners)
+  for (int i = tid; i < PCB + 2 * band; i += PCB) {
+    const int pos = index_of(s0 - band + i);
+    float v = 0.f;
+    if (pos >= 0)
+      v = MODE == 0 ? fmaf(-(float)alpha_d, q[pos], rin[pos])
+                    : (float)(from_b ? b[pos] : r64[pos]);
+    rs[i] = v;
+  }
+  __syncthreads();
+  const int k = s0 + tid;  // this thread's slot
+  const int own = index_of(k);
+  const float ri = rs[tid + band];
   double rd = 0.0;
-  float ri = 0.f;
-  if (pos >= 0) {
+  if (own >= 0) {
+    rout[own] = ri;
     if (MODE == 0) {
-      const double alpha_d = st->alpha;
-      x[pos] = fma(alpha_d, (double)p[pos], x[pos]);
-      ri = fmaf(-(float)alpha_d, q[pos], r[pos]);
+      x[own] = fma(alpha_d, (double)p[own], x[own]);
       rd = ri;
     } else {
-      rd = (MODE == 2 && *x_zero) ? b[pos] : r64[pos];
-      ri = (float)rd;
+      rd = from_b ? b[own] : r64[own];
     }
-    r[pos] = ri;
   }
-  rs[k] = ri;
-  __syncthreads();
-  // L in planes: plane m holds L[i][i - m] at slot i (consecutive threads
-  // read consecutive words in both passes)
-  const size_t ns = (size_t)gridDim.x * n_per;
-  float t = 0.f;
-  for (int m = 0; m <= band; ++m)
-    if (k + m < n_per) t = fmaf(L[(size_t)m * ns + slot + m], rs[k + m], t);
-  ts[k] = t;
+  for (int i = tid; i < PCB + band; i += PCB) {  // t of slot s0 - band + i
+    const int j = s0 - band + i;
+    float t = 0.f;
+    if (j >= 0)
+      for (int m = 0; m <= band; ++m)
+        if (j + m < n_slots) t = fmaf(L[(size_t)m * ns + j + m], rs[i + m], t);
+    ts[i] = t;
+  }
   __syncthreads();
   float zk = 0.f;
-  for (int m = 0; m <= band; ++m)
-    if (k - m >= 0) zk = fmaf(L[(size_t)m * ns + slot], ts[k - m], zk);
-  if (pos >= 0) {
-    z[pos] = zk;
-    if (MODE == 2) p[pos] = zk;
+  if (k < n_slots)
+    for (int m = 0; m <= band; ++m) zk = fmaf(L[(size_t)m * ns + k], ts[tid + band - m], zk);
+  if (own >= 0) {
+    z[own] = zk;
+    if (MODE == 2) p[own] = zk;
   }
-  const double srz = cta_sum((double)ri * (double)zk, pcd);
-  const double srr = cta_sum(rd * rd, pcd);
-  if (k == 0) {
-    part[2 * s] = srz;
-    part[2 * s + 1] = srr;
+  const double srz = block_sum<PCB>(own >= 0 ? (double)ri * (double)zk : 0.0, red);
+  const double srr = block_sum<PCB>(rd * rd, red);
+  if (tid == 0) {
+    part[2 * blockIdx.x] = srz;
+    part[2 * blockIdx.x + 1] = srr;
   }
   if (!last_block_arrive(&st->counter[3])) return;
-  double a = 0.0, c = 0.0;
-  for (int j = k; j < (int)gridDim.x; j += blockDim.x) {
-    a += __ldcg(part + 2 * j);
-    c += __ldcg(part + 2 * j + 1);
-  }
-  const double trz = cta_sum(a, pcd);
-  const double trr = cta_sum(c, pcd);
-  if (k != 0) return;
+  const double trz = reduce_partials<PCB>(part, gridDim.x, 2, 0, red);
+  const double trr = reduce_partials<PCB>(part, gridDim.x, 2, 1, red);
+  if (tid != 0) return;
   st->counter[3] = 0;
   if (MODE == 2) {
     st->rz = trz;
@@ -640,17 +641,23 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   };
   outer_residual(resid);
   const SkewerPC* pc = op->pc.get();
-  const size_t pc_smem = pc ? (size_t)pc->n_per * (sizeof(double) + 2 * sizeof(float)) : 0;
+  const int pc_slots = pc ? pc->n_sk * pc->n_per : 0;
+  const unsigned pc_grid = (unsigned)((pc_slots + PCB - 1) / PCB);
   // partial2 holds the p.q partials of K1 (one per row tile) and, in the
   // preconditioned form, the (r.z, |r|^2) partials per skewer after them.
   double* pc_part = op->partial2.p + op->pix.n_tiles;
+  // the band preconditioner updates r out of place: iteration it reads
+  // rbuf[(it - 1) & 1] and writes rbuf[it & 1] (the start writes rbuf[0])
+  float* rbuf[2] = {f.r.p, nullptr};
   if (pc) {
+    f.r2.alloc(np);
+    rbuf[1] = f.r2.p;
     // padding stays 0 in every FP32 vector
-    for (float* v : {f.z.p, f.r.p, f.p.p})
+    for (float* v : {f.z.p, f.r.p, f.r2.p, f.p.p})
       DS_CUDA(cudaMemsetAsync(v, 0, np * sizeof(float), st));
-    k_pc_iter<2><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-        pc->n_per, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, f.r.p, f.z.p, f.p.p,
-        nullptr, B, op->r.p, pc_part, f.hist.p, f.htrue.p);
+    k_pc_iter<2><<<pc_grid, PCB, 0, st>>>(
+        pc_slots, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, nullptr, rbuf[0], f.z.p,
+        f.p.p, nullptr, B, op->r.p, pc_part, f.hist.p, f.htrue.p);
     DS_CHECK_LAUNCH();
   } else {
     k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, B, op->r.p, f.r.p, f.z.p, f.p.p, PD,
@@ -687,7 +694,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // r.z, update test), K5 (FP64-accurate residual when an update is due),
   // K6 (the update), K7 (p = z + beta p).  Every kernel returns at once once
   // the solve is done, so iterations launched past the end change nothing.
-  auto iteration = [&]() {
+  auto iteration = [&](int it) {
     if (use_sg)
       skewer_product_f32(op, sv, prod.v, prod.out, prod.counter, prod.num, prod.alpha_out,
                          prod.den_out, prod.skip_flag, st);                  // K1
@@ -696,9 +703,10 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     else
       launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);
     if (pc) {
-      k_pc_iter<0><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, f.r.p, f.z.p, f.p.p,
-          f.q.p, nullptr, nullptr, pc_part, f.hist.p, f.htrue.p);             // K2
+      k_pc_iter<0><<<pc_grid, PCB, 0, st>>>(
+          pc_slots, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, rbuf[(it - 1) & 1],
+          rbuf[it & 1], f.z.p, f.p.p, f.q.p, nullptr, nullptr, pc_part, f.hist.p,
+          f.htrue.p);                                                         // K2
       DS_CHECK_LAUNCH();
     } else {
       k_mx_update<<<g, VB, 0, st>>>(np, S, X, f.r.p, f.z.p, f.p.p, f.q.p, PD, op->partial.p,
@@ -707,9 +715,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     }
     outer_residual(upd);                                                      // K5
     if (pc) {
-      k_pc_iter<1><<<pc->n_sk, pc->n_per, pc_smem, st>>>(
-          pc->n_per, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, f.r.p, f.z.p, f.p.p,
-          nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);           // K6
+      k_pc_iter<1><<<pc_grid, PCB, 0, st>>>(
+          pc_slots, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, nullptr, rbuf[it & 1],
+          f.z.p, f.p.p, nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);  // K6
       DS_CHECK_LAUNCH();
     } else {
       k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, PD, op->partial.p, f.hist.p,
@@ -735,7 +743,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     cudaGraph_t graph = nullptr;
     DS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      for (int k = 0; k < CHECK; ++k) iteration();
+      for (int k = 1; k <= CHECK; ++k) iteration(k);  // CHECK is even: parities repeat
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -753,7 +761,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       DS_CUDA(cudaGraphLaunch(gexec, st));
       ++replays;
     } else {
-      iteration();
+      iteration(it);
     }
     if (gexec || it % CHECK == 0) {
       const int slot = issued % NSLOT;

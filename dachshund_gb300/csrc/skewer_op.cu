@@ -43,20 +43,21 @@ namespace {
 
 constexpr int NB_CHUNK = 256;  // neighbour entries staged per round
 
-// sum_q p[q] V[(lev[q] + lev_base) plane + idx[q] stride + k] over the CSR
-// row q0 .. q1: the row's offsets and factors are staged in shared memory a
-// chunk at a time (so no V address waits on a load), and each thread keeps
-// eight independent loads in flight.  Every thread of the CTA calls it (it
-// synchronises); `live` false threads take part without loading.
-template <typename T>
-__device__ __forceinline__ T nbr_sum(int q0, int q1, const int* __restrict__ idx,
-                                     const int* __restrict__ lev, const T* __restrict__ pv,
-                                     int lev_base, size_t plane, int stride,
-                                     const T* __restrict__ V, int k, bool live,
-                                     size_t* s_off, T* s_p) {
-  T acc[8];
+// out[t] = sum_q p[q] V[(lev[q] + lev_base) plane + idx[q] stride + k0 + t
+// kstep] (t < PPT, entries with k >= kmax left 0) over the CSR row q0 .. q1:
+// the row's offsets and factors are staged in shared memory a chunk at a
+// time (so no V address waits on a load); each thread accumulates PPT
+// outputs in two chains each, 2 PPT independent loads per step.  Every
+// thread of the CTA calls it (it synchronises).
+template <typename T, int PPT>
+__device__ __forceinline__ void nbr_sum(int q0, int q1, const int* __restrict__ idx,
+                                        const int* __restrict__ lev,
+                                        const T* __restrict__ pv, int lev_base, size_t plane,
+                                        int stride, const T* __restrict__ V, int k0, int kstep,
+                                        int kmax, T (&out)[PPT], size_t* s_off, T* s_p) {
+  T acc[PPT][2];
 #pragma unroll
-  for (int u = 0; u < 8; ++u) acc[u] = T(0);
+  for (int t = 0; t < PPT; ++t) acc[t][0] = acc[t][1] = T(0);
   for (int c0 = q0; c0 < q1; c0 += NB_CHUNK) {
     const int cnt = min(NB_CHUNK, q1 - c0);
     __syncthreads();
@@ -65,18 +66,35 @@ __device__ __forceinline__ T nbr_sum(int q0, int q1, const int* __restrict__ idx
       s_p[t] = pv[c0 + t];
     }
     __syncthreads();
-    if (!live) continue;
     int i = 0;
-    for (; i + 8 <= cnt; i += 8) {
-      T v[8];
+    for (; i + 2 <= cnt; i += 2) {
+      const size_t o0 = s_off[i], o1 = s_off[i + 1];
+      const T f0 = s_p[i], f1 = s_p[i + 1];
+      T v0[PPT], v1[PPT];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = V[s_off[i + u] + k];
+      for (int t = 0; t < PPT; ++t) {
+        const int k = k0 + t * kstep;
+        v0[t] = k < kmax ? V[o0 + k] : T(0);
+        v1[t] = k < kmax ? V[o1 + k] : T(0);
+      }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) acc[u] = fma(s_p[i + u], v[u], acc[u]);
+      for (int t = 0; t < PPT; ++t) {
+        acc[t][0] = fma(f0, v0[t], acc[t][0]);
+        acc[t][1] = fma(f1, v1[t], acc[t][1]);
+      }
     }
-    for (; i < cnt; ++i) acc[0] = fma(s_p[i], V[s_off[i] + k], acc[0]);
+    if (i < cnt) {
+      const size_t o0 = s_off[i];
+      const T f0 = s_p[i];
+#pragma unroll
+      for (int t = 0; t < PPT; ++t) {
+        const int k = k0 + t * kstep;
+        if (k < kmax) acc[t][0] = fma(f0, V[o0 + k], acc[t][0]);
+      }
+    }
   }
-  return ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+#pragma unroll
+  for (int t = 0; t < PPT; ++t) out[t] = acc[t][0] + acc[t][1];
 }
 
 // V^(L) for L = 0..lmax of one skewer per CTA (n_per threads).
@@ -104,6 +122,10 @@ __global__ void k_sg_levels(int n_per, int lmax, size_t n, const int* __restrict
 }
 
 // out = A v (product) or b - A v (residual) for one skewer per CTA.
+constexpr int SG_PPT = 4;  // pixels per thread in the apply kernels
+
+// out = A v (product) or b - A v (residual) for one skewer per CTA
+// (ceil(n_per / SG_PPT) threads, pixels k, k + blockDim, ...).
 template <bool RESID>
 __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
                            const int* __restrict__ nb_idx, const int* __restrict__ nb_lev,
@@ -115,15 +137,22 @@ __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
   if (skip && *skip) return;
   __shared__ size_t s_off[NB_CHUNK];
   __shared__ double s_p[NB_CHUNK];
-  const int a = blockIdx.x, k = threadIdx.x;
+  const int a = blockIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
-  const double acc = nbr_sum<double>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, k, true,
-                                     s_off, s_p);
-  const size_t r = (size_t)a * n_per + k;
-  const size_t p = pos ? (size_t)pos[r] : r;
-  const double y = fma(wl[p], acc, e[p] * v[p]);
-  out[p] = RESID ? bvec[p] - y : y;
-  if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
+  double acc[SG_PPT];
+  nbr_sum<double, SG_PPT>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, threadIdx.x,
+                          blockDim.x, n_per, acc, s_off, s_p);
+#pragma unroll
+  for (int t = 0; t < SG_PPT; ++t) {
+    const int k = threadIdx.x + t * blockDim.x;
+    if (k >= n_per) break;
+    const size_t r = (size_t)a * n_per + k;
+    const size_t p = pos ? (size_t)pos[r] : r;
+    const double y = fma(wl[p], acc[t], e[p] * v[p]);
+    out[p] = RESID ? bvec[p] - y : y;
+  }
+  if (prof_terms && threadIdx.x == 0)
+    atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
 }
 
 // FP32 levels of the inner operator: u = wr p (FP32 vectors, sorted order).
@@ -179,24 +208,33 @@ __global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr
   __shared__ double sm[32];
   __shared__ size_t s_off[NB_CHUNK];
   __shared__ float s_p[NB_CHUNK];
-  const int a = blockIdx.x, k = threadIdx.x;
+  const int a = blockIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
-  const float acc = nbr_sum<float>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, k, true,
-                                   s_off, s_p);
-  const size_t r = (size_t)a * n_per + k;
-  const size_t ps = pos ? (size_t)pos[r] : r;
-  const float pv = p[ps];
-  const float qv = fmaf((float)wl[ps], acc, (float)e[ps] * pv);
-  q[ps] = qv;
-  if (prof_terms && k == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
+  float acc[SG_PPT];
+  nbr_sum<float, SG_PPT>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, threadIdx.x,
+                         blockDim.x, n_per, acc, s_off, s_p);
+  double dsum = 0.0;
+#pragma unroll
+  for (int t = 0; t < SG_PPT; ++t) {
+    const int k = threadIdx.x + t * blockDim.x;
+    if (k >= n_per) break;
+    const size_t r = (size_t)a * n_per + k;
+    const size_t ps = pos ? (size_t)pos[r] : r;
+    const float pv = p[ps];
+    const float qv = fmaf((float)wl[ps], acc[t], (float)e[ps] * pv);
+    q[ps] = qv;
+    dsum = fma((double)pv, (double)qv, dsum);
+  }
+  if (prof_terms && threadIdx.x == 0)
+    atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * n_per);
   if (!part) return;
-  const double s = sg_cta_sum((double)pv * (double)qv, sm);
-  if (k == 0) part[a] = s;
+  const double s = sg_cta_sum(dsum, sm);
+  if (threadIdx.x == 0) part[a] = s;
   if (!last_block_arrive(counter)) return;
   double t = 0.0;
-  for (int c = k; c < (int)gridDim.x; c += blockDim.x) t += __ldcg(part + c);
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) t += __ldcg(part + c);
   const double pq = sg_cta_sum(t, sm);
-  if (k == 0) {
+  if (threadIdx.x == 0) {
     *den_out = pq;
     *alpha_out = *num / pq;
     *counter = 0;
@@ -265,21 +303,27 @@ __global__ void k_mc_levels(int n_sk, int n_per, int nz, int W, int Q,
   }
 }
 
-// m[c nz + j] = sum over the skewers b near column c of P_cb R_b^(q_cb)[j].
+// m[c nz + j] = sum over the skewers b near column c of P_cb R_b^(q_cb)[j]
+// (z index j = threadIdx.x + t blockDim.x + blockIdx.y blockDim.x SG_PPT).
 __global__ void k_mc_apply(int n_sk, int nz, const int* __restrict__ ptr,
                            const int* __restrict__ idx, const int* __restrict__ lev,
                            const double* __restrict__ p64, const double* __restrict__ R,
                            double* __restrict__ m, unsigned long long* prof_terms) {
   __shared__ size_t s_off[NB_CHUNK];
   __shared__ double s_p[NB_CHUNK];
-  const int j = blockIdx.y * blockDim.x + threadIdx.x;
   const int c = blockIdx.x;
+  const int j0 = blockIdx.y * blockDim.x * SG_PPT + threadIdx.x;
   const int q0 = ptr[c], q1 = ptr[c + 1];
-  const double acc = nbr_sum<double>(q0, q1, idx, lev, p64, -1, (size_t)n_sk * nz, nz, R, j,
-                                     j < nz, s_off, s_p);
-  if (j >= nz) return;
-  m[(size_t)c * nz + j] = acc;
-  if (prof_terms && j == 0) atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * nz);
+  double acc[SG_PPT];
+  nbr_sum<double, SG_PPT>(q0, q1, idx, lev, p64, -1, (size_t)n_sk * nz, nz, R, j0, blockDim.x,
+                          nz, acc, s_off, s_p);
+#pragma unroll
+  for (int t = 0; t < SG_PPT; ++t) {
+    const int j = j0 + t * blockDim.x;
+    if (j < nz) m[(size_t)c * nz + j] = acc[t];
+  }
+  if (prof_terms && threadIdx.x == 0 && blockIdx.y == 0)
+    atomicAdd(prof_terms, (unsigned long long)(q1 - q0) * nz);
 }
 
 // ---- neighbour lists (on the device) --------------------------------------------
@@ -499,12 +543,13 @@ void skewer_apply_f64(ds_operator* op, const SkewerVecs& c, bool residual, const
   k_sg_levels<<<g.n_sk, g.n_per, g.n_per * sizeof(double), st>>>(
       g.n_per, g.outer.lmax, n, c.pos, c.wr, v, g.taps64.p, g.V64.p, skip);
   DS_CHECK_LAUNCH();
+  const unsigned threads = (unsigned)((g.n_per + SG_PPT - 1) / SG_PPT);
   if (residual)
-    k_sg_apply<true><<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.outer.ptr.p, g.outer.idx.p,
+    k_sg_apply<true><<<g.n_sk, threads, 0, st>>>(g.n_per, n, g.outer.ptr.p, g.outer.idx.p,
                                                  g.outer.lev.p, g.outer.p64.p, g.V64.p, c.pos,
                                                  c.wl, c.e, v, c.b, out, skip, prof_terms);
   else
-    k_sg_apply<false><<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.outer.ptr.p, g.outer.idx.p,
+    k_sg_apply<false><<<g.n_sk, threads, 0, st>>>(g.n_per, n, g.outer.ptr.p, g.outer.idx.p,
                                                   g.outer.lev.p, g.outer.p64.p, g.V64.p, c.pos,
                                                   c.wl, c.e, v, c.b, out, skip, prof_terms);
   DS_CHECK_LAUNCH();
@@ -664,7 +709,7 @@ bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, doubl
   k_mc_levels<<<dim3(g.n_sk, (mc.nz + 127) / 128), 128, 0, st>>>(
       g.n_sk, g.n_per, mc.nz, mc.W, mc.Q, mc.kstart.p, mc.cls.p, mc.taps.p, x_dev, mc.R.p);
   DS_CHECK_LAUNCH();
-  k_mc_apply<<<dim3(mc.ncol, (mc.nz + 255) / 256), 256, 0, st>>>(
+  k_mc_apply<<<dim3(mc.ncol, (mc.nz + 128 * SG_PPT - 1) / (128 * SG_PPT)), 128, 0, st>>>(
       g.n_sk, mc.nz, mc.ptr.p, mc.idx.p, mc.lev.p, mc.p64.p, mc.R.p, m_dev, prof_terms);
   DS_CHECK_LAUNCH();
   if (ev) pr.end(st, ev, 2);
@@ -698,10 +743,10 @@ void skewer_product_f32(ds_operator* op, const SkewerVecs& c, const float* p, fl
   k_sg32_levels<<<g.n_sk, g.n_per, g.n_per * sizeof(float), st>>>(
       g.n_per, g.inner.lmax, n, c.pos, c.wr, p, g.taps32.p, g.V32.p, skip);
   DS_CHECK_LAUNCH();
-  k_sg32_apply<<<g.n_sk, g.n_per, 0, st>>>(g.n_per, n, g.inner.ptr.p, g.inner.idx.p,
-                                           g.inner.lev.p, g.inner.p32.p, g.V32.p, c.pos, c.wl,
-                                           c.e, p, q, counter ? g.dot_part.p : nullptr, counter,
-                                           num, alpha_out, den_out, skip, prof_terms);
+  k_sg32_apply<<<g.n_sk, (g.n_per + SG_PPT - 1) / SG_PPT, 0, st>>>(
+      g.n_per, n, g.inner.ptr.p, g.inner.idx.p, g.inner.lev.p, g.inner.p32.p, g.V32.p, c.pos,
+      c.wl, c.e, p, q, counter ? g.dot_part.p : nullptr, counter, num, alpha_out, den_out, skip,
+      prof_terms);
   DS_CHECK_LAUNCH();
   if (ev) pr.end(st, ev, 1);
 }
