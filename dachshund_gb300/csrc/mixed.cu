@@ -349,20 +349,48 @@ __global__ void __launch_bounds__(VB) k_mx_dir(int n, MixedState* st,
 constexpr int PCB = 256;       // slots per CTA
 constexpr int PC_MAX_BAND = 32;
 
-template <int MODE>
-__global__ void __launch_bounds__(PCB) k_pc_iter(int n_slots, int band, MixedState* st,
-                                                 const int* x_zero, const int* __restrict__ crec,
-                                                 const int* __restrict__ inv,
-                                                 const float* __restrict__ L,
-                                                 double* __restrict__ x,
-                                                 const float* __restrict__ rin,
-                                                 float* __restrict__ rout, float* __restrict__ z,
-                                                 float* __restrict__ p,
-                                                 const float* __restrict__ q,
-                                                 const double* __restrict__ b,
-                                                 const double* __restrict__ r64,
-                                                 double* __restrict__ part, double* hist,
-                                                 double* htrue) {
+struct PcArgs {
+  int n_slots, band;
+  MixedState* st;
+  const int* x_zero;
+  const int* crec;  // slot -> record (null: the slot itself)
+  const int* inv;   // record -> vector index (null: the record itself)
+  const float* L;   // band + 1 planes of n_slots
+  double* x;
+  const float* rin;  // MODE 0: r of the previous iteration
+  float* rout;       // r of this iteration
+  float* z;
+  float* p;
+  const float* q;
+  const double* b;
+  const double* r64;
+  double* part;
+  double* hist;
+  double* htrue;
+};
+
+// BAND >= 0: the band as a constant (loops unrolled, all L loads of a slot
+// in flight together); -1: a.band at run time.
+template <int MODE, int BAND>
+__global__ void __launch_bounds__(PCB) k_pc_iter(PcArgs a) {
+  MixedState* st = a.st;
+  const int n_slots = a.n_slots;
+  const int band = BAND >= 0 ? BAND : a.band;
+  const int* __restrict__ crec = a.crec;
+  const int* __restrict__ inv = a.inv;
+  const float* __restrict__ L = a.L;
+  double* __restrict__ x = a.x;
+  const float* __restrict__ rin = a.rin;
+  float* __restrict__ rout = a.rout;
+  float* __restrict__ z = a.z;
+  float* __restrict__ p = a.p;
+  const float* __restrict__ q = a.q;
+  const double* __restrict__ b = a.b;
+  const double* __restrict__ r64 = a.r64;
+  double* __restrict__ part = a.part;
+  double* hist = a.hist;
+  double* htrue = a.htrue;
+  const int* x_zero = a.x_zero;
   if (MODE == 0 && st->done) return;
   if (MODE == 1 && (st->done || !st->need_update)) return;
   __shared__ float rs[PCB + 2 * PC_MAX_BAND];  // r of slots s0 - band ..
@@ -405,15 +433,20 @@ __global__ void __launch_bounds__(PCB) k_pc_iter(int n_slots, int band, MixedSta
   for (int i = tid; i < PCB + band; i += PCB) {  // t of slot s0 - band + i
     const int j = s0 - band + i;
     float t = 0.f;
-    if (j >= 0)
-      for (int m = 0; m <= band; ++m)
-        if (j + m < n_slots) t = fmaf(L[(size_t)m * ns + j + m], rs[i + m], t);
+    if (j >= 0) {
+#pragma unroll
+      for (int m = 0; m <= (BAND >= 0 ? BAND : PC_MAX_BAND); ++m)
+        if (m <= band && j + m < n_slots) t = fmaf(L[(size_t)m * ns + j + m], rs[i + m], t);
+    }
     ts[i] = t;
   }
   __syncthreads();
   float zk = 0.f;
-  if (k < n_slots)
-    for (int m = 0; m <= band; ++m) zk = fmaf(L[(size_t)m * ns + k], ts[tid + band - m], zk);
+  if (k < n_slots) {
+#pragma unroll
+    for (int m = 0; m <= (BAND >= 0 ? BAND : PC_MAX_BAND); ++m)
+      if (m <= band) zk = fmaf(L[(size_t)m * ns + k], ts[tid + band - m], zk);
+  }
   if (own >= 0) {
     z[own] = zk;
     if (MODE == 2) p[own] = zk;
@@ -469,6 +502,18 @@ __global__ void __launch_bounds__(PCB) k_pc_iter(int n_slots, int band, MixedSta
       restart_after_update(st, rt, trz);
     }
   }
+}
+
+template <int MODE>
+void pc_iter(const PcArgs& a, cudaStream_t st) {
+  const unsigned grid = (unsigned)((a.n_slots + PCB - 1) / PCB);
+  if (a.band == 16)
+    k_pc_iter<MODE, 16><<<grid, PCB, 0, st>>>(a);
+  else if (a.band == 2)
+    k_pc_iter<MODE, 2><<<grid, PCB, 0, st>>>(a);
+  else
+    k_pc_iter<MODE, -1><<<grid, PCB, 0, st>>>(a);
+  DS_CHECK_LAUNCH();
 }
 
 }  // namespace
@@ -641,8 +686,21 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   };
   outer_residual(resid);
   const SkewerPC* pc = op->pc.get();
-  const int pc_slots = pc ? pc->n_sk * pc->n_per : 0;
-  const unsigned pc_grid = (unsigned)((pc_slots + PCB - 1) / PCB);
+  PcArgs pa0{};
+  if (pc) {
+    pa0.n_slots = pc->n_sk * pc->n_per;
+    pa0.band = pc->band;
+    pa0.st = S;
+    pa0.x_zero = xzero;
+    pa0.crec = pc->crec.p;
+    pa0.inv = POS;
+    pa0.L = pc->L.p;
+    pa0.x = X;
+    pa0.z = f.z.p;
+    pa0.p = f.p.p;
+    pa0.hist = f.hist.p;
+    pa0.htrue = f.htrue.p;
+  }
   // partial2 holds the p.q partials of K1 (one per row tile) and, in the
   // preconditioned form, the (r.z, |r|^2) partials per skewer after them.
   double* pc_part = op->partial2.p + op->pix.n_tiles;
@@ -655,10 +713,12 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     // padding stays 0 in every FP32 vector
     for (float* v : {f.z.p, f.r.p, f.r2.p, f.p.p})
       DS_CUDA(cudaMemsetAsync(v, 0, np * sizeof(float), st));
-    k_pc_iter<2><<<pc_grid, PCB, 0, st>>>(
-        pc_slots, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, nullptr, rbuf[0], f.z.p,
-        f.p.p, nullptr, B, op->r.p, pc_part, f.hist.p, f.htrue.p);
-    DS_CHECK_LAUNCH();
+    PcArgs a = pa0;
+    a.rout = rbuf[0];
+    a.b = B;
+    a.r64 = op->r.p;
+    a.part = pc_part;
+    pc_iter<2>(a, st);
   } else {
     k_mx_init<<<g, VB, 0, st>>>(np, S, xzero, B, op->r.p, f.r.p, f.z.p, f.p.p, PD,
                                 op->partial.p, f.hist.p, f.htrue.p);
@@ -703,11 +763,12 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     else
       launch_pair_f32(f.formula, EPI_PRODUCT, prod, st);
     if (pc) {
-      k_pc_iter<0><<<pc_grid, PCB, 0, st>>>(
-          pc_slots, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, rbuf[(it - 1) & 1],
-          rbuf[it & 1], f.z.p, f.p.p, f.q.p, nullptr, nullptr, pc_part, f.hist.p,
-          f.htrue.p);                                                         // K2
-      DS_CHECK_LAUNCH();
+      PcArgs a = pa0;                                                         // K2
+      a.rin = rbuf[(it - 1) & 1];
+      a.rout = rbuf[it & 1];
+      a.q = f.q.p;
+      a.part = pc_part;
+      pc_iter<0>(a, st);
     } else {
       k_mx_update<<<g, VB, 0, st>>>(np, S, X, f.r.p, f.z.p, f.p.p, f.q.p, PD, op->partial.p,
                                     f.hist.p);                               // K2
@@ -715,10 +776,11 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     }
     outer_residual(upd);                                                      // K5
     if (pc) {
-      k_pc_iter<1><<<pc_grid, PCB, 0, st>>>(
-          pc_slots, pc->band, S, xzero, pc->crec.p, POS, pc->L.p, X, nullptr, rbuf[it & 1],
-          f.z.p, f.p.p, nullptr, nullptr, op->r.p, pc_part, f.hist.p, f.htrue.p);  // K6
-      DS_CHECK_LAUNCH();
+      PcArgs a = pa0;                                                         // K6
+      a.rout = rbuf[it & 1];
+      a.r64 = op->r.p;
+      a.part = pc_part;
+      pc_iter<1>(a, st);
     } else {
       k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, PD, op->partial.p, f.hist.p,
                                      f.htrue.p);                             // K6

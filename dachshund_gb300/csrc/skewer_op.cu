@@ -46,18 +46,20 @@ constexpr int NB_CHUNK = 256;  // neighbour entries staged per round
 // out[t] = sum_q p[q] V[(lev[q] + lev_base) plane + idx[q] stride + k0 + t
 // kstep] (t < PPT, entries with k >= kmax left 0) over the CSR row q0 .. q1:
 // the row's offsets and factors are staged in shared memory a chunk at a
-// time (so no V address waits on a load); each thread accumulates PPT
-// outputs in two chains each, 2 PPT independent loads per step.  Every
+// time (so no V address waits on a load), and each step issues U x PPT
+// independent loads (U neighbours, PPT outputs each, U chains).  Every
 // thread of the CTA calls it (it synchronises).
-template <typename T, int PPT>
+template <typename T, int PPT, int U>
 __device__ __forceinline__ void nbr_sum(int q0, int q1, const int* __restrict__ idx,
                                         const int* __restrict__ lev,
                                         const T* __restrict__ pv, int lev_base, size_t plane,
                                         int stride, const T* __restrict__ V, int k0, int kstep,
                                         int kmax, T (&out)[PPT], size_t* s_off, T* s_p) {
-  T acc[PPT][2];
+  T acc[PPT][U];
 #pragma unroll
-  for (int t = 0; t < PPT; ++t) acc[t][0] = acc[t][1] = T(0);
+  for (int t = 0; t < PPT; ++t)
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc[t][u] = T(0);
   for (int c0 = q0; c0 < q1; c0 += NB_CHUNK) {
     const int cnt = min(NB_CHUNK, q1 - c0);
     __syncthreads();
@@ -67,34 +69,41 @@ __device__ __forceinline__ void nbr_sum(int q0, int q1, const int* __restrict__ 
     }
     __syncthreads();
     int i = 0;
-    for (; i + 2 <= cnt; i += 2) {
-      const size_t o0 = s_off[i], o1 = s_off[i + 1];
-      const T f0 = s_p[i], f1 = s_p[i + 1];
-      T v0[PPT], v1[PPT];
+    for (; i + U <= cnt; i += U) {
+      T v[U][PPT];
 #pragma unroll
-      for (int t = 0; t < PPT; ++t) {
-        const int k = k0 + t * kstep;
-        v0[t] = k < kmax ? V[o0 + k] : T(0);
-        v1[t] = k < kmax ? V[o1 + k] : T(0);
+      for (int u = 0; u < U; ++u) {
+        const size_t o = s_off[i + u];
+#pragma unroll
+        for (int t = 0; t < PPT; ++t) {
+          const int k = k0 + t * kstep;
+          v[u][t] = k < kmax ? V[o + k] : T(0);
+        }
       }
 #pragma unroll
-      for (int t = 0; t < PPT; ++t) {
-        acc[t][0] = fma(f0, v0[t], acc[t][0]);
-        acc[t][1] = fma(f1, v1[t], acc[t][1]);
+      for (int u = 0; u < U; ++u) {
+        const T f = s_p[i + u];
+#pragma unroll
+        for (int t = 0; t < PPT; ++t) acc[t][u] = fma(f, v[u][t], acc[t][u]);
       }
     }
-    if (i < cnt) {
-      const size_t o0 = s_off[i];
-      const T f0 = s_p[i];
+    for (; i < cnt; ++i) {
+      const size_t o = s_off[i];
+      const T f = s_p[i];
 #pragma unroll
       for (int t = 0; t < PPT; ++t) {
         const int k = k0 + t * kstep;
-        if (k < kmax) acc[t][0] = fma(f0, V[o0 + k], acc[t][0]);
+        if (k < kmax) acc[t][0] = fma(f, V[o + k], acc[t][0]);
       }
     }
   }
 #pragma unroll
-  for (int t = 0; t < PPT; ++t) out[t] = acc[t][0] + acc[t][1];
+  for (int t = 0; t < PPT; ++t) {
+    T s = T(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) s += acc[t][u];
+    out[t] = s;
+  }
 }
 
 // V^(L) for L = 0..lmax of one skewer per CTA (n_per threads).
@@ -122,7 +131,10 @@ __global__ void k_sg_levels(int n_per, int lmax, size_t n, const int* __restrict
 }
 
 // out = A v (product) or b - A v (residual) for one skewer per CTA.
-constexpr int SG_PPT = 4;  // pixels per thread in the apply kernels
+// outputs per thread (SG_PPT: FP64 residual and FP32 inner product, which
+// need every thread they can get to keep loads in flight; MC_PPT: the map,
+// with 3.3M outputs) and neighbours per step in the apply kernels
+constexpr int SG_PPT = 1, SG_U = 8, SG32_U = 16, MC_PPT = 4, MC_U = 4;
 
 // out = A v (product) or b - A v (residual) for one skewer per CTA
 // (ceil(n_per / SG_PPT) threads, pixels k, k + blockDim, ...).
@@ -140,8 +152,8 @@ __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
   const int a = blockIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
   double acc[SG_PPT];
-  nbr_sum<double, SG_PPT>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, threadIdx.x,
-                          blockDim.x, n_per, acc, s_off, s_p);
+  nbr_sum<double, SG_PPT, SG_U>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, threadIdx.x,
+                                blockDim.x, n_per, acc, s_off, s_p);
 #pragma unroll
   for (int t = 0; t < SG_PPT; ++t) {
     const int k = threadIdx.x + t * blockDim.x;
@@ -211,8 +223,8 @@ __global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr
   const int a = blockIdx.x;
   const int q0 = nb_ptr[a], q1 = nb_ptr[a + 1];
   float acc[SG_PPT];
-  nbr_sum<float, SG_PPT>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, threadIdx.x,
-                         blockDim.x, n_per, acc, s_off, s_p);
+  nbr_sum<float, SG_PPT, SG32_U>(q0, q1, nb_idx, nb_lev, nb_p, -1, n, n_per, V, threadIdx.x,
+                                 blockDim.x, n_per, acc, s_off, s_p);
   double dsum = 0.0;
 #pragma unroll
   for (int t = 0; t < SG_PPT; ++t) {
@@ -304,7 +316,7 @@ __global__ void k_mc_levels(int n_sk, int n_per, int nz, int W, int Q,
 }
 
 // m[c nz + j] = sum over the skewers b near column c of P_cb R_b^(q_cb)[j]
-// (z index j = threadIdx.x + t blockDim.x + blockIdx.y blockDim.x SG_PPT).
+// (z index j = threadIdx.x + t blockDim.x + blockIdx.y blockDim.x MC_PPT).
 __global__ void k_mc_apply(int n_sk, int nz, const int* __restrict__ ptr,
                            const int* __restrict__ idx, const int* __restrict__ lev,
                            const double* __restrict__ p64, const double* __restrict__ R,
@@ -312,13 +324,13 @@ __global__ void k_mc_apply(int n_sk, int nz, const int* __restrict__ ptr,
   __shared__ size_t s_off[NB_CHUNK];
   __shared__ double s_p[NB_CHUNK];
   const int c = blockIdx.x;
-  const int j0 = blockIdx.y * blockDim.x * SG_PPT + threadIdx.x;
+  const int j0 = blockIdx.y * blockDim.x * MC_PPT + threadIdx.x;
   const int q0 = ptr[c], q1 = ptr[c + 1];
-  double acc[SG_PPT];
-  nbr_sum<double, SG_PPT>(q0, q1, idx, lev, p64, -1, (size_t)n_sk * nz, nz, R, j0, blockDim.x,
-                          nz, acc, s_off, s_p);
+  double acc[MC_PPT];
+  nbr_sum<double, MC_PPT, MC_U>(q0, q1, idx, lev, p64, -1, (size_t)n_sk * nz, nz, R, j0,
+                                blockDim.x, nz, acc, s_off, s_p);
 #pragma unroll
-  for (int t = 0; t < SG_PPT; ++t) {
+  for (int t = 0; t < MC_PPT; ++t) {
     const int j = j0 + t * blockDim.x;
     if (j < nz) m[(size_t)c * nz + j] = acc[t];
   }
@@ -709,7 +721,7 @@ bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, doubl
   k_mc_levels<<<dim3(g.n_sk, (mc.nz + 127) / 128), 128, 0, st>>>(
       g.n_sk, g.n_per, mc.nz, mc.W, mc.Q, mc.kstart.p, mc.cls.p, mc.taps.p, x_dev, mc.R.p);
   DS_CHECK_LAUNCH();
-  k_mc_apply<<<dim3(mc.ncol, (mc.nz + 128 * SG_PPT - 1) / (128 * SG_PPT)), 128, 0, st>>>(
+  k_mc_apply<<<dim3(mc.ncol, (mc.nz + 128 * MC_PPT - 1) / (128 * MC_PPT)), 128, 0, st>>>(
       g.n_sk, mc.nz, mc.ptr.p, mc.idx.p, mc.lev.p, mc.p64.p, mc.R.p, m_dev, prof_terms);
   DS_CHECK_LAUNCH();
   if (ev) pr.end(st, ev, 2);
