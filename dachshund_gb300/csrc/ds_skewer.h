@@ -54,12 +54,14 @@ void skewer_x_to_sorted(ds_operator* op, const double* x_rec, double* x_sorted, 
 
 // The FP32 inner product of the mixed solve, q = A32 p on FP32 vectors, with
 // the PCG step's p.q and alpha = *num / p.q (written by the last CTA,
-// counter reset to 0; counter null: no dot).  ensure_skewer_inner builds the
-// lists at the inner cutoff once.
+// counter reset to 0; counter null: no dot).  With beta non-null, p is first
+// updated to z + beta p (the CG direction step).  ensure_skewer_inner builds
+// the lists at the inner cutoff once.
 void ensure_skewer_inner(ds_operator* op, double inner_cut);
-void skewer_product_f32(ds_operator* op, const SkewerVecs& c, const float* p, float* q,
+void skewer_product_f32(ds_operator* op, const SkewerVecs& c, float* p, float* q,
                         unsigned int* counter, const double* num, double* alpha_out,
-                        double* den_out, const int* skip, cudaStream_t st);
+                        double* den_out, const int* skip, cudaStream_t st,
+                        const double* beta = nullptr, const float* z = nullptr);
 
 // r = b - A v (residual) or A v (product) with the structured FP64
 // operator; the launch returns at once when *skip != 0 (skip may be null).

@@ -310,6 +310,10 @@ __global__ void __launch_bounds__(VB) k_mx_replace(int n, MixedState* st,
         st->rz = trz;  // rz_old keeps the previous iteration's r.z
         restart_after_update(st, rt, trz);
       }
+      // the update is done: no FP64 residual until K2 asks for one again
+      // (every block read the flags before it arrived)
+      st->need_update = 0;
+      st->skip_update = 1;
       st->counter[1] = 0;
     }
   }
@@ -501,6 +505,8 @@ __global__ void __launch_bounds__(PCB) k_pc_iter(PcArgs a) {
       st->rz = trz;
       restart_after_update(st, rt, trz);
     }
+    st->need_update = 0;  // as k_mx_replace: the update is done
+    st->skip_update = 1;
   }
 }
 
@@ -756,8 +762,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // the solve is done, so iterations launched past the end change nothing.
   auto iteration = [&](int it) {
     if (use_sg)
-      skewer_product_f32(op, sv, prod.v, prod.out, prod.counter, prod.num, prod.alpha_out,
-                         prod.den_out, prod.skip_flag, st);                  // K1
+      // K7 of the previous iteration (p = z + beta p) is done by K1 here
+      skewer_product_f32(op, sv, f.p.p, prod.out, prod.counter, prod.num, prod.alpha_out,
+                         prod.den_out, prod.skip_flag, st, &S->beta, f.z.p);  // K1
     else if (use_tc)
       launch_pair_tc(prod, st);                                               // K1
     else
@@ -786,8 +793,10 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
                                      f.htrue.p);                             // K6
       DS_CHECK_LAUNCH();
     }
-    k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                        // K7
-    DS_CHECK_LAUNCH();
+    if (!use_sg) {
+      k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                      // K7
+      DS_CHECK_LAUNCH();
+    }
   };
 
   // The host reads the done flag every CHECK iterations, two reads behind,

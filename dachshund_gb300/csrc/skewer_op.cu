@@ -168,8 +168,11 @@ __global__ void k_sg_apply(int n_per, size_t n, const int* __restrict__ nb_ptr,
 }
 
 // FP32 levels of the inner operator: u = wr p (FP32 vectors, sorted order).
+// With beta non-null it first moves p along the CG direction, p = z + beta p
+// (the step that would otherwise be a kernel of its own after the update).
 __global__ void k_sg32_levels(int n_per, int lmax, size_t n, const int* __restrict__ pos,
-                              const double* __restrict__ wr, const float* __restrict__ p,
+                              const double* __restrict__ wr, float* __restrict__ p,
+                              const double* beta, const float* __restrict__ z,
                               const float* __restrict__ taps, float* __restrict__ V,
                               const int* skip) {
   if (skip && *skip) return;
@@ -177,7 +180,12 @@ __global__ void k_sg32_levels(int n_per, int lmax, size_t n, const int* __restri
   const int k = threadIdx.x;
   const size_t r = (size_t)blockIdx.x * n_per + k;
   const size_t ps = pos ? (size_t)pos[r] : r;
-  const float u = (float)wr[ps] * p[ps];
+  float pv = p[ps];
+  if (beta) {
+    pv = fmaf((float)*beta, pv, z[ps]);
+    p[ps] = pv;
+  }
+  const float u = (float)wr[ps] * pv;
   sf[k] = u;
   __syncthreads();
   float acc = u;
@@ -740,9 +748,10 @@ SkewerVecs skewer_vecs_sorted(ds_operator* op) {
   return SkewerVecs{op->inv.p, op->wl.p, op->wr.p, op->e.p, op->b.p};
 }
 
-void skewer_product_f32(ds_operator* op, const SkewerVecs& c, const float* p, float* q,
+void skewer_product_f32(ds_operator* op, const SkewerVecs& c, float* p, float* q,
                         unsigned int* counter, const double* num, double* alpha_out,
-                        double* den_out, const int* skip, cudaStream_t st) {
+                        double* den_out, const int* skip, cudaStream_t st, const double* beta,
+                        const float* z) {
   SkewerGrid& g = *op->sgrid;
   const size_t n = (size_t)op->n;
   Profiler& pr = op->ctx->prof;
@@ -753,7 +762,7 @@ void skewer_product_f32(ds_operator* op, const SkewerVecs& c, const float* p, fl
     pr.begin(st, &ev);
   }
   k_sg32_levels<<<g.n_sk, g.n_per, g.n_per * sizeof(float), st>>>(
-      g.n_per, g.inner.lmax, n, c.pos, c.wr, p, g.taps32.p, g.V32.p, skip);
+      g.n_per, g.inner.lmax, n, c.pos, c.wr, p, beta, z, g.taps32.p, g.V32.p, skip);
   DS_CHECK_LAUNCH();
   k_sg32_apply<<<g.n_sk, (g.n_per + SG_PPT - 1) / SG_PPT, 0, st>>>(
       g.n_per, n, g.inner.ptr.p, g.inner.idx.p, g.inner.lev.p, g.inner.p32.p, g.V32.p, c.pos,
