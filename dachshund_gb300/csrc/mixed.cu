@@ -650,7 +650,8 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   const float* PD = f.pdiag.p;
   const int* POS = op->inv.p;
   if (use_sg) {
-    ensure_skewer_inner(op, f.inner_cut);
+    ensure_skewer_inner(op, mp.inner_cutoff > 0.0 ? mp.inner_cutoff
+                                                  : DS_DEFAULT_STRUCTURED_INNER_CUTOFF);
     sv = skewer_vecs_rec(op, f.pdiag.p);
     X = op->sgrid->rx.p;
     B = sv.b;

@@ -70,6 +70,13 @@ typedef enum {
  * 24 down to 10 all take 162 iterations and 2 reliable updates; 9 takes 3
  * updates; 12 keeps a margin and evaluates half the pairs of 24. */
 #define DS_DEFAULT_INNER_CUTOFF 12.0
+/* The same cutoff for the structured FP32 inner operator
+ * (ds_operator_set_skewer_grid), which drops every term beyond it (the pair
+ * kernel keeps whole 32 x 32 sub-tiles that reach the cutoff, i.e. more
+ * terms): on the 262,144-pixel workload with the cluster preconditioner, 12
+ * takes 101 iterations and 3 reliable updates, 14 to 24 take 90 and 2, and 14
+ * is the fastest. */
+#define DS_DEFAULT_STRUCTURED_INNER_CUTOFF 14.0
 
 typedef struct {
   double var_s;          /* SignalCovarParams::var_s */
@@ -325,7 +332,8 @@ typedef struct {
   double reliable_delta; /* update when the FP32 residual fell by this factor
                             since the last update; <= 0: 1e-4 */
   double inner_cutoff;   /* exponent cutoff of the FP32 operator;
-                            <= 0: DS_DEFAULT_INNER_CUTOFF */
+                            <= 0: DS_DEFAULT_INNER_CUTOFF (pair kernels) or
+                            DS_DEFAULT_STRUCTURED_INNER_CUTOFF (structured) */
   int verbose;
 } ds_mixed_params;
 
