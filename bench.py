@@ -43,6 +43,12 @@ PAIRS_PER_CLK = {"expanded": min(FMA_LANES / 4, MUFU_RATE), "direct": min(FMA_LA
 # DRAM traffic of one k_pair_f32 launch on the 262,144-pixel workload, measured
 # once with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
 K_PAIR_F32_DRAM_BYTES = 9_174_528
+# DRAM bytes of one structured FP32 inner product (k_sg32_levels +
+# k_sg32_apply) on the 262,144-pixel workload, from one ncu capture
+# (profiles/k_sg32_inner_wf262144.md)
+K_SG32_DRAM_BYTES = None
+# the structured inner operator's cutoff (DS_DEFAULT_STRUCTURED_INNER_CUTOFF)
+SG_INNER_CUT = 14.0
 # FP64-pipe instructions per evaluated pair of the plain FP64 kernel
 # k_pair_f64<EXACT, PRODUCT> on the 262,144-pixel workload, from one ncu
 # capture (FP64-pipe busy fraction x 2 per clock x active SM cycles / the
@@ -68,6 +74,8 @@ def parse():
                     help="skip the batched-chunks (512 chunks x 64 RHS) measurement")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner measurement")
+    ap.add_argument("--no-pair-form", action="store_true",
+                    help="skip the pair-kernel form of the solve (k_pair_f32 roofline)")
     ap.add_argument("--no-map-covar", action="store_true",
                     help="skip the MapCovarDiag measurement")
     ap.add_argument("--no-wf32768", action="store_true",
@@ -683,11 +691,27 @@ def run_ours(args, rank, world, local):
     f64_n = agg(solve_prof, "f64_launches")
     map_ms = agg(map_prof, "map_ms")
     map_pairs = agg(map_prof, "map_evaluated")
+    # Bytes one structured FP32 inner product must move at least (HBM
+    # roofline): per pixel p (4) and wr (8) in, the z-convolved column values
+    # written once per level and read back once (2 x 4 (lmax + 1)), wl and e
+    # (8 + 8), q out (4); per neighbour entry 16 (index, level, factor, pointer
+    # share).  lmax: the z taps within the inner cutoff.
+    c_para = 1.0 / (2 * w.l_para ** 2)
+    lmax = 0
+    while lmax + 1 < w.pix_per_skewer and c_para * ((lmax + 1) * synth.DZ) ** 2 < SG_INNER_CUT:
+        lmax += 1
+    terms_per_product = (f32_pairs / f32_n) if f32_n else 0.0
+    sg_bytes = w.n * (4 + 8 + 8 * (lmax + 1) + 8 + 8 + 4) + 16 * terms_per_product / w.pix_per_skewer
+    sg_us = (f32_ms / f32_n * 1e3) if f32_n else None
     kernels = {
-        "fp32_inner_matvec": {
+        "fp32_inner_product": {
+            "kernel": "structured FP32 inner product (k_sg32_levels + k_sg32_apply)",
             "launches_per_step": f32_n / prof_steps, "ms_per_step": f32_ms / prof_steps,
-            "Gpair_per_s": f32_pairs / (f32_ms * 1e-3) / 1e9 if f32_ms else None,
-            "peak_Gpair_per_s": PAIRS_PER_CLK["expanded"] * SMS * sm_hz / 1e9},
+            "us_per_product": sg_us,
+            "terms_per_product": terms_per_product,
+            "term": "one FP32 FMA of a (skewer pair, pixel): perpendicular factor x "
+                    "z-convolved column value",
+            "algorithmic_bytes_per_product": sg_bytes},
         "fp64_outer_residual": {
             "kernel": "structured FP64 outer residual (k_sg_levels + k_sg_apply)",
             "launches_per_step": f64_n / prof_steps, "ms_per_step": f64_ms / prof_steps,
@@ -700,40 +724,23 @@ def run_ours(args, rank, world, local):
             "Gterm_per_s": map_pairs / (map_ms * 1e-3) / 1e9 if map_ms else None,
             "term": "one FP64 FMA of a (map column, skewer, map z) triple"},
     }
-    k = kernels["fp32_inner_matvec"]
-    # Roofline of the FP32 pair kernel: its pipes' nominal pair rate, 32
-    # pairs/clk/SM (4 FMA lanes as two FFMA2 + 1 MUFU ex2 per pair; FMA 128
-    # lanes and ex2 32 per clock per SM).  Beside it, the pair rate that
-    # instruction mix reaches on this GPU with nothing else in the loop,
-    # measured now by bench_pipes.cu: the practical ceiling of the mix.
-    cal = pipe_calibration(local) if rank == 0 else None
-    peak = k["peak_Gpair_per_s"]
-    mix = None
-    if cal and cal.get("mix_pairs_per_s"):
-        mix = {
-            "Gpair_per_s": cal["mix_pairs_per_s"] / 1e9,
-            "pairs_per_clk_per_sm": cal["mix_pairs_per_s"] / (SMS * sm_hz),
-            "ex2_per_clk_per_sm": cal["ex2_per_s"] / (SMS * sm_hz),
-            "ffma_lanes_per_clk_per_sm": cal["ffma_lanes_per_s"] / (SMS * sm_hz),
-            "frac": (k["Gpair_per_s"] * 1e9 / cal["mix_pairs_per_s"]) if k["Gpair_per_s"] else None,
-            "basis": ("bench_pipes.cu in this run: 3 FFMA2 + 2 ex2 + 1 FFMA2 per two pairs in "
-                      "independent chains, no memory traffic, best of 20-64 warps/SM and 1-8 "
-                      "chains per thread, at the sampled SM clock"),
-        }
+    hbm = measured_peaks().get("hbm_gbs")
+    sg_gbs = sg_bytes / (sg_us * 1e-6) / 1e9 if sg_us else None
     roofline = {
-        "kernel": "k_pair_f32 (FP32 inner matvec, exact kernel, MUFU ex2)",
-        "bound": "fp32-fma+mufu", "unit": "Gpair/s",
-        "achieved": k["Gpair_per_s"], "peak": peak,
-        "frac": (k["Gpair_per_s"] / peak) if k["Gpair_per_s"] else None,
-        "peak_basis": (f"{PAIRS_PER_CLK['expanded']:.0f} pairs/clk/SM (FMA 128 lanes and ex2 32 "
-                       f"per clk per SM, nominal; each measured alone within 7%) x {SMS} SMs x "
-                       f"median SM clock under load"),
-        "measured_mix_ceiling": mix,
-        # DRAM bytes (read + write) of one launch, from one ncu capture of this
-        # kernel on this workload (profiles/k_pair_f32_expanded_wf262144.md):
-        # the working set stays in L2, the kernel is pipe bound
-        "traffic": K_PAIR_F32_DRAM_BYTES,
-        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+        "kernel": "structured FP32 inner product (k_sg32_levels + k_sg32_apply), the "
+                  "dominant kernel pair of the chosen form's step",
+        "bound": "hbm", "unit": "GB/s",
+        "achieved": sg_gbs, "peak": hbm,
+        "frac": (sg_gbs / hbm) if (sg_gbs and hbm) else None,
+        "peak_basis": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+        "algorithmic_bytes_per_launch": sg_bytes,
+        "launch_us": sg_us,
+        # DRAM bytes (read + write) of one product (both kernels), from one ncu
+        # capture on this workload (profiles/k_sg32_inner_wf262144.md): the
+        # column values are re-read from L2 by every neighbour (70% L2 hits),
+        # and the kernels are latency-bound, not bandwidth-bound
+        "traffic": K_SG32_DRAM_BYTES,
+        "traffic_unit": "bytes per product (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
     }
 
     # Plain FP64 GPU PCG on the same system (once, untimed by the step loop).
@@ -770,6 +777,63 @@ def run_ours(args, rank, world, local):
                  "iters": rp.num_iters, "success": rp.success}
         map_err = float(np.max(np.abs(m_chosen - mref)) / np.max(np.abs(mref)))
         x_err = float(torch.max(torch.abs(x - xp)).item() / torch.max(torch.abs(xp)).item())
+
+    # The same solve with the matrix-free pair kernels instead of the
+    # structured operator (FP32 k_pair_f32 inner products, float-float outer
+    # residuals; same cluster preconditioner): the general path for pixels on
+    # no shared z grid, and the FP32 FMA/MUFU roofline of its pair kernel.
+    pair_form = None
+    if not args.no_pair_form:
+        op.set_skewer_grid(0, 0)
+        xq = torch.zeros_like(x)
+        op.solve_mixed_dev(mp, xq)
+        rq = None
+        for _ in range(3):
+            xq.zero_()
+            torch.cuda.synchronize()
+            r_ = op.solve_mixed_dev(mp, xq)
+            rq = r_ if (rq is None or r_.seconds < rq.seconds) else rq
+        xq.zero_()
+        torch.cuda.synchronize()
+        ctx.set_profiling(True)
+        op.solve_mixed_dev(mp, xq)
+        pq = ctx.profile()
+        ctx.set_profiling(False)
+        op.set_skewer_grid(w.n_skewers, w.pix_per_skewer)
+        gps = pq["f32_evaluated"] / (pq["f32_ms"] * 1e-3) / 1e9 if pq["f32_ms"] else None
+        peak = PAIRS_PER_CLK["expanded"] * SMS * sm_hz / 1e9
+        cal = pipe_calibration(local) if rank == 0 else None
+        mix = None
+        if cal and cal.get("mix_pairs_per_s") and gps:
+            mix = {
+                "Gpair_per_s": cal["mix_pairs_per_s"] / 1e9,
+                "pairs_per_clk_per_sm": cal["mix_pairs_per_s"] / (SMS * sm_hz),
+                "ex2_per_clk_per_sm": cal["ex2_per_s"] / (SMS * sm_hz),
+                "ffma_lanes_per_clk_per_sm": cal["ffma_lanes_per_s"] / (SMS * sm_hz),
+                "frac": gps * 1e9 / cal["mix_pairs_per_s"],
+                "basis": ("bench_pipes.cu in this run: 3 FFMA2 + 2 ex2 + 1 FFMA2 per two pairs "
+                          "in independent chains, no memory traffic, best of 20-64 warps/SM and "
+                          "1-8 chains per thread, at the sampled SM clock")}
+        pair_form = {
+            "solve_s": rq.seconds, "iters": rq.num_iters, "fp64_updates": rq.n_outer,
+            "success": rq.success,
+            "x_err_vs_structured": float(torch.max(torch.abs(xq - x)).item()
+                                         / torch.max(torch.abs(x)).item()),
+            "roofline": {
+                "kernel": "k_pair_f32 (FP32 matrix-free inner matvec, exact kernel, MUFU ex2)",
+                "bound": "fp32-fma+mufu", "unit": "Gpair/s", "achieved": gps, "peak": peak,
+                "frac": gps / peak if gps else None,
+                "peak_basis": (f"{PAIRS_PER_CLK['expanded']:.0f} pairs/clk/SM (FMA 128 lanes and "
+                               f"ex2 32 per clk per SM, nominal; each measured alone within 7%) "
+                               f"x {SMS} SMs x median SM clock under load"),
+                "launches": pq["f32_launches"],
+                "ms_per_launch": pq["f32_ms"] / max(pq["f32_launches"], 1),
+                "measured_mix_ceiling": mix,
+                "traffic": K_PAIR_F32_DRAM_BYTES,
+                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
+                                "dram__bytes_write.sum)"},
+            "ff_residual_ms": pq["f64_ms"],
+        }
 
     # End to end through the public API with host buffers: the records and the
     # map points sit in pinned (page-locked) host memory, numpy views of
@@ -830,6 +894,7 @@ def run_ours(args, rank, world, local):
             "map_err_vs_fp64": map_err if plain else None,
             "x_err_vs_fp64": x_err if plain else None,
             "roofline": roofline,
+            "pair_kernel_form": pair_form,
             "kernels": kernels,
             "cpu_baseline": base,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
