@@ -46,7 +46,7 @@ K_PAIR_F32_DRAM_BYTES = 9_174_528
 # DRAM bytes of one structured FP32 inner product (k_sg32_levels +
 # k_sg32_apply) on the 262,144-pixel workload, from one ncu capture
 # (profiles/k_sg32_inner_wf262144.md)
-K_SG32_DRAM_BYTES = None
+K_SG32_DRAM_BYTES = 16_603_136  # k_sg32_levels 4,202,496 + k_sg32_apply 12,400,640
 # the structured inner operator's cutoff (DS_DEFAULT_STRUCTURED_INNER_CUTOFF)
 SG_INNER_CUT = 14.0
 # FP64-pipe instructions per evaluated pair of the plain FP64 kernel
