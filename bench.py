@@ -76,6 +76,8 @@ def parse():
                     help="skip the learned-preconditioner measurement")
     ap.add_argument("--no-pair-form", action="store_true",
                     help="skip the pair-kernel form of the solve (k_pair_f32 roofline)")
+    ap.add_argument("--no-wf4096", action="store_true",
+                    help="skip the 4,096-pixel app-path measurement (GPU and CPU, whole)")
     ap.add_argument("--no-map-covar", action="store_true",
                     help="skip the MapCovarDiag measurement")
     ap.add_argument("--no-wf32768", action="store_true",
@@ -413,10 +415,11 @@ def run_batched(ctx, n_chunks=512, n_rhs=64, seed=0, plain_samples=6):
 def run_wf32768(ctx, hbm_gbs):
     """The 32,768-pixel workload (256 skewers x 128 pixels in [0,40)^2 x
     [0,256) Mpc/h, GRF data, exact kernel, W form, tol 1e-8, map 40 x 40 x
-    256), solved three ways from x = 0: the plain FP64 PCG with the dense
+    256), solved four ways from x = 0: the plain FP64 PCG with the dense
     operator in HBM (32,768^2 FP64 = 8.6 GB, float-pair matvec), the plain
-    FP64 PCG with the matrix-free FP64 kernel, and the chosen mixed-precision
-    form (+ FP32 map).  Device times from CUDA events; the dense matvec's
+    FP64 PCG with the matrix-free FP64 kernel, the mixed-precision form with
+    the pair kernels (+ FP32 map), and the chosen form (cluster factor,
+    structured operator, structured FP64 map).  Device times from CUDA events; the dense matvec's
     achieved HBM bandwidth = 8 n_pad^2 bytes per product / its event time,
     against the measured copy bandwidth."""
     import numpy as np
@@ -479,6 +482,26 @@ def run_wf32768(ctx, hbm_gbs):
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
+    # the chosen form: cluster factor, structured operator and structured map
+    mf.set_cluster_preconditioner(w.n_skewers, w.pix_per_skewer, PC_CLUSTER, PC_BAND)
+    mf.set_skewer_grid(w.n_skewers, w.pix_per_skewer)
+    grid.set_column_grid(w.map_nx * w.map_ny, w.map_nz)
+    xs = torch.zeros_like(xd)
+    ms = torch.empty_like(mref)
+    mf.solve_mixed_dev(mp, xs)  # warm-up
+    grid.product_f32_dev(mf, xs, ms)
+    ctimes = []
+    for _ in range(3):
+        xs.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        e0.record(stream)
+        rs = mf.solve_mixed_dev(mp, xs)
+        grid.product_f32_dev(mf, xs, ms)
+        e1.record(stream)
+        e1.synchronize()
+        ctimes.append(e0.elapsed_time(e1) / 1e3)
     # FP64 residuals of the dense and mixed solutions with the matrix-free operator
     wv = torch.tensor(rec[:, 3], device="cuda")
     nb = float(np.linalg.norm(rec[:, 4]))
@@ -500,11 +523,64 @@ def run_wf32768(ctx, hbm_gbs):
         "map_err_mixed_vs_fp64": float(torch.max(torch.abs(mc - mref)).item())
         / float(torch.max(torch.abs(mref)).item()),
         "speedup_dense_vs_matrix_free": rm.seconds / rd.seconds,
+        "chosen_solve_plus_map_s": statistics.mean(ctimes), "chosen_iters": rs.num_iters,
+        "chosen_fp64_updates": rs.n_outer, "chosen_rel_residual_fp64": rel_resid(xs),
+        "x_chosen_vs_matrix_free": float(torch.max(torch.abs(xs - xm)).item()) / xmax,
+        "map_err_chosen_vs_fp64": float(torch.max(torch.abs(ms - mref)).item())
+        / float(torch.max(torch.abs(mref)).item()),
+        "chosen_form": "cluster FSAI factor (4 skewers, band 16), structured operator and map",
     })
     grid.close()
     dn.close()
     mf.close()
     return out
+
+
+def run_wf4096(ctx):
+    """The reference's own CPU-runnable configuration, run whole on both sides
+    (no extrapolation): 4,096 pixels (64 skewers x 64 in [0,32)^2 x [0,128)
+    Mpc/h, dense-Cholesky data), the reference's app path (W form, table
+    kernel, PCG to 1e-5, at most 200 iterations, step_r 50) + the FP64 map on
+    the 32 x 32 x 128 grid.  GPU: the plain FP64 path through the library
+    (host buffers in and out, the operator and map grid created in the timed
+    region).  CPU baseline leg: the oracle port of the reference (bit-exact
+    with it) on all host threads, the same solve and map."""
+    import numpy as np
+
+    import oracle
+    from dachshund_gb300 import (MapGrid, PCGParams, SignalCovarParams, WFVectorW,
+                                 pixel_to_wpixel, synth)
+
+    w = synth.wf4096(0)
+    rec = pixel_to_wpixel(w.pixels)
+    sp = SignalCovarParams(w.var_s, w.l_perp, w.l_para)  # table kernel
+    pts = synth.uniform_map_coords(w.lx, w.ly, w.lz, w.map_nx, w.map_ny, w.map_nz)
+    pp = PCGParams(w.pcg_max_iter, w.pcg_step_r, w.pcg_tol)
+    times = []
+    for k in range(4):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        op = WFVectorW(ctx, rec, sp)
+        x, res = op.solve_pcg(pp)
+        grid = MapGrid(ctx, pts)
+        m = grid.product(op, x)
+        if k:
+            times.append(time.perf_counter() - t0)
+        grid.close()
+        op.close()
+    t0 = time.perf_counter()
+    xo, ok, it_o, _ = oracle.solve_pcg("w", rec, w.var_s, w.l_perp, w.l_para, w.pcg_max_iter,
+                                       w.pcg_step_r, w.pcg_tol)
+    mo = oracle.smp_product(w.pixels[:, :3], pts, xo, w.var_s, w.l_perp, w.l_para)
+    cpu_s = time.perf_counter() - t0
+    gpu_s = statistics.mean(times)
+    return {"workload": f"{w.name}: the reference's app path (W form, table kernel, tol "
+                        f"{w.pcg_tol}, step_r {w.pcg_step_r}) + FP64 map 32 x 32 x 128",
+            "gpu_s": gpu_s, "gpu_iters": res.num_iters, "gpu_success": res.success,
+            "cpu_s": cpu_s, "cpu_iters": int(it_o), "cpu_cores": os.cpu_count(),
+            "cpu_kind": "port (C/OpenMP restatement, bit-exact with the reference)",
+            "speedup_vs_cpu": cpu_s / gpu_s,
+            "map_err_vs_cpu": float(np.max(np.abs(m - mo)) / np.max(np.abs(mo)))}
 
 
 def run_map_covar(ctx, n_points=256):
@@ -867,6 +943,7 @@ def run_ours(args, rank, world, local):
     learned = None if args.no_learned else run_learned(ctx)
     wf32768 = None if args.no_wf32768 else run_wf32768(ctx, measured_peaks().get("hbm_gbs"))
     map_covar = None if args.no_map_covar else run_map_covar(ctx)
+    wf4096 = None if (args.no_wf4096 or rank != 0) else run_wf4096(ctx)
     if batched and batched["matvec_algorithmic_tflops"] and batched["variant"].startswith("tensor"):
         peak = measured_peaks().get("bf16_tflops")
         if peak:
@@ -907,6 +984,7 @@ def run_ours(args, rank, world, local):
             "learned_preconditioner": learned,
             "wf32768_dense_and_matrix_free": wf32768,
             "map_covar_diag": map_covar,
+            "wf4096_app_path": wf4096,
         }
         emit(line)
     if world > 1:
