@@ -390,7 +390,6 @@ int ds_operator_create(ds_context* ctx, int form, int n, const double* records,
 void ds_operator_destroy(ds_operator* op) {
   // cudaFree (in the buffer destructors) waits for work using the memory, so
   // the context (which may already be gone) is not touched here.
-  if (op && op->side_stream) cudaStreamDestroy(op->side_stream);
   delete op;
 }
 

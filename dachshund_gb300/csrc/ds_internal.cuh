@@ -343,9 +343,6 @@ struct ds_operator {
   std::unique_ptr<ds::SkewerPC, ds::SkewerPCDeleter> pc;
   // structured operator for skewers on a shared z grid (null: pair kernels)
   std::unique_ptr<ds::SkewerGrid, ds::SkewerGridDeleter> sgrid;
-  // second stream, used only to capture the mixed solve's conditional update
-  // bodies into its iteration graph (created on first use)
-  cudaStream_t side_stream = nullptr;
 };
 
 struct ds_map {

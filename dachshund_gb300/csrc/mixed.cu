@@ -227,8 +227,7 @@ __global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, double*
                                                   const float* __restrict__ p,
                                                   const float* __restrict__ q,
                                                   const float* __restrict__ pd,
-                                                  double* __restrict__ part, double* hist,
-                                                  cudaGraphConditionalHandle cond) {
+                                                  double* __restrict__ part, double* hist) {
   if (st->done) return;
   __shared__ double red[VB / 32];
   const double alpha_d = st->alpha;
@@ -265,7 +264,6 @@ __global__ void __launch_bounds__(VB) k_mx_update(int n, MixedState* st, double*
       st->skip_update = upd ? 0 : 1;
       st->beta = st->rz / st->rz_old;
       st->counter[1] = 0;
-      if (cond) cudaGraphSetConditional(cond, upd ? 1u : 0u);  // runs this iteration's update
     }
   }
 }
@@ -373,7 +371,6 @@ struct PcArgs {
   double* part;
   double* hist;
   double* htrue;
-  cudaGraphConditionalHandle cond;  // MODE 0 in a graph: the update node's condition
 };
 
 // BAND >= 0: the band as a constant (loops unrolled, all L loads of a slot
@@ -494,7 +491,6 @@ __global__ void __launch_bounds__(PCB) k_pc_iter(PcArgs a) {
     st->need_update = upd ? 1 : 0;
     st->skip_update = upd ? 0 : 1;
     st->beta = st->rz / st->rz_old;
-    if (a.cond) cudaGraphSetConditional(a.cond, upd ? 1u : 0u);
   } else {
     const double rt = sqrt(trr);
     st->rtrue = rt;
@@ -763,10 +759,9 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
 
   // One iteration: K1 (q = A32 p, p.q, alpha), K2 (x, r updates, z = M^-1 r,
   // r.z, update test), K5 (FP64-accurate residual when an update is due),
-  // K6 (the update), K7 (p = z + beta p; in the structured form K1 does it).
-  // Every kernel returns at once once the solve is done, so iterations
-  // launched past the end change nothing.
-  auto k1_k2 = [&](int it, cudaGraphConditionalHandle cond) {
+  // K6 (the update), K7 (p = z + beta p).  Every kernel returns at once once
+  // the solve is done, so iterations launched past the end change nothing.
+  auto iteration = [&](int it) {
     if (use_sg)
       // K7 of the previous iteration (p = z + beta p) is done by K1 here
       skewer_product_f32(op, sv, f.p.p, prod.out, prod.counter, prod.num, prod.alpha_out,
@@ -781,35 +776,24 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       a.rout = rbuf[it & 1];
       a.q = f.q.p;
       a.part = pc_part;
-      a.cond = cond;
       pc_iter<0>(a, st);
     } else {
       k_mx_update<<<g, VB, 0, st>>>(np, S, X, f.r.p, f.z.p, f.p.p, f.q.p, PD, op->partial.p,
-                                    f.hist.p, cond);                         // K2
+                                    f.hist.p);                               // K2
       DS_CHECK_LAUNCH();
     }
-  };
-  auto k5_k6 = [&](int it, cudaStream_t s) {
-    PairArgs u = upd;                                                         // K5
-    if (op->sgrid)
-      skewer_apply_f64(op, sv, true, u.v, u.out, u.skip_flag, s);
-    else if (f.use_ff)
-      launch_pair_ff_resid(op->kc, u, f.ffd.view, s);
-    else
-      launch_pair_f64(op->kc, EPI_RESIDUAL, u, s);
+    outer_residual(upd);                                                      // K5
     if (pc) {
       PcArgs a = pa0;                                                         // K6
       a.rout = rbuf[it & 1];
       a.r64 = op->r.p;
       a.part = pc_part;
-      pc_iter<1>(a, s);
+      pc_iter<1>(a, st);
     } else {
-      k_mx_replace<<<g, VB, 0, s>>>(np, S, op->r.p, f.r.p, f.z.p, PD, op->partial.p, f.hist.p,
-                                    f.htrue.p);                               // K6
+      k_mx_replace<<<g, VB, 0, st>>>(np, S, op->r.p, f.r.p, f.z.p, PD, op->partial.p, f.hist.p,
+                                     f.htrue.p);                             // K6
       DS_CHECK_LAUNCH();
     }
-  };
-  auto k7 = [&]() {
     if (!use_sg) {
       k_mx_dir<<<g, VB, 0, st>>>(np, S, f.z.p, f.p.p);                      // K7
       DS_CHECK_LAUNCH();
@@ -819,56 +803,19 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // The host reads the done flag every CHECK iterations, two reads behind,
   // so the stream never drains.  Without profiling (and with the CUDA-core or
   // structured inner product) the CHECK iterations are one CUDA graph,
-  // captured once per solve and replayed: 1 launch instead of ~5 CHECK, and
-  // each iteration's K5 + K6 sit in a conditional node that K2 switches on
-  // only when an update is due (otherwise they are not launched at all).
+  // captured once per solve and replayed: 1 launch instead of ~7 CHECK.
   constexpr int CHECK = 8;
   constexpr int NSLOT = 64;
   cudaEvent_t evs[NSLOT];
   for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   cudaGraphExec_t gexec = nullptr;
-  long long per_graph = 0, per_update = 0;
+  long long per_graph = 0;
   if (!op->ctx->prof.enabled && !use_tc && max_iter > 0) {
-    if (!op->side_stream) DS_CUDA(cudaStreamCreateWithFlags(&op->side_stream,
-                                                            cudaStreamNonBlocking));
     const long long l0 = launch_counter();
-    long long in_bodies = 0;
     cudaGraph_t graph = nullptr;
     DS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      cudaStreamCaptureStatus cs;
-      cudaGraph_t cap = nullptr;
-      DS_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cap, nullptr, nullptr, nullptr));
-      for (int k = 1; k <= CHECK; ++k) {  // CHECK is even: the r buffers' parities repeat
-        cudaGraphConditionalHandle h;
-        DS_CUDA(cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault));
-        k1_k2(k, h);
-        const cudaGraphNode_t* deps = nullptr;
-        size_t nd = 0;
-        DS_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd));
-        cudaGraphNodeParams cp{};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = h;
-        cp.conditional.type = cudaGraphCondTypeIf;
-        cp.conditional.size = 1;
-        cudaGraphNode_t node;
-        DS_CUDA(cudaGraphAddNode(&node, cap, deps, nullptr, nd, &cp));
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        DS_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
-                                                    cudaStreamSetCaptureDependencies));
-        const long long b0 = launch_counter();
-        DS_CUDA(cudaStreamBeginCaptureToGraph(op->side_stream, body, nullptr, nullptr, 0,
-                                              cudaStreamCaptureModeThreadLocal));
-        try {
-          k5_k6(k, op->side_stream);
-        } catch (...) {
-          cudaStreamEndCapture(op->side_stream, &body);
-          throw;
-        }
-        DS_CUDA(cudaStreamEndCapture(op->side_stream, &body));
-        in_bodies += launch_counter() - b0;
-        k7();
-      }
+      for (int k = 1; k <= CHECK; ++k) iteration(k);  // CHECK is even: parities repeat
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -878,9 +825,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     const cudaError_t inst = cudaGraphInstantiate(&gexec, graph, 0);
     cudaGraphDestroy(graph);
     DS_CUDA(inst);
-    per_update = in_bodies / CHECK;
-    per_graph = launch_counter() - l0 - in_bodies;
-    launch_counter() = l0;  // counted below, as launched
+    per_graph = launch_counter() - l0;
   }
   int issued = 0, waited = 0, replays = 0;
   for (int it = 1; it <= max_iter; it += gexec ? CHECK : 1) {
@@ -888,9 +833,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       DS_CUDA(cudaGraphLaunch(gexec, st));
       ++replays;
     } else {
-      k1_k2(it, 0);
-      k5_k6(it, st);
-      k7();
+      iteration(it);
     }
     if (gexec || it % CHECK == 0) {
       const int slot = issued % NSLOT;
@@ -906,18 +849,15 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
       }
     }
   }
-  long long graph_launches = 0;
   if (gexec) {
-    graph_launches = (long long)replays * per_graph;
+    // the capture counted one graph's launches; each further replay launches them again
+    launch_counter() += (long long)std::max(replays - 1, 0) * per_graph;
     cudaGraphExecDestroy(gexec);
   }
   if (use_sg) skewer_x_to_sorted(op, X, op->x.p, st);
   DS_CUDA(cudaEventRecord(ev1, st));
   DS_CUDA(cudaMemcpyAsync(&h, S, sizeof(h), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
-  // launches of the replayed graphs: the unconditional ones of every replay
-  // and the update bodies that ran (one per FP64 update after the start)
-  launch_counter() += graph_launches + (long long)std::max(h.n_updates, 0) * per_update;
   float ms = 0.f;
   DS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
   for (auto& e : evs) cudaEventDestroy(e);
