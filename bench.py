@@ -355,6 +355,7 @@ def run_batched(ctx, n_chunks=512, n_rhs=64, seed=0, plain_samples=6):
     launches0 = ctx.profile()["kernel_launches"]
     res = bs.solve_mixed_dev(bd, xd, mp)
     launches = ctx.profile()["kernel_launches"] - launches0
+    loop_its = bs.info()["graph_replays"]
     ctx.set_profiling(True)
     resp = bs.solve_mixed_dev(bd, xd, mp)
     prof = ctx.profile()
@@ -403,7 +404,12 @@ def run_batched(ctx, n_chunks=512, n_rhs=64, seed=0, plain_samples=6):
         "matvec_ms": mv_ms, "matvec_algorithmic_tflops": mv_flops / 1e12 if mv_flops else None,
         "matvec_tensor_frac_of_bf16_peak": None,
         "fp64_residual_ms_per_solve": prof["f64_ms"],
-        "graph_launches_per_solve": launches,
+        "kernel_launches_per_solve": launches,
+        "graph_launches_per_solve": 1,
+        "device_loop_iterations": loop_its,
+        "host_loop": ("none: after the first iteration the solve is one graph launch, a "
+                      "WHILE conditional node whose body is an iteration and a kernel that "
+                      "continues while a chunk is active"),
         "plain_fp64": {"sampled_solves": plain_samples, "sample_s": t_sum,
                        "iters_mean": it_sum / plain_samples,
                        "extrapolated_s": plain_est, "basis": "sample time per pixel x all pixels x RHS"},

@@ -1239,6 +1239,14 @@ void batch_autotune(ds_batch* B, bool force, double* best_ms_out) {
   g_tune[key] = {B->variant, B->rb};
 }
 
+// The device-side loop of the batched solve: counts the iteration just run
+// and continues while a chunk is active and fewer than `cap` have run.
+__global__ void k_batch_loop(cudaGraphConditionalHandle h, const int* active, int* count,
+                             int cap) {
+  const int n = ++*count;
+  cudaGraphSetConditional(h, (*active > 0 && n < cap) ? 1u : 0u);
+}
+
 // The batched solve on device vectors: rhs_dev and x_dev are [record][R] in
 // the caller's order (x0 = 0).  Per-(chunk, RHS) results go to the host
 // arrays that are given.
@@ -1323,35 +1331,57 @@ void batch_solve_dev(ds_batch* B, const ds_mixed_params& mp, const double* rhs_d
         DS_CUDA(cudaStreamSynchronize(st));
       }
     }
-  } else {
+  } else if (it < it_cap) {
+    // The rest of the solve is one graph launch: a WHILE conditional node
+    // whose body is one iteration followed by k_batch_loop, which counts the
+    // iterations on the device and keeps the loop going while a chunk is
+    // active and the count is under the cap (so the loop ends by itself).
     const long long launches0 = launch_counter();
-    DS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    B->loop_it.alloc(1);
+    DS_CUDA(cudaMemsetAsync(B->loop_it.p, 0, sizeof(int), st));
+    DS_CUDA(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    cudaGraphNodeParams cp{};
+    cudaGraphNode_t node;
     try {
-      issue_iteration();
+      DS_CUDA(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      DS_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      DS_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal));
+      try {
+        issue_iteration();
+        k_batch_loop<<<1, 1, 0, st>>>(h, B->active.p, B->loop_it.p, (int)(it_cap - it));
+        DS_CHECK_LAUNCH();
+      } catch (...) {
+        cudaStreamEndCapture(st, &body);
+        throw;
+      }
+      DS_CUDA(cudaStreamEndCapture(st, &body));
     } catch (...) {
-      cudaStreamEndCapture(st, &graph);
-      if (graph) cudaGraphDestroy(graph);
+      cudaGraphDestroy(graph);
+      graph = nullptr;
       cudaEventDestroy(ev0);
       cudaEventDestroy(ev1);
       throw;
     }
     const long long per_iter = launch_counter() - launches0;
-    DS_CUDA(cudaStreamEndCapture(st, &graph));
     const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
     if (inst != cudaSuccess) {
       cudaGraphDestroy(graph);
       DS_CUDA(inst);
     }
-    for (; it < it_cap && active > 0; ++it) {
-      DS_CUDA(cudaGraphLaunch(exec, st));
-      ++replays;
-      if (it % 8 == 7) {
-        DS_CUDA(cudaMemcpyAsync(&active, B->active.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        DS_CUDA(cudaStreamSynchronize(st));
-      }
-    }
-    // the capture counted one iteration's launches; each replay launches them
-    launch_counter() += (long long)(replays - 1) * per_iter;
+    DS_CUDA(cudaGraphLaunch(exec, st));
+    int ran = 0;
+    DS_CUDA(cudaMemcpyAsync(&ran, B->loop_it.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    replays = ran;
+    // the capture counted one iteration's launches; the loop ran `ran`
+    launch_counter() += (long long)(ran - 1) * per_iter;
   }
   DS_CUDA(cudaEventRecord(ev1, st));
   DS_CUDA(cudaStreamSynchronize(st));

@@ -144,6 +144,7 @@ struct ds_batch {
       s_tol_norm_b;
   ds::DevBuf<int> s_iter, s_n_updates, s_need, s_hold, s_done, s_converged, s_it_best, s_stalled;
   ds::DevBuf<int> chunk_done, chunk_update, active;
+  ds::DevBuf<int> loop_it;  // iterations run by the device-side loop of a solve
   ds::DevBuf<unsigned int> work;  // work-queue counters
   ds::DevBuf<unsigned short> panel;  // tensor-core variant: BF16 u panels (lazy)
   ds::DevBuf<int> err;               // tensor-core variant: time-out code
