@@ -32,6 +32,8 @@ DS_INNER_AUTO = 0
 DS_INNER_CUDA_CORE = 1
 DS_INNER_TENSOR = 2
 DS_INNER_STRUCTURED = 3
+DS_ITER_AUTO = 0
+DS_ITER_GRAPH = 1
 DS_BATCH_AUTO = -1
 DS_BATCH_CUDA_CORE = 0
 DS_BATCH_TENSOR = 1
@@ -162,6 +164,7 @@ SIGNATURES = {
     "ds_operator_set_dense_arith": (_i, [_vp, _i]),
     "ds_operator_get_dense_arith": (_i, [_vp, C.POINTER(C.c_int)]),
     "ds_operator_set_inner_matvec": (_i, [_vp, _i]),
+    "ds_operator_set_iteration_form": (_i, [_vp, _i]),
     "ds_solve_cf": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), _dp]),
     "ds_map_covar_diag": (_i, [_vp, _i, _dp, _i, _dp, C.POINTER(KernelParamsC),
                                C.POINTER(PcgParamsC), _dp, _ip, _ip]),

@@ -172,9 +172,10 @@ class Context:
         self.check(self._lib.ds_context_set_profiling(self.handle, int(bool(enable))), "profiling")
 
     def set_wait_limit(self, cycles: int = 0):
-        """Bound (SM clock cycles) of the batched tensor-core kernel's waits;
-        0 restores the default (4e9 cycles).  A wait that runs out makes the
-        call raise DsError with code DS_ERR_TIMEOUT."""
+        """Bound (SM clock cycles) of the device-side waits: the batched
+        tensor-core kernel's mbarrier waits and the persistent mixed solve's
+        grid barriers; 0 restores the default (4e9 cycles).  A wait that runs
+        out makes the call raise DsError with code DS_ERR_TIMEOUT."""
         self.check(self._lib.ds_context_set_wait_limit(self.handle, int(cycles)), "wait limit")
 
     def profile(self) -> dict:
@@ -261,6 +262,15 @@ class _WFVector:
              "tensor": _lib.DS_INNER_TENSOR, "structured": _lib.DS_INNER_STRUCTURED}[variant]
         self.ctx.check(self._lib.ds_operator_set_inner_matvec(self.handle, v),
                        "ds_operator_set_inner_matvec")
+
+    def set_iteration_form(self, form: str = "auto"):
+        """How solve_mixed launches its iterations: "auto" (one persistent
+        cooperative launch with the structured inner operator and a band
+        preconditioner, else a replayed CUDA graph) or "graph" (always the
+        graph of eight iterations)."""
+        v = {"auto": _lib.DS_ITER_AUTO, "graph": _lib.DS_ITER_GRAPH}[form]
+        self.ctx.check(self._lib.ds_operator_set_iteration_form(self.handle, v),
+                       "ds_operator_set_iteration_form")
 
     def set_cluster_preconditioner(self, n_skewers: int, n_per: int, cluster: int = 4,
                                    band: int = 16) -> int:

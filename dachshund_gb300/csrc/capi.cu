@@ -760,6 +760,14 @@ int ds_operator_set_inner_matvec(ds_operator* op, int variant) {
   });
 }
 
+int ds_operator_set_iteration_form(ds_operator* op, int form) {
+  if (!op) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    require(form == DS_ITER_AUTO || form == DS_ITER_GRAPH, "bad iteration form");
+    op->iter_form = form;
+  });
+}
+
 int ds_solve_cf(ds_context* ctx, int form, int n, const double* records,
                 const ds_kernel_params* kp, double* x) {
   if (!ctx) return DS_ERR_ARG;

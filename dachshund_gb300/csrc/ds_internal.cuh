@@ -339,6 +339,7 @@ struct ds_operator {
   ds::DevBuf<double> dense_part, dense_dot;
   ds::DevBuf<unsigned int> dense_cnt;
   int inner_variant = 0;     // inner matvec of the mixed form (InnerVariant)
+  int iter_form = 0;         // DS_ITER_AUTO / DS_ITER_GRAPH
   // skewer-band preconditioner of the mixed form (null: Jacobi)
   std::unique_ptr<ds::SkewerPC, ds::SkewerPCDeleter> pc;
   // structured operator for skewers on a shared z grid (null: pair kernels)

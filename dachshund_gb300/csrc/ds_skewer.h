@@ -36,6 +36,10 @@ struct SkewerGrid {
   // record-order copies for the mixed solve (built on first use)
   DevBuf<double> rwl, rwr, re, rb, rx;
   DevBuf<float> rpd;
+  // the persistent solve's CTA partials and barrier words (count, generation,
+  // error code)
+  DevBuf<double> p_part;
+  DevBuf<int> p_sync;
 };
 
 // The vectors a structured product addresses: pos maps a record to its
@@ -90,6 +94,17 @@ struct MapColumns {
   DevBuf<double> p64;              // var_s exp(-c_perp |dxy|^2)
   DevBuf<double> R;                // Q x n_sk x nz
 };
+
+struct OpF32;
+struct SkewerPC;
+// The structured mixed solve's iterations (band preconditioner, record
+// order) as one cooperative launch of CTAs that pass through the phases of
+// each iteration between bounded grid barriers; false when the launch's
+// conditions do not hold (nothing launched).  persistent_error reads (and
+// clears) the error code of its barriers: 0, or the phase that timed out.
+bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const SkewerVecs& sv,
+                          double* X, float* r0, float* r1, int max_iter, cudaStream_t st);
+int persistent_error(ds_operator* op, cudaStream_t st);
 
 // m = S_mp x (caller order, device) with the structured FP64 map; false when
 // the map or the operator has no grid (then nothing is launched).

@@ -24,6 +24,7 @@
 #include "ds_f32.h"
 #include "ds_learned.h"
 #include "ds_skewer.h"
+#include "ds_mixed_dev.cuh"
 #include "ds_ops.h"
 
 namespace ds {
@@ -101,32 +102,6 @@ __global__ void k_d2f(int n, const double* __restrict__ in, float* __restrict__ 
 }
 
 // ---- the iteration kernels -----------------------------------------------
-
-// Reliable-update decision after iteration `it` (st->rnorm, st->rmax set):
-// the recurrence residual fell by delta since the last update, reached
-// tol |b|, hit the iteration cap, or stagnated (did not halve in STALL_ITERS
-// iterations, which FP32 rounding can cause far from x or near tol; the
-// update then restarts the recurrence with beta = 0).
-constexpr int STALL_ITERS = 30;
-__device__ __forceinline__ bool update_due(MixedState* st, int it) {
-  if (st->rnorm < 0.5 * st->rbest) {
-    st->rbest = st->rnorm;
-    st->it_best = it;
-  }
-  const bool stall = it - st->it_best >= STALL_ITERS;
-  if (stall) st->stalled = 1;
-  return st->rnorm < st->delta * st->rmax || st->rnorm <= st->tol_norm_b ||
-         it >= st->max_iter || stall;
-}
-
-// Recurrence restart after an FP64 update that did not end the solve.
-__device__ __forceinline__ void restart_after_update(MixedState* st, double rt, double rz) {
-  st->beta = st->stalled ? 0.0 : rz / st->rz_old;
-  st->rmax = rt;
-  st->rbest = rt;
-  st->it_best = st->iter;
-  st->stalled = 0;
-}
 
 // Zero test of the initial guess: flag = 1 when every entry is 0.
 __global__ void k_is_zero(int n, const double* __restrict__ x, int* __restrict__ flag) {
@@ -810,7 +785,13 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   cudaGraphExec_t gexec = nullptr;
   long long per_graph = 0;
-  if (!op->ctx->prof.enabled && !use_tc && max_iter > 0) {
+  // With the structured inner operator and a band preconditioner the whole
+  // loop can be one cooperative launch (persist.cu); profiling keeps the
+  // per-kernel form, whose kernels it times one by one.
+  bool persisted = false;
+  if (use_sg && pc && op->iter_form == DS_ITER_AUTO && !op->ctx->prof.enabled && max_iter > 0)
+    persisted = run_mixed_persistent(op, f, pc, sv, X, rbuf[0], rbuf[1], max_iter, st);
+  if (!persisted && !op->ctx->prof.enabled && !use_tc && max_iter > 0) {
     const long long l0 = launch_counter();
     cudaGraph_t graph = nullptr;
     DS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -828,7 +809,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
     per_graph = launch_counter() - l0;
   }
   int issued = 0, waited = 0, replays = 0;
-  for (int it = 1; it <= max_iter; it += gexec ? CHECK : 1) {
+  for (int it = 1; !persisted && it <= max_iter; it += gexec ? CHECK : 1) {
     if (gexec) {
       DS_CUDA(cudaGraphLaunch(gexec, st));
       ++replays;
@@ -864,6 +845,12 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
 
+  if (persisted) {
+    const int code = persistent_error(op, st);
+    if (code)
+      throw Error{DS_ERR_TIMEOUT, "persistent mixed solve: a grid barrier wait timed out "
+                                  "(phase " + std::to_string(code) + ")"};
+  }
   if (use_tc) {
     int code = 0;
     DS_CUDA(cudaMemcpyAsync(&code, f.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));

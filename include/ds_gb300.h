@@ -148,8 +148,11 @@ int ds_context_get_profile(ds_context* ctx, ds_profile* out);
  * context; 0 restores the default of 4e9 cycles (about 2 s).  A wait that
  * runs out records its code, the kernel waits (with the default bound) for
  * its own MMAs and copies in flight, frees its tensor memory and returns, and
- * the call returns DS_ERR_TIMEOUT.  No reference counterpart (the reference
- * has no device code). */
+ * the call returns DS_ERR_TIMEOUT.  The same bound applies to each grid
+ * barrier wait of the persistent mixed solve (ds_operator_set_iteration_form):
+ * a CTA that runs out records the phase, every CTA leaves at its next
+ * barrier, and the call returns DS_ERR_TIMEOUT.  No reference counterpart
+ * (the reference has no device code). */
 int ds_context_set_wait_limit(ds_context* ctx, long long cycles);
 
 /* ---- the operator A over one pixel set --------------------------------- */
@@ -233,6 +236,18 @@ int ds_operator_get_dense_arith(ds_operator* op, int* arith);
 enum { DS_INNER_AUTO = 0, DS_INNER_CUDA_CORE = 1, DS_INNER_TENSOR = 2,
        DS_INNER_STRUCTURED = 3 };
 int ds_operator_set_inner_matvec(ds_operator* op, int variant);
+
+/* How the mixed-precision form launches its iterations (no reference
+ * counterpart).  DS_ITER_AUTO (default): with the structured inner operator
+ * and a band preconditioner (cluster or learned), the whole iteration loop
+ * is one cooperative launch whose CTAs stay resident and meet at bounded
+ * grid barriers (the call returns DS_ERR_TIMEOUT if a barrier wait runs out,
+ * see ds_context_set_wait_limit); otherwise, and with DS_ITER_GRAPH, eight
+ * iterations are one CUDA graph replayed until the solve ends.  Both run the
+ * same recurrence; sums are taken in a different order, so iteration counts
+ * can differ by rounding. */
+enum { DS_ITER_AUTO = 0, DS_ITER_GRAPH = 1 };
+int ds_operator_set_iteration_form(ds_operator* op, int form);
 
 /* ---- PCG ---------------------------------------------------------------- */
 /* PCGParams (lib/pcg.h:13-19); n is the operator's. */

@@ -152,3 +152,68 @@ def test_column_grid_refused_for_other_layouts(ctx):
         grid.set_column_grid(15, 10)
     grid.set_column_grid(16, 10)
     grid.close()
+
+
+@pytest.mark.parametrize("form", ["w", "sn"])
+@pytest.mark.parametrize("n_sk,n_per,cluster", [(64, 96, 4), (10, 50, 4)])
+def test_persistent_solve_matches_graph(ctx, form, n_sk, n_per, cluster):
+    """The structured mixed solve with the cluster preconditioner as one
+    cooperative launch (ds_operator_set_iteration_form AUTO) against the same
+    recurrence as a replayed graph of per-phase kernels (GRAPH): both stop on
+    the FP64 true residual <= tol |b|, their solutions agree with the oracle's
+    to 1e-6, their iteration counts to rounding, and the persistent solve's
+    launches do not grow with its iterations."""
+    w = synth.small(n_sk, n_per, 12.0 * np.sqrt(n_sk / 32), seed=23)
+    op, rec = make(ctx, form, w.pixels)
+    op.set_cluster_preconditioner(n_sk, n_per, cluster=cluster, band=16)
+    op.set_skewer_grid(n_sk, n_per)
+    mp = MixedParams(tol=1e-8)
+    op.set_iteration_form("graph")
+    xg, rg = op.solve_mixed(mp)
+    op.set_iteration_form("auto")
+    l0 = ctx.profile()["kernel_launches"]
+    xp, rp = op.solve_mixed(mp)
+    launches = ctx.profile()["kernel_launches"] - l0
+    assert rg.success and rp.success and rp.n_outer >= 1
+    assert launches < 40, (launches, rp.num_iters)
+    y = xp / rec[:, 3] if form == "w" else xp
+    assert np.linalg.norm(op.A_residual(y)) <= 1e-8 * (1 + 1e-6) * np.linalg.norm(rec[:, 4])
+    xo, ok, _, _ = oracle.solve_pcg(form, rec, VS, LP, LQ, 3000, 50, 1e-10, exact=True)
+    assert ok
+    scale = np.max(np.abs(xo))
+    assert np.max(np.abs(xp - xo)) / scale < 1e-6
+    assert np.max(np.abs(xp - xg)) / scale < 1e-6
+    assert abs(rp.num_iters - rg.num_iters) <= max(3, rg.num_iters // 10)
+    assert rp.residual_norms[0] == pytest.approx(rg.residual_norms[0], rel=1e-12)
+    # a second solve on the same operator (barrier words reused)
+    xp2, rp2 = op.solve_mixed(mp)
+    assert rp2.success and rp2.num_iters == rp.num_iters and np.array_equal(xp2, xp)
+    op.close()
+
+
+def test_persistent_barrier_timeout_is_reported_and_recoverable(ctx):
+    """The persistent solve's grid barriers are bounded: with a bound of one
+    SM clock cycle every CTA but the last to arrive gives up at the first
+    barrier, records the phase, and the launch ends; the solve raises
+    DS_ERR_TIMEOUT.  With the default bound the same operator then solves to
+    tolerance, so the failed launch left the context and buffers usable."""
+    from dachshund_gb300 import _lib
+
+    n_sk, n_per = 32, 64
+    w = synth.small(n_sk, n_per, 12.0, seed=29)
+    op, rec = make(ctx, "w", w.pixels)
+    op.set_cluster_preconditioner(n_sk, n_per, cluster=4, band=16)
+    op.set_skewer_grid(n_sk, n_per)
+    mp = MixedParams(tol=1e-8)
+    try:
+        ctx.set_wait_limit(1)
+        with pytest.raises(DsError) as ei:
+            op.solve_mixed(mp)
+        assert ei.value.code == _lib.DS_ERR_TIMEOUT
+    finally:
+        ctx.set_wait_limit(0)
+    x, res = op.solve_mixed(mp)
+    assert res.success
+    y = x / rec[:, 3]
+    assert np.linalg.norm(op.A_residual(y)) <= 1e-8 * (1 + 1e-6) * np.linalg.norm(rec[:, 4])
+    op.close()
