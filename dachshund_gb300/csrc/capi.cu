@@ -1,6 +1,8 @@
 // The C ABI (include/ds_gb300.h): argument checks, host <-> device staging,
 // object lifetimes and the mapping of internal errors to status codes.
 #include <atomic>
+#include <mutex>
+#include <unordered_set>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -11,6 +13,32 @@
 #include "ds_device.cuh"
 #include "ds_f32.h"
 #include "ds_ops.h"
+
+namespace ds {
+
+static std::mutex& streams_mutex() {
+  static std::mutex m;
+  return m;
+}
+static std::unordered_set<cudaStream_t>& live_streams() {
+  static std::unordered_set<cudaStream_t> s;
+  return s;
+}
+
+bool stream_alive(cudaStream_t s) {
+  std::lock_guard<std::mutex> lock(streams_mutex());
+  return live_streams().count(s) != 0;
+}
+
+void stream_register(cudaStream_t s, bool alive) {
+  std::lock_guard<std::mutex> lock(streams_mutex());
+  if (alive)
+    live_streams().insert(s);
+  else
+    live_streams().erase(s);
+}
+
+}  // namespace ds
 
 using namespace ds;
 
@@ -236,6 +264,7 @@ int ds_context_create(int device, ds_context** out) {
     if (prop.major < 10) throw Error{DS_ERR_NO_DEVICE, "device is not a Blackwell-class GPU"};
     ctx->num_sms = prop.multiProcessorCount;
     DS_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    stream_register(ctx->stream, true);
     // stream-ordered device buffers come from the default pool; keep what is
     // freed cached for the next allocations
     cudaMemPool_t pool;
@@ -252,6 +281,7 @@ void ds_context_destroy(ds_context* ctx) {
   if (!ctx) return;
   if (ctx->stream) {
     cudaStreamSynchronize(ctx->stream);
+    stream_register(ctx->stream, false);
     cudaStreamDestroy(ctx->stream);
   }
   delete ctx;

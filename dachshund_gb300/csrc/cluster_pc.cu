@@ -158,7 +158,7 @@ uint32_t morton2(uint32_t x, uint32_t y) {
 // z, then by skewer; each block of g n_per slots is padded with -1.
 void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>& sx,
                           const std::vector<double>& sy, const std::vector<double>& rz,
-                          std::vector<int>& crec, int& n_blocks) {
+                          std::vector<int>& crec, std::vector<int>& bsk, int& n_blocks) {
   const double x0 = *std::min_element(sx.begin(), sx.end());
   const double x1 = *std::max_element(sx.begin(), sx.end());
   const double y0 = *std::min_element(sy.begin(), sy.end());
@@ -197,6 +197,9 @@ void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>&
     clusters.push_back(std::move(c));
   }
   n_blocks = (int)clusters.size();
+  bsk.assign((size_t)n_blocks * g, -1);
+  for (int c = 0; c < n_blocks; ++c)
+    std::copy(clusters[c].begin(), clusters[c].end(), bsk.begin() + (size_t)c * g);
   const int B = g * n_per;
   crec.assign((size_t)n_blocks * B, -1);
   std::vector<int> recs;
@@ -226,9 +229,9 @@ void build_cluster_pc(ds_operator* op, int n_sk, int n_per, int g, int band) {
   DS_CUDA(cudaMemcpyAsync(sy.data(), dsy.p, n_sk * sizeof(double), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaMemcpyAsync(rz.data(), drz.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
-  std::vector<int> crec;
+  std::vector<int> crec, bsk;
   int n_blocks = 0;
-  plan_skewer_clusters(n_sk, n_per, g, sx, sy, rz, crec, n_blocks);
+  plan_skewer_clusters(n_sk, n_per, g, sx, sy, rz, crec, bsk, n_blocks);
 
   std::unique_ptr<SkewerPC, SkewerPCDeleter> pc(new SkewerPC());
   pc->n_sk = n_blocks;
@@ -240,6 +243,10 @@ void build_cluster_pc(ds_operator* op, int n_sk, int n_per, int g, int band) {
   DevBuf<int> nfb;
   nfb.alloc(1);
   DS_CUDA(cudaMemcpyAsync(pc->crec.p, crec.data(), n_slots * sizeof(int),
+                          cudaMemcpyHostToDevice, st));
+  pc->g = g;
+  pc->bsk.alloc(bsk.size());
+  DS_CUDA(cudaMemcpyAsync(pc->bsk.p, bsk.data(), bsk.size() * sizeof(int),
                           cudaMemcpyHostToDevice, st));
   DS_CUDA(cudaMemsetAsync(pc->L.p, 0, pc->L.bytes(), st));
   DS_CUDA(cudaMemsetAsync(nfb.p, 0, sizeof(int), st));

@@ -75,6 +75,14 @@ inline void require(bool ok, const char* msg) {
 // context.
 inline thread_local cudaStream_t g_alloc_stream = nullptr;
 
+// Streams of the live contexts (registered at ds_context_create, removed
+// before ds_context_destroy destroys the stream).  A buffer allocated in
+// stream order is freed in stream order while its stream exists, else with
+// cudaFree (which waits for the device), so an object destroyed after its
+// context (as a garbage collector may order it) never names a dead stream.
+bool stream_alive(cudaStream_t s);
+void stream_register(cudaStream_t s, bool alive);
+
 // Device buffer (owning).
 template <class T>
 struct DevBuf {
@@ -118,7 +126,7 @@ struct DevBuf {
   }
   void release() {
     if (p) {
-      if (async)
+      if (async && stream_alive(s))
         cudaFreeAsync(p, s);
       else
         cudaFree(p);

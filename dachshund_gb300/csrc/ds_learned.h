@@ -69,6 +69,10 @@ struct SkewerPC {
   DevBuf<float> L;    // band + 1 planes of n_sk n_per slots: L[k][k - m] at plane m
   DevBuf<int> crec;   // record of each slot (empty: slot = record)
   int n_fallback = 0;  // cluster factor: columns that fell back to Jacobi
+  // skewers per block and the skewers of each block (g per block, -1 on
+  // padding; empty: block b is skewer b, g = 1)
+  int g = 1;
+  DevBuf<int> bsk;
 };
 
 }  // namespace ds

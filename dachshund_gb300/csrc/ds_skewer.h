@@ -97,13 +97,15 @@ struct MapColumns {
 
 struct OpF32;
 struct SkewerPC;
-// The structured mixed solve's iterations (band preconditioner, record
-// order) as one cooperative launch of CTAs that pass through the phases of
-// each iteration between bounded grid barriers; false when the launch's
-// conditions do not hold (nothing launched).  persistent_error reads (and
+// The structured mixed solve's iterations (band preconditioner whose blocks
+// are whole skewers of the grid, record order) as one cooperative launch of
+// CTAs that each own whole blocks and pass through the phases of each
+// iteration between bounded grid barriers; r is the residual the start wrote
+// (the recurrence updates it in place); false when the launch's conditions
+// do not hold (nothing launched).  persistent_error reads (and
 // clears) the error code of its barriers: 0, or the phase that timed out.
 bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const SkewerVecs& sv,
-                          double* X, float* r0, float* r1, int max_iter, cudaStream_t st);
+                          double* X, float* r, int max_iter, cudaStream_t st);
 int persistent_error(ds_operator* op, cudaStream_t st);
 
 // m = S_mp x (caller order, device) with the structured FP64 map; false when

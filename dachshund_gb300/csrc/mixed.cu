@@ -790,7 +790,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // per-kernel form, whose kernels it times one by one.
   bool persisted = false;
   if (use_sg && pc && op->iter_form == DS_ITER_AUTO && !op->ctx->prof.enabled && max_iter > 0)
-    persisted = run_mixed_persistent(op, f, pc, sv, X, rbuf[0], rbuf[1], max_iter, st);
+    persisted = run_mixed_persistent(op, f, pc, sv, X, rbuf[0], max_iter, st);
   if (!persisted && !op->ctx->prof.enabled && !use_tc && max_iter > 0) {
     const long long l0 = launch_counter();
     cudaGraph_t graph = nullptr;

@@ -1,30 +1,36 @@
 // Persistent form of the structured mixed-precision iteration (no reference
 // counterpart; the recurrence is lib/pcg.h:27-160 with FP32 inner products
-// and FP64-accurate reliable updates, as in mixed.cu).
+// and FP64-accurate reliable updates, exactly as in mixed.cu).
 //
 // The per-kernel iteration (mixed.cu) spends most of its time waiting: each
-// of its kernels moves ~20 MB in ~20 us, the launch ramp, the chains of
-// dependent loads and the single CTA that reduces the partials at the end
-// of each kernel dominate.  Here one cooperative launch runs every
-// iteration: the CTAs stay resident and pass through phases separated by
-// grid-wide barriers, each CTA keeping its own copy of the CG scalars and
-// computing them from the same partials in the same order (so all copies
-// agree bit for bit and no CTA has to broadcast them):
-//   P1  p = z + beta p and the z-convolution levels of u = w p   (per skewer)
-//   P2  q = A32 p and the partial p.q                           (per skewer)
-//   P3  alpha = r.z / p.q; x += alpha p, r -= alpha q, z = G G^T r and the
-//       partials r.z, |r|^2                                     (per 256 slots)
-//   P4  the scalar recurrence: beta, |r|, the update test        (every CTA)
-// and, when an FP64 update is due, the structured FP64 residual (P5 levels,
-// P6 r64 = b - A x), the update (P7: r = r64, z = G G^T r, partials) and
-// its scalars (P8).  Three barriers per iteration, three more per update.
-// Data written by other CTAs during the kernel is read through L2
+// of its kernels moves a few MB of L2-resident data in ~20 us, and the
+// launch ramp, the chains of dependent loads and the single CTA that
+// reduces the partials at the end of each kernel dominate.  Here one
+// cooperative launch runs every iteration.  Each CTA owns whole blocks of the
+// band preconditioner (a cluster of neighbouring skewers, or one skewer) and
+// so every record of those skewers: only the structured product reads other
+// CTAs' data (the neighbour skewers' z-convolution levels).  The CTAs pass
+// through three phases per iteration, separated by grid-wide barriers, and
+// each keeps its own copy of the CG scalars, computed from the same partials
+// in the same order (so all copies agree bit for bit and nothing is
+// broadcast):
+//   A  p = z + beta p and the levels V^(L) of u = wr p, per owned skewer
+//                                                          (barrier: V read)
+//   B  q = A32 p and the partial p.q, per owned skewer     (barrier: alpha)
+//   C  alpha = r.z / p.q; x += alpha p, r -= alpha q; z = G G^T r over each
+//      owned block (in shared memory, no halo: G has no entry between
+//      blocks); partials r.z, |r|^2; then beta and the update test
+//                                                          (barrier: beta)
+// and, when an FP64 update is due, D the FP64 levels of u = wr x (barrier),
+// E r64 = b - A x and F r = r64, z = G G^T r with their partials (one CTA
+// owns both, so no barrier between them; barrier).
+// Data written by another CTA during the kernel is read through L2
 // (ld.global.cg), never from a possibly stale L1 line.
 //
 // Every barrier wait is bounded (`limit` SM clock cycles): a CTA that runs
-// out records an error code, and every CTA leaves at its next barrier; the
-// host reports DS_ERR_TIMEOUT.  The launch is cooperative, so all CTAs are
-// resident and a barrier always completes unless a CTA has left.
+// out records the barrier's code, and every CTA leaves at its next barrier;
+// the host reports DS_ERR_TIMEOUT.  The launch is cooperative (all CTAs
+// resident), so a barrier always completes unless a CTA has left.
 #include <algorithm>
 #include <cmath>
 
@@ -38,14 +44,20 @@
 namespace ds {
 namespace {
 
-constexpr int PT = 256;            // threads per CTA (also the slots per P3 tile)
-constexpr int PT_MAX_NPER = 1024;  // pixels per skewer at most
-constexpr int P_NB = 256;          // neighbour entries staged per round
-constexpr int P_MAXB = 32;         // band of the cluster factor at most
-constexpr int P_U = 8;             // neighbours per step in the apply phases
+constexpr int NT = 512;      // threads per CTA
+constexpr int MAX_S = 1024;  // slots (records) per preconditioner block
+constexpr int MAX_G = 8;     // skewers per block
+constexpr int NB = 128;      // neighbour entries staged per skewer per round
+constexpr int UF32 = 8;      // neighbour loads in flight per record: FP32 product
+constexpr int UF64 = 4;      // FP64 product
+constexpr int MAX_BAND = 32;
+constexpr int RPT = MAX_S / NT;  // records (slots) per thread
 
 struct PersistArgs {
-  int n, n_sk, n_per, n_slots, band, max_iter;
+  int n, n_per, n_blocks, S, g, band, max_iter;
+  const int* bsk;   // block -> its g skewers (-1: none); null: block b = skewer b
+  const int* crec;  // slot -> record (-1: padding); null: slot = record
+  const float* L;   // band + 1 planes of n_blocks S slots
   // FP32 inner operator
   const int *iptr, *iidx, *ilev;
   const float *ip32, *taps32;
@@ -56,17 +68,13 @@ struct PersistArgs {
   const double *op64, *taps64;
   int olmax;
   double* V64;
-  // record-order coefficients
+  // record-order coefficients and vectors
   const double *wl, *wr, *e, *b;
-  // record-order vectors
   double* x;
-  float *p, *q, *z, *r0, *r1;
+  float *p, *q, *r, *z;
   double* r64;
-  // cluster factor
-  const int* crec;
-  const float* L;
   // state and scratch
-  MixedState* S;
+  MixedState* S_;
   double *hist, *htrue, *part;
   unsigned int *bar_count, *bar_gen;
   int* err;
@@ -74,7 +82,7 @@ struct PersistArgs {
 };
 
 // Barrier codes: the phase whose closing barrier gave up.
-enum { B_LEVELS = 1, B_PRODUCT, B_STEP, B_LEVELS64, B_RESIDUAL, B_UPDATE };
+enum { B_LEVELS = 1, B_PRODUCT, B_STEP, B_LEVELS64, B_UPDATE };
 
 // Grid-wide barrier (all CTAs resident: cooperative launch).  Thread 0 reads
 // the generation before arriving; the last to arrive resets the count and
@@ -105,7 +113,6 @@ __device__ bool grid_sync(const PersistArgs& a, int code) {
           ok = 0;
           break;
         }
-        __nanosleep(64);
       }
     }
     __threadfence();
@@ -115,9 +122,13 @@ __device__ bool grid_sync(const PersistArgs& a, int code) {
   return ok_s != 0;
 }
 
-// Sum over the CTA of one value per thread, valid in every thread.
-__device__ __forceinline__ double cta_total(double v, double* red, double* out) {
-  const double s = block_sum<PT>(v, red);
+// Sum of n partials (stride, offset) in a fixed order, valid in every thread
+// of every CTA alike.
+__device__ __forceinline__ double partial_total(const double* part, int n, int stride, int off,
+                                                double* red, double* out) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += NT) v += __ldcg(part + (size_t)i * stride + off);
+  const double s = block_sum<NT>(v, red);
   if (threadIdx.x == 0) *out = s;
   __syncthreads();
   const double t = *out;
@@ -125,151 +136,205 @@ __device__ __forceinline__ double cta_total(double v, double* red, double* out) 
   return t;
 }
 
-// Sum of n partials (stride, offset) in a fixed order, in every CTA alike.
-__device__ __forceinline__ double partial_total(const double* part, int n, int stride, int off,
-                                                double* red, double* out) {
-  double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += PT) v += __ldcg(part + (size_t)i * stride + off);
-  return cta_total(v, red, out);
+__device__ __forceinline__ int skewer_of(const PersistArgs& a, int blk, int j) {
+  return a.bsk ? a.bsk[(size_t)blk * a.g + j] : (j == 0 ? blk : -1);
 }
 
-// Stages the offsets and factors of entries c0 .. c0 + cnt of a CSR row.
-template <typename T>
-__device__ __forceinline__ void stage_row(int c0, int cnt, const int* __restrict__ idx,
-                                          const int* __restrict__ lev,
-                                          const T* __restrict__ pv, size_t plane, int stride,
-                                          size_t* s_off, T* s_p) {
-  __syncthreads();
-  for (int t = threadIdx.x; t < cnt; t += PT) {
-    s_off[t] = (size_t)(lev[c0 + t] - 1) * plane + (size_t)idx[c0 + t] * stride;
-    s_p[t] = pv[c0 + t];
-  }
-  __syncthreads();
+__device__ __forceinline__ int record_of(const PersistArgs& a, int blk, int i) {
+  const size_t slot = (size_t)blk * a.S + i;
+  return a.crec ? a.crec[slot] : (int)slot;
 }
 
-// sum over the staged entries of p V[off + k] (V read through L2).
-template <typename T>
-__device__ __forceinline__ T staged_sum(int cnt, const size_t* s_off, const T* s_p,
-                                        const T* V, int k) {
-  T acc[P_U];
-#pragma unroll
-  for (int u = 0; u < P_U; ++u) acc[u] = T(0);
-  int i = 0;
-  for (; i + P_U <= cnt; i += P_U) {
-    T v[P_U];
-#pragma unroll
-    for (int u = 0; u < P_U; ++u) v[u] = __ldcg(V + s_off[i + u] + k);
-#pragma unroll
-    for (int u = 0; u < P_U; ++u) acc[u] = fma(s_p[i + u], v[u], acc[u]);
-  }
-  for (; i < cnt; ++i) acc[0] = fma(s_p[i], __ldcg(V + s_off[i] + k), acc[0]);
-  T s = T(0);
-#pragma unroll
-  for (int u = 0; u < P_U; ++u) s += acc[u];
-  return s;
-}
-
-// z = G G^T r over one tile of PT slots (halo `band` each side) from r
-// values produced by `rval` for any slot; returns the thread's own slot's
-// (index, r, z) through the references.
-template <class RVal>
-__device__ __forceinline__ void band_tile(const PersistArgs& a, int s0, float* rs, float* ts,
-                                          RVal&& rval, int& own, float& ri, float& zk) {
-  const int band = a.band;
-  const size_t ns = (size_t)a.n_slots;
-  auto index_of = [&](int slot) -> int {
-    if (slot < 0 || slot >= a.n_slots) return -1;
-    return a.crec ? a.crec[slot] : slot;
-  };
-  __syncthreads();
-  for (int i = threadIdx.x; i < PT + 2 * band; i += PT) {
-    const int pos = index_of(s0 - band + i);
-    rs[i] = pos >= 0 ? rval(pos) : 0.f;
-  }
-  __syncthreads();
-  const int k = s0 + threadIdx.x;
-  own = index_of(k);
-  ri = rs[threadIdx.x + band];
-  for (int i = threadIdx.x; i < PT + band; i += PT) {
-    const int j = s0 - band + i;
-    float t = 0.f;
-    if (j >= 0)
-      for (int m = 0; m <= band; ++m)
-        if (j + m < a.n_slots) t = fmaf(a.L[(size_t)m * ns + j + m], rs[i + m], t);
-    ts[i] = t;
-  }
-  __syncthreads();
-  zk = 0.f;
-  if (k < a.n_slots)
-    for (int m = 0; m <= band; ++m) zk = fmaf(a.L[(size_t)m * ns + k], ts[threadIdx.x + band - m], zk);
-}
-
-__global__ void __launch_bounds__(PT) k_mixed_persistent(PersistArgs a) {
-  __shared__ MixedState sS;
-  __shared__ double red[PT / 32];
-  __shared__ double tot;
-  __shared__ __align__(16) double su64[PT_MAX_NPER];  // u of one skewer (FP64 or FP32)
-  float* su = reinterpret_cast<float*>(su64);
-  __shared__ size_t s_off[P_NB];
-  __shared__ double s_p64[P_NB];
-  __shared__ float s_p32[P_NB];
-  __shared__ float rs[PT + 2 * P_MAXB];
-  __shared__ float ts[PT + P_MAXB];
-  const int tid = threadIdx.x;
+// Levels V^(L)[k] = sum_{|m| <= L} T_m u[k + m] (L = 0 .. lmax) of every
+// skewer of block blk, u = ufn(record) staged in shared memory (g n_per).
+template <typename T, class UFn>
+__device__ __forceinline__ void block_levels(const PersistArgs& a, int blk, int lmax,
+                                             const T* __restrict__ taps, T* __restrict__ V,
+                                             T* su, UFn&& ufn) {
+  const int m = a.g * a.n_per;
   const size_t n = (size_t)a.n;
-  const int n_tiles = (a.n_slots + PT - 1) / PT;
-  if (tid == 0) sS = *a.S;
   __syncthreads();
-  while (!sS.done && sS.iter <= a.max_iter + 1) {
-    const int it = sS.iter + 1;
-    float* rin = (it & 1) ? a.r0 : a.r1;   // rbuf[(it - 1) & 1]
-    float* rout = (it & 1) ? a.r1 : a.r0;  // rbuf[it & 1]
-    // ---- P1: p = z + beta p, levels of u = w p
-    const float beta = (float)sS.beta;
-    for (int s = blockIdx.x; s < a.n_sk; s += gridDim.x) {
-      __syncthreads();
-      for (int k = tid; k < a.n_per; k += PT) {
-        const size_t r = (size_t)s * a.n_per + k;
-        const float pv = fmaf(beta, __ldcg(a.p + r), __ldcg(a.z + r));
-        a.p[r] = pv;
-        su[k] = (float)a.wr[r] * pv;
-      }
-      __syncthreads();
-      for (int k = tid; k < a.n_per; k += PT) {
-        const size_t r = (size_t)s * a.n_per + k;
-        float acc = su[k];
-        a.V32[r] = acc;
-        for (int l = 1; l <= a.ilmax; ++l) {
-          float v = 0.f;
-          if (k + l < a.n_per) v = su[k + l];
-          if (k - l >= 0) v += su[k - l];
-          acc = fmaf(a.taps32[l], v, acc);
-          a.V32[(size_t)l * n + r] = acc;
-        }
+  for (int i = threadIdx.x; i < m; i += NT) {
+    const int j = i / a.n_per, k = i - j * a.n_per;
+    const int s = skewer_of(a, blk, j);
+    su[i] = s >= 0 ? ufn((size_t)s * a.n_per + k) : T(0);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += NT) {
+    const int j = i / a.n_per, k = i - j * a.n_per;
+    const int s = skewer_of(a, blk, j);
+    if (s < 0) continue;
+    const size_t r = (size_t)s * a.n_per + k;
+    T acc = su[i];
+    V[r] = acc;
+    for (int l = 1; l <= lmax; ++l) {
+      T v = T(0);
+      if (k + l < a.n_per) v = su[i + l];
+      if (k - l >= 0) v += su[i - l];
+      acc = fma(taps[l], v, acc);
+      V[(size_t)l * n + r] = acc;
+    }
+  }
+}
+
+// out[t] = sum over the neighbour list of the skewer of record t of
+// P V[(lev - 1) n + idx n_per + k], for the (up to RPT) records t = tid,
+// tid + NT, ... of block blk (record t: pixel k of the block's skewer j,
+// t = j n_per + k): the g lists are staged NB entries at a time; each step
+// keeps UF loads per record in flight.
+template <typename T, int UF>
+__device__ __forceinline__ void block_product(const PersistArgs& a, int blk,
+                                              const int* __restrict__ ptr,
+                                              const int* __restrict__ idx,
+                                              const int* __restrict__ lev,
+                                              const T* __restrict__ pv, const T* V,
+                                              size_t* s_off, T* s_p, int* s_cnt, T (&out)[RPT]) {
+  const int m = a.g * a.n_per;
+  const size_t n = (size_t)a.n;
+  T acc[RPT][UF];
+#pragma unroll
+  for (int t = 0; t < RPT; ++t)
+#pragma unroll
+    for (int u = 0; u < UF; ++u) acc[t][u] = T(0);
+  int jj[RPT], kk[RPT];
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = threadIdx.x + t * NT;
+    jj[t] = i < m ? i / a.n_per : -1;
+    kk[t] = i < m ? i - jj[t] * a.n_per : 0;
+  }
+  for (int c0 = 0;; c0 += NB) {
+    __syncthreads();
+    if (threadIdx.x < MAX_G) {
+      const int j = threadIdx.x;
+      const int s = j < a.g ? skewer_of(a, blk, j) : -1;
+      const int len = s >= 0 ? ptr[s + 1] - ptr[s] : 0;
+      s_cnt[j] = max(0, min(NB, len - c0));
+      s_cnt[MAX_G + j] = len - c0 > NB;  // another round
+    }
+    for (int t = threadIdx.x; t < a.g * NB; t += NT) {
+      const int j = t / NB, e = t - j * NB;
+      const int s = skewer_of(a, blk, j);
+      if (s < 0) continue;
+      const int q = ptr[s] + c0 + e;
+      if (q < ptr[s + 1]) {
+        s_off[t] = (size_t)(lev[q] - 1) * n + (size_t)idx[q] * a.n_per;
+        s_p[t] = pv[q];
       }
     }
+    __syncthreads();
+    int cnt[RPT];
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) cnt[t] = jj[t] >= 0 ? s_cnt[jj[t]] : 0;
+    int cmax = 0;
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) cmax = max(cmax, cnt[t]);
+    for (int e = 0; e < cmax; e += UF) {
+      T v[RPT][UF];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t)
+#pragma unroll
+        for (int u = 0; u < UF; ++u)
+          v[t][u] = e + u < cnt[t] ? __ldcg(V + s_off[jj[t] * NB + e + u] + kk[t]) : T(0);
+#pragma unroll
+      for (int t = 0; t < RPT; ++t)
+#pragma unroll
+        for (int u = 0; u < UF; ++u)
+          if (e + u < cnt[t]) acc[t][u] = fma(s_p[jj[t] * NB + e + u], v[t][u], acc[t][u]);
+    }
+    int more = 0;
+    for (int j = 0; j < MAX_G; ++j) more |= s_cnt[MAX_G + j];
+    if (!more) break;
+  }
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    T s = T(0);
+#pragma unroll
+    for (int u = 0; u < UF; ++u) s += acc[t][u];
+    out[t] = s;
+  }
+}
+
+// z = G G^T r over block blk from r in shared memory (slot order, 0 on
+// padding): t = G^T r, then z = G t; returns z of the thread's slots.
+template <int BAND>
+__device__ __forceinline__ void block_precond(const PersistArgs& a, int blk, const float* rs,
+                                              float* ts, float (&zk)[RPT]) {
+  const int band = BAND >= 0 ? BAND : a.band;
+  const size_t ns = (size_t)a.n_blocks * a.S;
+  const size_t s0 = (size_t)blk * a.S;
+  const float* __restrict__ L = a.L;
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = threadIdx.x + t * NT;
+    if (i < a.S) {
+      float v = 0.f;
+#pragma unroll
+      for (int m = 0; m <= (BAND >= 0 ? BAND : MAX_BAND); ++m)
+        if (m <= band && i + m < a.S) v = fmaf(L[(size_t)m * ns + s0 + i + m], rs[i + m], v);
+      ts[i] = v;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = threadIdx.x + t * NT;
+    float v = 0.f;
+    if (i < a.S) {
+#pragma unroll
+      for (int m = 0; m <= (BAND >= 0 ? BAND : MAX_BAND); ++m)
+        if (m <= band && i - m >= 0) v = fmaf(L[(size_t)m * ns + s0 + i], ts[i - m], v);
+    }
+    zk[t] = v;
+  }
+}
+
+template <int BAND>
+__global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
+  __shared__ MixedState sS;
+  __shared__ double red[NT / 32];
+  __shared__ double tot;
+  __shared__ __align__(16) double su64[MAX_S];  // u of a block (FP64 or FP32)
+  __shared__ float rs[MAX_S];
+  __shared__ float ts[MAX_S];
+  __shared__ size_t s_off[MAX_G * NB];
+  __shared__ double s_p64[MAX_G * NB];
+  __shared__ int s_cnt[2 * MAX_G];
+  float* su = reinterpret_cast<float*>(su64);
+  float* s_p32 = reinterpret_cast<float*>(s_p64);
+  const int tid = threadIdx.x;
+  const int G = gridDim.x;
+  if (tid == 0) sS = *a.S_;
+  __syncthreads();
+  // the recurrence sets done by iteration max_iter at the latest (the
+  // update it forces there ends the solve); the bound keeps hist in range
+  while (!sS.done && sS.iter < a.max_iter) {
+    const int it = sS.iter + 1;
+    // ---- A: p = z + beta p, levels of u = wr p
+    {
+      const float beta = (float)sS.beta;
+      for (int blk = blockIdx.x; blk < a.n_blocks; blk += G)
+        block_levels<float>(a, blk, a.ilmax, a.taps32, a.V32, su, [&](size_t r) {
+          const float pv = fmaf(beta, __ldcg(a.p + r), __ldcg(a.z + r));
+          a.p[r] = pv;
+          return (float)a.wr[r] * pv;
+        });
+    }
     if (!grid_sync(a, B_LEVELS)) break;
-    // ---- P2: q = A32 p, partial p.q
+    // ---- B: q = A32 p, partial p.q
     double dq = 0.0;
-    for (int s = blockIdx.x; s < a.n_sk; s += gridDim.x) {
-      const int q0 = a.iptr[s], q1 = a.iptr[s + 1];
-      float acc[PT_MAX_NPER / PT];
+    for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
+      float acc[RPT];
+      block_product<float, UF32>(a, blk, a.iptr, a.iidx, a.ilev, a.ip32, a.V32, s_off, s_p32, s_cnt,
+                           acc);
 #pragma unroll
-      for (int t = 0; t < PT_MAX_NPER / PT; ++t) acc[t] = 0.f;
-      for (int c0 = q0; c0 < q1; c0 += P_NB) {
-        const int cnt = min(P_NB, q1 - c0);
-        stage_row<float>(c0, cnt, a.iidx, a.ilev, a.ip32, n, a.n_per, s_off, s_p32);
-#pragma unroll
-        for (int t = 0; t < PT_MAX_NPER / PT; ++t) {
-          const int k = tid + t * PT;
-          if (k < a.n_per) acc[t] += staged_sum<float>(cnt, s_off, s_p32, a.V32, k);
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < PT_MAX_NPER / PT; ++t) {
-        const int k = tid + t * PT;
-        if (k >= a.n_per) break;
-        const size_t r = (size_t)s * a.n_per + k;
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        if (i >= a.g * a.n_per) continue;
+        const int j = i / a.n_per;
+        const int s = skewer_of(a, blk, j);
+        if (s < 0) continue;
+        const size_t r = (size_t)s * a.n_per + (i - j * a.n_per);
         const float pv = __ldcg(a.p + r);
         const float qv = fmaf((float)a.wl[r], acc[t], (float)a.e[r] * pv);
         a.q[r] = qv;
@@ -277,42 +342,58 @@ __global__ void __launch_bounds__(PT) k_mixed_persistent(PersistArgs a) {
       }
     }
     {
-      const double bs = block_sum<PT>(dq, red);
+      const double bs = block_sum<NT>(dq, red);
       if (tid == 0) a.part[blockIdx.x] = bs;
     }
     if (!grid_sync(a, B_PRODUCT)) break;
-    // ---- P3: alpha; x, r, z over slot tiles; partials r.z, |r|^2
-    const double pq = partial_total(a.part, gridDim.x, 1, 0, red, &tot);
+    // ---- C: alpha; x, r, z per owned block; partials r.z, |r|^2
+    const double pq = partial_total(a.part, G, 1, 0, red, &tot);
     const double alpha_d = sS.rz / pq;
     const float alpha = (float)alpha_d;
     double rz = 0.0, rr = 0.0;
-    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-      int own;
-      float ri, zk;
-      band_tile(a, t * PT, rs, ts,
-                [&](int pos) { return fmaf(-alpha, __ldcg(a.q + pos), __ldcg(rin + pos)); }, own,
-                ri, zk);
-      if (own >= 0) {
-        rout[own] = ri;
-        a.x[own] = fma(alpha_d, (double)__ldcg(a.p + own), __ldcg(a.x + own));
-        a.z[own] = zk;
-        rz = fma((double)ri, (double)zk, rz);
+    for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
+      __syncthreads();  // rs, ts of the previous block read
+      int rec[RPT];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        rec[t] = i < a.S ? record_of(a, blk, i) : -1;
+        if (i < a.S) {
+          float rv = 0.f;
+          if (rec[t] >= 0) {
+            const int k = rec[t];
+            rv = fmaf(-alpha, __ldcg(a.q + k), __ldcg(a.r + k));
+            a.x[k] = fma(alpha_d, (double)__ldcg(a.p + k), __ldcg(a.x + k));
+            a.r[k] = rv;
+          }
+          rs[i] = rv;
+        }
+      }
+      __syncthreads();
+      float zk[RPT];
+      block_precond<BAND>(a, blk, rs, ts, zk);
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        if (rec[t] < 0) continue;
+        const float ri = rs[tid + t * NT];
+        a.z[rec[t]] = zk[t];
+        rz = fma((double)ri, (double)zk[t], rz);
         rr = fma((double)ri, (double)ri, rr);
       }
     }
     {
-      const double b1 = block_sum<PT>(rz, red);
-      const double b2 = block_sum<PT>(rr, red);
+      const double b1 = block_sum<NT>(rz, red);
+      const double b2 = block_sum<NT>(rr, red);
       if (tid == 0) {
-        a.part[(size_t)gridDim.x + 2 * blockIdx.x] = b1;
-        a.part[(size_t)gridDim.x + 2 * blockIdx.x + 1] = b2;
+        a.part[(size_t)G + 2 * blockIdx.x] = b1;
+        a.part[(size_t)G + 2 * blockIdx.x + 1] = b2;
       }
     }
     if (!grid_sync(a, B_STEP)) break;
-    // ---- P4: the scalars (every CTA alike)
+    // the step's scalars (those of K2 in the per-kernel form), every CTA alike
     {
-      const double trz = partial_total(a.part + gridDim.x, gridDim.x, 2, 0, red, &tot);
-      const double trr = partial_total(a.part + gridDim.x, gridDim.x, 2, 1, red, &tot);
+      const double trz = partial_total(a.part + G, G, 2, 0, red, &tot);
+      const double trr = partial_total(a.part + G, G, 2, 1, red, &tot);
       if (tid == 0) {
         sS.alpha = alpha_d;
         sS.pq = pq;
@@ -322,89 +403,75 @@ __global__ void __launch_bounds__(PT) k_mixed_persistent(PersistArgs a) {
         sS.iter = it;
         if (blockIdx.x == 0) a.hist[it] = sS.rnorm;
         sS.rmax = fmax(sS.rmax, sS.rnorm);
-        const bool upd = update_due(&sS, it);
-        sS.need_update = upd ? 1 : 0;
+        sS.need_update = update_due(&sS, it) ? 1 : 0;
         sS.beta = sS.rz / sS.rz_old;
       }
       __syncthreads();
     }
     if (!sS.need_update) continue;
-    // ---- P5: levels of u = w x (FP64)
-    for (int s = blockIdx.x; s < a.n_sk; s += gridDim.x) {
-      __syncthreads();
-      for (int k = tid; k < a.n_per; k += PT) {
-        const size_t r = (size_t)s * a.n_per + k;
-        su64[k] = a.wr[r] * __ldcg(a.x + r);
-      }
-      __syncthreads();
-      for (int k = tid; k < a.n_per; k += PT) {
-        const size_t r = (size_t)s * a.n_per + k;
-        double acc = su64[k];
-        a.V64[r] = acc;
-        for (int l = 1; l <= a.olmax; ++l) {
-          double v = 0.0;
-          if (k + l < a.n_per) v = su64[k + l];
-          if (k - l >= 0) v += su64[k - l];
-          acc = fma(a.taps64[l], v, acc);
-          a.V64[(size_t)l * n + r] = acc;
-        }
-      }
-    }
+    // ---- D: FP64 levels of u = wr x
+    for (int blk = blockIdx.x; blk < a.n_blocks; blk += G)
+      block_levels<double>(a, blk, a.olmax, a.taps64, a.V64, su64,
+                           [&](size_t r) { return a.wr[r] * __ldcg(a.x + r); });
     if (!grid_sync(a, B_LEVELS64)) break;
-    // ---- P6: r64 = b - A x (FP64)
-    for (int s = blockIdx.x; s < a.n_sk; s += gridDim.x) {
-      const int q0 = a.optr[s], q1 = a.optr[s + 1];
-      double acc[PT_MAX_NPER / PT];
+    // ---- E, F: r64 = b - A x per owned skewer; r = r64, z = G G^T r
+    rz = 0.0;
+    rr = 0.0;
+    for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
+      double acc[RPT];
+      block_product<double, UF64>(a, blk, a.optr, a.oidx, a.olev, a.op64, a.V64, s_off, s_p64, s_cnt,
+                            acc);
 #pragma unroll
-      for (int t = 0; t < PT_MAX_NPER / PT; ++t) acc[t] = 0.0;
-      for (int c0 = q0; c0 < q1; c0 += P_NB) {
-        const int cnt = min(P_NB, q1 - c0);
-        stage_row<double>(c0, cnt, a.oidx, a.olev, a.op64, n, a.n_per, s_off, s_p64);
-#pragma unroll
-        for (int t = 0; t < PT_MAX_NPER / PT; ++t) {
-          const int k = tid + t * PT;
-          if (k < a.n_per) acc[t] += staged_sum<double>(cnt, s_off, s_p64, a.V64, k);
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < PT_MAX_NPER / PT; ++t) {
-        const int k = tid + t * PT;
-        if (k >= a.n_per) break;
-        const size_t r = (size_t)s * a.n_per + k;
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        if (i >= a.g * a.n_per) continue;
+        const int j = i / a.n_per;
+        const int s = skewer_of(a, blk, j);
+        if (s < 0) continue;
+        const size_t r = (size_t)s * a.n_per + (i - j * a.n_per);
         const double y = fma(a.wl[r], acc[t], a.e[r] * __ldcg(a.x + r));
         a.r64[r] = a.b[r] - y;
       }
-    }
-    if (!grid_sync(a, B_RESIDUAL)) break;
-    // ---- P7: r = r64, z = G G^T r, partials
-    rz = 0.0;
-    rr = 0.0;
-    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-      int own;
-      float ri, zk;
-      band_tile(a, t * PT, rs, ts, [&](int pos) { return (float)__ldcg(a.r64 + pos); }, own,
-                ri, zk);
-      if (own >= 0) {
-        const double rd = __ldcg(a.r64 + own);
-        rout[own] = ri;
-        a.z[own] = zk;
-        rz = fma((double)ri, (double)zk, rz);
-        rr = fma(rd, rd, rr);
+      __syncthreads();  // the block's r64 written (read below in slot order)
+      int rec[RPT];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        rec[t] = i < a.S ? record_of(a, blk, i) : -1;
+        if (i < a.S) {
+          float rv = 0.f;
+          if (rec[t] >= 0) {
+            const double rd = __ldcg(a.r64 + rec[t]);
+            rv = (float)rd;
+            a.r[rec[t]] = rv;
+            rr = fma(rd, rd, rr);
+          }
+          rs[i] = rv;
+        }
+      }
+      __syncthreads();
+      float zk[RPT];
+      block_precond<BAND>(a, blk, rs, ts, zk);
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        if (rec[t] < 0) continue;
+        a.z[rec[t]] = zk[t];
+        rz = fma((double)rs[tid + t * NT], (double)zk[t], rz);
       }
     }
     {
-      const double b1 = block_sum<PT>(rz, red);
-      const double b2 = block_sum<PT>(rr, red);
+      const double b1 = block_sum<NT>(rz, red);
+      const double b2 = block_sum<NT>(rr, red);
       if (tid == 0) {
-        a.part[(size_t)gridDim.x + 2 * blockIdx.x] = b1;
-        a.part[(size_t)gridDim.x + 2 * blockIdx.x + 1] = b2;
+        a.part[(size_t)G + 2 * blockIdx.x] = b1;
+        a.part[(size_t)G + 2 * blockIdx.x + 1] = b2;
       }
     }
     if (!grid_sync(a, B_UPDATE)) break;
-    // ---- P8: the update's scalars
+    // the update's scalars (those of K6), every CTA alike
     {
-      const double trz = partial_total(a.part + gridDim.x, gridDim.x, 2, 0, red, &tot);
-      const double trr = partial_total(a.part + gridDim.x, gridDim.x, 2, 1, red, &tot);
+      const double trz = partial_total(a.part + G, G, 2, 0, red, &tot);
+      const double trr = partial_total(a.part + G, G, 2, 1, red, &tot);
       if (tid == 0) {
         const double rt = sqrt(trr);
         sS.rtrue = rt;
@@ -426,41 +493,58 @@ __global__ void __launch_bounds__(PT) k_mixed_persistent(PersistArgs a) {
       }
       __syncthreads();
     }
-    // the next phase P3 reuses part[gridDim.x ..]: every CTA has read it
-    // above, and two barriers (P1 | P2, P2 | P3) come before it is rewritten
   }
   if (blockIdx.x == 0 && tid == 0) {
     sS.skip_update = 1;
-    *a.S = sS;
+    *a.S_ = sS;
   }
+}
+
+// CTAs of the cooperative launch: one per block, at most the resident count.
+template <int BAND>
+int persistent_grid(int num_sms, int n_blocks) {
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    DS_CUDA(cudaFuncSetAttribute(k_mixed_persistent<BAND>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
+    DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_persistent<BAND>, NT,
+                                                          0));
+  }
+  return std::min(per_sm * num_sms, n_blocks);
 }
 
 }  // namespace
 
-// The structured mixed solve's iterations as one cooperative launch; false
-// when its conditions do not hold (then the caller runs the per-kernel
-// iteration).  X, vectors and coefficients in record order; S initialised
-// by the start kernels.
 bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const SkewerVecs& sv,
-                          double* X, float* r0, float* r1, int max_iter, cudaStream_t st) {
+                          double* X, float* r, int max_iter, cudaStream_t st) {
   SkewerGrid& g = *op->sgrid;
-  if (!pc || pc->band > P_MAXB || g.n_per > PT_MAX_NPER || pc->n_per * pc->n_sk <= 0) return false;
+  if (!pc || pc->band > MAX_BAND || pc->g > MAX_G || pc->n_per > MAX_S || pc->n_sk <= 0)
+    return false;
+  // blocks of whole skewers of the grid: g skewers of n_per records each
+  if (pc->n_per != pc->g * g.n_per || (pc->g > 1 && !pc->bsk.p) ||
+      (long long)pc->n_sk * pc->g < g.n_sk)
+    return false;
   if (!g.inner.ptr.p || !g.V32.p || !g.V64.p) return false;
-  int per_sm = 0;
-  DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_persistent, PT, 0));
-  if (per_sm <= 0) return false;
-  const int grid = std::min(per_sm * op->ctx->num_sms,
-                            std::max(g.n_sk, (pc->n_sk * pc->n_per + PT - 1) / PT));
+  const int band = pc->band;
+  const int grid = band == 16  ? persistent_grid<16>(op->ctx->num_sms, pc->n_sk)
+                   : band == 2 ? persistent_grid<2>(op->ctx->num_sms, pc->n_sk)
+                               : persistent_grid<-1>(op->ctx->num_sms, pc->n_sk);
+  if (grid <= 0) return false;
   g.p_part.alloc((size_t)3 * grid);
   g.p_sync.alloc(3);
-  DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, 3 * sizeof(unsigned int), st));
+  DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, 3 * sizeof(int), st));
   PersistArgs a{};
   a.n = op->n;
-  a.n_sk = g.n_sk;
   a.n_per = g.n_per;
-  a.n_slots = pc->n_sk * pc->n_per;
-  a.band = pc->band;
+  a.n_blocks = pc->n_sk;
+  a.S = pc->n_per;
+  a.g = pc->g;
+  a.band = band;
   a.max_iter = max_iter;
+  a.bsk = pc->bsk.p;  // null: the learned per-skewer factor (block b = skewer b)
+  a.crec = pc->crec.p;
+  a.L = pc->L.p;
   a.iptr = g.inner.ptr.p;
   a.iidx = g.inner.idx.p;
   a.ilev = g.inner.lev.p;
@@ -482,13 +566,10 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.x = X;
   a.p = f.p.p;
   a.q = f.q.p;
+  a.r = r;
   a.z = f.z.p;
-  a.r0 = r0;
-  a.r1 = r1;
   a.r64 = op->r.p;
-  a.crec = pc->crec.p;
-  a.L = pc->L.p;
-  a.S = f.state.p;
+  a.S_ = f.state.p;
   a.hist = f.hist.p;
   a.htrue = f.htrue.p;
   a.part = g.p_part.p;
@@ -497,8 +578,10 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.err = g.p_sync.p + 2;
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
   void* args[] = {&a};
-  DS_CUDA(cudaLaunchCooperativeKernel((void*)k_mixed_persistent, dim3(grid), dim3(PT), args, 0,
-                                      st));
+  const void* fn = band == 16  ? (const void*)k_mixed_persistent<16>
+                   : band == 2 ? (const void*)k_mixed_persistent<2>
+                               : (const void*)k_mixed_persistent<-1>;
+  DS_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NT), args, 0, st));
   DS_CHECK_LAUNCH();
   return true;
 }

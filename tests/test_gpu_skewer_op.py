@@ -155,7 +155,8 @@ def test_column_grid_refused_for_other_layouts(ctx):
 
 
 @pytest.mark.parametrize("form", ["w", "sn"])
-@pytest.mark.parametrize("n_sk,n_per,cluster", [(64, 96, 4), (10, 50, 4)])
+@pytest.mark.parametrize("n_sk,n_per,cluster", [(64, 96, 4), (10, 50, 4), (24, 40, 8),
+                                               (12, 64, 1)])
 def test_persistent_solve_matches_graph(ctx, form, n_sk, n_per, cluster):
     """The structured mixed solve with the cluster preconditioner as one
     cooperative launch (ds_operator_set_iteration_form AUTO) against the same
