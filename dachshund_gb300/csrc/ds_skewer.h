@@ -40,6 +40,11 @@ struct SkewerGrid {
   // error code)
   DevBuf<double> p_part;
   DevBuf<int> p_sync;
+  // the longest FP32 neighbour list of a preconditioner block (for the
+  // preconditioner and inner cutoff it was counted for)
+  const void* res_pc = nullptr;
+  double res_cut = 0.0;
+  int res_max_list = 0;
 };
 
 // The vectors a structured product addresses: pos maps a record to its

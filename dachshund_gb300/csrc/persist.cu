@@ -34,7 +34,10 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cuda_fp16.h>
+
 #include "ds_device.cuh"
+#include "ds_ff.cuh"
 #include "ds_f32.h"
 #include "ds_learned.h"
 #include "ds_mixed_dev.cuh"
@@ -47,9 +50,11 @@ namespace {
 constexpr int NT = 512;      // threads per CTA
 constexpr int MAX_S = 1024;  // slots (records) per preconditioner block
 constexpr int MAX_G = 8;     // skewers per block
-constexpr int NB = 128;      // neighbour entries staged per skewer per round
+constexpr int NB = 128;      // neighbour entries staged per skewer per round (general form)
+constexpr int NB_R = 32;     // the same for the resident form's FP64 residual
 constexpr int UF32 = 8;      // neighbour loads in flight per record: FP32 product
 constexpr int UF64 = 4;      // FP64 product
+constexpr int UFR = 12;      // FP32 product of the resident form (one accumulator per record)
 constexpr int MAX_BAND = 32;
 constexpr int RPT = MAX_S / NT;  // records (slots) per thread
 
@@ -76,7 +81,7 @@ struct PersistArgs {
   // state and scratch
   MixedState* S_;
   double *hist, *htrue, *part;
-  unsigned int *bar_count, *bar_gen;
+  unsigned int* bar;  // barrier words: count, error code, a flag line per CTA
   int* err;
   long long limit;
 };
@@ -84,56 +89,134 @@ struct PersistArgs {
 // Barrier codes: the phase whose closing barrier gave up.
 enum { B_LEVELS = 1, B_PRODUCT, B_STEP, B_LEVELS64, B_UPDATE };
 
-// Grid-wide barrier (all CTAs resident: cooperative launch).  Thread 0 reads
-// the generation before arriving; the last to arrive resets the count and
-// bumps the generation; the others poll it, bounded by `limit`.  Returns
-// false when this CTA or another one has given up.
-__device__ bool grid_sync(const PersistArgs& a, int code) {
+// Grid-wide barrier (all CTAs resident: cooperative launch).  Every CTA's
+// thread 0 arrives on one monotonic count (atom.acq_rel: it releases the
+// CTA's writes, ordered before it by the CTA barrier); the CTA whose arrival
+// completes the epoch (count == epoch x CTAs) releases the others by writing
+// the epoch into each CTA's own flag line (a fence, then plain stores), and
+// each CTA polls only its own line (ld.acquire).  No line is polled by more
+// than one CTA, so the polls do not queue up on one L2 slice in front of the
+// data, and the epoch is counted locally, so arriving takes one atomic.  A
+// poll that runs out (`limit` SM cycles) records `code`, writes ERR_FLAG into
+// every flag line and returns false, as does a CTA that finds ERR_FLAG.
+// Words: [0] count, [1] error code, [BAR_LINE (1 + c)] flag of CTA c.
+constexpr int BAR_LINE = 32;  // words per 128-byte line
+constexpr unsigned int ERR_FLAG = 0xffffffffu;
+__device__ bool grid_sync(const PersistArgs& a, int code, unsigned int& epoch) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned int* gen = a.bar_gen;
-    volatile int* err = a.err;
-    const unsigned int g = *gen;
-    __threadfence();
-    if (atomicAdd(a.bar_count, 1u) == gridDim.x - 1) {
-      *(volatile unsigned int*)a.bar_count = 0;
-      __threadfence();
-      atomicAdd(a.bar_gen, 1u);
+    ++epoch;
+    const unsigned int target = epoch * gridDim.x;
+    unsigned int old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;"
+                 : "=r"(old)
+                 : "l"(a.bar)
+                 : "memory");
+    auto release_all = [&](unsigned int v) {
+      asm volatile("fence.acq_rel.gpu;" ::: "memory");
+      for (unsigned int c = 0; c < gridDim.x; ++c)
+        asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(a.bar + (size_t)(1 + c) * BAR_LINE),
+                     "r"(v)
+                     : "memory");
+    };
+    if (old + 1 == target) {
+      release_all(*(volatile int*)a.err ? ERR_FLAG : epoch);
     } else {
+      const unsigned int* flag = a.bar + (size_t)(1 + blockIdx.x) * BAR_LINE;
       const long long t0 = clock64();
-      while (*gen == g) {
-        if (*err) {
+      for (;;) {
+        unsigned int f;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(f) : "l"(flag) : "memory");
+        if (f == epoch) break;
+        if (f == ERR_FLAG) {
           ok = 0;
           break;
         }
         if (clock64() - t0 > a.limit) {
           atomicExch(a.err, code);
+          release_all(ERR_FLAG);
           ok = 0;
           break;
         }
       }
     }
-    __threadfence();
-    ok_s = ok && *err == 0;
+    ok_s = ok;
   }
   __syncthreads();
   return ok_s != 0;
 }
 
-// Sum of n partials (stride, offset) in a fixed order, valid in every thread
-// of every CTA alike.
-__device__ __forceinline__ double partial_total(const double* part, int n, int stride, int off,
-                                                double* red, double* out) {
-  double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += NT) v += __ldcg(part + (size_t)i * stride + off);
-  const double s = block_sum<NT>(v, red);
-  if (threadIdx.x == 0) *out = s;
+// Sum of n partials in a fixed order, valid in every thread of every CTA
+// alike: warp 0 alone sums them in FP64 (lane l takes l, l + 32, ..., then a
+// shuffle tree), so the FP64 pipe (2 operations per clock per SM on GB300)
+// sees n + 5 additions per CTA instead of a CTA-wide tree.
+__device__ __forceinline__ double partial_total(const double* part, int n, double* out) {
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(part + i);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) *out = v;
+  }
   __syncthreads();
   const double t = *out;
   __syncthreads();
   return t;
+}
+
+// The same for n pairs of partials (both sums from one pass over them).
+__device__ __forceinline__ double2 partial_total2(const double* part, int n, double* out) {
+  if (threadIdx.x < 32) {
+    double v0 = 0.0, v1 = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) {
+      const double2 pr = __ldcg(reinterpret_cast<const double2*>(part) + i);
+      v0 += pr.x;
+      v1 += pr.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      v0 += __shfl_down_sync(0xffffffffu, v0, o);
+      v1 += __shfl_down_sync(0xffffffffu, v1, o);
+    }
+    if (threadIdx.x == 0) {
+      out[0] = v0;
+      out[1] = v1;
+    }
+  }
+  __syncthreads();
+  const double2 t = make_double2(out[0], out[1]);
+  __syncthreads();
+  return t;
+}
+
+// Sum over the CTA of one float pair per thread (fixed order: a float-pair
+// shuffle tree within each warp, then the warps' sums in FP64 by thread 0,
+// where the result is valid).  The FP32 Krylov vectors' dot products are
+// summed this way: exact products (FMA) and compensated sums keep about 44
+// bits, and the FP64 pipe sees NT/32 additions per CTA.
+__device__ __forceinline__ double block_sum_ff(ff v, double* sm /* NT/32 */) {
+  for (int o = 16; o > 0; o >>= 1) {
+    ff w;
+    w.h = __shfl_down_sync(0xffffffffu, v.h, o);
+    w.l = __shfl_down_sync(0xffffffffu, v.l, o);
+    v = ff_add(v, w);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sm[wid] = (double)v.h + (double)v.l;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < NT / 32; ++w) s += sm[w];
+  return s;
+}
+
+// a += x y exactly rounded to a float pair (the product's error by FMA).
+__device__ __forceinline__ void ff_acc_prod(ff& a, float x, float y) {
+  ff p;
+  p.h = __fmul_rn(x, y);
+  p.l = __fmaf_rn(x, y, -p.h);
+  a = ff_add(a, p);
 }
 
 __device__ __forceinline__ int skewer_of(const PersistArgs& a, int blk, int j) {
@@ -182,7 +265,7 @@ __device__ __forceinline__ void block_levels(const PersistArgs& a, int blk, int 
 // tid + NT, ... of block blk (record t: pixel k of the block's skewer j,
 // t = j n_per + k): the g lists are staged NB entries at a time; each step
 // keeps UF loads per record in flight.
-template <typename T, int UF>
+template <typename T, int UF, int NB>
 __device__ __forceinline__ void block_product(const PersistArgs& a, int blk,
                                               const int* __restrict__ ptr,
                                               const int* __restrict__ idx,
@@ -256,20 +339,21 @@ __device__ __forceinline__ void block_product(const PersistArgs& a, int blk,
 }
 
 // z = G G^T r over block blk from r in shared memory (slot order, 0 on
-// padding): t = G^T r, then z = G t; returns z of the thread's slots.
+// padding): t = G^T r, then z = G t; returns z of the thread's slots.  The
+// factor's plane m, slot i of the block is L[m ls + i] (the CTA's copy in
+// shared memory, or the global planes).
 template <int BAND>
-__device__ __forceinline__ void block_precond(const PersistArgs& a, int blk, const float* rs,
-                                              float* ts, float (&zk)[RPT]) {
+__device__ __forceinline__ void block_precond(const PersistArgs& a, const float* L, size_t ls,
+                                              const float* rs, float* ts, float (&zk)[RPT]) {
   const int band = BAND >= 0 ? BAND : a.band;
-  const size_t ns = (size_t)a.n_blocks * a.S;
-  const size_t s0 = (size_t)blk * a.S;
-  const float* __restrict__ L = a.L;
+  const size_t ns = ls;
+  const size_t s0 = 0;
 #pragma unroll
   for (int t = 0; t < RPT; ++t) {
     const int i = threadIdx.x + t * NT;
     if (i < a.S) {
       float v = 0.f;
-#pragma unroll
+#pragma unroll(BAND >= 0 ? BAND + 1 : 1)
       for (int m = 0; m <= (BAND >= 0 ? BAND : MAX_BAND); ++m)
         if (m <= band && i + m < a.S) v = fmaf(L[(size_t)m * ns + s0 + i + m], rs[i + m], v);
       ts[i] = v;
@@ -281,7 +365,7 @@ __device__ __forceinline__ void block_precond(const PersistArgs& a, int blk, con
     const int i = threadIdx.x + t * NT;
     float v = 0.f;
     if (i < a.S) {
-#pragma unroll
+#pragma unroll(BAND >= 0 ? BAND + 1 : 1)
       for (int m = 0; m <= (BAND >= 0 ? BAND : MAX_BAND); ++m)
         if (m <= band && i - m >= 0) v = fmaf(L[(size_t)m * ns + s0 + i], ts[i - m], v);
     }
@@ -289,11 +373,50 @@ __device__ __forceinline__ void block_precond(const PersistArgs& a, int blk, con
   }
 }
 
+// The step's scalars (those of K2 in the per-kernel form), thread 0 of every
+// CTA alike; CTA 0 records the history.
+__device__ __forceinline__ void step_scalars(MixedState& sS, const PersistArgs& a, int it,
+                                             double alpha_d, double pq, double trz, double trr) {
+  sS.alpha = alpha_d;
+  sS.pq = pq;
+  sS.rz_old = sS.rz;
+  sS.rz = trz;
+  sS.rnorm = sqrt(trr);
+  sS.iter = it;
+  if (blockIdx.x == 0) a.hist[it] = sS.rnorm;
+  sS.rmax = fmax(sS.rmax, sS.rnorm);
+  sS.need_update = update_due(&sS, it) ? 1 : 0;
+  sS.beta = sS.rz / sS.rz_old;
+}
+
+// The update's scalars (those of K6), thread 0 of every CTA alike.
+__device__ __forceinline__ void update_scalars(MixedState& sS, const PersistArgs& a, double trz,
+                                               double trr) {
+  const double rt = sqrt(trr);
+  sS.rtrue = rt;
+  ++sS.n_updates;
+  if (blockIdx.x == 0) {
+    a.htrue[sS.n_updates] = rt;
+    a.hist[sS.iter] = rt;
+  }
+  if (rt <= sS.tol_norm_b) {
+    sS.done = 1;
+    sS.converged = 1;
+  } else if (sS.iter >= sS.max_iter) {
+    sS.done = 1;
+  } else {
+    sS.rz = trz;
+    restart_after_update(&sS, rt, trz);
+  }
+  sS.need_update = 0;
+}
+
+// ---- general form: any number of blocks per CTA, vectors in global memory
 template <int BAND>
 __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
   __shared__ MixedState sS;
   __shared__ double red[NT / 32];
-  __shared__ double tot;
+  __shared__ double tot[2];
   __shared__ __align__(16) double su64[MAX_S];  // u of a block (FP64 or FP32)
   __shared__ float rs[MAX_S];
   __shared__ float ts[MAX_S];
@@ -304,6 +427,9 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
   float* s_p32 = reinterpret_cast<float*>(s_p64);
   const int tid = threadIdx.x;
   const int G = gridDim.x;
+  const int P2 = (G + 1) & ~1;  // the pair partials start 16-byte aligned
+  const size_t ns = (size_t)a.n_blocks * a.S;
+  unsigned int epoch = 0;  // barriers passed (thread 0)
   if (tid == 0) sS = *a.S_;
   __syncthreads();
   // the recurrence sets done by iteration max_iter at the latest (the
@@ -320,13 +446,13 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
           return (float)a.wr[r] * pv;
         });
     }
-    if (!grid_sync(a, B_LEVELS)) break;
+    if (!grid_sync(a, B_LEVELS, epoch)) break;
     // ---- B: q = A32 p, partial p.q
     double dq = 0.0;
     for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
       float acc[RPT];
-      block_product<float, UF32>(a, blk, a.iptr, a.iidx, a.ilev, a.ip32, a.V32, s_off, s_p32, s_cnt,
-                           acc);
+      block_product<float, UF32, NB>(a, blk, a.iptr, a.iidx, a.ilev, a.ip32, a.V32, s_off, s_p32,
+                                 s_cnt, acc);
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
         const int i = tid + t * NT;
@@ -345,10 +471,12 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
       const double bs = block_sum<NT>(dq, red);
       if (tid == 0) a.part[blockIdx.x] = bs;
     }
-    if (!grid_sync(a, B_PRODUCT)) break;
+    if (!grid_sync(a, B_PRODUCT, epoch)) break;
     // ---- C: alpha; x, r, z per owned block; partials r.z, |r|^2
-    const double pq = partial_total(a.part, G, 1, 0, red, &tot);
-    const double alpha_d = sS.rz / pq;
+    const double pq = partial_total(a.part, G, tot);
+    if (tid == 0) tot[0] = sS.rz / pq;
+    __syncthreads();
+    const double alpha_d = tot[0];
     const float alpha = (float)alpha_d;
     double rz = 0.0, rr = 0.0;
     for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
@@ -371,7 +499,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
       }
       __syncthreads();
       float zk[RPT];
-      block_precond<BAND>(a, blk, rs, ts, zk);
+      block_precond<BAND>(a, a.L + (size_t)blk * a.S, ns, rs, ts, zk);
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
         if (rec[t] < 0) continue;
@@ -385,27 +513,14 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
       const double b1 = block_sum<NT>(rz, red);
       const double b2 = block_sum<NT>(rr, red);
       if (tid == 0) {
-        a.part[(size_t)G + 2 * blockIdx.x] = b1;
-        a.part[(size_t)G + 2 * blockIdx.x + 1] = b2;
+        a.part[(size_t)P2 + 2 * blockIdx.x] = b1;
+        a.part[(size_t)P2 + 2 * blockIdx.x + 1] = b2;
       }
     }
-    if (!grid_sync(a, B_STEP)) break;
-    // the step's scalars (those of K2 in the per-kernel form), every CTA alike
+    if (!grid_sync(a, B_STEP, epoch)) break;
     {
-      const double trz = partial_total(a.part + G, G, 2, 0, red, &tot);
-      const double trr = partial_total(a.part + G, G, 2, 1, red, &tot);
-      if (tid == 0) {
-        sS.alpha = alpha_d;
-        sS.pq = pq;
-        sS.rz_old = sS.rz;
-        sS.rz = trz;
-        sS.rnorm = sqrt(trr);
-        sS.iter = it;
-        if (blockIdx.x == 0) a.hist[it] = sS.rnorm;
-        sS.rmax = fmax(sS.rmax, sS.rnorm);
-        sS.need_update = update_due(&sS, it) ? 1 : 0;
-        sS.beta = sS.rz / sS.rz_old;
-      }
+      const double2 t2 = partial_total2(a.part + P2, G, tot);
+      if (tid == 0) step_scalars(sS, a, it, alpha_d, pq, t2.x, t2.y);
       __syncthreads();
     }
     if (!sS.need_update) continue;
@@ -413,14 +528,14 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
     for (int blk = blockIdx.x; blk < a.n_blocks; blk += G)
       block_levels<double>(a, blk, a.olmax, a.taps64, a.V64, su64,
                            [&](size_t r) { return a.wr[r] * __ldcg(a.x + r); });
-    if (!grid_sync(a, B_LEVELS64)) break;
+    if (!grid_sync(a, B_LEVELS64, epoch)) break;
     // ---- E, F: r64 = b - A x per owned skewer; r = r64, z = G G^T r
     rz = 0.0;
     rr = 0.0;
     for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
       double acc[RPT];
-      block_product<double, UF64>(a, blk, a.optr, a.oidx, a.olev, a.op64, a.V64, s_off, s_p64, s_cnt,
-                            acc);
+      block_product<double, UF64, NB>(a, blk, a.optr, a.oidx, a.olev, a.op64, a.V64, s_off, s_p64,
+                                  s_cnt, acc);
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
         const int i = tid + t * NT;
@@ -451,7 +566,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
       }
       __syncthreads();
       float zk[RPT];
-      block_precond<BAND>(a, blk, rs, ts, zk);
+      block_precond<BAND>(a, a.L + (size_t)blk * a.S, ns, rs, ts, zk);
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
         if (rec[t] < 0) continue;
@@ -463,34 +578,14 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
       const double b1 = block_sum<NT>(rz, red);
       const double b2 = block_sum<NT>(rr, red);
       if (tid == 0) {
-        a.part[(size_t)G + 2 * blockIdx.x] = b1;
-        a.part[(size_t)G + 2 * blockIdx.x + 1] = b2;
+        a.part[(size_t)P2 + 2 * blockIdx.x] = b1;
+        a.part[(size_t)P2 + 2 * blockIdx.x + 1] = b2;
       }
     }
-    if (!grid_sync(a, B_UPDATE)) break;
-    // the update's scalars (those of K6), every CTA alike
+    if (!grid_sync(a, B_UPDATE, epoch)) break;
     {
-      const double trz = partial_total(a.part + G, G, 2, 0, red, &tot);
-      const double trr = partial_total(a.part + G, G, 2, 1, red, &tot);
-      if (tid == 0) {
-        const double rt = sqrt(trr);
-        sS.rtrue = rt;
-        ++sS.n_updates;
-        if (blockIdx.x == 0) {
-          a.htrue[sS.n_updates] = rt;
-          a.hist[sS.iter] = rt;
-        }
-        if (rt <= sS.tol_norm_b) {
-          sS.done = 1;
-          sS.converged = 1;
-        } else if (sS.iter >= sS.max_iter) {
-          sS.done = 1;
-        } else {
-          sS.rz = trz;
-          restart_after_update(&sS, rt, trz);
-        }
-        sS.need_update = 0;
-      }
+      const double2 t2 = partial_total2(a.part + P2, G, tot);
+      if (tid == 0) update_scalars(sS, a, t2.x, t2.y);
       __syncthreads();
     }
   }
@@ -500,18 +595,418 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
   }
 }
 
-// CTAs of the cooperative launch: one per block, at most the resident count.
+// ---- resident form: one block per CTA, the block's vectors in shared memory
+//
+// With at most one block per CTA (the cooperative grid holds every block),
+// each CTA keeps its block's FP32 vectors p, z, q (record-local order j n_per
+// + k), r (slot order), the FP64 iterate x, the FP32 coefficients and its
+// skewers' FP32 neighbour lists in shared memory for the whole solve: the
+// phases then read global memory only for the neighbours' levels (B), the
+// factor (C) and the partials, and the levels they publish (A, D).  x goes
+// back to global memory at the end.  Same recurrence, same sums in the same
+// order as the general form.
+constexpr int NL = 1024;  // FP32 neighbour entries of a block kept in shared memory
+
+// Shared-memory layout of the resident form (bytes from the dynamic base).
+struct ResLayout {
+  static constexpr size_t xs = 0;                                   // double[MAX_S]
+  static constexpr size_t us = xs + MAX_S * sizeof(double);         // double[MAX_S]
+  static constexpr size_t loff = us + MAX_S * sizeof(double);       // uint32[NL]
+  static constexpr size_t ps = loff + NL * sizeof(unsigned int);    // float[MAX_S] x 8
+  static constexpr size_t lp = ps + 8 * MAX_S * sizeof(float);      // float[NL]
+  static constexpr size_t loc = lp + NL * sizeof(float);            // int[MAX_S]
+  static constexpr size_t lptr = loc + MAX_S * sizeof(int);         // int[MAX_G + 1]
+  static constexpr size_t sk = lptr + (MAX_G + 1) * sizeof(int);    // int[MAX_G]
+  static constexpr size_t lh = (sk + MAX_G * sizeof(int) + 15) / 16 * 16;  // half[(band + 1) S]
+  static size_t bytes(int band, int S) { return lh + ((size_t)(band + 1) * S * 2 + 15) / 16 * 16; }
+};
+
+// z = G G^T r over the CTA's block from r in shared memory, with the block's
+// factor in shared memory in FP16 (plane m, slot i at Lh[m S + i]; a
+// preconditioner needs no more: M^-1 = G G^T stays symmetric positive
+// definite whatever the rounding of G).
 template <int BAND>
-int persistent_grid(int num_sms, int n_blocks) {
-  static int per_sm = -1;
-  if (per_sm < 0) {
-    DS_CUDA(cudaFuncSetAttribute(k_mixed_persistent<BAND>,
-                                 cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared));
-    DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_persistent<BAND>, NT,
-                                                          0));
+__device__ __forceinline__ void block_precond_h(const PersistArgs& a, const __half* Lh,
+                                                const float* rs, float* ts, float (&zk)[RPT]) {
+  const int band = BAND >= 0 ? BAND : a.band;
+  const int S = a.S;
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = threadIdx.x + t * NT;
+    if (i < S) {
+      float v = 0.f;
+#pragma unroll(BAND >= 0 ? BAND + 1 : 1)
+      for (int m = 0; m <= (BAND >= 0 ? BAND : MAX_BAND); ++m)
+        if (m <= band && i + m < S) v = fmaf(__half2float(Lh[m * S + i + m]), rs[i + m], v);
+      ts[i] = v;
+    }
   }
-  return std::min(per_sm * num_sms, n_blocks);
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = threadIdx.x + t * NT;
+    float v = 0.f;
+    if (i < S) {
+#pragma unroll(BAND >= 0 ? BAND + 1 : 1)
+      for (int m = 0; m <= (BAND >= 0 ? BAND : MAX_BAND); ++m)
+        if (m <= band && i - m >= 0) v = fmaf(__half2float(Lh[m * S + i]), ts[i - m], v);
+    }
+    zk[t] = v;
+  }
+}
+
+template <int BAND>
+__global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  ff* xs = reinterpret_cast<ff*>(smraw + ResLayout::xs);  // the iterate, float pairs
+  double* us = reinterpret_cast<double*>(smraw + ResLayout::us);
+  unsigned int* loff = reinterpret_cast<unsigned int*>(smraw + ResLayout::loff);
+  float* ps = reinterpret_cast<float*>(smraw + ResLayout::ps);
+  float* zs = ps + MAX_S;
+  float* qs = zs + MAX_S;
+  float* rs = qs + MAX_S;   // slot order
+  float* ts = rs + MAX_S;   // scratch: u (A), t = G^T r (C, F)
+  float* wls = ts + MAX_S;  // FP32 coefficients
+  float* wrs = wls + MAX_S;
+  float* es = wrs + MAX_S;
+  float* lp = reinterpret_cast<float*>(smraw + ResLayout::lp);
+  int* loc = reinterpret_cast<int*>(smraw + ResLayout::loc);  // slot -> record-local index
+  int* lptr = reinterpret_cast<int*>(smraw + ResLayout::lptr);
+  int* sk = reinterpret_cast<int*>(smraw + ResLayout::sk);
+  __half* Lh = reinterpret_cast<__half*>(smraw + ResLayout::lh);
+  __shared__ MixedState sS;
+  __shared__ double red[NT / 32];
+  __shared__ double tot[2];
+  __shared__ ff s_alpha;  // alpha as a float pair (x update)
+  __shared__ float s_ab;  // alpha or beta in FP32
+  __shared__ size_t s_off[MAX_G * NB_R];  // staged FP64 lists (the update's residual)
+  __shared__ double s_p64[MAX_G * NB_R];
+  __shared__ int s_cnt[2 * MAX_G];
+  const int tid = threadIdx.x;
+  const int G = gridDim.x;
+  const int P2 = (G + 1) & ~1;
+  const int blk = blockIdx.x;
+  const int npr = a.n_per;
+  const int m = a.g * npr;  // records of the block (record-local index j n_per + k)
+  const size_t n = (size_t)a.n;
+  const size_t ns = (size_t)a.n_blocks * a.S;
+  unsigned int epoch = 0;  // barriers passed (thread 0)
+  if (tid == 0) sS = *a.S_;
+  if (tid < MAX_G) sk[tid] = tid < a.g ? skewer_of(a, blk, tid) : -1;
+  __syncthreads();
+  if (tid == 0) {
+    int c = 0;
+    for (int j = 0; j < a.g; ++j) {
+      lptr[j] = c;
+      if (sk[j] >= 0) c += a.iptr[sk[j] + 1] - a.iptr[sk[j]];
+    }
+    lptr[a.g] = c;
+  }
+  __syncthreads();
+  for (int j = 0; j < a.g; ++j) {
+    if (sk[j] < 0) continue;
+    const int q0 = a.iptr[sk[j]], c0 = lptr[j], cnt = lptr[j + 1] - c0;
+    for (int e = tid; e < cnt; e += NT) {
+      loff[c0 + e] = (unsigned int)((size_t)(a.ilev[q0 + e] - 1) * n + (size_t)a.iidx[q0 + e] * npr);
+      lp[c0 + e] = a.ip32[q0 + e];
+    }
+  }
+  for (int i = tid; i < m; i += NT) {
+    const int j = i / npr;
+    const int s = sk[j];
+    if (s < 0) {
+      xs[i] = ff{0.f, 0.f};
+      ps[i] = zs[i] = qs[i] = wls[i] = wrs[i] = es[i] = 0.f;
+      continue;
+    }
+    const size_t r = (size_t)s * npr + (i - j * npr);
+    xs[i] = ff_from_double(a.x[r]);
+    ps[i] = a.p[r];
+    zs[i] = a.z[r];
+    qs[i] = 0.f;
+    wls[i] = (float)a.wl[r];
+    wrs[i] = (float)a.wr[r];
+    es[i] = (float)a.e[r];
+  }
+  {  // the block's factor, FP16
+    const int nl = (a.band + 1) * a.S;
+    for (int i = tid; i < nl; i += NT) {
+      const int mm = i / a.S;
+      Lh[i] = __float2half_rn(a.L[(size_t)mm * ns + (size_t)blk * a.S + (i - mm * a.S)]);
+    }
+  }
+  for (int i = tid; i < a.S; i += NT) {
+    const int rec = record_of(a, blk, i);
+    int li = -1;
+    float rv = 0.f;
+    if (rec >= 0) {
+      const int s = rec / npr;
+      for (int j = 0; j < a.g; ++j)
+        if (sk[j] == s) li = j * npr + (rec - s * npr);
+      rv = a.r[rec];
+    }
+    loc[i] = li;
+    rs[i] = rv;
+  }
+  __syncthreads();
+  // the thread's records (A, B): i = tid + t NT, pixel k of skewer j
+  int jj[RPT], kk[RPT];
+  size_t rg[RPT];  // global record (valid when jj >= 0)
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = tid + t * NT;
+    jj[t] = -1;
+    kk[t] = 0;
+    rg[t] = 0;
+    if (i < m && sk[i / npr] >= 0) {
+      jj[t] = i / npr;
+      kk[t] = i - jj[t] * npr;
+      rg[t] = (size_t)sk[jj[t]] * npr + kk[t];
+    }
+  }
+  // The levels of u = wr z (FP32) of the block's skewers from zs (record
+  // order; ts is the scratch for u).
+  auto levels_z = [&]() {
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < RPT; ++t)
+      if (jj[t] >= 0) ts[tid + t * NT] = wrs[tid + t * NT] * zs[tid + t * NT];
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      const int i = tid + t * NT;
+      if (jj[t] < 0) continue;
+      const int k = kk[t];
+      float acc = ts[i];
+      a.V32[rg[t]] = acc;
+      for (int l = 1; l <= a.ilmax; ++l) {
+        float v = 0.f;
+        if (k + l < npr) v = ts[i + l];
+        if (k - l >= 0) v += ts[i - l];
+        acc = fmaf(a.taps32[l], v, acc);
+        a.V32[(size_t)l * n + rg[t]] = acc;
+      }
+    }
+  };
+  // Two grid barriers per iteration (Chronopoulos and Gear's arrangement of
+  // the same recurrence): the product phase forms w = A32 z from the
+  // published levels of z and moves both directions, p = z + beta p and
+  // q = w + beta q (= A32 p), so p.q is known at its barrier; the step phase
+  // then updates x and r, applies the preconditioner, publishes the levels of
+  // the new z and the partials of r.z and |r|^2 at the next barrier.
+  levels_z();
+  if (grid_sync(a, B_LEVELS, epoch))
+    while (!sS.done && sS.iter < a.max_iter) {
+      const int it = sS.iter + 1;
+      // ---- product: w = A32 z, p = z + beta p, q = w + beta q, partial p.q
+      ff dq{0.f, 0.f};
+      {
+        if (tid == 0) s_ab = (float)sS.beta;
+        float acc[RPT];
+        int c0[RPT], cnt[RPT];
+        int cmax = 0;
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          acc[t] = 0.f;
+          c0[t] = jj[t] >= 0 ? lptr[jj[t]] : 0;
+          cnt[t] = jj[t] >= 0 ? lptr[jj[t] + 1] - c0[t] : 0;
+          cmax = max(cmax, cnt[t]);
+        }
+        for (int e = 0; e < cmax; e += UFR) {
+          float v[RPT][UFR];
+#pragma unroll
+          for (int t = 0; t < RPT; ++t)
+#pragma unroll
+            for (int u = 0; u < UFR; ++u)
+              v[t][u] = e + u < cnt[t] ? __ldcg(a.V32 + loff[c0[t] + e + u] + kk[t]) : 0.f;
+#pragma unroll
+          for (int t = 0; t < RPT; ++t)
+#pragma unroll
+            for (int u = 0; u < UFR; ++u)
+              if (e + u < cnt[t]) acc[t] = fmaf(lp[c0[t] + e + u], v[t][u], acc[t]);
+        }
+        __syncthreads();  // s_ab
+        const float beta = s_ab;
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          if (jj[t] < 0) continue;
+          const int i = tid + t * NT;
+          const float zv = zs[i];
+          const float wv = fmaf(wls[i], acc[t], es[i] * zv);
+          const float pv = fmaf(beta, ps[i], zv);
+          const float qv = fmaf(beta, qs[i], wv);
+          ps[i] = pv;
+          qs[i] = qv;
+          ff_acc_prod(dq, pv, qv);
+        }
+      }
+      {
+        const double bs = block_sum_ff(dq, red);
+        if (tid == 0) a.part[blk] = bs;
+      }
+      if (!grid_sync(a, B_PRODUCT, epoch)) break;
+      // ---- step: alpha; x, r, z of the block; levels of z; partials
+      const double pq = partial_total(a.part, G, tot);
+      if (tid == 0) {
+        const double al = sS.rz / pq;
+        tot[0] = al;
+        s_alpha = ff_from_double(al);
+        s_ab = (float)al;
+      }
+      __syncthreads();
+      const double alpha_d = tot[0];
+      const float alpha = s_ab;
+      const ff alpha_ff = s_alpha;
+      ff rz{0.f, 0.f}, rr{0.f, 0.f};
+      int li[RPT];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        li[t] = i < a.S ? loc[i] : -1;
+        if (li[t] >= 0) {
+          const int l = li[t];
+          rs[i] = fmaf(-alpha, qs[l], rs[i]);
+          ff_mac(xs[l].h, xs[l].l, alpha_ff, ff{ps[l], 0.f});
+        }
+      }
+      __syncthreads();
+      {
+        float zk[RPT];
+        block_precond_h<BAND>(a, Lh, rs, ts, zk);
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          if (li[t] < 0) continue;
+          const float ri = rs[tid + t * NT];
+          zs[li[t]] = zk[t];
+          ff_acc_prod(rz, ri, zk[t]);
+          ff_acc_prod(rr, ri, ri);
+        }
+      }
+      {
+        const double b1 = block_sum_ff(rz, red);
+        const double b2 = block_sum_ff(rr, red);
+        if (tid == 0) {
+          a.part[(size_t)P2 + 2 * blk] = b1;
+          a.part[(size_t)P2 + 2 * blk + 1] = b2;
+        }
+      }
+      levels_z();
+      if (!grid_sync(a, B_STEP, epoch)) break;
+      {
+        const double2 t2 = partial_total2(a.part + P2, G, tot);
+        if (tid == 0) step_scalars(sS, a, it, alpha_d, pq, t2.x, t2.y);
+        __syncthreads();
+      }
+      if (!sS.need_update) continue;
+      // ---- FP64 update: levels of u = wr x (FP64 coefficients from global memory)
+#pragma unroll
+      for (int t = 0; t < RPT; ++t)
+        if (jj[t] >= 0) {
+          const ff xv = xs[tid + t * NT];
+          us[tid + t * NT] = a.wr[rg[t]] * ((double)xv.h + (double)xv.l);
+        }
+      __syncthreads();
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        if (jj[t] < 0) continue;
+        const int k = kk[t];
+        double acc = us[i];
+        a.V64[rg[t]] = acc;
+        for (int l = 1; l <= a.olmax; ++l) {
+          double v = 0.0;
+          if (k + l < npr) v = us[i + l];
+          if (k - l >= 0) v += us[i - l];
+          acc = fma(a.taps64[l], v, acc);
+          a.V64[(size_t)l * n + rg[t]] = acc;
+        }
+      }
+      if (!grid_sync(a, B_LEVELS64, epoch)) break;
+      // r64 = b - A x of the block (into us); r = r64, z = G G^T r, levels of z
+      {
+        double acc[RPT];
+        block_product<double, UF64, NB_R>(a, blk, a.optr, a.oidx, a.olev, a.op64, a.V64, s_off,
+                                          s_p64, s_cnt, acc);
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          if (jj[t] < 0) continue;
+          const int i = tid + t * NT;
+          const double xv = (double)xs[i].h + (double)xs[i].l;
+          us[i] = a.b[rg[t]] - fma(a.wl[rg[t]], acc[t], a.e[rg[t]] * xv);
+        }
+      }
+      __syncthreads();
+      ff rz_u{0.f, 0.f};
+      double rr_u = 0.0;
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+        if (i >= a.S) continue;
+        float rv = 0.f;
+        if (li[t] >= 0) {
+          const double rd = us[li[t]];
+          rv = (float)rd;
+          rr_u = fma(rd, rd, rr_u);
+        }
+        rs[i] = rv;
+      }
+      __syncthreads();
+      {
+        float zk[RPT];
+        block_precond_h<BAND>(a, Lh, rs, ts, zk);
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          if (li[t] < 0) continue;
+          zs[li[t]] = zk[t];
+          ff_acc_prod(rz_u, rs[tid + t * NT], zk[t]);
+        }
+      }
+      {
+        const double b1 = block_sum_ff(rz_u, red);
+        const double b2 = block_sum<NT>(rr_u, red);
+        if (tid == 0) {
+          a.part[(size_t)P2 + 2 * blk] = b1;
+          a.part[(size_t)P2 + 2 * blk + 1] = b2;
+        }
+      }
+      levels_z();
+      if (!grid_sync(a, B_UPDATE, epoch)) break;
+      {
+        const double2 t2 = partial_total2(a.part + P2, G, tot);
+        if (tid == 0) update_scalars(sS, a, t2.x, t2.y);
+        __syncthreads();
+      }
+    }
+  // the iterate back to global memory (record order)
+#pragma unroll
+  for (int t = 0; t < RPT; ++t)
+    if (jj[t] >= 0) a.x[rg[t]] = (double)xs[tid + t * NT].h + (double)xs[tid + t * NT].l;
+  if (blockIdx.x == 0 && tid == 0) {
+    sS.skip_update = 1;
+    *a.S_ = sS;
+  }
+}
+
+// Resident CTAs per SM of a kernel at `smem` dynamic bytes (0: does not fit).
+int resident_per_sm(const void* fn, size_t smem) {
+  cudaFuncAttributes fa;
+  DS_CUDA(cudaFuncGetAttributes(&fa, fn));
+  int dev = 0, optin = 0;
+  DS_CUDA(cudaGetDevice(&dev));
+  DS_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (fa.sharedSizeBytes + smem > (size_t)optin) return 0;
+  DS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared));
+  if (smem > 48 * 1024)
+    DS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  DS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem));
+  return per_sm;
+}
+
+template <int BAND>
+const void* kernel_of(bool resident) {
+  return resident ? (const void*)k_mixed_resident<BAND> : (const void*)k_mixed_persistent<BAND>;
 }
 
 }  // namespace
@@ -527,13 +1022,53 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
     return false;
   if (!g.inner.ptr.p || !g.V32.p || !g.V64.p) return false;
   const int band = pc->band;
-  const int grid = band == 16  ? persistent_grid<16>(op->ctx->num_sms, pc->n_sk)
-                   : band == 2 ? persistent_grid<2>(op->ctx->num_sms, pc->n_sk)
-                               : persistent_grid<-1>(op->ctx->num_sms, pc->n_sk);
+  auto pick = [&](bool resident) {
+    return band == 16 ? kernel_of<16>(resident)
+                      : band == 2 ? kernel_of<2>(resident) : kernel_of<-1>(resident);
+  };
+  // The resident form when every block gets its own resident CTA and the
+  // longest FP32 neighbour list of a block fits in shared memory.
+  if (g.res_pc != pc || g.res_cut != g.inner.cut) {
+    std::vector<int> ptr(g.n_sk + 1), bsk(pc->bsk.n);
+    DS_CUDA(cudaMemcpyAsync(ptr.data(), g.inner.ptr.p, ptr.size() * sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    if (pc->bsk.p)
+      DS_CUDA(cudaMemcpyAsync(bsk.data(), pc->bsk.p, bsk.size() * sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    int mx = 0;
+    for (int b = 0; b < pc->n_sk; ++b) {
+      int c = 0;
+      for (int j = 0; j < pc->g; ++j) {
+        const int s = pc->bsk.p ? bsk[(size_t)b * pc->g + j] : (j == 0 ? b : -1);
+        if (s >= 0) c += ptr[s + 1] - ptr[s];
+      }
+      mx = std::max(mx, c);
+    }
+    g.res_pc = pc;
+    g.res_cut = g.inner.cut;
+    g.res_max_list = mx;
+  }
+  const size_t res_bytes = ResLayout::bytes(band, pc->n_per);
+  static int per_sm0[3] = {-1, -1, -1};
+  static int per_sm1[3] = {-1, -1, -1};
+  static size_t res_last[3] = {0, 0, 0};
+  const int bi = band == 16 ? 0 : band == 2 ? 1 : 2;
+  if (per_sm0[bi] < 0) per_sm0[bi] = resident_per_sm(pick(false), 0);
+  if (res_last[bi] != res_bytes) {
+    per_sm1[bi] = resident_per_sm(pick(true), res_bytes);
+    res_last[bi] = res_bytes;
+  }
+  const int nsm = op->ctx->num_sms;
+  // the resident lists hold 32-bit offsets into the levels
+  const bool off32 = (double)(g.inner.lmax + 1) * (double)op->n < 4294967295.0;
+  const bool resident = off32 && g.res_max_list <= NL && per_sm1[bi] * nsm >= pc->n_sk;
+  const int grid = resident ? pc->n_sk : std::min(per_sm0[bi] * nsm, pc->n_sk);
   if (grid <= 0) return false;
-  g.p_part.alloc((size_t)3 * grid);
-  g.p_sync.alloc(3);
-  DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, 3 * sizeof(int), st));
+  g.p_part.alloc((size_t)3 * grid + 1);
+  const size_t n_sync = (size_t)(1 + grid) * BAR_LINE;
+  g.p_sync.alloc(n_sync);
+  DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, n_sync * sizeof(int), st));
   PersistArgs a{};
   a.n = op->n;
   a.n_per = g.n_per;
@@ -573,15 +1108,12 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.hist = f.hist.p;
   a.htrue = f.htrue.p;
   a.part = g.p_part.p;
-  a.bar_count = reinterpret_cast<unsigned int*>(g.p_sync.p);
-  a.bar_gen = reinterpret_cast<unsigned int*>(g.p_sync.p) + 1;
-  a.err = g.p_sync.p + 2;
+  a.bar = reinterpret_cast<unsigned int*>(g.p_sync.p);
+  a.err = g.p_sync.p + 1;
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
   void* args[] = {&a};
-  const void* fn = band == 16  ? (const void*)k_mixed_persistent<16>
-                   : band == 2 ? (const void*)k_mixed_persistent<2>
-                               : (const void*)k_mixed_persistent<-1>;
-  DS_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NT), args, 0, st));
+  DS_CUDA(cudaLaunchCooperativeKernel(pick(resident), dim3(grid), dim3(NT), args,
+                                      resident ? res_bytes : 0, st));
   DS_CHECK_LAUNCH();
   return true;
 }
@@ -590,9 +1122,9 @@ int persistent_error(ds_operator* op, cudaStream_t st) {
   SkewerGrid& g = *op->sgrid;
   if (!g.p_sync.p) return 0;
   int code = 0;
-  DS_CUDA(cudaMemcpyAsync(&code, g.p_sync.p + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(&code, g.p_sync.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
-  if (code) DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, 3 * sizeof(int), st));
+  if (code) DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, g.p_sync.bytes(), st));
   return code;
 }
 
