@@ -715,7 +715,7 @@ def run_ours(args, rank, world, local):
 
     clocks = ClockSampler(local)
     clocks.start()
-    times, results = [], []
+    times, results, parts = [], [], []
     launches0 = ctx.profile()["kernel_launches"]
     clocks.mark_start()
     for _ in range(args.steps):
@@ -725,22 +725,30 @@ def run_ours(args, rank, world, local):
         barrier()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
+        em = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         with torch.cuda.stream(stream):
             x.zero_()
         res = op.solve_mixed_dev(mp, x)
+        em.record(stream)
         grid.product_f32_dev(op, x, m)
         e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
         barrier()
         times.append(e0.elapsed_time(e1) / 1e3)
+        parts.append((e0.elapsed_time(em) / 1e3, em.elapsed_time(e1) / 1e3, res.seconds))
         results.append(res)
     clocks.mark_end()
     launches = (ctx.profile()["kernel_launches"] - launches0) / args.steps
     clk = clocks.stop()
     step_s = allmax(statistics.mean(times))
+    # the step's two calls (CUDA events between them) and the solve's own
+    # device time (the library's events around its launches)
+    step_parts = {"solve": statistics.mean(p[0] for p in parts),
+                  "map": statistics.mean(p[1] for p in parts),
+                  "solve_device": statistics.mean(p[2] for p in parts)}
 
     # One more step, untimed, with CUDA events around every pair-kernel launch
     # (the per-kernel times below; the events and the uncaptured launches make
@@ -969,6 +977,7 @@ def run_ours(args, rank, world, local):
                        "tol": w.pcg_tol, "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps (256 MiB write)"},
             "cg_iters": r0.num_iters, "fp64_updates": r0.n_outer,
+            "step_parts_s": step_parts,
             "preconditioner": pc_info,
             "jacobi_mixed": jacobi,
             "final_rel_residual": r0.final_norm / r0.norm_b,

@@ -165,6 +165,8 @@ SIGNATURES = {
     "ds_operator_get_dense_arith": (_i, [_vp, C.POINTER(C.c_int)]),
     "ds_operator_set_inner_matvec": (_i, [_vp, _i]),
     "ds_operator_set_iteration_form": (_i, [_vp, _i]),
+    "ds_operator_get_persistent_profile": (_i, [_vp, C.POINTER(C.c_double), _i, _i,
+                                              C.POINTER(C.c_int)]),
     "ds_solve_cf": (_i, [_vp, _i, _i, _dp, C.POINTER(KernelParamsC), _dp]),
     "ds_map_covar_diag": (_i, [_vp, _i, _dp, _i, _dp, C.POINTER(KernelParamsC),
                                C.POINTER(PcgParamsC), _dp, _ip, _ip]),

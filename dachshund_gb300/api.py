@@ -272,6 +272,27 @@ class _WFVector:
         self.ctx.check(self._lib.ds_operator_set_iteration_form(self.handle, v),
                        "ds_operator_set_iteration_form")
 
+    def persistent_profile(self, reset: bool = True):
+        """Phase timers of the persistent solve launches since the last reset
+        (device %globaltimer): launches, kernel_ms, ctas, barrier_us (one
+        empty grid barrier) and, per phase (levels0, product, step,
+        levels64, update), us_per_visit, cta_mean_us, cta_max_us, visits.
+        None before the first persistent launch."""
+        out = (C.c_double * 24)()
+        m = C.c_int(0)
+        self.ctx.check(self._lib.ds_operator_get_persistent_profile(
+            self.handle, out, 24, int(bool(reset)), C.byref(m)),
+            "ds_operator_get_persistent_profile")
+        if m.value == 0:
+            return None
+        v = list(out)
+        prof = {"launches": int(v[0]), "kernel_ms": v[1], "ctas": int(v[2]), "barrier_us": v[3]}
+        for c, name in enumerate(["levels0", "product", "step", "levels64", "update"]):
+            o = v[4 + 4 * c: 8 + 4 * c]
+            prof[name] = {"us_per_visit": o[0], "cta_mean_us": o[1], "cta_max_us": o[2],
+                          "visits": int(o[3])}
+        return prof
+
     def set_cluster_preconditioner(self, n_skewers: int, n_per: int, cluster: int = 4,
                                    band: int = 16) -> int:
         """Preconditions solve_mixed with the cluster factor M^-1 = G G^T

@@ -13,6 +13,7 @@
 #include "ds_device.cuh"
 #include "ds_f32.h"
 #include "ds_ops.h"
+#include "ds_skewer.h"
 
 namespace ds {
 
@@ -795,6 +796,15 @@ int ds_operator_set_iteration_form(ds_operator* op, int form) {
   return guarded(op->ctx, [&] {
     require(form == DS_ITER_AUTO || form == DS_ITER_GRAPH, "bad iteration form");
     op->iter_form = form;
+  });
+}
+
+int ds_operator_get_persistent_profile(ds_operator* op, double* out, int n, int reset,
+                                       int* written) {
+  if (!op || !out || n < 0) return DS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    const int m = persistent_profile(op, out, n, reset != 0);
+    if (written) *written = m;
   });
 }
 

@@ -127,6 +127,7 @@ struct OpF32 {
   DevBuf<float> p, q, r, z;         // FP32 iteration vectors (sorted, padded)
   DevBuf<float> r2;                 // second r buffer of the band preconditioner
   DevBuf<MixedState> state;
+  HostBuf<MixedState> h_state;      // pinned staging of the state
   DevBuf<double> hist, htrue;
   bool use_ff = false;  // outer residual in float-float arithmetic (else FP64)
   FFData ffd;

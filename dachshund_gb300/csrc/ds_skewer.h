@@ -40,6 +40,7 @@ struct SkewerGrid {
   // error code)
   DevBuf<double> p_part;
   DevBuf<int> p_sync;
+  DevBuf<unsigned long long> p_time;  // its phase timers
   // the longest FP32 neighbour list of a preconditioner block (for the
   // preconditioner and inner cutoff it was counted for)
   const void* res_pc = nullptr;
@@ -112,6 +113,9 @@ struct SkewerPC;
 bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const SkewerVecs& sv,
                           double* X, float* r, int max_iter, cudaStream_t st);
 int persistent_error(ds_operator* op, cudaStream_t st);
+// The persistent launches' phase timers (ds_operator_get_persistent_profile):
+// writes min(n, 24) values, returns that count (0: no launch yet).
+int persistent_profile(ds_operator* op, double* out, int n, bool reset);
 
 // m = S_mp x (caller order, device) with the structured FP64 map; false when
 // the map or the operator has no grid (then nothing is launched).

@@ -601,7 +601,11 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   h.tol_norm_b = mp.tol * op->norm_b;
   h.delta = mp.reliable_delta > 0.0 ? mp.reliable_delta : 1e-4;
   h.pad = 1;  // "x0 is zero" flag, cleared by k_is_zero
-  DS_CUDA(cudaMemcpyAsync(f.state.p, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  // the state goes up and comes back through pinned memory (a pageable copy
+  // can wait for the stream)
+  f.h_state.alloc(1);
+  *f.h_state.p = h;
+  DS_CUDA(cudaMemcpyAsync(f.state.p, f.h_state.p, sizeof(h), cudaMemcpyHostToDevice, st));
   MixedState* S = f.state.p;
   int* xzero = &S->pad;
 
@@ -781,8 +785,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // captured once per solve and replayed: 1 launch instead of ~7 CHECK.
   constexpr int CHECK = 8;
   constexpr int NSLOT = 64;
-  cudaEvent_t evs[NSLOT];
-  for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaEvent_t evs[NSLOT] = {};
   cudaGraphExec_t gexec = nullptr;
   long long per_graph = 0;
   // With the structured inner operator and a band preconditioner the whole
@@ -791,6 +794,8 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   bool persisted = false;
   if (use_sg && pc && op->iter_form == DS_ITER_AUTO && !op->ctx->prof.enabled && max_iter > 0)
     persisted = run_mixed_persistent(op, f, pc, sv, X, rbuf[0], max_iter, st);
+  if (!persisted)  // the host polls the done flag (the persistent launch needs no events)
+    for (auto& e : evs) DS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   if (!persisted && !op->ctx->prof.enabled && !use_tc && max_iter > 0) {
     const long long l0 = launch_counter();
     cudaGraph_t graph = nullptr;
@@ -837,11 +842,13 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   }
   if (use_sg) skewer_x_to_sorted(op, X, op->x.p, st);
   DS_CUDA(cudaEventRecord(ev1, st));
-  DS_CUDA(cudaMemcpyAsync(&h, S, sizeof(h), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(f.h_state.p, S, sizeof(h), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
+  h = *f.h_state.p;
   float ms = 0.f;
   DS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-  for (auto& e : evs) cudaEventDestroy(e);
+  for (auto& e : evs)
+    if (e) cudaEventDestroy(e);
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
 

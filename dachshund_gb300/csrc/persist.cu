@@ -33,6 +33,7 @@
 // resident), so a barrier always completes unless a CTA has left.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include <cuda_fp16.h>
 
@@ -84,10 +85,38 @@ struct PersistArgs {
   unsigned int* bar;  // barrier words: count, error code, a flag line per CTA
   int* err;
   long long limit;
+  unsigned long long* pt;  // phase timers (PT_* layout)
 };
 
-// Barrier codes: the phase whose closing barrier gave up.
-enum { B_LEVELS = 1, B_PRODUCT, B_STEP, B_LEVELS64, B_UPDATE };
+// Barrier codes: the phase whose closing barrier gave up (also the phase
+// timers' index); B_CALIB: the empty barrier after the start that
+// calibrates the barrier's own cost (the profile's barrier_us).  Measured on
+// GB300: without it the same solve ran ~20% slower (every iteration, not only
+// the first; a code-generation effect whose cause is not known), with 1 to
+// 16 of them the time is the same to 1%.
+enum { B_LEVELS = 1, B_PRODUCT, B_STEP, B_LEVELS64, B_UPDATE, B_CALIB };
+constexpr int N_CALIB = 1;
+
+// Phase timers (%globaltimer, ns), accumulated over launches until read:
+// CTA 0 records, per barrier code, the time from the previous barrier's exit
+// to this one's exit and the number of visits; every CTA records, per code,
+// its own work (from its previous exit to its arrival), so the slowest CTA
+// and the barrier's wait are told apart.
+enum {
+  PT_LAST = 0,       // CTA 0's last exit
+  PT_PHASE = 0,      // + code: exit-to-exit totals (codes 1..6)
+  PT_VISITS = 8,     // + code
+  PT_START = 16,     // kernel start (CTA 0)
+  PT_KERNEL = 17,    // kernel time
+  PT_LAUNCHES = 18,
+  PT_GRID = 19,
+  PT_CTA = 32        // + 8 blk + code: CTA work
+};
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // Grid-wide barrier (all CTAs resident: cooperative launch).  Every CTA's
 // thread 0 arrives on one monotonic count (atom.acq_rel: it releases the
@@ -104,8 +133,10 @@ constexpr int BAR_LINE = 32;  // words per 128-byte line
 constexpr unsigned int ERR_FLAG = 0xffffffffu;
 __device__ bool grid_sync(const PersistArgs& a, int code, unsigned int& epoch) {
   __shared__ int ok_s;
+  __shared__ unsigned long long prev_exit;
   __syncthreads();
   if (threadIdx.x == 0) {
+    if (epoch > 0) a.pt[PT_CTA + 8 * blockIdx.x + code] += global_ns() - prev_exit;
     int ok = 1;
     ++epoch;
     const unsigned int target = epoch * gridDim.x;
@@ -141,6 +172,13 @@ __device__ bool grid_sync(const PersistArgs& a, int code, unsigned int& epoch) {
           break;
         }
       }
+    }
+    const unsigned long long now = global_ns();
+    prev_exit = now;
+    if (blockIdx.x == 0) {
+      a.pt[PT_PHASE + code] += now - a.pt[PT_LAST];
+      a.pt[PT_LAST] = now;
+      a.pt[PT_VISITS + code] += 1;
     }
     ok_s = ok;
   }
@@ -431,7 +469,15 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
   const size_t ns = (size_t)a.n_blocks * a.S;
   unsigned int epoch = 0;  // barriers passed (thread 0)
   if (tid == 0) sS = *a.S_;
+  if (tid == 0 && blockIdx.x == 0) {
+    const unsigned long long now = global_ns();
+    a.pt[PT_LAST] = now;
+    a.pt[PT_START] = now;
+    a.pt[PT_GRID] = gridDim.x;
+    a.pt[PT_LAUNCHES] += 1;
+  }
   __syncthreads();
+  for (int k = 0; k < N_CALIB; ++k) grid_sync(a, B_CALIB, epoch);
   // the recurrence sets done by iteration max_iter at the latest (the
   // update it forces there ends the solve); the bound keeps hist in range
   while (!sS.done && sS.iter < a.max_iter) {
@@ -590,6 +636,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
     }
   }
   if (blockIdx.x == 0 && tid == 0) {
+    a.pt[PT_KERNEL] += global_ns() - a.pt[PT_START];
     sS.skip_update = 1;
     *a.S_ = sS;
   }
@@ -692,6 +739,13 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   const size_t ns = (size_t)a.n_blocks * a.S;
   unsigned int epoch = 0;  // barriers passed (thread 0)
   if (tid == 0) sS = *a.S_;
+  if (tid == 0 && blockIdx.x == 0) {
+    const unsigned long long now = global_ns();
+    a.pt[PT_LAST] = now;
+    a.pt[PT_START] = now;
+    a.pt[PT_GRID] = gridDim.x;
+    a.pt[PT_LAUNCHES] += 1;
+  }
   if (tid < MAX_G) sk[tid] = tid < a.g ? skewer_of(a, blk, tid) : -1;
   __syncthreads();
   if (tid == 0) {
@@ -795,8 +849,10 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   // then updates x and r, applies the preconditioner, publishes the levels of
   // the new z and the partials of r.z and |r|^2 at the next barrier.
   levels_z();
-  if (grid_sync(a, B_LEVELS, epoch))
-    while (!sS.done && sS.iter < a.max_iter) {
+  if (grid_sync(a, B_LEVELS, epoch)) {
+    for (int k = 0; k < N_CALIB; ++k) grid_sync(a, B_CALIB, epoch);
+  }
+  while (!sS.done && sS.iter < a.max_iter) {
       const int it = sS.iter + 1;
       // ---- product: w = A32 z, p = z + beta p, q = w + beta q, partial p.q
       ff dq{0.f, 0.f};
@@ -982,6 +1038,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   for (int t = 0; t < RPT; ++t)
     if (jj[t] >= 0) a.x[rg[t]] = (double)xs[tid + t * NT].h + (double)xs[tid + t * NT].l;
   if (blockIdx.x == 0 && tid == 0) {
+    a.pt[PT_KERNEL] += global_ns() - a.pt[PT_START];
     sS.skip_update = 1;
     *a.S_ = sS;
   }
@@ -1066,6 +1123,11 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   const int grid = resident ? pc->n_sk : std::min(per_sm0[bi] * nsm, pc->n_sk);
   if (grid <= 0) return false;
   g.p_part.alloc((size_t)3 * grid + 1);
+  const size_t n_pt = PT_CTA + 8 * (size_t)grid;
+  if (g.p_time.n < n_pt) {  // the phase timers accumulate until read
+    g.p_time.alloc(n_pt);
+    DS_CUDA(cudaMemsetAsync(g.p_time.p, 0, g.p_time.bytes(), st));
+  }
   const size_t n_sync = (size_t)(1 + grid) * BAR_LINE;
   g.p_sync.alloc(n_sync);
   DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, n_sync * sizeof(int), st));
@@ -1111,6 +1173,7 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.bar = reinterpret_cast<unsigned int*>(g.p_sync.p);
   a.err = g.p_sync.p + 1;
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
+  a.pt = g.p_time.p;
   void* args[] = {&a};
   DS_CUDA(cudaLaunchCooperativeKernel(pick(resident), dim3(grid), dim3(NT), args,
                                       resident ? res_bytes : 0, st));
@@ -1126,6 +1189,42 @@ int persistent_error(ds_operator* op, cudaStream_t st) {
   DS_CUDA(cudaStreamSynchronize(st));
   if (code) DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, g.p_sync.bytes(), st));
   return code;
+}
+
+// The phase timers as per-visit averages (see ds_operator_get_persistent_profile).
+int persistent_profile(ds_operator* op, double* out, int n, bool reset) {
+  if (!op->sgrid || !op->sgrid->p_time.p) return 0;
+  SkewerGrid& g = *op->sgrid;
+  cudaStream_t st = op->ctx->stream;
+  std::vector<unsigned long long> v(g.p_time.n);
+  DS_CUDA(cudaMemcpyAsync(v.data(), g.p_time.p, v.size() * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaStreamSynchronize(st));
+  if (reset) DS_CUDA(cudaMemsetAsync(g.p_time.p, 0, g.p_time.bytes(), st));
+  std::vector<double> r(4 + 4 * 5, 0.0);
+  const int grid = (int)v[PT_GRID];
+  r[0] = (double)v[PT_LAUNCHES];
+  r[1] = v[PT_KERNEL] * 1e-6;  // ms
+  r[2] = grid;
+  if (v[PT_VISITS + B_CALIB]) r[3] = v[PT_PHASE + B_CALIB] * 1e-3 / v[PT_VISITS + B_CALIB];
+  for (int c = 1; c <= 5; ++c) {
+    const double vis = (double)v[PT_VISITS + c];
+    double* o = r.data() + 4 + 4 * (c - 1);
+    o[3] = vis;
+    if (!vis) continue;
+    o[0] = v[PT_PHASE + c] * 1e-3 / vis;  // us per visit (CTA 0, exit to exit)
+    double sum = 0.0, mx = 0.0;
+    for (int b = 0; b < grid && PT_CTA + 8 * (size_t)b + c < v.size(); ++b) {
+      const double w = (double)v[PT_CTA + 8 * (size_t)b + c];
+      sum += w;
+      mx = std::max(mx, w);
+    }
+    o[1] = grid ? sum * 1e-3 / vis / grid : 0.0;  // mean CTA work, us
+    o[2] = mx * 1e-3 / vis;                       // slowest CTA's work, us
+  }
+  const int m = std::min<int>(n, (int)r.size());
+  for (int i = 0; i < m; ++i) out[i] = r[i];
+  return m;
 }
 
 }  // namespace ds

@@ -249,6 +249,20 @@ int ds_operator_set_inner_matvec(ds_operator* op, int variant);
 enum { DS_ITER_AUTO = 0, DS_ITER_GRAPH = 1 };
 int ds_operator_set_iteration_form(ds_operator* op, int form);
 
+/* Phase timers of the persistent launches (%globaltimer on the device,
+ * accumulated since the last reset).  out[0] launches, out[1] their total
+ * device time (ms), out[2] CTAs, out[3] one empty grid barrier (us, from the
+ * calibration barriers each launch starts with); then for each phase
+ * c = 1..5 (1 levels of the first direction, 2 product, 3 step, 4 FP64
+ * levels of an update, 5 the update's residual and preconditioner) four
+ * values at out[4 + 4 (c - 1)]: us per visit (exit of the previous barrier
+ * to exit of this one, CTA 0), the CTAs' mean work per visit (us, to their
+ * arrival), the slowest CTA's work per visit (us) and the visits.  Writes
+ * min(n, 24) values; *written (may be null) gets that count, 0 before the
+ * first persistent launch.  reset != 0 clears the timers after reading. */
+int ds_operator_get_persistent_profile(ds_operator* op, double* out, int n, int reset,
+                                       int* written);
+
 /* ---- PCG ---------------------------------------------------------------- */
 /* PCGParams (lib/pcg.h:13-19); n is the operator's. */
 typedef struct {

@@ -218,3 +218,29 @@ def test_persistent_barrier_timeout_is_reported_and_recoverable(ctx):
     y = x / rec[:, 3]
     assert np.linalg.norm(op.A_residual(y)) <= 1e-8 * (1 + 1e-6) * np.linalg.norm(rec[:, 4])
     op.close()
+
+
+def test_persistent_profile_counts_phases(ctx):
+    """The persistent launches' phase timers: one launch per solve, one
+    product and one step phase per iteration, one FP64 update phase per
+    reliable update, positive times, and the slowest CTA's work at least the
+    mean; the reset clears them."""
+    n_sk, n_per = 32, 64
+    w = synth.small(n_sk, n_per, 12.0, seed=41)
+    op, _ = make(ctx, "w", w.pixels)
+    op.set_cluster_preconditioner(n_sk, n_per, cluster=4, band=16)
+    op.set_skewer_grid(n_sk, n_per)
+    assert op.persistent_profile() is None
+    _, res = op.solve_mixed(MixedParams(tol=1e-8))
+    prof = op.persistent_profile(reset=True)
+    assert prof["launches"] == 1 and prof["ctas"] >= 1 and prof["kernel_ms"] > 0
+    assert prof["barrier_us"] > 0
+    assert prof["product"]["visits"] == res.num_iters
+    assert prof["step"]["visits"] == res.num_iters
+    assert prof["update"]["visits"] == res.n_outer
+    for ph in ("product", "step"):
+        assert prof[ph]["us_per_visit"] > 0
+        assert prof[ph]["cta_max_us"] >= prof[ph]["cta_mean_us"] > 0
+    again = op.persistent_profile()
+    assert again["launches"] == 0 and again["product"]["visits"] == 0
+    op.close()
