@@ -99,6 +99,11 @@ struct MapColumns {
   DevBuf<int> ptr, idx, lev;       // CSR column -> skewers, classes kept
   DevBuf<double> p64;              // var_s exp(-c_perp |dxy|^2)
   DevBuf<double> R;                // Q x n_sk x nz
+  // the fused float-pair form (k_mc_fused): each column's list sorted by
+  // classes kept (descending), its factor as a float pair, the class taps as
+  // float pairs, and the operand split into float pairs per product
+  DevBuf<int> fidx, flev;
+  DevBuf<float2> fp, ftaps, xff;
 };
 
 struct OpF32;

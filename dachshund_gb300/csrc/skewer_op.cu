@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "ds_device.cuh"
+#include "ds_ff.cuh"
 #include "ds_ops.h"
 #include "ds_skewer.h"
 
@@ -643,6 +644,147 @@ void skewer_x_to_sorted(ds_operator* op, const double* x_rec, double* x_sorted, 
 
 // Distance classes, pixel windows and column -> skewer lists of a column
 // grid against the operator's skewer grid, for one cutoff.
+// ---- fused float-pair map ------------------------------------------------------
+// The same terms as k_mc_levels + k_mc_apply (pair (c, b) keeps the classes
+// q < lev_cb of its z window) in a different order:
+//   m[c, j] = sum_{k in window(j)} T_cls(j,k) Z_c^(cls(j,k))[k],
+//   Z_c^(q)[k] = sum_{b: lev_cb > q} P_cb x_b[k],
+// so each column needs its neighbours' pixel rows once (not their
+// class-summed rows at every map z: 256 instead of 512 terms per pair on the
+// 262,144-pixel workload).  With the list sorted by lev descending, one
+// running sum over the list gives every Z^(q): when lev drops below q + 1,
+// the sum so far is Z^(q).  All arithmetic is in float pairs (about 48
+// significant bits; GB300 issues FP64 at 1/64 of FP32), rounded to FP64 once
+// per output.
+constexpr int MF_T = 256;  // threads per column
+constexpr int MF_KMAX = 4; // pixels per thread at most (n_per <= 1024)
+constexpr int MF_U = 8;    // neighbour rows in flight per thread
+
+// Sorts each column's list by lev descending (stable by skewer), the factor
+// split into a float pair.  One thread per column.
+__global__ void k_mc_sort(int ncol, int Q, const int* __restrict__ ptr,
+                          const int* __restrict__ idx, const int* __restrict__ lev,
+                          const double* __restrict__ p64, int* __restrict__ sidx,
+                          int* __restrict__ slev, float2* __restrict__ sp) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncol) return;
+  const int q0 = ptr[c], q1 = ptr[c + 1];
+  int pos = q0;
+  for (int L = Q; L >= 1; --L)
+    for (int e = q0; e < q1; ++e)
+      if (lev[e] == L) {
+        const ff f = ff_from_double(p64[e]);
+        sidx[pos] = idx[e];
+        slev[pos] = L;
+        sp[pos] = make_float2(f.h, f.l);
+        ++pos;
+      }
+  for (; pos < q1; ++pos) {  // no class kept: contributes nothing
+    sidx[pos] = 0;
+    slev[pos] = 0;
+    sp[pos] = make_float2(0.f, 0.f);
+  }
+}
+
+// *acc += (*n_pairs) x per_pair (the profiler's term count).
+__global__ void k_add_terms(unsigned long long* acc, const int* n_pairs,
+                            unsigned long long per_pair) {
+  atomicAdd(acc, (unsigned long long)*n_pairs * per_pair);
+}
+
+// x (FP64) as float pairs.
+__global__ void k_mc_split(int n, const double* __restrict__ x, float2* __restrict__ xff) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const ff f = ff_from_double(x[i]);
+    xff[i] = make_float2(f.h, f.l);
+  }
+}
+
+// One CTA per map column: Z^(q) in shared memory (Q x n_per float pairs),
+// then the window sums.  MF_K pixels per thread (MF_K MF_T >= n_per).
+template <int MF_K>
+__global__ void __launch_bounds__(MF_T) k_mc_fused(int nz, int n_per, int W, int Q,
+                                                   const int* __restrict__ ptr,
+                                                   const int* __restrict__ sidx,
+                                                   const int* __restrict__ slev,
+                                                   const float2* __restrict__ sp,
+                                                   const float2* __restrict__ xff,
+                                                   const int* __restrict__ kstart,
+                                                   const signed char* __restrict__ cls,
+                                                   const float2* __restrict__ taps,
+                                                   double* __restrict__ m) {
+  extern __shared__ float2 Zs[];  // Q x n_per
+  __shared__ int s_off[MF_T];
+  __shared__ int s_lev[MF_T];
+  __shared__ float2 s_p[MF_T];
+  const int c = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int q0 = ptr[c], q1 = ptr[c + 1];
+  ff S[MF_K];
+#pragma unroll
+  for (int t = 0; t < MF_K; ++t) S[t] = ff{0.f, 0.f};
+  int lprev = Q;  // the same in every thread (all walk the same list)
+  for (int c0 = q0; c0 < q1; c0 += MF_T) {
+    const int cnt = min(MF_T, q1 - c0);
+    __syncthreads();
+    if (tid < cnt) {
+      s_off[tid] = sidx[c0 + tid] * n_per;
+      s_lev[tid] = slev[c0 + tid];
+      s_p[tid] = sp[c0 + tid];
+    }
+    __syncthreads();
+    for (int e0 = 0; e0 < cnt; e0 += MF_U) {
+      float2 xv[MF_U][MF_K];
+#pragma unroll
+      for (int u = 0; u < MF_U; ++u)
+#pragma unroll
+        for (int t = 0; t < MF_K; ++t) {
+          const int k = tid + t * MF_T;
+          xv[u][t] = (e0 + u < cnt && k < n_per) ? __ldg(xff + s_off[e0 + u] + k)
+                                                 : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+      for (int u = 0; u < MF_U; ++u) {
+        if (e0 + u >= cnt) break;
+        const int L = s_lev[e0 + u];
+        if (L < lprev) {  // the sum so far is Z^(q) for q in [L, lprev)
+          for (int q = L; q < lprev; ++q)
+#pragma unroll
+            for (int t = 0; t < MF_K; ++t) {
+              const int k = tid + t * MF_T;
+              if (k < n_per) Zs[q * n_per + k] = make_float2(S[t].h, S[t].l);
+            }
+          lprev = L;
+        }
+        const float2 pv = s_p[e0 + u];
+#pragma unroll
+        for (int t = 0; t < MF_K; ++t)
+          ff_mac(S[t].h, S[t].l, ff{pv.x, pv.y}, ff{xv[u][t].x, xv[u][t].y});
+      }
+    }
+  }
+  for (int q = 0; q < lprev; ++q)
+#pragma unroll
+    for (int t = 0; t < MF_K; ++t) {
+      const int k = tid + t * MF_T;
+      if (k < n_per) Zs[q * n_per + k] = make_float2(S[t].h, S[t].l);
+    }
+  __syncthreads();
+  for (int j = tid; j < nz; j += MF_T) {
+    float ah = 0.f, al = 0.f;
+    const int k0 = kstart[j];
+    for (int w = 0; w < W; ++w) {
+      const int q = cls[(size_t)j * W + w];
+      const int k = k0 + w;
+      if (q < 0 || k < 0 || k >= n_per) continue;
+      const float2 z = Zs[q * n_per + k];
+      const float2 tp = taps[q];
+      ff_mac(ah, al, ff{tp.x, tp.y}, ff{z.x, z.y});
+    }
+    m[(size_t)c * nz + j] = (double)ah + (double)al;
+  }
+}
+
 static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
   MapColumns& mc = *map->cols;
   const SkewerGrid& g = *op->sgrid;
@@ -704,6 +846,21 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
   mc.cls.alloc(cls.size());
   mc.taps.alloc(Q);
   mc.R.alloc((size_t)Q * n_sk * nz);
+  // the fused form's sorted lists and float-pair taps
+  mc.fidx.alloc(mc.idx.n);
+  mc.flev.alloc(mc.idx.n);
+  mc.fp.alloc(mc.idx.n);
+  k_mc_sort<<<(mc.ncol + 127) / 128, 128, 0, st>>>(mc.ncol, Q, mc.ptr.p, mc.idx.p, mc.lev.p,
+                                                   mc.p64.p, mc.fidx.p, mc.flev.p, mc.fp.p);
+  DS_CHECK_LAUNCH();
+  std::vector<float2> ftaps(Q);
+  for (int q = 0; q < Q; ++q) {
+    const float h = (float)taps[q];
+    ftaps[q] = make_float2(h, (float)(taps[q] - (double)h));
+  }
+  mc.ftaps.alloc(Q);
+  DS_CUDA(cudaMemcpyAsync(mc.ftaps.p, ftaps.data(), Q * sizeof(float2), cudaMemcpyHostToDevice,
+                          st));
   DS_CUDA(cudaMemcpyAsync(mc.kstart.p, kstart.data(), nz * sizeof(int), cudaMemcpyHostToDevice,
                           st));
   DS_CUDA(cudaMemcpyAsync(mc.cls.p, cls.data(), cls.size(), cudaMemcpyHostToDevice, st));
@@ -726,12 +883,41 @@ bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, doubl
     prof_terms = pr.d_pairs + 2;  // kind 2: map products
     pr.begin(st, &ev);
   }
-  k_mc_levels<<<dim3(g.n_sk, (mc.nz + 127) / 128), 128, 0, st>>>(
-      g.n_sk, g.n_per, mc.nz, mc.W, mc.Q, mc.kstart.p, mc.cls.p, mc.taps.p, x_dev, mc.R.p);
-  DS_CHECK_LAUNCH();
-  k_mc_apply<<<dim3(mc.ncol, (mc.nz + 128 * MC_PPT - 1) / (128 * MC_PPT)), 128, 0, st>>>(
-      g.n_sk, mc.nz, mc.ptr.p, mc.idx.p, mc.lev.p, mc.p64.p, mc.R.p, m_dev, prof_terms);
-  DS_CHECK_LAUNCH();
+  // the fused float-pair form when a column's Z^(q) fit in shared memory
+  const size_t zs_bytes = (size_t)mc.Q * g.n_per * sizeof(float2);
+  static int smem_optin = -1;
+  if (smem_optin < 0) {
+    int dev = 0;
+    DS_CUDA(cudaGetDevice(&dev));
+    DS_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  }
+  if (g.n_per <= MF_T * MF_KMAX && zs_bytes + 4 * 1024 <= (size_t)smem_optin) {
+    const int K = (g.n_per + MF_T - 1) / MF_T;
+    auto fn = K == 1 ? k_mc_fused<1> : K == 2 ? k_mc_fused<2> : K == 3 ? k_mc_fused<3>
+                                                                         : k_mc_fused<4>;
+    if (zs_bytes > 48 * 1024)
+      DS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)zs_bytes));
+    const int n = g.n_sk * g.n_per;
+    mc.xff.alloc(n);
+    k_mc_split<<<std::min(1024, (n + 255) / 256), 256, 0, st>>>(n, x_dev, mc.xff.p);
+    DS_CHECK_LAUNCH();
+    fn<<<mc.ncol, MF_T, zs_bytes, st>>>(mc.nz, g.n_per, mc.W, mc.Q, mc.ptr.p, mc.fidx.p,
+                                        mc.flev.p, mc.fp.p, mc.xff.p, mc.kstart.p, mc.cls.p,
+                                        mc.ftaps.p, m_dev);
+    DS_CHECK_LAUNCH();
+    if (prof_terms) {  // the FP64 form's term count (pairs x map z), for comparable rates
+      k_add_terms<<<1, 1, 0, st>>>(prof_terms, mc.ptr.p + mc.ncol, (unsigned long long)mc.nz);
+      DS_CHECK_LAUNCH();
+    }
+  } else {
+    k_mc_levels<<<dim3(g.n_sk, (mc.nz + 127) / 128), 128, 0, st>>>(
+        g.n_sk, g.n_per, mc.nz, mc.W, mc.Q, mc.kstart.p, mc.cls.p, mc.taps.p, x_dev, mc.R.p);
+    DS_CHECK_LAUNCH();
+    k_mc_apply<<<dim3(mc.ncol, (mc.nz + 128 * MC_PPT - 1) / (128 * MC_PPT)), 128, 0, st>>>(
+        g.n_sk, mc.nz, mc.ptr.p, mc.idx.p, mc.lev.p, mc.p64.p, mc.R.p, m_dev, prof_terms);
+    DS_CHECK_LAUNCH();
+  }
   if (ev) pr.end(st, ev, 2);
   return true;
 }
