@@ -716,6 +716,7 @@ def run_ours(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     times, results, parts = [], [], []
+    op.persistent_profile(reset=True)  # the phase timers of the timed steps only
     launches0 = ctx.profile()["kernel_launches"]
     clocks.mark_start()
     for _ in range(args.steps):
@@ -744,6 +745,7 @@ def run_ours(args, rank, world, local):
     launches = (ctx.profile()["kernel_launches"] - launches0) / args.steps
     clk = clocks.stop()
     step_s = allmax(statistics.mean(times))
+    phases = op.persistent_profile(reset=True)
     # the step's two calls (CUDA events between them) and the solve's own
     # device time (the library's events around its launches)
     step_parts = {"solve": statistics.mean(p[0] for p in parts),
@@ -978,6 +980,7 @@ def run_ours(args, rank, world, local):
                        "l2": "flushed between steps (256 MiB write)"},
             "cg_iters": r0.num_iters, "fp64_updates": r0.n_outer,
             "step_parts_s": step_parts,
+            "persistent_phases": phases,
             "preconditioner": pc_info,
             "jacobi_mixed": jacobi,
             "final_rel_residual": r0.final_norm / r0.norm_b,

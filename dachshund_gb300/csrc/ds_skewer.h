@@ -41,6 +41,9 @@ struct SkewerGrid {
   DevBuf<double> p_part;
   DevBuf<int> p_sync;
   DevBuf<unsigned long long> p_time;  // its phase timers
+  // float-pair copies for the persistent solve's FP64-accurate update
+  // (record-order coefficients, outer factors, z taps; built on first use)
+  DevBuf<float2> ff_wl, ff_wr, ff_e, ff_b, ff_op, ff_taps;
   // the longest FP32 neighbour list of a preconditioner block (for the
   // preconditioner and inner cutoff it was counted for)
   const void* res_pc = nullptr;

@@ -86,6 +86,9 @@ struct PersistArgs {
   int* err;
   long long limit;
   unsigned long long* pt;  // phase timers (PT_* layout)
+  // float-pair copies for the resident form's update (record order; the
+  // outer lists' factors; the z taps)
+  const float2 *wl_ff, *wr_ff, *e_ff, *b_ff, *op_ff, *taps64_ff;
 };
 
 // Barrier codes: the phase whose closing barrier gave up (also the phase
@@ -642,6 +645,85 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
   }
 }
 
+// a b for float pairs, renormalised (the product's error by FMA, the cross
+// terms in FP32).
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  ff r;
+  fast_two_sum(p, e, r.h, r.l);
+  return r;
+}
+
+// The FP64-accurate product of block blk in float pairs: out[t] = sum over
+// the outer list of the skewer of record t of P V[(lev - 1) n + idx n_per +
+// k] with P and V float pairs (V the levels of the update, stored as float
+// pairs), the lists staged NB_R entries at a time as in block_product.
+__device__ __forceinline__ void block_product_ff(const PersistArgs& a, int blk, const float2* V,
+                                                size_t* s_off, float2* s_p, int* s_cnt,
+                                                ff (&out)[RPT]) {
+  const int m = a.g * a.n_per;
+  const size_t n = (size_t)a.n;
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) out[t] = ff{0.f, 0.f};
+  int jj[RPT], kk[RPT];
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = threadIdx.x + t * NT;
+    jj[t] = i < m ? i / a.n_per : -1;
+    kk[t] = i < m ? i - jj[t] * a.n_per : 0;
+  }
+  for (int c0 = 0;; c0 += NB_R) {
+    __syncthreads();
+    if (threadIdx.x < MAX_G) {
+      const int j = threadIdx.x;
+      const int s = j < a.g ? skewer_of(a, blk, j) : -1;
+      const int len = s >= 0 ? a.optr[s + 1] - a.optr[s] : 0;
+      s_cnt[j] = max(0, min(NB_R, len - c0));
+      s_cnt[MAX_G + j] = len - c0 > NB_R;
+    }
+    for (int t = threadIdx.x; t < a.g * NB_R; t += NT) {
+      const int j = t / NB_R, e = t - j * NB_R;
+      const int s = skewer_of(a, blk, j);
+      if (s < 0) continue;
+      const int q = a.optr[s] + c0 + e;
+      if (q < a.optr[s + 1]) {
+        s_off[t] = (size_t)(a.olev[q] - 1) * n + (size_t)a.oidx[q] * a.n_per;
+        s_p[t] = a.op_ff[q];
+      }
+    }
+    __syncthreads();
+    int cnt[RPT];
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) cnt[t] = jj[t] >= 0 ? s_cnt[jj[t]] : 0;
+    int cmax = 0;
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) cmax = max(cmax, cnt[t]);
+    for (int e = 0; e < cmax; e += UF64) {
+      float2 v[RPT][UF64];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t)
+#pragma unroll
+        for (int u = 0; u < UF64; ++u)
+          v[t][u] = e + u < cnt[t] ? __ldcg(V + s_off[jj[t] * NB_R + e + u] + kk[t])
+                                   : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int t = 0; t < RPT; ++t)
+#pragma unroll
+        for (int u = 0; u < UF64; ++u)
+          if (e + u < cnt[t]) {
+            const float2 pv = s_p[jj[t] * NB_R + e + u];
+            ff_mac(out[t].h, out[t].l, ff{pv.x, pv.y}, ff{v[t][u].x, v[t][u].y});
+          }
+    }
+    int more = 0;
+    for (int j = 0; j < MAX_G; ++j) more |= s_cnt[MAX_G + j];
+    if (!more) break;
+  }
+}
+
 // ---- resident form: one block per CTA, the block's vectors in shared memory
 //
 // With at most one block per CTA (the cooperative grid holds every block),
@@ -954,12 +1036,17 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
         __syncthreads();
       }
       if (!sS.need_update) continue;
-      // ---- FP64 update: levels of u = wr x (FP64 coefficients from global memory)
+      // ---- FP64-accurate update in float pairs (GB300 issues FP64 at 1/64 of
+      // FP32): levels of u = wr x, stored as float pairs in the FP64 levels'
+      // buffer
+      float2* ufs = reinterpret_cast<float2*>(us);
+      float2* V2 = reinterpret_cast<float2*>(a.V64);
 #pragma unroll
       for (int t = 0; t < RPT; ++t)
         if (jj[t] >= 0) {
-          const ff xv = xs[tid + t * NT];
-          us[tid + t * NT] = a.wr[rg[t]] * ((double)xv.h + (double)xv.l);
+          const float2 w = a.wr_ff[rg[t]];
+          const ff u = ff_mul(ff{w.x, w.y}, xs[tid + t * NT]);
+          ufs[tid + t * NT] = make_float2(u.h, u.l);
         }
       __syncthreads();
 #pragma unroll
@@ -967,28 +1054,31 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
         const int i = tid + t * NT;
         if (jj[t] < 0) continue;
         const int k = kk[t];
-        double acc = us[i];
-        a.V64[rg[t]] = acc;
+        ff acc{ufs[i].x, ufs[i].y};
+        V2[rg[t]] = make_float2(acc.h, acc.l);
         for (int l = 1; l <= a.olmax; ++l) {
-          double v = 0.0;
-          if (k + l < npr) v = us[i + l];
-          if (k - l >= 0) v += us[i - l];
-          acc = fma(a.taps64[l], v, acc);
-          a.V64[(size_t)l * n + rg[t]] = acc;
+          ff v{0.f, 0.f};
+          if (k + l < npr) v = ff{ufs[i + l].x, ufs[i + l].y};
+          if (k - l >= 0) v = ff_add(v, ff{ufs[i - l].x, ufs[i - l].y});
+          const float2 tp = a.taps64_ff[l];
+          ff_mac(acc.h, acc.l, ff{tp.x, tp.y}, v);
+          V2[(size_t)l * n + rg[t]] = make_float2(acc.h, acc.l);
         }
       }
       if (!grid_sync(a, B_LEVELS64, epoch)) break;
       // r64 = b - A x of the block (into us); r = r64, z = G G^T r, levels of z
       {
-        double acc[RPT];
-        block_product<double, UF64, NB_R>(a, blk, a.optr, a.oidx, a.olev, a.op64, a.V64, s_off,
-                                          s_p64, s_cnt, acc);
+        ff acc[RPT];
+        block_product_ff(a, blk, reinterpret_cast<const float2*>(a.V64), s_off,
+                         reinterpret_cast<float2*>(s_p64), s_cnt, acc);
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
           if (jj[t] < 0) continue;
           const int i = tid + t * NT;
-          const double xv = (double)xs[i].h + (double)xs[i].l;
-          us[i] = a.b[rg[t]] - fma(a.wl[rg[t]], acc[t], a.e[rg[t]] * xv);
+          const float2 wl = a.wl_ff[rg[t]], e = a.e_ff[rg[t]], b = a.b_ff[rg[t]];
+          const ff y = ff_add(ff_mul(ff{wl.x, wl.y}, acc[t]), ff_mul(ff{e.x, e.y}, xs[i]));
+          const ff r = ff_sub(ff{b.x, b.y}, y);
+          us[i] = (double)r.h + (double)r.l;
         }
       }
       __syncthreads();
@@ -1042,6 +1132,21 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
     sS.skip_update = 1;
     *a.S_ = sS;
   }
+}
+
+// out = in as float pairs.
+__global__ void k_to_ff(size_t n, const double* __restrict__ in, float2* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const ff f = ff_from_double(in[i]);
+    out[i] = make_float2(f.h, f.l);
+  }
+}
+
+void to_ff(DevBuf<float2>& out, const double* in, size_t n, cudaStream_t st) {
+  out.alloc(n);
+  k_to_ff<<<(unsigned)std::min<size_t>(1024, (n + 255) / 256), 256, 0, st>>>(n, in, out.p);
+  DS_CHECK_LAUNCH();
 }
 
 // Resident CTAs per SM of a kernel at `smem` dynamic bytes (0: does not fit).
@@ -1174,6 +1279,21 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.err = g.p_sync.p + 1;
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
   a.pt = g.p_time.p;
+  if (!g.ff_b.p) {  // float-pair copies for the update (fixed for the grid's life)
+    const size_t np = (size_t)op->pix.n_pad;
+    to_ff(g.ff_wl, sv.wl, np, st);
+    to_ff(g.ff_wr, sv.wr, np, st);
+    to_ff(g.ff_e, sv.e, np, st);
+    to_ff(g.ff_b, sv.b, np, st);
+    to_ff(g.ff_op, g.outer.p64.p, g.outer.p64.n, st);
+    to_ff(g.ff_taps, g.taps64.p, g.taps64.n, st);
+  }
+  a.wl_ff = g.ff_wl.p;
+  a.wr_ff = g.ff_wr.p;
+  a.e_ff = g.ff_e.p;
+  a.b_ff = g.ff_b.p;
+  a.op_ff = g.ff_op.p;
+  a.taps64_ff = g.ff_taps.p;
   void* args[] = {&a};
   DS_CUDA(cudaLaunchCooperativeKernel(pick(resident), dim3(grid), dim3(NT), args,
                                       resident ? res_bytes : 0, st));
