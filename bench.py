@@ -47,6 +47,9 @@ K_PAIR_F32_DRAM_BYTES = 9_174_528
 # k_sg32_apply) on the 262,144-pixel workload, from one ncu capture
 # (profiles/k_sg32_inner_wf262144.md)
 K_SG32_DRAM_BYTES = 16_603_136  # k_sg32_levels 4,202,496 + k_sg32_apply 12,400,640
+# DRAM bytes (read + write) of one launch of the persistent solve on the
+# 262,144-pixel workload (profiles/k_mixed_resident_wf262144.md)
+K_PERSIST_DRAM_BYTES = 44_816_384  # read 43,266,304 + write 1,550,080
 # the structured inner operator's cutoff (DS_DEFAULT_STRUCTURED_INNER_CUTOFF)
 SG_INNER_CUT = 14.0
 # FP64-pipe instructions per evaluated pair of the plain FP64 kernel
@@ -811,28 +814,58 @@ def run_ours(args, rank, world, local):
             "term": "one FP64 FMA of a (skewer pair, pixel): perpendicular factor x "
                     "z-convolved column value"},
         "map": {
-            "kernel": "structured FP64 map (k_mc_levels + k_mc_apply)",
+            "kernel": "structured map, fused float-pair form (k_mc_split + k_mc_fused)",
             "ms_per_step": map_ms / prof_steps,
             "Gterm_per_s": map_pairs / (map_ms * 1e-3) / 1e9 if map_ms else None,
-            "term": "one FP64 FMA of a (map column, skewer, map z) triple"},
+            "term": "one (map column, skewer, map z) triple of the FP64 form (the fused form "
+                    "does 256 float-pair multiply-adds per (column, skewer) pair instead of 512 "
+                    "FP64 FMAs)"},
     }
     hbm = measured_peaks().get("hbm_gbs")
-    sg_gbs = sg_bytes / (sg_us * 1e-6) / 1e9 if sg_us else None
+    # The timed step's dominant kernel is the persistent solve (one cooperative
+    # launch per solve, ~89% of the step: profiles/launch_list_wf262144_chosen.md).
+    # Its algorithmic bytes per launch: the start loads each block's state
+    # into shared memory (x 8, p z r 4 each, wl wr e 8 each per pixel; the
+    # FSAI planes 4 (band + 1) per slot, the slot map 4; the inner lists 12
+    # per entry), every iteration writes the z-convolution levels of z once
+    # and reads them back once (2 x 4 (lmax + 1) per pixel), every FP64 update
+    # does the same for the float-pair levels of x (2 x 8 (lmax64 + 1)) and
+    # reads wl wr e b as float pairs (32) and the outer lists (16 per entry),
+    # and the end writes x (8).  The neighbours re-read the levels from L2
+    # (terms x 4 bytes per iteration): that traffic, not HBM, bounds it.
+    c_para = 1.0 / (2 * w.l_para ** 2)
+    lmax64 = 0
+    while lmax64 + 1 < w.pix_per_skewer and \
+            c_para * ((lmax64 + 1) * synth.DZ) ** 2 < 40.0:  # DS_DEFAULT_EXACT_CUTOFF
+        lmax64 += 1
+    r_last = results[-1]
+    n_it, n_up = r_last.num_iters, r_last.n_outer
+    entries_in = terms_per_product / w.pix_per_skewer
+    entries_out = (f64_pairs / f64_n / w.pix_per_skewer) if f64_n else entries_in
+    persist_bytes = (w.n * (8 + 12 + 24 + 4 * (PC_BAND + 1) + 4 + 8) + 12 * entries_in
+                     + n_it * w.n * 2 * 4 * (lmax + 1)
+                     + n_up * (w.n * (2 * 8 * (lmax64 + 1) + 32) + 16 * entries_out))
+    persist_us = (phases["kernel_ms"] / phases["launches"] * 1e3) \
+        if phases and phases["launches"] else None
+    persist_gbs = persist_bytes / (persist_us * 1e-6) / 1e9 if persist_us else None
+    l2_reads = n_it * terms_per_product * 4
     roofline = {
-        "kernel": "structured FP32 inner product (k_sg32_levels + k_sg32_apply), the "
-                  "dominant kernel pair of the chosen form's step",
+        "kernel": "persistent structured mixed solve (k_mixed_resident<16>), the dominant "
+                  "kernel of the chosen form's step",
         "bound": "hbm", "unit": "GB/s",
-        "achieved": sg_gbs, "peak": hbm,
-        "frac": (sg_gbs / hbm) if (sg_gbs and hbm) else None,
+        "achieved": persist_gbs, "peak": hbm,
+        "frac": (persist_gbs / hbm) if (persist_gbs and hbm) else None,
         "peak_basis": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-        "algorithmic_bytes_per_launch": sg_bytes,
-        "launch_us": sg_us,
-        # DRAM bytes (read + write) of one product (both kernels), from one ncu
-        # capture on this workload (profiles/k_sg32_inner_wf262144.md): the
-        # column values are re-read from L2 by every neighbour (70% L2 hits),
-        # and the kernels are latency-bound, not bandwidth-bound
-        "traffic": K_SG32_DRAM_BYTES,
-        "traffic_unit": "bytes per product (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+        "algorithmic_bytes_per_launch": persist_bytes,
+        "launch_us": persist_us,
+        "iterations_per_launch": n_it, "fp64_updates_per_launch": n_up,
+        # DRAM bytes (read + write) of one launch, from one ncu capture of this
+        # workload (profiles/k_mixed_resident_wf262144.md); the state stays in
+        # shared memory and L2 for the whole solve
+        "traffic": K_PERSIST_DRAM_BYTES,
+        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+        "l2_neighbour_reads_per_launch": l2_reads,
+        "l2_neighbour_read_GBps": l2_reads / (persist_us * 1e-6) / 1e9 if persist_us else None,
     }
 
     # Plain FP64 GPU PCG on the same system (once, untimed by the step loop).
