@@ -44,11 +44,14 @@ struct SkewerGrid {
   // float-pair copies for the persistent solve's FP64-accurate update
   // (record-order coefficients, outer factors, z taps; built on first use)
   DevBuf<float2> ff_wl, ff_wr, ff_e, ff_b, ff_op, ff_taps;
-  // the longest FP32 neighbour list of a preconditioner block (for the
-  // preconditioner and inner cutoff it was counted for)
+  // the persistent solve's product items (for the preconditioner and inner
+  // cutoff they were built for)
   const void* res_pc = nullptr;
   double res_cut = 0.0;
-  int res_max_list = 0;
+  int res_max_list = 0;  // the most items of a block (above the limit: not built)
+  DevBuf<int> it_ptr;            // per block: its items
+  DevBuf<unsigned int> it_off;   // item: offset of its (neighbour, level) row in the levels
+  DevBuf<float4> it_coef;        // item: the factor for each of the block's skewers
 };
 
 // The vectors a structured product addresses: pos maps a record to its

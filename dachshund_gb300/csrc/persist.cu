@@ -55,7 +55,7 @@ constexpr int NB = 128;      // neighbour entries staged per skewer per round (g
 constexpr int NB_R = 32;     // the same for the resident form's FP64 residual
 constexpr int UF32 = 8;      // neighbour loads in flight per record: FP32 product
 constexpr int UF64 = 4;      // FP64 product
-constexpr int UFR = 12;      // FP32 product of the resident form (one accumulator per record)
+constexpr int UFI = 16;      // FP32 product of the resident form: neighbour rows in flight
 constexpr int MAX_BAND = 32;
 constexpr int RPT = MAX_S / NT;  // records (slots) per thread
 
@@ -86,6 +86,12 @@ struct PersistArgs {
   int* err;
   long long limit;
   unsigned long long* pt;  // phase timers (PT_* layout)
+  // the resident form's product items per block (it_ptr: n_blocks + 1; an
+  // item is one (neighbour skewer, level) row: its offset into the levels and
+  // the factor for each of the block's (<= 4) skewers, 0 where unused)
+  const int* it_ptr;
+  const unsigned int* it_off;
+  const float4* it_coef;
   // float-pair copies for the resident form's update (record order; the
   // outer lists' factors; the z taps)
   const float2 *wl_ff, *wr_ff, *e_ff, *b_ff, *op_ff, *taps64_ff;
@@ -734,18 +740,19 @@ __device__ __forceinline__ void block_product_ff(const PersistArgs& a, int blk, 
 // factor (C) and the partials, and the levels they publish (A, D).  x goes
 // back to global memory at the end.  Same recurrence, same sums in the same
 // order as the general form.
-constexpr int NL = 1024;  // FP32 neighbour entries of a block kept in shared memory
+constexpr int NI = 512;   // product items of a block kept in shared memory
+constexpr int GI = 4;     // skewers per block of the item form at most
 
 // Shared-memory layout of the resident form (bytes from the dynamic base).
 struct ResLayout {
   static constexpr size_t xs = 0;                                   // double[MAX_S]
   static constexpr size_t us = xs + MAX_S * sizeof(double);         // double[MAX_S]
-  static constexpr size_t loff = us + MAX_S * sizeof(double);       // uint32[NL]
-  static constexpr size_t ps = loff + NL * sizeof(unsigned int);    // float[MAX_S] x 8
-  static constexpr size_t lp = ps + 8 * MAX_S * sizeof(float);      // float[NL]
-  static constexpr size_t loc = lp + NL * sizeof(float);            // int[MAX_S]
-  static constexpr size_t lptr = loc + MAX_S * sizeof(int);         // int[MAX_G + 1]
-  static constexpr size_t sk = lptr + (MAX_G + 1) * sizeof(int);    // int[MAX_G]
+  static constexpr size_t ps = us + MAX_S * sizeof(double);         // float[MAX_S] x 8
+  static constexpr size_t icoef = ps + 8 * MAX_S * sizeof(float);   // float4[NI]
+  static constexpr size_t ioff = icoef + NI * sizeof(float4);       // uint32[NI]
+  static constexpr size_t loc = ioff + NI * sizeof(unsigned int);   // int[MAX_S]
+  static constexpr size_t nit = loc + MAX_S * sizeof(int);          // int (items)
+  static constexpr size_t sk = nit + 4 * sizeof(int);               // int[MAX_G]
   static constexpr size_t lh = (sk + MAX_G * sizeof(int) + 15) / 16 * 16;  // half[(band + 1) S]
   static size_t bytes(int band, int S) { return lh + ((size_t)(band + 1) * S * 2 + 15) / 16 * 16; }
 };
@@ -789,7 +796,9 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   ff* xs = reinterpret_cast<ff*>(smraw + ResLayout::xs);  // the iterate, float pairs
   double* us = reinterpret_cast<double*>(smraw + ResLayout::us);
-  unsigned int* loff = reinterpret_cast<unsigned int*>(smraw + ResLayout::loff);
+  float4* icoef = reinterpret_cast<float4*>(smraw + ResLayout::icoef);
+  unsigned int* ioff = reinterpret_cast<unsigned int*>(smraw + ResLayout::ioff);
+  int* s_nit = reinterpret_cast<int*>(smraw + ResLayout::nit);
   float* ps = reinterpret_cast<float*>(smraw + ResLayout::ps);
   float* zs = ps + MAX_S;
   float* qs = zs + MAX_S;
@@ -798,9 +807,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   float* wls = ts + MAX_S;  // FP32 coefficients
   float* wrs = wls + MAX_S;
   float* es = wrs + MAX_S;
-  float* lp = reinterpret_cast<float*>(smraw + ResLayout::lp);
   int* loc = reinterpret_cast<int*>(smraw + ResLayout::loc);  // slot -> record-local index
-  int* lptr = reinterpret_cast<int*>(smraw + ResLayout::lptr);
   int* sk = reinterpret_cast<int*>(smraw + ResLayout::sk);
   __half* Lh = reinterpret_cast<__half*>(smraw + ResLayout::lh);
   __shared__ MixedState sS;
@@ -829,24 +836,15 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
     a.pt[PT_LAUNCHES] += 1;
   }
   if (tid < MAX_G) sk[tid] = tid < a.g ? skewer_of(a, blk, tid) : -1;
-  __syncthreads();
-  if (tid == 0) {
-    int c = 0;
-    for (int j = 0; j < a.g; ++j) {
-      lptr[j] = c;
-      if (sk[j] >= 0) c += a.iptr[sk[j] + 1] - a.iptr[sk[j]];
-    }
-    lptr[a.g] = c;
-  }
-  __syncthreads();
-  for (int j = 0; j < a.g; ++j) {
-    if (sk[j] < 0) continue;
-    const int q0 = a.iptr[sk[j]], c0 = lptr[j], cnt = lptr[j + 1] - c0;
-    for (int e = tid; e < cnt; e += NT) {
-      loff[c0 + e] = (unsigned int)((size_t)(a.ilev[q0 + e] - 1) * n + (size_t)a.iidx[q0 + e] * npr);
-      lp[c0 + e] = a.ip32[q0 + e];
+  {  // the block's product items
+    const int i0 = a.it_ptr[blk], ni = a.it_ptr[blk + 1] - i0;
+    if (tid == 0) *s_nit = ni;
+    for (int e = tid; e < ni; e += NT) {
+      ioff[e] = a.it_off[i0 + e];
+      icoef[e] = a.it_coef[i0 + e];
     }
   }
+  __syncthreads();
   for (int i = tid; i < m; i += NT) {
     const int j = i / npr;
     const int s = sk[j];
@@ -936,41 +934,50 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   }
   while (!sS.done && sS.iter < a.max_iter) {
       const int it = sS.iter + 1;
-      // ---- product: w = A32 z, p = z + beta p, q = w + beta q, partial p.q
+      // ---- product: w = A32 z, p = z + beta p, q = w + beta q, partial p.q.
+      // Each (neighbour, level) row the block's skewers use is loaded once
+      // and applied to all of them: thread (part, k) takes pixel k of a
+      // share of the block's items, UFI rows in flight, one accumulator per
+      // skewer; the NT / n_per shares of a pixel are summed in order through
+      // shared memory (us, free in this phase).
       ff dq{0.f, 0.f};
       {
         if (tid == 0) s_ab = (float)sS.beta;
-        float acc[RPT];
-        int c0[RPT], cnt[RPT];
-        int cmax = 0;
+        float* red_w = reinterpret_cast<float*>(us);  // (NT / n_per) x GI x n_per
+        const int tk = NT / npr;  // threads per pixel
+        const int kq = tid % npr, part = tid / npr;
+        const int ni = *s_nit;
+        const int e0 = part * ni / tk, e1 = (part + 1) * ni / tk;
+        float acc[GI];
 #pragma unroll
-        for (int t = 0; t < RPT; ++t) {
-          acc[t] = 0.f;
-          c0[t] = jj[t] >= 0 ? lptr[jj[t]] : 0;
-          cnt[t] = jj[t] >= 0 ? lptr[jj[t] + 1] - c0[t] : 0;
-          cmax = max(cmax, cnt[t]);
+        for (int j = 0; j < GI; ++j) acc[j] = 0.f;
+        for (int e = e0; e < e1; e += UFI) {
+          float v[UFI];
+#pragma unroll
+          for (int u = 0; u < UFI; ++u)
+            v[u] = e + u < e1 ? __ldcg(a.V32 + ioff[e + u] + kq) : 0.f;
+#pragma unroll
+          for (int u = 0; u < UFI; ++u)
+            if (e + u < e1) {
+              const float4 c = icoef[e + u];
+              acc[0] = fmaf(c.x, v[u], acc[0]);
+              acc[1] = fmaf(c.y, v[u], acc[1]);
+              acc[2] = fmaf(c.z, v[u], acc[2]);
+              acc[3] = fmaf(c.w, v[u], acc[3]);
+            }
         }
-        for (int e = 0; e < cmax; e += UFR) {
-          float v[RPT][UFR];
 #pragma unroll
-          for (int t = 0; t < RPT; ++t)
-#pragma unroll
-            for (int u = 0; u < UFR; ++u)
-              v[t][u] = e + u < cnt[t] ? __ldcg(a.V32 + loff[c0[t] + e + u] + kk[t]) : 0.f;
-#pragma unroll
-          for (int t = 0; t < RPT; ++t)
-#pragma unroll
-            for (int u = 0; u < UFR; ++u)
-              if (e + u < cnt[t]) acc[t] = fmaf(lp[c0[t] + e + u], v[t][u], acc[t]);
-        }
-        __syncthreads();  // s_ab
+        for (int j = 0; j < GI; ++j) red_w[(part * GI + j) * npr + kq] = acc[j];
+        __syncthreads();  // red_w, s_ab
         const float beta = s_ab;
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
           if (jj[t] < 0) continue;
           const int i = tid + t * NT;
+          float sum = 0.f;
+          for (int pp = 0; pp < tk; ++pp) sum += red_w[(pp * GI + jj[t]) * npr + kk[t]];
           const float zv = zs[i];
-          const float wv = fmaf(wls[i], acc[t], es[i] * zv);
+          const float wv = fmaf(wls[i], sum, es[i] * zv);
           const float pv = fmaf(beta, ps[i], zv);
           const float qv = fmaf(beta, qs[i], wv);
           ps[i] = pv;
@@ -1190,26 +1197,73 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   };
   // The resident form when every block gets its own resident CTA and the
   // longest FP32 neighbour list of a block fits in shared memory.
+  // The resident form's product items, built once per preconditioner and
+  // inner cutoff: per block, the distinct (neighbour, level) rows its
+  // skewers' FP32 lists name, ordered by offset, with each skewer's factor.
+  const bool off32 = (double)(g.inner.lmax + 1) * (double)op->n < 4294967295.0;
   if (g.res_pc != pc || g.res_cut != g.inner.cut) {
-    std::vector<int> ptr(g.n_sk + 1), bsk(pc->bsk.n);
-    DS_CUDA(cudaMemcpyAsync(ptr.data(), g.inner.ptr.p, ptr.size() * sizeof(int),
-                            cudaMemcpyDeviceToHost, st));
-    if (pc->bsk.p)
-      DS_CUDA(cudaMemcpyAsync(bsk.data(), pc->bsk.p, bsk.size() * sizeof(int),
+    g.res_max_list = NI + 1;  // unusable until built
+    if (off32 && pc->g <= GI && NT % g.n_per == 0) {
+      const size_t ne = g.inner.idx.n;
+      std::vector<int> ptr(g.n_sk + 1), bsk(pc->bsk.n), idx(ne), lev(ne);
+      std::vector<float> pv(ne);
+      DS_CUDA(cudaMemcpyAsync(ptr.data(), g.inner.ptr.p, ptr.size() * sizeof(int),
                               cudaMemcpyDeviceToHost, st));
-    DS_CUDA(cudaStreamSynchronize(st));
-    int mx = 0;
-    for (int b = 0; b < pc->n_sk; ++b) {
-      int c = 0;
-      for (int j = 0; j < pc->g; ++j) {
-        const int s = pc->bsk.p ? bsk[(size_t)b * pc->g + j] : (j == 0 ? b : -1);
-        if (s >= 0) c += ptr[s + 1] - ptr[s];
+      DS_CUDA(cudaMemcpyAsync(idx.data(), g.inner.idx.p, ne * sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
+      DS_CUDA(cudaMemcpyAsync(lev.data(), g.inner.lev.p, ne * sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
+      DS_CUDA(cudaMemcpyAsync(pv.data(), g.inner.p32.p, ne * sizeof(float),
+                              cudaMemcpyDeviceToHost, st));
+      if (pc->bsk.p)
+        DS_CUDA(cudaMemcpyAsync(bsk.data(), pc->bsk.p, bsk.size() * sizeof(int),
+                                cudaMemcpyDeviceToHost, st));
+      DS_CUDA(cudaStreamSynchronize(st));
+      std::vector<int> iptr(pc->n_sk + 1, 0);
+      std::vector<unsigned int> ioff;
+      std::vector<float4> icoef;
+      std::vector<std::pair<unsigned int, std::pair<int, float>>> ent;  // (offset, (skewer j, factor))
+      int mx = 0;
+      for (int b = 0; b < pc->n_sk; ++b) {
+        ent.clear();
+        for (int j = 0; j < pc->g; ++j) {
+          const int sj = pc->bsk.p ? bsk[(size_t)b * pc->g + j] : (j == 0 ? b : -1);
+          if (sj < 0) continue;
+          for (int q = ptr[sj]; q < ptr[sj + 1]; ++q)
+            ent.push_back({(unsigned int)((size_t)(lev[q] - 1) * op->n + (size_t)idx[q] * g.n_per),
+                           {j, pv[q]}});
+        }
+        std::sort(ent.begin(), ent.end(),
+                  [](const auto& x, const auto& y) {
+                    return x.first < y.first || (x.first == y.first && x.second.first < y.second.first);
+                  });
+        int nb = 0;
+        for (size_t e = 0; e < ent.size(); ++e) {
+          if (e == 0 || ent[e].first != ent[e - 1].first) {
+            ioff.push_back(ent[e].first);
+            icoef.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+            ++nb;
+          }
+          float* c = &icoef.back().x;
+          c[ent[e].second.first] = ent[e].second.second;
+        }
+        iptr[b + 1] = iptr[b] + nb;
+        mx = std::max(mx, nb);
       }
-      mx = std::max(mx, c);
+      g.it_ptr.alloc(iptr.size());
+      g.it_off.alloc(std::max<size_t>(1, ioff.size()));
+      g.it_coef.alloc(std::max<size_t>(1, icoef.size()));
+      DS_CUDA(cudaMemcpyAsync(g.it_ptr.p, iptr.data(), iptr.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, st));
+      DS_CUDA(cudaMemcpyAsync(g.it_off.p, ioff.data(), ioff.size() * sizeof(unsigned int),
+                              cudaMemcpyHostToDevice, st));
+      DS_CUDA(cudaMemcpyAsync(g.it_coef.p, icoef.data(), icoef.size() * sizeof(float4),
+                              cudaMemcpyHostToDevice, st));
+      DS_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+      g.res_max_list = mx;
     }
     g.res_pc = pc;
     g.res_cut = g.inner.cut;
-    g.res_max_list = mx;
   }
   const size_t res_bytes = ResLayout::bytes(band, pc->n_per);
   static int per_sm0[3] = {-1, -1, -1};
@@ -1222,9 +1276,9 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
     res_last[bi] = res_bytes;
   }
   const int nsm = op->ctx->num_sms;
-  // the resident lists hold 32-bit offsets into the levels
-  const bool off32 = (double)(g.inner.lmax + 1) * (double)op->n < 4294967295.0;
-  const bool resident = off32 && g.res_max_list <= NL && per_sm1[bi] * nsm >= pc->n_sk;
+  // the item form: 32-bit offsets into the levels, <= GI skewers per block,
+  // n_per dividing the CTA, every block's items in shared memory
+  const bool resident = g.res_max_list <= NI && per_sm1[bi] * nsm >= pc->n_sk;
   const int grid = resident ? pc->n_sk : std::min(per_sm0[bi] * nsm, pc->n_sk);
   if (grid <= 0) return false;
   g.p_part.alloc((size_t)3 * grid + 1);
@@ -1279,6 +1333,9 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.err = g.p_sync.p + 1;
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
   a.pt = g.p_time.p;
+  a.it_ptr = g.it_ptr.p;
+  a.it_off = g.it_off.p;
+  a.it_coef = g.it_coef.p;
   if (!g.ff_b.p) {  // float-pair copies for the update (fixed for the grid's life)
     const size_t np = (size_t)op->pix.n_pad;
     to_ff(g.ff_wl, sv.wl, np, st);

@@ -156,11 +156,15 @@ def test_column_grid_refused_for_other_layouts(ctx):
 
 @pytest.mark.parametrize("form", ["w", "sn"])
 @pytest.mark.parametrize("n_sk,n_per,cluster", [(64, 96, 4), (10, 50, 4), (24, 40, 8),
-                                               (12, 64, 1)])
+                                               (12, 64, 1), (30, 64, 4), (30, 32, 3),
+                                               (16, 128, 2)])
 def test_persistent_solve_matches_graph(ctx, form, n_sk, n_per, cluster):
     """The structured mixed solve with the cluster preconditioner as one
     cooperative launch (ds_operator_set_iteration_form AUTO) against the same
-    recurrence as a replayed graph of per-phase kernels (GRAPH): both stop on
+    recurrence as a replayed graph of per-phase kernels (GRAPH) -- the
+    resident form where the pixels per skewer divide the CTA and clusters
+    have at most 4 skewers (ragged last clusters included), the general form
+    otherwise: both stop on
     the FP64 true residual <= tol |b|, their solutions agree with the oracle's
     to 1e-6, their iteration counts to rounding, and the persistent solve's
     launches do not grow with its iterations."""
