@@ -49,8 +49,9 @@ struct SkewerGrid {
   const void* res_pc = nullptr;
   double res_cut = 0.0;
   int res_max_list = 0;  // the most items of a block (above the limit: not built)
-  DevBuf<int> it_ptr;            // per block: its items
-  DevBuf<unsigned int> it_off;   // item: offset of its (neighbour, level) row in the levels
+  DevBuf<int> it_cnt;            // per block: its items (n_blocks + 1: the largest)
+  DevBuf<unsigned int> it_off;   // item (slots of 512 per block): offset of its
+                                 // (neighbour, level) row in the levels
   DevBuf<float4> it_coef;        // item: the factor for each of the block's skewers
 };
 

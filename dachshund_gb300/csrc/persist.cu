@@ -86,10 +86,11 @@ struct PersistArgs {
   int* err;
   long long limit;
   unsigned long long* pt;  // phase timers (PT_* layout)
-  // the resident form's product items per block (it_ptr: n_blocks + 1; an
-  // item is one (neighbour skewer, level) row: its offset into the levels and
-  // the factor for each of the block's (<= 4) skewers, 0 where unused)
-  const int* it_ptr;
+  // the resident form's product items, NI slots per block (it_cnt: the
+  // count of each block; an item is one (neighbour skewer, level) row: its
+  // offset into the levels and the factor for each of the block's (<= 4)
+  // skewers, 0 where unused)
+  const int* it_cnt;
   const unsigned int* it_off;
   const float4* it_coef;
   // float-pair copies for the resident form's update (record order; the
@@ -837,7 +838,8 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   }
   if (tid < MAX_G) sk[tid] = tid < a.g ? skewer_of(a, blk, tid) : -1;
   {  // the block's product items
-    const int i0 = a.it_ptr[blk], ni = a.it_ptr[blk + 1] - i0;
+    const size_t i0 = (size_t)blk * NI;
+    const int ni = a.it_cnt[blk];
     if (tid == 0) *s_nit = ni;
     for (int e = tid; e < ni; e += NT) {
       ioff[e] = a.it_off[i0 + e];
@@ -1141,6 +1143,116 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   }
 }
 
+// Product items of one block per CTA (NT threads): the entries of its
+// skewers' FP32 lists (at most NE_ITEMS) as (offset of the (neighbour,
+// level) row, skewer j, factor), sorted by offset (bitonic, in shared
+// memory), equal offsets merged into one item with a factor per skewer.
+// cnt[blk] = the block's items; cnt[n_blocks] = the largest count over the
+// blocks, or NI + 1 when a block has too many entries or items.
+constexpr int NE_ITEMS = 1024;
+__global__ void __launch_bounds__(NT) k_build_items(int g, int n_per, int n,
+                                                    const int* __restrict__ bsk,
+                                                    const int* __restrict__ ptr,
+                                                    const int* __restrict__ idx,
+                                                    const int* __restrict__ lev,
+                                                    const float* __restrict__ p32,
+                                                    int* __restrict__ cnt,
+                                                    unsigned int* __restrict__ ioff,
+                                                    float4* __restrict__ icoef) {
+  __shared__ unsigned int key[NE_ITEMS];
+  __shared__ unsigned int val[NE_ITEMS];  // j << 28 | entry index within the block
+  __shared__ int base[GI + 1], sk[GI];
+  __shared__ int scan[NE_ITEMS];
+  const int blk = blockIdx.x, tid = threadIdx.x;
+  if (tid == 0) {
+    int c = 0;
+    for (int j = 0; j < GI; ++j) {
+      base[j] = c;
+      const int s = j < g ? (bsk ? bsk[(size_t)blk * g + j] : (j == 0 ? blk : -1)) : -1;
+      sk[j] = s;
+      if (s >= 0) c += ptr[s + 1] - ptr[s];
+    }
+    base[GI] = c;
+  }
+  __syncthreads();
+  const int total = base[GI];
+  if (total > NE_ITEMS) {
+    if (tid == 0) {
+      cnt[blk] = 0;
+      atomicMax(cnt + gridDim.x, NI + 1);
+    }
+    return;
+  }
+  for (int i = tid; i < NE_ITEMS; i += NT) {
+    unsigned int k = 0xffffffffu, v = 0;
+    if (i < total) {
+      int j = 0;
+      while (j + 1 < GI && i >= base[j + 1]) ++j;
+      const int q = ptr[sk[j]] + (i - base[j]);
+      k = (unsigned int)((size_t)(lev[q] - 1) * n + (size_t)idx[q] * n_per);
+      v = ((unsigned int)j << 28) | (unsigned int)q;
+    }
+    key[i] = k;
+    val[i] = v;
+  }
+  __syncthreads();
+  // bitonic sort of (key, val) by key, ascending (keys are unique per skewer,
+  // so equal keys differ in j: ties ordered by val for a fixed order)
+  for (int size = 2; size <= NE_ITEMS; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = tid; i < NE_ITEMS / 2; i += NT) {
+        const int lo = 2 * i - (i & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const unsigned int ka = key[lo], kb = key[hi], va = val[lo], vb = val[hi];
+        const bool gt = ka > kb || (ka == kb && va > vb);
+        if (gt == up) {
+          key[lo] = kb;
+          key[hi] = ka;
+          val[lo] = vb;
+          val[hi] = va;
+        }
+      }
+      __syncthreads();
+    }
+  // item index of each entry: the count of distinct keys before it
+  for (int i = tid; i < NE_ITEMS; i += NT)
+    scan[i] = (i < total && (i == 0 || key[i] != key[i - 1])) ? 1 : 0;
+  __syncthreads();
+  for (int off = 1; off < NE_ITEMS; off <<= 1) {  // inclusive scan (Hillis-Steele)
+    int v[NE_ITEMS / NT];
+    for (int t = 0; t < NE_ITEMS / NT; ++t) {
+      const int i = tid + t * NT;
+      v[t] = scan[i] + (i >= off ? scan[i - off] : 0);
+    }
+    __syncthreads();
+    for (int t = 0; t < NE_ITEMS / NT; ++t) scan[tid + t * NT] = v[t];
+    __syncthreads();
+  }
+  const int n_items = total > 0 ? scan[total - 1] : 0;
+  if (n_items > NI) {
+    if (tid == 0) {
+      cnt[blk] = 0;
+      atomicMax(cnt + gridDim.x, NI + 1);
+    }
+    return;
+  }
+  const size_t o = (size_t)blk * NI;
+  for (int e = tid; e < n_items; e += NT) icoef[o + e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncthreads();
+  for (int i = tid; i < total; i += NT) {
+    const int it = scan[i] - 1;
+    const int j = (int)(val[i] >> 28);
+    const int q = (int)(val[i] & 0x0fffffffu);
+    if (i == 0 || key[i] != key[i - 1]) ioff[o + it] = key[i];
+    reinterpret_cast<float*>(icoef + o + it)[j] = p32[q];
+  }
+  if (tid == 0) {
+    cnt[blk] = n_items;
+    atomicMax(cnt + gridDim.x, n_items);
+  }
+}
+
 // out = in as float pairs.
 __global__ void k_to_ff(size_t n, const double* __restrict__ in, float2* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -1197,69 +1309,26 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   };
   // The resident form when every block gets its own resident CTA and the
   // longest FP32 neighbour list of a block fits in shared memory.
-  // The resident form's product items, built once per preconditioner and
-  // inner cutoff: per block, the distinct (neighbour, level) rows its
-  // skewers' FP32 lists name, ordered by offset, with each skewer's factor.
+  // The resident form's product items, built on the device once per
+  // preconditioner and inner cutoff (k_build_items): per block, the distinct
+  // (neighbour, level) rows its skewers' FP32 lists name, ordered by offset,
+  // with each skewer's factor, in slots of NI per block.
   const bool off32 = (double)(g.inner.lmax + 1) * (double)op->n < 4294967295.0;
   if (g.res_pc != pc || g.res_cut != g.inner.cut) {
-    g.res_max_list = NI + 1;  // unusable until built
-    if (off32 && pc->g <= GI && NT % g.n_per == 0) {
-      const size_t ne = g.inner.idx.n;
-      std::vector<int> ptr(g.n_sk + 1), bsk(pc->bsk.n), idx(ne), lev(ne);
-      std::vector<float> pv(ne);
-      DS_CUDA(cudaMemcpyAsync(ptr.data(), g.inner.ptr.p, ptr.size() * sizeof(int),
-                              cudaMemcpyDeviceToHost, st));
-      DS_CUDA(cudaMemcpyAsync(idx.data(), g.inner.idx.p, ne * sizeof(int),
-                              cudaMemcpyDeviceToHost, st));
-      DS_CUDA(cudaMemcpyAsync(lev.data(), g.inner.lev.p, ne * sizeof(int),
-                              cudaMemcpyDeviceToHost, st));
-      DS_CUDA(cudaMemcpyAsync(pv.data(), g.inner.p32.p, ne * sizeof(float),
-                              cudaMemcpyDeviceToHost, st));
-      if (pc->bsk.p)
-        DS_CUDA(cudaMemcpyAsync(bsk.data(), pc->bsk.p, bsk.size() * sizeof(int),
-                                cudaMemcpyDeviceToHost, st));
-      DS_CUDA(cudaStreamSynchronize(st));
-      std::vector<int> iptr(pc->n_sk + 1, 0);
-      std::vector<unsigned int> ioff;
-      std::vector<float4> icoef;
-      std::vector<std::pair<unsigned int, std::pair<int, float>>> ent;  // (offset, (skewer j, factor))
+    g.res_max_list = NI + 1;  // unusable unless built
+    if (off32 && pc->g <= GI && NT % g.n_per == 0 && g.inner.idx.n < (1u << 28)) {
+      g.it_cnt.alloc(pc->n_sk + 1);  // last: the largest count (or an overflow mark)
+      g.it_off.alloc((size_t)pc->n_sk * NI);
+      g.it_coef.alloc((size_t)pc->n_sk * NI);
+      DS_CUDA(cudaMemsetAsync(g.it_cnt.p, 0, g.it_cnt.bytes(), st));
+      k_build_items<<<pc->n_sk, NT, 0, st>>>(pc->g, g.n_per, op->n, pc->bsk.p, g.inner.ptr.p,
+                                             g.inner.idx.p, g.inner.lev.p, g.inner.p32.p,
+                                             g.it_cnt.p, g.it_off.p, g.it_coef.p);
+      DS_CHECK_LAUNCH();
       int mx = 0;
-      for (int b = 0; b < pc->n_sk; ++b) {
-        ent.clear();
-        for (int j = 0; j < pc->g; ++j) {
-          const int sj = pc->bsk.p ? bsk[(size_t)b * pc->g + j] : (j == 0 ? b : -1);
-          if (sj < 0) continue;
-          for (int q = ptr[sj]; q < ptr[sj + 1]; ++q)
-            ent.push_back({(unsigned int)((size_t)(lev[q] - 1) * op->n + (size_t)idx[q] * g.n_per),
-                           {j, pv[q]}});
-        }
-        std::sort(ent.begin(), ent.end(),
-                  [](const auto& x, const auto& y) {
-                    return x.first < y.first || (x.first == y.first && x.second.first < y.second.first);
-                  });
-        int nb = 0;
-        for (size_t e = 0; e < ent.size(); ++e) {
-          if (e == 0 || ent[e].first != ent[e - 1].first) {
-            ioff.push_back(ent[e].first);
-            icoef.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
-            ++nb;
-          }
-          float* c = &icoef.back().x;
-          c[ent[e].second.first] = ent[e].second.second;
-        }
-        iptr[b + 1] = iptr[b] + nb;
-        mx = std::max(mx, nb);
-      }
-      g.it_ptr.alloc(iptr.size());
-      g.it_off.alloc(std::max<size_t>(1, ioff.size()));
-      g.it_coef.alloc(std::max<size_t>(1, icoef.size()));
-      DS_CUDA(cudaMemcpyAsync(g.it_ptr.p, iptr.data(), iptr.size() * sizeof(int),
-                              cudaMemcpyHostToDevice, st));
-      DS_CUDA(cudaMemcpyAsync(g.it_off.p, ioff.data(), ioff.size() * sizeof(unsigned int),
-                              cudaMemcpyHostToDevice, st));
-      DS_CUDA(cudaMemcpyAsync(g.it_coef.p, icoef.data(), icoef.size() * sizeof(float4),
-                              cudaMemcpyHostToDevice, st));
-      DS_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+      DS_CUDA(cudaMemcpyAsync(&mx, g.it_cnt.p + pc->n_sk, sizeof(int), cudaMemcpyDeviceToHost,
+                              st));
+      DS_CUDA(cudaStreamSynchronize(st));
       g.res_max_list = mx;
     }
     g.res_pc = pc;
@@ -1333,7 +1402,7 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.err = g.p_sync.p + 1;
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
   a.pt = g.p_time.p;
-  a.it_ptr = g.it_ptr.p;
+  a.it_cnt = g.it_cnt.p;
   a.it_off = g.it_off.p;
   a.it_coef = g.it_coef.p;
   if (!g.ff_b.p) {  // float-pair copies for the update (fixed for the grid's life)
