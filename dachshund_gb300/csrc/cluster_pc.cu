@@ -202,6 +202,20 @@ void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>&
     std::copy(clusters[c].begin(), clusters[c].end(), bsk.begin() + (size_t)c * g);
   const int B = g * n_per;
   crec.assign((size_t)n_blocks * B, -1);
+  // every skewer on the z values of skewer 0, in increasing order (the usual
+  // layout): a cluster's order by z, then by rank, is pixel-major
+  bool shared = true;
+  for (int k = 1; k < n_per && shared; ++k) shared = rz[k - 1] < rz[k];
+  for (size_t r = n_per; r < rz.size() && shared; ++r) shared = rz[r] == rz[r % n_per];
+  if (shared) {
+    for (int c = 0; c < n_blocks; ++c) {
+      const std::vector<int>& cl = clusters[c];
+      int* out = crec.data() + (size_t)c * B;
+      for (int k = 0; k < n_per; ++k)
+        for (size_t j = 0; j < cl.size(); ++j) *out++ = cl[j] * n_per + k;
+    }
+    return;
+  }
   std::vector<int> recs;
   for (int c = 0; c < n_blocks; ++c) {
     recs.clear();

@@ -122,7 +122,8 @@ struct OpF32 {
   double inner_cut = 0.0;
   int formula = F32_EXPANDED;
   F32Points pts;
-  PairList pairs;
+  PairList pairs;                   // at inner_cut (built on first use: ensure_f32_pairs)
+  bool pairs_built = false;
   DevBuf<float> rowf, colw, ediag, pdiag;
   DevBuf<float> p, q, r, z;         // FP32 iteration vectors (sorted, padded)
   DevBuf<float> r2;                 // second r buffer of the band preconditioner

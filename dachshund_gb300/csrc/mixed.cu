@@ -536,10 +536,6 @@ void ensure_op_f32(ds_operator* op, double inner_cut) {
   build_f32_points(f->pts, op->pix, sp, sp, sq, st);
   // 2^|xi|^2 must stay well inside FP32 range for the EXPANDED formula.
   f->formula = f->pts.max_a <= 60.0 ? F32_EXPANDED : F32_DIRECT;
-  KernelConsts kc = op->kc;
-  kc.cull_arg = inner_cut * (1.0 + 1e-9);
-  build_pair_list(f->pairs, op->pix, op->pix, kc, st);
-  build_slice_items(f->pairs, st);
   const int np = op->pix.n_pad;
   f->rowf.alloc(np);
   f->colw.alloc(np);
@@ -558,6 +554,18 @@ void ensure_op_f32(ds_operator* op, double inner_cut) {
   if (f->use_ff) build_ff_points(f->ffd, op->pix, op->kc, st);
   DS_CUDA(cudaStreamSynchronize(st));
   op->f32 = std::move(f);
+}
+
+// The FP32 pair kernels' tile-pair list at the inner cutoff, built on the
+// first solve that runs them (the structured inner product needs none).
+void ensure_f32_pairs(ds_operator* op) {
+  OpF32& f = *op->f32;
+  if (f.pairs_built) return;
+  KernelConsts kc = op->kc;
+  kc.cull_arg = f.inner_cut * (1.0 + 1e-9);
+  build_pair_list(f.pairs, op->pix, op->pix, kc, op->ctx->stream);
+  build_slice_items(f.pairs, op->ctx->stream);
+  f.pairs_built = true;
 }
 
 F32Args op_f32_args(ds_operator* op, const float* v, float* out) {
@@ -623,6 +631,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   // order in use; x is converted in at the start and out at the end.
   const bool use_sg = op->sgrid && (op->inner_variant == INNER_AUTO ||
                                     op->inner_variant == INNER_STRUCTURED);
+  if (!use_sg) ensure_f32_pairs(op);
   SkewerVecs sv{};
   double* X = op->x.p;
   const double* B = op->b.p;

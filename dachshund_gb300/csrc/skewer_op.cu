@@ -837,7 +837,6 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
   for (int q = 0; q < Q; ++q) th[q] = kc.c_para * cls_d[q] * cls_d[q];
   build_lists(mc.ncol, mc.cx.p, mc.cy.p, g.n_sk, g.sx.p, g.sy.p, kc, cut, th, mc.ptr, mc.idx,
               mc.lev, mc.p64, nullptr, st);
-  const int n_sk = g.n_sk;
   mc.Q = Q;
   mc.W = W;
   mc.cut = cut;
@@ -845,8 +844,8 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
   mc.kstart.alloc(nz);
   mc.cls.alloc(cls.size());
   mc.taps.alloc(Q);
-  mc.R.alloc((size_t)Q * n_sk * nz);
-  // the fused form's sorted lists and float-pair taps
+  // the fused form's sorted lists and float-pair taps (R, the FP64 form's
+  // class sums, is allocated when that form runs)
   mc.fidx.alloc(mc.idx.n);
   mc.flev.alloc(mc.idx.n);
   mc.fp.alloc(mc.idx.n);
@@ -911,6 +910,7 @@ bool skewer_map_product(ds_map* map, ds_operator* op, const double* x_dev, doubl
       DS_CHECK_LAUNCH();
     }
   } else {
+    mc.R.alloc((size_t)mc.Q * g.n_sk * mc.nz);
     k_mc_levels<<<dim3(g.n_sk, (mc.nz + 127) / 128), 128, 0, st>>>(
         g.n_sk, g.n_per, mc.nz, mc.W, mc.Q, mc.kstart.p, mc.cls.p, mc.taps.p, x_dev, mc.R.p);
     DS_CHECK_LAUNCH();

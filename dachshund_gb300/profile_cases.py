@@ -14,9 +14,9 @@ leaves the GPU's clocks as they are):
   chosen_step    one step of the benchmark's chosen form on the 262,144-pixel
                  system, after one untimed warm-up step: cluster
                  preconditioner and skewer grid installed, the mixed solve
-                 (k_sg32_levels + k_sg32_apply, k_pc_iter, k_mx_dir, and
-                 k_sg_levels + k_sg_apply for the FP64 residuals) and the
-                 80 x 80 x 512 structured FP64 map (k_mc_levels + k_mc_apply)
+                 (the start kernels, then one persistent launch of
+                 k_mixed_resident) and the 80 x 80 x 512 structured map
+                 (k_mc_split + k_mc_fused)
   tc_matvec      one batched FP32 product of 64 chunks x 64 RHS with the
                  tensor-core variant (k_pack_panels + k_batch_mv_tc)
   tc_inner       one mixed-precision solve of the 262,144-pixel system with
