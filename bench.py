@@ -831,8 +831,9 @@ def run_ours(args, rank, world, local):
     # and reads them back once (2 x 4 (lmax + 1) per pixel), every FP64 update
     # does the same for the float-pair levels of x (2 x 8 (lmax64 + 1)) and
     # reads wl wr e b as float pairs (32) and the outer lists (16 per entry),
-    # and the end writes x (8).  The neighbours re-read the levels from L2
-    # (terms x 4 bytes per iteration): that traffic, not HBM, bounds it.
+    # and the end writes x (8).  The clusters re-read the neighbours' levels
+    # from L2 every iteration (each distinct (neighbour, level) row of a
+    # cluster once): that traffic and the barriers, not HBM, bound it.
     c_para = 1.0 / (2 * w.l_para ** 2)
     lmax64 = 0
     while lmax64 + 1 < w.pix_per_skewer and \
@@ -848,7 +849,10 @@ def run_ours(args, rank, world, local):
     persist_us = (phases["kernel_ms"] / phases["launches"] * 1e3) \
         if phases and phases["launches"] else None
     persist_gbs = persist_bytes / (persist_us * 1e-6) / 1e9 if persist_us else None
-    l2_reads = n_it * terms_per_product * 4
+    # the neighbours' level values one product loads from L2: each distinct
+    # (neighbour, level) row of a cluster once (the resident form's items)
+    loads = (phases or {}).get("product_loads") or terms_per_product
+    l2_reads = n_it * loads * 4
     roofline = {
         "kernel": "persistent structured mixed solve (k_mixed_resident<16>), the dominant "
                   "kernel of the chosen form's step",
@@ -865,6 +869,8 @@ def run_ours(args, rank, world, local):
         "traffic": K_PERSIST_DRAM_BYTES,
         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
         "l2_neighbour_reads_per_launch": l2_reads,
+        "neighbour_values_per_product": loads,
+        "skewer_pair_terms_per_product": terms_per_product,
         "l2_neighbour_read_GBps": l2_reads / (persist_us * 1e-6) / 1e9 if persist_us else None,
     }
 

@@ -276,12 +276,14 @@ class _WFVector:
         """Phase timers of the persistent solve launches since the last reset
         (device %globaltimer): launches, kernel_ms, ctas, barrier_us (one
         empty grid barrier) and, per phase (levels0, product, step,
-        levels64, update), us_per_visit, cta_mean_us, cta_max_us, visits.
-        None before the first persistent launch."""
-        out = (C.c_double * 24)()
+        levels64, update), us_per_visit, cta_mean_us, cta_max_us, visits;
+        product_loads / product_rows: the neighbour values / distinct rows
+        one product loads (resident form; 0 for the general form).  None
+        before the first persistent launch."""
+        out = (C.c_double * 26)()
         m = C.c_int(0)
         self.ctx.check(self._lib.ds_operator_get_persistent_profile(
-            self.handle, out, 24, int(bool(reset)), C.byref(m)),
+            self.handle, out, 26, int(bool(reset)), C.byref(m)),
             "ds_operator_get_persistent_profile")
         if m.value == 0:
             return None
@@ -291,6 +293,8 @@ class _WFVector:
             o = v[4 + 4 * c: 8 + 4 * c]
             prof[name] = {"us_per_visit": o[0], "cta_mean_us": o[1], "cta_max_us": o[2],
                           "visits": int(o[3])}
+        prof["product_loads"] = int(v[24])  # neighbour values loaded per product
+        prof["product_rows"] = int(v[25])
         return prof
 
     def set_cluster_preconditioner(self, n_skewers: int, n_per: int, cluster: int = 4,

@@ -126,7 +126,7 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
                           double* X, float* r, int max_iter, cudaStream_t st);
 int persistent_error(ds_operator* op, cudaStream_t st);
 // The persistent launches' phase timers (ds_operator_get_persistent_profile):
-// writes min(n, 24) values, returns that count (0: no launch yet).
+// writes min(n, 26) values, returns that count (0: no launch yet).
 int persistent_profile(ds_operator* op, double* out, int n, bool reset);
 
 // m = S_mp x (caller order, device) with the structured FP64 map; false when

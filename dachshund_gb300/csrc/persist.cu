@@ -1447,8 +1447,20 @@ int persistent_profile(ds_operator* op, double* out, int n, bool reset) {
                           cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
   if (reset) DS_CUDA(cudaMemsetAsync(g.p_time.p, 0, g.p_time.bytes(), st));
-  std::vector<double> r(4 + 4 * 5, 0.0);
+  std::vector<double> r(4 + 4 * 5 + 2, 0.0);
   const int grid = (int)v[PT_GRID];
+  // the resident form's product: neighbour values loaded per product
+  // (items x n_per); 0 for the general form
+  if (g.it_cnt.p && g.res_max_list <= NI && g.res_pc == op->pc.get()) {
+    std::vector<int> cnt(g.it_cnt.n);
+    DS_CUDA(cudaMemcpyAsync(cnt.data(), g.it_cnt.p, cnt.size() * sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+    long long items = 0;
+    for (size_t b = 0; b + 1 < cnt.size(); ++b) items += cnt[b];
+    r[24] = (double)items * g.n_per;
+    r[25] = (double)items;
+  }
   r[0] = (double)v[PT_LAUNCHES];
   r[1] = v[PT_KERNEL] * 1e-6;  // ms
   r[2] = grid;

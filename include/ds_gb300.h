@@ -257,9 +257,12 @@ int ds_operator_set_iteration_form(ds_operator* op, int form);
  * levels of an update, 5 the update's residual and preconditioner) four
  * values at out[4 + 4 (c - 1)]: us per visit (exit of the previous barrier
  * to exit of this one, CTA 0), the CTAs' mean work per visit (us, to their
- * arrival), the slowest CTA's work per visit (us) and the visits.  Writes
- * min(n, 24) values; *written (may be null) gets that count, 0 before the
- * first persistent launch.  reset != 0 clears the timers after reading. */
+ * arrival), the slowest CTA's work per visit (us) and the visits; out[24]
+ * the neighbour values one product loads (resident form: each distinct
+ * (neighbour skewer, level) row a cluster uses, once; 0 for the general
+ * form) and out[25] those rows.  Writes min(n, 26) values; *written (may be
+ * null) gets that count, 0 before the first persistent launch.  reset != 0
+ * clears the timers after reading. */
 int ds_operator_get_persistent_profile(ds_operator* op, double* out, int n, int reset,
                                        int* written);
 

@@ -245,6 +245,9 @@ def test_persistent_profile_counts_phases(ctx):
     for ph in ("product", "step"):
         assert prof[ph]["us_per_visit"] > 0
         assert prof[ph]["cta_max_us"] >= prof[ph]["cta_mean_us"] > 0
+    # the resident form (64 pixels per skewer divide the CTA, clusters of 4):
+    # each distinct (neighbour, level) row of a cluster loaded once
+    assert prof["product_rows"] > 0 and prof["product_loads"] == prof["product_rows"] * n_per
     again = op.persistent_profile()
     assert again["launches"] == 0 and again["product"]["visits"] == 0
     op.close()
