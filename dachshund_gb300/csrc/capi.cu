@@ -410,7 +410,8 @@ int ds_operator_create(ds_context* ctx, int form, int n, const double* records,
                                              op->wl.p, op->wr.p, op->e.p, op->b.p, op->pdiag.p,
                                              op->inv.p);
     DS_CHECK_LAUNCH();
-    build_pair_list(op->pairs, op->pix, op->pix, op->kc, st);
+    // the tile-pair list is built on the first pair-kernel call
+    // (ensure_op_pairs): the structured operator needs none
     DS_CUDA(cudaStreamSynchronize(st));
   });
   if (rc != DS_OK) return rc;
@@ -426,13 +427,15 @@ void ds_operator_destroy(ds_operator* op) {
 
 int ds_operator_get_info(ds_operator* op, ds_operator_info* info) {
   if (!op || !info) return DS_ERR_ARG;
-  info->n = op->n;
-  info->n_pad = op->pix.n_pad;
-  info->tile = TILE;
-  info->n_tiles = op->pix.n_tiles;
-  info->n_tile_pairs = op->pairs.n_pairs;
-  info->evaluated_pairs = op->pairs.n_pairs * (long long)TILE * TILE;
-  return DS_OK;
+  return guarded(op->ctx, [&] {
+    ensure_op_pairs(op);
+    info->n = op->n;
+    info->n_pad = op->pix.n_pad;
+    info->tile = TILE;
+    info->n_tiles = op->pix.n_tiles;
+    info->n_tile_pairs = op->pairs.n_pairs;
+    info->evaluated_pairs = op->pairs.n_pairs * (long long)TILE * TILE;
+  });
 }
 
 int ds_A_product(ds_operator* op, const double* a, double* b) {

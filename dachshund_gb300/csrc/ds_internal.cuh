@@ -346,6 +346,7 @@ struct ds_operator {
   ds::DevBuf<float2> dense_vff;
   ds::DevBuf<double> dense_part, dense_dot;
   ds::DevBuf<unsigned int> dense_cnt;
+  bool pairs_built = false;  // `pairs` (ensure_op_pairs)
   int inner_variant = 0;     // inner matvec of the mixed form (InnerVariant)
   int iter_form = 0;         // DS_ITER_AUTO / DS_ITER_GRAPH
   // skewer-band preconditioner of the mixed form (null: Jacobi)

@@ -57,6 +57,10 @@ void solve_cf_dev(ds_context* ctx, int form, int n, const double* d_rec, const K
 void map_covar_diag_multi(ds_operator* op, int n_map, const double* map_pts,
                           const ds_pcg_params& pp, double* sigma_m, int* iters, int* success);
 
+// The operator's tile-pair list, built on the first pair-kernel call
+// (pcg.cu; op_pair_args calls it).
+void ensure_op_pairs(ds_operator* op);
+
 // Mixed-precision form (mixed.cu).
 void ensure_op_f32(ds_operator* op, double inner_cut);
 void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,

@@ -669,7 +669,15 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   }
   k_r32_init<<<g, VB, 0, st>>>(np, S, xzero, B, f.q.p, op->r.p, op->partial.p);
   DS_CHECK_LAUNCH();
-  PairArgs resid = op_pair_args(op, X, op->r.p);
+  // the structured residual takes only v, out and the skip flag: no pair list
+  auto residual_args = [&](const double* v, double* out) {
+    if (!op->sgrid) return op_pair_args(op, v, out);
+    PairArgs pa{};
+    pa.v = v;
+    pa.out = out;
+    return pa;
+  };
+  PairArgs resid = residual_args(X, op->r.p);
   resid.skip_flag = &S->init_skip;
   auto outer_residual = [&](const PairArgs& pa) {
     if (op->sgrid)
@@ -728,7 +736,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
   prod.alpha_out = &S->alpha;
   prod.den_out = &S->pq;
   prod.skip_flag = &S->done;
-  PairArgs upd = op_pair_args(op, X, op->r.p);
+  PairArgs upd = residual_args(X, op->r.p);
   upd.skip_flag = &S->skip_update;
   if (!f.tc_err.p) {
     f.tc_err.alloc(1);

@@ -391,6 +391,7 @@ void map_covar_diag_multi(ds_operator* op, int n_map, const double* map_pts,
   sig.alloc(R);
   dst.alloc(R);
   dsh.alloc(1);
+  ensure_op_pairs(op);
   MPairArgs pa{};
   pa.rx = op->pix.x.p;
   pa.ry = op->pix.y.p;

@@ -150,7 +150,14 @@ void vec_mul(int n, const double* a, const double* b, double* c, cudaStream_t st
   DS_CHECK_LAUNCH();
 }
 
+void ensure_op_pairs(ds_operator* op) {
+  if (op->pairs_built) return;
+  build_pair_list(op->pairs, op->pix, op->pix, op->kc, op->ctx->stream);
+  op->pairs_built = true;
+}
+
 PairArgs op_pair_args(ds_operator* op, const double* v, double* out) {
+  ensure_op_pairs(op);
   PairArgs a{};
   a.rx = a.cx = op->pix.x.p;
   a.ry = a.cy = op->pix.y.p;
