@@ -1,36 +1,45 @@
 // Persistent form of the structured mixed-precision iteration (no reference
 // counterpart; the recurrence is lib/pcg.h:27-160 with FP32 inner products
-// and FP64-accurate reliable updates, exactly as in mixed.cu).
+// and FP64-accurate reliable updates, as in mixed.cu).
 //
 // The per-kernel iteration (mixed.cu) spends most of its time waiting: each
 // of its kernels moves a few MB of L2-resident data in ~20 us, and the
-// launch ramp, the chains of dependent loads and the single CTA that
-// reduces the partials at the end of each kernel dominate.  Here one
-// cooperative launch runs every iteration.  Each CTA owns whole blocks of the
-// band preconditioner (a cluster of neighbouring skewers, or one skewer) and
-// so every record of those skewers: only the structured product reads other
-// CTAs' data (the neighbour skewers' z-convolution levels).  The CTAs pass
-// through three phases per iteration, separated by grid-wide barriers, and
-// each keeps its own copy of the CG scalars, computed from the same partials
-// in the same order (so all copies agree bit for bit and nothing is
-// broadcast):
-//   A  p = z + beta p and the levels V^(L) of u = wr p, per owned skewer
-//                                                          (barrier: V read)
-//   B  q = A32 p and the partial p.q, per owned skewer     (barrier: alpha)
-//   C  alpha = r.z / p.q; x += alpha p, r -= alpha q; z = G G^T r over each
-//      owned block (in shared memory, no halo: G has no entry between
-//      blocks); partials r.z, |r|^2; then beta and the update test
-//                                                          (barrier: beta)
-// and, when an FP64 update is due, D the FP64 levels of u = wr x (barrier),
-// E r64 = b - A x and F r = r64, z = G G^T r with their partials (one CTA
-// owns both, so no barrier between them; barrier).
+// launch ramp, the chains of dependent loads, the single CTA that reduces
+// the partials at the end of each kernel and the FP64 arithmetic of the
+// iterate and the dot products (GB300 issues FP64 at 1/64 of FP32)
+// dominate.  Here one cooperative launch runs every iteration.  Each CTA
+// owns whole blocks of the band preconditioner (a cluster of neighbouring
+// skewers, or one skewer) and so every record of those skewers: only the
+// structured product reads other CTAs' data (the neighbour skewers'
+// z-convolution levels).  Every CTA keeps its own copy of the CG scalars,
+// computed from the same partials in the same order (so all copies agree bit
+// for bit and nothing is broadcast).
+//
+// Two forms:
+//  * k_mixed_resident (one block per CTA, every CTA resident): the block's
+//    vectors, product items and FP16 factor stay in shared memory; two
+//    phases per iteration (Chronopoulos and Gear's arrangement of the same
+//    recurrence):
+//      product  w = A32 z from the published levels of z (each distinct
+//               (neighbour, level) row of the cluster loaded once), p = z +
+//               beta p, q = w + beta q (= A32 p), the partial p.q   (barrier)
+//      step     alpha; x += alpha p (float pairs), r -= alpha q, z = G G^T r
+//               over the block (no halo: G has no entry between blocks), the
+//               levels of z, the partials r.z, |r|^2; beta and the update
+//               test                                                  (barrier)
+//    and, when a reliable update is due, the float-pair levels of x (barrier)
+//    and b - A x in float pairs, r, z and its levels (barrier).
+//  * k_mixed_persistent (any number of blocks per CTA): the vectors in
+//    global memory, three phases per iteration (p = z + beta p and the
+//    levels of p; q = A32 p; alpha and the step), FP64 iterate.
 // Data written by another CTA during the kernel is read through L2
 // (ld.global.cg), never from a possibly stale L1 line.
 //
 // Every barrier wait is bounded (`limit` SM clock cycles): a CTA that runs
 // out records the barrier's code, and every CTA leaves at its next barrier;
 // the host reports DS_ERR_TIMEOUT.  The launch is cooperative (all CTAs
-// resident), so a barrier always completes unless a CTA has left.
+// resident), so a barrier always completes unless a CTA has left.  Phase
+// timers (%globaltimer) accumulate per launch for the profile.
 #include <algorithm>
 #include <cmath>
 #include <vector>
