@@ -669,20 +669,34 @@ __global__ void k_mc_sort(int ncol, int Q, const int* __restrict__ ptr,
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncol) return;
   const int q0 = ptr[c], q1 = ptr[c + 1];
+  // counting sort: entries per level, then each entry to its level's next
+  // slot (levels descending, entries in list order within a level)
+  int start[MC_QMAX + 2];
+  for (int L = 0; L <= Q + 1; ++L) start[L] = 0;
+  for (int e = q0; e < q1; ++e) {
+    const int L = lev[e];
+    ++start[(L >= 1 && L <= Q) ? L : 0];
+  }
   int pos = q0;
-  for (int L = Q; L >= 1; --L)
-    for (int e = q0; e < q1; ++e)
-      if (lev[e] == L) {
-        const ff f = ff_from_double(p64[e]);
-        sidx[pos] = idx[e];
-        slev[pos] = L;
-        sp[pos] = make_float2(f.h, f.l);
-        ++pos;
-      }
-  for (; pos < q1; ++pos) {  // no class kept: contributes nothing
-    sidx[pos] = 0;
-    slev[pos] = 0;
-    sp[pos] = make_float2(0.f, 0.f);
+  for (int L = Q; L >= 0; --L) {  // level 0 (no class kept) last
+    const int cnt = start[L];
+    start[L] = pos;
+    pos += cnt;
+  }
+  for (int e = q0; e < q1; ++e) {
+    int L = lev[e];
+    if (L < 1 || L > Q) L = 0;
+    const int at = start[L]++;
+    if (L == 0) {  // contributes nothing
+      sidx[at] = 0;
+      slev[at] = 0;
+      sp[at] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const ff f = ff_from_double(p64[e]);
+    sidx[at] = idx[e];
+    slev[at] = L;
+    sp[at] = make_float2(f.h, f.l);
   }
 }
 
