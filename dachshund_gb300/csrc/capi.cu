@@ -39,6 +39,13 @@ void stream_register(cudaStream_t s, bool alive) {
     live_streams().erase(s);
 }
 
+void ensure_map_points(ds_map* map) {
+  if (map->pts_built) return;
+  build_point_set(map->pts, map->raw.p, map->n, 3, 1.0, 1.0, 1.0, map->ctx->stream,
+                  ORDER_MORTON);
+  map->pts_built = true;
+}
+
 }  // namespace ds
 
 using namespace ds;
@@ -197,6 +204,7 @@ int op_host_call(ds_operator* op, int epi, const double* in, double* out) {
 }
 
 void ensure_map_pairs(ds_map* map, ds_operator* op) {
+  ensure_map_points(map);
   if (map->op_serial == op->serial) return;
   build_pair_list(map->pairs, map->pts, op->pix, op->kc, map->ctx->stream);
   map->op_serial = op->serial;
@@ -606,9 +614,12 @@ int ds_map_create(ds_context* ctx, int n_map, const double* map_points, ds_map**
     require(n_map > 0 && map_points, "bad map points");
     cudaStream_t st = ctx->stream;
     map->ctx = ctx;
-    DevBuf<double> pts;
-    upload(map_points, (size_t)n_map * 3, pts, st);
-    build_point_set(map->pts, pts.p, n_map, 3, 1.0, 1.0, 1.0, st, ORDER_MORTON);
+    map->n = n_map;
+    // the points as given; the tiled copy is built by the first call that
+    // needs it (a column-grid map against a skewer grid never does)
+    upload(map_points, (size_t)n_map * 3, map->raw, st);
+    double lo[3], hi[3];
+    point_bbox(map->raw.p, n_map, 3, lo, hi, st);  // checks the coordinates
   });
   if (rc != DS_OK) return rc;
   *out = map.release();
@@ -633,9 +644,9 @@ int ds_map_product(ds_map* map, ds_operator* op, const double* x, double* m) {
     require(map->ctx == op->ctx, "map and operator belong to different contexts");
     cudaStream_t st = map->ctx->stream;
     upload(x, op->n, op->io_a, st);
-    map->out_dev.alloc(map->pts.n);
+    map->out_dev.alloc(map->n);
     map_product_dev(map, op, op->io_a.p, map->out_dev.p);
-    DS_CUDA(cudaMemcpyAsync(m, map->out_dev.p, map->pts.n * sizeof(double),
+    DS_CUDA(cudaMemcpyAsync(m, map->out_dev.p, map->n * sizeof(double),
                             cudaMemcpyDeviceToHost, st));
     DS_CUDA(cudaStreamSynchronize(st));
   });
@@ -658,9 +669,9 @@ int ds_map_product_f32(ds_map* map, ds_operator* op, double cutoff, const double
     require(map->ctx == op->ctx, "map and operator belong to different contexts");
     cudaStream_t st = map->ctx->stream;
     upload(x, op->n, op->io_a, st);
-    map->out_dev.alloc(map->pts.n);
+    map->out_dev.alloc(map->n);
     map_product_f32_dev(map, op, op->io_a.p, map->out_dev.p, cutoff > 0.0 ? cutoff : 30.0);
-    DS_CUDA(cudaMemcpyAsync(m, map->out_dev.p, map->pts.n * sizeof(double),
+    DS_CUDA(cudaMemcpyAsync(m, map->out_dev.p, map->n * sizeof(double),
                             cudaMemcpyDeviceToHost, st));
     DS_CUDA(cudaStreamSynchronize(st));
   });

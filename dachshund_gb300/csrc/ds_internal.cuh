@@ -195,6 +195,10 @@ enum PointOrder { ORDER_MORTON = 0, ORDER_KD = 1 };
 void build_point_set(PointSet& ps, const double* d_rec, int n, int stride,
                      double sx, double sy, double sz, cudaStream_t st,
                      int order = ORDER_KD);
+// Bounding box of n records of `stride` doubles (x, y, z first) in device
+// memory; DS_ERR_ARG for a non-finite coordinate (synchronises st).
+void point_bbox(const double* d_rec, int n, int stride, double lo[3], double hi[3],
+                cudaStream_t st);
 
 // Culled tile-pair list (CSR over row tiles).
 struct PairList {
@@ -357,7 +361,10 @@ struct ds_operator {
 
 struct ds_map {
   ds_context* ctx = nullptr;
-  ds::PointSet pts;
+  int n = 0;                  // map points
+  ds::DevBuf<double> raw;     // the points as given (x, y, z each), caller order
+  ds::PointSet pts;           // tiled copy, built on first use (ensure_map_points)
+  bool pts_built = false;
   // pair list cache for the last operator used
   unsigned long long op_serial = 0;
   ds::KernelConsts kc{};

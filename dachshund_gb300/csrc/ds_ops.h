@@ -61,6 +61,10 @@ void map_covar_diag_multi(ds_operator* op, int n_map, const double* map_pts,
 // (pcg.cu; op_pair_args calls it).
 void ensure_op_pairs(ds_operator* op);
 
+// The map's tiled point set, built on the first call that needs it (the
+// structured column-grid map reads the points as given).
+void ensure_map_points(ds_map* map);
+
 // Mixed-precision form (mixed.cu).
 void ensure_op_f32(ds_operator* op, double inner_cut);
 void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,

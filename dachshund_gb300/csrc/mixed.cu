@@ -908,6 +908,7 @@ void run_mixed(ds_operator* op, const ds_mixed_params& mp, ds_pcg_result& res,
 }
 
 void ensure_map_f32(ds_map* map, ds_operator* op, double cut) {
+  ensure_map_points(map);
   if (map->f32 && map->f32->op_serial == op->serial && map->f32->cut == cut) return;
   cudaStream_t st = map->ctx->stream;
   std::unique_ptr<MapF32, MapF32Deleter> f(new MapF32());

@@ -265,36 +265,31 @@ __global__ void k_sg32_apply(int n_per, size_t n, const int* __restrict__ nb_ptr
 // ---- structured map --------------------------------------------------------------
 constexpr int MC_QMAX = 32;  // distance classes at most
 
-// Column (x, y) and the Z_j of a map declared a column grid, from its sorted
-// point set (perm: sorted position -> caller index c nz + j).
-__global__ void k_mc_info(int n_pad, int nz, const int* __restrict__ perm,
-                          const double* __restrict__ px, const double* __restrict__ py,
-                          const double* __restrict__ pz, double* __restrict__ cx,
-                          double* __restrict__ cy, double* __restrict__ zj) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_pad) return;
-  const int p = perm[i];
-  if (p < 0) return;
+// Column (x, y) and the Z_j of a map declared a column grid, from its points
+// as given (x, y, z of point c nz + j at 3 (c nz + j)).
+__global__ void k_mc_info(int n, int nz, const double* __restrict__ pts,
+                          double* __restrict__ cx, double* __restrict__ cy,
+                          double* __restrict__ zj) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
   const int c = p / nz, j = p % nz;
+  const double* q = pts + (size_t)p * 3;
   if (j == 0) {
-    cx[c] = px[i];
-    cy[c] = py[i];
+    cx[c] = q[0];
+    cy[c] = q[1];
   }
-  if (c == 0) zj[j] = pz[i];
+  if (c == 0) zj[j] = q[2];
 }
 
 // Flags a point that is not at its column's (x, y) and its Z_j.
-__global__ void k_mc_check(int n_pad, int nz, const int* __restrict__ perm,
-                           const double* __restrict__ px, const double* __restrict__ py,
-                           const double* __restrict__ pz, const double* __restrict__ cx,
-                           const double* __restrict__ cy, const double* __restrict__ zj,
-                           int* __restrict__ bad) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_pad) return;
-  const int p = perm[i];
-  if (p < 0) return;
+__global__ void k_mc_check(int n, int nz, const double* __restrict__ pts,
+                           const double* __restrict__ cx, const double* __restrict__ cy,
+                           const double* __restrict__ zj, int* __restrict__ bad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
   const int c = p / nz, j = p % nz;
-  if (px[i] != cx[c] || py[i] != cy[c] || pz[i] != zj[j]) atomicOr(bad, 1);
+  const double* q = pts + (size_t)p * 3;
+  if (q[0] != cx[c] || q[1] != cy[c] || q[2] != zj[j]) atomicOr(bad, 1);
 }
 
 // R_b^(q)[j] = sum of T_class x_{b,k} over the window pixels of Z_j whose
@@ -996,7 +991,7 @@ int ds_map_set_column_grid(ds_map* map, int n_columns, int nz) {
       map->cols.reset();
       return;
     }
-    require(n_columns > 0 && nz > 0 && (long long)n_columns * nz == map->pts.n,
+    require(n_columns > 0 && nz > 0 && (long long)n_columns * nz == map->n,
             "n_columns x nz must equal the map's point count");
     cudaStream_t st = map->ctx->stream;
     std::unique_ptr<MapColumns, MapColumnsDeleter> mc(new MapColumns());
@@ -1010,14 +1005,11 @@ int ds_map_set_column_grid(ds_map* map, int n_columns, int nz) {
     zj.alloc(nz);
     bad.alloc(1);
     DS_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
-    const int np = map->pts.n_pad;
-    k_mc_info<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->pts.perm.p, map->pts.x.p,
-                                                 map->pts.y.p, map->pts.z.p, mc->cx.p, mc->cy.p,
-                                                 zj.p);
+    const int np = map->n;
+    k_mc_info<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->raw.p, mc->cx.p, mc->cy.p, zj.p);
     DS_CHECK_LAUNCH();
-    k_mc_check<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->pts.perm.p, map->pts.x.p,
-                                                  map->pts.y.p, map->pts.z.p, mc->cx.p,
-                                                  mc->cy.p, zj.p, bad.p);
+    k_mc_check<<<(np + 255) / 256, 256, 0, st>>>(np, nz, map->raw.p, mc->cx.p, mc->cy.p, zj.p,
+                                                  bad.p);
     DS_CHECK_LAUNCH();
     int hbad = 0;
     DS_CUDA(cudaMemcpyAsync(mc->z.data(), zj.p, nz * sizeof(double), cudaMemcpyDeviceToHost,

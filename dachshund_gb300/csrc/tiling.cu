@@ -494,14 +494,9 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
   }
 }
 
-void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, double sx,
-                     double sy, double sz, cudaStream_t st, int order) {
+void point_bbox(const double* d_rec, int n, int stride, double lo[3], double hi[3],
+                cudaStream_t st) {
   require(n > 0, "point count must be > 0");
-  ps.n = n;
-  ps.n_tiles = (n + TILE - 1) / TILE;
-  ps.n_pad = ps.n_tiles * TILE;
-
-  // Bounding box of all points.
   const int nb = std::min(256, (n + BLK - 1) / BLK);
   DevBuf<double> part;
   part.alloc((size_t)nb * 6);
@@ -511,7 +506,10 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
   DS_CUDA(cudaMemcpyAsync(hp.data(), part.p, hp.size() * sizeof(double),
                           cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
-  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = INFINITY;
+    hi[c] = -INFINITY;
+  }
   for (int b = 0; b < nb; ++b)
     for (int c = 0; c < 3; ++c) {
       lo[c] = std::min(lo[c], hp[b * 6 + c]);
@@ -519,6 +517,18 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
     }
   for (int c = 0; c < 3; ++c)
     require(std::isfinite(lo[c]) && std::isfinite(hi[c]), "non-finite coordinates");
+}
+
+void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, double sx,
+                     double sy, double sz, cudaStream_t st, int order) {
+  require(n > 0, "point count must be > 0");
+  ps.n = n;
+  ps.n_tiles = (n + TILE - 1) / TILE;
+  ps.n_pad = ps.n_tiles * TILE;
+
+  // Bounding box of all points.
+  double lo[3], hi[3];
+  point_bbox(d_rec, n, stride, lo, hi, st);
   const double ext = std::max({(hi[0] - lo[0]) * sx, (hi[1] - lo[1]) * sy,
                                (hi[2] - lo[2]) * sz, 1e-300});
   const double inv_h = 1023.0 / ext;

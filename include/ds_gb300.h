@@ -554,8 +554,10 @@ int ds_operator_skewer_product_dev(ds_operator* op, int residual,
 typedef struct ds_map ds_map;
 
 /* A map grid or point set (init_uniform_map_coords output or any Point
- * array, lib/util.h:16, lib/map.h:41-44), sorted and tiled on the device once
- * and reused by every product with it. */
+ * array, lib/util.h:16, lib/map.h:41-44), copied to the device (DS_ERR_ARG
+ * for a non-finite coordinate); sorted and tiled there by the first product
+ * that needs it (the structured column-grid map does not) and reused by
+ * every product with it. */
 int ds_map_create(ds_context* ctx, int n_map, const double* map_points,
                   ds_map** out);
 void ds_map_destroy(ds_map* map);
