@@ -49,7 +49,7 @@ K_PAIR_F32_DRAM_BYTES = 9_174_528
 K_SG32_DRAM_BYTES = 16_603_136  # k_sg32_levels 4,202,496 + k_sg32_apply 12,400,640
 # DRAM bytes (read + write) of one launch of the persistent solve on the
 # 262,144-pixel workload (profiles/k_mixed_resident_wf262144.md)
-K_PERSIST_DRAM_BYTES = 44_836_608  # read 43,101,184 + write 1,735,424
+K_PERSIST_DRAM_BYTES = 44_619_520  # read 43,064,576 + write 1,554,944
 # the structured inner operator's cutoff (DS_DEFAULT_STRUCTURED_INNER_CUTOFF)
 SG_INNER_CUT = 14.0
 # FP64-pipe instructions per evaluated pair of the plain FP64 kernel

@@ -36,8 +36,7 @@ struct SkewerGrid {
   // record-order copies for the mixed solve (built on first use)
   DevBuf<double> rwl, rwr, re, rb, rx;
   DevBuf<float> rpd;
-  // the persistent solve's CTA partials and barrier words (count, generation,
-  // error code)
+  // the persistent solve's CTA partials and barrier words (count, error code)
   DevBuf<double> p_part;
   DevBuf<int> p_sync;
   DevBuf<unsigned long long> p_time;  // its phase timers
@@ -50,6 +49,7 @@ struct SkewerGrid {
   double res_cut = 0.0;
   int res_max_list = 0;  // the most items of a block (above the limit: not built)
   DevBuf<int> it_cnt;            // per block: its items (n_blocks + 1: the largest)
+  DevBuf<int> it_own;            // per block: its items on its own skewers (the first)
   DevBuf<unsigned int> it_off;   // item (slots of 512 per block): offset of its
                                  // (neighbour, level) row in the levels
   DevBuf<float4> it_coef;        // item: the factor for each of the block's skewers

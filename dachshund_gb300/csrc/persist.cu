@@ -21,8 +21,10 @@
 //    phases per iteration (Chronopoulos and Gear's arrangement of the same
 //    recurrence):
 //      product  w = A32 z from the published levels of z (each distinct
-//               (neighbour, level) row of the cluster loaded once), p = z +
-//               beta p, q = w + beta q (= A32 p), the partial p.q   (barrier)
+//               (neighbour, level) row of the cluster loaded once; the rows
+//               of its own skewers while the previous barrier completes),
+//               p = z + beta p, q = w + beta q (= A32 p), the partial
+//               p.q                                                   (barrier)
 //      step     alpha; x += alpha p (float pairs), r -= alpha q, z = G G^T r
 //               over the block (no halo: G has no entry between blocks), the
 //               levels of z, the partials r.z, |r|^2; beta and the update
@@ -36,8 +38,9 @@
 // (ld.global.cg), never from a possibly stale L1 line.
 //
 // Every barrier wait is bounded (`limit` SM clock cycles): a CTA that runs
-// out records the barrier's code, and every CTA leaves at its next barrier;
-// the host reports DS_ERR_TIMEOUT.  The launch is cooperative (all CTAs
+// out records the barrier's code, and every CTA leaves when it finds the
+// code (in that barrier's wait or the next); the host reports
+// DS_ERR_TIMEOUT.  The launch is cooperative (all CTAs
 // resident), so a barrier always completes unless a CTA has left.  Phase
 // timers (%globaltimer) accumulate per launch for the profile.
 #include <algorithm>
@@ -91,7 +94,7 @@ struct PersistArgs {
   // state and scratch
   MixedState* S_;
   double *hist, *htrue, *part;
-  unsigned int* bar;  // barrier words: count, error code, a flag line per CTA
+  unsigned int* bar;  // barrier words: count, error code
   int* err;
   long long limit;
   unsigned long long* pt;  // phase timers (PT_* layout)
@@ -100,6 +103,7 @@ struct PersistArgs {
   // offset into the levels and the factor for each of the block's (<= 4)
   // skewers, 0 where unused)
   const int* it_cnt;
+  const int* it_own;  // per block: its items on the block's own skewers (the first ones)
   const unsigned int* it_off;
   const float4* it_coef;
   // float-pair copies for the resident form's update (record order; the
@@ -139,61 +143,68 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // Grid-wide barrier (all CTAs resident: cooperative launch).  Every CTA's
 // thread 0 arrives on one monotonic count (atom.acq_rel: it releases the
-// CTA's writes, ordered before it by the CTA barrier); the CTA whose arrival
-// completes the epoch (count == epoch x CTAs) releases the others by writing
-// the epoch into each CTA's own flag line (a fence, then plain stores), and
-// each CTA polls only its own line (ld.acquire).  No line is polled by more
-// than one CTA, so the polls do not queue up on one L2 slice in front of the
-// data, and the epoch is counted locally, so arriving takes one atomic.  A
-// poll that runs out (`limit` SM cycles) records `code`, writes ERR_FLAG into
-// every flag line and returns false, as does a CTA that finds ERR_FLAG.
-// Words: [0] count, [1] error code, [BAR_LINE (1 + c)] flag of CTA c.
-constexpr int BAR_LINE = 32;  // words per 128-byte line
-constexpr unsigned int ERR_FLAG = 0xffffffffu;
-__device__ bool grid_sync(const PersistArgs& a, int code, unsigned int& epoch) {
-  __shared__ int ok_s;
-  __shared__ unsigned long long prev_exit;
+// CTA's writes, ordered before it by the CTA barrier) and polls the same
+// count (ld.acquire) until it reaches epoch x CTAs: reading the last
+// arrival's value synchronises with every arrival (the arrivals form one
+// release sequence), and the CTA whose arrival completes the epoch does not
+// poll at all.  (Measured on GB300 against a broadcast in which that CTA
+// writes the epoch into a flag line per CTA after a fence: 2.90 against
+// 3.07 ms per 262,144-pixel solve; the broadcast adds a fence and a store
+// round trip to every barrier.)  A poll that runs out (`limit` SM cycles)
+// records `code` in the error word and returns false, as does a CTA that
+// finds the error word set (read every 16 polls, and by the last arrival).
+// Words: [0] count, [1] error code.
+// The barrier comes in two halves: between grid_arrive and grid_wait a CTA
+// may work on its own data (writing nothing another CTA reads in the next
+// phase), which hides that work behind the barrier's latency.
+constexpr int BAR_WORDS = 32;  // one 128-byte line
+struct BarState {                  // thread 0's barrier state
+  unsigned int epoch = 0;          // barriers passed
+  unsigned long long exit_ns = 0;  // last exit (%globaltimer)
+  int last = 0;                    // this CTA completed the current epoch
+};
+
+__device__ void grid_arrive(const PersistArgs& a, int code, BarState& b) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (epoch > 0) a.pt[PT_CTA + 8 * blockIdx.x + code] += global_ns() - prev_exit;
-    int ok = 1;
-    ++epoch;
-    const unsigned int target = epoch * gridDim.x;
+    if (b.epoch > 0) a.pt[PT_CTA + 8 * blockIdx.x + code] += global_ns() - b.exit_ns;
+    ++b.epoch;
+    const unsigned int target = b.epoch * gridDim.x;
     unsigned int old;
     asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;"
                  : "=r"(old)
                  : "l"(a.bar)
                  : "memory");
-    auto release_all = [&](unsigned int v) {
-      asm volatile("fence.acq_rel.gpu;" ::: "memory");
-      for (unsigned int c = 0; c < gridDim.x; ++c)
-        asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(a.bar + (size_t)(1 + c) * BAR_LINE),
-                     "r"(v)
-                     : "memory");
-    };
-    if (old + 1 == target) {
-      release_all(*(volatile int*)a.err ? ERR_FLAG : epoch);
-    } else {
-      const unsigned int* flag = a.bar + (size_t)(1 + blockIdx.x) * BAR_LINE;
+    b.last = old + 1 == target;
+  }
+}
+
+__device__ bool grid_wait(const PersistArgs& a, int code, BarState& b) {
+  __shared__ int ok_s;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    if (!b.last) {
+      const unsigned int target = b.epoch * gridDim.x;
       const long long t0 = clock64();
-      for (;;) {
+      for (int k = 0;; ++k) {
         unsigned int f;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(f) : "l"(flag) : "memory");
-        if (f == epoch) break;
-        if (f == ERR_FLAG) {
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(f) : "l"(a.bar) : "memory");
+        if ((int)(f - target) >= 0) break;
+        if ((k & 15) == 15 && *(volatile int*)a.err) {
           ok = 0;
           break;
         }
         if (clock64() - t0 > a.limit) {
           atomicExch(a.err, code);
-          release_all(ERR_FLAG);
           ok = 0;
           break;
         }
       }
+    } else if (*(volatile int*)a.err) {
+      ok = 0;
     }
     const unsigned long long now = global_ns();
-    prev_exit = now;
+    b.exit_ns = now;
     if (blockIdx.x == 0) {
       a.pt[PT_PHASE + code] += now - a.pt[PT_LAST];
       a.pt[PT_LAST] = now;
@@ -203,6 +214,11 @@ __device__ bool grid_sync(const PersistArgs& a, int code, unsigned int& epoch) {
   }
   __syncthreads();
   return ok_s != 0;
+}
+
+__device__ __forceinline__ bool grid_sync(const PersistArgs& a, int code, BarState& b) {
+  grid_arrive(a, code, b);
+  return grid_wait(a, code, b);
 }
 
 // Sum of n partials in a fixed order, valid in every thread of every CTA
@@ -486,7 +502,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
   const int G = gridDim.x;
   const int P2 = (G + 1) & ~1;  // the pair partials start 16-byte aligned
   const size_t ns = (size_t)a.n_blocks * a.S;
-  unsigned int epoch = 0;  // barriers passed (thread 0)
+  BarState bst;  // barrier state (thread 0)
   if (tid == 0) sS = *a.S_;
   if (tid == 0 && blockIdx.x == 0) {
     const unsigned long long now = global_ns();
@@ -496,7 +512,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
     a.pt[PT_LAUNCHES] += 1;
   }
   __syncthreads();
-  for (int k = 0; k < N_CALIB; ++k) grid_sync(a, B_CALIB, epoch);
+  for (int k = 0; k < N_CALIB; ++k) grid_sync(a, B_CALIB, bst);
   // the recurrence sets done by iteration max_iter at the latest (the
   // update it forces there ends the solve); the bound keeps hist in range
   while (!sS.done && sS.iter < a.max_iter) {
@@ -511,7 +527,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
           return (float)a.wr[r] * pv;
         });
     }
-    if (!grid_sync(a, B_LEVELS, epoch)) break;
+    if (!grid_sync(a, B_LEVELS, bst)) break;
     // ---- B: q = A32 p, partial p.q
     double dq = 0.0;
     for (int blk = blockIdx.x; blk < a.n_blocks; blk += G) {
@@ -536,7 +552,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
       const double bs = block_sum<NT>(dq, red);
       if (tid == 0) a.part[blockIdx.x] = bs;
     }
-    if (!grid_sync(a, B_PRODUCT, epoch)) break;
+    if (!grid_sync(a, B_PRODUCT, bst)) break;
     // ---- C: alpha; x, r, z per owned block; partials r.z, |r|^2
     const double pq = partial_total(a.part, G, tot);
     if (tid == 0) tot[0] = sS.rz / pq;
@@ -582,7 +598,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
         a.part[(size_t)P2 + 2 * blockIdx.x + 1] = b2;
       }
     }
-    if (!grid_sync(a, B_STEP, epoch)) break;
+    if (!grid_sync(a, B_STEP, bst)) break;
     {
       const double2 t2 = partial_total2(a.part + P2, G, tot);
       if (tid == 0) step_scalars(sS, a, it, alpha_d, pq, t2.x, t2.y);
@@ -593,7 +609,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
     for (int blk = blockIdx.x; blk < a.n_blocks; blk += G)
       block_levels<double>(a, blk, a.olmax, a.taps64, a.V64, su64,
                            [&](size_t r) { return a.wr[r] * __ldcg(a.x + r); });
-    if (!grid_sync(a, B_LEVELS64, epoch)) break;
+    if (!grid_sync(a, B_LEVELS64, bst)) break;
     // ---- E, F: r64 = b - A x per owned skewer; r = r64, z = G G^T r
     rz = 0.0;
     rr = 0.0;
@@ -647,7 +663,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_persistent(PersistArgs a) {
         a.part[(size_t)P2 + 2 * blockIdx.x + 1] = b2;
       }
     }
-    if (!grid_sync(a, B_UPDATE, epoch)) break;
+    if (!grid_sync(a, B_UPDATE, bst)) break;
     {
       const double2 t2 = partial_total2(a.part + P2, G, tot);
       if (tid == 0) update_scalars(sS, a, t2.x, t2.y);
@@ -836,7 +852,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   const int m = a.g * npr;  // records of the block (record-local index j n_per + k)
   const size_t n = (size_t)a.n;
   const size_t ns = (size_t)a.n_blocks * a.S;
-  unsigned int epoch = 0;  // barriers passed (thread 0)
+  BarState bst;  // barrier state (thread 0)
   if (tid == 0) sS = *a.S_;
   if (tid == 0 && blockIdx.x == 0) {
     const unsigned long long now = global_ns();
@@ -849,7 +865,10 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   {  // the block's product items
     const size_t i0 = (size_t)blk * NI;
     const int ni = a.it_cnt[blk];
-    if (tid == 0) *s_nit = ni;
+    if (tid == 0) {
+      s_nit[0] = ni;
+      s_nit[1] = a.it_own[blk];
+    }
     for (int e = tid; e < ni; e += NT) {
       ioff[e] = a.it_off[i0 + e];
       icoef[e] = a.it_coef[i0 + e];
@@ -939,44 +958,54 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
   // q = w + beta q (= A32 p), so p.q is known at its barrier; the step phase
   // then updates x and r, applies the preconditioner, publishes the levels of
   // the new z and the partials of r.z and |r|^2 at the next barrier.
+  // The product w = A32 z: each (neighbour, level) row the block's skewers
+  // use is loaded once and applied to all of them: thread (part, k) takes
+  // pixel k of a share of the block's items, UFI rows in flight, one
+  // accumulator per skewer (acc).  The rows of the block's own skewers (the
+  // first items) are done between the arrival at the barrier that publishes
+  // the levels and its wait; the others after it.
+  const int tk = NT / npr;  // threads per pixel
+  const int kq = tid % npr, part = tid / npr;
+  float acc[GI];
+  auto product_rows = [&](int e0, int e1) {
+    for (int e = e0; e < e1; e += UFI) {
+      float v[UFI];
+#pragma unroll
+      for (int u = 0; u < UFI; ++u) v[u] = e + u < e1 ? __ldcg(a.V32 + ioff[e + u] + kq) : 0.f;
+#pragma unroll
+      for (int u = 0; u < UFI; ++u)
+        if (e + u < e1) {
+          const float4 c = icoef[e + u];
+          acc[0] = fmaf(c.x, v[u], acc[0]);
+          acc[1] = fmaf(c.y, v[u], acc[1]);
+          acc[2] = fmaf(c.z, v[u], acc[2]);
+          acc[3] = fmaf(c.w, v[u], acc[3]);
+        }
+    }
+  };
+  auto own_rows = [&]() {
+#pragma unroll
+    for (int j = 0; j < GI; ++j) acc[j] = 0.f;
+    const int no = s_nit[1];
+    product_rows(part * no / tk, (part + 1) * no / tk);
+  };
   levels_z();
-  if (grid_sync(a, B_LEVELS, epoch)) {
-    for (int k = 0; k < N_CALIB; ++k) grid_sync(a, B_CALIB, epoch);
+  grid_arrive(a, B_LEVELS, bst);
+  own_rows();
+  if (grid_wait(a, B_LEVELS, bst)) {
+    for (int k = 0; k < N_CALIB; ++k) grid_sync(a, B_CALIB, bst);
   }
   while (!sS.done && sS.iter < a.max_iter) {
       const int it = sS.iter + 1;
-      // ---- product: w = A32 z, p = z + beta p, q = w + beta q, partial p.q.
-      // Each (neighbour, level) row the block's skewers use is loaded once
-      // and applied to all of them: thread (part, k) takes pixel k of a
-      // share of the block's items, UFI rows in flight, one accumulator per
-      // skewer; the NT / n_per shares of a pixel are summed in order through
-      // shared memory (us, free in this phase).
+      // ---- product: w = A32 z, p = z + beta p, q = w + beta q, partial p.q;
+      // the NT / n_per shares of a pixel are summed in order through shared
+      // memory (us, free in this phase).
       ff dq{0.f, 0.f};
       {
         if (tid == 0) s_ab = (float)sS.beta;
         float* red_w = reinterpret_cast<float*>(us);  // (NT / n_per) x GI x n_per
-        const int tk = NT / npr;  // threads per pixel
-        const int kq = tid % npr, part = tid / npr;
-        const int ni = *s_nit;
-        const int e0 = part * ni / tk, e1 = (part + 1) * ni / tk;
-        float acc[GI];
-#pragma unroll
-        for (int j = 0; j < GI; ++j) acc[j] = 0.f;
-        for (int e = e0; e < e1; e += UFI) {
-          float v[UFI];
-#pragma unroll
-          for (int u = 0; u < UFI; ++u)
-            v[u] = e + u < e1 ? __ldcg(a.V32 + ioff[e + u] + kq) : 0.f;
-#pragma unroll
-          for (int u = 0; u < UFI; ++u)
-            if (e + u < e1) {
-              const float4 c = icoef[e + u];
-              acc[0] = fmaf(c.x, v[u], acc[0]);
-              acc[1] = fmaf(c.y, v[u], acc[1]);
-              acc[2] = fmaf(c.z, v[u], acc[2]);
-              acc[3] = fmaf(c.w, v[u], acc[3]);
-            }
-        }
+        const int ni = s_nit[0] - s_nit[1], i0 = s_nit[1];  // the other blocks' rows
+        product_rows(i0 + part * ni / tk, i0 + (part + 1) * ni / tk);
 #pragma unroll
         for (int j = 0; j < GI; ++j) red_w[(part * GI + j) * npr + kq] = acc[j];
         __syncthreads();  // red_w, s_ab
@@ -1000,7 +1029,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
         const double bs = block_sum_ff(dq, red);
         if (tid == 0) a.part[blk] = bs;
       }
-      if (!grid_sync(a, B_PRODUCT, epoch)) break;
+      if (!grid_sync(a, B_PRODUCT, bst)) break;
       // ---- step: alpha; x, r, z of the block; levels of z; partials
       const double pq = partial_total(a.part, G, tot);
       if (tid == 0) {
@@ -1038,6 +1067,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
           ff_acc_prod(rr, ri, ri);
         }
       }
+
       {
         const double b1 = block_sum_ff(rz, red);
         const double b2 = block_sum_ff(rr, red);
@@ -1047,7 +1077,9 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
         }
       }
       levels_z();
-      if (!grid_sync(a, B_STEP, epoch)) break;
+      grid_arrive(a, B_STEP, bst);
+      own_rows();
+      if (!grid_wait(a, B_STEP, bst)) break;
       {
         const double2 t2 = partial_total2(a.part + P2, G, tot);
         if (tid == 0) step_scalars(sS, a, it, alpha_d, pq, t2.x, t2.y);
@@ -1083,7 +1115,7 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
           V2[(size_t)l * n + rg[t]] = make_float2(acc.h, acc.l);
         }
       }
-      if (!grid_sync(a, B_LEVELS64, epoch)) break;
+      if (!grid_sync(a, B_LEVELS64, bst)) break;
       // r64 = b - A x of the block (into us); r = r64, z = G G^T r, levels of z
       {
         ff acc[RPT];
@@ -1134,7 +1166,9 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
         }
       }
       levels_z();
-      if (!grid_sync(a, B_UPDATE, epoch)) break;
+      grid_arrive(a, B_UPDATE, bst);
+      own_rows();
+      if (!grid_wait(a, B_UPDATE, bst)) break;
       {
         const double2 t2 = partial_total2(a.part + P2, G, tot);
         if (tid == 0) update_scalars(sS, a, t2.x, t2.y);
@@ -1154,10 +1188,12 @@ __global__ void __launch_bounds__(NT, 2) k_mixed_resident(PersistArgs a) {
 
 // Product items of one block per CTA (NT threads): the entries of its
 // skewers' FP32 lists (at most NE_ITEMS) as (offset of the (neighbour,
-// level) row, skewer j, factor), sorted by offset (bitonic, in shared
-// memory), equal offsets merged into one item with a factor per skewer.
-// cnt[blk] = the block's items; cnt[n_blocks] = the largest count over the
-// blocks, or NI + 1 when a block has too many entries or items.
+// level) row, skewer j, factor), sorted by (row of another block, offset)
+// (bitonic, in shared memory), equal offsets merged into one item with a
+// factor per skewer: the rows of the block's own skewers come first.
+// cnt[blk] = the block's items, own[blk] = those on its own skewers;
+// cnt[n_blocks] = the largest count over the blocks, or NI + 1 when a block
+// has too many entries or items.  Offsets are below 2^31.
 constexpr int NE_ITEMS = 1024;
 __global__ void __launch_bounds__(NT) k_build_items(int g, int n_per, int n,
                                                     const int* __restrict__ bsk,
@@ -1166,12 +1202,14 @@ __global__ void __launch_bounds__(NT) k_build_items(int g, int n_per, int n,
                                                     const int* __restrict__ lev,
                                                     const float* __restrict__ p32,
                                                     int* __restrict__ cnt,
+                                                    int* __restrict__ own,
                                                     unsigned int* __restrict__ ioff,
                                                     float4* __restrict__ icoef) {
   __shared__ unsigned int key[NE_ITEMS];
   __shared__ unsigned int val[NE_ITEMS];  // j << 28 | entry index within the block
   __shared__ int base[GI + 1], sk[GI];
   __shared__ int scan[NE_ITEMS];
+  __shared__ int n_own;
   const int blk = blockIdx.x, tid = threadIdx.x;
   if (tid == 0) {
     int c = 0;
@@ -1182,6 +1220,7 @@ __global__ void __launch_bounds__(NT) k_build_items(int g, int n_per, int n,
       if (s >= 0) c += ptr[s + 1] - ptr[s];
     }
     base[GI] = c;
+    n_own = 0;
   }
   __syncthreads();
   const int total = base[GI];
@@ -1198,7 +1237,11 @@ __global__ void __launch_bounds__(NT) k_build_items(int g, int n_per, int n,
       int j = 0;
       while (j + 1 < GI && i >= base[j + 1]) ++j;
       const int q = ptr[sk[j]] + (i - base[j]);
-      k = (unsigned int)((size_t)(lev[q] - 1) * n + (size_t)idx[q] * n_per);
+      const int nb = idx[q];
+      bool mine = false;
+      for (int j2 = 0; j2 < GI; ++j2) mine |= nb == sk[j2];
+      k = (unsigned int)((size_t)(lev[q] - 1) * n + (size_t)nb * n_per) |
+          (mine ? 0u : 0x80000000u);
       v = ((unsigned int)j << 28) | (unsigned int)q;
     }
     key[i] = k;
@@ -1253,11 +1296,16 @@ __global__ void __launch_bounds__(NT) k_build_items(int g, int n_per, int n,
     const int it = scan[i] - 1;
     const int j = (int)(val[i] >> 28);
     const int q = (int)(val[i] & 0x0fffffffu);
-    if (i == 0 || key[i] != key[i - 1]) ioff[o + it] = key[i];
+    if (i == 0 || key[i] != key[i - 1]) {
+      ioff[o + it] = key[i] & 0x7fffffffu;
+      if (!(key[i] & 0x80000000u)) atomicAdd(&n_own, 1);
+    }
     reinterpret_cast<float*>(icoef + o + it)[j] = p32[q];
   }
+  __syncthreads();
   if (tid == 0) {
     cnt[blk] = n_items;
+    own[blk] = n_own;
     atomicMax(cnt + gridDim.x, n_items);
   }
 }
@@ -1322,17 +1370,19 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   // preconditioner and inner cutoff (k_build_items): per block, the distinct
   // (neighbour, level) rows its skewers' FP32 lists name, ordered by offset,
   // with each skewer's factor, in slots of NI per block.
-  const bool off32 = (double)(g.inner.lmax + 1) * (double)op->n < 4294967295.0;
+  const bool off31 = (double)(g.inner.lmax + 1) * (double)op->n < 2147483647.0;
   if (g.res_pc != pc || g.res_cut != g.inner.cut) {
     g.res_max_list = NI + 1;  // unusable unless built
-    if (off32 && pc->g <= GI && NT % g.n_per == 0 && g.inner.idx.n < (1u << 28)) {
+    if (off31 && pc->g <= GI && NT % g.n_per == 0 && g.inner.idx.n < (1u << 28)) {
       g.it_cnt.alloc(pc->n_sk + 1);  // last: the largest count (or an overflow mark)
+      g.it_own.alloc(pc->n_sk);
       g.it_off.alloc((size_t)pc->n_sk * NI);
       g.it_coef.alloc((size_t)pc->n_sk * NI);
       DS_CUDA(cudaMemsetAsync(g.it_cnt.p, 0, g.it_cnt.bytes(), st));
       k_build_items<<<pc->n_sk, NT, 0, st>>>(pc->g, g.n_per, op->n, pc->bsk.p, g.inner.ptr.p,
                                              g.inner.idx.p, g.inner.lev.p, g.inner.p32.p,
-                                             g.it_cnt.p, g.it_off.p, g.it_coef.p);
+                                             g.it_cnt.p, g.it_own.p, g.it_off.p,
+                                             g.it_coef.p);
       DS_CHECK_LAUNCH();
       int mx = 0;
       DS_CUDA(cudaMemcpyAsync(&mx, g.it_cnt.p + pc->n_sk, sizeof(int), cudaMemcpyDeviceToHost,
@@ -1365,7 +1415,7 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
     g.p_time.alloc(n_pt);
     DS_CUDA(cudaMemsetAsync(g.p_time.p, 0, g.p_time.bytes(), st));
   }
-  const size_t n_sync = (size_t)(1 + grid) * BAR_LINE;
+  const size_t n_sync = BAR_WORDS;
   g.p_sync.alloc(n_sync);
   DS_CUDA(cudaMemsetAsync(g.p_sync.p, 0, n_sync * sizeof(int), st));
   PersistArgs a{};
@@ -1412,6 +1462,7 @@ bool run_mixed_persistent(ds_operator* op, OpF32& f, const SkewerPC* pc, const S
   a.limit = op->ctx->wait_limit > 0 ? op->ctx->wait_limit : 4000000000LL;
   a.pt = g.p_time.p;
   a.it_cnt = g.it_cnt.p;
+  a.it_own = g.it_own.p;
   a.it_off = g.it_off.p;
   a.it_coef = g.it_coef.p;
   if (!g.ff_b.p) {  // float-pair copies for the update (fixed for the grid's life)
