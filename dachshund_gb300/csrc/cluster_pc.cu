@@ -37,90 +37,112 @@ namespace ds {
 namespace {
 
 constexpr int CPC_MAX_BAND = 24;
-constexpr int CPC_PACKED = (CPC_MAX_BAND + 1) * (CPC_MAX_BAND + 2) / 2;
 
 // Column `j` (a slot) of G: rows j .. j + m - 1, the next non-padding slots
 // of its block (at most band + 1).  A_ab = wl_a S_ab wr_b + e_a delta_ab with
 // the exact Gaussian S evaluated in FP32 (the table kernel differs from it by
-// ~1e-4, FP32 by ~1e-6: immaterial to a preconditioner).
-__global__ void k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc,
-                               const int* __restrict__ crec, const int* __restrict__ inv,
-                               const double* __restrict__ px, const double* __restrict__ py,
-                               const double* __restrict__ pz, const double* __restrict__ wl,
-                               const double* __restrict__ wr, const double* __restrict__ e,
-                               float* __restrict__ L, int* __restrict__ n_fallback) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_slots) return;
-  if (crec[j] < 0) return;  // padding slot: its row stays 0
+// ~1e-4, FP32 by ~1e-6: immaterial to a preconditioner).  One warp per
+// column: lane a holds row a's coordinates and coefficients and forms row a
+// of the system in shared memory; the Cholesky factor overwrites it column
+// by column (lanes over the rows), then C y = e_1 (lanes over the rows) and
+// C^T g = y (one row at a time); every entry takes the same operations in
+// the same order as a one-thread-per-column solve, with the system in shared
+// memory instead of 2 KB of per-thread stack.
+constexpr int CPC_N = CPC_MAX_BAND + 1;  // rows of a column's system at most
+constexpr int CPC_WARPS = 4;             // columns per CTA
+__global__ void __launch_bounds__(32 * CPC_WARPS)
+    k_cluster_fsai(int n_slots, int block, int band, KernelConsts kc, const int* __restrict__ crec,
+                   const int* __restrict__ inv, const double* __restrict__ px,
+                   const double* __restrict__ py, const double* __restrict__ pz,
+                   const double* __restrict__ wl, const double* __restrict__ wr,
+                   const double* __restrict__ e, float* __restrict__ L,
+                   int* __restrict__ n_fallback) {
+  __shared__ float sC[CPC_WARPS][CPC_N * CPC_N];  // row a at a CPC_N
+  __shared__ float sy[CPC_WARPS][CPC_N];
+  const int w = threadIdx.x >> 5, a = threadIdx.x & 31;
+  const int j = blockIdx.x * CPC_WARPS + w;
+  if (j >= n_slots || crec[j] < 0) return;  // the whole warp: padding slot (its row stays 0)
+  float* C = sC[w];
+  float* y = sy[w];
   const int blk_end = (j / block + 1) * block;
-  int pos[CPC_MAX_BAND + 1];
-  int m = 0;
-  while (m <= band && j + m < blk_end && crec[j + m] >= 0) {
-    pos[m] = inv[crec[j + m]];
-    ++m;
-  }
+  const bool in = a <= band && j + a < blk_end && crec[j + a] >= 0;
+  const unsigned out = __ballot_sync(0xffffffffu, !in);
+  const int m = out ? __ffs(out) - 1 : 32;  // the first slot that is not a row ends them
+  const int pa = a < m ? inv[crec[j + a]] : 0;
+  const int p0 = __shfl_sync(0xffffffffu, pa, 0);
   // coordinates relative to the column's own pixel, in FP32 (a
-  // preconditioner needs no more), and the coefficients of each position
-  float rx[CPC_MAX_BAND + 1], ry[CPC_MAX_BAND + 1], rz[CPC_MAX_BAND + 1];
-  float wa[CPC_MAX_BAND + 1], wb[CPC_MAX_BAND + 1], ea[CPC_MAX_BAND + 1];
-  {
-    const double x0 = px[pos[0]], y0 = py[pos[0]], z0 = pz[pos[0]];
-    for (int a = 0; a < m; ++a) {
-      const int pa = pos[a];
-      rx[a] = (float)(px[pa] - x0);
-      ry[a] = (float)(py[pa] - y0);
-      rz[a] = (float)(pz[pa] - z0);
-      wa[a] = (float)(wl[pa] * kc.var_s);
-      wb[a] = (float)wr[pa];
-      ea[a] = (float)e[pa];
-    }
+  // preconditioner needs no more), and the coefficients of row a
+  float rx = 0.f, ry = 0.f, rz = 0.f, wa = 0.f, wb = 0.f, ea = 0.f;
+  if (a < m) {
+    rx = (float)(px[pa] - px[p0]);
+    ry = (float)(py[pa] - py[p0]);
+    rz = (float)(pz[pa] - pz[p0]);
+    wa = (float)(wl[pa] * kc.var_s);
+    wb = (float)wr[pa];
+    ea = (float)e[pa];
   }
   const float cp = (float)kc.c_perp, cq = (float)kc.c_para, cut = (float)kc.exact_cut;
-  float C[CPC_PACKED];  // packed lower Cholesky factor: row a starts at a (a + 1) / 2
-  bool ok = true;
-  for (int a = 0; a < m && ok; ++a) {
-    float* Ca = C + a * (a + 1) / 2;
-    for (int b = 0; b <= a; ++b) {
-      const float dx = rx[a] - rx[b], dy = ry[a] - ry[b], dz = rz[a] - rz[b];
+  for (int b = 0; b < m; ++b) {
+    const float xb = __shfl_sync(0xffffffffu, rx, b), yb = __shfl_sync(0xffffffffu, ry, b);
+    const float zb = __shfl_sync(0xffffffffu, rz, b), wbb = __shfl_sync(0xffffffffu, wb, b);
+    if (a < m && b <= a) {
+      const float dx = rx - xb, dy = ry - yb, dz = rz - zb;
       const float arg = fmaf(cp, fmaf(dx, dx, dy * dy), cq * dz * dz);
-      float v = arg < cut ? wa[a] * expf(-arg) * wb[b] : 0.f;
-      if (a == b) v += ea[a];
-      const float* Cb = C + b * (b + 1) / 2;
-      for (int k = 0; k < b; ++k) v = fmaf(-Ca[k], Cb[k], v);
-      if (a == b) {
-        if (!(v > 0.f)) {
-          ok = false;
-          break;
-        }
-        Ca[a] = sqrtf(v);
-      } else {
-        Ca[b] = v / Cb[b];
-      }
+      float v = arg < cut ? wa * expf(-arg) * wbb : 0.f;
+      if (a == b) v += ea;
+      C[a * CPC_N + b] = v;
     }
   }
+  __syncwarp();
+  // lower Cholesky factor, column b by lanes a >= b
+  bool ok = true;
+  for (int b = 0; b < m; ++b) {
+    float v = 0.f;
+    if (a >= b && a < m) {
+      v = C[a * CPC_N + b];
+      for (int k = 0; k < b; ++k) v = fmaf(-C[a * CPC_N + k], C[b * CPC_N + k], v);
+    }
+    const float d = __shfl_sync(0xffffffffu, v, b);
+    if (!(d > 0.f)) {
+      ok = false;
+      break;
+    }
+    const float cbb = sqrtf(d);
+    __syncwarp();
+    if (a == b)
+      C[a * CPC_N + a] = cbb;
+    else if (a > b && a < m)
+      C[a * CPC_N + b] = v / cbb;
+    __syncwarp();
+  }
   if (!ok) {
-    const int p0 = pos[0];
-    const double a00 = wl[p0] * kc.var_s * wr[p0] + e[p0];
-    L[j] = (float)(1.0 / sqrt(a00));  // plane 0: the diagonal
-    atomicAdd(n_fallback, 1);
+    if (a == 0) {
+      const double a00 = wl[p0] * kc.var_s * wr[p0] + e[p0];
+      L[j] = (float)(1.0 / sqrt(a00));  // plane 0: the diagonal
+      atomicAdd(n_fallback, 1);
+    }
     return;
   }
-  // C y = e_1, then C^T g = y (g overwrites y)
-  float y[CPC_MAX_BAND + 1];
-  for (int a = 0; a < m; ++a) {
-    const float* Ca = C + a * (a + 1) / 2;
-    float v = a == 0 ? 1.f : 0.f;
-    for (int k = 0; k < a; ++k) v = fmaf(-Ca[k], y[k], v);
-    y[a] = v / Ca[a];
+  // C y = e_1: lane a finishes y_a once y_0 .. y_{a-1} are known
+  float yv = a == 0 ? 1.f : 0.f;
+  for (int k = 0; k < m; ++k) {
+    if (a == k) yv = yv / C[k * CPC_N + k];
+    const float yk = __shfl_sync(0xffffffffu, yv, k);
+    if (a > k && a < m) yv = fmaf(-C[a * CPC_N + k], yk, yv);
   }
-  for (int a = m - 1; a >= 0; --a) {
-    float v = y[a];
-    for (int k = a + 1; k < m; ++k) v = fmaf(-C[k * (k + 1) / 2 + a], y[k], v);
-    y[a] = v / C[a * (a + 1) / 2 + a];
+  if (a < m) y[a] = yv;
+  __syncwarp();
+  // C^T g = y (g overwrites y), from the last row up
+  for (int r = m - 1; r >= 0; --r) {
+    if (a == r) {
+      float v = y[r];
+      for (int k = r + 1; k < m; ++k) v = fmaf(-C[k * CPC_N + r], y[k], v);
+      y[r] = v / C[r * CPC_N + r];
+    }
+    __syncwarp();
   }
   // G[j + a][j] is plane a at slot j + a
-  const float sc = rsqrtf(y[0]);
-  for (int a = 0; a < m; ++a) L[(size_t)a * n_slots + (j + a)] = y[a] * sc;
+  if (a < m) L[(size_t)a * n_slots + (j + a)] = y[a] * rsqrtf(y[0]);
 }
 
 // Record r's z, and skewer s's (x, y) from its first record (r = s n_per).
@@ -136,6 +158,35 @@ __global__ void k_rec_coords(int n, int n_per, const int* __restrict__ inv,
     sx[r / n_per] = px[p];
     sy[r / n_per] = py[p];
   }
+}
+
+// *bad = 1 unless every record's z equals skewer 0's z at the same pixel and
+// skewer 0's z values increase (the shared z grid of plan_skewer_clusters).
+__global__ void k_shared_z(int n, int n_per, const double* __restrict__ rz, int* __restrict__ bad) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int k = r % n_per;
+  if (rz[r] != rz[k] || (r < n_per && k > 0 && !(rz[k - 1] < rz[k]))) atomicOr(bad, 1);
+}
+
+// The slots of the shared z grid: a cluster of sz skewers (the first sz of
+// its g) holds pixel k of its j-th skewer at slot k sz + j, then -1 up to
+// g n_per.
+__global__ void k_crec_shared(int n_slots, int n_per, int g, const int* __restrict__ bsk,
+                              int* __restrict__ crec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_slots) return;
+  const int B = g * n_per;
+  const int c = i / B, o = i - c * B;
+  const int* sk = bsk + (size_t)c * g;
+  int sz = 0;
+  while (sz < g && sk[sz] >= 0) ++sz;
+  int v = -1;
+  if (o < sz * n_per) {
+    const int k = o / sz, j = o - k * sz;
+    v = sk[j] * n_per + k;
+  }
+  crec[i] = v;
 }
 
 // 32-bit Morton key of (x, y) quantised to 16 bits each.
@@ -155,10 +206,14 @@ uint32_t morton2(uint32_t x, uint32_t y) {
 // skewers are visited in Morton order of their (x, y); each unassigned one
 // seeds a cluster with its g - 1 nearest unassigned skewers among the next
 // 256 unassigned in that order.  A cluster's slots hold its records sorted by
-// z, then by skewer; each block of g n_per slots is padded with -1.
+// z, then by skewer; each block of g n_per slots is padded with -1.  With
+// every skewer on skewer 0's increasing z values (`shared`) that order is
+// pixel-major and crec is left empty (built on the device); otherwise rz
+// holds every record's z.
 void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>& sx,
-                          const std::vector<double>& sy, const std::vector<double>& rz,
-                          std::vector<int>& crec, std::vector<int>& bsk, int& n_blocks) {
+                          const std::vector<double>& sy, bool shared,
+                          const std::vector<double>& rz, std::vector<int>& crec,
+                          std::vector<int>& bsk, int& n_blocks) {
   const double x0 = *std::min_element(sx.begin(), sx.end());
   const double x1 = *std::max_element(sx.begin(), sx.end());
   const double y0 = *std::min_element(sy.begin(), sy.end());
@@ -200,22 +255,9 @@ void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>&
   bsk.assign((size_t)n_blocks * g, -1);
   for (int c = 0; c < n_blocks; ++c)
     std::copy(clusters[c].begin(), clusters[c].end(), bsk.begin() + (size_t)c * g);
+  if (shared) return;  // pixel-major: k_crec_shared
   const int B = g * n_per;
   crec.assign((size_t)n_blocks * B, -1);
-  // every skewer on the z values of skewer 0, in increasing order (the usual
-  // layout): a cluster's order by z, then by rank, is pixel-major
-  bool shared = true;
-  for (int k = 1; k < n_per && shared; ++k) shared = rz[k - 1] < rz[k];
-  for (size_t r = n_per; r < rz.size() && shared; ++r) shared = rz[r] == rz[r % n_per];
-  if (shared) {
-    for (int c = 0; c < n_blocks; ++c) {
-      const std::vector<int>& cl = clusters[c];
-      int* out = crec.data() + (size_t)c * B;
-      for (int k = 0; k < n_per; ++k)
-        for (size_t j = 0; j < cl.size(); ++j) *out++ = cl[j] * n_per + k;
-    }
-    return;
-  }
   std::vector<int> recs;
   for (int c = 0; c < n_blocks; ++c) {
     recs.clear();
@@ -238,33 +280,50 @@ void build_cluster_pc(ds_operator* op, int n_sk, int n_per, int g, int band) {
   k_rec_coords<<<(n + 255) / 256, 256, 0, st>>>(n, n_per, op->inv.p, op->pix.x.p, op->pix.y.p,
                                                 op->pix.z.p, dsx.p, dsy.p, drz.p);
   DS_CHECK_LAUNCH();
-  std::vector<double> sx(n_sk), sy(n_sk), rz(n);
+  DevBuf<int> dbad;
+  dbad.alloc(1);
+  DS_CUDA(cudaMemsetAsync(dbad.p, 0, sizeof(int), st));
+  k_shared_z<<<(n + 255) / 256, 256, 0, st>>>(n, n_per, drz.p, dbad.p);
+  DS_CHECK_LAUNCH();
+  std::vector<double> sx(n_sk), sy(n_sk), rz;
+  int bad = 0;
   DS_CUDA(cudaMemcpyAsync(sx.data(), dsx.p, n_sk * sizeof(double), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaMemcpyAsync(sy.data(), dsy.p, n_sk * sizeof(double), cudaMemcpyDeviceToHost, st));
-  DS_CUDA(cudaMemcpyAsync(rz.data(), drz.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DS_CUDA(cudaMemcpyAsync(&bad, dbad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   DS_CUDA(cudaStreamSynchronize(st));
+  if (bad) {  // records off the shared z grid: the host orders each cluster by z
+    rz.resize(n);
+    DS_CUDA(cudaMemcpyAsync(rz.data(), drz.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DS_CUDA(cudaStreamSynchronize(st));
+  }
   std::vector<int> crec, bsk;
   int n_blocks = 0;
-  plan_skewer_clusters(n_sk, n_per, g, sx, sy, rz, crec, bsk, n_blocks);
+  plan_skewer_clusters(n_sk, n_per, g, sx, sy, !bad, rz, crec, bsk, n_blocks);
 
   std::unique_ptr<SkewerPC, SkewerPCDeleter> pc(new SkewerPC());
   pc->n_sk = n_blocks;
   pc->n_per = g * n_per;
   pc->band = band;
-  const size_t n_slots = crec.size();
+  const size_t n_slots = (size_t)n_blocks * g * n_per;
   pc->crec.alloc(n_slots);
   pc->L.alloc(n_slots * (band + 1));
   DevBuf<int> nfb;
   nfb.alloc(1);
-  DS_CUDA(cudaMemcpyAsync(pc->crec.p, crec.data(), n_slots * sizeof(int),
-                          cudaMemcpyHostToDevice, st));
   pc->g = g;
   pc->bsk.alloc(bsk.size());
   DS_CUDA(cudaMemcpyAsync(pc->bsk.p, bsk.data(), bsk.size() * sizeof(int),
                           cudaMemcpyHostToDevice, st));
+  if (crec.empty()) {
+    k_crec_shared<<<(unsigned)((n_slots + 255) / 256), 256, 0, st>>>((int)n_slots, n_per, g,
+                                                                     pc->bsk.p, pc->crec.p);
+    DS_CHECK_LAUNCH();
+  } else {
+    DS_CUDA(cudaMemcpyAsync(pc->crec.p, crec.data(), n_slots * sizeof(int),
+                            cudaMemcpyHostToDevice, st));
+  }
   DS_CUDA(cudaMemsetAsync(pc->L.p, 0, pc->L.bytes(), st));
   DS_CUDA(cudaMemsetAsync(nfb.p, 0, sizeof(int), st));
-  k_cluster_fsai<<<(unsigned)((n_slots + 127) / 128), 128, 0, st>>>(
+  k_cluster_fsai<<<(unsigned)((n_slots + CPC_WARPS - 1) / CPC_WARPS), 32 * CPC_WARPS, 0, st>>>(
       (int)n_slots, pc->n_per, band, op->kc, pc->crec.p, op->inv.p, op->pix.x.p, op->pix.y.p,
       op->pix.z.p, op->wl.p, op->wr.p, op->e.p, pc->L.p, nfb.p);
   DS_CHECK_LAUNCH();

@@ -150,9 +150,10 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // poll at all.  (Measured on GB300 against a broadcast in which that CTA
 // writes the epoch into a flag line per CTA after a fence: 2.90 against
 // 3.07 ms per 262,144-pixel solve; the broadcast adds a fence and a store
-// round trip to every barrier.)  A poll that runs out (`limit` SM cycles)
-// records `code` in the error word and returns false, as does a CTA that
-// finds the error word set (read every 16 polls, and by the last arrival).
+// round trip to every barrier.)  A wait that runs out (`limit` SM cycles,
+// checked before each poll) records `code` in the error word and returns
+// false, as does a CTA that finds the error word set (read every 16 polls,
+// and by the last arrival).
 // Words: [0] count, [1] error code.
 // The barrier comes in two halves: between grid_arrive and grid_wait a CTA
 // may work on its own data (writing nothing another CTA reads in the next
@@ -187,15 +188,17 @@ __device__ bool grid_wait(const PersistArgs& a, int code, BarState& b) {
       const unsigned int target = b.epoch * gridDim.x;
       const long long t0 = clock64();
       for (int k = 0;; ++k) {
+        // the bound first: a CTA gives up once it has waited `limit`
+        // cycles, whatever its next poll would read
+        if (clock64() - t0 >= a.limit) {
+          atomicExch(a.err, code);
+          ok = 0;
+          break;
+        }
         unsigned int f;
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(f) : "l"(a.bar) : "memory");
         if ((int)(f - target) >= 0) break;
         if ((k & 15) == 15 && *(volatile int*)a.err) {
-          ok = 0;
-          break;
-        }
-        if (clock64() - t0 > a.limit) {
-          atomicExch(a.err, code);
           ok = 0;
           break;
         }

@@ -347,7 +347,10 @@ __global__ void k_mc_apply(int n_sk, int nz, const int* __restrict__ ptr,
 // neighbours when c_perp |dxy|^2 + th[0] < cut; the entry keeps
 // lev = #{q < Q : c_perp |dxy|^2 + th[q] < cut} (th ascending: the z part of
 // the argument per level) and var_s exp(-c_perp |dxy|^2).  One warp per
-// target scans the sources in order, so each row is in ascending b.
+// target scans the sources in order, so each row is in ascending b, and
+// stores each entry's b and argument; k_list_finish then forms the levels
+// and factors one thread per entry (in the scan, the FP64 work of the few
+// lanes with an entry would hold the whole warp on GB300's FP64 pipe).
 __global__ void k_list_count(int nt, const double* __restrict__ tx,
                              const double* __restrict__ ty, int ns,
                              const double* __restrict__ sx, const double* __restrict__ sy,
@@ -367,10 +370,8 @@ __global__ void k_list_count(int nt, const double* __restrict__ tx,
 __global__ void k_list_fill(int nt, const double* __restrict__ tx, const double* __restrict__ ty,
                             int ns, const double* __restrict__ sx,
                             const double* __restrict__ sy, double c_perp, double cut,
-                            double var_s, int Q, const double* __restrict__ th,
-                            const int* __restrict__ ptr, int* __restrict__ idx,
-                            int* __restrict__ lev, double* __restrict__ p64,
-                            float* __restrict__ p32) {
+                            const double* __restrict__ th, const int* __restrict__ ptr,
+                            int* __restrict__ idx, double* __restrict__ p64) {
   const int t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (t >= nt) return;
@@ -387,16 +388,33 @@ __global__ void k_list_fill(int nt, const double* __restrict__ tx, const double*
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     if (ok) {
       const int at = base + __popc(m & ((1u << lane) - 1u));
-      int L = 0;
-      while (L < Q && parg + th[L] < cut) ++L;
-      const double pv = var_s * exp(-parg);
       idx[at] = b;
-      lev[at] = L;
-      p64[at] = pv;
-      if (p32) p32[at] = (float)pv;
+      p64[at] = parg;
     }
     base += __popc(m);
   }
+}
+
+// Entry e's level (the count of th[q] with arg + th[q] < cut: a binary
+// search, the predicate falling with q) and factor, from its argument in p64.
+__global__ void k_list_finish(long long n, double cut, double var_s, int Q,
+                              const double* __restrict__ th, int* __restrict__ lev,
+                              double* __restrict__ p64, float* __restrict__ p32) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const double parg = p64[e];
+  int lo = 0, hi = Q;  // the count lies in [lo, hi]
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (parg + th[mid] < cut)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  const double pv = var_s * exp(-parg);
+  lev[e] = lo;
+  p64[e] = pv;
+  if (p32) p32[e] = (float)pv;
 }
 
 // Skewer (x, y) and skewer 0's z values, then a flag for any record not at
@@ -455,9 +473,14 @@ static long long build_lists(int nt, const double* tx, const double* ty, int ns,
   p64.alloc(std::max<long long>(1, total));
   if (p32) p32->alloc(std::max<long long>(1, total));
   DS_CUDA(cudaMemcpyAsync(ptr.p, h.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
-  k_list_fill<<<blocks, 256, 0, st>>>(nt, tx, ty, ns, sx, sy, kc.c_perp, cut, kc.var_s, Q, dth.p,
-                                      ptr.p, idx.p, lev.p, p64.p, p32 ? p32->p : nullptr);
+  k_list_fill<<<blocks, 256, 0, st>>>(nt, tx, ty, ns, sx, sy, kc.c_perp, cut, dth.p, ptr.p,
+                                      idx.p, p64.p);
   DS_CHECK_LAUNCH();
+  if (total > 0) {
+    k_list_finish<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(
+        total, cut, kc.var_s, Q, dth.p, lev.p, p64.p, p32 ? p32->p : nullptr);
+    DS_CHECK_LAUNCH();
+  }
   DS_CUDA(cudaStreamSynchronize(st));  // h, dth, cnt go out of scope
   return total;
 }

@@ -149,9 +149,10 @@ int ds_context_get_profile(ds_context* ctx, ds_profile* out);
  * runs out records its code, the kernel waits (with the default bound) for
  * its own MMAs and copies in flight, frees its tensor memory and returns, and
  * the call returns DS_ERR_TIMEOUT.  The same bound applies to each grid
- * barrier wait of the persistent mixed solve (ds_operator_set_iteration_form):
- * a CTA that runs out records the phase, every CTA leaves at its next
- * barrier, and the call returns DS_ERR_TIMEOUT.  No reference counterpart
+ * barrier wait of the persistent mixed solve (ds_operator_set_iteration_form;
+ * checked before each poll, so a bound of 1 gives up at once): a CTA that
+ * runs out records the phase, every CTA leaves when it finds the record (in
+ * that wait or at its next barrier), and the call returns DS_ERR_TIMEOUT.  No reference counterpart
  * (the reference has no device code). */
 int ds_context_set_wait_limit(ds_context* ctx, long long cycles);
 
