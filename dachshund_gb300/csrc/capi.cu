@@ -399,10 +399,6 @@ int ds_operator_create(ds_context* ctx, int form, int n, const double* records,
     op->kc = make_consts(k);
     op->serial = g_serial++;
     load_table(op->table, k, st);
-    // norm_b on the host in record order, as lib/wf_vector.cc:105-112.
-    double sb2 = 0.0;
-    for (int i = 0; i < n; ++i) sb2 += records[(size_t)i * 5 + 4] * records[(size_t)i * 5 + 4];
-    op->norm_b = std::sqrt(sb2);
     DevBuf<double> rec;
     upload(records, (size_t)n * 5, rec, st);
     build_point_set(op->pix, rec.p, n, 5, std::sqrt(op->kc.c_perp), std::sqrt(op->kc.c_perp),
@@ -419,7 +415,12 @@ int ds_operator_create(ds_context* ctx, int form, int n, const double* records,
                                              op->inv.p);
     DS_CHECK_LAUNCH();
     // the tile-pair list is built on the first pair-kernel call
-    // (ensure_op_pairs): the structured operator needs none
+    // (ensure_op_pairs): the structured operator needs none.
+    // norm_b on the host in record order, as lib/wf_vector.cc:105-112, while
+    // the device sorts and tiles the records.
+    double sb2 = 0.0;
+    for (int i = 0; i < n; ++i) sb2 += records[(size_t)i * 5 + 4] * records[(size_t)i * 5 + 4];
+    op->norm_b = std::sqrt(sb2);
     DS_CUDA(cudaStreamSynchronize(st));
   });
   if (rc != DS_OK) return rc;

@@ -181,8 +181,6 @@ __global__ void k_unit_boxes_idx(const double* __restrict__ rec, int n, int stri
   if (threadIdx.x < 6) box[t * 6 + threadIdx.x] = sm[threadIdx.x][0];
 }
 
-// key = node << 32 | order-preserving bits of the coordinate along the
-// node's split axis (0 for nodes that are already leaves).
 // node_of_unit for the units of every node of a level (one CTA per node).
 __global__ void k_node_units(const int2* __restrict__ nodes, int* __restrict__ node_of_unit) {
   const int k = blockIdx.x;
@@ -191,10 +189,12 @@ __global__ void k_node_units(const int2* __restrict__ nodes, int* __restrict__ n
 }
 
 // Split axis of every node of a level with at least two units: the longest
-// side of the union of its unit boxes (the first of equal sides), else -1.
-// Min and max are exact, so the order of the reduction does not matter.
+// side of the union of its unit boxes (the first of equal sides), else -1,
+// and the map of that side onto the key's cb coordinate bits (range[k] =
+// (lo, (2^cb - 1) / (hi - lo))).  Min and max are exact, so the order of the
+// reduction does not matter.
 __global__ void k_node_axis(const int2* __restrict__ nodes, const double* __restrict__ box,
-                            int* __restrict__ node_axis) {
+                            int cb, int* __restrict__ node_axis, double2* __restrict__ range) {
   __shared__ double sm[6][128];
   const int k = blockIdx.x, t = threadIdx.x;
   const int2 nd = nodes[k];
@@ -226,13 +226,21 @@ __global__ void k_node_axis(const int2* __restrict__ nodes, const double* __rest
     for (int c = 1; c < 3; ++c)
       if (sm[3 + c][0] - sm[c][0] > sm[3 + ax][0] - sm[ax][0]) ax = c;
     node_axis[k] = ax;
+    const double ext = sm[3 + ax][0] - sm[ax][0];
+    range[k] = make_double2(sm[ax][0], ext > 0.0 ? (double)((1u << cb) - 1u) / ext : 0.0);
   }
 }
 
+// key = node << cb | the scaled coordinate along the node's split axis
+// mapped onto cb bits over the node's range (0 for nodes that are already
+// leaves).  A node of a level with nn nodes holds at most 32 n / nn points
+// and gets 2^cb >= 2^32 / nn levels, so only coordinates closer than the
+// node's extent / 2^cb share a key (and keep their order: the sort is stable).
 __global__ void k_kd_keys(const double* __restrict__ rec, int n, int stride,
                           const int* __restrict__ idx, const int* __restrict__ node_of_unit,
-                          const int* __restrict__ node_axis, double sx, double sy, double sz,
-                          unsigned long long* __restrict__ keys) {
+                          const int* __restrict__ node_axis, const double2* __restrict__ range,
+                          int cb, double sx, double sy, double sz,
+                          unsigned int* __restrict__ keys) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int node = node_of_unit[i / SUBTILE];
@@ -241,11 +249,12 @@ __global__ void k_kd_keys(const double* __restrict__ rec, int n, int stride,
   if (axis >= 0) {
     const double* p = rec + (size_t)idx[i] * stride;
     const double s = axis == 0 ? sx : (axis == 1 ? sy : sz);
-    const float f = (float)(p[axis] * s);
-    u = __float_as_uint(f);
-    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    const double2 rg = range[node];
+    const double q = (p[axis] * s - rg.x) * rg.y;
+    const unsigned int top = (1u << cb) - 1u;
+    u = q <= 0.0 ? 0u : (q >= (double)top ? top : (unsigned int)q);
   }
-  keys[i] = ((unsigned long long)node << 32) | u;
+  keys[i] = ((unsigned int)node << cb) | u;
 }
 
 __global__ void k_iota(int n, int* __restrict__ out) {
@@ -416,8 +425,8 @@ __global__ void k_pair_mask(int n_rows, const int* __restrict__ row_ptr,
 // a node larger than a tile splits at a tile boundary near its middle, a node
 // within a tile splits at a unit boundary, so every TILE-point tile is a k-d
 // node and its four SUBTILE-point quarters are k-d nodes too (compact boxes
-// for each warp's rows).  Each level is one stable radix sort on (node,
-// coordinate along the node's longest scaled axis), which keeps every node's
+// for each warp's rows).  Each level is one stable radix sort of 32-bit keys
+// (node, coordinate along the node's longest scaled axis), which keeps every node's
 // points contiguous.  idx (sorted position -> record) is updated in place.
 void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, double sx,
                   double sy, double sz, DevBuf<int>& idx, cudaStream_t st) {
@@ -463,10 +472,12 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
   DevBuf<double> box;
   box.alloc((size_t)nu * 6);
   DevBuf<int> d_not, d_axis, idx2;
+  DevBuf<double2> d_range;
   d_not.alloc(nu);
   d_axis.alloc(level_off[n_levels] - level_off[n_levels - 1]);
+  d_range.alloc(level_off[n_levels] - level_off[n_levels - 1]);
   idx2.alloc(n);
-  DevBuf<unsigned long long> keys, keys2;
+  DevBuf<unsigned int> keys, keys2;
   keys.alloc(n);
   keys2.alloc(n);
   DevBuf<unsigned char> tmp;
@@ -477,19 +488,20 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
     DS_CHECK_LAUNCH();
     k_unit_boxes_idx<<<nu, SUBTILE, 0, st>>>(d_rec, n, stride, idx.p, sx, sy, sz, box.p);
     DS_CHECK_LAUNCH();
-    k_node_axis<<<nn, 128, 0, st>>>(nodes, box.p, d_axis.p);
-    DS_CHECK_LAUNCH();
-    k_kd_keys<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, idx.p, d_not.p, d_axis.p, sx,
-                                                  sy, sz, keys.p);
-    DS_CHECK_LAUNCH();
     int node_bits = 1;
     while ((1ull << node_bits) < (unsigned long long)nn) ++node_bits;
+    const int cb = 32 - node_bits;  // coordinate bits of the key
+    k_node_axis<<<nn, 128, 0, st>>>(nodes, box.p, cb, d_axis.p, d_range.p);
+    DS_CHECK_LAUNCH();
+    k_kd_keys<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, idx.p, d_not.p, d_axis.p,
+                                                  d_range.p, cb, sx, sy, sz, keys.p);
+    DS_CHECK_LAUNCH();
     size_t tmp_bytes = 0;
     DS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
-                                            0, 32 + node_bits, st));
+                                            0, 32, st));
     if (tmp.n < tmp_bytes) tmp.alloc(tmp_bytes);
     DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
-                                            0, 32 + node_bits, st));
+                                            0, 32, st));
     std::swap(idx.p, idx2.p);
   }
 }
@@ -572,8 +584,8 @@ void build_point_set(PointSet& ps, const double* d_rec, int n, int stride, doubl
   DS_CHECK_LAUNCH();
   k_box_f32<<<(int)((ns6 + BLK - 1) / BLK), BLK, 0, st>>>(ns6, ps.sbox.p, ps.sbox32.p);
   DS_CHECK_LAUNCH();
-  // The temporaries are freed on return; make sure the stream is done with them.
-  DS_CUDA(cudaStreamSynchronize(st));
+  // The temporaries are freed on return in stream order (or by cudaFree,
+  // which waits for the device), so the stream need not be drained here.
 }
 
 // Items per tile pair: the column sub-tiles w with (mask >> w) & 0x1111 != 0.
