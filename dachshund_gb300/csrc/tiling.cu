@@ -144,41 +144,60 @@ __global__ void k_tile_boxes(const double* __restrict__ x, const double* __restr
 
 // ---- k-d partition -----------------------------------------------------
 
-// Bounding boxes (scaled units) of every SUBTILE-point unit of the current
-// order idx (one CTA of SUBTILE threads per unit).
-__global__ void k_unit_boxes_idx(const double* __restrict__ rec, int n, int stride,
-                                 const int* __restrict__ idx, double sx, double sy, double sz,
-                                 double* __restrict__ box) {
-  const int t = blockIdx.x;
-  const int i = t * SUBTILE + threadIdx.x;
-  __shared__ double sm[6][SUBTILE];
-  double c[3];
+// Working points of the partition: the scaled coordinates in FP32 and the
+// record index (its bits in w), permuted with the keys by each level's sort,
+// so the levels read them contiguously (the axis choices need no more than
+// FP32; the tiles' boxes are formed afterwards from the FP64 coordinates).
+static_assert(SUBTILE == 32, "one warp per unit");
+__global__ void k_kd_points(const double* __restrict__ rec, int n, int stride,
+                            const int* __restrict__ idx, double sx, double sy, double sz,
+                            float4* __restrict__ pv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = idx[i];
+  const double* p = rec + (size_t)r * stride;
+  pv[i] = make_float4((float)(p[0] * sx), (float)(p[1] * sy), (float)(p[2] * sz),
+                      __int_as_float(r));
+}
+
+__global__ void k_kd_index(int n, const float4* __restrict__ pv, int* __restrict__ idx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) idx[i] = __float_as_int(pv[i].w);
+}
+
+// Boxes (lo x y z, hi x y z) of every SUBTILE-point unit of the current
+// order: one warp per unit.
+__global__ void k_unit_boxes(int n, int nu, const float4* __restrict__ pv,
+                             float* __restrict__ box) {
+  const int u = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (u >= nu) return;
+  const int i = u * SUBTILE + lane;
+  float lx = INFINITY, ly = INFINITY, lz = INFINITY, hx = -INFINITY, hy = -INFINITY,
+        hz = -INFINITY;
   if (i < n) {
-    const double* p = rec + (size_t)idx[i] * stride;
-    c[0] = p[0] * sx;
-    c[1] = p[1] * sy;
-    c[2] = p[2] * sz;
-    for (int k = 0; k < 3; ++k) {
-      sm[k][threadIdx.x] = c[k];
-      sm[3 + k][threadIdx.x] = c[k];
-    }
-  } else {
-    for (int k = 0; k < 3; ++k) {
-      sm[k][threadIdx.x] = INFINITY;
-      sm[3 + k][threadIdx.x] = -INFINITY;
-    }
+    const float4 q = pv[i];
+    lx = hx = q.x;
+    ly = hy = q.y;
+    lz = hz = q.z;
   }
-  __syncthreads();
-  for (int s = SUBTILE / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      for (int k = 0; k < 3; ++k) {
-        sm[k][threadIdx.x] = fmin(sm[k][threadIdx.x], sm[k][threadIdx.x + s]);
-        sm[3 + k][threadIdx.x] = fmax(sm[3 + k][threadIdx.x], sm[3 + k][threadIdx.x + s]);
-      }
-    }
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+    ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+    lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+    hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+    hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+    hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
   }
-  if (threadIdx.x < 6) box[t * 6 + threadIdx.x] = sm[threadIdx.x][0];
+  if (lane == 0) {
+    float* b = box + (size_t)u * 6;
+    b[0] = lx;
+    b[1] = ly;
+    b[2] = lz;
+    b[3] = hx;
+    b[4] = hy;
+    b[5] = hz;
+  }
 }
 
 // node_of_unit for the units of every node of a level (one CTA per node).
@@ -188,58 +207,89 @@ __global__ void k_node_units(const int2* __restrict__ nodes, int* __restrict__ n
   for (int u = nd.x + threadIdx.x; u < nd.y; u += blockDim.x) node_of_unit[u] = k;
 }
 
-// Split axis of every node of a level with at least two units: the longest
-// side of the union of its unit boxes (the first of equal sides), else -1,
-// and the map of that side onto the key's cb coordinate bits (range[k] =
-// (lo, (2^cb - 1) / (hi - lo))).  Min and max are exact, so the order of the
-// reduction does not matter.
-__global__ void k_node_axis(const int2* __restrict__ nodes, const double* __restrict__ box,
-                            int cb, int* __restrict__ node_axis, double2* __restrict__ range) {
-  __shared__ double sm[6][128];
-  const int k = blockIdx.x, t = threadIdx.x;
-  const int2 nd = nodes[k];
-  if (nd.y - nd.x < 2) {
-    if (t == 0) node_axis[k] = -1;
+// Split axis of every node of a level with at least two units (TPN threads
+// per node: a warp, or a whole CTA where the nodes hold thousands of
+// units): the longest side of the union of its unit boxes (the first of
+// equal sides), else -1, and the map of that side onto the key's cb
+// coordinate bits (range[k] = (lo, (2^cb - 1) / (hi - lo))).  Min and max
+// are exact, so the order of the reduction does not matter.
+template <int TPN>
+__global__ void __launch_bounds__(BLK) k_node_axis(int nn, const int2* __restrict__ nodes,
+                                                   const float* __restrict__ box, int cb,
+                                                   int* __restrict__ node_axis,
+                                                   double2* __restrict__ range) {
+  static_assert(TPN == 32 || TPN == BLK, "a warp or the CTA per node");
+  __shared__ float red[BLK / 32][6];
+  const int k = blockIdx.x * (BLK / TPN) + threadIdx.x / TPN;
+  const int g = threadIdx.x % TPN, lane = threadIdx.x & 31;
+  const bool live = k < nn;
+  const int2 nd = live ? nodes[k] : make_int2(0, 0);
+  if (TPN == 32 && (!live || nd.y - nd.x < 2)) {  // warp-uniform
+    if (live && lane == 0) node_axis[k] = -1;
     return;
   }
-  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int u = nd.x + t; u < nd.y; u += blockDim.x)
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+#pragma unroll 4
+  for (int u = nd.x + g; u < nd.y; u += TPN) {
+    const float* b = box + (size_t)u * 6;
+#pragma unroll
     for (int c = 0; c < 3; ++c) {
-      lo[c] = fmin(lo[c], box[(size_t)u * 6 + c]);
-      hi[c] = fmax(hi[c], box[(size_t)u * 6 + 3 + c]);
+      lo[c] = fminf(lo[c], b[c]);
+      hi[c] = fmaxf(hi[c], b[3 + c]);
     }
-  for (int c = 0; c < 3; ++c) {
-    sm[c][t] = lo[c];
-    sm[3 + c][t] = hi[c];
   }
-  __syncthreads();
-  for (int s = 64; s > 0; s >>= 1) {
-    if (t < s)
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  if (TPN > 32) {  // the CTA's warps (one node per CTA)
+    const int w = threadIdx.x >> 5;
+    if (lane == 0)
       for (int c = 0; c < 3; ++c) {
-        sm[c][t] = fmin(sm[c][t], sm[c][t + s]);
-        sm[3 + c][t] = fmax(sm[3 + c][t], sm[3 + c][t + s]);
+        red[w][c] = lo[c];
+        red[w][3 + c] = hi[c];
       }
     __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w2 = 1; w2 < BLK / 32; ++w2)
+        for (int c = 0; c < 3; ++c) {
+          lo[c] = fminf(lo[c], red[w2][c]);
+          hi[c] = fmaxf(hi[c], red[w2][3 + c]);
+        }
   }
-  if (t == 0) {
+  if (g == 0 && live) {
+    if (nd.y - nd.x < 2) {
+      node_axis[k] = -1;
+      return;
+    }
+    const float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
     int ax = 0;
-    for (int c = 1; c < 3; ++c)
-      if (sm[3 + c][0] - sm[c][0] > sm[3 + ax][0] - sm[ax][0]) ax = c;
+    float ext = e0, l = lo[0];
+    if (e1 > ext) {
+      ax = 1;
+      ext = e1;
+      l = lo[1];
+    }
+    if (e2 > ext) {
+      ax = 2;
+      ext = e2;
+      l = lo[2];
+    }
     node_axis[k] = ax;
-    const double ext = sm[3 + ax][0] - sm[ax][0];
-    range[k] = make_double2(sm[ax][0], ext > 0.0 ? (double)((1u << cb) - 1u) / ext : 0.0);
+    range[k] = make_double2(l, ext > 0.f ? (double)((1u << cb) - 1u) / (double)ext : 0.0);
   }
 }
 
-// key = node << cb | the scaled coordinate along the node's split axis
+// key = node << cb | the point's coordinate along the node's split axis
 // mapped onto cb bits over the node's range (0 for nodes that are already
 // leaves).  A node of a level with nn nodes holds at most 32 n / nn points
 // and gets 2^cb >= 2^32 / nn levels, so only coordinates closer than the
 // node's extent / 2^cb share a key (and keep their order: the sort is stable).
-__global__ void k_kd_keys(const double* __restrict__ rec, int n, int stride,
-                          const int* __restrict__ idx, const int* __restrict__ node_of_unit,
-                          const int* __restrict__ node_axis, const double2* __restrict__ range,
-                          int cb, double sx, double sy, double sz,
+__global__ void k_kd_keys(int n, const float4* __restrict__ pv,
+                          const int* __restrict__ node_of_unit, const int* __restrict__ node_axis,
+                          const double2* __restrict__ range, int cb,
                           unsigned int* __restrict__ keys) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -247,12 +297,12 @@ __global__ void k_kd_keys(const double* __restrict__ rec, int n, int stride,
   const int axis = node_axis[node];
   unsigned int u = 0;
   if (axis >= 0) {
-    const double* p = rec + (size_t)idx[i] * stride;
-    const double s = axis == 0 ? sx : (axis == 1 ? sy : sz);
+    const float4 q = pv[i];
+    const float v = axis == 0 ? q.x : (axis == 1 ? q.y : q.z);
     const double2 rg = range[node];
-    const double q = (p[axis] * s - rg.x) * rg.y;
+    const double f = ((double)v - rg.x) * rg.y;
     const unsigned int top = (1u << cb) - 1u;
-    u = q <= 0.0 ? 0u : (q >= (double)top ? top : (unsigned int)q);
+    u = f <= 0.0 ? 0u : (f >= (double)top ? top : (unsigned int)f);
   }
   keys[i] = ((unsigned int)node << cb) | u;
 }
@@ -426,7 +476,8 @@ __global__ void k_pair_mask(int n_rows, const int* __restrict__ row_ptr,
 // within a tile splits at a unit boundary, so every TILE-point tile is a k-d
 // node and its four SUBTILE-point quarters are k-d nodes too (compact boxes
 // for each warp's rows).  Each level is one stable radix sort of 32-bit keys
-// (node, coordinate along the node's longest scaled axis), which keeps every node's
+// (node, coordinate along the node's longest scaled axis) that carries the
+// points' FP32 coordinates and record indices, which keeps every node's
 // points contiguous.  idx (sorted position -> record) is updated in place.
 void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, double sx,
                   double sy, double sz, DevBuf<int>& idx, cudaStream_t st) {
@@ -469,41 +520,52 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
   d_nodes.alloc(all_nodes.size());
   DS_CUDA(cudaMemcpyAsync(d_nodes.p, all_nodes.data(), all_nodes.size() * sizeof(int2),
                           cudaMemcpyHostToDevice, st));
-  DevBuf<double> box;
+  DevBuf<float> box;
   box.alloc((size_t)nu * 6);
-  DevBuf<int> d_not, d_axis, idx2;
+  DevBuf<int> d_not, d_axis;
   DevBuf<double2> d_range;
   d_not.alloc(nu);
   d_axis.alloc(level_off[n_levels] - level_off[n_levels - 1]);
   d_range.alloc(level_off[n_levels] - level_off[n_levels - 1]);
-  idx2.alloc(n);
+  DevBuf<float4> pv, pv2;
+  pv.alloc(n);
+  pv2.alloc(n);
   DevBuf<unsigned int> keys, keys2;
   keys.alloc(n);
   keys2.alloc(n);
   DevBuf<unsigned char> tmp;
+  k_kd_points<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, idx.p, sx, sy, sz, pv.p);
+  DS_CHECK_LAUNCH();
+  constexpr int WPB = BLK / 32;  // warps per CTA
   for (int level = 0; level < n_levels; ++level) {
     const int nn = (int)(level_off[level + 1] - level_off[level]);
     const int2* nodes = d_nodes.p + level_off[level];
     k_node_units<<<nn, 128, 0, st>>>(nodes, d_not.p);
     DS_CHECK_LAUNCH();
-    k_unit_boxes_idx<<<nu, SUBTILE, 0, st>>>(d_rec, n, stride, idx.p, sx, sy, sz, box.p);
+    k_unit_boxes<<<(nu + WPB - 1) / WPB, BLK, 0, st>>>(n, nu, pv.p, box.p);
     DS_CHECK_LAUNCH();
     int node_bits = 1;
     while ((1ull << node_bits) < (unsigned long long)nn) ++node_bits;
     const int cb = 32 - node_bits;  // coordinate bits of the key
-    k_node_axis<<<nn, 128, 0, st>>>(nodes, box.p, cb, d_axis.p, d_range.p);
+    if (nu >= 256 * nn)  // thousands of units per node: a CTA per node
+      k_node_axis<BLK><<<nn, BLK, 0, st>>>(nn, nodes, box.p, cb, d_axis.p, d_range.p);
+    else
+      k_node_axis<32><<<(nn + WPB - 1) / WPB, BLK, 0, st>>>(nn, nodes, box.p, cb, d_axis.p,
+                                                            d_range.p);
     DS_CHECK_LAUNCH();
-    k_kd_keys<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(d_rec, n, stride, idx.p, d_not.p, d_axis.p,
-                                                  d_range.p, cb, sx, sy, sz, keys.p);
+    k_kd_keys<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(n, pv.p, d_not.p, d_axis.p, d_range.p, cb,
+                                                  keys.p);
     DS_CHECK_LAUNCH();
     size_t tmp_bytes = 0;
-    DS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
+    DS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, pv.p, pv2.p, n,
                                             0, 32, st));
     if (tmp.n < tmp_bytes) tmp.alloc(tmp_bytes);
-    DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, idx2.p, n,
-                                            0, 32, st));
-    std::swap(idx.p, idx2.p);
+    DS_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, pv.p, pv2.p, n, 0,
+                                            32, st));
+    std::swap(pv.p, pv2.p);
   }
+  k_kd_index<<<(n + BLK - 1) / BLK, BLK, 0, st>>>(n, pv.p, idx.p);
+  DS_CHECK_LAUNCH();
 }
 
 void point_bbox(const double* d_rec, int n, int stride, double lo[3], double hi[3],
