@@ -679,42 +679,69 @@ constexpr int MF_KMAX = 4; // pixels per thread at most (n_per <= 1024)
 constexpr int MF_U = 8;    // neighbour rows in flight per thread
 
 // Sorts each column's list by lev descending (stable by skewer), the factor
-// split into a float pair.  One thread per column.
-__global__ void k_mc_sort(int ncol, int Q, const int* __restrict__ ptr,
-                          const int* __restrict__ idx, const int* __restrict__ lev,
-                          const double* __restrict__ p64, int* __restrict__ sidx,
-                          int* __restrict__ slev, float2* __restrict__ sp) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncol) return;
+// split into a float pair.  One warp per column, a counting sort: the
+// entries' levels counted 32 at a time, each level's first slot (levels
+// descending, level 0 -- no class kept -- last), then each entry to its
+// level's next slot, ranked within its 32 by the lanes of equal level below
+// it (list order kept within a level).
+constexpr int MC_SW = 8;  // columns (warps) per CTA of the sort
+__global__ void __launch_bounds__(32 * MC_SW)
+    k_mc_sort(int ncol, int Q, const int* __restrict__ ptr, const int* __restrict__ idx,
+              const int* __restrict__ lev, const double* __restrict__ p64,
+              int* __restrict__ sidx, int* __restrict__ slev, float2* __restrict__ sp) {
+  __shared__ int s_next[MC_SW][MC_QMAX + 2];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * MC_SW + w;
+  if (c >= ncol) return;  // the whole warp
+  int* next = s_next[w];
   const int q0 = ptr[c], q1 = ptr[c + 1];
-  // counting sort: entries per level, then each entry to its level's next
-  // slot (levels descending, entries in list order within a level)
-  int start[MC_QMAX + 2];
-  for (int L = 0; L <= Q + 1; ++L) start[L] = 0;
-  for (int e = q0; e < q1; ++e) {
-    const int L = lev[e];
-    ++start[(L >= 1 && L <= Q) ? L : 0];
-  }
-  int pos = q0;
-  for (int L = Q; L >= 0; --L) {  // level 0 (no class kept) last
-    const int cnt = start[L];
-    start[L] = pos;
-    pos += cnt;
-  }
-  for (int e = q0; e < q1; ++e) {
-    int L = lev[e];
-    if (L < 1 || L > Q) L = 0;
-    const int at = start[L]++;
-    if (L == 0) {  // contributes nothing
-      sidx[at] = 0;
-      slev[at] = 0;
-      sp[at] = make_float2(0.f, 0.f);
-      continue;
+  for (int L = lane; L <= Q + 1; L += 32) next[L] = 0;
+  __syncwarp();
+  const unsigned below = (1u << lane) - 1u;
+  for (int e0 = q0; e0 < q1; e0 += 32) {
+    const int e = e0 + lane;
+    int L = -1;  // no entry
+    if (e < q1) {
+      L = lev[e];
+      if (L < 1 || L > Q) L = 0;
     }
-    const ff f = ff_from_double(p64[e]);
-    sidx[at] = idx[e];
-    slev[at] = L;
-    sp[at] = make_float2(f.h, f.l);
+    const unsigned same = __match_any_sync(0xffffffffu, L);
+    if (L >= 0 && (same & below) == 0) next[L] += __popc(same);
+    __syncwarp();
+  }
+  if (lane == 0) {
+    int pos = q0;
+    for (int L = Q; L >= 0; --L) {
+      const int cnt = next[L];
+      next[L] = pos;
+      pos += cnt;
+    }
+  }
+  __syncwarp();
+  for (int e0 = q0; e0 < q1; e0 += 32) {
+    const int e = e0 + lane;
+    int L = -1;
+    if (e < q1) {
+      L = lev[e];
+      if (L < 1 || L > Q) L = 0;
+    }
+    const unsigned same = __match_any_sync(0xffffffffu, L);
+    if (L >= 0) {
+      const int at = next[L] + __popc(same & below);
+      if (L == 0) {  // contributes nothing
+        sidx[at] = 0;
+        slev[at] = 0;
+        sp[at] = make_float2(0.f, 0.f);
+      } else {
+        const ff f = ff_from_double(p64[e]);
+        sidx[at] = idx[e];
+        slev[at] = L;
+        sp[at] = make_float2(f.h, f.l);
+      }
+    }
+    __syncwarp();
+    if (L >= 0 && (same & below) == 0) next[L] += __popc(same);
+    __syncwarp();
   }
 }
 
@@ -881,8 +908,8 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
   mc.fidx.alloc(mc.idx.n);
   mc.flev.alloc(mc.idx.n);
   mc.fp.alloc(mc.idx.n);
-  k_mc_sort<<<(mc.ncol + 127) / 128, 128, 0, st>>>(mc.ncol, Q, mc.ptr.p, mc.idx.p, mc.lev.p,
-                                                   mc.p64.p, mc.fidx.p, mc.flev.p, mc.fp.p);
+  k_mc_sort<<<(mc.ncol + MC_SW - 1) / MC_SW, 32 * MC_SW, 0, st>>>(
+      mc.ncol, Q, mc.ptr.p, mc.idx.p, mc.lev.p, mc.p64.p, mc.fidx.p, mc.flev.p, mc.fp.p);
   DS_CHECK_LAUNCH();
   std::vector<float2> ftaps(Q);
   for (int q = 0; q < Q; ++q) {
