@@ -152,6 +152,42 @@ def test_column_grid_refused_for_other_layouts(ctx):
         grid.set_column_grid(15, 10)
     grid.set_column_grid(16, 10)
     grid.close()
+    bad = pts.copy()
+    bad[5, 2] = np.inf  # map points are checked when the map is created
+    with pytest.raises(DsError):
+        MapGrid(ctx, bad)
+
+
+def test_map_points_tiled_on_first_pair_product(ctx):
+    """A column-grid map against a skewer grid reads its points as given;
+    their sorted, tiled copy is built by the first product that needs it
+    (here the pair-kernel maps after the column grid is removed), with the
+    same results as on a map tiled from the start."""
+    from dachshund_gb300 import MapGrid
+
+    n_sk, n_per = 20, 40
+    w = synth.small(n_sk, n_per, 8.0, seed=11)
+    op, rec = make(ctx, "sn", w.pixels)
+    op.set_skewer_grid(n_sk, n_per)
+    nx, ny, nz = 6, 5, 2 * n_per
+    pts = synth.uniform_map_coords(8.0, 8.0, n_per * synth.DZ, nx, ny, nz)
+    x = np.random.default_rng(3).standard_normal(rec.shape[0])
+    grid = MapGrid(ctx, pts)
+    grid.set_column_grid(nx * ny, nz)
+    m_col = grid.product_f32(op, x)
+    grid.set_column_grid(0, 0)
+    m32_late = grid.product_f32(op, x)
+    m64_late = grid.product(op, x)
+    grid.close()
+    grid = MapGrid(ctx, pts)
+    m32_first = grid.product_f32(op, x)
+    m64_first = grid.product(op, x)
+    grid.close()
+    scale = np.max(np.abs(m_col))
+    assert np.max(np.abs(m32_late - m32_first)) / scale < 1e-12
+    assert np.max(np.abs(m64_late - m64_first)) / scale < 1e-12
+    assert np.max(np.abs(m64_late - m_col)) / scale < 1e-12
+    op.close()
 
 
 @pytest.mark.parametrize("form", ["w", "sn"])
