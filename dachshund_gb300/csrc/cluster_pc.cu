@@ -321,25 +321,33 @@ void plan_skewer_clusters(int n_sk, int n_per, int g, const std::vector<double>&
   constexpr int WINDOW = 256;
   std::vector<char> used(n_sk, 0);
   std::vector<std::vector<int>> clusters;
-  std::vector<std::pair<double, int>> cand;
+  const int kmax = g - 1;
+  std::vector<std::pair<double, int>> best(std::max(1, kmax));
   for (int oi = 0; oi < n_sk; ++oi) {
     const int s0 = order[oi];
     if (used[s0]) continue;
     used[s0] = 1;
-    cand.clear();
-    for (int oj = oi + 1, seen = 0; oj < n_sk && seen < WINDOW; ++oj) {
+    // the g - 1 nearest by (squared distance, skewer index), ascending: an
+    // insertion into the g - 1 best so far
+    int take = 0;
+    for (int oj = oi + 1, seen = 0; kmax > 0 && oj < n_sk && seen < WINDOW; ++oj) {
       const int s = order[oj];
       if (used[s]) continue;
       ++seen;
       const double dx = sx[s] - sx[s0], dy = sy[s] - sy[s0];
-      cand.push_back({dx * dx + dy * dy, s});
+      const std::pair<double, int> p{dx * dx + dy * dy, s};
+      if (take == kmax && !(p < best[kmax - 1])) continue;
+      int at = take < kmax ? take++ : kmax - 1;
+      while (at > 0 && p < best[at - 1]) {
+        best[at] = best[at - 1];
+        --at;
+      }
+      best[at] = p;
     }
-    const int take = std::min<int>(g - 1, (int)cand.size());
-    std::partial_sort(cand.begin(), cand.begin() + take, cand.end());
     std::vector<int> c{s0};
     for (int k = 0; k < take; ++k) {
-      c.push_back(cand[k].second);
-      used[cand[k].second] = 1;
+      c.push_back(best[k].second);
+      used[best[k].second] = 1;
     }
     clusters.push_back(std::move(c));
   }
