@@ -869,9 +869,23 @@ static void build_map_columns(ds_map* map, ds_operator* op, double cut) {
       const double d = dist(j, k);
       if (kc.c_para * d * d < cut) ds.push_back(d);
     }
-  std::sort(ds.begin(), ds.end());
-  std::vector<double> cls_d;  // one representative per class (ulp-level ties merged)
-  for (double d : ds)
+  // the distinct distances in ascending order (on grids of commensurate
+  // spacing a few dozen: a sorted insertion; past 256, a sort of all), then
+  // one representative per class, ulp-level ties merged (exact duplicates
+  // never open a class, so dropping them first changes nothing)
+  std::vector<double> du;
+  for (double d : ds) {
+    const auto it = std::lower_bound(du.begin(), du.end(), d);
+    if (it != du.end() && *it == d) continue;
+    if (du.size() >= 256) {
+      du = ds;
+      std::sort(du.begin(), du.end());
+      break;
+    }
+    du.insert(it, d);
+  }
+  std::vector<double> cls_d;  // one representative per class
+  for (double d : du)
     if (cls_d.empty() || d - cls_d.back() > 1e-12 * std::max(1.0, d)) cls_d.push_back(d);
   const int Q = (int)cls_d.size();
   require(Q >= 1 && Q <= MC_QMAX,
