@@ -55,6 +55,10 @@ __global__ void k_bbox_partial(const double* __restrict__ rec, int n, int stride
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     for (int c = 0; c < 3; ++c) {
       const double v = rec[(size_t)i * stride + c];
+      if (v != v) {  // NaN (fmin and fmax would skip it): the bounds go infinite
+        lo[c] = -INFINITY;
+        hi[c] = INFINITY;
+      }
       lo[c] = fmin(lo[c], v);
       hi[c] = fmax(hi[c], v);
     }
@@ -571,7 +575,7 @@ void kd_partition(const PointSet& ps, const double* d_rec, int n, int stride, do
 void point_bbox(const double* d_rec, int n, int stride, double lo[3], double hi[3],
                 cudaStream_t st) {
   require(n > 0, "point count must be > 0");
-  const int nb = std::min(256, (n + BLK - 1) / BLK);
+  const int nb = std::min(1216, (n + BLK - 1) / BLK);  // 8 CTAs per SM of 152
   DevBuf<double> part;
   part.alloc((size_t)nb * 6);
   k_bbox_partial<<<nb, BLK, 0, st>>>(d_rec, n, stride, part.p);

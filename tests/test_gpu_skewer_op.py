@@ -152,10 +152,11 @@ def test_column_grid_refused_for_other_layouts(ctx):
         grid.set_column_grid(15, 10)
     grid.set_column_grid(16, 10)
     grid.close()
-    bad = pts.copy()
-    bad[5, 2] = np.inf  # map points are checked when the map is created
-    with pytest.raises(DsError):
-        MapGrid(ctx, bad)
+    for v in (np.inf, np.nan):  # map points are checked when the map is created
+        bad = pts.copy()
+        bad[5, 2] = v
+        with pytest.raises(DsError):
+            MapGrid(ctx, bad)
 
 
 def test_map_points_tiled_on_first_pair_product(ctx):
